@@ -1,0 +1,27 @@
+"""GB300 (sm_103a) stochastic-Galerkin hot path of ExtendableASGFEM.jl.
+
+Host-side mirror of the reference API (Python names for the Julia ones,
+``solve!`` -> ``solve``) over the C ABI of libsgfem.so (include/sgfem.h).
+The directory name follows the Julia package naming; import it through
+``load_package()`` in ``__graft_entry__`` or by path.
+"""
+from . import _lib
+from ._lib import FP32, FP64, MIXED, PREC_JACOBI, PREC_LATTICE, PREC_NONE, SGError
+from .coefficients import StochasticCoefficientCosinus
+from .fem import H1Pk, assemble_rhs, assemble_stiffness, line_rule, triangle_rule, unit_square_mesh
+from .modelproblems import AbstractModelProblem, PoissonProblemPrimal, SGOperator, assemble, solve
+from .mopcontrol import (add_boundary_modes, classify_modes, generate_multiindices, get_neighbours,
+                         prepare_multi_indices, stochastic_marking, top_weight_multiindices,
+                         total_degree_multiindices)
+from .orthopolys import HermitePolynomials, LegendrePolynomials, ONBasis
+from .sgfevector import SGFEVector
+from .tensorizedbasis import TensorizedBasis, coupling_matrix
+
+__all__ = [
+    "FP32", "FP64", "MIXED", "PREC_JACOBI", "PREC_LATTICE", "PREC_NONE", "SGError",
+    "StochasticCoefficientCosinus", "H1Pk", "assemble_rhs", "assemble_stiffness", "line_rule", "triangle_rule",
+    "unit_square_mesh", "AbstractModelProblem", "PoissonProblemPrimal", "SGOperator", "assemble", "solve",
+    "add_boundary_modes", "classify_modes", "generate_multiindices", "get_neighbours", "prepare_multi_indices",
+    "stochastic_marking", "top_weight_multiindices", "total_degree_multiindices", "HermitePolynomials",
+    "LegendrePolynomials", "ONBasis", "SGFEVector", "TensorizedBasis", "coupling_matrix",
+]

@@ -1,0 +1,171 @@
+// K1: the stochastic-Galerkin operator apply on sm_103a.
+//
+// Computes, for every device row i (mul!(Ax, S, x), src/modelproblems/
+// solvers_poisson_primal.jl:86-124):
+//     Y[i, mu] = sum_j K_0[i,j] X[j, mu] + sum_{m, nu} G[(m-1)P+mu, nu] sum_j K_m[i,j] X[j, nu]
+// and Y[i, :] = 0 on Dirichlet rows.  The reference performs one full SpMV per
+// nonzero of G (solvers_poisson_primal.jl:108-115); here every CSR nonzero of
+// the shared pattern is read once and applied to all modes:
+//   phase 1 (per nonzero, per pair q = (m, nu) of the pair list Q):
+//       acc[q] += K_m[i, j] * X[j, nu]
+//   phase 2 (per output mode mu):
+//       Y[i, mu] = acc[(0, mu)] + sum_{(g, q) in comb(mu)} g * acc[q]
+// Pairs (m, nu) exist only where column nu of G_m is nonzero, so the flop
+// count is 2 nnz (P + sum_m nzcols(G_m)) + 2 n nnz(G), the minimum for an
+// assembled operator.
+//
+// Mapping: one warp per row, pairs spread over the lanes (lane-strided), the
+// gathered mode vector X[j, :] and the M+1 values of the nonzero staged in the
+// warp's shared memory, the per-row pair accumulators stored to shared memory
+// for phase 2.  Per-block FP64 partials of X .* Y (the p'Ap of CG) are fused
+// into the epilogue.
+#include <algorithm>
+
+#include "sgfem_internal.h"
+
+namespace {
+
+constexpr int WPB = 4;  // warps per block
+
+template <typename T> struct Vec16;
+template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };
+template <> struct Vec16<double> { using type = double2; static constexpr int n = 2; };
+
+template <typename T, int QT>
+__global__ void __launch_bounds__(WPB * 32)
+k_apply(const int* __restrict__ rowptr, const int* __restrict__ col, const T* __restrict__ vals, int M1,
+        const T* __restrict__ X, T* __restrict__ Y, int n, int P, int ld, const unsigned char* __restrict__ bmask,
+        const int* __restrict__ qtab, int Qn, const int* __restrict__ combptr, const int* __restrict__ combq,
+        const T* __restrict__ combg, double* __restrict__ partials, const KrylovScalars* __restrict__ scal) {
+    if (scal && scal->done) return;
+    extern __shared__ unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int per_warp = (ld + (M1 + 1) + Qn + 3) & ~3;  // elements of T, 16-byte multiple per slice
+    T* su = reinterpret_cast<T*>(smem_raw) + (size_t)warp * per_warp;
+    T* sc = su + ld;
+    T* sacc = sc + M1 + 1;
+    __shared__ double red[WPB];
+
+    if (lane == 0) sc[M1] = T(0);  // zero slot for padded pairs
+    using V = typename Vec16<T>::type;
+    const int nvec = ld / Vec16<T>::n;
+    double dot = 0.0;
+
+    for (int row = blockIdx.x * WPB + warp; row < n; row += gridDim.x * WPB) {
+        T* yrow = Y + (size_t)row * ld;
+        if (bmask[row]) {
+            for (int c = lane; c < ld; c += 32) yrow[c] = T(0);
+            continue;
+        }
+        const int nz0 = rowptr[row], nz1 = rowptr[row + 1];
+        for (int base = 0; base < Qn; base += QT * 32) {
+            int om[QT], on[QT];
+#pragma unroll
+            for (int t = 0; t < QT; ++t) {
+                const int q = base + t * 32 + lane;
+                if (q < Qn) {
+                    const int e = qtab[q];
+                    om[t] = e >> 16;
+                    on[t] = e & 0xffff;
+                } else {
+                    om[t] = M1;
+                    on[t] = 0;
+                }
+            }
+            T acc[QT];
+#pragma unroll
+            for (int t = 0; t < QT; ++t) acc[t] = T(0);
+            for (int nz = nz0; nz < nz1; ++nz) {
+                const int j = col[nz];
+                const V* xs = reinterpret_cast<const V*>(X + (size_t)j * ld);
+                V* sv = reinterpret_cast<V*>(su);
+                for (int c = lane; c < nvec; c += 32) sv[c] = __ldg(xs + c);
+                if (lane < M1) sc[lane] = vals[(size_t)nz * M1 + lane];
+                __syncwarp();
+#pragma unroll
+                for (int t = 0; t < QT; ++t) acc[t] = fma(sc[om[t]], su[on[t]], acc[t]);
+                __syncwarp();
+            }
+#pragma unroll
+            for (int t = 0; t < QT; ++t) {
+                const int q = base + t * 32 + lane;
+                if (q < Qn) sacc[q] = acc[t];
+            }
+        }
+        __syncwarp();
+        const T* xrow = X + (size_t)row * ld;
+        for (int mu = lane; mu < ld; mu += 32) {
+            T y = T(0);
+            if (mu < P) {
+                y = sacc[mu];
+                for (int e = combptr[mu]; e < combptr[mu + 1]; ++e) y = fma(combg[e], sacc[combq[e]], y);
+            }
+            yrow[mu] = y;
+            if (partials) dot += (double)xrow[mu] * (double)y;
+        }
+        __syncwarp();
+    }
+    if (partials) {
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
+        if (lane == 0) red[warp] = dot;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0;
+            for (int w = 0; w < WPB; ++w) s += red[w];
+            partials[blockIdx.x] = s;
+        }
+    }
+}
+
+template <typename T, int QT>
+int launch_qt(sgfem_context* ctx, const T* vals, const T* combg, const void* X, void* Y, double* partials,
+              int grid, const KrylovScalars* scal) {
+    const size_t per_warp = ((size_t)ctx->ld + ctx->M1 + 1 + ctx->Qn + 3) & ~(size_t)3;
+    const size_t smem = per_warp * sizeof(T) * WPB;
+    if (grid == 0) {  // configuration call
+        if (smem > 48 * 1024)
+            SG_CUDA(ctx, cudaFuncSetAttribute(k_apply<T, QT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        return SGFEM_OK;
+    }
+    k_apply<T, QT><<<grid, WPB * 32, smem, ctx->stream>>>(
+        ctx->d_rowptr, ctx->d_col, vals, ctx->M1, (const T*)X, (T*)Y, (int)ctx->n, (int)ctx->P, (int)ctx->ld,
+        ctx->d_bmask, ctx->d_qtab, ctx->Qn, ctx->d_combptr, ctx->d_combq, combg, partials, scal);
+    SG_CUDA(ctx, cudaGetLastError());
+    return SGFEM_OK;
+}
+
+template <typename T>
+int launch_t(sgfem_context* ctx, const T* vals, const T* combg, const void* X, void* Y, double* partials, int grid,
+             const KrylovScalars* scal) {
+    const int need = (ctx->Qn + 31) / 32;
+    if (need <= 1) return launch_qt<T, 1>(ctx, vals, combg, X, Y, partials, grid, scal);
+    if (need <= 2) return launch_qt<T, 2>(ctx, vals, combg, X, Y, partials, grid, scal);
+    if (need <= 4) return launch_qt<T, 4>(ctx, vals, combg, X, Y, partials, grid, scal);
+    if (need <= 8) return launch_qt<T, 8>(ctx, vals, combg, X, Y, partials, grid, scal);
+    if (need <= 12) return launch_qt<T, 12>(ctx, vals, combg, X, Y, partials, grid, scal);
+    if (need <= 16) return launch_qt<T, 16>(ctx, vals, combg, X, Y, partials, grid, scal);
+    if (need <= 20) return launch_qt<T, 20>(ctx, vals, combg, X, Y, partials, grid, scal);
+    return launch_qt<T, 24>(ctx, vals, combg, X, Y, partials, grid, scal);  // rounds for larger Q
+}
+
+}  // namespace
+
+int sg_apply_configure(sgfem_context* ctx) {
+    SG_TRY(launch_t<double>(ctx, ctx->d_val64, ctx->d_combg64, nullptr, nullptr, nullptr, 0, nullptr));
+    SG_TRY(launch_t<float>(ctx, ctx->d_val32, ctx->d_combg32, nullptr, nullptr, nullptr, 0, nullptr));
+    return SGFEM_OK;
+}
+
+int sg_launch_apply(sgfem_context* ctx, int precision, const void* X, void* Y, double* dot_partials, int* nblocks,
+                    const KrylovScalars* skip_if_done) {
+    const size_t per_warp = ((size_t)ctx->ld + ctx->M1 + 1 + ctx->Qn + 3) & ~(size_t)3;
+    const size_t smem = per_warp * sg_elem_bytes(precision) * WPB;
+    if (smem > 200 * 1024)
+        return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "apply: per-row pair list too large for shared memory");
+    int grid = (int)std::min<int64_t>((ctx->n + WPB - 1) / WPB, (int64_t)ctx->num_sms * 8);
+    if (grid < 1) grid = 1;
+    if (nblocks) *nblocks = grid;
+    if (precision == SGFEM_FP64)
+        return launch_t<double>(ctx, ctx->d_val64, ctx->d_combg64, X, Y, dot_partials, grid, skip_if_done);
+    return launch_t<float>(ctx, ctx->d_val32, ctx->d_combg32, X, Y, dot_partials, grid, skip_if_done);
+}

@@ -1,0 +1,554 @@
+// Context, operator setup and the host <-> device layout boundary of libsgfem.
+//
+// Replaces the construction side of the reference solver:
+//   MySystemPrimal(A0, Am, G, bdofs, nmodes)   src/modelproblems/solvers_poisson_primal.jl:14-21,144
+//   boundary dofs from FES[BFaceDofs]          solvers_poisson_primal.jl:136-142
+// and the SGFEVector layout (src/sgfevector.jl:86-106): a caller vector is
+// column-major n x P; on the device it becomes row-major n x ld (see
+// sgfem_internal.h).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+
+#include "sgfem_internal.h"
+
+int sg_fail(sgfem_context* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+int sg_cuda_fail(sgfem_context* ctx, cudaError_t e, const char* what) {
+    std::string m = std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e);
+    return sg_fail(ctx, SGFEM_ERR_CUDA, m);
+}
+
+int sg_ensure(sgfem_context* ctx, DeviceBuf& b, size_t bytes) {
+    if (b.bytes >= bytes && b.p) return SGFEM_OK;
+    if (b.p) {
+        SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        SG_CUDA(ctx, cudaFree(b.p));
+        b.p = nullptr;
+        b.bytes = 0;
+    }
+    SG_CUDA(ctx, cudaMalloc(&b.p, bytes));
+    b.bytes = bytes;
+    return SGFEM_OK;
+}
+
+size_t sg_elem_bytes(int precision) { return precision == SGFEM_FP64 ? 8 : 4; }
+
+size_t sg_vec_bytes(const sgfem_context* ctx, int precision) {
+    return (size_t)ctx->n * (size_t)ctx->ld * sg_elem_bytes(precision);
+}
+
+int sg_check_ready(sgfem_context* ctx) {
+    if (!ctx) return SGFEM_ERR_ARGUMENT;
+    if (!ctx->finalized) return sg_fail(ctx, SGFEM_ERR_STATE, "sgfem_finalize has not been called");
+    return SGFEM_OK;
+}
+
+static void free_dev(void* p) {
+    if (p) cudaFree(p);
+}
+
+extern "C" int sgfem_version(void) { return 10000; }
+
+extern "C" int sgfem_create(sgfem_context** out, int device) {
+    if (!out) return SGFEM_ERR_ARGUMENT;
+    *out = nullptr;
+    sgfem_context* ctx = new sgfem_context();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_scal, sizeof(KrylovScalars));
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_scal, sizeof(KrylovScalars));
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+    if (e != cudaSuccess) {
+        // report through a transient context so the caller sees the reason
+        *out = ctx;
+        return sg_cuda_fail(ctx, e, "sgfem_create");
+    }
+    *out = ctx;
+    return SGFEM_OK;
+}
+
+extern "C" int sgfem_destroy(sgfem_context* ctx) {
+    if (!ctx) return SGFEM_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    void* ptrs[] = {ctx->d_rowptr, ctx->d_col, ctx->d_val64, ctx->d_val32, ctx->d_bmask, ctx->d_iperm,
+                    ctx->d_dinv64, ctx->d_dinv32, ctx->d_qtab, ctx->d_combptr, ctx->d_combq,
+                    ctx->d_combg64, ctx->d_combg32, ctx->d_lat_tab64, ctx->d_lat_tab32,
+                    ctx->d_lat_scale64, ctx->d_lat_scale32, ctx->d_scal, ctx->w_stage.p, ctx->w_partials.p};
+    for (void* p : ptrs) free_dev(p);
+    for (int i = 0; i < SG_NBUF; ++i) free_dev(ctx->w_vec[i].p);
+    if (ctx->h_scal) cudaFreeHost(ctx->h_scal);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return SGFEM_OK;
+}
+
+extern "C" const char* sgfem_last_error(const sgfem_context* ctx) {
+    if (!ctx) return "null context";
+    return ctx->err.c_str();
+}
+
+// ------------------------------------------------------------------ setup
+static int invalidate(sgfem_context* ctx) {
+    if (ctx->finalized) return sg_fail(ctx, SGFEM_ERR_STATE, "context already finalized");
+    return SGFEM_OK;
+}
+
+extern "C" int sgfem_set_spatial_matrix(sgfem_context* ctx, int m, int64_t n, const int64_t* colptr,
+                                        const int64_t* rowval, const double* nzval) {
+    if (!ctx) return SGFEM_ERR_ARGUMENT;
+    SG_TRY(invalidate(ctx));
+    if (m < 0 || m > 4096 || n <= 0 || n > (int64_t)INT32_MAX || !colptr || !rowval || !nzval)
+        return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "sgfem_set_spatial_matrix: bad arguments");
+    if (ctx->n >= 0 && ctx->n != n) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "matrix size differs from earlier matrices");
+    int64_t nnz = colptr[n] - 1;
+    if (colptr[0] != 1 || nnz < 0) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "colptr must be 1-based");
+    HostCSC c;
+    c.n = n;
+    c.colptr.resize(n + 1);
+    for (int64_t j = 0; j <= n; ++j) {
+        c.colptr[j] = colptr[j] - 1;
+        if (j > 0 && c.colptr[j] < c.colptr[j - 1]) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "colptr not monotone");
+    }
+    c.rowval.resize(nnz);
+    c.nzval.assign(nzval, nzval + nnz);
+    for (int64_t k = 0; k < nnz; ++k) {
+        int64_t r = rowval[k] - 1;
+        if (r < 0 || r >= n) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "rowval out of range");
+        c.rowval[k] = r;
+    }
+    c.set = true;
+    ctx->n = n;
+    if ((int64_t)ctx->mats.size() <= m) ctx->mats.resize(m + 1);
+    ctx->mats[m] = std::move(c);
+    return SGFEM_OK;
+}
+
+extern "C" int sgfem_set_coupling(sgfem_context* ctx, int64_t P, int64_t M, const int64_t* colptr,
+                                  const int64_t* rowval, const double* nzval) {
+    if (!ctx) return SGFEM_ERR_ARGUMENT;
+    SG_TRY(invalidate(ctx));
+    if (P <= 0 || P > 32767 || M < 0 || M > 4095 || !colptr || (!rowval && colptr[P] > 1))
+        return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "sgfem_set_coupling: bad sizes (P <= 32767, M <= 4095)");
+    int64_t nnz = colptr[P] - 1;
+    if (colptr[0] != 1 || nnz < 0) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "G colptr must be 1-based");
+    ctx->G_colptr.assign(colptr, colptr + P + 1);
+    for (auto& v : ctx->G_colptr) v -= 1;
+    ctx->G_rowval.resize(nnz);
+    for (int64_t k = 0; k < nnz; ++k) {
+        int64_t r = rowval[k] - 1;
+        if (r < 0 || r >= M * P) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "G rowval out of range");
+        ctx->G_rowval[k] = r;
+    }
+    ctx->G_val.assign(nzval, nzval + nnz);
+    ctx->P = P;
+    ctx->M = M;
+    ctx->has_G = true;
+    return SGFEM_OK;
+}
+
+extern "C" int sgfem_set_boundary_dofs(sgfem_context* ctx, int64_t count, const int64_t* bdofs) {
+    if (!ctx) return SGFEM_ERR_ARGUMENT;
+    SG_TRY(invalidate(ctx));
+    if (count < 0 || (count > 0 && !bdofs)) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad boundary dof list");
+    ctx->bdofs.resize(count);
+    for (int64_t k = 0; k < count; ++k) ctx->bdofs[k] = bdofs[k] - 1;
+    ctx->has_bdofs = true;
+    return SGFEM_OK;
+}
+
+extern "C" int sgfem_set_dof_coordinates(sgfem_context* ctx, int64_t n, const double* xy) {
+    if (!ctx) return SGFEM_ERR_ARGUMENT;
+    SG_TRY(invalidate(ctx));
+    if (n <= 0 || !xy) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad coordinates");
+    ctx->dof_xy.assign(xy, xy + 2 * n);
+    return SGFEM_OK;
+}
+
+extern "C" int sgfem_has_lattice(const sgfem_context* ctx) { return (ctx && ctx->lattice) ? 1 : 0; }
+
+// lattice detection: every dof at (ix/Nl, iy/Nl), all (Nl+1)^2 points present once
+static bool detect_lattice(sgfem_context* ctx, std::vector<int32_t>& iperm) {
+    int64_t n = ctx->n;
+    if ((int64_t)ctx->dof_xy.size() != 2 * n) return false;
+    int64_t side = (int64_t)std::llround(std::sqrt((double)n));
+    if (side * side != n || side < 3) return false;
+    int Nl = (int)(side - 1);
+    iperm.assign(n, -1);
+    std::vector<char> seen(n, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        double x = ctx->dof_xy[2 * i] * Nl, y = ctx->dof_xy[2 * i + 1] * Nl;
+        double rx = std::nearbyint(x), ry = std::nearbyint(y);
+        if (std::fabs(x - rx) > 1e-6 || std::fabs(y - ry) > 1e-6) return false;
+        if (rx < 0 || ry < 0 || rx > Nl || ry > Nl) return false;
+        int64_t r = (int64_t)ry * (Nl + 1) + (int64_t)rx;
+        if (seen[r]) return false;
+        seen[r] = 1;
+        iperm[i] = (int32_t)r;
+    }
+    ctx->Nl = Nl;
+    return true;
+}
+
+template <typename T>
+static int upload(sgfem_context* ctx, T** dst, const T* src, size_t count) {
+    SG_CUDA(ctx, cudaMalloc((void**)dst, std::max<size_t>(count, 1) * sizeof(T)));
+    if (count) SG_CUDA(ctx, cudaMemcpy(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice));
+    return SGFEM_OK;
+}
+
+extern "C" int sgfem_finalize(sgfem_context* ctx) {
+    if (!ctx) return SGFEM_ERR_ARGUMENT;
+    SG_TRY(invalidate(ctx));
+    SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (!ctx->has_G) return sg_fail(ctx, SGFEM_ERR_STATE, "coupling matrix not set");
+    if (!ctx->has_bdofs) return sg_fail(ctx, SGFEM_ERR_STATE, "boundary dofs not set");
+    const int64_t M = ctx->M, P = ctx->P, n = ctx->n;
+    if ((int64_t)ctx->mats.size() < M + 1) return sg_fail(ctx, SGFEM_ERR_STATE, "spatial matrices K_0..K_M not all set");
+    for (int64_t m = 0; m <= M; ++m)
+        if (!ctx->mats[m].set) return sg_fail(ctx, SGFEM_ERR_STATE, "spatial matrix K_" + std::to_string(m) + " not set");
+    ctx->M1 = (int)(M + 1);
+    ctx->ld = (P + 3) / 4 * 4;
+    for (int64_t b : ctx->bdofs)
+        if (b < 0 || b >= n) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "boundary dof out of range");
+
+    // ---- numbering
+    std::vector<int32_t> iperm;
+    ctx->lattice = detect_lattice(ctx, iperm);
+    if (!ctx->lattice) {
+        iperm.resize(n);
+        std::iota(iperm.begin(), iperm.end(), 0);
+    }
+    ctx->iperm = iperm;
+    ctx->perm.assign(n, 0);
+    for (int64_t i = 0; i < n; ++i) ctx->perm[iperm[i]] = (int32_t)i;
+
+    // ---- union pattern (CSR in device numbering); K_m are given as CSC in caller numbering
+    bool same = true;
+    for (int64_t m = 1; m <= M && same; ++m) {
+        same = ctx->mats[m].colptr == ctx->mats[0].colptr && ctx->mats[m].rowval == ctx->mats[0].rowval;
+    }
+    // entries (devrow, devcol) of the union pattern
+    std::vector<int64_t> rowcount(n + 1, 0);
+    std::vector<std::vector<std::pair<int32_t, int64_t>>> rows;  // unused when same
+    std::vector<int32_t> col;
+    std::vector<int64_t> rowptr(n + 1, 0);
+    if (same) {
+        const HostCSC& A = ctx->mats[0];
+        // CSC of A in caller numbering == CSR of A^T; row i of A = column entries with rowval == i
+        for (int64_t j = 0; j < n; ++j)
+            for (int64_t k = A.colptr[j]; k < A.colptr[j + 1]; ++k) rowcount[iperm[A.rowval[k]] + 1]++;
+    } else {
+        // merge: collect all (devrow, devcol) keys, dedupe
+        std::vector<int64_t> keys;
+        for (int64_t m = 0; m <= M; ++m) {
+            const HostCSC& A = ctx->mats[m];
+            for (int64_t j = 0; j < n; ++j)
+                for (int64_t k = A.colptr[j]; k < A.colptr[j + 1]; ++k)
+                    keys.push_back((int64_t)iperm[A.rowval[k]] * n + iperm[j]);
+        }
+        std::sort(keys.begin(), keys.end());
+        keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+        col.resize(keys.size());
+        for (size_t t = 0; t < keys.size(); ++t) {
+            rowcount[keys[t] / n + 1]++;
+            col[t] = (int32_t)(keys[t] % n);
+        }
+    }
+    for (int64_t i = 0; i < n; ++i) rowptr[i + 1] = rowptr[i] + rowcount[i + 1];
+    const int64_t nnz = rowptr[n];
+    if (nnz > (int64_t)INT32_MAX) return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "more than 2^31 nonzeros");
+    ctx->nnz = nnz;
+    if (same) {
+        col.assign(nnz, 0);
+        std::vector<int64_t> fill(rowptr.begin(), rowptr.end() - 1);
+        const HostCSC& A = ctx->mats[0];
+        for (int64_t j = 0; j < n; ++j)
+            for (int64_t k = A.colptr[j]; k < A.colptr[j + 1]; ++k) col[fill[iperm[A.rowval[k]]]++] = iperm[j];
+        for (int64_t i = 0; i < n; ++i) std::sort(col.begin() + rowptr[i], col.begin() + rowptr[i + 1]);
+    }
+    // values: locate each (row, col) by binary search in the row
+    const int M1 = ctx->M1;
+    std::vector<double> val64((size_t)nnz * M1, 0.0);
+    for (int64_t m = 0; m <= M; ++m) {
+        const HostCSC& A = ctx->mats[m];
+        for (int64_t j = 0; j < n; ++j) {
+            int32_t cj = iperm[j];
+            for (int64_t k = A.colptr[j]; k < A.colptr[j + 1]; ++k) {
+                int32_t r = iperm[A.rowval[k]];
+                auto b = col.begin() + rowptr[r], e = col.begin() + rowptr[r + 1];
+                auto it = std::lower_bound(b, e, cj);
+                val64[(size_t)(it - col.begin()) * M1 + m] += A.nzval[k];
+            }
+        }
+    }
+    std::vector<float> val32(val64.size());
+    for (size_t t = 0; t < val64.size(); ++t) val32[t] = (float)val64[t];
+    std::vector<int32_t> rowptr32(n + 1);
+    for (int64_t i = 0; i <= n; ++i) rowptr32[i] = (int32_t)rowptr[i];
+
+    // boundary mask and Jacobi diagonal
+    ctx->bmask_host.assign(n, 0);
+    for (int64_t b : ctx->bdofs) ctx->bmask_host[iperm[b]] = 1;
+    std::vector<double> dinv(n, 0.0);
+    std::vector<float> dinv32(n, 0.0f);
+    double dsum = 0.0;
+    int64_t dcount = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        double d = 0.0;
+        for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+            if (col[k] == i) d = val64[(size_t)k * M1 + 0];
+        if (!ctx->bmask_host[i]) {
+            if (!(d > 0.0)) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "K_0 has a non-positive interior diagonal entry");
+            dinv[i] = 1.0 / d;
+            dinv32[i] = (float)dinv[i];
+            dsum += d;
+            dcount++;
+        }
+    }
+    ctx->lat_scale = dcount ? dsum / (4.0 * dcount) : 1.0;
+
+    // ---- coupling schedule from G ((M*P) x P, CSC): entry (row = m'*P + mu, col = nu), m = m'+1
+    std::vector<std::vector<char>> nzcol(M + 1, std::vector<char>(P, 0));
+    struct GE { int m; int mu; int nu; double g; };
+    std::vector<GE> ges;
+    for (int64_t nu = 0; nu < P; ++nu)
+        for (int64_t k = ctx->G_colptr[nu]; k < ctx->G_colptr[nu + 1]; ++k) {
+            double g = ctx->G_val[k];
+            if (g == 0.0) continue;  // the reference skips zero couplings (solvers_poisson_primal.jl:111)
+            int64_t r = ctx->G_rowval[k];
+            int m = (int)(r / P) + 1;
+            int mu = (int)(r % P);
+            nzcol[m][nu] = 1;
+            ges.push_back({m, mu, (int)nu, g});
+        }
+    std::vector<int32_t> qtab;
+    std::map<std::pair<int, int>, int> qidx;
+    for (int64_t nu = 0; nu < P; ++nu) {
+        qidx[{0, (int)nu}] = (int)qtab.size();
+        qtab.push_back((int32_t)nu);  // m = 0
+    }
+    for (int64_t m = 1; m <= M; ++m)
+        for (int64_t nu = 0; nu < P; ++nu)
+            if (nzcol[m][nu]) {
+                qidx[{(int)m, (int)nu}] = (int)qtab.size();
+                qtab.push_back((int32_t)((m << 16) | nu));
+            }
+    ctx->Qn = (int)qtab.size();
+    std::sort(ges.begin(), ges.end(), [](const GE& a, const GE& b) {
+        if (a.mu != b.mu) return a.mu < b.mu;
+        if (a.m != b.m) return a.m < b.m;
+        return a.nu < b.nu;
+    });
+    std::vector<int32_t> combptr(P + 1, 0), combq;
+    std::vector<double> combg;
+    for (const GE& e : ges) {
+        combptr[e.mu + 1]++;
+        combq.push_back(qidx[{e.m, e.nu}]);
+        combg.push_back(e.g);
+    }
+    for (int64_t mu = 0; mu < P; ++mu) combptr[mu + 1] += combptr[mu];
+    ctx->ncomb = (int)combq.size();
+    std::vector<float> combg32(combg.begin(), combg.end());
+
+    // ---- upload
+    SG_TRY(upload(ctx, &ctx->d_rowptr, rowptr32.data(), rowptr32.size()));
+    SG_TRY(upload(ctx, &ctx->d_col, col.data(), col.size()));
+    SG_TRY(upload(ctx, &ctx->d_val64, val64.data(), val64.size()));
+    SG_TRY(upload(ctx, &ctx->d_val32, val32.data(), val32.size()));
+    SG_TRY(upload(ctx, &ctx->d_bmask, ctx->bmask_host.data(), ctx->bmask_host.size()));
+    SG_TRY(upload(ctx, &ctx->d_iperm, ctx->iperm.data(), ctx->iperm.size()));
+    SG_TRY(upload(ctx, &ctx->d_dinv64, dinv.data(), dinv.size()));
+    SG_TRY(upload(ctx, &ctx->d_dinv32, dinv32.data(), dinv32.size()));
+    SG_TRY(upload(ctx, &ctx->d_qtab, qtab.data(), qtab.size()));
+    SG_TRY(upload(ctx, &ctx->d_combptr, combptr.data(), combptr.size()));
+    SG_TRY(upload(ctx, &ctx->d_combq, combq.data(), combq.size()));
+    SG_TRY(upload(ctx, &ctx->d_combg64, combg.data(), combg.size()));
+    SG_TRY(upload(ctx, &ctx->d_combg32, combg32.data(), combg32.size()));
+
+    if (ctx->lattice) {
+        int s = sg_lattice_setup(ctx);
+        if (s != SGFEM_OK) {
+            if (s == SGFEM_ERR_UNSUPPORTED) {
+                ctx->lattice = false;  // e.g. Nl not a power of two: Jacobi only
+                ctx->err.clear();
+            } else {
+                return s;
+            }
+        }
+    }
+    SG_TRY(sg_apply_configure(ctx));
+    if (ctx->lattice) SG_TRY(sg_lattice_configure(ctx));
+    // host copies of the pattern are no longer needed
+    for (auto& A : ctx->mats) {
+        A.colptr.clear(); A.colptr.shrink_to_fit();
+        A.rowval.clear(); A.rowval.shrink_to_fit();
+        A.nzval.clear(); A.nzval.shrink_to_fit();
+    }
+    ctx->finalized = true;
+    return SGFEM_OK;
+}
+
+// ------------------------------------------------------------------ layout kernels
+// stage: caller layout, FP64, column-major n x P.  X: device layout (T), n x ld.
+template <typename T>
+__global__ void k_to_device(const double* __restrict__ stage, T* __restrict__ X, const int* __restrict__ iperm,
+                            int n, int P, int ld) {
+    __shared__ double tile[32][33];
+    int i0 = blockIdx.x * 32, mu0 = blockIdx.y * 32;
+    int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+    for (int r = ty; r < 32; r += 8) {
+        int mu = mu0 + r, i = i0 + tx;
+        tile[r][tx] = (mu < P && i < n) ? stage[(size_t)mu * n + i] : 0.0;
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+        int i = i0 + r, mu = mu0 + tx;
+        if (i < n && mu < ld) X[(size_t)iperm[i] * ld + mu] = (T)tile[tx][r];
+    }
+}
+
+template <typename T>
+__global__ void k_from_device(const T* __restrict__ X, double* __restrict__ stage, const int* __restrict__ iperm,
+                              int n, int P, int ld) {
+    __shared__ double tile[32][33];
+    int i0 = blockIdx.x * 32, mu0 = blockIdx.y * 32;
+    int tx = threadIdx.x, ty = threadIdx.y;
+    for (int r = ty; r < 32; r += 8) {
+        int i = i0 + r, mu = mu0 + tx;
+        tile[r][tx] = (i < n && mu < P) ? (double)X[(size_t)iperm[i] * ld + mu] : 0.0;
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+        int mu = mu0 + r, i = i0 + tx;
+        if (mu < P && i < n) stage[(size_t)mu * n + i] = tile[tx][r];
+    }
+}
+
+int sg_launch_to_device(sgfem_context* ctx, const double* stage, void* X, int precision) {
+    dim3 block(32, 8), grid((unsigned)((ctx->n + 31) / 32), (unsigned)((ctx->ld + 31) / 32));
+    if (precision == SGFEM_FP64)
+        k_to_device<double><<<grid, block, 0, ctx->stream>>>(stage, (double*)X, ctx->d_iperm, (int)ctx->n, (int)ctx->P, (int)ctx->ld);
+    else
+        k_to_device<float><<<grid, block, 0, ctx->stream>>>(stage, (float*)X, ctx->d_iperm, (int)ctx->n, (int)ctx->P, (int)ctx->ld);
+    SG_CUDA(ctx, cudaGetLastError());
+    return SGFEM_OK;
+}
+
+int sg_launch_from_device(sgfem_context* ctx, const void* X, double* stage, int precision) {
+    dim3 block(32, 8), grid((unsigned)((ctx->n + 31) / 32), (unsigned)((ctx->P + 31) / 32));
+    if (precision == SGFEM_FP64)
+        k_from_device<double><<<grid, block, 0, ctx->stream>>>((const double*)X, stage, ctx->d_iperm, (int)ctx->n, (int)ctx->P, (int)ctx->ld);
+    else
+        k_from_device<float><<<grid, block, 0, ctx->stream>>>((const float*)X, stage, ctx->d_iperm, (int)ctx->n, (int)ctx->P, (int)ctx->ld);
+    SG_CUDA(ctx, cudaGetLastError());
+    return SGFEM_OK;
+}
+
+static int check_precision(sgfem_context* ctx, int precision) {
+    if (precision != SGFEM_FP64 && precision != SGFEM_FP32)
+        return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "precision must be SGFEM_FP64 or SGFEM_FP32");
+    return SGFEM_OK;
+}
+
+// host vector (caller layout) -> device buffer (device layout)
+static int host_to_device_layout(sgfem_context* ctx, const double* x, void* dst, int precision) {
+    size_t hb = (size_t)ctx->n * ctx->P * sizeof(double);
+    SG_TRY(sg_ensure(ctx, ctx->w_stage, hb));
+    SG_CUDA(ctx, cudaMemcpyAsync(ctx->w_stage.p, x, hb, cudaMemcpyHostToDevice, ctx->stream));
+    return sg_launch_to_device(ctx, (const double*)ctx->w_stage.p, dst, precision);
+}
+
+static int device_to_host_layout(sgfem_context* ctx, const void* src, double* y, int precision) {
+    size_t hb = (size_t)ctx->n * ctx->P * sizeof(double);
+    SG_TRY(sg_ensure(ctx, ctx->w_stage, hb));
+    SG_TRY(sg_launch_from_device(ctx, src, (double*)ctx->w_stage.p, precision));
+    SG_CUDA(ctx, cudaMemcpyAsync(y, ctx->w_stage.p, hb, cudaMemcpyDeviceToHost, ctx->stream));
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SGFEM_OK;
+}
+
+extern "C" int sgfem_device_layout(const sgfem_context* ctx, int64_t* n_dev, int64_t* ld) {
+    if (!ctx || !ctx->finalized) return SGFEM_ERR_STATE;
+    if (n_dev) *n_dev = ctx->n;
+    if (ld) *ld = ctx->ld;
+    return SGFEM_OK;
+}
+
+extern "C" int sgfem_to_device_layout(sgfem_context* ctx, const double* x_host, void* x_dev, int precision) {
+    SG_TRY(sg_check_ready(ctx));
+    SG_TRY(check_precision(ctx, precision));
+    if (!x_host || !x_dev) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "null pointer");
+    SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    SG_TRY(host_to_device_layout(ctx, x_host, x_dev, precision));
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SGFEM_OK;
+}
+
+extern "C" int sgfem_from_device_layout(sgfem_context* ctx, const void* x_dev, double* x_host, int precision) {
+    SG_TRY(sg_check_ready(ctx));
+    SG_TRY(check_precision(ctx, precision));
+    if (!x_host || !x_dev) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "null pointer");
+    SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    return device_to_host_layout(ctx, x_dev, x_host, precision);
+}
+
+extern "C" int sgfem_apply(sgfem_context* ctx, const double* x, double* y, int precision) {
+    SG_TRY(sg_check_ready(ctx));
+    SG_TRY(check_precision(ctx, precision));
+    if (!x || !y) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "null pointer");
+    SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    size_t vb = sg_vec_bytes(ctx, precision);
+    SG_TRY(sg_ensure(ctx, ctx->w_vec[0], vb));
+    SG_TRY(sg_ensure(ctx, ctx->w_vec[1], vb));
+    SG_TRY(host_to_device_layout(ctx, x, ctx->w_vec[0].p, precision));
+    SG_TRY(sg_launch_apply(ctx, precision, ctx->w_vec[0].p, ctx->w_vec[1].p, nullptr, nullptr, nullptr));
+    return device_to_host_layout(ctx, ctx->w_vec[1].p, y, precision);
+}
+
+extern "C" int sgfem_apply_device(sgfem_context* ctx, const void* x_dev, void* y_dev, int precision) {
+    SG_TRY(sg_check_ready(ctx));
+    SG_TRY(check_precision(ctx, precision));
+    if (!x_dev || !y_dev) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "null pointer");
+    SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    SG_TRY(sg_launch_apply(ctx, precision, x_dev, y_dev, nullptr, nullptr, nullptr));
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SGFEM_OK;
+}
+
+extern "C" int sgfem_time_apply(sgfem_context* ctx, int precision, int reps, double* ms_per_apply) {
+    SG_TRY(sg_check_ready(ctx));
+    SG_TRY(check_precision(ctx, precision));
+    if (reps <= 0 || !ms_per_apply) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad reps");
+    SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    size_t vb = sg_vec_bytes(ctx, precision);
+    SG_TRY(sg_ensure(ctx, ctx->w_vec[0], vb));
+    SG_TRY(sg_ensure(ctx, ctx->w_vec[1], vb));
+    SG_CUDA(ctx, cudaMemsetAsync(ctx->w_vec[0].p, 0, vb, ctx->stream));
+    SG_TRY(sg_launch_apply(ctx, precision, ctx->w_vec[0].p, ctx->w_vec[1].p, nullptr, nullptr, nullptr));
+    SG_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    for (int r = 0; r < reps; ++r) {
+        // alternate the roles so consecutive launches do not reuse one output in L2
+        const void* xin = (r & 1) ? ctx->w_vec[1].p : ctx->w_vec[0].p;
+        void* yout = (r & 1) ? ctx->w_vec[0].p : ctx->w_vec[1].p;
+        SG_TRY(sg_launch_apply(ctx, precision, xin, yout, nullptr, nullptr, nullptr));
+    }
+    SG_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    SG_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+    float ms = 0.f;
+    SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    *ms_per_apply = ms / reps;
+    return SGFEM_OK;
+}

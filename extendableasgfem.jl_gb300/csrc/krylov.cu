@@ -1,0 +1,496 @@
+// K3: device-resident preconditioned CG and mixed-precision refinement.
+//
+// Replaces solve_primal! (src/modelproblems/solvers_poisson_primal.jl:130-169):
+//   * right-hand side b = x0 + e_1 (x) b0 with Dirichlet rows zeroed (:149-155),
+//     x0 the warm start taken from SGFEVector.entries;
+//   * the reference's left-preconditioned GMRES (Krylov.gmres, :160) becomes
+//     PCG: the SG operator of PoissonProblemPrimal is symmetric positive
+//     definite on interior dofs and the mean-based preconditioner is SPD, so
+//     both reach the same solution; PCG needs two inner products per step.
+// Iteration (all scalars live in device memory, no host round trip):
+//   q = A p (+ p'q partials)      -> finalize: alpha = rho / p'q
+//   x += alpha p, r -= alpha q    -> finalize: rr, convergence flag
+//   z = B r (three lattice passes, r'z by Parseval) -> finalize: beta
+//   p = z + beta p (fused into the last preconditioner pass)
+// Reductions are per-block FP64 partials summed by one block in a fixed
+// order, so results are bitwise reproducible run to run.  A batch of
+// iterations is captured once in a CUDA graph and replayed; kernels return
+// immediately once the convergence flag is set.
+// SGFEM_MIXED: FP64 x, b and true residual r = b - A x; each refinement step
+// solves A d = r with FP32 PCG (FP32 operator values, vectors and
+// accumulation; FP64 inner products) to inner_rtol and adds d to x in FP64.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "sgfem_internal.h"
+
+namespace {
+
+constexpr int VT = 256;  // threads of vector kernels
+
+enum FinMode { FIN_ALPHA = 0, FIN_RR = 1, FIN_BETA = 2, FIN_TOL = 3, FIN_SUM = 4 };
+
+struct FinArgs {
+    double rtol2;  // FIN_TOL: tol2 = rtol2 * sum
+    int maxit;
+};
+
+__global__ void k_finalize(const double* __restrict__ partials, int nb, KrylovScalars* __restrict__ s, int mode,
+                           FinArgs fa, double* __restrict__ out_sum) {
+    __shared__ double red[VT];
+    double v = 0.0;
+    for (int i = threadIdx.x; i < nb; i += VT) v += partials[i];
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = VT / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    const double sum = red[0];
+    if (mode == FIN_SUM) {
+        *out_sum = sum;
+        return;
+    }
+    if (mode == FIN_TOL) {
+        s->tol2 = fa.rtol2 * sum;
+        if (out_sum) *out_sum = sum;
+        return;
+    }
+    if (s->done) return;
+    if (mode == FIN_ALPHA) {
+        s->pq = sum;
+        if (!isfinite(sum)) { s->status = SGFEM_ERR_NONFINITE; s->done = 1; return; }
+        if (!(sum > 0.0)) { s->status = SGFEM_ERR_BREAKDOWN; s->done = 1; return; }
+        s->alpha = s->rho / sum;
+    } else if (mode == FIN_RR) {
+        s->rr = sum;
+        if (!s->first) s->iters += 1;
+        if (!isfinite(sum)) { s->status = SGFEM_ERR_NONFINITE; s->done = 1; return; }
+        if (sum <= s->tol2) { s->done = 1; return; }
+        if (s->iters >= fa.maxit) { s->status = SGFEM_ERR_MAXIT; s->done = 1; return; }
+    } else if (mode == FIN_BETA) {
+        if (!isfinite(sum)) { s->status = SGFEM_ERR_NONFINITE; s->done = 1; return; }
+        if (!(sum > 0.0)) { s->status = SGFEM_ERR_BREAKDOWN; s->done = 1; return; }
+        if (s->first) {
+            s->beta = 0.0;
+            s->first = 0;
+        } else {
+            s->beta = sum / s->rho;
+        }
+        s->rho = sum;
+    }
+}
+
+__device__ __forceinline__ void block_partial(double acc, double* partials) {
+    __shared__ double red[VT / 32];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < VT / 32; ++w) s += red[w];
+        partials[blockIdx.x] = s;
+    }
+}
+
+// x += alpha p ; r -= alpha q ; partial ||r||^2
+template <typename T>
+__global__ void __launch_bounds__(VT) k_update(T* __restrict__ x, const T* __restrict__ p, T* __restrict__ r,
+                                               const T* __restrict__ q, size_t total, const KrylovScalars* __restrict__ s,
+                                               double* __restrict__ partials) {
+    if (s->done) return;
+    const T alpha = (T)s->alpha;
+    double acc = 0.0;
+    for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT) {
+        x[i] = fma(alpha, p[i], x[i]);
+        const T rn = fma(-alpha, q[i], r[i]);
+        r[i] = rn;
+        acc += (double)rn * (double)rn;
+    }
+    block_partial(acc, partials);
+}
+
+// r = b - ax ; partial ||r||^2
+__global__ void __launch_bounds__(VT) k_residual(const double* __restrict__ b, const double* __restrict__ ax,
+                                                 double* __restrict__ r, size_t total, double* __restrict__ partials) {
+    double acc = 0.0;
+    for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT) {
+        const double v = b[i] - ax[i];
+        r[i] = v;
+        acc += v * v;
+    }
+    block_partial(acc, partials);
+}
+
+// partial sum of a .* b
+template <typename T>
+__global__ void __launch_bounds__(VT) k_dot(const T* __restrict__ a, const T* __restrict__ b, size_t total,
+                                            double* __restrict__ partials) {
+    double acc = 0.0;
+    for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT)
+        acc += (double)a[i] * (double)b[i];
+    block_partial(acc, partials);
+}
+
+// r32 = (float) r64 ; d32 = 0 ; partial ||r32||^2
+__global__ void __launch_bounds__(VT) k_demote(const double* __restrict__ r64, float* __restrict__ r32,
+                                               float* __restrict__ d32, size_t total, double* __restrict__ partials) {
+    double acc = 0.0;
+    for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT) {
+        const float v = (float)r64[i];
+        r32[i] = v;
+        d32[i] = 0.0f;
+        acc += (double)v * (double)v;
+    }
+    block_partial(acc, partials);
+}
+
+// x64 += (double) d32
+__global__ void __launch_bounds__(VT) k_promote_add(double* __restrict__ x, const float* __restrict__ d, size_t total) {
+    for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT) x[i] += (double)d[i];
+}
+
+// b = (x0 or 0) + e_1 (x) b0, Dirichlet rows zeroed.  b0 in caller order.
+__global__ void k_build_rhs(const double* __restrict__ b0, const double* __restrict__ x0, double* __restrict__ b,
+                            const int* __restrict__ iperm, const unsigned char* __restrict__ bmask, int n, int ld,
+                            int use_x0) {
+    const size_t total = (size_t)n * ld;
+    for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT) {
+        const int row = (int)(i / ld);
+        b[i] = (use_x0 && !bmask[row]) ? x0[i] : 0.0;
+    }
+}
+
+__global__ void k_add_b0(const double* __restrict__ b0, double* __restrict__ b, const int* __restrict__ iperm,
+                         const unsigned char* __restrict__ bmask, int n, int ld) {
+    for (int i = blockIdx.x * VT + threadIdx.x; i < n; i += gridDim.x * VT) {
+        const int row = iperm[i];
+        if (!bmask[row]) b[(size_t)row * ld] += b0[i];
+    }
+}
+
+int vgrid(const sgfem_context* ctx) {
+    const int64_t total = ctx->n * ctx->ld;
+    return (int)std::max<int64_t>(1, std::min<int64_t>((total + VT * 4 - 1) / (VT * 4), (int64_t)ctx->num_sms * 8));
+}
+
+struct Solver {
+    sgfem_context* ctx;
+    int prec_kind;
+    double* partials;
+    KrylovScalars* s;
+
+    int fin(int nb, int mode, FinArgs fa = FinArgs{0.0, 0}, double* out = nullptr) {
+        k_finalize<<<1, VT, 0, ctx->stream>>>(partials, nb, s, mode, fa, out);
+        SG_CUDA(ctx, cudaGetLastError());
+        return SGFEM_OK;
+    }
+
+    // z = B r and p = z + beta p, with rho/beta finalized in between
+    template <typename T>
+    int precond_block(int precision, T* r, T* p, T* tmp, int maxit) {
+        int nb = 0;
+        FinArgs fa{0.0, maxit};
+        if (prec_kind == SGFEM_PREC_LATTICE) {
+            SG_TRY(sg_lat_pass_x(ctx, precision, r, tmp, s));
+            SG_TRY(sg_lat_pass_y(ctx, precision, tmp, partials, &nb, s));
+            SG_TRY(fin(nb, FIN_BETA, fa));
+            SG_TRY(sg_lat_pass_xinv(ctx, precision, tmp, p, 1, s));
+        } else {
+            const int identity = prec_kind == SGFEM_PREC_NONE ? 1 : 0;
+            SG_TRY(sg_jacobi(ctx, precision, r, p, 2, identity, partials, &nb, s));
+            SG_TRY(fin(nb, FIN_BETA, fa));
+            SG_TRY(sg_jacobi(ctx, precision, r, p, 1, identity, nullptr, nullptr, s));
+        }
+        return SGFEM_OK;
+    }
+
+    template <typename T>
+    int iteration(int precision, T* x, T* r, T* p, T* q, T* tmp, int maxit) {
+        int nb = 0;
+        FinArgs fa{0.0, maxit};
+        SG_TRY(sg_launch_apply(ctx, precision, p, q, partials, &nb, s));
+        SG_TRY(fin(nb, FIN_ALPHA, fa));
+        const size_t total = (size_t)ctx->n * ctx->ld;
+        const int g = vgrid(ctx);
+        k_update<T><<<g, VT, 0, ctx->stream>>>(x, p, r, q, total, s, partials);
+        SG_CUDA(ctx, cudaGetLastError());
+        SG_TRY(fin(g, FIN_RR, fa));
+        SG_TRY(precond_block<T>(precision, r, p, tmp, maxit));
+        return SGFEM_OK;
+    }
+
+    // PCG on A x = b given r = b - A x on entry, stopping when ||r||^2 <= s->tol2
+    // (set by the caller).  Returns the status; iterations in *iters.
+    template <typename T>
+    int pcg(int precision, T* x, T* r, T* p, T* q, T* tmp, int maxit, int check_every, int* iters) {
+        const size_t vb = (size_t)ctx->n * ctx->ld * sizeof(T);
+        SG_CUDA(ctx, cudaMemsetAsync(p, 0, vb, ctx->stream));
+        // initial residual norm and flags
+        {
+            // reset everything except tol2
+            KrylovScalars* h = ctx->h_scal;
+            SG_CUDA(ctx, cudaMemcpyAsync(h, s, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, ctx->stream));
+            SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            double tol2 = h->tol2;
+            std::memset(h, 0, sizeof(KrylovScalars));
+            h->tol2 = tol2;
+            h->first = 1;
+            SG_CUDA(ctx, cudaMemcpyAsync(s, h, sizeof(KrylovScalars), cudaMemcpyHostToDevice, ctx->stream));
+        }
+        const size_t total = (size_t)ctx->n * ctx->ld;
+        const int g = vgrid(ctx);
+        k_dot<T><<<g, VT, 0, ctx->stream>>>(r, r, total, partials);
+        SG_CUDA(ctx, cudaGetLastError());
+        SG_TRY(fin(g, FIN_RR, FinArgs{0.0, maxit}));
+        SG_TRY(precond_block<T>(precision, r, p, tmp, maxit));
+
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        SG_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        int st = SGFEM_OK;
+        for (int k = 0; k < check_every && st == SGFEM_OK; ++k) st = iteration<T>(precision, x, r, p, q, tmp, maxit);
+        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+        if (st != SGFEM_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return st;
+        }
+        SG_CUDA(ctx, ce);
+        SG_CUDA(ctx, cudaGraphInstantiate(&exec, graph, 0));
+        int status = SGFEM_OK;
+        for (;;) {
+            SG_CUDA(ctx, cudaMemcpyAsync(ctx->h_scal, s, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, ctx->stream));
+            SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            if (ctx->h_scal->done) {
+                status = ctx->h_scal->status;
+                break;
+            }
+            cudaError_t le = cudaGraphLaunch(exec, ctx->stream);
+            if (le != cudaSuccess) {
+                cudaGraphExecDestroy(exec);
+                cudaGraphDestroy(graph);
+                return sg_cuda_fail(ctx, le, "cudaGraphLaunch");
+            }
+        }
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
+        *iters = ctx->h_scal->iters;
+        return status;
+    }
+};
+
+int status_message(sgfem_context* ctx, int status) {
+    if (status == SGFEM_ERR_BREAKDOWN) return sg_fail(ctx, status, "PCG breakdown (p'Ap <= 0 or r'z <= 0)");
+    if (status == SGFEM_ERR_NONFINITE) return sg_fail(ctx, status, "non-finite value in a PCG iterate");
+    if (status == SGFEM_ERR_MAXIT) return sg_fail(ctx, status, "tolerance not reached within maxit");
+    return status;
+}
+
+}  // namespace
+
+extern "C" void sgfem_default_options(sgfem_solve_options* o) {
+    if (!o) return;
+    o->precision = SGFEM_MIXED;
+    o->preconditioner = SGFEM_PREC_LATTICE;
+    o->rtol = 1e-8;
+    o->maxit = 2000;
+    o->inner_rtol = 1e-5;
+    o->reference_rhs = 1;
+    o->check_every = 8;
+}
+
+extern "C" int sgfem_precondition(sgfem_context* ctx, const double* b, double* y, int kind, int precision) {
+    SG_TRY(sg_check_ready(ctx));
+    if (!b || !y) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "null pointer");
+    if (precision != SGFEM_FP64 && precision != SGFEM_FP32) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad precision");
+    if (kind == SGFEM_PREC_LATTICE && !ctx->lattice)
+        return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice preconditioner unavailable (dofs do not form a power-of-two lattice)");
+    if (kind != SGFEM_PREC_LATTICE && kind != SGFEM_PREC_JACOBI && kind != SGFEM_PREC_NONE)
+        return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad preconditioner kind");
+    SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t vb = sg_vec_bytes(ctx, precision);
+    for (int i = 0; i < 3; ++i) SG_TRY(sg_ensure(ctx, ctx->w_vec[i], vb));
+    SG_TRY(sgfem_to_device_layout(ctx, b, ctx->w_vec[0].p, precision));
+    SG_CUDA(ctx, cudaMemsetAsync(ctx->w_vec[1].p, 0, vb, ctx->stream));
+    if (kind == SGFEM_PREC_LATTICE) {
+        SG_TRY(sg_lat_pass_x(ctx, precision, ctx->w_vec[0].p, ctx->w_vec[2].p, nullptr));
+        SG_TRY(sg_lat_pass_y(ctx, precision, ctx->w_vec[2].p, nullptr, nullptr, nullptr));
+        SG_TRY(sg_lat_pass_xinv(ctx, precision, ctx->w_vec[2].p, ctx->w_vec[1].p, 0, nullptr));
+    } else if (kind == SGFEM_PREC_JACOBI) {
+        SG_TRY(sg_jacobi(ctx, precision, ctx->w_vec[0].p, ctx->w_vec[1].p, 0, 0, nullptr, nullptr, nullptr));
+    } else {
+        SG_CUDA(ctx, cudaMemcpyAsync(ctx->w_vec[1].p, ctx->w_vec[0].p, vb, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    return sgfem_from_device_layout(ctx, ctx->w_vec[1].p, y, precision);
+}
+
+// core solve on device buffers: x64 (in/out, device layout), b0 host (caller order)
+static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const sgfem_solve_options* o,
+                      sgfem_solve_stats* st) {
+    if (o->precision != SGFEM_FP64 && o->precision != SGFEM_FP32 && o->precision != SGFEM_MIXED)
+        return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad precision");
+    int prec_kind = o->preconditioner;
+    if (prec_kind == SGFEM_PREC_LATTICE && !ctx->lattice)
+        return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice preconditioner unavailable (dofs do not form a power-of-two lattice)");
+    if (prec_kind != SGFEM_PREC_LATTICE && prec_kind != SGFEM_PREC_JACOBI && prec_kind != SGFEM_PREC_NONE)
+        return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad preconditioner kind");
+    if (!(o->rtol > 0.0) || o->maxit <= 0) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "rtol must be > 0 and maxit > 0");
+    const int check_every = std::max(1, std::min(o->check_every, 64));
+    const size_t n64 = sg_vec_bytes(ctx, SGFEM_FP64), n32 = sg_vec_bytes(ctx, SGFEM_FP32);
+    const size_t total = (size_t)ctx->n * ctx->ld;
+    // buffers: 0 b64, 1 r64, 2 t64/p64, 3 q64, 4 tmp64 ; 5 d32, 6 r32, 7 p32, 8 q32, 9 tmp32
+    SG_TRY(sg_ensure(ctx, ctx->w_vec[0], n64));
+    SG_TRY(sg_ensure(ctx, ctx->w_vec[1], n64));
+    SG_TRY(sg_ensure(ctx, ctx->w_vec[2], n64));
+    SG_TRY(sg_ensure(ctx, ctx->w_vec[3], n64));
+    SG_TRY(sg_ensure(ctx, ctx->w_vec[4], n64));
+    const bool low = o->precision != SGFEM_FP64;
+    if (low)
+        for (int i = 5; i < 10; ++i) SG_TRY(sg_ensure(ctx, ctx->w_vec[i], n32));
+    const int maxblocks = std::max<int>(ctx->num_sms * 8, ctx->lattice ? (ctx->Nl - 1) * (int)((ctx->ld + 31) / 32) : 1);
+    SG_TRY(sg_ensure(ctx, ctx->w_partials, (size_t)(maxblocks + 8) * sizeof(double)));
+    double* partials = (double*)ctx->w_partials.p;
+    double* b = (double*)ctx->w_vec[0].p;
+    double* r = (double*)ctx->w_vec[1].p;
+    double* t = (double*)ctx->w_vec[2].p;
+    double* q = (double*)ctx->w_vec[3].p;
+    double* tmp = (double*)ctx->w_vec[4].p;
+
+    // b0 upload (caller order) into the staging buffer
+    SG_TRY(sg_ensure(ctx, ctx->w_stage, (size_t)ctx->n * sizeof(double) * 2));
+    double* d_b0 = (double*)ctx->w_stage.p;
+    SG_CUDA(ctx, cudaMemcpyAsync(d_b0, b0, (size_t)ctx->n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+
+    SG_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    const int g = vgrid(ctx);
+    k_build_rhs<<<g, VT, 0, ctx->stream>>>(d_b0, x64, b, ctx->d_iperm, ctx->d_bmask, (int)ctx->n, (int)ctx->ld,
+                                          o->reference_rhs ? 1 : 0);
+    k_add_b0<<<(int)std::min<int64_t>((ctx->n + VT - 1) / VT, 4096), VT, 0, ctx->stream>>>(
+        d_b0, b, ctx->d_iperm, ctx->d_bmask, (int)ctx->n, (int)ctx->ld);
+    SG_CUDA(ctx, cudaGetLastError());
+
+    Solver S{ctx, prec_kind, partials, ctx->d_scal};
+    // ||b||^2 -> host
+    k_dot<double><<<g, VT, 0, ctx->stream>>>(b, b, total, partials);
+    double* d_sum = partials + maxblocks + 2;
+    SG_TRY(S.fin(g, FIN_SUM, FinArgs{0.0, 0}, d_sum));
+    double bb = 0.0;
+    SG_CUDA(ctx, cudaMemcpyAsync(&bb, d_sum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    st->iterations = 0;
+    st->outer_iterations = 0;
+    st->fp64_applies = 0;
+    st->relres = 0.0;
+    st->apply_ms = -1.0;
+    st->precond_ms = -1.0;
+    if (!std::isfinite(bb)) return sg_fail(ctx, SGFEM_ERR_NONFINITE, "non-finite right-hand side");
+    if (bb == 0.0) {
+        SG_CUDA(ctx, cudaMemsetAsync(x64, 0, n64, ctx->stream));
+        SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        st->time_ms = 0.0;
+        return SGFEM_OK;
+    }
+    const double rtol2 = o->rtol * o->rtol;
+
+    // true FP64 residual r = b - A x ; returns ||r||^2 on host
+    auto true_residual = [&](double* rr_out) -> int {
+        int nb = 0;
+        SG_TRY(sg_launch_apply(ctx, SGFEM_FP64, x64, t, nullptr, &nb, nullptr));
+        k_residual<<<g, VT, 0, ctx->stream>>>(b, t, r, total, partials);
+        SG_CUDA(ctx, cudaGetLastError());
+        SG_TRY(S.fin(g, FIN_SUM, FinArgs{0.0, 0}, d_sum));
+        SG_CUDA(ctx, cudaMemcpyAsync(rr_out, d_sum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        st->fp64_applies += 1;
+        return SGFEM_OK;
+    };
+
+    int status = SGFEM_OK;
+    double rr = 0.0;
+    SG_TRY(true_residual(&rr));
+    int remaining = o->maxit;
+    if (!low) {
+        // FP64 PCG; restart from the true residual if the recurrence drifted
+        for (int restart = 0; restart < 8; ++restart) {
+            if (!std::isfinite(rr)) { status = SGFEM_ERR_NONFINITE; break; }
+            if (rr <= rtol2 * bb || remaining <= 0) break;
+            KrylovScalars h{};
+            h.tol2 = rtol2 * bb;
+            SG_CUDA(ctx, cudaMemcpyAsync(ctx->d_scal, &h, sizeof(KrylovScalars), cudaMemcpyHostToDevice, ctx->stream));
+            int it = 0;
+            status = S.pcg<double>(SGFEM_FP64, x64, r, t, q, tmp, remaining, check_every, &it);
+            st->iterations += it;
+            st->outer_iterations += 1;
+            remaining -= it;
+            SG_TRY(true_residual(&rr));
+            if (status != SGFEM_OK) break;
+        }
+    } else {
+        float* d32 = (float*)ctx->w_vec[5].p;
+        float* r32 = (float*)ctx->w_vec[6].p;
+        float* p32 = (float*)ctx->w_vec[7].p;
+        float* q32 = (float*)ctx->w_vec[8].p;
+        float* tmp32 = (float*)ctx->w_vec[9].p;
+        const double in2 = o->precision == SGFEM_FP32 ? rtol2 : o->inner_rtol * o->inner_rtol;
+        for (int outer = 0; outer < 64; ++outer) {
+            if (!std::isfinite(rr)) { status = SGFEM_ERR_NONFINITE; break; }
+            if (rr <= rtol2 * bb) break;
+            if (remaining <= 0) { status = SGFEM_ERR_MAXIT; break; }
+            k_demote<<<g, VT, 0, ctx->stream>>>(r, r32, d32, total, partials);
+            SG_CUDA(ctx, cudaGetLastError());
+            // inner target: reduce ||r|| by inner_rtol, but never below what the outer tolerance needs
+            const double want = std::max(in2, 0.25 * rtol2 * bb / rr);
+            SG_TRY(S.fin(g, FIN_TOL, FinArgs{want, 0}, nullptr));
+            int it = 0;
+            int s2 = S.pcg<float>(SGFEM_FP32, d32, r32, p32, q32, tmp32, remaining, check_every, &it);
+            st->iterations += it;
+            st->outer_iterations += 1;
+            remaining -= it;
+            if (s2 == SGFEM_ERR_BREAKDOWN || s2 == SGFEM_ERR_NONFINITE) { status = s2; break; }
+            k_promote_add<<<g, VT, 0, ctx->stream>>>(x64, d32, total);
+            SG_CUDA(ctx, cudaGetLastError());
+            SG_TRY(true_residual(&rr));
+            if (o->precision == SGFEM_FP32) break;  // plain FP32 PCG: no refinement
+        }
+    }
+    SG_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    SG_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+    float ms = 0.f;
+    SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    st->time_ms = ms;
+    st->relres = std::sqrt(rr / bb);
+    if (status == SGFEM_OK && !(st->relres <= o->rtol)) status = (o->precision == SGFEM_FP32) ? SGFEM_OK : SGFEM_ERR_MAXIT;
+    return status_message(ctx, status);
+}
+
+extern "C" int sgfem_solve_device(sgfem_context* ctx, const double* b0, void* x_dev, const sgfem_solve_options* opts,
+                                  sgfem_solve_stats* stats) {
+    SG_TRY(sg_check_ready(ctx));
+    if (!b0 || !x_dev) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "null pointer");
+    sgfem_solve_options o;
+    if (opts) o = *opts; else sgfem_default_options(&o);
+    sgfem_solve_stats s{};
+    SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    int rc = solve_core(ctx, b0, (double*)x_dev, &o, &s);
+    if (stats) *stats = s;
+    return rc;
+}
+
+extern "C" int sgfem_solve(sgfem_context* ctx, const double* b0, double* x_inout, const sgfem_solve_options* opts,
+                           sgfem_solve_stats* stats) {
+    SG_TRY(sg_check_ready(ctx));
+    if (!b0 || !x_inout) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "null pointer");
+    SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t n64 = sg_vec_bytes(ctx, SGFEM_FP64);
+    SG_TRY(sg_ensure(ctx, ctx->w_vec[10], n64));
+    SG_TRY(sgfem_to_device_layout(ctx, x_inout, ctx->w_vec[10].p, SGFEM_FP64));
+    int rc = sgfem_solve_device(ctx, b0, ctx->w_vec[10].p, opts, stats);
+    if (rc != SGFEM_OK && rc != SGFEM_ERR_MAXIT) return rc;
+    std::string keep = ctx->err;
+    int rc2 = sgfem_from_device_layout(ctx, ctx->w_vec[10].p, x_inout, SGFEM_FP64);
+    if (rc2 != SGFEM_OK) return rc2;
+    ctx->err = keep;
+    return rc;
+}

@@ -1,0 +1,404 @@
+// K2: the mean-based preconditioner  Z = (I (x) (a0 L)^-1) R  on sm_103a.
+//
+// Replaces MyPreconditionerPrimal / ldiv! (src/modelproblems/
+// solvers_poisson_primal.jl:23-78), which applies LU(K_0)^-1 (K_0 with 1e60 on
+// the boundary diagonals) to every mode.  When the dofs form a uniform
+// lattice of the unit square (P1 or P2 on grid_unitsquare-type meshes), L is
+// the 5-point Laplacian of that lattice on interior points:
+//   * P1 with the diagonal split: K_0 restricted to interior rows equals
+//     a0 * L exactly, so this IS the reference's preconditioner;
+//   * P2: the lattice holds vertices and edge midpoints and L is the P1
+//     stiffness of the once-refined mesh, spectrally equivalent to K_0 with
+//     eigenvalues of L^-1 K_0 / a0 in [2/3, 4/3] for every mesh size.
+// L is diagonalised by the orthonormal sine transform S (DST-I):
+//   L^-1 = S diag(1 / (lam_kx + lam_ky)) S,  lam_k = 4 sin^2(pi k / (2 Nl)).
+// The transform of a line of Nl-1 interior values is computed with one
+// complex FFT of length Nl/2 (radix-2 decimation in frequency, bit-reversal,
+// real-FFT unpacking, running sum for the odd outputs).
+//
+// Three passes over the SG vector (device layout: row-major dofs x modes):
+//   pass X    : for each lattice row,    T = DST_x(R)
+//   pass Y    : for each lattice column, T = DST_y(scale .* DST_y(T));
+//               r'z = sum (DST_y T)^2 * scale  (Parseval) as block partials
+//   pass X^-1 : for each lattice row,    z = DST_x(T); out = z or z + beta*out
+// A CTA owns one line and 32 consecutive modes: the tile is points x 32 modes
+// in shared memory, every lane works on its own mode, so each global access
+// is a contiguous 32-mode segment of one dof and every shared-memory access
+// is bank-conflict free.
+#include <cmath>
+#include <vector>
+
+#include "sgfem_internal.h"
+
+namespace {
+
+constexpr int LAT_THREADS = 256;
+constexpr int LAT_WARPS = LAT_THREADS / 32;
+
+struct LatGeom {
+    int Nl;     // transform length n = Nl (power of two), interior points N = Nl - 1
+    int lg;     // log2(Nl)
+    int ld;     // row stride of SG vectors
+    int nchunk; // ceil(ld / 32)
+};
+
+// table layout (length 3*Nl/2 + 1):
+//   [0, Nl/2)          cos(2 pi k / Nl)
+//   [Nl/2, Nl)         sin(2 pi k / Nl)
+//   [Nl, 3Nl/2 + 1)    sin(pi j / Nl), j = 0..Nl/2
+template <typename T>
+__device__ void dst_line(T* tile, const T* tab, int Nl, int lg) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int L = Nl >> 1;
+    const T* cs = tab;
+    const T* sn = tab + L;
+    const T* sh = tab + Nl;
+    // pre-processing: y_j = s_j (x_j + x_{n-j}) + (x_j - x_{n-j}) / 2, y_0 = 0
+    for (int j = 1 + warp; j <= L; j += LAT_WARPS) {
+        const T a = tile[j * 32 + lane];
+        const T b = tile[(Nl - j) * 32 + lane];
+        const T s = sh[j] * (a + b);
+        const T d = T(0.5) * (a - b);
+        tile[j * 32 + lane] = s + d;
+        if (j != L) tile[(Nl - j) * 32 + lane] = s - d;
+    }
+    if (warp == 0) tile[lane] = T(0);
+    __syncthreads();
+    // complex FFT (sign +) of z_k = (y_2k, y_2k+1), k < L, decimation in frequency
+    for (int s = lg - 2; s >= 0; --s) {
+        const int h = 1 << s;       // half span
+        const int tstep = Nl >> (s + 1);  // twiddle index step: n / (2h)
+        for (int b = warp; b < (L >> 1); b += LAT_WARPS) {
+            const int g = b >> s, t = b & (h - 1);
+            const int i1 = 2 * g * h + t, i2 = i1 + h;
+            T* z1 = tile + 2 * i1 * 32 + lane;
+            T* z2 = tile + 2 * i2 * 32 + lane;
+            const T ar = z1[0], ai = z1[32], cr = z2[0], ci = z2[32];
+            const T dr = ar - cr, di = ai - ci;
+            z1[0] = ar + cr;
+            z1[32] = ai + ci;
+            const int ti = t * tstep;
+            const T wr = cs[ti], wi = sn[ti];
+            z2[0] = dr * wr - di * wi;
+            z2[32] = dr * wi + di * wr;
+        }
+        __syncthreads();
+    }
+    // bit reversal of the L complex slots
+    for (int k = warp; k < L; k += LAT_WARPS) {
+        const int r = (int)(__brev((unsigned)k) >> (32 - (lg - 1)));
+        if (k < r) {
+            T* a = tile + 2 * k * 32 + lane;
+            T* c = tile + 2 * r * 32 + lane;
+            const T t0 = a[0], t1 = a[32];
+            a[0] = c[0];
+            a[32] = c[32];
+            c[0] = t0;
+            c[32] = t1;
+        }
+    }
+    __syncthreads();
+    // unpack F_k = E_k + w^k O_k for the pair (k, L-k); write X_2k = Im F_k at 2k,
+    // Re F_k at 2k+1 (prefix-summed below)
+    for (int k = warp; k <= (L >> 1); k += LAT_WARPS) {
+        const int kc = (L - k) & (L - 1);
+        T* a = tile + 2 * k * 32 + lane;
+        T* c = tile + 2 * kc * 32 + lane;
+        const T zr = a[0], zi = a[32], yr = c[0], yi = c[32];
+        // E_k = (Z_k + conj Z_{L-k}) / 2 ; O_k = (Z_k - conj Z_{L-k}) / (2i)
+        const T er = T(0.5) * (zr + yr), ei = T(0.5) * (zi - yi);
+        const T orr = T(0.5) * (zi + yi), oi = T(-0.5) * (zr - yr);
+        const T wr = cs[k], wi = sn[k];
+        const T fr = er + wr * orr - wi * oi, fi = ei + wr * oi + wi * orr;
+        if (kc != k) {
+            // F_{L-k}: E_{L-k} = conj E_k, O_{L-k} = conj O_k, w^{L-k} = -conj w^k
+            const T gr = er - wr * orr + wi * oi;
+            const T gi = -ei + wr * oi + wi * orr;
+            c[0] = gi;
+            c[32] = gr;
+        }
+        a[0] = fi;
+        a[32] = fr;
+    }
+    __syncthreads();
+    // odd outputs: X_1 = R_0 / 2, X_{2k+1} = X_{2k-1} + R_k  (chunked scan over k)
+    __shared__ T part[LAT_WARPS][32];
+    const int chunk = (L + LAT_WARPS - 1) / LAT_WARPS;
+    const int k0 = warp * chunk, k1 = min(L, k0 + chunk);
+    T run = T(0);
+    for (int k = k0; k < k1; ++k) run += (k == 0 ? T(0.5) : T(1)) * tile[(2 * k + 1) * 32 + lane];
+    part[warp][lane] = run;
+    __syncthreads();
+    T off = T(0);
+    for (int w = 0; w < warp; ++w) off += part[w][lane];
+    for (int k = k0; k < k1; ++k) {
+        off += (k == 0 ? T(0.5) : T(1)) * tile[(2 * k + 1) * 32 + lane];
+        tile[(2 * k + 1) * 32 + lane] = off;
+    }
+    __syncthreads();
+    if (warp == 0) tile[lane] = T(0);
+    __syncthreads();
+}
+
+template <typename T>
+__device__ void load_tab(T* stab, const T* tab, int Nl) {
+    for (int i = threadIdx.x; i < Nl + Nl / 2 + 1; i += blockDim.x) stab[i] = tab[i];
+}
+
+// row of the lattice point (line, p): pass along x (dir 0) or y (dir 1)
+__device__ __forceinline__ size_t lat_row(int dir, int line, int p, int Nl) {
+    return dir == 0 ? (size_t)line * (Nl + 1) + p : (size_t)p * (Nl + 1) + line;
+}
+
+template <typename T>
+__device__ void load_line(T* tile, const T* __restrict__ in, int dir, int line, int chunk, LatGeom g) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int mode = chunk * 32 + lane;
+    for (int p = 1 + warp; p < g.Nl; p += LAT_WARPS) {
+        T v = T(0);
+        if (mode < g.ld) v = in[lat_row(dir, line, p, g.Nl) * g.ld + mode];
+        tile[p * 32 + lane] = v;
+    }
+}
+
+// pass X (dir 0) / pass X^-1 (dir 0, store variants)
+template <typename T>
+__global__ void __launch_bounds__(LAT_THREADS)
+k_lat_pass_x(const T* __restrict__ in, T* __restrict__ out, const T* __restrict__ tab, LatGeom g, int mode,
+             const KrylovScalars* __restrict__ scal) {
+    if (scal && scal->done) return;
+    extern __shared__ unsigned char smem_raw[];
+    T* tile = reinterpret_cast<T*>(smem_raw);
+    T* stab = tile + (size_t)g.Nl * 32;
+    const int line = 1 + blockIdx.x / g.nchunk, chunk = blockIdx.x % g.nchunk;
+    load_tab(stab, tab, g.Nl);
+    load_line(tile, in, 0, line, chunk, g);
+    __syncthreads();
+    dst_line(tile, stab, g.Nl, g.lg);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int m = chunk * 32 + lane;
+    if (m >= g.ld) return;
+    T beta = T(0);
+    if (mode == 1 && scal && !scal->first) beta = (T)scal->beta;
+    for (int p = 1 + warp; p < g.Nl; p += LAT_WARPS) {
+        const size_t idx = lat_row(0, line, p, g.Nl) * g.ld + m;
+        const T z = tile[p * 32 + lane];
+        if (mode == 1)
+            out[idx] = z + beta * out[idx];
+        else
+            out[idx] = z;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(LAT_THREADS)
+k_lat_pass_y(T* __restrict__ buf, const T* __restrict__ tab, const T* __restrict__ scale, LatGeom g,
+             double* __restrict__ rz, const KrylovScalars* __restrict__ scal) {
+    if (scal && scal->done) return;
+    extern __shared__ unsigned char smem_raw[];
+    T* tile = reinterpret_cast<T*>(smem_raw);
+    T* stab = tile + (size_t)g.Nl * 32;
+    __shared__ double red[LAT_WARPS];
+    const int line = 1 + blockIdx.x / g.nchunk, chunk = blockIdx.x % g.nchunk;
+    load_tab(stab, tab, g.Nl);
+    load_line(tile, buf, 1, line, chunk, g);
+    __syncthreads();
+    dst_line(tile, stab, g.Nl, g.lg);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int N = g.Nl - 1;
+    double acc = 0.0;
+    for (int p = 1 + warp; p < g.Nl; p += LAT_WARPS) {
+        const T sc = scale[(size_t)(line - 1) * N + (p - 1)];
+        const T v = tile[p * 32 + lane];
+        acc += (double)v * (double)v * (double)sc;
+        tile[p * 32 + lane] = v * sc;
+    }
+    __syncthreads();
+    dst_line(tile, stab, g.Nl, g.lg);
+    const int m = chunk * 32 + lane;
+    if (m < g.ld) {
+        for (int p = 1 + warp; p < g.Nl; p += LAT_WARPS)
+            buf[lat_row(1, line, p, g.Nl) * g.ld + m] = tile[p * 32 + lane];
+    }
+    if (rz) {
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) red[warp] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0;
+            for (int w = 0; w < LAT_WARPS; ++w) s += red[w];
+            rz[blockIdx.x] = s;
+        }
+    }
+}
+
+LatGeom geom(const sgfem_context* ctx) {
+    LatGeom g;
+    g.Nl = ctx->Nl;
+    g.lg = ctx->lat_log2;
+    g.ld = (int)ctx->ld;
+    g.nchunk = (int)((ctx->ld + 31) / 32);
+    return g;
+}
+
+size_t lat_smem(const sgfem_context* ctx, size_t es) {
+    return ((size_t)ctx->Nl * 32 + ctx->Nl + ctx->Nl / 2 + 1) * es;
+}
+
+template <typename K>
+int set_smem(sgfem_context* ctx, K kernel, size_t smem) {
+    if (smem > 48 * 1024) SG_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return SGFEM_OK;
+}
+
+// ---------------------------------------------------------------- Jacobi
+template <typename T>
+__global__ void k_jacobi(const T* __restrict__ R, T* __restrict__ out, const T* __restrict__ dinv, int n, int ld,
+                         int identity, int mode, double* __restrict__ rz, const KrylovScalars* __restrict__ scal) {
+    if (scal && scal->done) return;
+    __shared__ double red[8];
+    T beta = T(0);
+    if (mode == 1 && scal && !scal->first) beta = (T)scal->beta;
+    double acc = 0.0;
+    const size_t total = (size_t)n * ld;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+        const int row = (int)(idx / ld);
+        T d = dinv[row];
+        if (identity) d = (d != T(0)) ? T(1) : T(0);
+        const T r = R[idx];
+        const T z = d * r;
+        if (mode == 2) {
+            acc += (double)r * (double)z;
+        } else if (mode == 1) {
+            if (d != T(0)) out[idx] = z + beta * out[idx];
+        } else {
+            out[idx] = z;
+        }
+    }
+    if (mode == 2) {
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+            rz[blockIdx.x] = s;
+        }
+    }
+}
+
+}  // namespace
+
+int sg_lattice_setup(sgfem_context* ctx) {
+    const int Nl = ctx->Nl;
+    if (Nl < 4 || (Nl & (Nl - 1)) != 0)
+        return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice preconditioner needs a power-of-two lattice");
+    int lg = 0;
+    while ((1 << lg) < Nl) ++lg;
+    ctx->lat_log2 = lg;
+    // smem: FP64 tile must fit
+    if (lat_smem(ctx, 8) > 220 * 1024)
+        return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice too large for the shared-memory line transform");
+    const double pi = 3.14159265358979323846;
+    const int L = Nl / 2;
+    std::vector<double> tab(Nl + L + 1);
+    for (int k = 0; k < L; ++k) {
+        tab[k] = std::cos(2.0 * pi * k / Nl);
+        tab[L + k] = std::sin(2.0 * pi * k / Nl);
+    }
+    for (int j = 0; j <= L; ++j) tab[Nl + j] = std::sin(pi * j / Nl);
+    std::vector<float> tab32(tab.begin(), tab.end());
+    const int N = Nl - 1;
+    std::vector<double> lam(Nl);
+    for (int k = 1; k < Nl; ++k) {
+        double s = std::sin(pi * k / (2.0 * Nl));
+        lam[k] = 4.0 * s * s;
+    }
+    // unnormalised transforms: T^2 = (Nl/2) I, so the composite carries (2/Nl)^2
+    std::vector<double> sc((size_t)N * N);
+    std::vector<float> sc32((size_t)N * N);
+    const double a0 = ctx->lat_scale;
+    const double norm = 4.0 / ((double)Nl * (double)Nl);
+    for (int kx = 1; kx < Nl; ++kx)
+        for (int ky = 1; ky < Nl; ++ky) {
+            double v = norm / (a0 * (lam[kx] + lam[ky]));
+            sc[(size_t)(kx - 1) * N + (ky - 1)] = v;
+            sc32[(size_t)(kx - 1) * N + (ky - 1)] = (float)v;
+        }
+    SG_CUDA(ctx, cudaMalloc(&ctx->d_lat_tab64, tab.size() * sizeof(double)));
+    SG_CUDA(ctx, cudaMemcpy(ctx->d_lat_tab64, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+    SG_CUDA(ctx, cudaMalloc(&ctx->d_lat_tab32, tab32.size() * sizeof(float)));
+    SG_CUDA(ctx, cudaMemcpy(ctx->d_lat_tab32, tab32.data(), tab32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    SG_CUDA(ctx, cudaMalloc(&ctx->d_lat_scale64, sc.size() * sizeof(double)));
+    SG_CUDA(ctx, cudaMemcpy(ctx->d_lat_scale64, sc.data(), sc.size() * sizeof(double), cudaMemcpyHostToDevice));
+    SG_CUDA(ctx, cudaMalloc(&ctx->d_lat_scale32, sc32.size() * sizeof(float)));
+    SG_CUDA(ctx, cudaMemcpy(ctx->d_lat_scale32, sc32.data(), sc32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return SGFEM_OK;
+}
+
+int sg_lattice_configure(sgfem_context* ctx) {
+    SG_TRY(set_smem(ctx, k_lat_pass_x<double>, lat_smem(ctx, 8)));
+    SG_TRY(set_smem(ctx, k_lat_pass_y<double>, lat_smem(ctx, 8)));
+    SG_TRY(set_smem(ctx, k_lat_pass_x<float>, lat_smem(ctx, 4)));
+    SG_TRY(set_smem(ctx, k_lat_pass_y<float>, lat_smem(ctx, 4)));
+    return SGFEM_OK;
+}
+
+int sg_lat_pass_x(sgfem_context* ctx, int precision, const void* R, void* T, const KrylovScalars* scal) {
+    LatGeom g = geom(ctx);
+    const int grid = (g.Nl - 1) * g.nchunk;
+    if (precision == SGFEM_FP64) {
+        size_t smem = lat_smem(ctx, 8);
+        k_lat_pass_x<double><<<grid, LAT_THREADS, smem, ctx->stream>>>((const double*)R, (double*)T, ctx->d_lat_tab64, g, 0, scal);
+    } else {
+        size_t smem = lat_smem(ctx, 4);
+        k_lat_pass_x<float><<<grid, LAT_THREADS, smem, ctx->stream>>>((const float*)R, (float*)T, ctx->d_lat_tab32, g, 0, scal);
+    }
+    SG_CUDA(ctx, cudaGetLastError());
+    return SGFEM_OK;
+}
+
+int sg_lat_pass_y(sgfem_context* ctx, int precision, void* T, double* rz, int* nblocks, const KrylovScalars* scal) {
+    LatGeom g = geom(ctx);
+    const int grid = (g.Nl - 1) * g.nchunk;
+    if (nblocks) *nblocks = grid;
+    if (precision == SGFEM_FP64) {
+        size_t smem = lat_smem(ctx, 8);
+        k_lat_pass_y<double><<<grid, LAT_THREADS, smem, ctx->stream>>>((double*)T, ctx->d_lat_tab64, ctx->d_lat_scale64, g, rz, scal);
+    } else {
+        size_t smem = lat_smem(ctx, 4);
+        k_lat_pass_y<float><<<grid, LAT_THREADS, smem, ctx->stream>>>((float*)T, ctx->d_lat_tab32, ctx->d_lat_scale32, g, rz, scal);
+    }
+    SG_CUDA(ctx, cudaGetLastError());
+    return SGFEM_OK;
+}
+
+int sg_lat_pass_xinv(sgfem_context* ctx, int precision, const void* T, void* out, int mode, const KrylovScalars* scal) {
+    LatGeom g = geom(ctx);
+    const int grid = (g.Nl - 1) * g.nchunk;
+    if (precision == SGFEM_FP64) {
+        size_t smem = lat_smem(ctx, 8);
+        k_lat_pass_x<double><<<grid, LAT_THREADS, smem, ctx->stream>>>((const double*)T, (double*)out, ctx->d_lat_tab64, g, mode, scal);
+    } else {
+        size_t smem = lat_smem(ctx, 4);
+        k_lat_pass_x<float><<<grid, LAT_THREADS, smem, ctx->stream>>>((const float*)T, (float*)out, ctx->d_lat_tab32, g, mode, scal);
+    }
+    SG_CUDA(ctx, cudaGetLastError());
+    return SGFEM_OK;
+}
+
+int sg_jacobi(sgfem_context* ctx, int precision, const void* R, void* out, int mode, int identity, double* rz,
+              int* nblocks, const KrylovScalars* scal) {
+    const int threads = 256;
+    int grid = (int)std::min<int64_t>(((int64_t)ctx->n * ctx->ld + threads - 1) / threads, (int64_t)ctx->num_sms * 8);
+    if (grid < 1) grid = 1;
+    if (nblocks) *nblocks = grid;
+    if (precision == SGFEM_FP64)
+        k_jacobi<double><<<grid, threads, 0, ctx->stream>>>((const double*)R, (double*)out, ctx->d_dinv64, (int)ctx->n,
+                                                            (int)ctx->ld, identity, mode, rz, scal);
+    else
+        k_jacobi<float><<<grid, threads, 0, ctx->stream>>>((const float*)R, (float*)out, ctx->d_dinv32, (int)ctx->n,
+                                                           (int)ctx->ld, identity, mode, rz, scal);
+    SG_CUDA(ctx, cudaGetLastError());
+    return SGFEM_OK;
+}

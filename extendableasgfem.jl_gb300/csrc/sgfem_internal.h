@@ -1,0 +1,164 @@
+// Internal declarations of the sm_103a stochastic-Galerkin library (libsgfem).
+//
+// Device data layout (all in HBM, owned by the context):
+//   * SG vectors: n rows (device dof order) x ld columns, row-major, ld = P
+//     rounded up to a multiple of 4; padding columns are kept at zero.  One
+//     CSR nonzero (i, j) thus gathers the contiguous mode vector of dof j.
+//   * spatial operators: one CSR pattern (union of the K_m patterns, int32
+//     rowptr / colidx) with the M+1 values of a nonzero stored contiguously,
+//     vals[nz * M1 + m], in FP64 and in FP32.
+//   * coupling: the pair list Q = {(0, nu)} u {(m, nu) : G_m column nu != 0}
+//     and, per output mode mu, the list of (g, q) with g = G_m[mu, nu].
+// The device dof order is the lattice order (row by row) when the dof
+// coordinates form a uniform lattice of the unit square, else the caller's.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/sgfem.h"
+
+struct HostCSC {
+    int64_t n = 0;
+    std::vector<int64_t> colptr;  // 0-based
+    std::vector<int64_t> rowval;  // 0-based
+    std::vector<double> nzval;
+    bool set = false;
+};
+
+// scalars of a Krylov solve kept on the device (no host round trip per iteration)
+struct KrylovScalars {
+    double rho;      // r'z of the current iterate
+    double pq;       // p'Ap
+    double alpha;
+    double beta;
+    double rr;       // ||r||^2
+    double tol2;     // stop when rr <= tol2
+    int done;        // 1 once converged or failed; kernels return early
+    int status;      // SGFEM_OK / SGFEM_ERR_BREAKDOWN / SGFEM_ERR_NONFINITE
+    int iters;       // iterations completed
+    int first;       // 1 before the first preconditioner application (beta = 0)
+};
+
+struct DeviceBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+enum { SG_NBUF = 12 };
+
+struct sgfem_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int num_sms = 0;
+
+    // ---- host-side setup state ----
+    int64_t n = -1;          // spatial dofs
+    int64_t P = -1;          // modes
+    int64_t M = -1;          // number of K_m beyond K_0
+    std::vector<HostCSC> mats;
+    std::vector<int64_t> G_colptr, G_rowval;
+    std::vector<double> G_val;
+    bool has_G = false;
+    std::vector<int64_t> bdofs;  // 0-based caller numbering
+    bool has_bdofs = false;
+    std::vector<double> dof_xy;  // 2 x n column-major
+    bool finalized = false;
+
+    // ---- device-side structures ----
+    int64_t ld = 0;            // row stride of device SG vectors
+    int64_t nnz = 0;
+    int M1 = 0;                // M + 1
+    std::vector<int32_t> perm;   // device row -> caller dof
+    std::vector<int32_t> iperm;  // caller dof -> device row
+    int* d_rowptr = nullptr;
+    int* d_col = nullptr;
+    double* d_val64 = nullptr;
+    float* d_val32 = nullptr;
+    unsigned char* d_bmask = nullptr;
+    int* d_iperm = nullptr;    // caller dof -> device row
+    std::vector<unsigned char> bmask_host;
+    double* d_dinv64 = nullptr;  // 1/diag(K_0), 0 on boundary rows (Jacobi)
+    float* d_dinv32 = nullptr;
+
+    // coupling schedule
+    int Qn = 0;
+    int* d_qtab = nullptr;         // packed (m << 16) | nu, length Qn
+    int* d_combptr = nullptr;      // P + 1
+    int* d_combq = nullptr;
+    double* d_combg64 = nullptr;
+    float* d_combg32 = nullptr;
+    int ncomb = 0;
+
+    // lattice preconditioner
+    bool lattice = false;
+    int Nl = 0;                 // lattice intervals per side; points (Nl+1)^2
+    int lat_log2 = 0;           // Nl = 2^lat_log2
+    double lat_scale = 1.0;     // a0: K_0 ~ a0 * L on interior rows
+    double* d_lat_tab64 = nullptr;  // see lattice.cu
+    float* d_lat_tab32 = nullptr;
+    double* d_lat_scale64 = nullptr;  // per (kx, ky) scale, (Nl-1)^2
+    float* d_lat_scale32 = nullptr;
+
+    // workspaces (lazily sized)
+    DeviceBuf w_stage;         // host-layout staging (n*P doubles)
+    DeviceBuf w_vec[SG_NBUF];  // SG vectors
+    DeviceBuf w_partials;      // per-block reduction partials (double)
+    KrylovScalars* d_scal = nullptr;
+    KrylovScalars* h_scal = nullptr;  // pinned
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+// ------------------------------------------------------------------ errors / memory
+int sg_fail(sgfem_context* ctx, int code, const std::string& msg);
+int sg_cuda_fail(sgfem_context* ctx, cudaError_t e, const char* what);
+
+#define SG_CUDA(ctx, call)                                              \
+    do {                                                                \
+        cudaError_t _e = (call);                                        \
+        if (_e != cudaSuccess) return sg_cuda_fail((ctx), _e, #call);   \
+    } while (0)
+
+#define SG_TRY(call)                   \
+    do {                               \
+        int _s = (call);               \
+        if (_s != SGFEM_OK) return _s; \
+    } while (0)
+
+int sg_ensure(sgfem_context* ctx, DeviceBuf& b, size_t bytes);
+size_t sg_elem_bytes(int precision);
+size_t sg_vec_bytes(const sgfem_context* ctx, int precision);
+int sg_check_ready(sgfem_context* ctx);
+
+// ------------------------------------------------------------------ apply (apply.cu)
+// Y = S X in device layout.  If dot_partials != nullptr each block writes the FP64
+// partial sum of X .* Y to dot_partials[block]; *nblocks receives the block count.
+int sg_launch_apply(sgfem_context* ctx, int precision, const void* X, void* Y,
+                    double* dot_partials, int* nblocks, const KrylovScalars* skip_if_done);
+
+// ------------------------------------------------------------------ layout (context.cu)
+int sg_launch_to_device(sgfem_context* ctx, const double* stage, void* X, int precision);
+int sg_launch_from_device(sgfem_context* ctx, const void* X, double* stage, int precision);
+
+// ------------------------------------------------------------------ preconditioners (lattice.cu)
+int sg_lattice_setup(sgfem_context* ctx);
+// pass 1: T = DST_x(R) on interior rows
+int sg_lat_pass_x(sgfem_context* ctx, int precision, const void* R, void* T,
+                  const KrylovScalars* skip_if_done);
+// pass 2: T <- DST_y(scale .* DST_y(T)); rz partials (Parseval) if rz != nullptr
+int sg_lat_pass_y(sgfem_context* ctx, int precision, void* T, double* rz, int* nblocks,
+                  const KrylovScalars* skip_if_done);
+// pass 3: z = DST_x(T); mode 0: out = z (boundary rows untouched), mode 1: out = z + beta*out
+int sg_lat_pass_xinv(sgfem_context* ctx, int precision, const void* T, void* out, int mode,
+                     const KrylovScalars* scal);
+// Jacobi (identity=1: plain identity on interior rows): mode 0: out = D^-1 R ;
+// mode 1: out = D^-1 R + beta*out on interior rows ; mode 2: r'z partials only
+int sg_jacobi(sgfem_context* ctx, int precision, const void* R, void* out, int mode, int identity,
+              double* rz, int* nblocks, const KrylovScalars* scal);
+// set the dynamic shared-memory limits once (before any graph capture)
+int sg_lattice_configure(sgfem_context* ctx);
+int sg_apply_configure(sgfem_context* ctx);

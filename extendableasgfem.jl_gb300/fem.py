@@ -1,0 +1,207 @@
+"""Spatial finite-element layer on the host (the part ExtendableGrids /
+ExtendableFEMBase / ExtendableFEM provide to the reference).
+
+* ``unit_square_mesh(N)``: N x N squares of the unit square, each split along
+  the (i,j)-(i+1,j+1) diagonal (ExtendableGrids.simplexgrid-style); faces are
+  numbered in order of first appearance over cells, local faces (0,1),(1,2),(2,0).
+* ``H1Pk``: continuous P1 / P2 Lagrange space; dofs are the nodes, then (P2)
+  one dof per face; boundary dofs are all dofs on boundary faces
+  (FES[BFaceDofs], src/modelproblems/solvers_poisson_primal.jl:136-142).
+* ``triangle_rule(order)``: reference-triangle quadrature with weights summing
+  to one (the ExtendableFEMBase convention used in src/estimate.jl:345-346).
+* ``assemble_stiffness``: K_m = (a_m grad u, grad v) for m = 0..M on one
+  shared CSR pattern (src/modelproblems/poisson_primal.jl:56-63), vectorised
+  over cells; ``assemble_rhs``: b = (f, v) (poisson_primal.jl:66-68).
+"""
+import math
+
+import numpy as np
+import scipy.sparse as sp
+from scipy.special import roots_jacobi
+
+
+def triangle_rule(order):
+    if order <= 1:
+        return np.array([[1.0 / 3.0, 1.0 / 3.0]]), np.array([1.0])
+    if order == 2:
+        return (np.array([[1.0 / 6.0, 1.0 / 6.0], [2.0 / 3.0, 1.0 / 6.0], [1.0 / 6.0, 2.0 / 3.0]]),
+                np.full(3, 1.0 / 3.0))
+    n = int(math.ceil((order + 1) / 2.0))
+    xj, wj = roots_jacobi(n, 1.0, 0.0)  # collapsed direction, weight (1 - xi)
+    xl, wl = np.polynomial.legendre.leggauss(n)
+    xi = (xj + 1.0) / 2.0
+    t = (xl + 1.0) / 2.0
+    pts = np.array([[xi[a], (1.0 - xi[a]) * t[b]] for a in range(n) for b in range(n)])
+    w = np.array([wj[a] * wl[b] for a in range(n) for b in range(n)])
+    return pts, w / w.sum()
+
+
+def line_rule(npts):
+    x, w = np.polynomial.legendre.leggauss(npts)
+    return (x + 1.0) / 2.0, w / w.sum()
+
+
+class Mesh:
+    def __init__(self, coords, cells):
+        self.coords = np.asarray(coords, dtype=np.float64)
+        self.cells = np.asarray(cells, dtype=np.int64)
+        self.nnodes = len(self.coords)
+        self.ncells = len(self.cells)
+        loc = np.array([[0, 1], [1, 2], [2, 0]])
+        e = self.cells[:, loc]                       # ncells x 3 x 2
+        key = np.sort(e, axis=2).reshape(-1, 2)
+        code = key[:, 0] * self.nnodes + key[:, 1]
+        uniq, first, inv = np.unique(code, return_index=True, return_inverse=True)
+        order = np.argsort(first, kind="stable")      # number faces by first appearance
+        rank = np.empty_like(order)
+        rank[order] = np.arange(len(order))
+        self.cellfaces = rank[inv].reshape(self.ncells, 3)
+        self.nfaces = len(uniq)
+        self.face_nodes = key[first[order]]
+        fc = np.full((self.nfaces, 2), -1, dtype=np.int64)
+        flat_faces = self.cellfaces.ravel()
+        flat_cells = np.repeat(np.arange(self.ncells), 3)
+        o = np.argsort(flat_faces, kind="stable")  # cells stay in traversal order per face
+        ff = flat_faces[o]
+        fcell = flat_cells[o]
+        starts = np.searchsorted(ff, np.arange(self.nfaces))
+        counts = np.bincount(ff, minlength=self.nfaces)
+        fc[:, 0] = fcell[starts]
+        two = counts == 2
+        fc[two, 1] = fcell[starts[two] + 1]
+        self.face_cells = fc
+        self.bfaces = np.nonzero(fc[:, 1] < 0)[0]
+        p = self.coords
+        t = self.cells
+        self.cell_volumes = 0.5 * np.abs((p[t[:, 1], 0] - p[t[:, 0], 0]) * (p[t[:, 2], 1] - p[t[:, 0], 1])
+                                         - (p[t[:, 2], 0] - p[t[:, 0], 0]) * (p[t[:, 1], 1] - p[t[:, 0], 1]))
+        fn = self.face_nodes
+        self.face_volumes = np.hypot(p[fn[:, 1], 0] - p[fn[:, 0], 0], p[fn[:, 1], 1] - p[fn[:, 0], 1])
+        # affine maps: x = p0 + J (xi, eta); grad lambda_i per cell
+        J = np.stack([p[t[:, 1]] - p[t[:, 0]], p[t[:, 2]] - p[t[:, 0]]], axis=2)  # nc x 2 x 2 (columns)
+        self.J = J
+        Jinv = np.linalg.inv(J)
+        gl = np.zeros((self.ncells, 3, 2))
+        gl[:, 1] = Jinv[:, 0, :]
+        gl[:, 2] = Jinv[:, 1, :]
+        gl[:, 0] = -gl[:, 1] - gl[:, 2]
+        self.grad_lambda = gl
+
+
+def unit_square_mesh(N):
+    idx = lambda i, j: j * (N + 1) + i
+    xs = np.arange(N + 1) / N
+    X, Y = np.meshgrid(xs, xs)
+    coords = np.stack([X.ravel(), Y.ravel()], axis=1)
+    i, j = np.meshgrid(np.arange(N), np.arange(N))
+    i = i.ravel()
+    j = j.ravel()
+    t1 = np.stack([idx(i, j), idx(i + 1, j), idx(i + 1, j + 1)], axis=1)
+    t2 = np.stack([idx(i, j), idx(i + 1, j + 1), idx(i, j + 1)], axis=1)
+    cells = np.stack([t1, t2], axis=1).reshape(-1, 3)
+    return Mesh(coords, cells)
+
+
+class H1Pk:
+    def __init__(self, mesh, order):
+        if order not in (1, 2):
+            raise ValueError("H1Pk: order 1 or 2")
+        self.mesh = mesh
+        self.order = order
+        if order == 1:
+            self.celldofs = mesh.cells.copy()
+            self.ndofs = mesh.nnodes
+            self.dof_coords = mesh.coords.copy()
+        else:
+            self.celldofs = np.concatenate([mesh.cells, mesh.nnodes + mesh.cellfaces], axis=1)
+            self.ndofs = mesh.nnodes + mesh.nfaces
+            fn = mesh.face_nodes
+            self.dof_coords = np.concatenate([mesh.coords, 0.5 * (mesh.coords[fn[:, 0]] + mesh.coords[fn[:, 1]])])
+        bf = mesh.bfaces
+        bd = [mesh.face_nodes[bf, 0], mesh.face_nodes[bf, 1]]
+        if order == 2:
+            bd.append(mesh.nnodes + bf)
+        self.bdofs = np.unique(np.concatenate(bd))
+
+    @property
+    def ndofs4cell(self):
+        return 3 if self.order == 1 else 6
+
+    def basis(self, lam):
+        """values (nd,), gradient factors and laplacians at barycentric lam for all cells:
+        returns vals (nd,), grads (nc, nd, 2), laps (nc, nd)."""
+        gl = self.mesh.grad_lambda
+        if self.order == 1:
+            return lam.copy(), gl.copy(), np.zeros(gl.shape[:2])
+        nc = gl.shape[0]
+        v = np.zeros(6)
+        g = np.zeros((nc, 6, 2))
+        lap = np.zeros((nc, 6))
+        for i in range(3):
+            v[i] = lam[i] * (2 * lam[i] - 1)
+            g[:, i] = (4 * lam[i] - 1) * gl[:, i]
+            lap[:, i] = 4 * np.sum(gl[:, i] ** 2, axis=1)
+        for e, (a, b) in enumerate(((0, 1), (1, 2), (2, 0))):
+            v[3 + e] = 4 * lam[a] * lam[b]
+            g[:, 3 + e] = 4 * (lam[a] * gl[:, b] + lam[b] * gl[:, a])
+            lap[:, 3 + e] = 8 * np.sum(gl[:, a] * gl[:, b], axis=1)
+        return v, g, lap
+
+    def physical_points(self, pts):
+        """(nc, nq, 2) physical coordinates of reference points."""
+        p0 = self.mesh.coords[self.mesh.cells[:, 0]]
+        return p0[:, None, :] + np.einsum("cij,qj->cqi", self.mesh.J, pts)
+
+    def pattern(self):
+        """CSR pattern of the cell connectivity and the scatter map cell-entry -> nnz."""
+        nd = self.ndofs4cell
+        cd = self.celldofs
+        rows = np.repeat(cd, nd, axis=1).ravel()
+        cols = np.tile(cd, (1, nd)).ravel()
+        n = self.ndofs
+        code = rows * n + cols
+        uniq, inv = np.unique(code, return_inverse=True)
+        r = uniq // n
+        c = uniq % n
+        indptr = np.zeros(n + 1, dtype=np.int64)
+        np.add.at(indptr, r + 1, 1)
+        indptr = np.cumsum(indptr)
+        return indptr, c, inv
+
+
+def assemble_stiffness(space, coef, ms, quadorder):
+    """[K_m for m in ms] as CSR matrices sharing one pattern."""
+    pts, wts = triangle_rule(quadorder)
+    X = space.physical_points(pts)  # nc x nq x 2
+    vol = space.mesh.cell_volumes
+    nd = space.ndofs4cell
+    nc = space.mesh.ncells
+    GG = []
+    for q in range(len(wts)):
+        lam = np.array([1 - pts[q, 0] - pts[q, 1], pts[q, 0], pts[q, 1]])
+        _, g, _ = space.basis(lam)
+        GG.append(np.einsum("cik,cjk->cij", g, g))
+    indptr, col, inv = space.pattern()
+    n = space.ndofs
+    out = []
+    for m in ms:
+        a = coef.get_am(X[..., 0], X[..., 1], m)  # nc x nq
+        loc = np.zeros((nc, nd, nd))
+        for q in range(len(wts)):
+            loc += (wts[q] * vol * a[:, q])[:, None, None] * GG[q]
+        data = np.bincount(inv, weights=loc.ravel(), minlength=len(col))
+        out.append(sp.csr_matrix((data, col, indptr), shape=(n, n)))
+    return out
+
+
+def assemble_rhs(space, f, quadorder):
+    pts, wts = triangle_rule(quadorder)
+    X = space.physical_points(pts)
+    vol = space.mesh.cell_volumes
+    b = np.zeros(space.ndofs)
+    fx = np.broadcast_to(np.asarray(f(X[..., 0], X[..., 1]), dtype=np.float64), X.shape[:2])
+    for q in range(len(wts)):
+        lam = np.array([1 - pts[q, 0] - pts[q, 1], pts[q, 0], pts[q, 1]])
+        v, _, _ = space.basis(lam)
+        np.add.at(b, space.celldofs, (wts[q] * vol * fx[:, q])[:, None] * v[None, :])
+    return b

@@ -1,0 +1,107 @@
+"""Model problems and the GPU stochastic-Galerkin solve (host side).
+
+Mirrors src/modelproblems/ of ExtendableASGFEM.jl:
+  AbstractModelProblem / solve        modelproblems.jl:1-31
+  PoissonProblemPrimal / solve        poisson_primal.jl:38-81: assemble K_0..K_M
+                                      (M = maxlength_multiindices(TB)) and b = (f, v),
+                                      then solve_primal!
+  SGOperator                          solvers_poisson_primal.jl:14-124 (MySystemPrimal
+                                      + MyPreconditionerPrimal), backed by one libsgfem
+                                      context on the GPU: mul / ldiv / solve_primal
+All arithmetic of mul!, ldiv! and the Krylov solve runs in the CUDA library;
+this module only assembles the spatial blocks (the caller's side of the
+boundary, ExtendableFEM in the reference) and moves arrays across the C ABI.
+"""
+import numpy as np
+
+from . import _lib
+from .fem import assemble_rhs, assemble_stiffness
+
+
+class AbstractModelProblem:
+    pass
+
+
+class PoissonProblemPrimal(AbstractModelProblem):
+    """-div(a(y, x) grad u) = f with the affine coefficient a = a_0 + sum_m y_m a_m."""
+
+
+class SGOperator:
+    """The SG operator S and the mean-based preconditioner on one GPU."""
+
+    def __init__(self, FES, TB, Ks, device=0):
+        self.FES = FES
+        self.TB = TB
+        self.n = FES.ndofs
+        self.P = TB.nmodes
+        self.M = len(Ks) - 1
+        if TB.G.shape != (self.M * self.P, self.P):
+            raise ValueError("G must be (M*P) x P with M = len(Ks) - 1")
+        self.ctx = _lib.Context(device)
+        for m, K in enumerate(Ks):
+            self.ctx.set_spatial_matrix(m, K)
+        self.ctx.set_coupling(TB.G, self.P, self.M)
+        self.bdofs = np.asarray(FES.bdofs, dtype=np.int64)
+        self.ctx.set_boundary_dofs(self.bdofs)
+        self.ctx.set_dof_coordinates(FES.dof_coords)
+        self.ctx.finalize()
+
+    @property
+    def has_lattice(self):
+        return self.ctx.has_lattice
+
+    def mul(self, x, precision=_lib.FP64):
+        """mul!(Ax, S, x) on SGFEVector.entries."""
+        return self.ctx.apply(x, precision)
+
+    def ldiv(self, b, kind=None, precision=_lib.FP64):
+        """ldiv!(y, P, b): mean-based preconditioner on every mode."""
+        if kind is None:
+            kind = _lib.PREC_LATTICE if self.has_lattice else _lib.PREC_JACOBI
+        return self.ctx.precondition(b, kind, precision)
+
+    def solve_primal(self, b0, x, rtol=1e-12, precision=_lib.MIXED, preconditioner=None, maxit=5000,
+                     inner_rtol=1e-5, reference_rhs=True, check_every=8, allow_maxit=False):
+        """solve_primal!: x (SGFEVector.entries) is the warm start and receives the solution."""
+        if preconditioner is None:
+            preconditioner = _lib.PREC_LATTICE if self.has_lattice else _lib.PREC_JACOBI
+        o = self.ctx.default_options(precision=precision, preconditioner=preconditioner, rtol=rtol, maxit=maxit,
+                                     inner_rtol=inner_rtol, reference_rhs=1 if reference_rhs else 0,
+                                     check_every=check_every)
+        return self.ctx.solve(b0, x, o, allow_maxit=allow_maxit).as_dict()
+
+    def close(self):
+        self.ctx.close()
+
+
+def assemble(problem, sol, C, rhs, bonus_quadorder_a=2, bonus_quadorder_f=0):
+    """Spatial blocks of poisson_primal.jl:55-68: [K_0..K_M], b."""
+    if problem is not PoissonProblemPrimal:
+        raise NotImplementedError(f"no assembly for {problem}")
+    if rhs is None:
+        raise ValueError("need right-hand side")
+    FES = sol.FES_space[0]
+    p = FES.order
+    M = sol.TB.maxlength_multiindices()
+    Ks = assemble_stiffness(FES, C, list(range(M + 1)), 2 * (p - 1) + bonus_quadorder_a)
+    b0 = assemble_rhs(FES, rhs, p + bonus_quadorder_f)
+    return Ks, b0
+
+
+def solve(problem, sol, C, rhs=None, bonus_quadorder_a=2, bonus_quadorder_f=0, use_iterative_solver=True,
+          device=0, **solver_kwargs):
+    """solve!(problem, sol, C; rhs, ...): solves on the GPU, writes sol.entries,
+    returns the (0-based) boundary dofs like the reference returns bdofs.
+    ``solver_kwargs`` go to SGOperator.solve_primal (rtol, precision, ...)."""
+    if not issubclass(problem, AbstractModelProblem) or problem is AbstractModelProblem:
+        raise NotImplementedError("This model problem seems to have no solver implemented!")
+    if not use_iterative_solver:
+        raise NotImplementedError("the GPU path has no assembled Kronecker solver; use_iterative_solver=True")
+    Ks, b0 = assemble(problem, sol, C, rhs, bonus_quadorder_a, bonus_quadorder_f)
+    op = SGOperator(sol.FES_space[0], sol.TB, Ks, device=device)
+    try:
+        stats = op.solve_primal(b0, sol.entries, **solver_kwargs)
+    finally:
+        op.close()
+    sol.solve_stats = stats
+    return op.bdofs

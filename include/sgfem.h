@@ -1,0 +1,146 @@
+/*
+ * sgfem.h - C ABI of the GB300 (sm_103a) stochastic-Galerkin hot path.
+ *
+ * Drop-in boundary for the Julia package ExtendableASGFEM.jl: every entry
+ * point replaces one reference routine (cited as path:line inside that
+ * project) and takes the reference's own data as plain pointers:
+ *   - sparse matrices as Julia SparseMatrixCSC{Float64,Int64} arrays
+ *     (1-based colptr / rowval, nzval), i.e. ExtendableSparseMatrix.cscmatrix;
+ *   - SG vectors as SGFEVector.entries: Float64[n*P], column-major n x P
+ *     (mode mu occupies entries[mu*n : (mu+1)*n], src/sgfevector.jl:94-103);
+ *   - index lists 1-based Int64.
+ * Host pointers are borrowed for the duration of a call only; the library
+ * copies what it needs into device memory owned by the context and never
+ * writes to caller data except the documented outputs.
+ *
+ * Every function returns an int status (SGFEM_OK = 0); on failure
+ * sgfem_last_error() returns a message.  One context per host thread; all
+ * calls on a context are synchronous with respect to the host.
+ */
+#ifndef SGFEM_H
+#define SGFEM_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SGFEM_API __attribute__((visibility("default")))
+#else
+#define SGFEM_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SGFEM_OK 0
+#define SGFEM_ERR_ARGUMENT 1    /* bad size, null pointer, index out of range */
+#define SGFEM_ERR_STATE 2       /* call order violated (e.g. apply before finalize) */
+#define SGFEM_ERR_CUDA 3        /* CUDA runtime error (message has the detail) */
+#define SGFEM_ERR_NONFINITE 4   /* NaN/Inf met in an input or an iterate */
+#define SGFEM_ERR_BREAKDOWN 5   /* Krylov breakdown (p'Ap <= 0 or r'z <= 0) */
+#define SGFEM_ERR_MAXIT 6       /* tolerance not reached within maxit */
+#define SGFEM_ERR_UNSUPPORTED 7 /* configuration not handled by this build */
+
+#define SGFEM_FP64 0            /* all arithmetic in FP64 */
+#define SGFEM_FP32 1            /* FP32 operator values, vectors and accumulation */
+#define SGFEM_MIXED 2           /* FP32 inner PCG inside FP64 iterative refinement */
+
+#define SGFEM_PREC_NONE 0
+#define SGFEM_PREC_LATTICE 1    /* mean-based I (x) (a0 L)^-1, L = 5-point lattice Laplacian */
+#define SGFEM_PREC_JACOBI 2     /* I (x) diag(K_0)^-1 */
+
+typedef struct sgfem_context sgfem_context;
+
+typedef struct {
+    int precision;      /* SGFEM_FP64 or SGFEM_MIXED (SGFEM_FP32: FP32 PCG, no refinement) */
+    int preconditioner; /* SGFEM_PREC_* ; LATTICE needs sgfem_set_dof_coordinates */
+    double rtol;        /* stop when ||b - A x||_2 <= rtol ||b||_2 (FP64 true residual) */
+    int maxit;          /* total PCG iterations (inner ones for MIXED) */
+    double inner_rtol;  /* MIXED: relative reduction asked of each FP32 inner solve */
+    int reference_rhs;  /* 1: b = x0 + e_1 (x) b0 as solvers_poisson_primal.jl:149-150 does;
+                           0: b = e_1 (x) b0.  Boundary rows of b are zeroed either way. */
+    int check_every;    /* iterations between host-side convergence checks (>= 1) */
+} sgfem_solve_options;
+
+typedef struct {
+    int iterations;        /* PCG iterations (inner ones for MIXED) */
+    int outer_iterations;  /* MIXED: refinement steps; FP64: 1 */
+    int fp64_applies;      /* FP64 operator applications made */
+    double relres;         /* final ||b - A x|| / ||b|| in FP64 */
+    double time_ms;        /* device time of the solve (CUDA events) */
+    double apply_ms;       /* device time spent in operator applications */
+    double precond_ms;     /* device time spent in the preconditioner */
+} sgfem_solve_stats;
+
+/* context */
+SGFEM_API int sgfem_create(sgfem_context** ctx, int device);
+SGFEM_API int sgfem_destroy(sgfem_context* ctx);
+SGFEM_API const char* sgfem_last_error(const sgfem_context* ctx);
+SGFEM_API int sgfem_version(void);
+
+/*
+ * Operator setup.  Replaces the construction of MySystemPrimal and
+ * MyPreconditionerPrimal (src/modelproblems/solvers_poisson_primal.jl:14-44,
+ * :136-146): K_0..K_M from poisson_primal.jl:56-63, G from
+ * TensorizedBasis.G (src/tensorizedbasis.jl:193-218), boundary dofs from
+ * FES[BFaceDofs].
+ */
+SGFEM_API int sgfem_set_spatial_matrix(sgfem_context* ctx, int m, int64_t n, const int64_t* colptr,
+                             const int64_t* rowval, const double* nzval);
+SGFEM_API int sgfem_set_coupling(sgfem_context* ctx, int64_t P, int64_t M, const int64_t* colptr,
+                       const int64_t* rowval, const double* nzval);
+SGFEM_API int sgfem_set_boundary_dofs(sgfem_context* ctx, int64_t count, const int64_t* bdofs);
+/* dof coordinates, 2 x n column-major (Julia's xgrid[Coordinates] layout); when they
+   form a uniform lattice of the unit square the lattice preconditioner is enabled
+   and the device numbering follows the lattice. */
+SGFEM_API int sgfem_set_dof_coordinates(sgfem_context* ctx, int64_t n, const double* xy);
+SGFEM_API int sgfem_finalize(sgfem_context* ctx);
+/* 1 if the lattice preconditioner is available after finalize */
+SGFEM_API int sgfem_has_lattice(const sgfem_context* ctx);
+
+/*
+ * mul!(Ax, S::MySystemPrimal, x), solvers_poisson_primal.jl:86-124:
+ *   Y_mu = K_0 X_mu + sum_{m,nu} G[(m-1)P+mu, nu] K_m X_nu, boundary rows zeroed.
+ * x, y: host SGFEVector.entries (n*P doubles).  precision: SGFEM_FP64 / SGFEM_FP32.
+ */
+SGFEM_API int sgfem_apply(sgfem_context* ctx, const double* x, double* y, int precision);
+
+/*
+ * ldiv!(y, P::MyPreconditionerPrimal, b), solvers_poisson_primal.jl:47-78, with the
+ * mean-based operator selected by `kind` (SGFEM_PREC_*).  For P1 lattices
+ * SGFEM_PREC_LATTICE equals the reference's LU solve on interior rows.
+ */
+SGFEM_API int sgfem_precondition(sgfem_context* ctx, const double* b, double* y, int kind, int precision);
+
+/*
+ * solve_primal!(sol, A0, Am, b0, G, nmodes, 1), solvers_poisson_primal.jl:130-169:
+ * solves S x = b with b built from b0 (n doubles, the assembled (f, v)) and the
+ * warm start x_inout (SGFEVector.entries, in/out).  Uses PCG (the SG operator of
+ * PoissonProblemPrimal is SPD on interior dofs) instead of the reference's GMRES.
+ */
+SGFEM_API int sgfem_solve(sgfem_context* ctx, const double* b0, double* x_inout,
+                const sgfem_solve_options* opts, sgfem_solve_stats* stats);
+SGFEM_API void sgfem_default_options(sgfem_solve_options* opts);
+
+/*
+ * Device-resident variants for callers that keep SG vectors on the GPU.  Vectors
+ * are in the device layout: n_dev rows (device dof order) x ld columns, row-major,
+ * where sgfem_device_layout() reports n_dev, ld and the element size.
+ * Pointers are device pointers; calls are ordered on the context's stream and
+ * return after the work has completed.
+ */
+SGFEM_API int sgfem_device_layout(const sgfem_context* ctx, int64_t* n_dev, int64_t* ld);
+SGFEM_API int sgfem_apply_device(sgfem_context* ctx, const void* x_dev, void* y_dev, int precision);
+SGFEM_API int sgfem_to_device_layout(sgfem_context* ctx, const double* x_host, void* x_dev, int precision);
+SGFEM_API int sgfem_from_device_layout(sgfem_context* ctx, const void* x_dev, double* x_host, int precision);
+/* solve with b0 (n doubles, host) and a device-resident FP64 solution x_dev (in/out) */
+SGFEM_API int sgfem_solve_device(sgfem_context* ctx, const double* b0, void* x_dev,
+                       const sgfem_solve_options* opts, sgfem_solve_stats* stats);
+
+/* time (ms, CUDA events on the context stream) of `reps` back-to-back device applies */
+SGFEM_API int sgfem_time_apply(sgfem_context* ctx, int precision, int reps, double* ms_per_apply);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SGFEM_H */

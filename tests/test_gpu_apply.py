@@ -1,0 +1,147 @@
+"""GPU parity of the SG operator apply (K1) and the mean-based preconditioner
+(K2) against the oracle, through the C ABI.
+
+Tolerances: FP64 apply 1e-12 relative in the 2-norm (the bar for the plain
+FP64 operator); FP32 apply 1e-5 relative to the FP64 result; lattice
+preconditioner 1e-10 against the oracle's LU solve (P1, where the two
+operators are identical) or against a direct solve with the lattice
+Laplacian (P2)."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+from oracle import sg as osg
+from tests.problems import build, config1_like
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def problems():
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    return {
+        "config1": lambda: config1_like(),
+        "p2_top_weight": lambda: build(16, 2, 6, pkg.top_weight_multiindices(6, 30, C.decay_factors)),
+        "hermite_full": lambda: build(8, 1, 3, pkg.generate_multiindices(3, 2), basis="hermite", mean=2.0),
+        "p1_odd_mesh": lambda: build(12, 1, 4, pkg.total_degree_multiindices(4, 2)),
+        "single_mode": lambda: build(8, 1, 2, [[0, 0]]),
+    }
+
+
+@pytest.fixture(scope="module", params=list(problems().keys()))
+def case(request, built_pkg):
+    p = problems()[request.param]()
+    op = p.pkg.SGOperator(p.V, p.TB, p.Kall, device=0)
+    yield p, op
+    op.close()
+
+
+def test_apply_fp64_matches_oracle(case):
+    p, op = case
+    x = np.random.default_rng(0).standard_normal(p.n * p.P)
+    y = op.mul(x, p.pkg.FP64)
+    yref = osg.mul_literal(x, p.K0, p.Ks, p.G, p.bdofs, p.P)
+    assert rel(y, yref) <= 1e-12
+    n = p.n
+    for mu in range(p.P):
+        assert np.all(y[mu * n + p.bdofs] == 0.0)
+
+
+def test_apply_fp32_error(case):
+    p, op = case
+    x = np.random.default_rng(1).standard_normal(p.n * p.P)
+    y64 = op.mul(x, p.pkg.FP64)
+    y32 = op.mul(x, p.pkg.FP32)
+    assert rel(y32, y64) <= 1e-5
+
+
+def test_apply_deterministic(case):
+    p, op = case
+    x = np.random.default_rng(2).standard_normal(p.n * p.P)
+    assert np.array_equal(op.mul(x, p.pkg.FP64), op.mul(x, p.pkg.FP64))
+
+
+def test_apply_linearity(case):
+    p, op = case
+    rng = np.random.default_rng(3)
+    x, z = rng.standard_normal((2, p.n * p.P))
+    lhs = op.mul(2.0 * x - 0.5 * z)
+    rhs = 2.0 * op.mul(x) - 0.5 * op.mul(z)
+    assert rel(lhs, rhs) <= 1e-13
+
+
+def test_preconditioner(case):
+    p, op = case
+    pkg = p.pkg
+    rng = np.random.default_rng(4)
+    b = rng.standard_normal(p.n * p.P)
+    for mu in range(p.P):
+        b[mu * p.n + p.bdofs] = 0.0
+    inner = np.setdiff1d(np.arange(p.n), p.bdofs)
+    if p.V.order == 1:
+        ref = osg.MeanPreconditioner(p.K0, p.bdofs, p.P).ldiv(b)
+    else:
+        # lattice Laplacian on the P2 dofs (vertices + edge midpoints)
+        Nl = int(round(np.sqrt(p.n))) - 1
+        ij = np.rint(p.V.dof_coords * Nl).astype(int)
+        pos = {(a, c): k for k, (a, c) in enumerate(ij)}
+        rows, cols, vals = [], [], []
+        for k, (a, c) in enumerate(ij):
+            rows.append(k); cols.append(k); vals.append(4.0)
+            for da, dc in ((1, 0), (-1, 0), (0, 1), (0, -1)):
+                j = pos.get((a + da, c + dc))
+                if j is not None:
+                    rows.append(k); cols.append(j); vals.append(-1.0)
+        L = sp.csr_matrix((vals, (rows, cols)), shape=(p.n, p.n))
+        d = p.K0.diagonal()[inner]
+        a0 = d.sum() / (4 * len(inner))
+        lu = spla.splu((a0 * L[inner][:, inner]).tocsc())
+        ref = np.zeros_like(b)
+        for mu in range(p.P):
+            ref[mu * p.n + inner] = lu.solve(b[mu * p.n + inner])
+    if op.has_lattice:
+        y = op.ldiv(b, pkg.PREC_LATTICE, pkg.FP64)
+        mask = osg.interior_mask(p.n, p.P, p.bdofs)
+        assert rel(y[mask], ref[mask]) <= 1e-10
+        assert np.all(y[~mask] == 0.0)
+        y32 = op.ldiv(b, pkg.PREC_LATTICE, pkg.FP32)
+        assert rel(y32[mask], ref[mask]) <= 1e-4
+    yj = op.ldiv(b, pkg.PREC_JACOBI, pkg.FP64)
+    dj = np.zeros(p.n)
+    dj[inner] = 1.0 / p.K0.diagonal()[inner]
+    assert rel(yj, b * np.tile(dj, p.P)) <= 1e-14
+
+
+def test_lattice_detection(case):
+    p, op = case
+    Nl = int(round(np.sqrt(p.n))) - 1
+    expect = (Nl & (Nl - 1)) == 0
+    assert op.has_lattice == expect
+
+
+def test_apply_non_lattice_numbering(built_pkg):
+    """A shuffled dof numbering without coordinates takes the generic path."""
+    p = config1_like(N=8, M=3, deg=2)
+    rng = np.random.default_rng(7)
+    perm = rng.permutation(p.n)
+    inv = np.argsort(perm)
+    Kp = [K[perm][:, perm] for K in p.Kall]
+    ctx = p.pkg._lib.Context(0)
+    for m, K in enumerate(Kp):
+        ctx.set_spatial_matrix(m, K)
+    ctx.set_coupling(p.TB.G, p.P, p.M)
+    ctx.set_boundary_dofs(inv[p.bdofs])
+    ctx.finalize()
+    assert not ctx.has_lattice
+    x = rng.standard_normal(p.n * p.P)
+    X = x.reshape(p.P, p.n)
+    y = ctx.apply(X[:, perm].ravel())
+    yref = osg.mul_literal(x, p.K0, p.Ks, p.G, p.bdofs, p.P).reshape(p.P, p.n)[:, perm].ravel()
+    assert rel(y, yref) <= 1e-12
+    ctx.close()

@@ -1,0 +1,131 @@
+"""GPU parity of the device-resident PCG (FP64 and mixed precision) against
+the oracle's restatement of the reference solve (left-preconditioned GMRES
+with the LU mean preconditioner, atol = rtol = 1e-14).
+
+Bar: the solution matches the oracle to within the CG tolerance: relative
+2-norm error <= 100 * rtol (the preconditioned operator has condition number
+<= ~40 here), and the reported FP64 true residual is <= rtol."""
+import numpy as np
+import pytest
+
+from oracle import sg as osg
+from tests.problems import build, config1_like
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def oracle_solution(p, x0=None):
+    n, P = p.n, p.P
+    x0 = np.zeros(n * P) if x0 is None else x0
+    prec = osg.MeanPreconditioner(p.K0, p.bdofs, P)
+    b = osg.reference_rhs(x0, p.b0, p.bdofs, P)
+    xg, st = osg.gmres_left(lambda v: osg.apply_fast(v, p.K0, p.Ks, p.G, p.bdofs, P), prec.ldiv, b, x0.copy())
+    return xg
+
+
+@pytest.fixture(scope="module")
+def c1(built_pkg):
+    p = config1_like()
+    op = p.pkg.SGOperator(p.V, p.TB, p.Kall, device=0)
+    ref = oracle_solution(p)
+    yield p, op, ref
+    op.close()
+
+
+@pytest.mark.parametrize("precision", ["FP64", "MIXED"])
+@pytest.mark.parametrize("rtol", [1e-8, 1e-10])
+def test_solve_matches_oracle(c1, precision, rtol):
+    p, op, ref = c1
+    x = np.zeros(p.n * p.P)
+    st = op.solve_primal(p.b0, x, rtol=rtol, precision=getattr(p.pkg, precision))
+    assert st["relres"] <= rtol
+    assert rel(x, ref) <= 100 * rtol
+    mask = osg.interior_mask(p.n, p.P, p.bdofs)
+    assert np.all(x[~mask] == 0.0)
+
+
+def test_mixed_uses_few_fp64_applies(c1):
+    p, op, ref = c1
+    x = np.zeros(p.n * p.P)
+    st = op.solve_primal(p.b0, x, rtol=1e-10, precision=p.pkg.MIXED)
+    assert st["outer_iterations"] <= 4 and st["fp64_applies"] <= 5
+
+
+def test_iteration_count_matches_exact_preconditioner(c1):
+    """For P1 the lattice preconditioner is the reference's LU(K_0): FP64 PCG
+    needs the same number of iterations as the oracle's PCG with LU."""
+    p, op, ref = c1
+    n, P = p.n, p.P
+    prec = osg.MeanPreconditioner(p.K0, p.bdofs, P)
+    b = osg.reference_rhs(np.zeros(n * P), p.b0, p.bdofs, P)
+    _, st_o = osg.pcg(lambda v: osg.apply_fast(v, p.K0, p.Ks, p.G, p.bdofs, P), prec.ldiv, b, np.zeros(n * P),
+                      osg.interior_mask(n, P, p.bdofs), tol=1e-10)
+    x = np.zeros(n * P)
+    st = op.solve_primal(p.b0, x, rtol=1e-10, precision=p.pkg.FP64, check_every=1)
+    assert abs(st["iterations"] - st_o["niter"]) <= 1
+
+
+def test_warm_start_reference_rhs(c1):
+    """solve_primal! builds b = x0 + e_1 (x) b0 (solvers_poisson_primal.jl:149-150)."""
+    p, op, _ = c1
+    rng = np.random.default_rng(11)
+    x0 = 0.1 * rng.standard_normal(p.n * p.P)
+    for mu in range(p.P):
+        x0[mu * p.n + p.bdofs] = 0.0
+    ref = oracle_solution(p, x0)
+    x = x0.copy()
+    st = op.solve_primal(p.b0, x, rtol=1e-11, precision=p.pkg.FP64, reference_rhs=True)
+    assert rel(x, ref) <= 1e-9
+    x = x0.copy()
+    op.solve_primal(p.b0, x, rtol=1e-11, precision=p.pkg.FP64, reference_rhs=False)
+    assert rel(x, oracle_solution(p)) <= 1e-9
+
+
+def test_jacobi_and_none_paths(c1):
+    p, op, ref = c1
+    for kind in (p.pkg.PREC_JACOBI, p.pkg.PREC_NONE):
+        x = np.zeros(p.n * p.P)
+        st = op.solve_primal(p.b0, x, rtol=1e-9, precision=p.pkg.MIXED, preconditioner=kind)
+        assert rel(x, ref) <= 1e-7
+
+
+def test_maxit_reports_status(c1):
+    p, op, _ = c1
+    x = np.zeros(p.n * p.P)
+    with pytest.raises(p.pkg.SGError) as e:
+        op.solve_primal(p.b0, x, rtol=1e-12, precision=p.pkg.FP64, maxit=2)
+    assert e.value.code == 6
+    st = op.solve_primal(p.b0, x, rtol=1e-12, precision=p.pkg.FP64, maxit=2, allow_maxit=True)
+    assert st["iterations"] <= 2 + 8
+
+
+@pytest.mark.parametrize("order,N,M,P", [(2, 8, 4, 12), (2, 16, 6, 30)])
+def test_solve_p2_mixed(built_pkg, order, N, M, P):
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    p = build(N, order, M, pkg.top_weight_multiindices(M, P, C.decay_factors))
+    ref = oracle_solution(p)
+    op = pkg.SGOperator(p.V, p.TB, p.Kall, device=0)
+    assert op.has_lattice
+    for prec in (pkg.FP64, pkg.MIXED):
+        x = np.zeros(p.n * p.P)
+        st = op.solve_primal(p.b0, x, rtol=1e-10, precision=prec)
+        assert st["relres"] <= 1e-10
+        assert rel(x, ref) <= 1e-8
+    op.close()
+
+
+def test_package_solve_entry_point(built_pkg):
+    """solve(PoissonProblemPrimal, sol, C; rhs) writes sol.entries like solve! does."""
+    p = config1_like(N=16, M=3, deg=2)
+    pkg = p.pkg
+    bd = pkg.solve(pkg.PoissonProblemPrimal, p.sol, p.C, rhs=lambda x, y: np.ones_like(x), rtol=1e-11)
+    assert np.array_equal(np.sort(bd), p.bdofs)
+    assert rel(p.sol.entries, oracle_solution(p)) <= 1e-9
+    with pytest.raises(ValueError):
+        pkg.solve(pkg.PoissonProblemPrimal, p.sol, p.C, rhs=None)

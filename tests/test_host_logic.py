@@ -1,0 +1,167 @@
+"""Host-side logic of the package against the oracle (CPU only): multi-index
+control (bit-exact integer work), coupling tensor, coefficient, spatial
+assembly, the top-weight index set with its tie-break, and marking."""
+import itertools
+import math
+
+import numpy as np
+import pytest
+
+from oracle import basis as ob
+from oracle import coefficient as oc
+from oracle import fem as of
+from oracle import mopcontrol as om
+
+
+SETS = [
+    [[0], [1, 0], [0, 1], [2, 0], [0, 0, 1]],                 # scripts/poisson_simple.jl:24
+    [[0]],                                                    # scripts/poisson.jl:74
+    [[0, 0], [1, 0], [0, 1], [1, 1], [2, 0], [0, 2], [3, 0]],
+    [[0, 0, 0], [1, 0, 0], [0, 0, 1], [2, 0, 0], [1, 0, 1], [0, 1, 0]],
+]
+
+
+def _copy(s):
+    return [list(m) for m in s]
+
+
+@pytest.mark.parametrize("mis", SETS)
+@pytest.mark.parametrize("tail", [(10, 2), (3, 1), (5, 3)])
+def test_add_boundary_modes_bitexact(pkg, mis, tail):
+    a = om.add_boundary_modes(_copy(mis), tail_extension=tail)
+    b = pkg.add_boundary_modes(_copy(mis), tail_extension=tail)
+    assert a == b
+
+
+@pytest.mark.parametrize("mis", SETS)
+def test_classify_and_neighbours_bitexact(pkg, mis):
+    ext = om.add_boundary_modes(_copy(mis))
+    for nact in (1, len(mis), len(ext)):
+        assert om.classify_modes(ext, ext[:nact]) == pkg.classify_modes(ext, ext[:nact])
+    assert om.get_neighbours(ext) == pkg.get_neighbours(ext)
+
+
+def test_classify_random_sets(pkg):
+    rng = np.random.default_rng(3)
+    for trial in range(20):
+        M = int(rng.integers(2, 5))
+        full = pkg.generate_multiindices(M, 2)
+        keep = [full[0]] + [full[i] for i in range(1, len(full)) if rng.random() < 0.3]
+        ext = om.add_boundary_modes(_copy(keep))
+        assert pkg.add_boundary_modes(_copy(keep)) == ext
+        assert om.classify_modes(ext, ext[:len(keep)]) == pkg.classify_modes(ext, ext[:len(keep)])
+
+
+def test_generate_multiindices(pkg):
+    for M, d in [(1, 3), (2, 2), (3, 3), (4, 1)]:
+        assert pkg.generate_multiindices(M, d) == om.generate_multiindices(M, d)
+
+
+def test_marking_bitexact(pkg):
+    rng = np.random.default_rng(5)
+    mis = _copy(SETS[0])
+    ext = om.add_boundary_modes(_copy(mis))
+    for trial in range(10):
+        eta = rng.random(len(ext)) ** 3
+        eta[rng.integers(0, len(ext), 3)] = eta[0]  # ties exercise the stable sort
+        a = om.stochastic_marking(list(eta), ext, len(mis), mis, theta_stochastic=0.5)
+        b = pkg.stochastic_marking(list(eta), ext, len(mis), mis, theta_stochastic=0.5)
+        assert a[0] == b[0] and a[1] == b[1]
+        assert a[2]["sorted_id"] == b[2]["sorted_id"] and a[2]["added"] == b[2]["added"]
+
+
+@pytest.mark.parametrize("name,obt", [("legendre", ob.LEGENDRE), ("hermite", ob.HERMITE)])
+def test_coupling_matrix_matches_oracle(pkg, name, obt):
+    basis = pkg.LegendrePolynomials if name == "legendre" else pkg.HermitePolynomials
+    for mis in (pkg.total_degree_multiindices(4, 3), pkg.generate_multiindices(3, 2)):
+        Go = ob.get_tensor_multiplication_with_ym(obt, mis)
+        Gp = pkg.coupling_matrix(basis, mis).toarray()
+        assert np.array_equal(Go, Gp)
+
+
+def test_onbasis_matches_oracle(pkg):
+    for obt, basis in ((ob.HERMITE, pkg.HermitePolynomials), (ob.LEGENDRE, pkg.LegendrePolynomials)):
+        a = ob.ONBasis(obt, 6, 12)
+        b = pkg.ONBasis(basis, 6, 12)
+        assert np.allclose(a.norms, b.norms, rtol=0, atol=1e-13)
+        assert np.allclose(a.evaluate(0.3), b.evaluate(0.3), rtol=1e-13, atol=1e-14)
+
+
+def test_coefficient_matches_oracle(pkg):
+    a = oc.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    b = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    assert np.array_equal(a.b1, b.b1) and np.array_equal(a.b2, b.b2)
+    assert np.allclose(a.decay_factors, b.decay_factors, rtol=1e-15, atol=0)
+    assert abs(b.decay_factors[0] - 0.9 * 6 / math.pi ** 2) < 1e-15  # 0.547 m^-2
+    x = np.linspace(0, 1, 7)
+    for m in (0, 1, 5, 40):
+        assert np.allclose(a.get_am(x, x[::-1], m), b.get_am(x, x[::-1], m), rtol=1e-15, atol=1e-16)
+        ga, gb = a.get_gradam(x, x[::-1], m), b.get_gradam(x, x[::-1], m)
+        assert np.allclose(ga[0], gb[0], atol=1e-15) and np.allclose(ga[1], gb[1], atol=1e-15)
+
+
+@pytest.mark.parametrize("order,N", [(1, 6), (2, 4)])
+def test_assembly_matches_oracle(pkg, order, N):
+    C = oc.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=10)
+    Cp = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=10)
+    Vo = of.LagrangeSpace(of.StructuredMesh(N), order)
+    Vp = pkg.H1Pk(pkg.unit_square_mesh(N), order)
+    assert Vo.ndofs == Vp.ndofs
+    assert np.array_equal(Vo.celldofs, Vp.celldofs)
+    assert np.array_equal(Vo.bdofs, Vp.bdofs)
+    assert np.allclose(Vo.dof_coords, Vp.dof_coords)
+    q = 2 * (order - 1) + 2
+    Ko = of.assemble_stiffness(Vo, C, [0, 1, 3], q)
+    Kp = pkg.assemble_stiffness(Vp, Cp, [0, 1, 3], q)
+    for a, b in zip(Ko, Kp):
+        d = (a - b).toarray()
+        assert np.abs(d).max() < 1e-14 * max(1.0, np.abs(a).max())
+    bo = of.assemble_rhs(Vo, lambda x, y: 1.0, order)
+    bp = pkg.assemble_rhs(Vp, lambda x, y: np.ones_like(x), order)
+    assert np.allclose(bo, bp, rtol=0, atol=1e-15)
+    mo, mp = Vo.mesh, Vp.mesh
+    assert np.array_equal(mo.cellfaces, mp.cellfaces)
+    assert np.array_equal(mo.face_cells, mp.face_cells)
+    assert np.array_equal(mo.bfaces, mp.bfaces)
+
+
+def test_p2_sizes_config2_mesh(pkg):
+    """263 169 dofs on the 256 x 256 P2 mesh; 3 018 753 stiffness nonzeros."""
+    V = pkg.H1Pk(pkg.unit_square_mesh(256), 2)
+    assert V.ndofs == 263169
+    indptr, col, _ = V.pattern()
+    assert len(col) == 3018753
+
+
+def _brute_top(M, P, d, maxdeg):
+    best = []
+    for mu in itertools.product(*[range(maxdeg + 1)] * M):
+        w = sum(k * math.log(v) for k, v in zip(mu, d))
+        best.append((-round(w, 11), sum(mu), tuple(-k for k in mu), list(mu)))
+    best.sort()
+    return [b[3] for b in best[:P]]
+
+
+def test_top_weight_set_bruteforce(pkg):
+    d = [0.9 * 6 / math.pi ** 2 / (m + 1) ** 2 for m in range(4)]
+    for P in (5, 12, 30):
+        assert pkg.top_weight_multiindices(4, P, d) == _brute_top(4, P, d, 8)
+
+
+def test_top_weight_set_config2_tie(pkg):
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    mis = pkg.top_weight_multiindices(20, 150, C.decay_factors)
+    assert len(mis) == 150 and mis[0] == [0] * 20
+    assert max(mi[0] for mi in mis) == 12
+    # the 150th index wins the tie with two others by lexicographic order
+    assert mis[149] == [0, 1] + [0] * 9 + [1] + [0] * 8
+    # downward closed
+    s = {tuple(m) for m in mis}
+    for mi in mis:
+        for m in range(20):
+            if mi[m] > 0:
+                t = list(mi)
+                t[m] -= 1
+                assert tuple(t) in s
+    G = pkg.coupling_matrix(pkg.LegendrePolynomials, mis)
+    assert G.nnz == 560

@@ -1,0 +1,68 @@
+"""Identities that pin the oracle's operator and solvers where the reference
+has no tests (CPU only): the literal per-G-nonzero apply equals the explicit
+Kronecker matrix of solve_full_primal!, the C restatement equals the Python
+one, the operator is symmetric on interior dofs, GMRES (the reference's
+solver) and PCG agree with the direct Kronecker solve, and P = 1 reduces to
+the deterministic problem."""
+import numpy as np
+import pytest
+import scipy.sparse.linalg as spla
+
+from oracle import cbuild
+from oracle import sg as osg
+from tests.problems import config1_like
+
+
+@pytest.fixture(scope="module")
+def prob():
+    return config1_like(N=8, M=3, deg=2)
+
+
+def test_literal_apply_equals_grouped(prob):
+    x = np.random.default_rng(0).standard_normal(prob.n * prob.P)
+    a = osg.mul_literal(x, prob.K0, prob.Ks, prob.G, prob.bdofs, prob.P)
+    b = osg.apply_fast(x, prob.K0, prob.Ks, prob.G, prob.bdofs, prob.P)
+    assert np.linalg.norm(a - b) <= 1e-14 * np.linalg.norm(a)
+
+
+def test_c_restatement_equals_python(prob):
+    op = cbuild.COperator([prob.K0] + prob.Ks, prob.G, prob.bdofs, prob.P)
+    x = np.random.default_rng(1).standard_normal(prob.n * prob.P)
+    a = osg.mul_literal(x, prob.K0, prob.Ks, prob.G, prob.bdofs, prob.P)
+    for th in (1, 4):
+        b = op.mul(x, nthreads=th)
+        assert np.linalg.norm(a - b) <= 1e-14 * np.linalg.norm(a)
+
+
+def test_symmetric_on_interior(prob):
+    rng = np.random.default_rng(2)
+    mask = osg.interior_mask(prob.n, prob.P, prob.bdofs)
+    u = rng.standard_normal(prob.n * prob.P) * mask
+    v = rng.standard_normal(prob.n * prob.P) * mask
+    au = osg.mul_literal(u, prob.K0, prob.Ks, prob.G, prob.bdofs, prob.P)
+    av = osg.mul_literal(v, prob.K0, prob.Ks, prob.G, prob.bdofs, prob.P)
+    assert abs(v @ au - u @ av) <= 1e-13 * abs(v @ au)
+    assert u @ au > 0
+
+
+def test_gmres_pcg_direct_agree(prob):
+    n, P = prob.n, prob.P
+    prec = osg.MeanPreconditioner(prob.K0, prob.bdofs, P)
+    b = osg.reference_rhs(np.zeros(n * P), prob.b0, prob.bdofs, P)
+    ap = lambda v: osg.mul_literal(v, prob.K0, prob.Ks, prob.G, prob.bdofs, P)
+    xg, st = osg.gmres_left(ap, prec.ldiv, b, np.zeros(n * P))
+    assert st["solved"]
+    xk = osg.kron_direct(prob.K0, prob.Ks, prob.G, prob.b0, prob.bdofs, P)
+    xp, _ = osg.pcg(ap, prec.ldiv, b, np.zeros(n * P), osg.interior_mask(n, P, prob.bdofs), tol=1e-13)
+    assert np.linalg.norm(xg - xk) <= 1e-12 * np.linalg.norm(xk)
+    assert np.linalg.norm(xp - xk) <= 1e-11 * np.linalg.norm(xk)
+
+
+def test_single_mode_is_deterministic_solve():
+    p = config1_like(N=8, M=2, deg=0)
+    assert p.P == 1
+    xk = osg.kron_direct(p.K0, p.Ks, p.G, p.b0, p.bdofs, 1)
+    inner = np.setdiff1d(np.arange(p.n), p.bdofs)
+    u = np.zeros(p.n)
+    u[inner] = spla.spsolve(p.K0[inner][:, inner].tocsc(), p.b0[inner])
+    assert np.linalg.norm(xk - u) <= 1e-12 * np.linalg.norm(u)
