@@ -42,7 +42,7 @@ class SolveOptions(ctypes.Structure):
 class SolveStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("outer_iterations", ctypes.c_int), ("fp64_applies", ctypes.c_int),
                 ("relres", ctypes.c_double), ("time_ms", ctypes.c_double), ("apply_ms", ctypes.c_double),
-                ("precond_ms", ctypes.c_double)]
+                ("precond_ms", ctypes.c_double), ("kernel_launches", ctypes.c_longlong)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -70,6 +70,7 @@ SIGNATURES = {
     "sgfem_from_device_layout": (ctypes.c_int, [_P, _P, _DP, ctypes.c_int]),
     "sgfem_solve_device": (ctypes.c_int, [_P, _DP, _P, ctypes.POINTER(SolveOptions), ctypes.POINTER(SolveStats)]),
     "sgfem_time_apply": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _DP]),
+    "sgfem_kernel_launches": (ctypes.c_longlong, [_P]),
 }
 
 _lib = None
@@ -232,6 +233,9 @@ class Context:
         self._check(self.lib.sgfem_solve_device(self.h, _dp(b0), _P(x_ptr), ctypes.byref(o), ctypes.byref(st)),
                     allow=(ERR_MAXIT,) if allow_maxit else ())
         return st
+
+    def kernel_launches(self):
+        return int(self.lib.sgfem_kernel_launches(self.h))
 
     def time_apply(self, precision=FP64, reps=10):
         ms = ctypes.c_double()

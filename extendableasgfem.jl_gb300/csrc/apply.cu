@@ -130,7 +130,7 @@ int launch_qt(sgfem_context* ctx, const T* vals, const T* combg, const void* X, 
     k_apply<T, QT><<<grid, WPB * 32, smem, ctx->stream>>>(
         ctx->d_rowptr, ctx->d_col, vals, ctx->M1, (const T*)X, (T*)Y, (int)ctx->n, (int)ctx->P, (int)ctx->ld,
         ctx->d_bmask, ctx->d_qtab, ctx->Qn, ctx->d_combptr, ctx->d_combq, combg, partials, scal);
-    SG_CUDA(ctx, cudaGetLastError());
+    SG_LAUNCHED(ctx);
     return SGFEM_OK;
 }
 

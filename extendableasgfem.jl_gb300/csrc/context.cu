@@ -56,6 +56,8 @@ static void free_dev(void* p) {
 
 extern "C" int sgfem_version(void) { return 10000; }
 
+extern "C" long long sgfem_kernel_launches(const sgfem_context* ctx) { return ctx ? ctx->launches : 0; }
+
 extern "C" int sgfem_create(sgfem_context** out, int device) {
     if (!out) return SGFEM_ERR_ARGUMENT;
     *out = nullptr;
@@ -443,7 +445,7 @@ int sg_launch_to_device(sgfem_context* ctx, const double* stage, void* X, int pr
         k_to_device<double><<<grid, block, 0, ctx->stream>>>(stage, (double*)X, ctx->d_iperm, (int)ctx->n, (int)ctx->P, (int)ctx->ld);
     else
         k_to_device<float><<<grid, block, 0, ctx->stream>>>(stage, (float*)X, ctx->d_iperm, (int)ctx->n, (int)ctx->P, (int)ctx->ld);
-    SG_CUDA(ctx, cudaGetLastError());
+    SG_LAUNCHED(ctx);
     return SGFEM_OK;
 }
 
@@ -453,7 +455,7 @@ int sg_launch_from_device(sgfem_context* ctx, const void* X, double* stage, int 
         k_from_device<double><<<grid, block, 0, ctx->stream>>>((const double*)X, stage, ctx->d_iperm, (int)ctx->n, (int)ctx->P, (int)ctx->ld);
     else
         k_from_device<float><<<grid, block, 0, ctx->stream>>>((const float*)X, stage, ctx->d_iperm, (int)ctx->n, (int)ctx->P, (int)ctx->ld);
-    SG_CUDA(ctx, cudaGetLastError());
+    SG_LAUNCHED(ctx);
     return SGFEM_OK;
 }
 

@@ -184,7 +184,7 @@ struct Solver {
 
     int fin(int nb, int mode, FinArgs fa = FinArgs{0.0, 0}, double* out = nullptr) {
         k_finalize<<<1, VT, 0, ctx->stream>>>(partials, nb, s, mode, fa, out);
-        SG_CUDA(ctx, cudaGetLastError());
+        SG_LAUNCHED(ctx);
         return SGFEM_OK;
     }
 
@@ -216,7 +216,7 @@ struct Solver {
         const size_t total = (size_t)ctx->n * ctx->ld;
         const int g = vgrid(ctx);
         k_update<T><<<g, VT, 0, ctx->stream>>>(x, p, r, q, total, s, partials);
-        SG_CUDA(ctx, cudaGetLastError());
+        SG_LAUNCHED(ctx);
         SG_TRY(fin(g, FIN_RR, fa));
         SG_TRY(precond_block<T>(precision, r, p, tmp, maxit));
         return SGFEM_OK;
@@ -243,7 +243,7 @@ struct Solver {
         const size_t total = (size_t)ctx->n * ctx->ld;
         const int g = vgrid(ctx);
         k_dot<T><<<g, VT, 0, ctx->stream>>>(r, r, total, partials);
-        SG_CUDA(ctx, cudaGetLastError());
+        SG_LAUNCHED(ctx);
         SG_TRY(fin(g, FIN_RR, FinArgs{0.0, maxit}));
         SG_TRY(precond_block<T>(precision, r, p, tmp, maxit));
 
@@ -251,7 +251,10 @@ struct Solver {
         cudaGraphExec_t exec = nullptr;
         SG_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
         int st = SGFEM_OK;
+        const long long before = ctx->launches;
         for (int k = 0; k < check_every && st == SGFEM_OK; ++k) st = iteration<T>(precision, x, r, p, q, tmp, maxit);
+        const long long per_graph = ctx->launches - before;  // kernel nodes per replay
+        ctx->launches = before;
         cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
         if (st != SGFEM_OK) {
             if (graph) cudaGraphDestroy(graph);
@@ -268,6 +271,7 @@ struct Solver {
                 break;
             }
             cudaError_t le = cudaGraphLaunch(exec, ctx->stream);
+            ctx->launches += per_graph;
             if (le != cudaSuccess) {
                 cudaGraphExecDestroy(exec);
                 cudaGraphDestroy(graph);
@@ -364,12 +368,14 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
     SG_CUDA(ctx, cudaMemcpyAsync(d_b0, b0, (size_t)ctx->n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
 
     SG_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    const long long launches0 = ctx->launches;
     const int g = vgrid(ctx);
     k_build_rhs<<<g, VT, 0, ctx->stream>>>(d_b0, x64, b, ctx->d_iperm, ctx->d_bmask, (int)ctx->n, (int)ctx->ld,
                                           o->reference_rhs ? 1 : 0);
+    ctx->launches++;
     k_add_b0<<<(int)std::min<int64_t>((ctx->n + VT - 1) / VT, 4096), VT, 0, ctx->stream>>>(
         d_b0, b, ctx->d_iperm, ctx->d_bmask, (int)ctx->n, (int)ctx->ld);
-    SG_CUDA(ctx, cudaGetLastError());
+    SG_LAUNCHED(ctx);
 
     Solver S{ctx, prec_kind, partials, ctx->d_scal};
     // ||b||^2 -> host
@@ -385,6 +391,7 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
     st->relres = 0.0;
     st->apply_ms = -1.0;
     st->precond_ms = -1.0;
+    st->kernel_launches = 0;
     if (!std::isfinite(bb)) return sg_fail(ctx, SGFEM_ERR_NONFINITE, "non-finite right-hand side");
     if (bb == 0.0) {
         SG_CUDA(ctx, cudaMemsetAsync(x64, 0, n64, ctx->stream));
@@ -399,7 +406,7 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
         int nb = 0;
         SG_TRY(sg_launch_apply(ctx, SGFEM_FP64, x64, t, nullptr, &nb, nullptr));
         k_residual<<<g, VT, 0, ctx->stream>>>(b, t, r, total, partials);
-        SG_CUDA(ctx, cudaGetLastError());
+        SG_LAUNCHED(ctx);
         SG_TRY(S.fin(g, FIN_SUM, FinArgs{0.0, 0}, d_sum));
         SG_CUDA(ctx, cudaMemcpyAsync(rr_out, d_sum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
         SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -439,7 +446,7 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
             if (rr <= rtol2 * bb) break;
             if (remaining <= 0) { status = SGFEM_ERR_MAXIT; break; }
             k_demote<<<g, VT, 0, ctx->stream>>>(r, r32, d32, total, partials);
-            SG_CUDA(ctx, cudaGetLastError());
+            SG_LAUNCHED(ctx);
             // inner target: reduce ||r|| by inner_rtol, but never below what the outer tolerance needs
             const double want = std::max(in2, 0.25 * rtol2 * bb / rr);
             SG_TRY(S.fin(g, FIN_TOL, FinArgs{want, 0}, nullptr));
@@ -450,7 +457,7 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
             remaining -= it;
             if (s2 == SGFEM_ERR_BREAKDOWN || s2 == SGFEM_ERR_NONFINITE) { status = s2; break; }
             k_promote_add<<<g, VT, 0, ctx->stream>>>(x64, d32, total);
-            SG_CUDA(ctx, cudaGetLastError());
+            SG_LAUNCHED(ctx);
             SG_TRY(true_residual(&rr));
             if (o->precision == SGFEM_FP32) break;  // plain FP32 PCG: no refinement
         }
@@ -460,6 +467,7 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
     float ms = 0.f;
     SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     st->time_ms = ms;
+    st->kernel_launches = ctx->launches - launches0;
     st->relres = std::sqrt(rr / bb);
     if (status == SGFEM_OK && !(st->relres <= o->rtol)) status = (o->precision == SGFEM_FP32) ? SGFEM_OK : SGFEM_ERR_MAXIT;
     return status_message(ctx, status);

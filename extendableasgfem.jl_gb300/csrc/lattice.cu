@@ -354,7 +354,7 @@ int sg_lat_pass_x(sgfem_context* ctx, int precision, const void* R, void* T, con
         size_t smem = lat_smem(ctx, 4);
         k_lat_pass_x<float><<<grid, LAT_THREADS, smem, ctx->stream>>>((const float*)R, (float*)T, ctx->d_lat_tab32, g, 0, scal);
     }
-    SG_CUDA(ctx, cudaGetLastError());
+    SG_LAUNCHED(ctx);
     return SGFEM_OK;
 }
 
@@ -369,7 +369,7 @@ int sg_lat_pass_y(sgfem_context* ctx, int precision, void* T, double* rz, int* n
         size_t smem = lat_smem(ctx, 4);
         k_lat_pass_y<float><<<grid, LAT_THREADS, smem, ctx->stream>>>((float*)T, ctx->d_lat_tab32, ctx->d_lat_scale32, g, rz, scal);
     }
-    SG_CUDA(ctx, cudaGetLastError());
+    SG_LAUNCHED(ctx);
     return SGFEM_OK;
 }
 
@@ -383,7 +383,7 @@ int sg_lat_pass_xinv(sgfem_context* ctx, int precision, const void* T, void* out
         size_t smem = lat_smem(ctx, 4);
         k_lat_pass_x<float><<<grid, LAT_THREADS, smem, ctx->stream>>>((const float*)T, (float*)out, ctx->d_lat_tab32, g, mode, scal);
     }
-    SG_CUDA(ctx, cudaGetLastError());
+    SG_LAUNCHED(ctx);
     return SGFEM_OK;
 }
 
@@ -399,6 +399,6 @@ int sg_jacobi(sgfem_context* ctx, int precision, const void* R, void* out, int m
     else
         k_jacobi<float><<<grid, threads, 0, ctx->stream>>>((const float*)R, (float*)out, ctx->d_dinv32, (int)ctx->n,
                                                            (int)ctx->ld, identity, mode, rz, scal);
-    SG_CUDA(ctx, cudaGetLastError());
+    SG_LAUNCHED(ctx);
     return SGFEM_OK;
 }

@@ -111,6 +111,7 @@ struct sgfem_context {
     KrylovScalars* d_scal = nullptr;
     KrylovScalars* h_scal = nullptr;  // pinned
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    long long launches = 0;    // kernels launched by this context (graph replays included)
 };
 
 // ------------------------------------------------------------------ errors / memory
@@ -121,6 +122,13 @@ int sg_cuda_fail(sgfem_context* ctx, cudaError_t e, const char* what);
     do {                                                                \
         cudaError_t _e = (call);                                        \
         if (_e != cudaSuccess) return sg_cuda_fail((ctx), _e, #call);   \
+    } while (0)
+
+// after a kernel launch: count it and check the launch
+#define SG_LAUNCHED(ctx)                                   \
+    do {                                                   \
+        (ctx)->launches++;                                 \
+        SG_CUDA(ctx, cudaGetLastError());                  \
     } while (0)
 
 #define SG_TRY(call)                   \

@@ -70,6 +70,7 @@ typedef struct {
     double time_ms;        /* device time of the solve (CUDA events) */
     double apply_ms;       /* device time spent in operator applications */
     double precond_ms;     /* device time spent in the preconditioner */
+    long long kernel_launches; /* kernels this solve launched (graph replays included) */
 } sgfem_solve_stats;
 
 /* context */
@@ -139,6 +140,8 @@ SGFEM_API int sgfem_solve_device(sgfem_context* ctx, const double* b0, void* x_d
 
 /* time (ms, CUDA events on the context stream) of `reps` back-to-back device applies */
 SGFEM_API int sgfem_time_apply(sgfem_context* ctx, int precision, int reps, double* ms_per_apply);
+/* kernels launched by this context so far (graph replays included) */
+SGFEM_API long long sgfem_kernel_launches(const sgfem_context* ctx);
 
 #ifdef __cplusplus
 }
