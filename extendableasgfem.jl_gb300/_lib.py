@@ -71,6 +71,7 @@ SIGNATURES = {
     "sgfem_solve_device": (ctypes.c_int, [_P, _DP, _P, ctypes.POINTER(SolveOptions), ctypes.POINTER(SolveStats)]),
     "sgfem_time_apply": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _DP]),
     "sgfem_kernel_launches": (ctypes.c_longlong, [_P]),
+    "sgfem_precondition_device_static": (ctypes.c_int, [_P, _P, _P, ctypes.c_int]),
 }
 
 _lib = None
@@ -233,6 +234,11 @@ class Context:
         self._check(self.lib.sgfem_solve_device(self.h, _dp(b0), _P(x_ptr), ctypes.byref(o), ctypes.byref(st)),
                     allow=(ERR_MAXIT,) if allow_maxit else ())
         return st
+
+    def precondition_device_static(self, r_ptr, z_ptr, precision=FP64):
+        """Lattice preconditioner on device-layout vectors using the library's
+        static scratch array (no device allocation; see include/sgfem.h)."""
+        self._check(self.lib.sgfem_precondition_device_static(self.h, _P(r_ptr), _P(z_ptr), int(precision)))
 
     def kernel_launches(self):
         return int(self.lib.sgfem_kernel_launches(self.h))

@@ -140,6 +140,25 @@ SGFEM_API int sgfem_solve_device(sgfem_context* ctx, const double* b0, void* x_d
 
 /* time (ms, CUDA events on the context stream) of `reps` back-to-back device applies */
 SGFEM_API int sgfem_time_apply(sgfem_context* ctx, int precision, int reps, double* ms_per_apply);
+/*
+ * No counterpart in the reference package.  Applies the mean-based lattice
+ * preconditioner (what sgfem_precondition does with SGFEM_PREC_LATTICE) to
+ * device vectors without allocating any device memory.  It is meant for
+ * callers that cannot allocate at that point: a Julia process whose CUDA.jl
+ * memory pool already owns the GPU, an application held to a fixed
+ * device-memory budget, or a loop in which the implicit synchronisation of
+ * cudaMalloc is not acceptable.  r_dev (input) and z_dev (output) are vectors
+ * in the device layout (sgfem_device_layout).  The intermediate buffer is a
+ * static device array of SGFEM_STATIC_SCRATCH_BYTES that every GPU loading the
+ * library holds until the process exits; a vector needing more than that
+ * (n_dev * ld * element size) is rejected with SGFEM_ERR_ARGUMENT.  The first
+ * call on a device looks up the array's device address, so make that first
+ * call before any stream capture.  All calls share the one array: calls that
+ * overlap on the same GPU (from other contexts or host threads) race on it.
+ */
+#define SGFEM_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
+SGFEM_API int sgfem_precondition_device_static(sgfem_context* ctx, const void* r_dev, void* z_dev, int precision);
+
 /* kernels launched by this context so far (graph replays included) */
 SGFEM_API long long sgfem_kernel_launches(const sgfem_context* ctx);
 
