@@ -302,7 +302,10 @@ def run_ours(args, rank, world, local, pg):
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(n * P * 8 + n * 8),
                 "d2h_bytes_per_step": int(n * P * 8)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": "k_apply<float> (SG operator apply, FP32)",
+        "apply_variant": ctx.apply_variant[1],
+        "roofline": {"bound": "hbm",
+                     "kernel": ("sg_apply_jit (SG operator apply, FP32, specialised by NVRTC)"
+                                if ctx.apply_variant[0] == 1 else "k_apply<float> (SG operator apply, FP32)"),
                      "achieved": ach, "peak": peak_gbs, "unit": "GB/s", "frac": ach / peak_gbs,
                      "traffic": traffic, "algorithmic_bytes": B32, "ms_per_launch": t32,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs" if pk else "fallback 6.8 TB/s"},

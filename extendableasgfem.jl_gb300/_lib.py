@@ -72,6 +72,8 @@ SIGNATURES = {
     "sgfem_time_apply": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _DP]),
     "sgfem_kernel_launches": (ctypes.c_longlong, [_P]),
     "sgfem_precondition_device_static": (ctypes.c_int, [_P, _P, _P, ctypes.c_int]),
+    "sgfem_apply_variant": (ctypes.c_int, [_P]),
+    "sgfem_apply_variant_log": (ctypes.c_char_p, [_P]),
 }
 
 _lib = None
@@ -239,6 +241,11 @@ class Context:
         """Lattice preconditioner on device-layout vectors using the library's
         static scratch array (no device allocation; see include/sgfem.h)."""
         self._check(self.lib.sgfem_precondition_device_static(self.h, _P(r_ptr), _P(z_ptr), int(precision)))
+
+    @property
+    def apply_variant(self):
+        """(1 if the FP32 apply is specialised to this coupling structure else 0, log)."""
+        return int(self.lib.sgfem_apply_variant(self.h)), self.lib.sgfem_apply_variant_log(self.h).decode()
 
     def kernel_launches(self):
         return int(self.lib.sgfem_kernel_launches(self.h))

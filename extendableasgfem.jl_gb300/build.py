@@ -60,7 +60,7 @@ def build(verbose=False, ptxas_verbose=False, force=False):
                 raise RuntimeError("nvcc failed for " + cmd[-3])
     if force or jobs or _stale(OUT, objs):
         tmp = OUT + ".tmp"
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)

@@ -162,6 +162,11 @@ int sg_launch_apply(sgfem_context* ctx, int precision, const void* X, void* Y, d
     const size_t smem = per_warp * sg_elem_bytes(precision) * WPB;
     if (smem > 200 * 1024)
         return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "apply: per-row pair list too large for shared memory");
+    if (precision == SGFEM_FP32 && ctx->jit_ok) {
+        const int jgrid = sg_jit_grid(ctx);
+        if (nblocks) *nblocks = jgrid;
+        return sg_jit_launch(ctx, X, Y, dot_partials, jgrid, skip_if_done);
+    }
     int grid = (int)std::min<int64_t>((ctx->n + WPB - 1) / WPB, (int64_t)ctx->num_sms * 8);
     if (grid < 1) grid = 1;
     if (nblocks) *nblocks = grid;

@@ -86,7 +86,9 @@ extern "C" int sgfem_destroy(sgfem_context* ctx) {
     void* ptrs[] = {ctx->d_rowptr, ctx->d_col, ctx->d_val64, ctx->d_val32, ctx->d_bmask, ctx->d_iperm,
                     ctx->d_dinv64, ctx->d_dinv32, ctx->d_qtab, ctx->d_combptr, ctx->d_combq,
                     ctx->d_combg64, ctx->d_combg32, ctx->d_lat_tab64, ctx->d_lat_tab32,
-                    ctx->d_lat_scale64, ctx->d_lat_scale32, ctx->d_scal, ctx->w_stage.p, ctx->w_partials.p};
+                    ctx->d_lat_scale64, ctx->d_lat_scale32, ctx->d_scal, ctx->w_stage.p, ctx->w_partials.p,
+                    ctx->d_jptr, ctx->d_joff, ctx->d_jg, ctx->d_jtab, ctx->d_val32p, ctx->d_mode_of_col};
+    sg_jit_release(ctx);
     for (void* p : ptrs) free_dev(p);
     for (int i = 0; i < SG_NBUF; ++i) free_dev(ctx->w_vec[i].p);
     if (ctx->h_scal) cudaFreeHost(ctx->h_scal);
@@ -202,6 +204,89 @@ static bool detect_lattice(sgfem_context* ctx, std::vector<int32_t>& iperm) {
     }
     ctx->Nl = Nl;
     return true;
+}
+
+// Device column order of the P modes.  Column c belongs to group c/32 (one
+// lane per column in the specialised apply).  For every pair p >= 1 of KLE
+// terms (K_2p, K_2p+1) the apply spends one packed FMA per group that holds a
+// column coupled to that pair (pair 0 holds K_0, which couples every column),
+// so the order minimises
+//   cost = sum_{p>=1} #{groups holding a column coupled to pair p}.
+// Start: columns sorted by the number of pairs they couple to (hubs first);
+// then simulated annealing over swaps of two columns in different groups
+// (fixed seeds, incremental cost), best of four runs.
+void sg_mode_order(const sgfem_context* ctx, const std::vector<std::vector<char>>& nzcol,
+                   std::vector<int32_t>& mode_of_col) {
+    const int64_t P = ctx->P, M = ctx->M;
+    const int NP = (int)((M + 2) / 2);  // pairs 0..NP-1, pair 0 = (K_0, K_1)
+    const int KG = (int)((P + 31) / 32);
+    std::vector<std::vector<char>> part(P, std::vector<char>(NP, 0));
+    std::vector<int> deg(P, 0);
+    for (int64_t nu = 0; nu < P; ++nu)
+        for (int pr = 1; pr < NP; ++pr) {
+            for (int m = 2 * pr; m <= std::min<int64_t>(M, 2 * pr + 1); ++m)
+                if (nzcol[m][nu]) part[nu][pr] = 1;
+            deg[nu] += part[nu][pr];
+        }
+    std::vector<int32_t> start(P);
+    std::iota(start.begin(), start.end(), 0);
+    std::stable_sort(start.begin(), start.end(), [&](int a, int b) { return deg[a] > deg[b]; });
+    mode_of_col = start;
+    if (KG <= 1 || NP <= 1) return;
+
+    auto delta_of = [&](const std::vector<int>& cnt, int n1, int n2, int a, int b) {
+        int delta = 0;
+        for (int pr = 1; pr < NP; ++pr) {
+            const int d = part[n1][pr] - part[n2][pr];  // +1: a column of pair pr moves from a to b
+            if (d == 0) continue;
+            const int ca = cnt[(size_t)pr * KG + a], cb = cnt[(size_t)pr * KG + b];
+            delta += ((ca - d) > 0) - (ca > 0) + ((cb + d) > 0) - (cb > 0);
+        }
+        return delta;
+    };
+    int best_cost = -1;
+    const int iters = (int)std::min<int64_t>(400000, 2000 * P);
+    for (int run = 0; run < 4; ++run) {
+        std::vector<int32_t> order = start;
+        std::vector<int> cnt((size_t)NP * KG, 0);
+        for (int64_t c = 0; c < P; ++c)
+            for (int pr = 1; pr < NP; ++pr) cnt[(size_t)pr * KG + c / 32] += part[order[c]][pr];
+        int cost = 0;
+        for (size_t t = 0; t < cnt.size(); ++t) cost += cnt[t] > 0;
+        std::vector<int32_t> best_order = order;
+        int run_best = cost;
+        uint64_t rs = 0x9E3779B97F4A7C15ull * (uint64_t)(run + 1);
+        auto rnd = [&]() {
+            rs ^= rs << 13; rs ^= rs >> 7; rs ^= rs << 17;
+            return rs;
+        };
+        for (int it = 0; it < iters; ++it) {
+            const int64_t c1 = (int64_t)(rnd() % (uint64_t)P), c2 = (int64_t)(rnd() % (uint64_t)P);
+            const int a = (int)(c1 / 32), b = (int)(c2 / 32);
+            if (a == b) continue;
+            const int n1 = order[c1], n2 = order[c2];
+            const int delta = delta_of(cnt, n1, n2, a, b);
+            const double T = 2.0 * (1.0 - (double)it / iters) + 1e-3;
+            const double u = (double)(rnd() >> 11) * (1.0 / 9007199254740992.0);
+            if (delta <= 0 || u < std::exp(-delta / T)) {
+                for (int pr = 1; pr < NP; ++pr) {
+                    const int d = part[n1][pr] - part[n2][pr];
+                    cnt[(size_t)pr * KG + a] -= d;
+                    cnt[(size_t)pr * KG + b] += d;
+                }
+                std::swap(order[c1], order[c2]);
+                cost += delta;
+                if (cost < run_best) {
+                    run_best = cost;
+                    best_order = order;
+                }
+            }
+        }
+        if (best_cost < 0 || run_best < best_cost) {
+            best_cost = run_best;
+            mode_of_col = best_order;
+        }
+    }
 }
 
 template <typename T>
@@ -322,7 +407,7 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
     }
     ctx->lat_scale = dcount ? dsum / (4.0 * dcount) : 1.0;
 
-    // ---- coupling schedule from G ((M*P) x P, CSC): entry (row = m'*P + mu, col = nu), m = m'+1
+    // ---- coupling structure from G ((M*P) x P, CSC): entry (row = m'*P + mu, col = nu), m = m'+1
     std::vector<std::vector<char>> nzcol(M + 1, std::vector<char>(P, 0));
     struct GE { int m; int mu; int nu; double g; };
     std::vector<GE> ges;
@@ -336,19 +421,33 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
             nzcol[m][nu] = 1;
             ges.push_back({m, mu, (int)nu, g});
         }
+
+    // ---- device column order of the modes (sg_mode_order): packs the coupled
+    // columns of each pair of KLE terms into few 32-column groups
+    std::vector<int32_t> mode_of_col;  // device column -> caller mode
+    sg_mode_order(ctx, nzcol, mode_of_col);
+    ctx->imode.assign(P, 0);
+    for (int64_t c = 0; c < P; ++c) ctx->imode[mode_of_col[c]] = (int32_t)c;
+    const std::vector<int32_t>& imode = ctx->imode;
+
+    // pair list Q in device columns: (0, c) for all c, then (m, c) for nonzero columns of G_m
     std::vector<int32_t> qtab;
     std::map<std::pair<int, int>, int> qidx;
-    for (int64_t nu = 0; nu < P; ++nu) {
-        qidx[{0, (int)nu}] = (int)qtab.size();
-        qtab.push_back((int32_t)nu);  // m = 0
+    for (int64_t c = 0; c < P; ++c) {
+        qidx[{0, (int)c}] = (int)qtab.size();
+        qtab.push_back((int32_t)c);
     }
     for (int64_t m = 1; m <= M; ++m)
-        for (int64_t nu = 0; nu < P; ++nu)
-            if (nzcol[m][nu]) {
-                qidx[{(int)m, (int)nu}] = (int)qtab.size();
-                qtab.push_back((int32_t)((m << 16) | nu));
+        for (int64_t c = 0; c < P; ++c)
+            if (nzcol[m][mode_of_col[c]]) {
+                qidx[{(int)m, (int)c}] = (int)qtab.size();
+                qtab.push_back((int32_t)((m << 16) | c));
             }
     ctx->Qn = (int)qtab.size();
+    for (GE& e : ges) {
+        e.mu = imode[e.mu];
+        e.nu = imode[e.nu];
+    }
     std::sort(ges.begin(), ges.end(), [](const GE& a, const GE& b) {
         if (a.mu != b.mu) return a.mu < b.mu;
         if (a.m != b.m) return a.m < b.m;
@@ -364,6 +463,84 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
     for (int64_t mu = 0; mu < P; ++mu) combptr[mu + 1] += combptr[mu];
     ctx->ncomb = (int)combq.size();
     std::vector<float> combg32(combg.begin(), combg.end());
+
+    // ---- slot tables of the specialised FP32 apply: slot (pair p = m/2, group k = c/32)
+    // exists if some column of group k couples to K_2p or K_2p+1 (K_0 couples to all)
+    const int KG = (int)((P + 31) / 32);
+    const int NPAIR = (ctx->M1 + 1) / 2;
+    ctx->M1P = (ctx->M1 + 3) / 4 * 4;
+    ctx->jit_slot_of.assign((size_t)NPAIR * KG, -1);
+    ctx->jit_slots.clear();
+    for (int pr = 0; pr < NPAIR; ++pr)
+        for (int k = 0; k < KG; ++k) {
+            bool need = false;
+            for (int c = 32 * k; c < std::min<int64_t>(P, 32 * k + 32) && !need; ++c)
+                for (int m = 2 * pr; m <= std::min<int64_t>(M, 2 * pr + 1) && !need; ++m)
+                    need = (m == 0) || nzcol[m][mode_of_col[c]];
+            if (need) {
+                ctx->jit_slot_of[(size_t)pr * KG + k] = (int)ctx->jit_slots.size();
+                ctx->jit_slots.push_back({pr, k});
+            }
+        }
+    auto slot_off = [&](int m, int c) {
+        int sl = ctx->jit_slot_of[(size_t)(m / 2) * KG + c / 32];
+        return sl * 64 + 2 * (c % 32) + (m % 2);
+    };
+    // combination list per output column: (1, acc(0, c)) then (g, acc(m, nu))
+    std::vector<int32_t> jptr(P + 1, 0), joff;
+    std::vector<float> jg;
+    for (int64_t c = 0; c < P; ++c) {
+        joff.push_back(slot_off(0, (int)c));
+        jg.push_back(1.0f);
+        for (int32_t e = combptr[c]; e < combptr[c + 1]; ++e) {
+            int q = combq[e];
+            int m = qtab[q] >> 16, nu = qtab[q] & 0xffff;
+            joff.push_back(slot_off(m, nu));
+            jg.push_back((float)combg[e]);
+        }
+        jptr[c + 1] = (int32_t)joff.size();
+    }
+    std::vector<float> val32p((size_t)nnz * ctx->M1P, 0.0f);
+    for (int64_t k = 0; k < nnz; ++k)
+        for (int m = 0; m < ctx->M1; ++m) val32p[(size_t)k * ctx->M1P + m] = (float)val64[(size_t)k * ctx->M1 + m];
+    SG_TRY(upload(ctx, &ctx->d_jptr, jptr.data(), jptr.size()));
+    SG_TRY(upload(ctx, &ctx->d_joff, joff.data(), joff.size()));
+    SG_TRY(upload(ctx, &ctx->d_jg, jg.data(), jg.size()));
+    // lane schedule of the combination: columns assigned to the 32 lanes longest
+    // first (each to the least loaded lane); per lane its columns' entries in
+    // sequence, padded to a common length T; entry (i, lane) at [i * 32 + lane]
+    // x = sacc offset | column << 13 | (last entry of the column) << 28, y = g bits
+    {
+        std::vector<int> order(P);
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            return (jptr[a + 1] - jptr[a]) > (jptr[b + 1] - jptr[b]);
+        });
+        std::vector<std::vector<int2>> lanes(32);
+        for (int c : order) {
+            int best = 0;
+            for (int l = 1; l < 32; ++l)
+                if (lanes[l].size() < lanes[best].size()) best = l;
+            for (int32_t e = jptr[c]; e < jptr[c + 1]; ++e) {
+                int bits;
+                std::memcpy(&bits, &jg[e], sizeof(int));
+                const bool last = (e + 1 == jptr[c + 1]);
+                lanes[best].push_back(make_int2(joff[e] | (int)(c << 13) | ((last ? 1 : 0) << 28), bits));
+            }
+        }
+        size_t T = 0;
+        for (auto& l : lanes) T = std::max(T, l.size());
+        ctx->jit_T = (int)T;
+        std::vector<int2> jtab(T * 32, make_int2(0, 0));
+        for (int l = 0; l < 32; ++l)
+            for (size_t i = 0; i < lanes[l].size(); ++i) jtab[i * 32 + l] = lanes[l][i];
+        const bool fits = (ctx->jit_slots.size() * 64 <= 8192) && P <= 32767;
+        if (!fits) ctx->jit_T = -1;
+        SG_TRY(upload(ctx, &ctx->d_jtab, jtab.data(), jtab.size()));
+    }
+    SG_TRY(upload(ctx, &ctx->d_val32p, val32p.data(), val32p.size()));
+    ctx->mode_of_col = mode_of_col;
+    SG_TRY(upload(ctx, &ctx->d_mode_of_col, mode_of_col.data(), mode_of_col.size()));
 
     // ---- upload
     SG_TRY(upload(ctx, &ctx->d_rowptr, rowptr32.data(), rowptr32.size()));
@@ -393,6 +570,8 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
     }
     SG_TRY(sg_apply_configure(ctx));
     if (ctx->lattice) SG_TRY(sg_lattice_configure(ctx));
+    // specialised FP32 apply; on failure the generic kernel stays in use (reason in the variant log)
+    if (sg_jit_build(ctx) != SGFEM_OK) ctx->err.clear();
     // host copies of the pattern are no longer needed
     for (auto& A : ctx->mats) {
         A.colptr.clear(); A.colptr.shrink_to_fit();
@@ -405,46 +584,48 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
 
 // ------------------------------------------------------------------ layout kernels
 // stage: caller layout, FP64, column-major n x P.  X: device layout (T), n x ld.
+// tile of 32 dofs x 32 device columns; column c holds caller mode mode_of_col[c]
+// (pad columns c >= P are written as zero)
 template <typename T>
 __global__ void k_to_device(const double* __restrict__ stage, T* __restrict__ X, const int* __restrict__ iperm,
-                            int n, int P, int ld) {
+                            const int* __restrict__ mode_of_col, int n, int P, int ld) {
     __shared__ double tile[32][33];
-    int i0 = blockIdx.x * 32, mu0 = blockIdx.y * 32;
+    int i0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
     int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
     for (int r = ty; r < 32; r += 8) {
-        int mu = mu0 + r, i = i0 + tx;
-        tile[r][tx] = (mu < P && i < n) ? stage[(size_t)mu * n + i] : 0.0;
+        int c = c0 + r, i = i0 + tx;
+        tile[r][tx] = (c < P && i < n) ? stage[(size_t)mode_of_col[c] * n + i] : 0.0;
     }
     __syncthreads();
     for (int r = ty; r < 32; r += 8) {
-        int i = i0 + r, mu = mu0 + tx;
-        if (i < n && mu < ld) X[(size_t)iperm[i] * ld + mu] = (T)tile[tx][r];
+        int i = i0 + r, c = c0 + tx;
+        if (i < n && c < ld) X[(size_t)iperm[i] * ld + c] = (T)tile[tx][r];
     }
 }
 
 template <typename T>
 __global__ void k_from_device(const T* __restrict__ X, double* __restrict__ stage, const int* __restrict__ iperm,
-                              int n, int P, int ld) {
+                              const int* __restrict__ mode_of_col, int n, int P, int ld) {
     __shared__ double tile[32][33];
-    int i0 = blockIdx.x * 32, mu0 = blockIdx.y * 32;
+    int i0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
     int tx = threadIdx.x, ty = threadIdx.y;
     for (int r = ty; r < 32; r += 8) {
-        int i = i0 + r, mu = mu0 + tx;
-        tile[r][tx] = (i < n && mu < P) ? (double)X[(size_t)iperm[i] * ld + mu] : 0.0;
+        int i = i0 + r, c = c0 + tx;
+        tile[r][tx] = (i < n && c < P) ? (double)X[(size_t)iperm[i] * ld + c] : 0.0;
     }
     __syncthreads();
     for (int r = ty; r < 32; r += 8) {
-        int mu = mu0 + r, i = i0 + tx;
-        if (mu < P && i < n) stage[(size_t)mu * n + i] = tile[tx][r];
+        int c = c0 + r, i = i0 + tx;
+        if (c < P && i < n) stage[(size_t)mode_of_col[c] * n + i] = tile[tx][r];
     }
 }
 
 int sg_launch_to_device(sgfem_context* ctx, const double* stage, void* X, int precision) {
     dim3 block(32, 8), grid((unsigned)((ctx->n + 31) / 32), (unsigned)((ctx->ld + 31) / 32));
     if (precision == SGFEM_FP64)
-        k_to_device<double><<<grid, block, 0, ctx->stream>>>(stage, (double*)X, ctx->d_iperm, (int)ctx->n, (int)ctx->P, (int)ctx->ld);
+        k_to_device<double><<<grid, block, 0, ctx->stream>>>(stage, (double*)X, ctx->d_iperm, ctx->d_mode_of_col, (int)ctx->n, (int)ctx->P, (int)ctx->ld);
     else
-        k_to_device<float><<<grid, block, 0, ctx->stream>>>(stage, (float*)X, ctx->d_iperm, (int)ctx->n, (int)ctx->P, (int)ctx->ld);
+        k_to_device<float><<<grid, block, 0, ctx->stream>>>(stage, (float*)X, ctx->d_iperm, ctx->d_mode_of_col, (int)ctx->n, (int)ctx->P, (int)ctx->ld);
     SG_LAUNCHED(ctx);
     return SGFEM_OK;
 }
@@ -452,9 +633,9 @@ int sg_launch_to_device(sgfem_context* ctx, const double* stage, void* X, int pr
 int sg_launch_from_device(sgfem_context* ctx, const void* X, double* stage, int precision) {
     dim3 block(32, 8), grid((unsigned)((ctx->n + 31) / 32), (unsigned)((ctx->P + 31) / 32));
     if (precision == SGFEM_FP64)
-        k_from_device<double><<<grid, block, 0, ctx->stream>>>((const double*)X, stage, ctx->d_iperm, (int)ctx->n, (int)ctx->P, (int)ctx->ld);
+        k_from_device<double><<<grid, block, 0, ctx->stream>>>((const double*)X, stage, ctx->d_iperm, ctx->d_mode_of_col, (int)ctx->n, (int)ctx->P, (int)ctx->ld);
     else
-        k_from_device<float><<<grid, block, 0, ctx->stream>>>((const float*)X, stage, ctx->d_iperm, (int)ctx->n, (int)ctx->P, (int)ctx->ld);
+        k_from_device<float><<<grid, block, 0, ctx->stream>>>((const float*)X, stage, ctx->d_iperm, ctx->d_mode_of_col, (int)ctx->n, (int)ctx->P, (int)ctx->ld);
     SG_LAUNCHED(ctx);
     return SGFEM_OK;
 }

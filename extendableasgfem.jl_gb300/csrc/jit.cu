@@ -1,0 +1,463 @@
+// Specialised FP32 SG apply, compiled at finalize time with NVRTC for the
+// coupling structure of the operator (the same operator as k_apply, see
+// apply.cu; mul!(Ax, S, x), src/modelproblems/solvers_poisson_primal.jl:86-124).
+//
+// Schedule (one warp per row):
+//   * lane L owns device columns c = 32 k + L (k < KG): for each nonzero (i, j)
+//     it loads X[j, c] once into a register and duplicates it into a float2;
+//   * the M+1 values of the nonzero are loaded once as float4 vectors with a
+//     warp-uniform address and read as pairs (K_2p, K_2p+1);
+//   * one packed FP32x2 FMA per slot (pair p, group k) accumulates
+//     (acc(2p, c), acc(2p+1, c)) += (K_2p[i,j], K_2p+1[i,j]) * X[j, c];
+//     slots exist only where group k holds a column coupled to pair p, and the
+//     device column order (sg_mode_order) packs those columns into few groups;
+//   * after the row: accumulators to shared memory, then
+//     Y[i, c] = sum_e g_e acc[off_e] over the per-column combination list
+//     (K_0 term with g = 1, then the G entries), Dirichlet rows zero,
+//     p'Ap partial in FP64.
+// The slot list is compile-time, so every accumulator, KLE value and X value
+// is a register and no instruction needs a lane-dependent shared-memory index.
+// NVRTC and the driver entry points are loaded at run time; when they are not
+// available the generic kernel (apply.cu) stays in use.
+#include <cuda.h>
+#include <dlfcn.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+
+#include "sgfem_internal.h"
+
+namespace {
+
+constexpr int JWPB = 4;  // warps per block
+
+struct Nvrtc {
+    bool loaded = false;
+    bool tried = false;
+    std::string err;
+    nvrtcResult (*create)(nvrtcProgram*, const char*, const char*, int, const char* const*, const char* const*) = nullptr;
+    nvrtcResult (*compile)(nvrtcProgram, int, const char* const*) = nullptr;
+    nvrtcResult (*log_size)(nvrtcProgram, size_t*) = nullptr;
+    nvrtcResult (*log)(nvrtcProgram, char*) = nullptr;
+    nvrtcResult (*cubin_size)(nvrtcProgram, size_t*) = nullptr;
+    nvrtcResult (*cubin)(nvrtcProgram, char*) = nullptr;
+    nvrtcResult (*destroy)(nvrtcProgram*) = nullptr;
+};
+
+struct Driver {
+    bool loaded = false;
+    bool tried = false;
+    std::string err;
+    CUresult (*module_load_data)(CUmodule*, const void*) = nullptr;
+    CUresult (*module_get_function)(CUfunction*, CUmodule, const char*) = nullptr;
+    CUresult (*module_unload)(CUmodule) = nullptr;
+    CUresult (*func_set_attribute)(CUfunction, CUfunction_attribute, int) = nullptr;
+    CUresult (*launch_kernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
+                              CUstream, void**, void**) = nullptr;
+    CUresult (*occupancy)(int*, CUfunction, int, size_t) = nullptr;
+};
+
+Nvrtc g_nvrtc;
+Driver g_drv;
+
+template <typename F>
+bool sym(void* h, const char* name, F& f) {
+    f = reinterpret_cast<F>(dlsym(h, name));
+    return f != nullptr;
+}
+
+bool load_nvrtc() {
+    if (g_nvrtc.tried) return g_nvrtc.loaded;
+    g_nvrtc.tried = true;
+    const char* names[] = {"libnvrtc.so.13", "/usr/local/cuda/lib64/libnvrtc.so.13", "libnvrtc.so",
+                           "/usr/local/cuda/lib64/libnvrtc.so"};
+    void* h = nullptr;
+    for (const char* nm : names)
+        if ((h = dlopen(nm, RTLD_NOW | RTLD_LOCAL))) break;
+    if (!h) {
+        g_nvrtc.err = "libnvrtc not found";
+        return false;
+    }
+    bool ok = sym(h, "nvrtcCreateProgram", g_nvrtc.create) && sym(h, "nvrtcCompileProgram", g_nvrtc.compile) &&
+              sym(h, "nvrtcGetProgramLogSize", g_nvrtc.log_size) && sym(h, "nvrtcGetProgramLog", g_nvrtc.log) &&
+              sym(h, "nvrtcGetCUBINSize", g_nvrtc.cubin_size) && sym(h, "nvrtcGetCUBIN", g_nvrtc.cubin) &&
+              sym(h, "nvrtcDestroyProgram", g_nvrtc.destroy);
+    if (!ok) g_nvrtc.err = "libnvrtc lacks an entry point";
+    g_nvrtc.loaded = ok;
+    return ok;
+}
+
+template <typename F>
+bool entry(const char* name, F& f) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !p)
+        return false;
+    f = reinterpret_cast<F>(p);
+    return true;
+}
+
+bool load_driver() {
+    if (g_drv.tried) return g_drv.loaded;
+    g_drv.tried = true;
+    bool ok = entry("cuModuleLoadData", g_drv.module_load_data) &&
+              entry("cuModuleGetFunction", g_drv.module_get_function) &&
+              entry("cuModuleUnload", g_drv.module_unload) && entry("cuFuncSetAttribute", g_drv.func_set_attribute) &&
+              entry("cuLaunchKernel", g_drv.launch_kernel) &&
+              entry("cuOccupancyMaxActiveBlocksPerMultiprocessor", g_drv.occupancy);
+    if (!ok) g_drv.err = "driver entry points unavailable";
+    g_drv.loaded = ok;
+    return ok;
+}
+
+std::string generate_source(const sgfem_context* ctx) {
+    const int LD = (int)ctx->ld, P = (int)ctx->P, M1P = ctx->M1P;
+    const int KG = (int)((P + 31) / 32);
+    const int NS = (int)ctx->jit_slots.size();
+    std::string s;
+    char buf[512];
+    snprintf(buf, sizeof(buf),
+             "#define LD %d\n#define P %d\n#define KG %d\n#define M1P %d\n#define NS %d\n#define WPB %d\n"
+             "#define RCHUNK %d\n#define PREFETCH %d\n#define T %d\n#define STAGE %d\n",
+             LD, P, KG, M1P, NS, JWPB, ctx->jit_rchunk, ctx->jit_prefetch, ctx->jit_T, ctx->jit_stage);
+    s += buf;
+    s += R"(
+#define NV4 (M1P / 4)                 /* float4 per nonzero */
+#if STAGE
+#define CBUF (32 * M1P)               /* floats per value buffer (32 nonzeros) */
+#else
+#define CBUF 0
+#endif
+#define WSMEM (NS * 64 + 2 * CBUF + ((LD + 3) & ~3))   /* floats per warp */
+struct Scal { double rho, pq, alpha, beta, rr, tol2; int done, status, iters, first; };
+
+__device__ __forceinline__ void pf_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
+// X rows of a row (columns lane-parallel in jl), prefetched into L1
+__device__ __forceinline__ void prefetch_x(const float* __restrict__ X, int jl, int cnt, int lane) {
+    const int total = cnt * KG;
+    for (int q0 = 0; q0 < total; q0 += 32) {
+        const int q = min(q0 + lane, total - 1);
+        const int t = q / KG, k = q - t * KG;
+        const int j = __shfl_sync(0xffffffffu, jl, t);
+        if (q0 + lane < total) pf_l1(X + (size_t)j * LD + 32 * k);
+    }
+}
+
+// values of up to 32 nonzeros starting at nz (cnt of them) -> registers (lane-parallel float4)
+#define LOAD_VALUES(pv, nz, cnt)                                                        \
+    _Pragma("unroll") for (int i_ = 0; i_ < NV4; ++i_) {                                \
+        const int q_ = lane + 32 * i_;                                                  \
+        pv[i_] = (q_ < (cnt) * NV4) ? __ldg(reinterpret_cast<const float4*>(vals + (size_t)(nz) * M1P) + q_) \
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);                  \
+    }
+#define STORE_VALUES(dst, pv)                                                           \
+    _Pragma("unroll") for (int i_ = 0; i_ < NV4; ++i_)                                  \
+        reinterpret_cast<float4*>(dst)[lane + 32 * i_] = pv[i_];
+
+extern "C" __global__ void __launch_bounds__(WPB * 32)
+sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const float* __restrict__ vals,
+             const float* __restrict__ X, float* __restrict__ Y, int n, const unsigned char* __restrict__ bmask,
+             const int2* __restrict__ jtab, double* __restrict__ partials, const Scal* __restrict__ scal) {
+    if (scal && scal->done) return;
+    extern __shared__ __align__(16) float smem[];
+    __shared__ double red[WPB];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int2* stab = reinterpret_cast<int2*>(smem);
+    float* wb = smem + 2 * T * 32 + warp * WSMEM;
+    float* sacc = wb;
+    float* cbuf = wb + NS * 64;
+    float* ybuf = cbuf + 2 * CBUF;
+    for (int i = threadIdx.x; i < T * 32; i += blockDim.x) stab[i] = __ldg(jtab + i);
+    __syncthreads();
+    double dot = 0.0;
+    // rows in bands: warp w takes RCHUNK consecutive rows of each band of
+    // nw * RCHUNK rows (X rows reused across consecutive rows and across warps)
+    const int nw = gridDim.x * WPB, w = blockIdx.x * WPB + warp;
+    const int stride = nw * RCHUNK;
+#define NEXT_ROW(r) ((((r) + 1) % RCHUNK) ? ((r) + 1) : ((r) + 1 - RCHUNK + stride))
+    int row = w * RCHUNK;
+    int jn1 = 0, cn1 = 0, b = 0;
+    float4 pv[NV4];
+    if (row < n) {
+        const int a = rowptr[row];
+        cn1 = min(32, rowptr[row + 1] - a);
+        jn1 = (lane < cn1) ? __ldg(col + a + lane) : 0;
+#if STAGE
+        LOAD_VALUES(pv, a, cn1);
+        STORE_VALUES(cbuf, pv);
+#endif
+        if (PREFETCH) prefetch_x(X, jn1, cn1, lane);
+        __syncwarp();
+    }
+    for (; row < n; row = NEXT_ROW(row)) {
+        const int jcur = jn1, ccur = cn1;
+        const int r1n = NEXT_ROW(row);
+        if (r1n < n) {  // next row: columns and values (first 32 nonzeros) into registers
+            const int a = __ldg(rowptr + r1n);
+            cn1 = min(32, __ldg(rowptr + r1n + 1) - a);
+            jn1 = (lane < cn1) ? __ldg(col + a + lane) : 0;
+#if STAGE
+            LOAD_VALUES(pv, a, cn1);
+#else
+            if (PREFETCH) {  // values of the row after next into L1
+                const int r2n = NEXT_ROW(r1n);
+                if (r2n < n) {
+                    const char* v0 = reinterpret_cast<const char*>(vals + (size_t)__ldg(rowptr + r2n) * M1P);
+                    const char* v1 = reinterpret_cast<const char*>(vals + (size_t)__ldg(rowptr + r2n + 1) * M1P);
+                    for (const char* q = v0 + lane * 128; q < v1; q += 32 * 128) pf_l1(q);
+                }
+            }
+#endif
+        }
+        float* yrow = Y + (size_t)row * LD;
+        if (bmask[row]) {
+            for (int c = lane; c < LD; c += 32) yrow[c] = 0.f;
+        } else {
+)";
+    for (int q = 0; q < NS; ++q) {
+        snprintf(buf, sizeof(buf), "            float2 a%d = make_float2(0.f, 0.f);\n", q);
+        s += buf;
+    }
+    s += R"(            const int nz0 = rowptr[row], nz1 = rowptr[row + 1];
+            if (PREFETCH && r1n < n) prefetch_x(X, jn1, cn1, lane);
+            const float* cb = cbuf + b * CBUF;
+            for (int base = nz0; base < nz1; base += 32) {
+                const int cnt = min(32, nz1 - base);
+                int jl = jcur;
+                if (base != nz0) {  // rows longer than 32 nonzeros: later chunks load synchronously
+                    jl = (lane < cnt) ? __ldg(col + base + lane) : 0;
+#if STAGE
+                    float4 lv[NV4];
+                    __syncwarp();
+                    LOAD_VALUES(lv, base, cnt);
+                    STORE_VALUES(cbuf + b * CBUF, lv);
+                    __syncwarp();
+#endif
+                }
+#pragma unroll 2
+                for (int t = 0; t < cnt; ++t) {
+                const int j = __shfl_sync(0xffffffffu, jl, t);
+#if STAGE
+                const float4* cv = reinterpret_cast<const float4*>(cb + t * M1P);
+#else
+                const float4* cv = reinterpret_cast<const float4*>(vals + (size_t)(base + t) * M1P);
+#endif
+                const float* xr = X + (size_t)j * LD + lane;
+)";
+    for (int v = 0; v < M1P / 4; ++v) {
+        snprintf(buf, sizeof(buf), "                const float4 c%d = STAGE ? cv[%d] : __ldg(cv + %d);\n", v, v, v);
+        s += buf;
+    }
+    for (int k = 0; k < KG; ++k) {
+        const int valid = LD - 32 * k;
+        if (valid >= 32)
+            snprintf(buf, sizeof(buf), "                const float u%d = __ldg(xr + %d);\n", k, 32 * k);
+        else
+            snprintf(buf, sizeof(buf), "                const float u%d = (lane < %d) ? __ldg(xr + %d) : 0.f;\n",
+                     k, valid, 32 * k);
+        s += buf;
+        snprintf(buf, sizeof(buf), "                const float2 w%d = make_float2(u%d, u%d);\n", k, k, k);
+        s += buf;
+    }
+    for (int q = 0; q < NS; ++q) {
+        const int pr = ctx->jit_slots[q].first, k = ctx->jit_slots[q].second;
+        const int v = pr / 2;
+        const char* comp = (pr % 2 == 0) ? "x, c%d.y" : "z, c%d.w";
+        char cpair[64];
+        snprintf(cpair, sizeof(cpair), comp, v);
+        snprintf(buf, sizeof(buf), "                a%d = __ffma2_rn(make_float2(c%d.%s), w%d, a%d);\n", q, v, cpair,
+                 k, q);
+        s += buf;
+    }
+    s += "                }\n            }\n";
+    for (int q = 0; q < NS; ++q) {
+        snprintf(buf, sizeof(buf), "            *reinterpret_cast<float2*>(sacc + %d + 2 * lane) = a%d;\n", q * 64, q);
+        s += buf;
+    }
+    s += R"(            __syncwarp();
+            // combination: lane schedule, T entries per lane, store Y[c] at each column's last entry
+            float acc = 0.f;
+#pragma unroll
+            for (int i = 0; i < T; ++i) {
+                const int2 e = stab[i * 32 + lane];
+                acc = fmaf(__int_as_float(e.y), sacc[e.x & 0x1fff], acc);
+                if (e.x >> 28) {
+                    ybuf[(e.x >> 13) & 0x7fff] = acc;
+                    acc = 0.f;
+                }
+            }
+            __syncwarp();
+            const float* xrow = X + (size_t)row * LD;
+            for (int c = lane; c < LD; c += 32) {
+                const float y = (c < P) ? ybuf[c] : 0.f;
+                yrow[c] = y;
+                if (partials) dot += (double)xrow[c] * (double)y;
+            }
+        }
+#if STAGE
+        if (r1n < n) {  // stage the next row's values
+            __syncwarp();
+            b ^= 1;
+            STORE_VALUES(cbuf + b * CBUF, pv);
+            __syncwarp();
+        }
+#endif
+    }
+    if (partials) {
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
+        if (lane == 0) red[warp] = dot;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t2 = 0.0;
+            for (int w2 = 0; w2 < WPB; ++w2) t2 += red[w2];
+            partials[blockIdx.x] = t2;
+        }
+    }
+}
+)";
+    return s;
+}
+
+size_t jit_smem_bytes(const sgfem_context* ctx) {
+    const int NS = (int)ctx->jit_slots.size();
+    const size_t wsmem = (size_t)NS * 64 + (ctx->jit_stage ? 2 * 32 * ctx->M1P : 0) + ((ctx->ld + 3) & ~3);
+    return (2 * (size_t)ctx->jit_T * 32 + JWPB * wsmem) * sizeof(float);
+}
+
+}  // namespace
+
+int sg_jit_build(sgfem_context* ctx) {
+    ctx->jit_ok = false;
+    const char* env = getenv("SGFEM_APPLY");
+    if (env && std::string(env) == "generic") {
+        ctx->jit_log = "disabled by SGFEM_APPLY=generic";
+        return SGFEM_ERR_UNSUPPORTED;
+    }
+    const char* er = getenv("SGFEM_JIT_RCHUNK");
+    const char* ep = getenv("SGFEM_JIT_PREFETCH");
+    ctx->jit_rchunk = er ? std::max(1, atoi(er)) : 2;
+    ctx->jit_prefetch = ep ? (atoi(ep) != 0) : 0;
+    const char* es = getenv("SGFEM_JIT_STAGE");
+    const char* eb = getenv("SGFEM_JIT_BPS");
+    const char* ec = getenv("SGFEM_JIT_CARVEOUT");
+    ctx->jit_stage = es ? (atoi(es) != 0) : 1;
+    ctx->jit_bps_cap = eb ? std::max(1, atoi(eb)) : 8;
+    ctx->jit_carveout = ec ? atoi(ec) : -1;
+    const int NS = (int)ctx->jit_slots.size();
+    if (NS == 0 || NS > 96 || ctx->M1P > 64 || ctx->jit_T <= 0 || ctx->jit_T > 256) {
+        ctx->jit_log = "slot count outside the specialised kernel's range";
+        return SGFEM_ERR_UNSUPPORTED;
+    }
+    if (!load_nvrtc()) {
+        ctx->jit_log = g_nvrtc.err;
+        return SGFEM_ERR_UNSUPPORTED;
+    }
+    if (!load_driver()) {
+        ctx->jit_log = g_drv.err;
+        return SGFEM_ERR_UNSUPPORTED;
+    }
+    const std::string src = generate_source(ctx);
+    nvrtcProgram prog = nullptr;
+    if (g_nvrtc.create(&prog, src.c_str(), "sgfem_apply_jit.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) {
+        ctx->jit_log = "nvrtcCreateProgram failed";
+        return SGFEM_ERR_UNSUPPORTED;
+    }
+    const char* opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-default-device", "-lineinfo"};
+    nvrtcResult rc = g_nvrtc.compile(prog, 4, opts);
+    size_t ls = 0;
+    g_nvrtc.log_size(prog, &ls);
+    std::string log(ls, '\0');
+    if (ls) g_nvrtc.log(prog, &log[0]);
+    if (rc != NVRTC_SUCCESS) {
+        ctx->jit_log = "NVRTC compile failed: " + log;
+        g_nvrtc.destroy(&prog);
+        return SGFEM_ERR_UNSUPPORTED;
+    }
+    size_t cs = 0;
+    g_nvrtc.cubin_size(prog, &cs);
+    std::vector<char> cubin(cs);
+    g_nvrtc.cubin(prog, cubin.data());
+    g_nvrtc.destroy(&prog);
+    CUmodule mod = nullptr;
+    CUfunction fn = nullptr;
+    if (g_drv.module_load_data(&mod, cubin.data()) != CUDA_SUCCESS) {
+        ctx->jit_log = "cuModuleLoadData failed";
+        return SGFEM_ERR_UNSUPPORTED;
+    }
+    if (g_drv.module_get_function(&fn, mod, "sg_apply_jit") != CUDA_SUCCESS) {
+        g_drv.module_unload(mod);
+        ctx->jit_log = "cuModuleGetFunction failed";
+        return SGFEM_ERR_UNSUPPORTED;
+    }
+    const int smem = (int)jit_smem_bytes(ctx);
+    if (smem > 220 * 1024) {
+        g_drv.module_unload(mod);
+        ctx->jit_log = "specialised apply needs too much shared memory";
+        return SGFEM_ERR_UNSUPPORTED;
+    }
+    if (smem > 48 * 1024 &&
+        g_drv.func_set_attribute(fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, smem) != CUDA_SUCCESS) {
+        g_drv.module_unload(mod);
+        ctx->jit_log = "cuFuncSetAttribute failed";
+        return SGFEM_ERR_UNSUPPORTED;
+    }
+    if (ctx->jit_carveout >= 0)
+        g_drv.func_set_attribute(fn, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, ctx->jit_carveout);
+    int bps = 0;
+    if (g_drv.occupancy(&bps, fn, JWPB * 32, (size_t)smem) != CUDA_SUCCESS || bps < 1) {
+        g_drv.module_unload(mod);
+        ctx->jit_log = "occupancy query failed";
+        return SGFEM_ERR_UNSUPPORTED;
+    }
+    ctx->jit_blocks_per_sm = std::min(bps, ctx->jit_bps_cap);
+    ctx->jit_module = mod;
+    ctx->jit_func = fn;
+    ctx->jit_ok = true;
+    ctx->jit_log = "specialised FP32 apply: " + std::to_string(NS) + " slots, " + std::to_string(bps) +
+                   " blocks/SM, rows/chunk " + std::to_string(ctx->jit_rchunk) + ", prefetch " +
+                   std::to_string(ctx->jit_prefetch) + ", staged values " + std::to_string(ctx->jit_stage);
+    return SGFEM_OK;
+}
+
+int sg_jit_grid(const sgfem_context* ctx) {
+    // persistent: one wave of resident blocks, each warp a contiguous row range
+    const int64_t want = (ctx->n + JWPB - 1) / JWPB;
+    const int64_t resident = (int64_t)ctx->num_sms * std::min(ctx->jit_blocks_per_sm, 8);
+    return (int)std::max<int64_t>(1, std::min<int64_t>(want, resident));
+}
+
+int sg_jit_launch(sgfem_context* ctx, const void* X, void* Y, double* partials, int grid, const KrylovScalars* scal) {
+    const unsigned smem = (unsigned)jit_smem_bytes(ctx);
+    const int* rowptr = ctx->d_rowptr;
+    const int* colp = ctx->d_col;
+    const float* vals = ctx->d_val32p;
+    int n = (int)ctx->n;
+    const unsigned char* bm = ctx->d_bmask;
+    const int2* jtab = ctx->d_jtab;
+    void* args[] = {(void*)&rowptr, (void*)&colp, (void*)&vals, (void*)&X, (void*)&Y, (void*)&n, (void*)&bm,
+                    (void*)&jtab, (void*)&partials, (void*)&scal};
+    CUresult r = g_drv.launch_kernel((CUfunction)ctx->jit_func, grid, 1, 1, JWPB * 32, 1, 1, smem,
+                                     (CUstream)ctx->stream, args, nullptr);
+    if (r != CUDA_SUCCESS) return sg_fail(ctx, SGFEM_ERR_CUDA, "cuLaunchKernel(sg_apply_jit) failed: " + std::to_string((int)r));
+    ctx->launches++;
+    return SGFEM_OK;
+}
+
+void sg_jit_release(sgfem_context* ctx) {
+    if (ctx->jit_module && g_drv.loaded) g_drv.module_unload((CUmodule)ctx->jit_module);
+    ctx->jit_module = nullptr;
+    ctx->jit_func = nullptr;
+    ctx->jit_ok = false;
+}
+
+extern "C" int sgfem_apply_variant(const sgfem_context* ctx) { return (ctx && ctx->jit_ok) ? 1 : 0; }
+
+extern "C" const char* sgfem_apply_variant_log(const sgfem_context* ctx) {
+    return ctx ? ctx->jit_log.c_str() : "null context";
+}

@@ -416,7 +416,21 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
 
     int status = SGFEM_OK;
     double rr = 0.0;
-    SG_TRY(true_residual(&rr));
+    {
+        // initial residual: with a zero warm start r = b and no FP64 apply is needed
+        k_dot<double><<<g, VT, 0, ctx->stream>>>(x64, x64, total, partials);
+        SG_LAUNCHED(ctx);
+        SG_TRY(S.fin(g, FIN_SUM, FinArgs{0.0, 0}, d_sum));
+        double xx = 0.0;
+        SG_CUDA(ctx, cudaMemcpyAsync(&xx, d_sum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (xx == 0.0) {
+            SG_CUDA(ctx, cudaMemcpyAsync(r, b, n64, cudaMemcpyDeviceToDevice, ctx->stream));
+            rr = bb;
+        } else {
+            SG_TRY(true_residual(&rr));
+        }
+    }
     int remaining = o->maxit;
     if (!low) {
         // FP64 PCG; restart from the true residual if the recurrence drifted

@@ -94,6 +94,32 @@ struct sgfem_context {
     float* d_combg32 = nullptr;
     int ncomb = 0;
 
+    // device column order of the modes
+    std::vector<int32_t> mode_of_col;  // device column -> caller mode
+    std::vector<int32_t> imode;        // caller mode -> device column
+    int* d_mode_of_col = nullptr;
+
+    // specialised FP32 apply (NVRTC): slots (KLE pair, 32-column group)
+    int M1P = 0;                            // value stride of d_val32p (M+1 rounded up to 4)
+    float* d_val32p = nullptr;              // [nnz][M1P]
+    std::vector<int> jit_slot_of;           // [pair * KG + group] -> slot or -1
+    std::vector<std::pair<int, int>> jit_slots;  // (pair, group)
+    int* d_jptr = nullptr;                  // P + 1
+    int* d_joff = nullptr;                  // accumulator offsets
+    float* d_jg = nullptr;                  // coefficients
+    int2* d_jtab = nullptr;                 // lane schedule of the combination, [T][32]
+    int jit_T = 0;                          // entries per lane in d_jtab (-1: does not fit)
+    int jit_rchunk = 8;                     // rows per warp chunk
+    int jit_prefetch = 0;
+    int jit_stage = 1;                      // KLE values staged in shared memory
+    int jit_bps_cap = 8;                    // resident blocks per SM used by the grid
+    int jit_carveout = -1;                  // preferred shared-memory carve-out (%), -1 default
+    void* jit_module = nullptr;             // CUmodule
+    void* jit_func = nullptr;               // CUfunction
+    bool jit_ok = false;
+    int jit_blocks_per_sm = 1;
+    std::string jit_log;
+
     // lattice preconditioner
     bool lattice = false;
     int Nl = 0;                 // lattice intervals per side; points (Nl+1)^2
@@ -147,6 +173,16 @@ int sg_check_ready(sgfem_context* ctx);
 // partial sum of X .* Y to dot_partials[block]; *nblocks receives the block count.
 int sg_launch_apply(sgfem_context* ctx, int precision, const void* X, void* Y,
                     double* dot_partials, int* nblocks, const KrylovScalars* skip_if_done);
+
+// ------------------------------------------------------------------ specialised apply (jit.cu)
+void sg_mode_order(const sgfem_context* ctx, const std::vector<std::vector<char>>& nzcol,
+                   std::vector<int32_t>& mode_of_col);
+// compile the FP32 apply for this coupling structure; returns SGFEM_OK or an error
+// (the generic kernel stays in use then)
+int sg_jit_build(sgfem_context* ctx);
+int sg_jit_grid(const sgfem_context* ctx);
+int sg_jit_launch(sgfem_context* ctx, const void* X, void* Y, double* partials, int grid, const KrylovScalars* scal);
+void sg_jit_release(sgfem_context* ctx);
 
 // ------------------------------------------------------------------ layout (context.cu)
 int sg_launch_to_device(sgfem_context* ctx, const double* stage, void* X, int precision);

@@ -159,6 +159,11 @@ SGFEM_API int sgfem_time_apply(sgfem_context* ctx, int precision, int reps, doub
 #define SGFEM_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
 SGFEM_API int sgfem_precondition_device_static(sgfem_context* ctx, const void* r_dev, void* z_dev, int precision);
 
+/* which FP32 apply kernel a finalized context uses: 1 = specialised to the coupling
+   structure (compiled with NVRTC at finalize), 0 = generic; the log says why */
+SGFEM_API int sgfem_apply_variant(const sgfem_context* ctx);
+SGFEM_API const char* sgfem_apply_variant_log(const sgfem_context* ctx);
+
 /* kernels launched by this context so far (graph replays included) */
 SGFEM_API long long sgfem_kernel_launches(const sgfem_context* ctx);
 

@@ -145,3 +145,28 @@ def test_apply_non_lattice_numbering(built_pkg):
     yref = osg.mul_literal(x, p.K0, p.Ks, p.G, p.bdofs, p.P).reshape(p.P, p.n)[:, perm].ravel()
     assert rel(y, yref) <= 1e-12
     ctx.close()
+
+
+def test_specialised_fp32_apply_active_and_matches_generic(built_pkg, monkeypatch):
+    """The FP32 apply compiled for the coupling structure (NVRTC) is the one in
+    use, and it agrees with the generic kernel and with FP64."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    for p in (config1_like(), build(16, 2, 8, pkg.top_weight_multiindices(8, 60, C.decay_factors))):
+        op = pkg.SGOperator(p.V, p.TB, p.Kall, device=0)
+        variant, log = op.ctx.apply_variant
+        assert variant == 1, log
+        monkeypatch.setenv("SGFEM_APPLY", "generic")
+        opg = pkg.SGOperator(p.V, p.TB, p.Kall, device=0)
+        monkeypatch.delenv("SGFEM_APPLY")
+        assert opg.ctx.apply_variant[0] == 0
+        x = np.random.default_rng(9).standard_normal(p.n * p.P)
+        y64 = op.mul(x, pkg.FP64)
+        ys = op.mul(x, pkg.FP32)
+        yg = opg.mul(x, pkg.FP32)
+        assert rel(ys, y64) <= 1e-5 and rel(yg, y64) <= 1e-5
+        assert rel(ys, yg) <= 1e-5
+        op.close()
+        opg.close()
+
