@@ -309,6 +309,7 @@ def run_ours(args, rank, world, local, pg):
                      "achieved": ach, "peak": peak_gbs, "unit": "GB/s", "frac": ach / peak_gbs,
                      "traffic": traffic, "algorithmic_bytes": B32, "ms_per_launch": t32,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs" if pk else "fallback 6.8 TB/s"},
+        "precondition_ms": {"fp32": ctx.time_precondition(pkg.FP32, 10), "fp64": ctx.time_precondition(pkg.FP64, 5)},
         "apply_fp64": {"ms_per_launch": t64, "GB/s": B64 / (t64 * 1e-3) / 1e9,
                        "GFLOP/s": algorithmic_flops(n, P, nnz, ctx_qn(op), TB.G.nnz) / (t64 * 1e-3) / 1e9},
         "clocks": clk,

@@ -71,6 +71,7 @@ SIGNATURES = {
     "sgfem_solve_device": (ctypes.c_int, [_P, _DP, _P, ctypes.POINTER(SolveOptions), ctypes.POINTER(SolveStats)]),
     "sgfem_time_apply": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _DP]),
     "sgfem_kernel_launches": (ctypes.c_longlong, [_P]),
+    "sgfem_time_precondition": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _DP]),
     "sgfem_precondition_device_static": (ctypes.c_int, [_P, _P, _P, ctypes.c_int]),
     "sgfem_apply_variant": (ctypes.c_int, [_P]),
     "sgfem_apply_variant_log": (ctypes.c_char_p, [_P]),
@@ -249,6 +250,11 @@ class Context:
 
     def kernel_launches(self):
         return int(self.lib.sgfem_kernel_launches(self.h))
+
+    def time_precondition(self, precision=FP64, reps=10):
+        ms = ctypes.c_double()
+        self._check(self.lib.sgfem_time_precondition(self.h, int(precision), int(reps), ctypes.byref(ms)))
+        return ms.value
 
     def time_apply(self, precision=FP64, reps=10):
         ms = ctypes.c_double()

@@ -330,6 +330,31 @@ extern "C" int sgfem_precondition(sgfem_context* ctx, const double* b, double* y
     return sgfem_from_device_layout(ctx, ctx->w_vec[1].p, y, precision);
 }
 
+extern "C" int sgfem_time_precondition(sgfem_context* ctx, int precision, int reps, double* ms_per_application) {
+    SG_TRY(sg_check_ready(ctx));
+    if (reps <= 0 || !ms_per_application) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad reps");
+    if (precision != SGFEM_FP64 && precision != SGFEM_FP32) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad precision");
+    if (!ctx->lattice) return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice preconditioner unavailable");
+    SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t vb = sg_vec_bytes(ctx, precision);
+    for (int i = 0; i < 3; ++i) SG_TRY(sg_ensure(ctx, ctx->w_vec[i], vb));
+    SG_CUDA(ctx, cudaMemsetAsync(ctx->w_vec[0].p, 0, vb, ctx->stream));
+    auto once = [&]() -> int {
+        SG_TRY(sg_lat_pass_x(ctx, precision, ctx->w_vec[0].p, ctx->w_vec[2].p, nullptr));
+        SG_TRY(sg_lat_pass_y(ctx, precision, ctx->w_vec[2].p, nullptr, nullptr, nullptr));
+        return sg_lat_pass_xinv(ctx, precision, ctx->w_vec[2].p, ctx->w_vec[1].p, 0, nullptr);
+    };
+    SG_TRY(once());
+    SG_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    for (int r = 0; r < reps; ++r) SG_TRY(once());
+    SG_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    SG_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+    float ms = 0.f;
+    SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    *ms_per_application = ms / reps;
+    return SGFEM_OK;
+}
+
 // core solve on device buffers: x64 (in/out, device layout), b0 host (caller order)
 static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const sgfem_solve_options* o,
                       sgfem_solve_stats* st) {

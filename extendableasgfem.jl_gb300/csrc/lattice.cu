@@ -46,10 +46,70 @@ struct LatGeom {
 //   [0, Nl/2)          cos(2 pi k / Nl)
 //   [Nl/2, Nl)         sin(2 pi k / Nl)
 //   [Nl, 3Nl/2 + 1)    sin(pi j / Nl), j = 0..Nl/2
-template <typename T>
-__device__ void dst_line(T* tile, const T* tab, int Nl, int lg) {
+// Radix-2 DIF FFT of the L = 2^LGL complex slots of every line of the tile,
+// sign +.  Stages are done in chunks of up to 4 bits: each thread loads the
+// 16 points of one group (indices differing only in the chunk's bits) into
+// registers, runs the chunk's stages there and writes back, so a 256-point
+// transform takes two shared-memory round trips instead of eight.
+template <typename T, int LGL>
+__device__ __forceinline__ void fft_dif(T* tile, const T* cs, const T* sn, int lane, int warp) {
+    constexpr int L = 1 << LGL;
+    constexpr int RB = LGL < 4 ? LGL : 4;
+#pragma unroll
+    for (int hi = LGL - 1; hi >= 0; hi -= RB) {
+        const int lo = hi - RB + 1 > 0 ? hi - RB + 1 : 0;
+        const int nb = hi - lo + 1;
+        const int G = 1 << nb;
+        const int ngroups = L >> nb;
+        for (int g = warp; g < ngroups; g += LAT_WARPS) {
+            const int base = ((g >> lo) << (hi + 1)) | (g & ((1 << lo) - 1));
+            T re[1 << RB], im[1 << RB];
+#pragma unroll
+            for (int k = 0; k < (1 << RB); ++k)
+                if (k < G) {
+                    const int idx = base | (k << lo);
+                    re[k] = tile[(2 * idx) * 32 + lane];
+                    im[k] = tile[(2 * idx + 1) * 32 + lane];
+                }
+#pragma unroll
+            for (int bb = RB - 1; bb >= 0; --bb) {
+                if (bb >= nb) continue;
+                const int b = lo + bb;
+                const int hs = 1 << bb;
+                const int h = 1 << b;
+                const int tstep = (2 * L) >> (b + 1);  // Nl / (2h)
+#pragma unroll
+                for (int k = 0; k < (1 << RB); ++k)
+                    if (k < G && !(k & hs)) {
+                        const int k2 = k | hs;
+                        const int t = (base | (k << lo)) & (h - 1);
+                        const T ar = re[k], ai = im[k], cr = re[k2], ci = im[k2];
+                        re[k] = ar + cr;
+                        im[k] = ai + ci;
+                        const T dr = ar - cr, di = ai - ci;
+                        const T wr = cs[t * tstep], wi = sn[t * tstep];
+                        re[k2] = dr * wr - di * wi;
+                        im[k2] = dr * wi + di * wr;
+                    }
+            }
+#pragma unroll
+            for (int k = 0; k < (1 << RB); ++k)
+                if (k < G) {
+                    const int idx = base | (k << lo);
+                    tile[(2 * idx) * 32 + lane] = re[k];
+                    tile[(2 * idx + 1) * 32 + lane] = im[k];
+                }
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T, int LGL>
+__device__ void dst_line(T* tile, const T* tab) {
+    constexpr int Nl = 2 << LGL;
+    constexpr int lg = LGL + 1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int L = Nl >> 1;
+    constexpr int L = Nl >> 1;
     const T* cs = tab;
     const T* sn = tab + L;
     const T* sh = tab + Nl;
@@ -65,25 +125,7 @@ __device__ void dst_line(T* tile, const T* tab, int Nl, int lg) {
     if (warp == 0) tile[lane] = T(0);
     __syncthreads();
     // complex FFT (sign +) of z_k = (y_2k, y_2k+1), k < L, decimation in frequency
-    for (int s = lg - 2; s >= 0; --s) {
-        const int h = 1 << s;       // half span
-        const int tstep = Nl >> (s + 1);  // twiddle index step: n / (2h)
-        for (int b = warp; b < (L >> 1); b += LAT_WARPS) {
-            const int g = b >> s, t = b & (h - 1);
-            const int i1 = 2 * g * h + t, i2 = i1 + h;
-            T* z1 = tile + 2 * i1 * 32 + lane;
-            T* z2 = tile + 2 * i2 * 32 + lane;
-            const T ar = z1[0], ai = z1[32], cr = z2[0], ci = z2[32];
-            const T dr = ar - cr, di = ai - ci;
-            z1[0] = ar + cr;
-            z1[32] = ai + ci;
-            const int ti = t * tstep;
-            const T wr = cs[ti], wi = sn[ti];
-            z2[0] = dr * wr - di * wi;
-            z2[32] = dr * wi + di * wr;
-        }
-        __syncthreads();
-    }
+    fft_dif<T, LGL>(tile, cs, sn, lane, warp);
     // bit reversal of the L complex slots
     for (int k = warp; k < L; k += LAT_WARPS) {
         const int r = (int)(__brev((unsigned)k) >> (32 - (lg - 1)));
@@ -162,7 +204,7 @@ __device__ void load_line(T* tile, const T* __restrict__ in, int dir, int line, 
 }
 
 // pass X (dir 0) / pass X^-1 (dir 0, store variants)
-template <typename T>
+template <typename T, int LGL>
 __global__ void __launch_bounds__(LAT_THREADS)
 k_lat_pass_x(const T* __restrict__ in, T* __restrict__ out, const T* __restrict__ tab, LatGeom g, int mode,
              const KrylovScalars* __restrict__ scal) {
@@ -174,7 +216,7 @@ k_lat_pass_x(const T* __restrict__ in, T* __restrict__ out, const T* __restrict_
     load_tab(stab, tab, g.Nl);
     load_line(tile, in, 0, line, chunk, g);
     __syncthreads();
-    dst_line(tile, stab, g.Nl, g.lg);
+    dst_line<T, LGL>(tile, stab);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int m = chunk * 32 + lane;
     if (m >= g.ld) return;
@@ -190,7 +232,7 @@ k_lat_pass_x(const T* __restrict__ in, T* __restrict__ out, const T* __restrict_
     }
 }
 
-template <typename T>
+template <typename T, int LGL>
 __global__ void __launch_bounds__(LAT_THREADS)
 k_lat_pass_y(T* __restrict__ buf, const T* __restrict__ tab, const T* __restrict__ scale, LatGeom g,
              double* __restrict__ rz, const KrylovScalars* __restrict__ scal) {
@@ -203,7 +245,7 @@ k_lat_pass_y(T* __restrict__ buf, const T* __restrict__ tab, const T* __restrict
     load_tab(stab, tab, g.Nl);
     load_line(tile, buf, 1, line, chunk, g);
     __syncthreads();
-    dst_line(tile, stab, g.Nl, g.lg);
+    dst_line<T, LGL>(tile, stab);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int N = g.Nl - 1;
     double acc = 0.0;
@@ -214,7 +256,7 @@ k_lat_pass_y(T* __restrict__ buf, const T* __restrict__ tab, const T* __restrict
         tile[p * 32 + lane] = v * sc;
     }
     __syncthreads();
-    dst_line(tile, stab, g.Nl, g.lg);
+    dst_line<T, LGL>(tile, stab);
     const int m = chunk * 32 + lane;
     if (m < g.ld) {
         for (int p = 1 + warp; p < g.Nl; p += LAT_WARPS)
@@ -291,8 +333,8 @@ __global__ void k_jacobi(const T* __restrict__ R, T* __restrict__ out, const T* 
 
 int sg_lattice_setup(sgfem_context* ctx) {
     const int Nl = ctx->Nl;
-    if (Nl < 4 || (Nl & (Nl - 1)) != 0)
-        return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice preconditioner needs a power-of-two lattice");
+    if (Nl < 4 || Nl > 512 || (Nl & (Nl - 1)) != 0)
+        return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice preconditioner needs a power-of-two lattice of 4..512 intervals");
     int lg = 0;
     while ((1 << lg) < Nl) ++lg;
     ctx->lat_log2 = lg;
@@ -336,55 +378,92 @@ int sg_lattice_setup(sgfem_context* ctx) {
     return SGFEM_OK;
 }
 
+namespace {
+
+template <typename T>
+using PassXFn = void (*)(const T*, T*, const T*, LatGeom, int, const KrylovScalars*);
+template <typename T>
+using PassYFn = void (*)(T*, const T*, const T*, LatGeom, double*, const KrylovScalars*);
+
+// instantiations for L = Nl/2 = 2^LGL complex points, Nl = 4 .. 512
+template <typename T>
+PassXFn<T> pass_x_fn(int LGL) {
+    switch (LGL) {
+        case 1: return k_lat_pass_x<T, 1>;
+        case 2: return k_lat_pass_x<T, 2>;
+        case 3: return k_lat_pass_x<T, 3>;
+        case 4: return k_lat_pass_x<T, 4>;
+        case 5: return k_lat_pass_x<T, 5>;
+        case 6: return k_lat_pass_x<T, 6>;
+        case 7: return k_lat_pass_x<T, 7>;
+        case 8: return k_lat_pass_x<T, 8>;
+    }
+    return nullptr;
+}
+template <typename T>
+PassYFn<T> pass_y_fn(int LGL) {
+    switch (LGL) {
+        case 1: return k_lat_pass_y<T, 1>;
+        case 2: return k_lat_pass_y<T, 2>;
+        case 3: return k_lat_pass_y<T, 3>;
+        case 4: return k_lat_pass_y<T, 4>;
+        case 5: return k_lat_pass_y<T, 5>;
+        case 6: return k_lat_pass_y<T, 6>;
+        case 7: return k_lat_pass_y<T, 7>;
+        case 8: return k_lat_pass_y<T, 8>;
+    }
+    return nullptr;
+}
+
+template <typename T>
+int launch_x(sgfem_context* ctx, const void* in, void* out, const T* tab, int mode, const KrylovScalars* scal) {
+    LatGeom g = geom(ctx);
+    PassXFn<T> fn = pass_x_fn<T>(ctx->lat_log2 - 1);
+    if (!fn) return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice size outside the compiled range");
+    const int grid = (g.Nl - 1) * g.nchunk;
+    fn<<<grid, LAT_THREADS, lat_smem(ctx, sizeof(T)), ctx->stream>>>((const T*)in, (T*)out, tab, g, mode, scal);
+    SG_LAUNCHED(ctx);
+    return SGFEM_OK;
+}
+
+template <typename T>
+int launch_y(sgfem_context* ctx, void* buf, const T* tab, const T* scale, double* rz, int* nblocks,
+             const KrylovScalars* scal) {
+    LatGeom g = geom(ctx);
+    PassYFn<T> fn = pass_y_fn<T>(ctx->lat_log2 - 1);
+    if (!fn) return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice size outside the compiled range");
+    const int grid = (g.Nl - 1) * g.nchunk;
+    if (nblocks) *nblocks = grid;
+    fn<<<grid, LAT_THREADS, lat_smem(ctx, sizeof(T)), ctx->stream>>>((T*)buf, tab, scale, g, rz, scal);
+    SG_LAUNCHED(ctx);
+    return SGFEM_OK;
+}
+
+}  // namespace
+
 int sg_lattice_configure(sgfem_context* ctx) {
-    SG_TRY(set_smem(ctx, k_lat_pass_x<double>, lat_smem(ctx, 8)));
-    SG_TRY(set_smem(ctx, k_lat_pass_y<double>, lat_smem(ctx, 8)));
-    SG_TRY(set_smem(ctx, k_lat_pass_x<float>, lat_smem(ctx, 4)));
-    SG_TRY(set_smem(ctx, k_lat_pass_y<float>, lat_smem(ctx, 4)));
+    const int LGL = ctx->lat_log2 - 1;
+    if (!pass_x_fn<double>(LGL)) return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice size outside the compiled range");
+    SG_TRY(set_smem(ctx, pass_x_fn<double>(LGL), lat_smem(ctx, 8)));
+    SG_TRY(set_smem(ctx, pass_y_fn<double>(LGL), lat_smem(ctx, 8)));
+    SG_TRY(set_smem(ctx, pass_x_fn<float>(LGL), lat_smem(ctx, 4)));
+    SG_TRY(set_smem(ctx, pass_y_fn<float>(LGL), lat_smem(ctx, 4)));
     return SGFEM_OK;
 }
 
 int sg_lat_pass_x(sgfem_context* ctx, int precision, const void* R, void* T, const KrylovScalars* scal) {
-    LatGeom g = geom(ctx);
-    const int grid = (g.Nl - 1) * g.nchunk;
-    if (precision == SGFEM_FP64) {
-        size_t smem = lat_smem(ctx, 8);
-        k_lat_pass_x<double><<<grid, LAT_THREADS, smem, ctx->stream>>>((const double*)R, (double*)T, ctx->d_lat_tab64, g, 0, scal);
-    } else {
-        size_t smem = lat_smem(ctx, 4);
-        k_lat_pass_x<float><<<grid, LAT_THREADS, smem, ctx->stream>>>((const float*)R, (float*)T, ctx->d_lat_tab32, g, 0, scal);
-    }
-    SG_LAUNCHED(ctx);
-    return SGFEM_OK;
+    if (precision == SGFEM_FP64) return launch_x<double>(ctx, R, T, ctx->d_lat_tab64, 0, scal);
+    return launch_x<float>(ctx, R, T, ctx->d_lat_tab32, 0, scal);
 }
 
 int sg_lat_pass_y(sgfem_context* ctx, int precision, void* T, double* rz, int* nblocks, const KrylovScalars* scal) {
-    LatGeom g = geom(ctx);
-    const int grid = (g.Nl - 1) * g.nchunk;
-    if (nblocks) *nblocks = grid;
-    if (precision == SGFEM_FP64) {
-        size_t smem = lat_smem(ctx, 8);
-        k_lat_pass_y<double><<<grid, LAT_THREADS, smem, ctx->stream>>>((double*)T, ctx->d_lat_tab64, ctx->d_lat_scale64, g, rz, scal);
-    } else {
-        size_t smem = lat_smem(ctx, 4);
-        k_lat_pass_y<float><<<grid, LAT_THREADS, smem, ctx->stream>>>((float*)T, ctx->d_lat_tab32, ctx->d_lat_scale32, g, rz, scal);
-    }
-    SG_LAUNCHED(ctx);
-    return SGFEM_OK;
+    if (precision == SGFEM_FP64) return launch_y<double>(ctx, T, ctx->d_lat_tab64, ctx->d_lat_scale64, rz, nblocks, scal);
+    return launch_y<float>(ctx, T, ctx->d_lat_tab32, ctx->d_lat_scale32, rz, nblocks, scal);
 }
 
 int sg_lat_pass_xinv(sgfem_context* ctx, int precision, const void* T, void* out, int mode, const KrylovScalars* scal) {
-    LatGeom g = geom(ctx);
-    const int grid = (g.Nl - 1) * g.nchunk;
-    if (precision == SGFEM_FP64) {
-        size_t smem = lat_smem(ctx, 8);
-        k_lat_pass_x<double><<<grid, LAT_THREADS, smem, ctx->stream>>>((const double*)T, (double*)out, ctx->d_lat_tab64, g, mode, scal);
-    } else {
-        size_t smem = lat_smem(ctx, 4);
-        k_lat_pass_x<float><<<grid, LAT_THREADS, smem, ctx->stream>>>((const float*)T, (float*)out, ctx->d_lat_tab32, g, mode, scal);
-    }
-    SG_LAUNCHED(ctx);
-    return SGFEM_OK;
+    if (precision == SGFEM_FP64) return launch_x<double>(ctx, T, out, ctx->d_lat_tab64, mode, scal);
+    return launch_x<float>(ctx, T, out, ctx->d_lat_tab32, mode, scal);
 }
 
 int sg_jacobi(sgfem_context* ctx, int precision, const void* R, void* out, int mode, int identity, double* rz,

@@ -140,6 +140,8 @@ SGFEM_API int sgfem_solve_device(sgfem_context* ctx, const double* b0, void* x_d
 
 /* time (ms, CUDA events on the context stream) of `reps` back-to-back device applies */
 SGFEM_API int sgfem_time_apply(sgfem_context* ctx, int precision, int reps, double* ms_per_apply);
+/* the same for the lattice preconditioner (three passes per application) */
+SGFEM_API int sgfem_time_precondition(sgfem_context* ctx, int precision, int reps, double* ms_per_application);
 /*
  * No counterpart in the reference package.  Applies the mean-based lattice
  * preconditioner (what sgfem_precondition does with SGFEM_PREC_LATTICE) to
