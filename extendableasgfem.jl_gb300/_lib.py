@@ -72,6 +72,7 @@ SIGNATURES = {
     "sgfem_time_apply": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _DP]),
     "sgfem_kernel_launches": (ctypes.c_longlong, [_P]),
     "sgfem_time_precondition": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _DP]),
+    "sgfem_estimate_primal": (ctypes.c_int, [_P, _DP, _P, _P, _DP, _P, _P, _DP, _DP]),
     "sgfem_precondition_device_static": (ctypes.c_int, [_P, _P, _P, ctypes.c_int]),
     "sgfem_apply_variant": (ctypes.c_int, [_P]),
     "sgfem_apply_variant_log": (ctypes.c_char_p, [_P]),

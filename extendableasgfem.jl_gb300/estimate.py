@@ -1,0 +1,156 @@
+"""Residual error estimator for PoissonProblemPrimal (host side of K4).
+
+Mirrors estimate(::Type{PoissonProblemPrimal}, sol, C; rhs, bonus_quadorder,
+tail_extension) of src/estimate.jl:260-418.  The integer work of the
+reference runs here (extended multi-index set, add_boundary_modes,
+mopcontrol.jl:60-132; neighbour tables, estimate.jl:1-22; the coupling tensor
+of the extended set, tensorizedbasis.jl:193-218) and is reduced to one list
+per extended mode j of its couplings to active modes; the per-cell and
+per-face arithmetic runs in libsgfem (sgfem_estimate_primal).
+Returns (eta4modes, eta4cell, multi_indices_extended) like the reference,
+eta4cell with shape (ncells, P_ext).
+"""
+import copy
+import ctypes
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _lib
+from .fem import line_rule, triangle_rule
+from .modelproblems import PoissonProblemPrimal
+from .mopcontrol import add_boundary_modes, get_neighbours
+from .tensorizedbasis import coupling_matrix
+
+
+class _Mesh(ctypes.Structure):
+    _fields_ = [("order", ctypes.c_int), ("nnodes", ctypes.c_int64), ("ncells", ctypes.c_int64),
+                ("nfaces", ctypes.c_int64), ("coords", ctypes.c_void_p), ("cell_nodes", ctypes.c_void_p),
+                ("cell_dofs", ctypes.c_void_p), ("face_nodes", ctypes.c_void_p), ("face_cells", ctypes.c_void_p),
+                ("cell_faces", ctypes.c_void_p), ("cell_volumes", ctypes.c_void_p),
+                ("face_volumes", ctypes.c_void_p)]
+
+
+class _Quad(ctypes.Structure):
+    _fields_ = [("nq", ctypes.c_int), ("xref", ctypes.c_void_p), ("w", ctypes.c_void_p), ("nqf", ctypes.c_int),
+                ("tref", ctypes.c_void_p), ("wf", ctypes.c_void_p)]
+
+
+class _Cosine(ctypes.Structure):
+    _fields_ = [("maxm", ctypes.c_int), ("mean", ctypes.c_double), ("freq", ctypes.c_double),
+                ("decay_factors", ctypes.c_void_p), ("b1", ctypes.c_void_p), ("b2", ctypes.c_void_p)]
+
+
+class _Ext(ctypes.Structure):
+    _fields_ = [("P_ext", ctypes.c_int64), ("M_ext", ctypes.c_int64), ("ptr", ctypes.c_void_p),
+                ("m", ctypes.c_void_p), ("nu", ctypes.c_void_p), ("g", ctypes.c_void_p)]
+
+
+def _ptr(a):
+    return a.ctypes.data
+
+
+def extension_couplings(multi_indices, basis, tail_extension=(10, 2)):
+    """Extended set and, per extended mode j, its couplings to active modes:
+    (0, j, 1) if j is active, (m, nu, G_ext[(m-1)P_ext + j, nu]) for active
+    neighbours nu = j +/- e_m (estimate.jl:343-353, :385-393)."""
+    nmodes = len(multi_indices)
+    ext = add_boundary_modes(copy.deepcopy([list(m) for m in multi_indices]), tail_extension=tail_extension)
+    P_ext = len(ext)
+    M_ext = len(ext[0])
+    G = coupling_matrix(basis, ext).tocsr()
+    plus, minus = get_neighbours(ext)
+    ptr = [0]
+    ms, nus, gs = [], [], []
+    for j in range(P_ext):
+        if j < nmodes:
+            ms.append(0)
+            nus.append(j)
+            gs.append(1.0)
+        for m in range(1, M_ext + 1):
+            for nb in (plus[m - 1][j], minus[m - 1][j]):
+                if 0 < nb <= nmodes:
+                    ms.append(m)
+                    nus.append(nb - 1)
+                    gs.append(G[(m - 1) * P_ext + j, nb - 1])
+        ptr.append(len(ms))
+    return ext, (np.array(ptr, dtype=np.int64), np.array(ms, dtype=np.int32), np.array(nus, dtype=np.int32),
+                 np.array(gs, dtype=np.float64))
+
+
+def _light_context(FES, TB, device):
+    """A context that carries only the dof/mode layout (identity blocks)."""
+    n = FES.ndofs
+    I = sp.identity(n, format="csr")
+    M = TB.maxlength_multiindices()
+    ctx = _lib.Context(device)
+    for m in range(M + 1):
+        ctx.set_spatial_matrix(m, I)
+    ctx.set_coupling(TB.G, TB.nmodes, M)
+    ctx.set_boundary_dofs(FES.bdofs)
+    ctx.set_dof_coordinates(FES.dof_coords)
+    ctx.finalize()
+    return ctx
+
+
+def estimate(problem, sol, C, rhs=None, bonus_quadorder=1, tail_extension=(10, 2), face_points=None, device=0,
+             op=None):
+    """estimate(PoissonProblemPrimal, sol, C; rhs, bonus_quadorder, tail_extension) on the GPU.
+
+    ``op``: an SGOperator of the same space and basis to reuse its context.
+    ``face_points``: Gauss points per face for the jump term (default quadorder + 1).
+    """
+    if problem is not PoissonProblemPrimal:
+        raise NotImplementedError(f"no estimator for {problem}")
+    if rhs is None:
+        raise ValueError("need right-hand side")
+    FES = sol.FES_space[0]
+    mesh = FES.mesh
+    TB = sol.TB
+    ext, (ptr, ms, nus, gs) = extension_couplings(TB.multi_indices, TB.basis, tail_extension)
+    P_ext, M_ext = len(ext), len(ext[0])
+    if C.maxm() < M_ext:
+        raise ValueError(f"coefficient maxm = {C.maxm()} < extended length {M_ext}")
+    order = FES.order
+    quadorder = 2 * (order - 1) + bonus_quadorder
+    pts, wts = triangle_rule(quadorder)
+    tq, tw = line_rule(face_points if face_points is not None else quadorder + 1)
+    X = FES.physical_points(pts)
+    fq = np.ascontiguousarray(np.broadcast_to(np.asarray(rhs(X[..., 0], X[..., 1]), dtype=np.float64), X.shape[:2]))
+
+    coords = np.ascontiguousarray(mesh.coords, dtype=np.float64)
+    cell_nodes = np.ascontiguousarray(mesh.cells + 1, dtype=np.int64)
+    cell_dofs = np.ascontiguousarray(FES.celldofs + 1, dtype=np.int64)
+    face_nodes = np.ascontiguousarray(mesh.face_nodes + 1, dtype=np.int64)
+    face_cells = np.ascontiguousarray(np.where(mesh.face_cells >= 0, mesh.face_cells + 1, 0), dtype=np.int64)
+    cell_faces = np.ascontiguousarray(mesh.cellfaces + 1, dtype=np.int64)
+    cvol = np.ascontiguousarray(mesh.cell_volumes, dtype=np.float64)
+    fvol = np.ascontiguousarray(mesh.face_volumes, dtype=np.float64)
+    m = _Mesh(order, mesh.nnodes, mesh.ncells, mesh.nfaces, _ptr(coords), _ptr(cell_nodes), _ptr(cell_dofs),
+              _ptr(face_nodes), _ptr(face_cells), _ptr(cell_faces), _ptr(cvol), _ptr(fvol))
+    xref = np.ascontiguousarray(pts, dtype=np.float64)
+    w = np.ascontiguousarray(wts, dtype=np.float64)
+    tq = np.ascontiguousarray(tq, dtype=np.float64)
+    tw = np.ascontiguousarray(tw, dtype=np.float64)
+    q = _Quad(len(w), _ptr(xref), _ptr(w), len(tw), _ptr(tq), _ptr(tw))
+    dfac = np.ascontiguousarray(C.decay_factors, dtype=np.float64)
+    b1 = np.ascontiguousarray(C.b1, dtype=np.int64)
+    b2 = np.ascontiguousarray(C.b2, dtype=np.int64)
+    c = _Cosine(C.maxm(), C.mean_value, C.freq, _ptr(dfac), _ptr(b1), _ptr(b2))
+    e = _Ext(P_ext, M_ext, _ptr(ptr), _ptr(ms), _ptr(nus), _ptr(gs))
+    eta4modes = np.zeros(P_ext)
+    eta4cell = np.zeros((P_ext, mesh.ncells))
+    ctx = op.ctx if op is not None else _light_context(FES, TB, device)
+    try:
+        solv = np.ascontiguousarray(sol.entries, dtype=np.float64)
+        lib = _lib.load()
+        rc = lib.sgfem_estimate_primal(ctx.h, solv.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(m),
+                                       ctypes.byref(q), fq.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                       ctypes.byref(c), ctypes.byref(e),
+                                       eta4modes.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                       eta4cell.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        ctx._check(rc)
+    finally:
+        if op is None:
+            ctx.close()
+    return eta4modes, eta4cell.T, ext

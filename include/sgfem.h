@@ -143,6 +143,68 @@ SGFEM_API int sgfem_time_apply(sgfem_context* ctx, int precision, int reps, doub
 /* the same for the lattice preconditioner (three passes per application) */
 SGFEM_API int sgfem_time_precondition(sgfem_context* ctx, int precision, int reps, double* ms_per_application);
 /*
+ * Residual error estimator, estimate(::Type{PoissonProblemPrimal}, sol, C; rhs,
+ * bonus_quadorder, tail_extension), src/estimate.jl:260-418.  The caller (the
+ * host layer, which also runs the integer work add_boundary_modes /
+ * get_neighbours of mopcontrol.jl:60-132, estimate.jl:1-22) passes the mesh in
+ * ExtendableGrids' layout, the quadrature rules, f at the cell quadrature
+ * points, the cosine coefficient and, for every extended mode j, the list of
+ * its couplings to ACTIVE modes (the terms the reference adds):
+ *   (m = 0, nu = j, g = 1) if j is active, and (m, nu, g = G_ext[(m-1)P_ext+j, nu])
+ *   for every active neighbour nu = j +/- e_m, m = 1..M_ext.
+ * Outputs follow the reference: eta4modes[P_ext], eta4cell (ncells x P_ext,
+ * column-major).  The jump term integrates |sum_m a_m [[grad w_{j,m}]]|^2 on
+ * every interior face with the given face rule (the reference projects onto a
+ * face space first, ExtendableFEM's FaceInterpolator; that projection is not
+ * restated).  All arithmetic in FP64.
+ */
+typedef struct {
+    int order;                     /* 1 or 2: H1 Pk on triangles */
+    int64_t nnodes, ncells, nfaces;
+    const double* coords;          /* 2 x nnodes (xgrid[Coordinates]) */
+    const int64_t* cell_nodes;     /* 3 x ncells, 1-based (xgrid[CellNodes]) */
+    const int64_t* cell_dofs;      /* nd x ncells, 1-based (FES[CellDofs]); P2: vertex dofs then the
+                                      dofs of faces (1,2), (2,3), (3,1) */
+    const int64_t* face_nodes;     /* 2 x nfaces, 1-based (xgrid[FaceNodes]) */
+    const int64_t* face_cells;     /* 2 x nfaces, 1-based, 0 = none (xgrid[FaceCells]) */
+    const int64_t* cell_faces;     /* 3 x ncells, 1-based (xgrid[CellFaces]) */
+    const double* cell_volumes;    /* ncells */
+    const double* face_volumes;    /* nfaces */
+} sgfem_mesh;
+
+typedef struct {
+    int nq;                        /* cell rule: reference points (xi, eta) 2 x nq, weights (sum 1) */
+    const double* xref;
+    const double* w;
+    int nqf;                       /* face rule on [0, 1]: points, weights (sum 1) */
+    const double* tref;
+    const double* wf;
+} sgfem_quadrature;
+
+typedef struct {                   /* StochasticCoefficientCosinus, src/coefficients/cosinus.jl:11-76 */
+    int maxm;
+    double mean;                   /* a_0 */
+    double freq;                   /* multiplies pi (1 in the reference) */
+    const double* decay_factors;   /* maxm */
+    const int64_t* b1;             /* maxm */
+    const int64_t* b2;             /* maxm */
+} sgfem_cosine;
+
+typedef struct {
+    int64_t P_ext;                 /* extended modes, the active ones first */
+    int64_t M_ext;                 /* length of the extended multi-indices */
+    const int64_t* ptr;            /* P_ext + 1, 0-based offsets into the lists */
+    const int32_t* m;              /* coupling term: 0..M_ext */
+    const int32_t* nu;             /* active mode, 0-based */
+    const double* g;
+} sgfem_extension;
+
+SGFEM_API int sgfem_estimate_primal(sgfem_context* ctx, const double* sol, const sgfem_mesh* mesh,
+                                    const sgfem_quadrature* quad, const double* f_qp /* nq x ncells */,
+                                    const sgfem_cosine* coef, const sgfem_extension* ext, double* eta4modes,
+                                    double* eta4cell);
+
+/*
  * No counterpart in the reference package.  Applies the mean-based lattice
  * preconditioner (what sgfem_precondition does with SGFEM_PREC_LATTICE) to
  * device vectors without allocating any device memory.  It is meant for
