@@ -73,6 +73,8 @@ SIGNATURES = {
     "sgfem_kernel_launches": (ctypes.c_longlong, [_P]),
     "sgfem_time_precondition": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _DP]),
     "sgfem_estimate_primal": (ctypes.c_int, [_P, _DP, _P, _P, _DP, _P, _P, _DP, _DP]),
+    "sgfem_set_samples": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int64, _DP]),
+    "sgfem_solve_samples": (ctypes.c_int, [_P, _DP, _DP, ctypes.POINTER(SolveOptions), ctypes.POINTER(SolveStats)]),
     "sgfem_precondition_device_static": (ctypes.c_int, [_P, _P, _P, ctypes.c_int]),
     "sgfem_apply_variant": (ctypes.c_int, [_P]),
     "sgfem_apply_variant_log": (ctypes.c_char_p, [_P]),
@@ -166,6 +168,23 @@ class Context:
         colptr, rowval, nzval = _csc_arrays(G)
         self._check(self.lib.sgfem_set_coupling(self.h, int(P), int(M), _i64p(colptr), _i64p(rowval), _dp(nzval)))
         self.P = P
+
+    def set_samples(self, y):
+        """y: (M, S) sample matrix (Julia M x S column-major == NumPy (S, M) C-order)."""
+        y = np.asarray(y, dtype=np.float64)
+        M, S = y.shape
+        yc = np.ascontiguousarray(y.T)
+        self._check(self.lib.sgfem_set_samples(self.h, int(S), int(M), _dp(yc)))
+        self.P = S
+
+    def solve_samples(self, b0, x_inout, options=None, allow_maxit=False):
+        b0 = np.ascontiguousarray(b0, dtype=np.float64)
+        assert x_inout.dtype == np.float64 and x_inout.flags.c_contiguous
+        o = options if options is not None else self.default_options()
+        st = SolveStats()
+        self._check(self.lib.sgfem_solve_samples(self.h, _dp(b0), _dp(x_inout), ctypes.byref(o), ctypes.byref(st)),
+                    allow=(ERR_MAXIT,) if allow_maxit else ())
+        return st
 
     def set_boundary_dofs(self, bdofs0):
         b = np.ascontiguousarray(np.asarray(bdofs0, dtype=np.int64) + 1)

@@ -156,8 +156,12 @@ int sg_apply_configure(sgfem_context* ctx) {
     return SGFEM_OK;
 }
 
+int sg_launch_apply_samples(sgfem_context* ctx, int precision, const void* X, void* Y, double* dot_partials,
+                            int* nblocks, const KrylovScalars* skip_if_done);
+
 int sg_launch_apply(sgfem_context* ctx, int precision, const void* X, void* Y, double* dot_partials, int* nblocks,
                     const KrylovScalars* skip_if_done) {
+    if (ctx->batched) return sg_launch_apply_samples(ctx, precision, X, Y, dot_partials, nblocks, skip_if_done);
     const size_t per_warp = ((size_t)ctx->ld + ctx->M1 + 1 + ctx->Qn + 3) & ~(size_t)3;
     const size_t smem = per_warp * sg_elem_bytes(precision) * WPB;
     if (smem > 200 * 1024)
@@ -173,4 +177,91 @@ int sg_launch_apply(sgfem_context* ctx, int precision, const void* X, void* Y, d
     if (precision == SGFEM_FP64)
         return launch_t<double>(ctx, ctx->d_val64, ctx->d_combg64, X, Y, dot_partials, grid, skip_if_done);
     return launch_t<float>(ctx, ctx->d_val32, ctx->d_combg32, X, Y, dot_partials, grid, skip_if_done);
+}
+
+// ---------------------------------------------------------------------------
+// Block-diagonal sample operator (sgfem_set_samples): column s of Y is
+//   Y[i, s] = sum_j (K_0[i,j] + sum_{m<=M} y_{s,m} K_m[i,j]) X[j, s],
+// Dirichlet rows zero.  Warp per (row, 32-sample chunk), lane = sample; the
+// lane's coefficients y_{s,0..M} live in registers (MMAX >= M+1), the M+1
+// values of a nonzero are read with a warp-uniform address.  This is the
+// operator of the S deterministic problems of the sampling error
+// (src/sampling_error.jl:118-128, src/modelproblems/poisson_primal.jl:14-35).
+namespace {
+
+template <typename T, int MMAX>
+__global__ void __launch_bounds__(128)
+k_apply_samples(const int* __restrict__ rowptr, const int* __restrict__ col, const T* __restrict__ vals, int M1,
+                const T* __restrict__ ycoef, const T* __restrict__ X, T* __restrict__ Y, int n, int S, int ld,
+                const unsigned char* __restrict__ bmask, double* __restrict__ partials,
+                const KrylovScalars* __restrict__ scal) {
+    if (scal && scal->done) return;
+    __shared__ double red[4];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nchunk = (ld + 31) / 32;
+    const long long items = (long long)n * nchunk;
+    double dot = 0.0;
+    for (long long it = (long long)blockIdx.x * 4 + warp; it < items; it += (long long)gridDim.x * 4) {
+        const int row = (int)(it / nchunk), ch = (int)(it - (long long)row * nchunk);
+        const int s = ch * 32 + lane;
+        T y[MMAX];
+#pragma unroll
+        for (int m = 0; m < MMAX; ++m) y[m] = (s < S && m < M1) ? ycoef[(size_t)s * M1 + m] : T(0);
+        T acc = T(0);
+        if (!bmask[row]) {
+            for (int nz = rowptr[row]; nz < rowptr[row + 1]; ++nz) {
+                const int j = col[nz];
+                const T* v = vals + (size_t)nz * M1;
+                T c = T(0);
+#pragma unroll
+                for (int m = 0; m < MMAX; ++m)
+                    if (m < M1) c = fma(y[m], v[m], c);
+                if (s < ld) acc = fma(c, X[(size_t)j * ld + s], acc);
+            }
+        }
+        if (s < ld) {
+            Y[(size_t)row * ld + s] = acc;
+            if (partials) dot += (double)X[(size_t)row * ld + s] * (double)acc;
+        }
+    }
+    if (partials) {
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
+        if (lane == 0) red[warp] = dot;
+        __syncthreads();
+        if (threadIdx.x == 0) partials[blockIdx.x] = red[0] + red[1] + red[2] + red[3];
+    }
+}
+
+template <typename T, int MMAX>
+int launch_samples_t(sgfem_context* ctx, const T* vals, const T* y, const void* X, void* Y, double* partials,
+                     int grid, const KrylovScalars* scal) {
+    k_apply_samples<T, MMAX><<<grid, 128, 0, ctx->stream>>>(ctx->d_rowptr, ctx->d_col, vals, ctx->M1, y,
+                                                              (const T*)X, (T*)Y, (int)ctx->n, (int)ctx->P,
+                                                              (int)ctx->ld, ctx->d_bmask, partials, scal);
+    SG_LAUNCHED(ctx);
+    return SGFEM_OK;
+}
+
+template <typename T>
+int launch_samples(sgfem_context* ctx, const T* vals, const T* y, const void* X, void* Y, double* partials, int grid,
+                   const KrylovScalars* scal) {
+    if (ctx->M1 <= 8) return launch_samples_t<T, 8>(ctx, vals, y, X, Y, partials, grid, scal);
+    if (ctx->M1 <= 16) return launch_samples_t<T, 16>(ctx, vals, y, X, Y, partials, grid, scal);
+    if (ctx->M1 <= 24) return launch_samples_t<T, 24>(ctx, vals, y, X, Y, partials, grid, scal);
+    if (ctx->M1 <= 32) return launch_samples_t<T, 32>(ctx, vals, y, X, Y, partials, grid, scal);
+    if (ctx->M1 <= 64) return launch_samples_t<T, 64>(ctx, vals, y, X, Y, partials, grid, scal);
+    return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "sample operator: more than 63 KLE terms");
+}
+
+}  // namespace
+
+int sg_launch_apply_samples(sgfem_context* ctx, int precision, const void* X, void* Y, double* dot_partials,
+                            int* nblocks, const KrylovScalars* skip_if_done) {
+    const int64_t items = ctx->n * ((ctx->ld + 31) / 32);
+    int grid = (int)std::min<int64_t>((items + 3) / 4, (int64_t)ctx->num_sms * 8);
+    if (grid < 1) grid = 1;
+    if (nblocks) *nblocks = grid;
+    if (precision == SGFEM_FP64)
+        return launch_samples<double>(ctx, ctx->d_val64, ctx->d_y64, X, Y, dot_partials, grid, skip_if_done);
+    return launch_samples<float>(ctx, ctx->d_val32, ctx->d_y32, X, Y, dot_partials, grid, skip_if_done);
 }

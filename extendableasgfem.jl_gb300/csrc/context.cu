@@ -87,7 +87,8 @@ extern "C" int sgfem_destroy(sgfem_context* ctx) {
                     ctx->d_dinv64, ctx->d_dinv32, ctx->d_qtab, ctx->d_combptr, ctx->d_combq,
                     ctx->d_combg64, ctx->d_combg32, ctx->d_lat_tab64, ctx->d_lat_tab32,
                     ctx->d_lat_scale64, ctx->d_lat_scale32, ctx->d_scal, ctx->w_stage.p, ctx->w_partials.p,
-                    ctx->d_jptr, ctx->d_joff, ctx->d_jg, ctx->d_jtab, ctx->d_val32p, ctx->d_mode_of_col};
+                    ctx->d_jptr, ctx->d_joff, ctx->d_jg, ctx->d_jtab, ctx->d_val32p, ctx->d_mode_of_col,
+                    ctx->d_y64, ctx->d_y32};
     sg_jit_release(ctx);
     for (void* p : ptrs) free_dev(p);
     for (int i = 0; i < SG_NBUF; ++i) free_dev(ctx->w_vec[i].p);
@@ -159,6 +160,21 @@ extern "C" int sgfem_set_coupling(sgfem_context* ctx, int64_t P, int64_t M, cons
     ctx->G_val.assign(nzval, nzval + nnz);
     ctx->P = P;
     ctx->M = M;
+    ctx->has_G = true;
+    return SGFEM_OK;
+}
+
+extern "C" int sgfem_set_samples(sgfem_context* ctx, int64_t S, int64_t M, const double* y) {
+    if (!ctx) return SGFEM_ERR_ARGUMENT;
+    SG_TRY(invalidate(ctx));
+    if (S <= 0 || S > 32767 || M < 0 || M > 4095 || (M > 0 && !y))
+        return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "sgfem_set_samples: bad sizes (S <= 32767, M <= 4095)");
+    ctx->ysamp.assign(y, y + M * S);
+    for (double v : ctx->ysamp)
+        if (!std::isfinite(v)) return sg_fail(ctx, SGFEM_ERR_NONFINITE, "non-finite sample");
+    ctx->P = S;
+    ctx->M = M;
+    ctx->batched = true;
     ctx->has_G = true;
     return SGFEM_OK;
 }
@@ -407,140 +423,164 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
     }
     ctx->lat_scale = dcount ? dsum / (4.0 * dcount) : 1.0;
 
+    if (ctx->batched) {
+        // block-diagonal sample operator: identity mode order, per-sample coefficients
+        std::vector<int32_t> ident(P);
+        std::iota(ident.begin(), ident.end(), 0);
+        ctx->mode_of_col = ident;
+        ctx->imode = ident;
+        SG_TRY(upload(ctx, &ctx->d_mode_of_col, ident.data(), ident.size()));
+        std::vector<double> y64((size_t)P * ctx->M1);
+        std::vector<float> y32((size_t)P * ctx->M1);
+        for (int64_t sidx = 0; sidx < P; ++sidx) {
+            y64[(size_t)sidx * ctx->M1] = 1.0;
+            for (int64_t m = 1; m <= M; ++m) y64[(size_t)sidx * ctx->M1 + m] = ctx->ysamp[(size_t)sidx * M + (m - 1)];
+        }
+        for (size_t t = 0; t < y64.size(); ++t) y32[t] = (float)y64[t];
+        SG_TRY(upload(ctx, &ctx->d_y64, y64.data(), y64.size()));
+        SG_TRY(upload(ctx, &ctx->d_y32, y32.data(), y32.size()));
+        ctx->Qn = 0;
+    } else {
     // ---- coupling structure from G ((M*P) x P, CSC): entry (row = m'*P + mu, col = nu), m = m'+1
-    std::vector<std::vector<char>> nzcol(M + 1, std::vector<char>(P, 0));
-    struct GE { int m; int mu; int nu; double g; };
-    std::vector<GE> ges;
-    for (int64_t nu = 0; nu < P; ++nu)
-        for (int64_t k = ctx->G_colptr[nu]; k < ctx->G_colptr[nu + 1]; ++k) {
-            double g = ctx->G_val[k];
-            if (g == 0.0) continue;  // the reference skips zero couplings (solvers_poisson_primal.jl:111)
-            int64_t r = ctx->G_rowval[k];
-            int m = (int)(r / P) + 1;
-            int mu = (int)(r % P);
-            nzcol[m][nu] = 1;
-            ges.push_back({m, mu, (int)nu, g});
-        }
-
-    // ---- device column order of the modes (sg_mode_order): packs the coupled
-    // columns of each pair of KLE terms into few 32-column groups
-    std::vector<int32_t> mode_of_col;  // device column -> caller mode
-    sg_mode_order(ctx, nzcol, mode_of_col);
-    ctx->imode.assign(P, 0);
-    for (int64_t c = 0; c < P; ++c) ctx->imode[mode_of_col[c]] = (int32_t)c;
-    const std::vector<int32_t>& imode = ctx->imode;
-
-    // pair list Q in device columns: (0, c) for all c, then (m, c) for nonzero columns of G_m
-    std::vector<int32_t> qtab;
-    std::map<std::pair<int, int>, int> qidx;
-    for (int64_t c = 0; c < P; ++c) {
-        qidx[{0, (int)c}] = (int)qtab.size();
-        qtab.push_back((int32_t)c);
-    }
-    for (int64_t m = 1; m <= M; ++m)
-        for (int64_t c = 0; c < P; ++c)
-            if (nzcol[m][mode_of_col[c]]) {
-                qidx[{(int)m, (int)c}] = (int)qtab.size();
-                qtab.push_back((int32_t)((m << 16) | c));
+        std::vector<std::vector<char>> nzcol(M + 1, std::vector<char>(P, 0));
+        struct GE { int m; int mu; int nu; double g; };
+        std::vector<GE> ges;
+        for (int64_t nu = 0; nu < P; ++nu)
+            for (int64_t k = ctx->G_colptr[nu]; k < ctx->G_colptr[nu + 1]; ++k) {
+                double g = ctx->G_val[k];
+                if (g == 0.0) continue;  // the reference skips zero couplings (solvers_poisson_primal.jl:111)
+                int64_t r = ctx->G_rowval[k];
+                int m = (int)(r / P) + 1;
+                int mu = (int)(r % P);
+                nzcol[m][nu] = 1;
+                ges.push_back({m, mu, (int)nu, g});
             }
-    ctx->Qn = (int)qtab.size();
-    for (GE& e : ges) {
-        e.mu = imode[e.mu];
-        e.nu = imode[e.nu];
-    }
-    std::sort(ges.begin(), ges.end(), [](const GE& a, const GE& b) {
-        if (a.mu != b.mu) return a.mu < b.mu;
-        if (a.m != b.m) return a.m < b.m;
-        return a.nu < b.nu;
-    });
-    std::vector<int32_t> combptr(P + 1, 0), combq;
-    std::vector<double> combg;
-    for (const GE& e : ges) {
-        combptr[e.mu + 1]++;
-        combq.push_back(qidx[{e.m, e.nu}]);
-        combg.push_back(e.g);
-    }
-    for (int64_t mu = 0; mu < P; ++mu) combptr[mu + 1] += combptr[mu];
-    ctx->ncomb = (int)combq.size();
-    std::vector<float> combg32(combg.begin(), combg.end());
-
-    // ---- slot tables of the specialised FP32 apply: slot (pair p = m/2, group k = c/32)
-    // exists if some column of group k couples to K_2p or K_2p+1 (K_0 couples to all)
-    const int KG = (int)((P + 31) / 32);
-    const int NPAIR = (ctx->M1 + 1) / 2;
-    ctx->M1P = (ctx->M1 + 3) / 4 * 4;
-    ctx->jit_slot_of.assign((size_t)NPAIR * KG, -1);
-    ctx->jit_slots.clear();
-    for (int pr = 0; pr < NPAIR; ++pr)
-        for (int k = 0; k < KG; ++k) {
-            bool need = false;
-            for (int c = 32 * k; c < std::min<int64_t>(P, 32 * k + 32) && !need; ++c)
-                for (int m = 2 * pr; m <= std::min<int64_t>(M, 2 * pr + 1) && !need; ++m)
-                    need = (m == 0) || nzcol[m][mode_of_col[c]];
-            if (need) {
-                ctx->jit_slot_of[(size_t)pr * KG + k] = (int)ctx->jit_slots.size();
-                ctx->jit_slots.push_back({pr, k});
-            }
+    
+        // ---- device column order of the modes (sg_mode_order): packs the coupled
+        // columns of each pair of KLE terms into few 32-column groups
+        std::vector<int32_t> mode_of_col;  // device column -> caller mode
+        sg_mode_order(ctx, nzcol, mode_of_col);
+        ctx->imode.assign(P, 0);
+        for (int64_t c = 0; c < P; ++c) ctx->imode[mode_of_col[c]] = (int32_t)c;
+        const std::vector<int32_t>& imode = ctx->imode;
+    
+        // pair list Q in device columns: (0, c) for all c, then (m, c) for nonzero columns of G_m
+        std::vector<int32_t> qtab;
+        std::map<std::pair<int, int>, int> qidx;
+        for (int64_t c = 0; c < P; ++c) {
+            qidx[{0, (int)c}] = (int)qtab.size();
+            qtab.push_back((int32_t)c);
         }
-    auto slot_off = [&](int m, int c) {
-        int sl = ctx->jit_slot_of[(size_t)(m / 2) * KG + c / 32];
-        return sl * 64 + 2 * (c % 32) + (m % 2);
-    };
-    // combination list per output column: (1, acc(0, c)) then (g, acc(m, nu))
-    std::vector<int32_t> jptr(P + 1, 0), joff;
-    std::vector<float> jg;
-    for (int64_t c = 0; c < P; ++c) {
-        joff.push_back(slot_off(0, (int)c));
-        jg.push_back(1.0f);
-        for (int32_t e = combptr[c]; e < combptr[c + 1]; ++e) {
-            int q = combq[e];
-            int m = qtab[q] >> 16, nu = qtab[q] & 0xffff;
-            joff.push_back(slot_off(m, nu));
-            jg.push_back((float)combg[e]);
+        for (int64_t m = 1; m <= M; ++m)
+            for (int64_t c = 0; c < P; ++c)
+                if (nzcol[m][mode_of_col[c]]) {
+                    qidx[{(int)m, (int)c}] = (int)qtab.size();
+                    qtab.push_back((int32_t)((m << 16) | c));
+                }
+        ctx->Qn = (int)qtab.size();
+        for (GE& e : ges) {
+            e.mu = imode[e.mu];
+            e.nu = imode[e.nu];
         }
-        jptr[c + 1] = (int32_t)joff.size();
-    }
-    std::vector<float> val32p((size_t)nnz * ctx->M1P, 0.0f);
-    for (int64_t k = 0; k < nnz; ++k)
-        for (int m = 0; m < ctx->M1; ++m) val32p[(size_t)k * ctx->M1P + m] = (float)val64[(size_t)k * ctx->M1 + m];
-    SG_TRY(upload(ctx, &ctx->d_jptr, jptr.data(), jptr.size()));
-    SG_TRY(upload(ctx, &ctx->d_joff, joff.data(), joff.size()));
-    SG_TRY(upload(ctx, &ctx->d_jg, jg.data(), jg.size()));
-    // lane schedule of the combination: columns assigned to the 32 lanes longest
-    // first (each to the least loaded lane); per lane its columns' entries in
-    // sequence, padded to a common length T; entry (i, lane) at [i * 32 + lane]
-    // x = sacc offset | column << 13 | (last entry of the column) << 28, y = g bits
-    {
-        std::vector<int> order(P);
-        std::iota(order.begin(), order.end(), 0);
-        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-            return (jptr[a + 1] - jptr[a]) > (jptr[b + 1] - jptr[b]);
+        std::sort(ges.begin(), ges.end(), [](const GE& a, const GE& b) {
+            if (a.mu != b.mu) return a.mu < b.mu;
+            if (a.m != b.m) return a.m < b.m;
+            return a.nu < b.nu;
         });
-        std::vector<std::vector<int2>> lanes(32);
-        for (int c : order) {
-            int best = 0;
-            for (int l = 1; l < 32; ++l)
-                if (lanes[l].size() < lanes[best].size()) best = l;
-            for (int32_t e = jptr[c]; e < jptr[c + 1]; ++e) {
-                int bits;
-                std::memcpy(&bits, &jg[e], sizeof(int));
-                const bool last = (e + 1 == jptr[c + 1]);
-                lanes[best].push_back(make_int2(joff[e] | (int)(c << 13) | ((last ? 1 : 0) << 28), bits));
-            }
+        std::vector<int32_t> combptr(P + 1, 0), combq;
+        std::vector<double> combg;
+        for (const GE& e : ges) {
+            combptr[e.mu + 1]++;
+            combq.push_back(qidx[{e.m, e.nu}]);
+            combg.push_back(e.g);
         }
-        size_t T = 0;
-        for (auto& l : lanes) T = std::max(T, l.size());
-        ctx->jit_T = (int)T;
-        std::vector<int2> jtab(T * 32, make_int2(0, 0));
-        for (int l = 0; l < 32; ++l)
-            for (size_t i = 0; i < lanes[l].size(); ++i) jtab[i * 32 + l] = lanes[l][i];
-        const bool fits = (ctx->jit_slots.size() * 64 <= 8192) && P <= 32767;
-        if (!fits) ctx->jit_T = -1;
-        SG_TRY(upload(ctx, &ctx->d_jtab, jtab.data(), jtab.size()));
+        for (int64_t mu = 0; mu < P; ++mu) combptr[mu + 1] += combptr[mu];
+        ctx->ncomb = (int)combq.size();
+        std::vector<float> combg32(combg.begin(), combg.end());
+    
+        // ---- slot tables of the specialised FP32 apply: slot (pair p = m/2, group k = c/32)
+        // exists if some column of group k couples to K_2p or K_2p+1 (K_0 couples to all)
+        const int KG = (int)((P + 31) / 32);
+        const int NPAIR = (ctx->M1 + 1) / 2;
+        ctx->M1P = (ctx->M1 + 3) / 4 * 4;
+        ctx->jit_slot_of.assign((size_t)NPAIR * KG, -1);
+        ctx->jit_slots.clear();
+        for (int pr = 0; pr < NPAIR; ++pr)
+            for (int k = 0; k < KG; ++k) {
+                bool need = false;
+                for (int c = 32 * k; c < std::min<int64_t>(P, 32 * k + 32) && !need; ++c)
+                    for (int m = 2 * pr; m <= std::min<int64_t>(M, 2 * pr + 1) && !need; ++m)
+                        need = (m == 0) || nzcol[m][mode_of_col[c]];
+                if (need) {
+                    ctx->jit_slot_of[(size_t)pr * KG + k] = (int)ctx->jit_slots.size();
+                    ctx->jit_slots.push_back({pr, k});
+                }
+            }
+        auto slot_off = [&](int m, int c) {
+            int sl = ctx->jit_slot_of[(size_t)(m / 2) * KG + c / 32];
+            return sl * 64 + 2 * (c % 32) + (m % 2);
+        };
+        // combination list per output column: (1, acc(0, c)) then (g, acc(m, nu))
+        std::vector<int32_t> jptr(P + 1, 0), joff;
+        std::vector<float> jg;
+        for (int64_t c = 0; c < P; ++c) {
+            joff.push_back(slot_off(0, (int)c));
+            jg.push_back(1.0f);
+            for (int32_t e = combptr[c]; e < combptr[c + 1]; ++e) {
+                int q = combq[e];
+                int m = qtab[q] >> 16, nu = qtab[q] & 0xffff;
+                joff.push_back(slot_off(m, nu));
+                jg.push_back((float)combg[e]);
+            }
+            jptr[c + 1] = (int32_t)joff.size();
+        }
+        std::vector<float> val32p((size_t)nnz * ctx->M1P, 0.0f);
+        for (int64_t k = 0; k < nnz; ++k)
+            for (int m = 0; m < ctx->M1; ++m) val32p[(size_t)k * ctx->M1P + m] = (float)val64[(size_t)k * ctx->M1 + m];
+        SG_TRY(upload(ctx, &ctx->d_jptr, jptr.data(), jptr.size()));
+        SG_TRY(upload(ctx, &ctx->d_joff, joff.data(), joff.size()));
+        SG_TRY(upload(ctx, &ctx->d_jg, jg.data(), jg.size()));
+        // lane schedule of the combination: columns assigned to the 32 lanes longest
+        // first (each to the least loaded lane); per lane its columns' entries in
+        // sequence, padded to a common length T; entry (i, lane) at [i * 32 + lane]
+        // x = sacc offset | column << 13 | (last entry of the column) << 28, y = g bits
+        {
+            std::vector<int> order(P);
+            std::iota(order.begin(), order.end(), 0);
+            std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+                return (jptr[a + 1] - jptr[a]) > (jptr[b + 1] - jptr[b]);
+            });
+            std::vector<std::vector<int2>> lanes(32);
+            for (int c : order) {
+                int best = 0;
+                for (int l = 1; l < 32; ++l)
+                    if (lanes[l].size() < lanes[best].size()) best = l;
+                for (int32_t e = jptr[c]; e < jptr[c + 1]; ++e) {
+                    int bits;
+                    std::memcpy(&bits, &jg[e], sizeof(int));
+                    const bool last = (e + 1 == jptr[c + 1]);
+                    lanes[best].push_back(make_int2(joff[e] | (int)(c << 13) | ((last ? 1 : 0) << 28), bits));
+                }
+            }
+            size_t T = 0;
+            for (auto& l : lanes) T = std::max(T, l.size());
+            ctx->jit_T = (int)T;
+            std::vector<int2> jtab(T * 32, make_int2(0, 0));
+            for (int l = 0; l < 32; ++l)
+                for (size_t i = 0; i < lanes[l].size(); ++i) jtab[i * 32 + l] = lanes[l][i];
+            const bool fits = (ctx->jit_slots.size() * 64 <= 8192) && P <= 32767;
+            if (!fits) ctx->jit_T = -1;
+            SG_TRY(upload(ctx, &ctx->d_jtab, jtab.data(), jtab.size()));
+        }
+        SG_TRY(upload(ctx, &ctx->d_val32p, val32p.data(), val32p.size()));
+        ctx->mode_of_col = mode_of_col;
+        SG_TRY(upload(ctx, &ctx->d_mode_of_col, mode_of_col.data(), mode_of_col.size()));
+        SG_TRY(upload(ctx, &ctx->d_qtab, qtab.data(), qtab.size()));
+        SG_TRY(upload(ctx, &ctx->d_combptr, combptr.data(), combptr.size()));
+        SG_TRY(upload(ctx, &ctx->d_combq, combq.data(), combq.size()));
+        SG_TRY(upload(ctx, &ctx->d_combg64, combg.data(), combg.size()));
+        SG_TRY(upload(ctx, &ctx->d_combg32, combg32.data(), combg32.size()));
     }
-    SG_TRY(upload(ctx, &ctx->d_val32p, val32p.data(), val32p.size()));
-    ctx->mode_of_col = mode_of_col;
-    SG_TRY(upload(ctx, &ctx->d_mode_of_col, mode_of_col.data(), mode_of_col.size()));
 
     // ---- upload
     SG_TRY(upload(ctx, &ctx->d_rowptr, rowptr32.data(), rowptr32.size()));
@@ -551,11 +591,6 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
     SG_TRY(upload(ctx, &ctx->d_iperm, ctx->iperm.data(), ctx->iperm.size()));
     SG_TRY(upload(ctx, &ctx->d_dinv64, dinv.data(), dinv.size()));
     SG_TRY(upload(ctx, &ctx->d_dinv32, dinv32.data(), dinv32.size()));
-    SG_TRY(upload(ctx, &ctx->d_qtab, qtab.data(), qtab.size()));
-    SG_TRY(upload(ctx, &ctx->d_combptr, combptr.data(), combptr.size()));
-    SG_TRY(upload(ctx, &ctx->d_combq, combq.data(), combq.size()));
-    SG_TRY(upload(ctx, &ctx->d_combg64, combg.data(), combg.size()));
-    SG_TRY(upload(ctx, &ctx->d_combg32, combg32.data(), combg32.size()));
 
     if (ctx->lattice) {
         int s = sg_lattice_setup(ctx);
@@ -568,10 +603,11 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
             }
         }
     }
-    SG_TRY(sg_apply_configure(ctx));
+    if (!ctx->batched) SG_TRY(sg_apply_configure(ctx));
     if (ctx->lattice) SG_TRY(sg_lattice_configure(ctx));
     // specialised FP32 apply; on failure the generic kernel stays in use (reason in the variant log)
-    if (sg_jit_build(ctx) != SGFEM_OK) ctx->err.clear();
+    if (!ctx->batched && sg_jit_build(ctx) != SGFEM_OK) ctx->err.clear();
+    if (ctx->batched) ctx->jit_log = "block-diagonal sample operator";
     // host copies of the pattern are no longer needed
     for (auto& A : ctx->mats) {
         A.colptr.clear(); A.colptr.shrink_to_fit();

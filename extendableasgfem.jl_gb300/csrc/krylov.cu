@@ -171,6 +171,34 @@ __global__ void k_add_b0(const double* __restrict__ b0, double* __restrict__ b, 
     }
 }
 
+// b[row, s] = b0[caller dof] in every column (sample problems), Dirichlet rows zero
+__global__ void k_build_rhs_all(const double* __restrict__ b0, double* __restrict__ b, const int* __restrict__ iperm,
+                                const unsigned char* __restrict__ bmask, int n, int S, int ld) {
+    const size_t total = (size_t)n * ld;
+    for (size_t t = (size_t)blockIdx.x * VT + threadIdx.x; t < total; t += (size_t)gridDim.x * VT) {
+        const int i = (int)(t / ld), s = (int)(t - (size_t)i * ld);
+        const int row = iperm[i];
+        b[(size_t)row * ld + s] = (s < S && !bmask[row]) ? b0[i] : 0.0;
+    }
+}
+
+// out[s] = sum_i v[i * ld + s]^2, one block per column
+__global__ void k_colnorm2(const double* __restrict__ v, int n, int ld, double* __restrict__ out) {
+    __shared__ double red[VT];
+    double a = 0.0;
+    for (int i = threadIdx.x; i < n; i += VT) {
+        const double x = v[(size_t)i * ld + blockIdx.x];
+        a += x * x;
+    }
+    red[threadIdx.x] = a;
+    __syncthreads();
+    for (int w = VT / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
 int vgrid(const sgfem_context* ctx) {
     const int64_t total = ctx->n * ctx->ld;
     return (int)std::max<int64_t>(1, std::min<int64_t>((total + VT * 4 - 1) / (VT * 4), (int64_t)ctx->num_sms * 8));
@@ -356,8 +384,9 @@ extern "C" int sgfem_time_precondition(sgfem_context* ctx, int precision, int re
 }
 
 // core solve on device buffers: x64 (in/out, device layout), b0 host (caller order)
+// rhs_mode 0: b = (x0 or 0) + e_1 (x) b0 (solve_primal!); 1: b0 in every column (sample problems)
 static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const sgfem_solve_options* o,
-                      sgfem_solve_stats* st) {
+                      sgfem_solve_stats* st, int rhs_mode) {
     if (o->precision != SGFEM_FP64 && o->precision != SGFEM_FP32 && o->precision != SGFEM_MIXED)
         return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad precision");
     int prec_kind = o->preconditioner;
@@ -395,12 +424,18 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
     SG_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
     const long long launches0 = ctx->launches;
     const int g = vgrid(ctx);
-    k_build_rhs<<<g, VT, 0, ctx->stream>>>(d_b0, x64, b, ctx->d_iperm, ctx->d_bmask, (int)ctx->n, (int)ctx->ld,
-                                          o->reference_rhs ? 1 : 0);
-    ctx->launches++;
-    k_add_b0<<<(int)std::min<int64_t>((ctx->n + VT - 1) / VT, 4096), VT, 0, ctx->stream>>>(
-        d_b0, b, ctx->d_iperm, ctx->d_bmask, (int)ctx->n, (int)ctx->ld);
-    SG_LAUNCHED(ctx);
+    if (rhs_mode == 1) {
+        k_build_rhs_all<<<g, VT, 0, ctx->stream>>>(d_b0, b, ctx->d_iperm, ctx->d_bmask, (int)ctx->n, (int)ctx->P,
+                                                  (int)ctx->ld);
+        SG_LAUNCHED(ctx);
+    } else {
+        k_build_rhs<<<g, VT, 0, ctx->stream>>>(d_b0, x64, b, ctx->d_iperm, ctx->d_bmask, (int)ctx->n, (int)ctx->ld,
+                                              o->reference_rhs ? 1 : 0);
+        ctx->launches++;
+        k_add_b0<<<(int)std::min<int64_t>((ctx->n + VT - 1) / VT, 4096), VT, 0, ctx->stream>>>(
+            d_b0, b, ctx->d_iperm, ctx->d_bmask, (int)ctx->n, (int)ctx->ld);
+        SG_LAUNCHED(ctx);
+    }
 
     Solver S{ctx, prec_kind, partials, ctx->d_scal};
     // ||b||^2 -> host
@@ -457,49 +492,73 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
         }
     }
     int remaining = o->maxit;
-    if (!low) {
-        // FP64 PCG; restart from the true residual if the recurrence drifted
-        for (int restart = 0; restart < 8; ++restart) {
-            if (!std::isfinite(rr)) { status = SGFEM_ERR_NONFINITE; break; }
-            if (rr <= rtol2 * bb || remaining <= 0) break;
-            KrylovScalars h{};
-            h.tol2 = rtol2 * bb;
-            SG_CUDA(ctx, cudaMemcpyAsync(ctx->d_scal, &h, sizeof(KrylovScalars), cudaMemcpyHostToDevice, ctx->stream));
-            int it = 0;
-            status = S.pcg<double>(SGFEM_FP64, x64, r, t, q, tmp, remaining, check_every, &it);
-            st->iterations += it;
-            st->outer_iterations += 1;
-            remaining -= it;
-            SG_TRY(true_residual(&rr));
-            if (status != SGFEM_OK) break;
+    // sample problems: the global residual is driven down until every column
+    // meets rtol relative to its own right-hand side
+    double tol2e = rtol2;
+    double colmax = 0.0;
+    std::vector<double> cr, cb;
+    for (int pass = 0; pass < 6; ++pass) {
+        if (!low) {
+            // FP64 PCG; restart from the true residual if the recurrence drifted
+            for (int restart = 0; restart < 8; ++restart) {
+                if (!std::isfinite(rr)) { status = SGFEM_ERR_NONFINITE; break; }
+                if (rr <= tol2e * bb || remaining <= 0) break;
+                KrylovScalars h{};
+                h.tol2 = tol2e * bb;
+                SG_CUDA(ctx, cudaMemcpyAsync(ctx->d_scal, &h, sizeof(KrylovScalars), cudaMemcpyHostToDevice, ctx->stream));
+                int it = 0;
+                status = S.pcg<double>(SGFEM_FP64, x64, r, t, q, tmp, remaining, check_every, &it);
+                st->iterations += it;
+                st->outer_iterations += 1;
+                remaining -= it;
+                SG_TRY(true_residual(&rr));
+                if (status != SGFEM_OK) break;
+            }
+        } else {
+            float* d32 = (float*)ctx->w_vec[5].p;
+            float* r32 = (float*)ctx->w_vec[6].p;
+            float* p32 = (float*)ctx->w_vec[7].p;
+            float* q32 = (float*)ctx->w_vec[8].p;
+            float* tmp32 = (float*)ctx->w_vec[9].p;
+            const double in2 = o->precision == SGFEM_FP32 ? tol2e : o->inner_rtol * o->inner_rtol;
+            for (int outer = 0; outer < 64; ++outer) {
+                if (!std::isfinite(rr)) { status = SGFEM_ERR_NONFINITE; break; }
+                if (rr <= tol2e * bb) break;
+                if (remaining <= 0) { status = SGFEM_ERR_MAXIT; break; }
+                k_demote<<<g, VT, 0, ctx->stream>>>(r, r32, d32, total, partials);
+                SG_LAUNCHED(ctx);
+                // inner target: reduce ||r|| by inner_rtol, but never below what the outer tolerance needs
+                const double want = std::max(in2, 0.25 * tol2e * bb / rr);
+                SG_TRY(S.fin(g, FIN_TOL, FinArgs{want, 0}, nullptr));
+                int it = 0;
+                int s2 = S.pcg<float>(SGFEM_FP32, d32, r32, p32, q32, tmp32, remaining, check_every, &it);
+                st->iterations += it;
+                st->outer_iterations += 1;
+                remaining -= it;
+                if (s2 == SGFEM_ERR_BREAKDOWN || s2 == SGFEM_ERR_NONFINITE) { status = s2; break; }
+                k_promote_add<<<g, VT, 0, ctx->stream>>>(x64, d32, total);
+                SG_LAUNCHED(ctx);
+                SG_TRY(true_residual(&rr));
+                if (o->precision == SGFEM_FP32) break;  // plain FP32 PCG: no refinement
+            }
         }
-    } else {
-        float* d32 = (float*)ctx->w_vec[5].p;
-        float* r32 = (float*)ctx->w_vec[6].p;
-        float* p32 = (float*)ctx->w_vec[7].p;
-        float* q32 = (float*)ctx->w_vec[8].p;
-        float* tmp32 = (float*)ctx->w_vec[9].p;
-        const double in2 = o->precision == SGFEM_FP32 ? rtol2 : o->inner_rtol * o->inner_rtol;
-        for (int outer = 0; outer < 64; ++outer) {
-            if (!std::isfinite(rr)) { status = SGFEM_ERR_NONFINITE; break; }
-            if (rr <= rtol2 * bb) break;
-            if (remaining <= 0) { status = SGFEM_ERR_MAXIT; break; }
-            k_demote<<<g, VT, 0, ctx->stream>>>(r, r32, d32, total, partials);
-            SG_LAUNCHED(ctx);
-            // inner target: reduce ||r|| by inner_rtol, but never below what the outer tolerance needs
-            const double want = std::max(in2, 0.25 * rtol2 * bb / rr);
-            SG_TRY(S.fin(g, FIN_TOL, FinArgs{want, 0}, nullptr));
-            int it = 0;
-            int s2 = S.pcg<float>(SGFEM_FP32, d32, r32, p32, q32, tmp32, remaining, check_every, &it);
-            st->iterations += it;
-            st->outer_iterations += 1;
-            remaining -= it;
-            if (s2 == SGFEM_ERR_BREAKDOWN || s2 == SGFEM_ERR_NONFINITE) { status = s2; break; }
-            k_promote_add<<<g, VT, 0, ctx->stream>>>(x64, d32, total);
-            SG_LAUNCHED(ctx);
-            SG_TRY(true_residual(&rr));
-            if (o->precision == SGFEM_FP32) break;  // plain FP32 PCG: no refinement
-        }
+        if (!ctx->batched || status != SGFEM_OK) break;
+        const int S = (int)ctx->P;
+        cr.resize(S);
+        cb.resize(S);
+        double* d_cols = partials;  // S column norms (partials is no longer in use)
+        k_colnorm2<<<S, VT, 0, ctx->stream>>>(r, (int)ctx->n, (int)ctx->ld, d_cols);
+        SG_LAUNCHED(ctx);
+        SG_CUDA(ctx, cudaMemcpyAsync(cr.data(), d_cols, S * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        k_colnorm2<<<S, VT, 0, ctx->stream>>>(b, (int)ctx->n, (int)ctx->ld, d_cols);
+        SG_LAUNCHED(ctx);
+        SG_CUDA(ctx, cudaMemcpyAsync(cb.data(), d_cols, S * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        colmax = 0.0;
+        for (int c = 0; c < S; ++c)
+            if (cb[c] > 0.0) colmax = std::max(colmax, std::sqrt(cr[c] / cb[c]));
+        if (colmax <= o->rtol) break;
+        tol2e = std::min(tol2e, rr / bb) * 0.25 * (o->rtol / colmax) * (o->rtol / colmax);
     }
     SG_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
     SG_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
@@ -507,7 +566,7 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
     SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     st->time_ms = ms;
     st->kernel_launches = ctx->launches - launches0;
-    st->relres = std::sqrt(rr / bb);
+    st->relres = ctx->batched ? colmax : std::sqrt(rr / bb);
     if (status == SGFEM_OK && !(st->relres <= o->rtol)) status = (o->precision == SGFEM_FP32) ? SGFEM_OK : SGFEM_ERR_MAXIT;
     return status_message(ctx, status);
 }
@@ -520,7 +579,7 @@ extern "C" int sgfem_solve_device(sgfem_context* ctx, const double* b0, void* x_
     if (opts) o = *opts; else sgfem_default_options(&o);
     sgfem_solve_stats s{};
     SG_CUDA(ctx, cudaSetDevice(ctx->device));
-    int rc = solve_core(ctx, b0, (double*)x_dev, &o, &s);
+    int rc = solve_core(ctx, b0, (double*)x_dev, &o, &s, 0);
     if (stats) *stats = s;
     return rc;
 }
@@ -534,6 +593,28 @@ extern "C" int sgfem_solve(sgfem_context* ctx, const double* b0, double* x_inout
     SG_TRY(sg_ensure(ctx, ctx->w_vec[10], n64));
     SG_TRY(sgfem_to_device_layout(ctx, x_inout, ctx->w_vec[10].p, SGFEM_FP64));
     int rc = sgfem_solve_device(ctx, b0, ctx->w_vec[10].p, opts, stats);
+    if (rc != SGFEM_OK && rc != SGFEM_ERR_MAXIT) return rc;
+    std::string keep = ctx->err;
+    int rc2 = sgfem_from_device_layout(ctx, ctx->w_vec[10].p, x_inout, SGFEM_FP64);
+    if (rc2 != SGFEM_OK) return rc2;
+    ctx->err = keep;
+    return rc;
+}
+
+extern "C" int sgfem_solve_samples(sgfem_context* ctx, const double* b0, double* x_inout,
+                                   const sgfem_solve_options* opts, sgfem_solve_stats* stats) {
+    SG_TRY(sg_check_ready(ctx));
+    if (!ctx->batched) return sg_fail(ctx, SGFEM_ERR_STATE, "sgfem_solve_samples needs a context set up with sgfem_set_samples");
+    if (!b0 || !x_inout) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "null pointer");
+    sgfem_solve_options o;
+    if (opts) o = *opts; else sgfem_default_options(&o);
+    SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t n64 = sg_vec_bytes(ctx, SGFEM_FP64);
+    SG_TRY(sg_ensure(ctx, ctx->w_vec[10], n64));
+    SG_TRY(sgfem_to_device_layout(ctx, x_inout, ctx->w_vec[10].p, SGFEM_FP64));
+    sgfem_solve_stats s{};
+    int rc = solve_core(ctx, b0, (double*)ctx->w_vec[10].p, &o, &s, 1);
+    if (stats) *stats = s;
     if (rc != SGFEM_OK && rc != SGFEM_ERR_MAXIT) return rc;
     std::string keep = ctx->err;
     int rc2 = sgfem_from_device_layout(ctx, ctx->w_vec[10].p, x_inout, SGFEM_FP64);

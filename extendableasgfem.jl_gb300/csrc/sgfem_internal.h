@@ -64,6 +64,10 @@ struct sgfem_context {
     std::vector<int64_t> G_colptr, G_rowval;
     std::vector<double> G_val;
     bool has_G = false;
+    bool batched = false;        // block-diagonal sample operator (sgfem_set_samples)
+    std::vector<double> ysamp;   // M x S
+    double* d_y64 = nullptr;     // [S][M1] coefficients, y_{s,0} = 1
+    float* d_y32 = nullptr;
     std::vector<int64_t> bdofs;  // 0-based caller numbering
     bool has_bdofs = false;
     std::vector<double> dof_xy;  // 2 x n column-major

@@ -143,6 +143,22 @@ SGFEM_API int sgfem_time_apply(sgfem_context* ctx, int precision, int reps, doub
 /* the same for the lattice preconditioner (three passes per application) */
 SGFEM_API int sgfem_time_precondition(sgfem_context* ctx, int precision, int reps, double* ms_per_application);
 /*
+ * Batched deterministic sample problems, deterministic_problem(problem, C, y_s)
+ * + ExtendableFEM.solve (src/modelproblems/poisson_primal.jl:14-35,
+ * src/sampling_error.jl:118-128): -div(a(y_s) grad u_s) = f, homogeneous
+ * Dirichlet data, s = 1..S, a(y) = a_0 + sum_{m<=M} y_m a_m.  Instead of
+ * sgfem_set_coupling, a context gets the samples (y: M x S, column-major) and
+ * K_0..K_M of the deterministic space; its operator is then block diagonal,
+ * column s holding K_0 + sum_m y_{s,m} K_m, and the SG entry points (apply,
+ * preconditioner, solve) act on n x S vectors.  sgfem_solve_samples solves all
+ * S problems with b0 in every column and reports the largest per-sample
+ * relative residual in stats->relres.
+ */
+SGFEM_API int sgfem_set_samples(sgfem_context* ctx, int64_t S, int64_t M, const double* y);
+SGFEM_API int sgfem_solve_samples(sgfem_context* ctx, const double* b0, double* x_inout,
+                                  const sgfem_solve_options* opts, sgfem_solve_stats* stats);
+
+/*
  * Residual error estimator, estimate(::Type{PoissonProblemPrimal}, sol, C; rhs,
  * bonus_quadorder, tail_extension), src/estimate.jl:260-418.  The caller (the
  * host layer, which also runs the integer work add_boundary_modes /
