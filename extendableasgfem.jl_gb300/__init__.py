@@ -15,7 +15,7 @@ from .mopcontrol import (add_boundary_modes, classify_modes, generate_multiindic
                          prepare_multi_indices, stochastic_marking, top_weight_multiindices,
                          total_degree_multiindices)
 from .orthopolys import HermitePolynomials, LegendrePolynomials, ONBasis
-from .sampling_error import SampleProblems
+from .sampling_error import SampleProblems, calculate_sampling_error, evaluate_samples
 from .sgfevector import SGFEVector
 from .tensorizedbasis import TensorizedBasis, coupling_matrix
 
@@ -25,5 +25,6 @@ __all__ = [
     "unit_square_mesh", "AbstractModelProblem", "PoissonProblemPrimal", "SGOperator", "assemble", "solve",
     "add_boundary_modes", "classify_modes", "generate_multiindices", "get_neighbours", "prepare_multi_indices",
     "stochastic_marking", "top_weight_multiindices", "total_degree_multiindices", "HermitePolynomials",
-    "LegendrePolynomials", "ONBasis", "SampleProblems", "SGFEVector", "TensorizedBasis", "coupling_matrix",
+    "LegendrePolynomials", "ONBasis", "SampleProblems", "calculate_sampling_error", "evaluate_samples",
+    "SGFEVector", "TensorizedBasis", "coupling_matrix",
 ]

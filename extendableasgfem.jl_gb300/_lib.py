@@ -75,6 +75,9 @@ SIGNATURES = {
     "sgfem_estimate_primal": (ctypes.c_int, [_P, _DP, _P, _P, _DP, _P, _P, _DP, _DP]),
     "sgfem_set_samples": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int64, _DP]),
     "sgfem_solve_samples": (ctypes.c_int, [_P, _DP, _DP, ctypes.POINTER(SolveOptions), ctypes.POINTER(SolveStats)]),
+    "sgfem_evaluate_samples": (ctypes.c_int, [_P, _DP, ctypes.c_int64, _P, _DP, ctypes.c_int64, ctypes.c_int64,
+                                              ctypes.c_int64, _DP]),
+    "sgfem_sampling_error": (ctypes.c_int, [_P, _DP, _P, _P, _DP, _P, _P, _DP, _DP]),
     "sgfem_precondition_device_static": (ctypes.c_int, [_P, _P, _P, ctypes.c_int]),
     "sgfem_apply_variant": (ctypes.c_int, [_P]),
     "sgfem_apply_variant_log": (ctypes.c_char_p, [_P]),
@@ -178,11 +181,14 @@ class Context:
         self.P = S
 
     def solve_samples(self, b0, x_inout, options=None, allow_maxit=False):
+        """x_inout None: zero start, solutions stay on the device."""
         b0 = np.ascontiguousarray(b0, dtype=np.float64)
-        assert x_inout.dtype == np.float64 and x_inout.flags.c_contiguous
+        if x_inout is not None:
+            assert x_inout.dtype == np.float64 and x_inout.flags.c_contiguous
         o = options if options is not None else self.default_options()
         st = SolveStats()
-        self._check(self.lib.sgfem_solve_samples(self.h, _dp(b0), _dp(x_inout), ctypes.byref(o), ctypes.byref(st)),
+        xp = _dp(x_inout) if x_inout is not None else None
+        self._check(self.lib.sgfem_solve_samples(self.h, _dp(b0), xp, ctypes.byref(o), ctypes.byref(st)),
                     allow=(ERR_MAXIT,) if allow_maxit else ())
         return st
 

@@ -164,14 +164,23 @@ extern "C" int sgfem_set_coupling(sgfem_context* ctx, int64_t P, int64_t M, cons
     return SGFEM_OK;
 }
 
+static int upload_samples(sgfem_context* ctx);
+
 extern "C" int sgfem_set_samples(sgfem_context* ctx, int64_t S, int64_t M, const double* y) {
     if (!ctx) return SGFEM_ERR_ARGUMENT;
-    SG_TRY(invalidate(ctx));
     if (S <= 0 || S > 32767 || M < 0 || M > 4095 || (M > 0 && !y))
         return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "sgfem_set_samples: bad sizes (S <= 32767, M <= 4095)");
+    for (int64_t t = 0; t < M * S; ++t)
+        if (!std::isfinite(y[t])) return sg_fail(ctx, SGFEM_ERR_NONFINITE, "non-finite sample");
+    if (ctx->finalized) {
+        // next batch of the same shape
+        if (!ctx->batched || S != ctx->P || M != ctx->M)
+            return sg_fail(ctx, SGFEM_ERR_STATE, "finalized context: new samples need the same S and M of a samples context");
+        ctx->ysamp.assign(y, y + M * S);
+        SG_CUDA(ctx, cudaSetDevice(ctx->device));
+        return upload_samples(ctx);
+    }
     ctx->ysamp.assign(y, y + M * S);
-    for (double v : ctx->ysamp)
-        if (!std::isfinite(v)) return sg_fail(ctx, SGFEM_ERR_NONFINITE, "non-finite sample");
     ctx->P = S;
     ctx->M = M;
     ctx->batched = true;
@@ -312,6 +321,28 @@ static int upload(sgfem_context* ctx, T** dst, const T* src, size_t count) {
     return SGFEM_OK;
 }
 
+// per-sample coefficient rows [S][M1], y_{s,0} = 1, to d_y64 / d_y32 (allocated on first use)
+static int upload_samples(sgfem_context* ctx) {
+    const int64_t S = ctx->P, M = ctx->M, M1 = M + 1;
+    std::vector<double> y64((size_t)S * M1);
+    std::vector<float> y32((size_t)S * M1);
+    for (int64_t sidx = 0; sidx < S; ++sidx) {
+        y64[(size_t)sidx * M1] = 1.0;
+        for (int64_t m = 1; m <= M; ++m) y64[(size_t)sidx * M1 + m] = ctx->ysamp[(size_t)sidx * M + (m - 1)];
+    }
+    for (size_t t = 0; t < y64.size(); ++t) y32[t] = (float)y64[t];
+    if (!ctx->d_y64) {
+        SG_TRY(upload(ctx, &ctx->d_y64, y64.data(), y64.size()));
+        SG_TRY(upload(ctx, &ctx->d_y32, y32.data(), y32.size()));
+    } else {
+        SG_CUDA(ctx, cudaMemcpy(ctx->d_y64, y64.data(), y64.size() * sizeof(double), cudaMemcpyHostToDevice));
+        SG_CUDA(ctx, cudaMemcpy(ctx->d_y32, y32.data(), y32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    ctx->samples_x_valid = false;
+    return SGFEM_OK;
+}
+
+
 extern "C" int sgfem_finalize(sgfem_context* ctx) {
     if (!ctx) return SGFEM_ERR_ARGUMENT;
     SG_TRY(invalidate(ctx));
@@ -430,15 +461,7 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
         ctx->mode_of_col = ident;
         ctx->imode = ident;
         SG_TRY(upload(ctx, &ctx->d_mode_of_col, ident.data(), ident.size()));
-        std::vector<double> y64((size_t)P * ctx->M1);
-        std::vector<float> y32((size_t)P * ctx->M1);
-        for (int64_t sidx = 0; sidx < P; ++sidx) {
-            y64[(size_t)sidx * ctx->M1] = 1.0;
-            for (int64_t m = 1; m <= M; ++m) y64[(size_t)sidx * ctx->M1 + m] = ctx->ysamp[(size_t)sidx * M + (m - 1)];
-        }
-        for (size_t t = 0; t < y64.size(); ++t) y32[t] = (float)y64[t];
-        SG_TRY(upload(ctx, &ctx->d_y64, y64.data(), y64.size()));
-        SG_TRY(upload(ctx, &ctx->d_y32, y32.data(), y32.size()));
+        SG_TRY(upload_samples(ctx));
         ctx->Qn = 0;
     } else {
     // ---- coupling structure from G ((M*P) x P, CSC): entry (row = m'*P + mu, col = nu), m = m'+1

@@ -24,6 +24,7 @@
 #include <string>
 #include <vector>
 
+#include "fe_basis.cuh"
 #include "sgfem_internal.h"
 
 namespace {
@@ -63,23 +64,7 @@ __device__ __forceinline__ void p2_laplacians(const double* g, double* lap) {
         lap[3 + e] = 8.0 * (g[2 * ea[e]] * g[2 * eb[e]] + g[2 * ea[e] + 1] * g[2 * eb[e] + 1]);
 }
 
-// gradients of the local basis at barycentric lam
-__device__ __forceinline__ void basis_grad(int order, const double* g, const double* lam, double* out) {
-    if (order == 1) {
-        for (int i = 0; i < 6; ++i) out[i] = g[i];
-        return;
-    }
-    const int ea[3] = {0, 1, 2}, eb[3] = {1, 2, 0};
-    for (int i = 0; i < 3; ++i) {
-        out[2 * i] = (4.0 * lam[i] - 1.0) * g[2 * i];
-        out[2 * i + 1] = (4.0 * lam[i] - 1.0) * g[2 * i + 1];
-    }
-    for (int e = 0; e < 3; ++e) {
-        const int a = ea[e], b = eb[e];
-        out[6 + 2 * e] = 4.0 * (lam[a] * g[2 * b] + lam[b] * g[2 * a]);
-        out[6 + 2 * e + 1] = 4.0 * (lam[a] * g[2 * b + 1] + lam[b] * g[2 * a + 1]);
-    }
-}
+using sgfem_fe::basis_grad;
 
 struct EstArgs {
     int order, nd, nq, nqf, P, Pext, ncells, nfaces, ld;

@@ -591,6 +591,7 @@ extern "C" int sgfem_solve(sgfem_context* ctx, const double* b0, double* x_inout
     SG_CUDA(ctx, cudaSetDevice(ctx->device));
     const size_t n64 = sg_vec_bytes(ctx, SGFEM_FP64);
     SG_TRY(sg_ensure(ctx, ctx->w_vec[10], n64));
+    ctx->samples_x_valid = false;
     SG_TRY(sgfem_to_device_layout(ctx, x_inout, ctx->w_vec[10].p, SGFEM_FP64));
     int rc = sgfem_solve_device(ctx, b0, ctx->w_vec[10].p, opts, stats);
     if (rc != SGFEM_OK && rc != SGFEM_ERR_MAXIT) return rc;
@@ -605,17 +606,23 @@ extern "C" int sgfem_solve_samples(sgfem_context* ctx, const double* b0, double*
                                    const sgfem_solve_options* opts, sgfem_solve_stats* stats) {
     SG_TRY(sg_check_ready(ctx));
     if (!ctx->batched) return sg_fail(ctx, SGFEM_ERR_STATE, "sgfem_solve_samples needs a context set up with sgfem_set_samples");
-    if (!b0 || !x_inout) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "null pointer");
+    if (!b0) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "null pointer");
     sgfem_solve_options o;
     if (opts) o = *opts; else sgfem_default_options(&o);
     SG_CUDA(ctx, cudaSetDevice(ctx->device));
     const size_t n64 = sg_vec_bytes(ctx, SGFEM_FP64);
     SG_TRY(sg_ensure(ctx, ctx->w_vec[10], n64));
-    SG_TRY(sgfem_to_device_layout(ctx, x_inout, ctx->w_vec[10].p, SGFEM_FP64));
+    ctx->samples_x_valid = false;
+    if (x_inout)
+        SG_TRY(sgfem_to_device_layout(ctx, x_inout, ctx->w_vec[10].p, SGFEM_FP64));
+    else
+        SG_CUDA(ctx, cudaMemsetAsync(ctx->w_vec[10].p, 0, n64, ctx->stream));
     sgfem_solve_stats s{};
     int rc = solve_core(ctx, b0, (double*)ctx->w_vec[10].p, &o, &s, 1);
     if (stats) *stats = s;
     if (rc != SGFEM_OK && rc != SGFEM_ERR_MAXIT) return rc;
+    ctx->samples_x_valid = rc == SGFEM_OK;
+    if (!x_inout) return rc;
     std::string keep = ctx->err;
     int rc2 = sgfem_from_device_layout(ctx, ctx->w_vec[10].p, x_inout, SGFEM_FP64);
     if (rc2 != SGFEM_OK) return rc2;

@@ -68,6 +68,7 @@ struct sgfem_context {
     std::vector<double> ysamp;   // M x S
     double* d_y64 = nullptr;     // [S][M1] coefficients, y_{s,0} = 1
     float* d_y32 = nullptr;
+    bool samples_x_valid = false;  // w_vec[10] holds the solutions of the current samples
     std::vector<int64_t> bdofs;  // 0-based caller numbering
     bool has_bdofs = false;
     std::vector<double> dof_xy;  // 2 x n column-major

@@ -152,11 +152,15 @@ SGFEM_API int sgfem_time_precondition(sgfem_context* ctx, int precision, int rep
  * column s holding K_0 + sum_m y_{s,m} K_m, and the SG entry points (apply,
  * preconditioner, solve) act on n x S vectors.  sgfem_solve_samples solves all
  * S problems with b0 in every column and reports the largest per-sample
- * relative residual in stats->relres.
+ * relative residual in stats->relres.  After finalize, sgfem_set_samples with
+ * the same S and M replaces the samples (the next batch) without rebuilding
+ * the context.  x_inout = NULL: start from zero and keep the solutions on the
+ * device only (for sgfem_sampling_error).  M <= 64.
  */
 SGFEM_API int sgfem_set_samples(sgfem_context* ctx, int64_t S, int64_t M, const double* y);
 SGFEM_API int sgfem_solve_samples(sgfem_context* ctx, const double* b0, double* x_inout,
                                   const sgfem_solve_options* opts, sgfem_solve_stats* stats);
+
 
 /*
  * Residual error estimator, estimate(::Type{PoissonProblemPrimal}, sol, C; rhs,
@@ -219,6 +223,54 @@ SGFEM_API int sgfem_estimate_primal(sgfem_context* ctx, const double* sol, const
                                     const sgfem_quadrature* quad, const double* f_qp /* nq x ncells */,
                                     const sgfem_cosine* coef, const sgfem_extension* ext, double* eta4modes,
                                     double* eta4cell);
+
+/*
+ * Evaluation of an SG solution at parameter samples and the sampling error.
+ *
+ * sgfem_evaluate_samples: batched set_sample!(SGFEV, y[1:m])
+ * (src/sgfevector.jl:43-69, src/tensorizedbasis.jl:226-252):
+ *   out[:, s] = sum_k Psi_k(y_s) U[:, k],  Psi_k(y) = prod_{d<M} v_d[mu_k[d]],
+ *   v_d[j] = p_j(y_d) / ||p_j|| for d < m and v_d = (1, 0, 0, ...) for d >= m,
+ * p_j from the three-term recurrence (orthogonal_polynomials.jl:63-73).
+ * U: n x P column-major (SGFEVector entries); y: Ms x S column-major, Ms >= m;
+ * out: n x S column-major.  Any finalized context serves (device and stream).
+ *
+ * sgfem_sampling_error: the error integrals of calculate_sampling_error
+ * (src/sampling_error.jl:2-44, :149-191) for a batch of samples,
+ *   errH1[s][m] = sum_T int_T |grad(u_s - u_sg,m(y_s))|^2
+ *   errL2[s][m] = sum_T int_T (u_s - u_sg,m(y_s))^2,    m = 0..basis->M,
+ * with u_sg,m the SG solution evaluated at y_s[1:m] and u_s the deterministic
+ * solution of sample s.  ctx is a samples context (sgfem_set_samples) whose
+ * samples are the y_s; det_solutions = NULL takes the solutions of its last
+ * sgfem_solve_samples from the device, otherwise n_det x S (column-major,
+ * host).  mesh: geometry (coords, cell_nodes, cell_volumes) and the
+ * deterministic space (order, cell_dofs); sg_space: order and cell_dofs of
+ * the SG space on the same cells.  quad: the cell rule (2 * order of the
+ * deterministic space in the reference).  Outputs are (M+1) x S column-major.
+ * The SG part is evaluated with Psi_k at the full sample (m = M); for modes
+ * active at truncation m this differs from the reference's truncated product
+ * only by the factors 1/||p_0|| of the dimensions m..M-1 (1 up to rounding).
+ */
+typedef struct {                   /* TensorizedBasis + ONBasis, src/tensorizedbasis.jl:28-34, onbasis.jl:13-18 */
+    int64_t P;                     /* multi-indices */
+    int64_t M;                     /* their length (maxlength_multiindices) */
+    const int32_t* multi_indices;  /* M x P column-major: entry d of multi-index k at [k * M + d] */
+    int32_t maxorder;              /* highest degree in the multi-indices */
+    const double* recurrence;      /* 3 x maxorder: (a_j, b_j, c_j), p_{j+1} = (a_j + b_j y) p_j - c_j p_{j-1} */
+    const double* norms;           /* maxorder + 1: ||p_j|| */
+} sgfem_sg_basis;
+
+typedef struct {                   /* H1Pk space on the cells of an sgfem_mesh */
+    int order;                     /* 1 or 2 */
+    int64_t ndofs;
+    const int64_t* cell_dofs;      /* nd x ncells, 1-based */
+} sgfem_fe_space;
+
+SGFEM_API int sgfem_evaluate_samples(sgfem_context* ctx, const double* U, int64_t n, const sgfem_sg_basis* basis,
+                                     const double* y, int64_t Ms, int64_t S, int64_t m, double* out);
+SGFEM_API int sgfem_sampling_error(sgfem_context* ctx, const double* det_solutions, const sgfem_mesh* mesh,
+                                   const sgfem_fe_space* sg_space, const double* U, const sgfem_sg_basis* basis,
+                                   const sgfem_quadrature* quad, double* errH1, double* errL2);
 
 /*
  * No counterpart in the reference package.  Applies the mean-based lattice
