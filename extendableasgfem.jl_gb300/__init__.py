@@ -9,8 +9,10 @@ from . import _lib
 from ._lib import FP32, FP64, MIXED, PREC_JACOBI, PREC_LATTICE, PREC_NONE, SGError
 from .coefficients import StochasticCoefficientCosinus
 from .estimate import estimate, extension_couplings
-from .fem import H1Pk, assemble_rhs, assemble_stiffness, line_rule, triangle_rule, unit_square_mesh
-from .modelproblems import AbstractModelProblem, PoissonProblemPrimal, SGOperator, assemble, solve
+from .fem import (H1Pk, assemble_convection, assemble_laplacian, assemble_pce_rhs, assemble_rhs, assemble_stiffness,
+                  line_rule, pce_lambda, triangle_rule, unit_square_mesh)
+from .modelproblems import (AbstractModelProblem, LogTransformedPoissonProblemPrimal, PoissonProblemPrimal, SGOperator,
+                            assemble, solve)
 from .mopcontrol import (add_boundary_modes, classify_modes, generate_multiindices, get_neighbours,
                          prepare_multi_indices, stochastic_marking, top_weight_multiindices,
                          total_degree_multiindices)
@@ -21,8 +23,10 @@ from .tensorizedbasis import TensorizedBasis, coupling_matrix
 
 __all__ = [
     "FP32", "FP64", "MIXED", "PREC_JACOBI", "PREC_LATTICE", "PREC_NONE", "SGError",
-    "StochasticCoefficientCosinus", "estimate", "extension_couplings", "H1Pk", "assemble_rhs", "assemble_stiffness", "line_rule", "triangle_rule",
-    "unit_square_mesh", "AbstractModelProblem", "PoissonProblemPrimal", "SGOperator", "assemble", "solve",
+    "StochasticCoefficientCosinus", "estimate", "extension_couplings", "H1Pk", "assemble_convection",
+    "assemble_laplacian", "assemble_pce_rhs", "assemble_rhs", "assemble_stiffness", "line_rule", "pce_lambda",
+    "triangle_rule", "unit_square_mesh", "AbstractModelProblem", "LogTransformedPoissonProblemPrimal",
+    "PoissonProblemPrimal", "SGOperator", "assemble", "solve",
     "add_boundary_modes", "classify_modes", "generate_multiindices", "get_neighbours", "prepare_multi_indices",
     "stochastic_marking", "top_weight_multiindices", "total_degree_multiindices", "HermitePolynomials",
     "LegendrePolynomials", "ONBasis", "SampleProblems", "calculate_sampling_error", "evaluate_samples",

@@ -75,6 +75,8 @@ SIGNATURES = {
     "sgfem_estimate_primal": (ctypes.c_int, [_P, _DP, _P, _P, _DP, _P, _P, _DP, _DP]),
     "sgfem_set_samples": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int64, _DP]),
     "sgfem_solve_samples": (ctypes.c_int, [_P, _DP, _DP, ctypes.POINTER(SolveOptions), ctypes.POINTER(SolveStats)]),
+    "sgfem_solve_gmres": (ctypes.c_int, [_P, _DP, _DP, ctypes.POINTER(SolveOptions), ctypes.c_int,
+                                         ctypes.POINTER(SolveStats)]),
     "sgfem_evaluate_samples": (ctypes.c_int, [_P, _DP, ctypes.c_int64, _P, _DP, ctypes.c_int64, ctypes.c_int64,
                                               ctypes.c_int64, _DP]),
     "sgfem_sampling_error": (ctypes.c_int, [_P, _DP, _P, _P, _DP, _P, _P, _DP, _DP]),
@@ -245,6 +247,17 @@ class Context:
         return st
 
     # ---- device-resident operations (pointers are integers, e.g. torch tensor.data_ptr())
+    def solve_gmres(self, b0_full, x_inout, options=None, restart=20, allow_maxit=False):
+        """b0_full: n*P right-hand side blocks (mode-major), x_inout: warm start / solution."""
+        b0 = np.ascontiguousarray(b0_full, dtype=np.float64)
+        assert x_inout.dtype == np.float64 and x_inout.flags.c_contiguous
+        o = options if options is not None else self.default_options()
+        st = SolveStats()
+        self._check(self.lib.sgfem_solve_gmres(self.h, _dp(b0), _dp(x_inout), ctypes.byref(o), int(restart),
+                                               ctypes.byref(st)),
+                    allow=(ERR_MAXIT,) if allow_maxit else ())
+        return st
+
     def apply_device(self, x_ptr, y_ptr, precision=FP64):
         self._check(self.lib.sgfem_apply_device(self.h, _P(x_ptr), _P(y_ptr), int(precision)))
 

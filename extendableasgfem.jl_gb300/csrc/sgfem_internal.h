@@ -139,6 +139,8 @@ struct sgfem_context {
     DeviceBuf w_stage;         // host-layout staging (n*P doubles)
     DeviceBuf w_vec[SG_NBUF];  // SG vectors
     DeviceBuf w_partials;      // per-block reduction partials (double)
+    DeviceBuf w_basis;         // GMRES Krylov basis (restart + 1 vectors)
+    DeviceBuf w_gsmall;        // GMRES multi-dot partials and coefficients
     KrylovScalars* d_scal = nullptr;
     KrylovScalars* h_scal = nullptr;  // pinned
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;

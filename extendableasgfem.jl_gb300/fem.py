@@ -205,3 +205,86 @@ def assemble_rhs(space, f, quadorder):
         v, _, _ = space.basis(lam)
         np.add.at(b, space.celldofs, (wts[q] * vol * fx[:, q])[:, None] * v[None, :])
     return b
+
+
+def assemble_laplacian(space, quadorder=None):
+    """A = (grad u, grad v) (logpoisson_primal.jl:97-99)."""
+    class _One:
+        mean_value = 1.0
+
+        @staticmethod
+        def get_am(x1, x2, m):
+            return np.ones(np.shape(x1))
+    q = 2 * (space.order - 1) if quadorder is None else quadorder
+    return assemble_stiffness(space, _One, [0], q)[0]
+
+
+def assemble_convection(space, coef, ms, quadorder):
+    """[N_m for m in ms], N_m[i, j] = -(grad a_m . grad phi_j, phi_i) on the shared
+    CSR pattern (logpoisson_primal.jl:101-107: test function id, ansatz grad)."""
+    pts, wts = triangle_rule(quadorder)
+    X = space.physical_points(pts)
+    vol = space.mesh.cell_volumes
+    nd = space.ndofs4cell
+    nc = space.mesh.ncells
+    VG = []
+    for q in range(len(wts)):
+        lam = np.array([1 - pts[q, 0] - pts[q, 1], pts[q, 0], pts[q, 1]])
+        v, g, _ = space.basis(lam)
+        VG.append((v, g))
+    indptr, col, inv = space.pattern()
+    n = space.ndofs
+    out = []
+    for m in ms:
+        gx, gy = coef.get_gradam(X[..., 0], X[..., 1], m)  # nc x nq
+        loc = np.zeros((nc, nd, nd))
+        for q in range(len(wts)):
+            v, g = VG[q]
+            conv = gx[:, q, None] * g[:, :, 0] + gy[:, q, None] * g[:, :, 1]  # nc x nd (ansatz j)
+            loc -= (wts[q] * vol)[:, None, None] * v[None, :, None] * conv[:, None, :]
+        data = np.bincount(inv, weights=loc.ravel(), minlength=len(col))
+        out.append(sp.csr_matrix((data, col, indptr), shape=(n, n)))
+    return out
+
+
+def pce_lambda(coef, multi_indices, x1, x2, factor=-1.0, N_truncate=None):
+    """lambda_mu(x) of exp(factor * a) = sum_mu lambda_mu H_mu (coefficients.jl:219-260):
+    exp(sum_{m<=N} a_m^2 / 2) exp(factor a_0) prod_d a_d^mu_d / (sqrt(prod mu_d!) factor^|mu|).
+    Returns (P,) + x1.shape."""
+    N = coef.maxm() if N_truncate is None else N_truncate
+    x1 = np.asarray(x1, dtype=np.float64)
+    x2 = np.asarray(x2, dtype=np.float64)
+    s = np.zeros(x1.shape)
+    for m in range(1, N + 1):
+        s = s + coef.get_am(x1, x2, m) ** 2
+    s = np.exp(s / 2) * math.exp(coef.meanvalue() * factor)
+    M = max(len(mi) for mi in multi_indices)
+    am = [coef.get_am(x1, x2, d) for d in range(1, M + 1)]
+    out = np.empty((len(multi_indices),) + x1.shape)
+    for k, mi in enumerate(multi_indices):
+        a = np.ones(x1.shape)
+        fac = 1
+        for d, e in enumerate(mi):
+            a = a * am[d] ** e
+            fac *= math.factorial(e)
+        out[k] = a / (math.sqrt(fac) * factor ** sum(mi)) * s
+    return out
+
+
+def assemble_pce_rhs(space, coef, multi_indices, f, quadorder, factor=-1.0, N_truncate=None):
+    """b_mu = (lambda_mu f, v) for every multi-index (logpoisson_primal.jl:109-131);
+    returns the n x P blocks flattened mode-major (SGFEVector layout)."""
+    pts, wts = triangle_rule(quadorder)
+    X = space.physical_points(pts)
+    vol = space.mesh.cell_volumes
+    lam_mu = pce_lambda(coef, multi_indices, X[..., 0], X[..., 1], factor, N_truncate)  # P x nc x nq
+    fx = np.broadcast_to(np.asarray(f(X[..., 0], X[..., 1]), dtype=np.float64), X.shape[:2])
+    P = len(multi_indices)
+    n = space.ndofs
+    b = np.zeros((P, n))
+    for q in range(len(wts)):
+        lam = np.array([1 - pts[q, 0] - pts[q, 1], pts[q, 0], pts[q, 1]])
+        v, _, _ = space.basis(lam)
+        for k in range(P):
+            np.add.at(b[k], space.celldofs, (wts[q] * vol * lam_mu[k][:, q] * fx[:, q])[:, None] * v[None, :])
+    return b.ravel()

@@ -8,6 +8,11 @@ Mirrors src/modelproblems/ of ExtendableASGFEM.jl:
   SGOperator                          solvers_poisson_primal.jl:14-124 (MySystemPrimal
                                       + MyPreconditionerPrimal), backed by one libsgfem
                                       context on the GPU: mul / ldiv / solve_primal
+  LogTransformedPoissonProblemPrimal  logpoisson_primal.jl:85-153: A = (grad u, grad v),
+                                      N_m = -(grad a_m . grad u, v), b_mu = (lambda_mu f, v);
+                                      MySystemLogPrimal (solvers_logpoisson_primal.jl:14-127)
+                                      is the same SGOperator with K_0 = A, K_m = N_m, solved
+                                      by solve_logpoisson (device GMRES)
 All arithmetic of mul!, ldiv! and the Krylov solve runs in the CUDA library;
 this module only assembles the spatial blocks (the caller's side of the
 boundary, ExtendableFEM in the reference) and moves arrays across the C ABI.
@@ -15,7 +20,7 @@ boundary, ExtendableFEM in the reference) and moves arrays across the C ABI.
 import numpy as np
 
 from . import _lib
-from .fem import assemble_rhs, assemble_stiffness
+from .fem import assemble_convection, assemble_laplacian, assemble_pce_rhs, assemble_rhs, assemble_stiffness
 
 
 class AbstractModelProblem:
@@ -24,6 +29,11 @@ class AbstractModelProblem:
 
 class PoissonProblemPrimal(AbstractModelProblem):
     """-div(a(y, x) grad u) = f with the affine coefficient a = a_0 + sum_m y_m a_m."""
+
+
+class LogTransformedPoissonProblemPrimal(AbstractModelProblem):
+    """-div(exp(a) grad u) = f, solved in the transformed form
+    -Laplace u - grad a . grad u = exp(-a) f (logpoisson_primal.jl:1-13), a = sum_m y_m a_m."""
 
 
 class SGOperator:
@@ -70,19 +80,35 @@ class SGOperator:
                                      check_every=check_every)
         return self.ctx.solve(b0, x, o, allow_maxit=allow_maxit).as_dict()
 
+    def solve_logpoisson(self, b_full, x, rtol=1e-12, precision=_lib.FP64, preconditioner=None, maxit=5000,
+                         inner_rtol=1e-5, reference_rhs=True, restart=20, allow_maxit=False):
+        """solve_logpoisson_primal!: GMRES for the non-symmetric operator; b_full holds
+        the n x P right-hand side blocks, x the warm start (receives the solution)."""
+        if preconditioner is None:
+            preconditioner = _lib.PREC_LATTICE if self.has_lattice else _lib.PREC_JACOBI
+        o = self.ctx.default_options(precision=precision, preconditioner=preconditioner, rtol=rtol, maxit=maxit,
+                                     inner_rtol=inner_rtol, reference_rhs=1 if reference_rhs else 0)
+        return self.ctx.solve_gmres(b_full, x, o, restart=restart, allow_maxit=allow_maxit).as_dict()
+
     def close(self):
         self.ctx.close()
 
 
 def assemble(problem, sol, C, rhs, bonus_quadorder_a=2, bonus_quadorder_f=0):
-    """Spatial blocks of poisson_primal.jl:55-68: [K_0..K_M], b."""
-    if problem is not PoissonProblemPrimal:
+    """Spatial blocks: poisson_primal.jl:55-68 ([K_0..K_M], b = (f, v)) or
+    logpoisson_primal.jl:97-131 ([A, N_1..N_M], b_mu = (lambda_mu f, v) for all modes)."""
+    if problem is not PoissonProblemPrimal and problem is not LogTransformedPoissonProblemPrimal:
         raise NotImplementedError(f"no assembly for {problem}")
     if rhs is None:
         raise ValueError("need right-hand side")
     FES = sol.FES_space[0]
     p = FES.order
     M = sol.TB.maxlength_multiindices()
+    if problem is LogTransformedPoissonProblemPrimal:
+        A = assemble_laplacian(FES)
+        Ns = assemble_convection(FES, C, list(range(1, M + 1)), p + (p - 1) + bonus_quadorder_a)
+        b = assemble_pce_rhs(FES, C, [sol.TB.multi_indices[k] for k in sol.active_modes], rhs, p + bonus_quadorder_f)
+        return [A] + Ns, b
     Ks = assemble_stiffness(FES, C, list(range(M + 1)), 2 * (p - 1) + bonus_quadorder_a)
     b0 = assemble_rhs(FES, rhs, p + bonus_quadorder_f)
     return Ks, b0
@@ -100,7 +126,10 @@ def solve(problem, sol, C, rhs=None, bonus_quadorder_a=2, bonus_quadorder_f=0, u
     Ks, b0 = assemble(problem, sol, C, rhs, bonus_quadorder_a, bonus_quadorder_f)
     op = SGOperator(sol.FES_space[0], sol.TB, Ks, device=device)
     try:
-        stats = op.solve_primal(b0, sol.entries, **solver_kwargs)
+        if problem is LogTransformedPoissonProblemPrimal:
+            stats = op.solve_logpoisson(b0, sol.entries, **solver_kwargs)
+        else:
+            stats = op.solve_primal(b0, sol.entries, **solver_kwargs)
     finally:
         op.close()
     sol.solve_stats = stats

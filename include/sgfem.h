@@ -124,6 +124,22 @@ SGFEM_API int sgfem_solve(sgfem_context* ctx, const double* b0, double* x_inout,
 SGFEM_API void sgfem_default_options(sgfem_solve_options* opts);
 
 /*
+ * solve_logpoisson_primal!(sol, A, N0, Nm, b0, G, nmodes, bfac),
+ * src/modelproblems/solvers_logpoisson_primal.jl:130-172: the same SG operator
+ * structure with non-symmetric blocks (K_0 = A + N_0, K_m = N_m =
+ * -(grad a_m . grad u, v) of LogTransformedPoissonProblemPrimal, set with
+ * sgfem_set_spatial_matrix).  b0 is n x P column-major (the assembled
+ * (lambda_mu f, v) of every mode); b = x0 + b0 (reference_rhs = 1, as :149-155)
+ * or b0, Dirichlet rows zeroed.  Right-preconditioned restarted GMRES(restart)
+ * (restart <= 0: 20, the Krylov.jl default memory) with the mean-based
+ * preconditioner opts->preconditioner, stopping on ||b - A x|| <= rtol ||b||
+ * (FP64 true residual).  SGFEM_MIXED: FP32 GMRES to inner_rtol inside FP64
+ * iterative refinement.  Also valid for symmetric operators.
+ */
+SGFEM_API int sgfem_solve_gmres(sgfem_context* ctx, const double* b0, double* x_inout,
+                                const sgfem_solve_options* opts, int restart, sgfem_solve_stats* stats);
+
+/*
  * Device-resident variants for callers that keep SG vectors on the GPU.  Vectors
  * are in the device layout: n_dev rows (device dof order) x ld columns, row-major,
  * where sgfem_device_layout() reports n_dev, ld and the element size.

@@ -73,3 +73,21 @@ class StochasticCoefficientCosinus:
         for m in range(1, len(y) + 1):
             r = r + y[m - 1] * self.get_am(x1, x2, m)
         return r
+
+
+def pce_lambda(coef, mu, x1, x2, factor=-1.0, N_truncate=None):
+    """lambda_mu(x) of expa_PCE_mop (src/coefficients/coefficients.jl:219-260), one
+    point, one multi-index: the Hermite chaos coefficient of exp(factor a(x, y)),
+    exp(sum_{m<=N} a_m(x)^2 / 2) exp(a_0 factor) prod_d a_d(x)^mu_d / (sqrt(prod_d mu_d!) factor^|mu|)."""
+    N = coef.maxm() if N_truncate is None else N_truncate
+    s = 0.0
+    for m in range(1, N + 1):
+        s += float(coef.get_am(x1, x2, m)) ** 2
+    s = math.exp(s / 2) * math.exp(coef.mean_value * factor)
+    amu = 1.0
+    fac = 1
+    for d, e in enumerate(mu):
+        amu *= float(coef.get_am(x1, x2, d + 1)) ** e
+        fac *= math.factorial(e)
+    amu /= math.sqrt(fac) * factor ** sum(mu)
+    return amu * s

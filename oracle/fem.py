@@ -199,3 +199,61 @@ def assemble_rhs(space, f, quadorder):
             v, _, _ = space.local_basis(lam, gl)
             b[space.celldofs[c]] += wts[q] * vol * f(x[0], x[1]) * v
     return b
+
+
+def assemble_convection(space, coef, ms, quadorder):
+    """N_m = -(grad a_m . grad u, v), test function v = phi_i (row), ansatz
+    u = phi_j (column): src/modelproblems/logpoisson_primal.jl:101-107
+    (BilinearOperator(get_gradam_x_sigma, [id(1)], [grad(1)]; factor = -1))."""
+    pts, wts = triangle_rule(quadorder)
+    nd = space.ndofs4cell()
+    rows, cols = [], []
+    vals = {m: [] for m in ms}
+    for c in range(space.mesh.ncells):
+        p, J, gl = space.cell_geometry(c)
+        vol = space.mesh.cell_volumes[c]
+        loc = {m: np.zeros((nd, nd)) for m in ms}
+        for q in range(len(wts)):
+            xi, eta = pts[q]
+            lam = np.array([1 - xi - eta, xi, eta])
+            x = p[0] + J @ np.array([xi, eta])
+            v, g, _ = space.local_basis(lam, gl)
+            for m in ms:
+                ga = np.array([float(t) for t in coef.get_gradam(x[0], x[1], m)])
+                loc[m] -= wts[q] * vol * np.outer(v, g @ ga)
+        dofs = space.celldofs[c]
+        for a_ in range(nd):
+            for b_ in range(nd):
+                rows.append(dofs[a_])
+                cols.append(dofs[b_])
+        for m in ms:
+            vals[m].extend(loc[m].ravel().tolist())
+    n = space.ndofs
+    out = []
+    for m in ms:
+        K = sp.coo_matrix((np.array(vals[m]), (np.array(rows), np.array(cols))), shape=(n, n)).tocsr()
+        K.sum_duplicates()
+        K.sort_indices()
+        out.append(K)
+    return out
+
+
+def assemble_pce_rhs(space, coef, multi_indices, f, quadorder, factor=-1.0, N_truncate=None):
+    """b_mu = (lambda_mu f, v) (logpoisson_primal.jl:109-131), mode-major n*P."""
+    from .coefficient import pce_lambda
+    pts, wts = triangle_rule(quadorder)
+    P = len(multi_indices)
+    b = np.zeros((P, space.ndofs))
+    for c in range(space.mesh.ncells):
+        p, J, gl = space.cell_geometry(c)
+        vol = space.mesh.cell_volumes[c]
+        for q in range(len(wts)):
+            xi, eta = pts[q]
+            lam = np.array([1 - xi - eta, xi, eta])
+            x = p[0] + J @ np.array([xi, eta])
+            v, _, _ = space.local_basis(lam, gl)
+            fx = f(x[0], x[1])
+            for k in range(P):
+                b[k, space.celldofs[c]] += wts[q] * vol * pce_lambda(coef, multi_indices[k], x[0], x[1], factor,
+                                                                     N_truncate) * fx * v
+    return b.ravel()

@@ -203,3 +203,34 @@ def interior_mask(n, P, bdofs):
     for mu in range(P):
         m[mu * n + bdofs] = False
     return m
+
+
+def kron_direct_full(K0, Ks, G, b_full, bdofs, P, gtol=1e-12):
+    """solve_logpoisson_primal_full!, solvers_logpoisson_primal.jl:175-233 (small
+    cases): the assembled SG matrix with A + N_0 on the diagonal blocks, g N_e for
+    |g| > 1e-12, 1e60 on boundary diagonals; right-hand side blocks b_mu with
+    boundary entries zeroed."""
+    n = K0.shape[0]
+    M = len(Ks)
+    blocks = [[None] * P for _ in range(P)]
+    for j in range(P):
+        blocks[j][j] = K0.copy().tolil()
+    for j in range(P):
+        for k in range(P):
+            for e in range(M):
+                g = G[e * P + j, k]
+                if abs(g) > gtol:
+                    add = g * Ks[e]
+                    blocks[j][k] = (add if blocks[j][k] is None else blocks[j][k] + add)
+    for j in range(P):
+        for k in range(P):
+            if blocks[j][k] is not None:
+                blocks[j][k] = sp.lil_matrix(blocks[j][k])
+    for m in range(P):
+        for d in bdofs:
+            blocks[m][m][d, d] = 1.0e60
+    S = sp.bmat(blocks, format="csc")
+    rhs = np.array(b_full, dtype=np.float64).copy()
+    for m in range(P):
+        rhs[m * n + bdofs] = 0.0
+    return spla.spsolve(S, rhs)

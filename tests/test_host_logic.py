@@ -165,3 +165,30 @@ def test_top_weight_set_config2_tie(pkg):
                 assert tuple(t) in s
     G = pkg.coupling_matrix(pkg.LegendrePolynomials, mis)
     assert G.nnz == 560
+
+
+def test_lognormal_assembly_matches_oracle(pkg):
+    """A, N_m = -(grad a_m . grad u, v) and b_mu = (lambda_mu f, v) of the host
+    assembly against the oracle's element loops (logpoisson_primal.jl:97-131)."""
+    from oracle import coefficient as oc
+    from oracle import fem as of
+    for order in (1, 2):
+        V = pkg.H1Pk(pkg.unit_square_mesh(4), order)
+        C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=0.0, maxm=6)
+        Co = oc.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=0.0, maxm=6)
+        Vo = of.LagrangeSpace(of.StructuredMesh(4), order)
+        q = 2 * order - 1 + 2
+        Ns = pkg.assemble_convection(V, C, [1, 2, 3], q)
+        No = of.assemble_convection(Vo, Co, [1, 2, 3], q)
+        for N, Nr in zip(Ns, No):
+            d = (N - Nr).toarray()
+            assert np.abs(d).max() <= 1e-13 * np.abs(Nr.toarray()).max()
+            assert np.abs((N - N.T).toarray()).max() > 1e-3 * np.abs(Nr.toarray()).max()  # not symmetric
+        A = pkg.assemble_laplacian(V)
+        Ar = of.assemble_stiffness(Vo, type("One", (), {"get_am": staticmethod(lambda x1, x2, m: np.ones_like(np.asarray(x1, dtype=float)))})(), [0], 2 * (order - 1))[0]
+        assert np.abs((A - Ar).toarray()).max() <= 1e-13 * np.abs(Ar.toarray()).max()
+        mis = [[0, 0, 0], [1, 0, 0], [0, 1, 0], [2, 0, 0], [1, 1, 1]]
+        f = lambda x, y: 1.0 + x * 0
+        b = pkg.assemble_pce_rhs(V, C, mis, lambda x, y: np.ones_like(x), order + 1)
+        br = of.assemble_pce_rhs(Vo, Co, mis, f, order + 1)
+        assert np.abs(b - br).max() <= 1e-13 * np.abs(br).max()

@@ -66,3 +66,22 @@ def test_single_mode_is_deterministic_solve():
     u = np.zeros(p.n)
     u[inner] = spla.spsolve(p.K0[inner][:, inner].tocsc(), p.b0[inner])
     assert np.linalg.norm(xk - u) <= 1e-12 * np.linalg.norm(u)
+
+
+def test_pce_lambda_generating_function():
+    """lambda_mu of exp(factor a) (coefficients.jl:219-260) are the normalised
+    Hermite chaos coefficients: sum_mu lambda_mu H_mu(y) -> exp(factor a(x, y))
+    (generating function exp(t y - t^2/2) = sum_k t^k He_k(y) / k!)."""
+    from oracle import basis as ob
+    from oracle import coefficient as oc
+    C = oc.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=0.3, maxm=2)
+    x1, x2 = 0.31, 0.77
+    y = np.array([0.7, -1.3])
+    K = 28
+    mis = [[i, j] for i in range(K + 1) for j in range(K + 1 - i)]
+    TB = ob.TensorizedBasis(ob.HERMITE, 2, K, K, multi_indices=mis)
+    TB.set_sample(list(y))
+    for factor in (-1.0, 1.0):
+        s = sum(oc.pce_lambda(C, mu, x1, x2, factor, N_truncate=2) * TB.evaluate(k) for k, mu in enumerate(mis))
+        a = C.get_a(x1, x2, y)
+        assert abs(s - np.exp(factor * float(a))) <= 1e-11 * np.exp(factor * float(a))
