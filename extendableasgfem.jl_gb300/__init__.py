@@ -7,10 +7,12 @@ The directory name follows the Julia package naming; import it through
 """
 from . import _lib
 from ._lib import FP32, FP64, MIXED, PREC_JACOBI, PREC_LATTICE, PREC_NONE, SGError
+from .adjoint import MeanQoI
 from .coefficients import StochasticCoefficientCosinus
 from .estimate import estimate, extension_couplings
 from .fem import (H1Pk, assemble_convection, assemble_laplacian, assemble_pce_rhs, assemble_rhs, assemble_stiffness,
-                  line_rule, pce_lambda, triangle_rule, unit_square_mesh)
+                  assemble_stiffness_nodal_mean, box_functional, line_rule, pce_lambda, triangle_rule,
+                  unit_square_mesh)
 from .modelproblems import (AbstractModelProblem, LogTransformedPoissonProblemPrimal, PoissonProblemPrimal, SGOperator,
                             assemble, solve)
 from .mopcontrol import (add_boundary_modes, classify_modes, generate_multiindices, get_neighbours,
@@ -22,7 +24,8 @@ from .sgfevector import SGFEVector
 from .tensorizedbasis import TensorizedBasis, coupling_matrix
 
 __all__ = [
-    "FP32", "FP64", "MIXED", "PREC_JACOBI", "PREC_LATTICE", "PREC_NONE", "SGError",
+    "FP32", "FP64", "MIXED", "PREC_JACOBI", "PREC_LATTICE", "PREC_NONE", "SGError", "MeanQoI",
+    "assemble_stiffness_nodal_mean", "box_functional",
     "StochasticCoefficientCosinus", "estimate", "extension_couplings", "H1Pk", "assemble_convection",
     "assemble_laplacian", "assemble_pce_rhs", "assemble_rhs", "assemble_stiffness", "line_rule", "pce_lambda",
     "triangle_rule", "unit_square_mesh", "AbstractModelProblem", "LogTransformedPoissonProblemPrimal",

@@ -77,6 +77,7 @@ SIGNATURES = {
     "sgfem_solve_samples": (ctypes.c_int, [_P, _DP, _DP, ctypes.POINTER(SolveOptions), ctypes.POINTER(SolveStats)]),
     "sgfem_solve_gmres": (ctypes.c_int, [_P, _DP, _DP, ctypes.POINTER(SolveOptions), ctypes.c_int,
                                          ctypes.POINTER(SolveStats)]),
+    "sgfem_adjoint_gradient": (ctypes.c_int, [_P, _DP, _DP, _DP, _P, _DP]),
     "sgfem_evaluate_samples": (ctypes.c_int, [_P, _DP, ctypes.c_int64, _P, _DP, ctypes.c_int64, ctypes.c_int64,
                                               ctypes.c_int64, _DP]),
     "sgfem_sampling_error": (ctypes.c_int, [_P, _DP, _P, _P, _DP, _P, _P, _DP, _DP]),

@@ -631,8 +631,8 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
     if (!ctx->batched) SG_TRY(sg_apply_configure(ctx));
     if (ctx->lattice) SG_TRY(sg_lattice_configure(ctx));
     // specialised FP32 apply; on failure the generic kernel stays in use (reason in the variant log)
-    if (!ctx->batched && sg_jit_build(ctx) != SGFEM_OK) ctx->err.clear();
-    if (ctx->batched) ctx->jit_log = "block-diagonal sample operator";
+    sg_jit_configure(ctx);
+    ctx->jit_log = ctx->batched ? "block-diagonal sample operator" : "not compiled yet (at the first FP32 apply)";
     // host copies of the pattern are no longer needed
     for (auto& A : ctx->mats) {
         A.colptr.clear(); A.colptr.shrink_to_fit();
@@ -754,6 +754,7 @@ extern "C" int sgfem_apply(sgfem_context* ctx, const double* x, double* y, int p
     SG_TRY(check_precision(ctx, precision));
     if (!x || !y) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "null pointer");
     SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (precision == SGFEM_FP32) SG_TRY(sg_jit_ensure(ctx));
     size_t vb = sg_vec_bytes(ctx, precision);
     SG_TRY(sg_ensure(ctx, ctx->w_vec[0], vb));
     SG_TRY(sg_ensure(ctx, ctx->w_vec[1], vb));
@@ -767,6 +768,7 @@ extern "C" int sgfem_apply_device(sgfem_context* ctx, const void* x_dev, void* y
     SG_TRY(check_precision(ctx, precision));
     if (!x_dev || !y_dev) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "null pointer");
     SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (precision == SGFEM_FP32) SG_TRY(sg_jit_ensure(ctx));
     SG_TRY(sg_launch_apply(ctx, precision, x_dev, y_dev, nullptr, nullptr, nullptr));
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return SGFEM_OK;
@@ -777,6 +779,7 @@ extern "C" int sgfem_time_apply(sgfem_context* ctx, int precision, int reps, dou
     SG_TRY(check_precision(ctx, precision));
     if (reps <= 0 || !ms_per_apply) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad reps");
     SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (precision == SGFEM_FP32) SG_TRY(sg_jit_ensure(ctx));
     size_t vb = sg_vec_bytes(ctx, precision);
     SG_TRY(sg_ensure(ctx, ctx->w_vec[0], vb));
     SG_TRY(sg_ensure(ctx, ctx->w_vec[1], vb));

@@ -290,8 +290,10 @@ extern "C" int sgfem_solve_gmres(sgfem_context* ctx, const double* b0, double* x
     const size_t esz = low ? sizeof(float) : sizeof(double);
     for (int i = 0; i < 4; ++i) SG_TRY(sg_ensure(ctx, ctx->w_vec[i], n64));
     SG_TRY(sg_ensure(ctx, ctx->w_vec[10], n64));
-    if (low)
+    if (low) {
         for (int i = 5; i < 10; ++i) SG_TRY(sg_ensure(ctx, ctx->w_vec[i], n32));
+        SG_TRY(sg_jit_ensure(ctx));
+    }
     SG_TRY(sg_ensure(ctx, ctx->w_basis, (size_t)(restart + 1) * total * esz));
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)((total + GT * 4 - 1) / (GT * 4)),
                                                                  (int64_t)ctx->num_sms * 8));

@@ -332,13 +332,10 @@ size_t jit_smem_bytes(const sgfem_context* ctx) {
 
 }  // namespace
 
-int sg_jit_build(sgfem_context* ctx) {
-    ctx->jit_ok = false;
+// knobs are read when the context is finalized (the kernel itself is compiled later)
+void sg_jit_configure(sgfem_context* ctx) {
     const char* env = getenv("SGFEM_APPLY");
-    if (env && std::string(env) == "generic") {
-        ctx->jit_log = "disabled by SGFEM_APPLY=generic";
-        return SGFEM_ERR_UNSUPPORTED;
-    }
+    ctx->jit_disabled = env && std::string(env) == "generic";
     const char* er = getenv("SGFEM_JIT_RCHUNK");
     const char* ep = getenv("SGFEM_JIT_PREFETCH");
     ctx->jit_rchunk = er ? std::max(1, atoi(er)) : 2;
@@ -349,6 +346,14 @@ int sg_jit_build(sgfem_context* ctx) {
     ctx->jit_stage = es ? (atoi(es) != 0) : 1;
     ctx->jit_bps_cap = eb ? std::max(1, atoi(eb)) : 8;
     ctx->jit_carveout = ec ? atoi(ec) : -1;
+}
+
+int sg_jit_build(sgfem_context* ctx) {
+    ctx->jit_ok = false;
+    if (ctx->jit_disabled) {
+        ctx->jit_log = "disabled by SGFEM_APPLY=generic";
+        return SGFEM_ERR_UNSUPPORTED;
+    }
     const int NS = (int)ctx->jit_slots.size();
     if (NS == 0 || NS > 96 || ctx->M1P > 64 || ctx->jit_T <= 0 || ctx->jit_T > 256) {
         ctx->jit_log = "slot count outside the specialised kernel's range";
@@ -456,8 +461,23 @@ void sg_jit_release(sgfem_context* ctx) {
     ctx->jit_ok = false;
 }
 
-extern "C" int sgfem_apply_variant(const sgfem_context* ctx) { return (ctx && ctx->jit_ok) ? 1 : 0; }
+int sg_jit_ensure(sgfem_context* ctx) {
+    if (ctx->jit_tried || ctx->batched || !ctx->finalized) return SGFEM_OK;
+    ctx->jit_tried = true;
+    if (sg_jit_build(ctx) != SGFEM_OK) ctx->err.clear();  // the generic kernel stays in use
+    return SGFEM_OK;
+}
+
+// queries compile the specialised kernel if that has not happened yet
+extern "C" int sgfem_apply_variant(const sgfem_context* ctx) {
+    if (!ctx) return 0;
+    if (ctx->finalized && !ctx->jit_tried && cudaSetDevice(ctx->device) == cudaSuccess)
+        sg_jit_ensure(const_cast<sgfem_context*>(ctx));
+    return ctx->jit_ok ? 1 : 0;
+}
 
 extern "C" const char* sgfem_apply_variant_log(const sgfem_context* ctx) {
-    return ctx ? ctx->jit_log.c_str() : "null context";
+    if (!ctx) return "null context";
+    sgfem_apply_variant(ctx);
+    return ctx->jit_log.c_str();
 }

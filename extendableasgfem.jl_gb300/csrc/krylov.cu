@@ -405,8 +405,10 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
     SG_TRY(sg_ensure(ctx, ctx->w_vec[3], n64));
     SG_TRY(sg_ensure(ctx, ctx->w_vec[4], n64));
     const bool low = o->precision != SGFEM_FP64;
-    if (low)
+    if (low) {
         for (int i = 5; i < 10; ++i) SG_TRY(sg_ensure(ctx, ctx->w_vec[i], n32));
+        SG_TRY(sg_jit_ensure(ctx));
+    }
     const int maxblocks = std::max<int>(ctx->num_sms * 8, ctx->lattice ? (ctx->Nl - 1) * (int)((ctx->ld + 31) / 32) : 1);
     SG_TRY(sg_ensure(ctx, ctx->w_partials, (size_t)(maxblocks + 8) * sizeof(double)));
     double* partials = (double*)ctx->w_partials.p;

@@ -122,6 +122,8 @@ struct sgfem_context {
     void* jit_module = nullptr;             // CUmodule
     void* jit_func = nullptr;               // CUfunction
     bool jit_ok = false;
+    bool jit_tried = false;      // the specialised FP32 apply is compiled at its first use
+    bool jit_disabled = false;   // SGFEM_APPLY=generic at finalize
     int jit_blocks_per_sm = 1;
     std::string jit_log;
 
@@ -186,7 +188,10 @@ void sg_mode_order(const sgfem_context* ctx, const std::vector<std::vector<char>
                    std::vector<int32_t>& mode_of_col);
 // compile the FP32 apply for this coupling structure; returns SGFEM_OK or an error
 // (the generic kernel stays in use then)
+void sg_jit_configure(sgfem_context* ctx);
 int sg_jit_build(sgfem_context* ctx);
+// compile it once, before the first FP32 apply of a context (never inside a graph capture)
+int sg_jit_ensure(sgfem_context* ctx);
 int sg_jit_grid(const sgfem_context* ctx);
 int sg_jit_launch(sgfem_context* ctx, const void* X, void* Y, double* partials, int grid, const KrylovScalars* scal);
 void sg_jit_release(sgfem_context* ctx);

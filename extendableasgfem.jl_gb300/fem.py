@@ -288,3 +288,36 @@ def assemble_pce_rhs(space, coef, multi_indices, f, quadorder, factor=-1.0, N_tr
         for k in range(P):
             np.add.at(b[k], space.celldofs, (wts[q] * vol * lam_mu[k][:, q] * fx[:, q])[:, None] * v[None, :])
     return b.ravel()
+
+
+def assemble_stiffness_nodal_mean(space, alpha, quadorder):
+    """K_0(alpha) = (a_0 grad u, grad v) with the nodal P1 mean field
+    a_0 = sum_i alpha_i phi_i (alpha: one value per mesh node); alpha = 1
+    gives the constant mean 1."""
+    alpha = np.asarray(alpha, dtype=np.float64)
+    mesh = space.mesh
+    if alpha.shape != (mesh.nnodes,):
+        raise ValueError("alpha needs one value per mesh node")
+    pts, wts = triangle_rule(quadorder)
+    vol = mesh.cell_volumes
+    nd = space.ndofs4cell
+    nc = mesh.ncells
+    av = alpha[mesh.cells]  # nc x 3
+    loc = np.zeros((nc, nd, nd))
+    for q in range(len(wts)):
+        lam = np.array([1 - pts[q, 0] - pts[q, 1], pts[q, 0], pts[q, 1]])
+        _, g, _ = space.basis(lam)
+        a0 = av @ lam
+        loc += (wts[q] * vol * a0)[:, None, None] * np.einsum("cik,cjk->cij", g, g)
+    indptr, col, inv = space.pattern()
+    data = np.bincount(inv, weights=loc.ravel(), minlength=len(col))
+    n = space.ndofs
+    return sp.csr_matrix((data, col, indptr), shape=(n, n))
+
+
+def box_functional(space, box, quadorder=None):
+    """l_i = int_box phi_i for an axis-aligned box (x0, x1, y0, y1) whose edges
+    lie on mesh lines (the indicator is evaluated at interior quadrature points)."""
+    x0, x1, y0, y1 = box
+    ind = lambda x, y: ((x >= x0) & (x <= x1) & (y >= y0) & (y <= y1)).astype(np.float64)
+    return assemble_rhs(space, ind, space.order + 1 if quadorder is None else quadorder)

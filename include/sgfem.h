@@ -307,6 +307,23 @@ SGFEM_API int sgfem_sampling_error(sgfem_context* ctx, const double* det_solutio
 #define SGFEM_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
 SGFEM_API int sgfem_precondition_device_static(sgfem_context* ctx, const void* r_dev, void* z_dev, int precision);
 
+/*
+ * Adjoint gradient of a mean quantity of interest J = l . U_0 (no counterpart in
+ * the reference package; the reference's Julia API has no derivative).  For the
+ * symmetric SG operator S = I (x) K_0 + sum_m G_m (x) K_m of the context, U the
+ * solution of S U = b and Lambda the adjoint solution of S Lambda = e_1 (x) l
+ * (both n x P column-major, host):
+ *   dblocks[m-1] = -Lambda^T (G_m (x) K_m) U, the derivative of J with respect
+ *                  to a factor multiplying K_m (m = 1..M);
+ *   dalpha[i]    = -sum_mu Lambda_mu^T K_0^(i) U_mu, K_0^(i) = (phi_i grad u, grad v):
+ *                  the derivative with respect to the nodal values of a P1 mean
+ *                  field a_0 = sum_i alpha_i phi_i (mesh: the P1 space of the
+ *                  context, one dof per node).
+ * Either output may be NULL.  FP64; reductions in a fixed order.
+ */
+SGFEM_API int sgfem_adjoint_gradient(sgfem_context* ctx, const double* U, const double* Lambda, double* dblocks,
+                                     const sgfem_mesh* mesh, double* dalpha);
+
 /* which FP32 apply kernel a finalized context uses: 1 = specialised to the coupling
    structure (compiled with NVRTC at finalize), 0 = generic; the log says why */
 SGFEM_API int sgfem_apply_variant(const sgfem_context* ctx);

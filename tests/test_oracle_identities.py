@@ -85,3 +85,30 @@ def test_pce_lambda_generating_function():
         s = sum(oc.pce_lambda(C, mu, x1, x2, factor, N_truncate=2) * TB.evaluate(k) for k, mu in enumerate(mis))
         a = C.get_a(x1, x2, y)
         assert abs(s - np.exp(factor * float(a))) <= 1e-11 * np.exp(factor * float(a))
+
+
+def test_adjoint_oracle_matches_finite_differences():
+    """The oracle's adjoint gradient of J = int_box E[u] against central
+    differences of its own assembled Kronecker solves."""
+    from oracle import adjoint as oa
+    from oracle import basis as ob
+    from oracle import coefficient as oc
+    from oracle import fem as of
+    from oracle import mopcontrol as om
+    M = 2
+    mis = om.generate_multiindices(M, 2)
+    TB = ob.TensorizedBasis(ob.LEGENDRE, M, 2, 4, multi_indices=mis)
+    V = of.LagrangeSpace(of.StructuredMesh(4), 1)
+    C = oc.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=10)
+    Q = oa.QoIOracle(V, C, TB.G, len(mis), M, lambda x, y: 1.0)
+    rng = np.random.default_rng(0)
+    theta = 1.0 + 0.1 * rng.standard_normal(M)
+    alpha = 1.0 + 0.1 * rng.standard_normal(V.mesh.nnodes)
+    J, gt, ga = Q.gradient(theta, alpha)
+    h = 1e-6
+    for _ in range(3):
+        dt = rng.standard_normal(M)
+        da = rng.standard_normal(V.mesh.nnodes)
+        fd = (Q.value(theta + h * dt, alpha + h * da) - Q.value(theta - h * dt, alpha - h * da)) / (2 * h)
+        an = gt @ dt + ga @ da
+        assert abs(fd - an) <= 1e-6 * abs(an)
