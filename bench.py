@@ -345,6 +345,214 @@ def run_profile(args):
     op.close()
 
 
+# ---------------------------------------------------------------- other workloads
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _timed(fn):
+    import torch
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    r = fn()
+    torch.cuda.synchronize()
+    return r, (time.perf_counter() - t) * 1e3
+
+
+def config1_problem(pkg, N=32, M=5, deg=2):
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    V = pkg.H1Pk(pkg.unit_square_mesh(N), 1)
+    mis = pkg.total_degree_multiindices(M, deg)
+    TB = pkg.TensorizedBasis(pkg.LegendrePolynomials, M, deg, deg + 4, multi_indices=mis)
+    sol = pkg.SGFEVector(V, TB)
+    Ks, b0 = pkg.assemble(pkg.PoissonProblemPrimal, sol, C, rhs=lambda x, y: np.ones_like(x))
+    return C, V, TB, sol, Ks, b0
+
+
+def run_config1(args):
+    """Config 1 (P1 32x32, M=5, total degree 2, P=21): FP64 PCG to 1e-10 and one
+    estimator pass; config 3's mixed-precision errors against FP64 (solution,
+    energy norm, estimator)."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C, V, TB, sol, Ks, b0 = config1_problem(pkg)
+    f = lambda x, y: np.ones_like(x)
+    op = pkg.SGOperator(V, TB, Ks, device=0)
+    n, P = V.ndofs, TB.nmodes
+    res = {}
+    for name, prec in (("fp64", pkg.FP64), ("mixed", pkg.MIXED)):
+        ts = []
+        for k in range(args.warmup + args.steps):
+            x = np.zeros(n * P)
+            st = op.solve_primal(b0, x, rtol=1e-10, precision=prec)
+            if k >= args.warmup:
+                ts.append(st["time_ms"])
+        res[name] = (x, st, statistics.median(ts))
+    x64, xm = res["fp64"][0], res["mixed"][0]
+    e64 = float(np.sqrt(x64 @ op.mul(x64)))
+    em = float(np.sqrt(xm @ op.mul(xm)))
+    sol.entries[:] = x64
+    pkg.estimate(pkg.PoissonProblemPrimal, sol, C, rhs=f, bonus_quadorder=2, tail_extension=(10, 2), op=op)
+    tes = []
+    for _ in range(max(1, args.steps)):
+        (eta64, ec64, ext), t = _timed(lambda: pkg.estimate(pkg.PoissonProblemPrimal, sol, C, rhs=f, bonus_quadorder=2,
+                                                            tail_extension=(10, 2), op=op))
+        tes.append(t)
+    sol.entries[:] = xm
+    etam, ecm, _ = pkg.estimate(pkg.PoissonProblemPrimal, sol, C, rhs=f, bonus_quadorder=2, tail_extension=(10, 2),
+                                op=op)
+    line = {"workload": "config1: P1 32x32 (1089 dofs), M=5, total degree 2 (P=21), PCG to 1e-10 + estimator",
+            "fp64_solve_ms": res["fp64"][2], "fp64_iterations": res["fp64"][1]["iterations"],
+            "mixed_solve_ms": res["mixed"][2], "mixed_iterations": res["mixed"][1]["iterations"],
+            "mixed_outer": res["mixed"][1]["outer_iterations"],
+            "estimate_ms_wall": statistics.median(tes), "P_ext": len(ext),
+            "mixed_vs_fp64": {"solution_rel_2norm": _rel(xm, x64), "energy_norm_rel": abs(em - e64) / e64,
+                              "eta4modes_rel": _rel(etam, eta64), "eta4cell_rel_max":
+                                  float(np.max(np.abs(ecm - ec64)) / np.max(np.abs(ec64)))},
+            "relres": {"fp64": res["fp64"][1]["relres"], "mixed": res["mixed"][1]["relres"]},
+            "note": "estimate_ms_wall includes the host-side extension of the multi-index set and argument setup"}
+    op.close()
+    print(json.dumps(line), flush=True)
+
+
+def run_lognormal(args):
+    """Config 3 lognormal variant: LogTransformedPoissonProblemPrimal, Hermite,
+    P1 128x128 (16641 dofs), M=10, 80 top-weight multi-indices, mean 0, tau=0.9;
+    device GMRES(20) to 1e-8, FP64 against mixed precision."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=0.0, maxm=150)
+    M, P = 10, 80
+    mis = pkg.top_weight_multiindices(M, P, C.decay_factors)
+    deg = max(max(m) for m in mis)
+    V = pkg.H1Pk(pkg.unit_square_mesh(128), 1)
+    TB = pkg.TensorizedBasis(pkg.HermitePolynomials, M, deg, deg + 4, multi_indices=mis)
+    sol = pkg.SGFEVector(V, TB)
+    (Ks, b), t_asm = _timed(lambda: pkg.assemble(pkg.LogTransformedPoissonProblemPrimal, sol, C,
+                                                 rhs=lambda x, y: np.ones_like(x)))
+    op = pkg.SGOperator(V, TB, Ks, device=0)
+    out = {}
+    restart = args.restart
+    for name, prec in (("fp64", pkg.FP64), ("mixed", pkg.MIXED)):
+        ts = []
+        for k in range(args.warmup + args.steps):
+            x = np.zeros(V.ndofs * P)
+            st = op.solve_logpoisson(b, x, rtol=1e-8, precision=prec, restart=restart, maxit=3000, allow_maxit=True)
+            if k >= args.warmup:
+                ts.append(st["time_ms"])
+        out[name] = (x, st, statistics.median(ts))
+    x64, xm = out["fp64"][0], out["mixed"][0]
+    line = {"workload": f"lognormal: P1 128x128 (16641 dofs), Hermite, M=10, P=80, GMRES({restart}) to 1e-8",
+            "fp64_solve_ms": out["fp64"][2], "fp64_iterations": out["fp64"][1]["iterations"],
+            "mixed_solve_ms": out["mixed"][2], "mixed_iterations": out["mixed"][1]["iterations"],
+            "mixed_outer": out["mixed"][1]["outer_iterations"],
+            "mixed_speedup_vs_fp64": out["fp64"][2] / out["mixed"][2],
+            "mixed_vs_fp64_solution_rel_2norm": _rel(xm, x64),
+            "relres": {"fp64": out["fp64"][1]["relres"], "mixed": out["mixed"][1]["relres"]},
+            "host_assembly_ms": t_asm, "apply_fp64_ms": op.ctx.time_apply(pkg.FP64, 10),
+            "apply_fp32_ms": op.ctx.time_apply(pkg.FP32, 10)}
+    op.close()
+    print(json.dumps(line), flush=True)
+
+
+def run_sampling(args):
+    """Config 4 sampling: 1e5 samples y ~ U[-1,1]^20 (NumPy PCG64, seed 123) on the
+    config-1 mesh: per batch of 512, the P2 deterministic problems solved on the
+    device (mixed PCG to 1e-10) and the errors of the config-1 SG solution for the
+    truncations m = 0..5 (sampling-error kernel)."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C, V, TB, sol, Ks, b0 = config1_problem(pkg)
+    op = pkg.SGOperator(V, TB, Ks, device=0)
+    op.solve_primal(b0, sol.entries, rtol=1e-12, precision=pkg.FP64)
+    op.close()
+    S_total = args.samples
+    Ms, B = 20, 512
+    rng = np.random.default_rng(123)
+    Y = rng.uniform(-1.0, 1.0, size=(Ms, S_total))
+    w = np.full(S_total, 0.5 ** Ms)
+    f = lambda x, y: np.ones_like(x)
+    (res, per), t_all = _timed(lambda: pkg.calculate_sampling_error(
+        sol, C, order=2, rhs=f, Msamples=Ms, samples=Y, weights=w, batch=B, rtol=1e-10, precision=pkg.MIXED,
+        return_per_sample=True))
+    # phase split on one batch
+    Vd = pkg.H1Pk(V.mesh, 2)
+    Kd = pkg.assemble_stiffness(Vd, C, list(range(Ms + 1)), 12)
+    bd = pkg.assemble_rhs(Vd, f, 2)
+    sp_ = pkg.SampleProblems(Vd, Kd, Y[:, :B])
+    sp_.solve(bd, rtol=1e-10, keep_on_device=True)
+    _, t_solve = _timed(lambda: sp_.solve(bd, rtol=1e-10, keep_on_device=True))
+    st = sp_.stats
+    _, t_err = _timed(lambda: sp_.sampling_error(sol, 4))
+    sp_.close()
+    line = {"workload": f"sampling: {S_total} samples U[-1,1]^20, config-1 SG solution (P1, P=21) vs P2 "
+                        f"deterministic solves on the 32x32 mesh (4225 dofs), batches of {B}, m=0..5",
+            "samples_per_s": S_total / (t_all * 1e-3), "total_s": t_all * 1e-3,
+            "batch_solve_ms": t_solve, "batch_solve_device_ms": st["time_ms"], "batch_iterations": st["iterations"],
+            "batch_error_ms": t_err, "stress_uniform": [float(v) for v in res[2]],
+            "u_uniform": [float(v) for v in res[3]]}
+    if not args.no_cpu_baseline:
+        from oracle import sampling as osm
+        from oracle import basis as ob
+        from oracle import fem as of
+        from oracle import coefficient as oc
+        mesh = of.StructuredMesh(32)
+        Vo_sg, Vo_det = of.LagrangeSpace(mesh, 1), of.LagrangeSpace(mesh, 2)
+        Co = oc.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+        Kdo = [K.tocsr() for K in Kd]
+        TBo = ob.TensorizedBasis(ob.LEGENDRE, 5, 2, 6, multi_indices=TB.multi_indices)
+        osm.calculate_sampling_error(sol.entries, TBo, Vo_sg, Vo_det, Kdo, bd, Y[:, :1], w[:1], order=2)
+        ns = 40
+        t = time.perf_counter()
+        osm.calculate_sampling_error(sol.entries, TBo, Vo_sg, Vo_det, Kdo, bd, Y[:, :ns], w[:ns], order=2)
+        per_sample = (time.perf_counter() - t) / ns
+        line["cpu_baseline"] = {"value": 1.0 / per_sample, "unit": "samples/s", "cores": 1, "kind": "port",
+                                "sample": f"{ns} samples through the oracle (SuperLU solve of the P2 problem + "
+                                          f"vectorised error integrals for m=0..5), single thread"}
+    print(json.dumps(line), flush=True)
+
+
+def run_adjoint(args):
+    """Config 5: J = int_[0.25,0.75]^2 E[u] dx, gradient with respect to the KLE
+    block factors theta_m and the nodal P1 mean field alpha by one adjoint solve;
+    central finite differences (h = 1e-6) on random directions."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    N, M = args.mesh, 20 if args.mesh >= 128 else 5
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    V = pkg.H1Pk(pkg.unit_square_mesh(N), 1)
+    mis = pkg.total_degree_multiindices(M, 2) if M <= 5 else pkg.top_weight_multiindices(M, 150, C.decay_factors)
+    deg = max(max(m) for m in mis)
+    TB = pkg.TensorizedBasis(pkg.LegendrePolynomials, M, deg, deg + 4, multi_indices=mis)
+    Q = pkg.MeanQoI(V, TB, C, rhs=lambda x, y: np.ones_like(x))
+    theta, alpha = np.ones(M), np.ones(V.mesh.nnodes)
+    # FP64 PCG floor: 1e-12 is attainable on the small mesh only; the finite-difference
+    # step grows with the solve tolerance there (error ~ rtol / h + h^2)
+    small = N <= 64
+    rtol, rtol_fd, h = (1e-12, 2e-13, 1e-6) if small else (1e-10, 1e-10, 1e-4)
+    Q.value_and_gradient(theta, alpha, rtol=rtol)
+    (r, t_grad) = _timed(lambda: Q.value_and_gradient(theta, alpha, rtol=rtol))
+    J, gt, ga, st = r
+    (_, t_fwd) = _timed(lambda: Q.value(theta, alpha, rtol=rtol))
+    rng = np.random.default_rng(5)
+    errs = []
+    for _ in range(args.directions):
+        dt = rng.standard_normal(M)
+        da = rng.standard_normal(V.mesh.nnodes)
+        fd = (Q.value(theta + h * dt, alpha + h * da, rtol=rtol_fd) - Q.value(theta - h * dt, alpha - h * da,
+                                                                                rtol=rtol_fd)) / (2 * h)
+        an = gt @ dt + ga @ da
+        errs.append(abs(fd - an) / abs(an))
+    line = {"workload": f"adjoint: P1 {N}x{N} ({V.ndofs} nodes), M={M}, P={TB.nmodes}, FP64 PCG to {rtol:g}",
+            "fd_step": h, "fd_solve_rtol": rtol_fd,
+            "J": J, "gradient_ms_wall": t_grad, "forward_ms_wall": t_fwd, "gradient_cost_vs_forward": t_grad / t_fwd,
+            "forward_device_ms": st["forward"]["time_ms"], "adjoint_device_ms": st["adjoint"]["time_ms"],
+            "fd_directions": len(errs), "fd_rel_err_max": max(errs) if errs else None,
+            "fd_rel_err_median": statistics.median(errs) if errs else None,
+            "note": "wall times include host assembly of K_0(alpha) and the context setup in both arms"}
+    print(json.dumps(line), flush=True)
+
+
 def ctx_qn(op):
     # pair count P + sum_m nzcols(G_m), from the coupling matrix
     G = op.TB.G.tocsr()
@@ -365,10 +573,18 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", choices=["apply32", "apply64", "solve"], default=None,
                     help="profiling target for ncu: set up the workload, run the kernel(s) a few times, exit")
-    ap.add_argument("--mesh", type=int, default=256, help="mesh size for --profile (256 = the workload)")
+    ap.add_argument("--mesh", type=int, default=256, help="mesh size for --profile / --workload adjoint")
+    ap.add_argument("--workload", choices=["config2", "config1", "lognormal", "sampling", "adjoint"],
+                    default="config2", help="config2 is the headline bench line; the others print their own line")
+    ap.add_argument("--samples", type=int, default=100000, help="--workload sampling: number of samples")
+    ap.add_argument("--directions", type=int, default=20, help="--workload adjoint: finite-difference directions")
+    ap.add_argument("--restart", type=int, default=100, help="--workload lognormal: GMRES restart length")
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)
+    if args.workload != "config2":
+        return {"config1": run_config1, "lognormal": run_lognormal, "sampling": run_sampling,
+                "adjoint": run_adjoint}[args.workload](args)
     rank, world, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world, pg)

@@ -163,11 +163,12 @@ __global__ void k_build_rhs(const double* __restrict__ b0, const double* __restr
     }
 }
 
+// b0 goes to the device column c0 of caller mode 0 (the column order is permuted)
 __global__ void k_add_b0(const double* __restrict__ b0, double* __restrict__ b, const int* __restrict__ iperm,
-                         const unsigned char* __restrict__ bmask, int n, int ld) {
+                         const unsigned char* __restrict__ bmask, int n, int ld, int c0) {
     for (int i = blockIdx.x * VT + threadIdx.x; i < n; i += gridDim.x * VT) {
         const int row = iperm[i];
-        if (!bmask[row]) b[(size_t)row * ld] += b0[i];
+        if (!bmask[row]) b[(size_t)row * ld + c0] += b0[i];
     }
 }
 
@@ -435,7 +436,7 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
                                               o->reference_rhs ? 1 : 0);
         ctx->launches++;
         k_add_b0<<<(int)std::min<int64_t>((ctx->n + VT - 1) / VT, 4096), VT, 0, ctx->stream>>>(
-            d_b0, b, ctx->d_iperm, ctx->d_bmask, (int)ctx->n, (int)ctx->ld);
+            d_b0, b, ctx->d_iperm, ctx->d_bmask, (int)ctx->n, (int)ctx->ld, (int)ctx->imode[0]);
         SG_LAUNCHED(ctx);
     }
 

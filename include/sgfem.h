@@ -133,8 +133,9 @@ SGFEM_API void sgfem_default_options(sgfem_solve_options* opts);
  * or b0, Dirichlet rows zeroed.  Right-preconditioned restarted GMRES(restart)
  * (restart <= 0: 20, the Krylov.jl default memory) with the mean-based
  * preconditioner opts->preconditioner, stopping on ||b - A x|| <= rtol ||b||
- * (FP64 true residual).  SGFEM_MIXED: FP32 GMRES to inner_rtol inside FP64
- * iterative refinement.  Also valid for symmetric operators.
+ * (FP64 true residual).  SGFEM_MIXED: FP64 iterative refinement, each step one
+ * FP32 GMRES(restart) cycle to max(inner_rtol, 1e-4) (about the accuracy FP32
+ * GMRES reaches).  Also valid for symmetric operators.
  */
 SGFEM_API int sgfem_solve_gmres(sgfem_context* ctx, const double* b0, double* x_inout,
                                 const sgfem_solve_options* opts, int restart, sgfem_solve_stats* stats);

@@ -45,8 +45,22 @@ def deterministic_solve(Kdet, bdet, bdofs, y):
     return u
 
 
+_QP_CACHE = {}
+
+
 def _qp_values(space, pts):
-    """Basis values and gradients at reference points per cell: (nc, nq, nd), (nc, nq, nd, 2)."""
+    """Basis values and gradients at reference points per cell: (nc, nq, nd), (nc, nq, nd, 2)
+    (they depend on the space and the rule only, so they are kept per pair)."""
+    key = (id(space), np.asarray(pts).tobytes())
+    hit = _QP_CACHE.get(key)
+    if hit is not None and hit[0] is space:
+        return hit[1]
+    out = _qp_values_uncached(space, pts)
+    _QP_CACHE[key] = (space, out)
+    return out
+
+
+def _qp_values_uncached(space, pts):
     nc = space.mesh.ncells
     nd = space.ndofs4cell()
     V = np.zeros((nc, len(pts), nd))

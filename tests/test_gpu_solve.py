@@ -120,6 +120,23 @@ def test_solve_p2_mixed(built_pkg, order, N, M, P):
     op.close()
 
 
+def test_solve_rhs_lands_on_mode_zero_for_permuted_columns(built_pkg):
+    """M=20, P=150 top-weight set (the bench's coupling structure) on a small mesh:
+    the device column order differs from the caller's mode order there, and
+    e_1 (x) b0 must still land on caller mode 0."""
+    import __graft_entry__ as ge
+    from oracle import sg as osg
+    pkg = ge.load_package()
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    p = build(4, 1, 20, pkg.top_weight_multiindices(20, 150, C.decay_factors))
+    ref = osg.kron_direct(p.K0, p.Ks, p.G, p.b0, p.bdofs, p.P)
+    op = pkg.SGOperator(p.V, p.TB, p.Kall, device=0)
+    x = np.zeros(p.n * p.P)
+    op.solve_primal(p.b0, x, rtol=1e-12, precision=pkg.FP64, preconditioner=pkg.PREC_JACOBI)
+    assert rel(x, ref) <= 1e-9
+    op.close()
+
+
 def test_package_solve_entry_point(built_pkg):
     """solve(PoissonProblemPrimal, sol, C; rhs) writes sol.entries like solve! does."""
     p = config1_like(N=16, M=3, deg=2)
