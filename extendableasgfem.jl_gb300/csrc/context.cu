@@ -356,7 +356,13 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
     for (int64_t m = 0; m <= M; ++m)
         if (!ctx->mats[m].set) return sg_fail(ctx, SGFEM_ERR_STATE, "spatial matrix K_" + std::to_string(m) + " not set");
     ctx->M1 = (int)(M + 1);
-    ctx->ld = (P + 3) / 4 * 4;
+    {
+        // row stride of SG vectors in the device layout: P rounded up to `align` values
+        const char* ea = getenv("SGFEM_LD_ALIGN");
+        int align = ea ? atoi(ea) : 4;
+        if (align != 4 && align != 8 && align != 16 && align != 32) align = 4;
+        ctx->ld = (P + align - 1) / align * align;
+    }
     for (int64_t b : ctx->bdofs)
         if (b < 0 || b >= n) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "boundary dof out of range");
 
@@ -524,37 +530,81 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
         std::vector<float> combg32(combg.begin(), combg.end());
     
         // ---- slot tables of the specialised FP32 apply: slot (pair p = m/2, group k = c/32)
-        // exists if some column of group k couples to K_2p or K_2p+1 (K_0 couples to all)
+        // exists if some column of group k couples to K_2p or K_2p+1 (K_0 couples to all).
+        // The column groups are split into jit_np passes (contiguous group ranges with
+        // balanced slot counts); a pass keeps only its own slots' accumulators.  Slots are
+        // numbered pass by pass; jit_pass_slot0[p] is the first slot of pass p.
+        sg_jit_configure(ctx);
         const int KG = (int)((P + 31) / 32);
         const int NPAIR = (ctx->M1 + 1) / 2;
         ctx->M1P = (ctx->M1 + 3) / 4 * 4;
-        ctx->jit_slot_of.assign((size_t)NPAIR * KG, -1);
-        ctx->jit_slots.clear();
+        std::vector<std::vector<char>> needs(NPAIR, std::vector<char>(KG, 0));
+        std::vector<int> slots_in_group(KG, 0);
         for (int pr = 0; pr < NPAIR; ++pr)
             for (int k = 0; k < KG; ++k) {
                 bool need = false;
                 for (int c = 32 * k; c < std::min<int64_t>(P, 32 * k + 32) && !need; ++c)
                     for (int m = 2 * pr; m <= std::min<int64_t>(M, 2 * pr + 1) && !need; ++m)
                         need = (m == 0) || nzcol[m][mode_of_col[c]];
-                if (need) {
-                    ctx->jit_slot_of[(size_t)pr * KG + k] = (int)ctx->jit_slots.size();
-                    ctx->jit_slots.push_back({pr, k});
-                }
+                needs[pr][k] = need;
+                slots_in_group[k] += need;
             }
+        const int np = std::max(1, std::min(ctx->jit_np_req, KG));
+        ctx->jit_pass_k0.assign(np + 1, KG);
+        {
+            int total = 0;
+            for (int k = 0; k < KG; ++k) total += slots_in_group[k];
+            int p = 0, acc = 0;
+            ctx->jit_pass_k0[0] = 0;
+            for (int k = 0; k < KG; ++k) {
+                // close pass p once it holds its share and groups remain for the others
+                if (p + 1 < np && acc > 0 && acc + slots_in_group[k] / 2 > (long long)total * (p + 1) / np &&
+                    KG - k >= np - p - 1) {
+                    ctx->jit_pass_k0[++p] = k;
+                }
+                acc += slots_in_group[k];
+            }
+            for (int q = p + 1; q <= np; ++q) ctx->jit_pass_k0[q] = KG;
+            ctx->jit_np = p + 1;
+            ctx->jit_pass_k0.resize(ctx->jit_np + 1);
+            ctx->jit_pass_k0[ctx->jit_np] = KG;
+        }
+        std::vector<int> pass_of_k(KG, 0);
+        for (int p = 0; p < ctx->jit_np; ++p)
+            for (int k = ctx->jit_pass_k0[p]; k < ctx->jit_pass_k0[p + 1]; ++k) pass_of_k[k] = p;
+        ctx->jit_slot_of.assign((size_t)NPAIR * KG, -1);
+        ctx->jit_slots.clear();
+        ctx->jit_pass_slot0.assign(ctx->jit_np + 1, 0);
+        for (int p = 0; p < ctx->jit_np; ++p) {
+            ctx->jit_pass_slot0[p] = (int)ctx->jit_slots.size();
+            for (int pr = 0; pr < NPAIR; ++pr)
+                for (int k = ctx->jit_pass_k0[p]; k < ctx->jit_pass_k0[p + 1]; ++k)
+                    if (needs[pr][k]) {
+                        ctx->jit_slot_of[(size_t)pr * KG + k] = (int)ctx->jit_slots.size();
+                        ctx->jit_slots.push_back({pr, k});
+                    }
+        }
+        ctx->jit_pass_slot0[ctx->jit_np] = (int)ctx->jit_slots.size();
+        // sacc offset of F(m, c) within its pass's accumulator block
         auto slot_off = [&](int m, int c) {
-            int sl = ctx->jit_slot_of[(size_t)(m / 2) * KG + c / 32];
-            return sl * 64 + 2 * (c % 32) + (m % 2);
+            const int sl = ctx->jit_slot_of[(size_t)(m / 2) * KG + c / 32];
+            const int ls = sl - ctx->jit_pass_slot0[pass_of_k[c / 32]];
+            return ls * 64 + 2 * (c % 32) + (m % 2);
         };
-        // combination list per output column: (1, acc(0, c)) then (g, acc(m, nu))
-        std::vector<int32_t> jptr(P + 1, 0), joff;
+        auto pass_of = [&](int c) { return pass_of_k[c / 32]; };
+        // combination list per output column: (1, acc(0, c)) then (g, acc(m, nu)); jpass is
+        // the pass whose accumulators hold the entry
+        std::vector<int32_t> jptr(P + 1, 0), joff, jpass;
         std::vector<float> jg;
         for (int64_t c = 0; c < P; ++c) {
             joff.push_back(slot_off(0, (int)c));
+            jpass.push_back(pass_of((int)c));
             jg.push_back(1.0f);
             for (int32_t e = combptr[c]; e < combptr[c + 1]; ++e) {
                 int q = combq[e];
                 int m = qtab[q] >> 16, nu = qtab[q] & 0xffff;
                 joff.push_back(slot_off(m, nu));
+                jpass.push_back(pass_of(nu));
                 jg.push_back((float)combg[e]);
             }
             jptr[c + 1] = (int32_t)joff.size();
@@ -575,25 +625,47 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
             std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
                 return (jptr[a + 1] - jptr[a]) > (jptr[b + 1] - jptr[b]);
             });
-            std::vector<std::vector<int2>> lanes(32);
+            const int NPS = ctx->jit_np;
+            // lanes[p][l]: lane l's entries of pass p; a column stays on one lane in every pass
+            std::vector<std::vector<std::vector<int2>>> lanes(NPS, std::vector<std::vector<int2>>(32));
+            std::vector<size_t> load(32, 0);
             for (int c : order) {
                 int best = 0;
                 for (int l = 1; l < 32; ++l)
-                    if (lanes[l].size() < lanes[best].size()) best = l;
-                for (int32_t e = jptr[c]; e < jptr[c + 1]; ++e) {
-                    int bits;
-                    std::memcpy(&bits, &jg[e], sizeof(int));
-                    const bool last = (e + 1 == jptr[c + 1]);
-                    lanes[best].push_back(make_int2(joff[e] | (int)(c << 13) | ((last ? 1 : 0) << 28), bits));
+                    if (load[l] < load[best]) best = l;
+                load[best] += jptr[c + 1] - jptr[c];
+                for (int p = 0; p < NPS; ++p) {
+                    int lastp = -1;
+                    for (int32_t e = jptr[c]; e < jptr[c + 1]; ++e)
+                        if (jpass[e] == p) lastp = e;
+                    for (int32_t e = jptr[c]; e < jptr[c + 1]; ++e) {
+                        if (jpass[e] != p) continue;
+                        int bits;
+                        std::memcpy(&bits, &jg[e], sizeof(int));
+                        const bool last = (e == lastp);
+                        lanes[p][best].push_back(make_int2(joff[e] | (int)(c << 13) | ((last ? 1 : 0) << 28), bits));
+                    }
                 }
             }
+            ctx->jit_pass_T.assign(NPS, 0);
             size_t T = 0;
-            for (auto& l : lanes) T = std::max(T, l.size());
+            for (int p = 0; p < NPS; ++p) {
+                size_t tp = 0;
+                for (auto& l : lanes[p]) tp = std::max(tp, l.size());
+                ctx->jit_pass_T[p] = (int)tp;
+                T += tp;
+            }
             ctx->jit_T = (int)T;
-            std::vector<int2> jtab(T * 32, make_int2(0, 0));
-            for (int l = 0; l < 32; ++l)
-                for (size_t i = 0; i < lanes[l].size(); ++i) jtab[i * 32 + l] = lanes[l][i];
-            const bool fits = (ctx->jit_slots.size() * 64 <= 8192) && P <= 32767;
+            std::vector<int2> jtab(std::max<size_t>(T, 1) * 32, make_int2(0, 0));
+            size_t off = 0;
+            for (int p = 0; p < NPS; ++p) {
+                for (int l = 0; l < 32; ++l)
+                    for (size_t i = 0; i < lanes[p][l].size(); ++i) jtab[(off + i) * 32 + l] = lanes[p][l][i];
+                off += ctx->jit_pass_T[p];
+            }
+            int maxps = 0;
+            for (int p = 0; p < NPS; ++p) maxps = std::max(maxps, ctx->jit_pass_slot0[p + 1] - ctx->jit_pass_slot0[p]);
+            const bool fits = ((size_t)maxps * 64 <= 8192) && P <= 32767;
             if (!fits) ctx->jit_T = -1;
             SG_TRY(upload(ctx, &ctx->d_jtab, jtab.data(), jtab.size()));
         }
@@ -631,7 +703,6 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
     if (!ctx->batched) SG_TRY(sg_apply_configure(ctx));
     if (ctx->lattice) SG_TRY(sg_lattice_configure(ctx));
     // specialised FP32 apply; on failure the generic kernel stays in use (reason in the variant log)
-    sg_jit_configure(ctx);
     ctx->jit_log = ctx->batched ? "block-diagonal sample operator" : "not compiled yet (at the first FP32 apply)";
     // host copies of the pattern are no longer needed
     for (auto& A : ctx->mats) {
@@ -760,6 +831,7 @@ extern "C" int sgfem_apply(sgfem_context* ctx, const double* x, double* y, int p
     SG_TRY(sg_ensure(ctx, ctx->w_vec[1], vb));
     SG_TRY(host_to_device_layout(ctx, x, ctx->w_vec[0].p, precision));
     SG_TRY(sg_launch_apply(ctx, precision, ctx->w_vec[0].p, ctx->w_vec[1].p, nullptr, nullptr, nullptr));
+    if (precision == SGFEM_FP32) SG_TRY(sg_jit_check(ctx));
     return device_to_host_layout(ctx, ctx->w_vec[1].p, y, precision);
 }
 
@@ -771,6 +843,7 @@ extern "C" int sgfem_apply_device(sgfem_context* ctx, const void* x_dev, void* y
     if (precision == SGFEM_FP32) SG_TRY(sg_jit_ensure(ctx));
     SG_TRY(sg_launch_apply(ctx, precision, x_dev, y_dev, nullptr, nullptr, nullptr));
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (precision == SGFEM_FP32) SG_TRY(sg_jit_check(ctx));
     return SGFEM_OK;
 }
 
@@ -797,5 +870,6 @@ extern "C" int sgfem_time_apply(sgfem_context* ctx, int precision, int reps, dou
     float ms = 0.f;
     SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     *ms_per_apply = ms / reps;
+    if (precision == SGFEM_FP32) SG_TRY(sg_jit_check(ctx));
     return SGFEM_OK;
 }

@@ -391,6 +391,7 @@ extern "C" int sgfem_solve_gmres(sgfem_context* ctx, const double* b0, double* x
     float ms = 0.f;
     SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     st.time_ms = ms;
+    if (low) SG_TRY(sg_jit_check(ctx));
     st.fp64_applies = (int)G.applies64;
     st.kernel_launches = ctx->launches - launches0;
     if (stats) *stats = st;

@@ -115,16 +115,58 @@ bool load_driver() {
     return ok;
 }
 
+// the packed-FMA slots of one nonzero: a_q += (c[pair].lo, c[pair].hi) * (x_k, x_k)
+std::string slot_fmas(const sgfem_context* ctx, const char* ind) {
+    std::string s;
+    char buf[256];
+    const int NS = (int)ctx->jit_slots.size();
+    for (int q = 0; q < NS; ++q) {
+        const int pr = ctx->jit_slots[q].first, k = ctx->jit_slots[q].second;
+        const int v = pr / 2;
+        const char* comp = (pr % 2 == 0) ? "x, c%d.y" : "z, c%d.w";
+        char cpair[64];
+        snprintf(cpair, sizeof(cpair), comp, v);
+        snprintf(buf, sizeof(buf), "%sa%d = __ffma2_rn(make_float2(c%d.%s), w%d, a%d);\n", ind, q, v, cpair, k, q);
+        s += buf;
+    }
+    return s;
+}
+
+// x<d>_k = X[col of nonzero t, 32k + lane] for t < cnt (t warp-uniform), else 0
+std::string loadx(const sgfem_context* ctx, int d, const std::string& t, const char* ind) {
+    const int LD = (int)ctx->ld, KG = (int)((ctx->P + 31) / 32);
+    std::string s;
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s{\n%s    const int tt_ = %s;\n%s    const int jj_ = __shfl_sync(0xffffffffu, jl, tt_ < cnt ? tt_ : 0);\n"
+                               "%s    const float* xr_ = X + (size_t)jj_ * LD + lane;\n",
+             ind, ind, t.c_str(), ind, ind);
+    s += buf;
+    for (int k = 0; k < KG; ++k) {
+        const int valid = LD - 32 * k;
+        if (valid >= 32)
+            snprintf(buf, sizeof(buf), "%s    x%d_%d = (tt_ < cnt) ? __ldg(xr_ + %d) : 0.f;\n", ind, d, k, 32 * k);
+        else
+            snprintf(buf, sizeof(buf), "%s    x%d_%d = (tt_ < cnt && lane < %d) ? __ldg(xr_ + %d) : 0.f;\n", ind, d, k,
+                     valid, 32 * k);
+        s += buf;
+    }
+    s += ind;
+    s += "}\n";
+    return s;
+}
+
 std::string generate_source(const sgfem_context* ctx) {
     const int LD = (int)ctx->ld, P = (int)ctx->P, M1P = ctx->M1P;
     const int KG = (int)((P + 31) / 32);
     const int NS = (int)ctx->jit_slots.size();
+    const int pfd = std::max(1, ctx->jit_pfd);
     std::string s;
     char buf[512];
     snprintf(buf, sizeof(buf),
              "#define LD %d\n#define P %d\n#define KG %d\n#define M1P %d\n#define NS %d\n#define WPB %d\n"
-             "#define RCHUNK %d\n#define PREFETCH %d\n#define T %d\n#define STAGE %d\n",
-             LD, P, KG, M1P, NS, JWPB, ctx->jit_rchunk, ctx->jit_prefetch, ctx->jit_T, ctx->jit_stage);
+             "#define RCHUNK %d\n#define PREFETCH %d\n#define T %d\n#define STAGE %d\n#define PFD %d\n#define MINB %d\n",
+             LD, P, KG, M1P, NS, JWPB, ctx->jit_rchunk, ctx->jit_prefetch, ctx->jit_T, ctx->jit_stage, pfd,
+             ctx->jit_minb);
     s += buf;
     s += R"(
 #define NV4 (M1P / 4)                 /* float4 per nonzero */
@@ -160,10 +202,15 @@ __device__ __forceinline__ void prefetch_x(const float* __restrict__ X, int jl, 
     _Pragma("unroll") for (int i_ = 0; i_ < NV4; ++i_)                                  \
         reinterpret_cast<float4*>(dst)[lane + 32 * i_] = pv[i_];
 
+#if MINB > 0
+extern "C" __global__ void __launch_bounds__(WPB * 32, MINB)
+#else
 extern "C" __global__ void __launch_bounds__(WPB * 32)
+#endif
 sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const float* __restrict__ vals,
              const float* __restrict__ X, float* __restrict__ Y, int n, const unsigned char* __restrict__ bmask,
-             const int2* __restrict__ jtab, double* __restrict__ partials, const Scal* __restrict__ scal) {
+             const int2* __restrict__ jtab, double* __restrict__ partials, const Scal* __restrict__ scal,
+             int* __restrict__ err) {
     if (scal && scal->done) return;
     extern __shared__ __align__(16) float smem[];
     __shared__ double red[WPB];
@@ -240,6 +287,7 @@ sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const 
                     __syncwarp();
 #endif
                 }
+#if PFD <= 1
 #pragma unroll 2
                 for (int t = 0; t < cnt; ++t) {
                 const int j = __shfl_sync(0xffffffffu, jl, t);
@@ -265,17 +313,41 @@ sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const 
         snprintf(buf, sizeof(buf), "                const float2 w%d = make_float2(u%d, u%d);\n", k, k, k);
         s += buf;
     }
-    for (int q = 0; q < NS; ++q) {
-        const int pr = ctx->jit_slots[q].first, k = ctx->jit_slots[q].second;
-        const int v = pr / 2;
-        const char* comp = (pr % 2 == 0) ? "x, c%d.y" : "z, c%d.w";
-        char cpair[64];
-        snprintf(cpair, sizeof(cpair), comp, v);
-        snprintf(buf, sizeof(buf), "                a%d = __ffma2_rn(make_float2(c%d.%s), w%d, a%d);\n", q, v, cpair,
-                 k, q);
+    s += slot_fmas(ctx, "                ");
+    s += "                }\n";
+    s += "#else\n";
+    // X values of the next PFD nonzeros rotate through PFD register sets: the loads
+    // for nonzero t + PFD are issued right after nonzero t's values are taken
+    for (int d = 0; d < pfd; ++d)
+        for (int k = 0; k < KG; ++k) {
+            snprintf(buf, sizeof(buf), "                float x%d_%d;\n", d, k);
+            s += buf;
+        }
+    for (int d = 0; d < pfd; ++d) s += loadx(ctx, d, std::to_string(d), "                ");
+    s += "                for (int t0 = 0; t0 < cnt; t0 += PFD) {\n";
+    for (int d = 0; d < pfd; ++d) {
+        snprintf(buf, sizeof(buf), "                if (t0 + %d < cnt) {\n", d);
         s += buf;
+        snprintf(buf, sizeof(buf),
+                 "#if STAGE\n                    const float4* cv = reinterpret_cast<const float4*>(cb + (t0 + %d) * M1P);\n"
+                 "#else\n                    const float4* cv = reinterpret_cast<const float4*>(vals + (size_t)(base + t0 + %d) * M1P);\n#endif\n",
+                 d, d);
+        s += buf;
+        for (int v = 0; v < M1P / 4; ++v) {
+            snprintf(buf, sizeof(buf), "                    const float4 c%d = STAGE ? cv[%d] : __ldg(cv + %d);\n", v, v, v);
+            s += buf;
+        }
+        for (int k = 0; k < KG; ++k) {
+            snprintf(buf, sizeof(buf), "                    const float2 w%d = make_float2(x%d_%d, x%d_%d);\n", k, d, k, d, k);
+            s += buf;
+        }
+        s += loadx(ctx, d, "t0 + " + std::to_string(d + pfd), "                    ");
+        s += slot_fmas(ctx, "                    ");
+        s += "                }\n";
     }
-    s += "                }\n            }\n";
+    s += "                }\n";
+    s += "#endif\n";
+    s += "            }\n";
     for (int q = 0; q < NS; ++q) {
         snprintf(buf, sizeof(buf), "            *reinterpret_cast<float2*>(sacc + %d + 2 * lane) = a%d;\n", q * 64, q);
         s += buf;
@@ -294,11 +366,13 @@ sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const 
             }
             __syncwarp();
             const float* xrow = X + (size_t)row * LD;
+            float rowdot = 0.f;  // per-row products in FP32, rows summed in FP64
             for (int c = lane; c < LD; c += 32) {
                 const float y = (c < P) ? ybuf[c] : 0.f;
                 yrow[c] = y;
-                if (partials) dot += (double)xrow[c] * (double)y;
+                if (partials) rowdot = fmaf(xrow[c], y, rowdot);
             }
+            dot += (double)rowdot;
         }
 #if STAGE
         if (r1n < n) {  // stage the next row's values
@@ -324,8 +398,623 @@ sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const 
     return s;
 }
 
+// Variant with an asynchronous copy pipeline: every warp streams, for the
+// nonzeros of its rows in order, the X row of the nonzero's column and the
+// nonzero's KLE values into a ring of ADEPTH shared-memory slots (cp.async,
+// one commit group per nonzero) and consumes nonzero t while the copies of
+// t+1 .. t+ADEPTH-1 are in flight.  The bytes in flight per SM then come
+// from shared memory instead of registers.  The producer keeps the row
+// metadata (row pointers, the column indices of 32 nonzeros) of its current
+// and next row in registers, loaded one row ahead.
+std::string generate_source_async(const sgfem_context* ctx) {
+    const int LD = (int)ctx->ld, P = (int)ctx->P, M1P = ctx->M1P;
+    const int KG = (int)((P + 31) / 32);
+    const int NS = (int)ctx->jit_slots.size();
+    std::string s;
+    char buf[512];
+    snprintf(buf, sizeof(buf),
+             "#define LD %d\n#define P %d\n#define KG %d\n#define M1P %d\n#define NS %d\n#define WPB %d\n"
+             "#define RCHUNK %d\n#define T %d\n#define ADEPTH %d\n#define MINB %d\n",
+             LD, P, KG, M1P, NS, JWPB, ctx->jit_rchunk, ctx->jit_T, ctx->jit_adepth, ctx->jit_minb);
+    s += buf;
+    s += R"(
+#define SLOTF (LD + M1P)              /* floats per ring slot: X row, then the KLE values */
+#define NCH (SLOTF / 4)               /* 16-byte chunks per slot */
+#define WSMEM (ADEPTH * SLOTF + NS * 64 + LD)   /* floats per warp */
+struct Scal { double rho, pq, alpha, beta, rr, tol2; int done, status, iters, first; };
+
+__device__ __forceinline__ void cp16(float* dst, const float* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_depth() { asm volatile("cp.async.wait_group %0;" ::"n"(ADEPTH - 1) : "memory"); }
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+#if MINB > 0
+extern "C" __global__ void __launch_bounds__(WPB * 32, MINB)
+#else
+extern "C" __global__ void __launch_bounds__(WPB * 32)
+#endif
+sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const float* __restrict__ vals,
+             const float* __restrict__ X, float* __restrict__ Y, int n, const unsigned char* __restrict__ bmask,
+             const int2* __restrict__ jtab, double* __restrict__ partials, const Scal* __restrict__ scal,
+             int* __restrict__ err) {
+    if (scal && scal->done) return;
+    extern __shared__ __align__(16) float smem[];
+    __shared__ double red[WPB];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int2* stab = reinterpret_cast<int2*>(smem);
+    float* ring = smem + 2 * T * 32 + warp * WSMEM;
+    float* sacc = ring + ADEPTH * SLOTF;
+    float* ybuf = sacc + NS * 64;
+    for (int i = threadIdx.x; i < T * 32; i += blockDim.x) stab[i] = __ldg(jtab + i);
+    __syncthreads();
+    double dot = 0.0;
+    const int nw = gridDim.x * WPB, w = blockIdx.x * WPB + warp;
+    const int stride = nw * RCHUNK;
+#define NEXT_ROW(r) ((((r) + 1) % RCHUNK) ? ((r) + 1) : ((r) + 1 - RCHUNK + stride))
+    // ---- producer: the row being copied (prow: nonzeros [pnz, pend), column indices of
+    // [pbase, pbase + 32) lane-wise in pjl) and the next row's metadata (q*), loaded ahead
+    int prow = w * RCHUNK, pnz = 0, pend = 0, pbase = 0, pjl = 0;
+    int qrow = 0, qnz = 0, qend = 0, qjl = 0;
+    // first producer row with nonzeros off the boundary
+    while (prow < n && (bmask[prow] || rowptr[prow] == rowptr[prow + 1])) prow = NEXT_ROW(prow);
+    if (prow < n) {
+        pnz = pbase = rowptr[prow];
+        pend = rowptr[prow + 1];
+        pjl = (lane < pend - pbase) ? __ldg(col + pbase + lane) : 0;
+    }
+    // next producer row (skips boundary and empty rows)
+#define FETCH_NEXT()                                                                     \
+    {                                                                                    \
+        qrow = (prow < n) ? NEXT_ROW(prow) : n;                                          \
+        while (qrow < n && (bmask[qrow] || rowptr[qrow] == rowptr[qrow + 1])) qrow = NEXT_ROW(qrow); \
+        if (qrow < n) {                                                                  \
+            qnz = rowptr[qrow];                                                          \
+            qend = rowptr[qrow + 1];                                                     \
+            qjl = (lane < qend - qnz) ? __ldg(col + qnz + lane) : 0;                     \
+        }                                                                                \
+    }
+    FETCH_NEXT();
+    int sp = 0;  // next slot to fill
+    // copy one nonzero into slot sp; one commit group per call (empty once the rows run out)
+#define PRODUCE()                                                                        \
+    {                                                                                    \
+        if (prow < n) {                                                                  \
+            if (pnz - pbase >= 32) {                                                     \
+                pbase = pnz;                                                             \
+                pjl = (lane < pend - pbase) ? __ldg(col + pbase + lane) : 0;             \
+            }                                                                            \
+            const int j_ = __shfl_sync(0xffffffffu, pjl, pnz - pbase);                   \
+            float* dst_ = ring + sp * SLOTF;                                             \
+            const float* sx_ = X + (size_t)j_ * LD;                                      \
+            const float* sv_ = vals + (size_t)pnz * M1P;                                 \
+            for (int q_ = lane; q_ < NCH; q_ += 32)                                      \
+                cp16(dst_ + 4 * q_, q_ < LD / 4 ? sx_ + 4 * q_ : sv_ + 4 * (q_ - LD / 4)); \
+            if (++pnz == pend) {                                                         \
+                prow = qrow; pnz = pbase = qnz; pend = qend; pjl = qjl;                  \
+                FETCH_NEXT();                                                            \
+            }                                                                            \
+        }                                                                                \
+        cp_commit();                                                                     \
+        sp = (sp + 1 == ADEPTH) ? 0 : sp + 1;                                            \
+    }
+    for (int i = 0; i < ADEPTH - 1; ++i) PRODUCE();
+    int sc = 0;  // next slot to consume
+    for (int row = w * RCHUNK; row < n; row = NEXT_ROW(row)) {
+        float* yrow = Y + (size_t)row * LD;
+        if (bmask[row]) {
+            for (int c = lane; c < LD; c += 32) yrow[c] = 0.f;
+            continue;
+        }
+        const int nz0 = rowptr[row], nz1 = rowptr[row + 1];
+)";
+    for (int q = 0; q < NS; ++q) {
+        snprintf(buf, sizeof(buf), "        float2 a%d = make_float2(0.f, 0.f);\n", q);
+        s += buf;
+    }
+    s += R"(        for (int t = nz0; t < nz1; ++t) {
+            PRODUCE();
+            cp_wait_depth();
+            __syncwarp();
+            const float* sl = ring + sc * SLOTF;
+            const float4* cv = reinterpret_cast<const float4*>(sl + LD);
+)";
+    for (int v = 0; v < M1P / 4; ++v) {
+        snprintf(buf, sizeof(buf), "            const float4 c%d = cv[%d];\n", v, v);
+        s += buf;
+    }
+    for (int k = 0; k < KG; ++k) {
+        const int valid = LD - 32 * k;
+        if (valid >= 32)
+            snprintf(buf, sizeof(buf), "            const float u%d = sl[%d + lane];\n", k, 32 * k);
+        else
+            snprintf(buf, sizeof(buf), "            const float u%d = (lane < %d) ? sl[%d + lane] : 0.f;\n", k, valid,
+                     32 * k);
+        s += buf;
+        snprintf(buf, sizeof(buf), "            const float2 w%d = make_float2(u%d, u%d);\n", k, k, k);
+        s += buf;
+    }
+    s += R"(            __syncwarp();  // every lane has read the slot before it is refilled
+            sc = (sc + 1 == ADEPTH) ? 0 : sc + 1;
+)";
+    s += slot_fmas(ctx, "            ");
+    s += "        }\n";
+    for (int q = 0; q < NS; ++q) {
+        snprintf(buf, sizeof(buf), "        *reinterpret_cast<float2*>(sacc + %d + 2 * lane) = a%d;\n", q * 64, q);
+        s += buf;
+    }
+    s += R"(        __syncwarp();
+        float acc = 0.f;
+#pragma unroll
+        for (int i = 0; i < T; ++i) {
+            const int2 e = stab[i * 32 + lane];
+            acc = fmaf(__int_as_float(e.y), sacc[e.x & 0x1fff], acc);
+            if (e.x >> 28) {
+                ybuf[(e.x >> 13) & 0x7fff] = acc;
+                acc = 0.f;
+            }
+        }
+        __syncwarp();
+        const float* xrow = X + (size_t)row * LD;
+        float rowdot = 0.f;
+        for (int c = lane; c < LD; c += 32) {
+            const float y = (c < P) ? ybuf[c] : 0.f;
+            yrow[c] = y;
+            if (partials) rowdot = fmaf(xrow[c], y, rowdot);
+        }
+        dot += (double)rowdot;
+        __syncwarp();
+    }
+    cp_wait_all();
+    if (partials) {
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
+        if (lane == 0) red[warp] = dot;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t2 = 0.0;
+            for (int w2 = 0; w2 < WPB; ++w2) t2 += red[w2];
+            partials[blockIdx.x] = t2;
+        }
+    }
+}
+)";
+    return s;
+}
+
+// Variant with bulk copies: one lane per warp moves each nonzero's X row
+// (LD floats) and KLE values (M1P floats) into a ring of ADEPTH shared-memory
+// slots with two cp.async.bulk copies that complete on the slot's mbarrier
+// (expect-tx of the slot's bytes); the other lanes only consume.  Waits on a
+// slot poll mbarrier.try_wait.parity at most WAIT_LIMIT times; on a timeout
+// the kernel sets *err, waits (bounded) for the copies it has in flight and
+// returns.
+std::string generate_source_bulk(const sgfem_context* ctx) {
+    const int LD = (int)ctx->ld, P = (int)ctx->P, M1P = ctx->M1P;
+    const int KG = (int)((P + 31) / 32);
+    const int NS = (int)ctx->jit_slots.size();
+    std::string s;
+    char buf[512];
+    snprintf(buf, sizeof(buf),
+             "#define LD %d\n#define P %d\n#define KG %d\n#define M1P %d\n#define NS %d\n#define WPB %d\n"
+             "#define RCHUNK %d\n#define T %d\n#define ADEPTH %d\n#define MINB %d\n",
+             LD, P, KG, M1P, NS, JWPB, ctx->jit_rchunk, ctx->jit_T, ctx->jit_adepth, ctx->jit_minb);
+    s += buf;
+    s += R"(
+#define SLOTF (LD + M1P)                          /* floats per ring slot: X row, then the KLE values */
+#define WSMEM (ADEPTH * SLOTF + NS * 64 + LD + 2 * ADEPTH)   /* floats per warp (+ ADEPTH mbarriers) */
+#define WAIT_LIMIT (1 << 20)
+struct Scal { double rho, pq, alpha, beta, rr, tol2; int done, status, iters, first; };
+
+__device__ __forceinline__ unsigned sh_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect(unsigned bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_copy(unsigned dst, const void* src, unsigned bytes, unsigned bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
+}
+__device__ __forceinline__ unsigned mbar_try(unsigned bar, unsigned parity) {
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    return ok;
+}
+// bounded wait; 0 on timeout
+__device__ __forceinline__ int mbar_wait(unsigned bar, unsigned parity) {
+    for (int i = 0; i < WAIT_LIMIT; ++i)
+        if (mbar_try(bar, parity)) return 1;
+    return 0;
+}
+
+#if MINB > 0
+extern "C" __global__ void __launch_bounds__(WPB * 32, MINB)
+#else
+extern "C" __global__ void __launch_bounds__(WPB * 32)
+#endif
+sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const float* __restrict__ vals,
+             const float* __restrict__ X, float* __restrict__ Y, int n, const unsigned char* __restrict__ bmask,
+             const int2* __restrict__ jtab, double* __restrict__ partials, const Scal* __restrict__ scal,
+             int* __restrict__ err) {
+    if (scal && scal->done) return;
+    extern __shared__ __align__(16) float smem[];
+    __shared__ double red[WPB];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int2* stab = reinterpret_cast<int2*>(smem);
+    float* ring = smem + 2 * T * 32 + warp * WSMEM;
+    float* sacc = ring + ADEPTH * SLOTF;
+    float* ybuf = sacc + NS * 64;
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(ybuf + LD);
+    const unsigned ring_a = sh_addr(ring), bars_a = sh_addr(bars);
+    for (int i = threadIdx.x; i < T * 32; i += blockDim.x) stab[i] = __ldg(jtab + i);
+    if (lane == 0) {
+        for (int k = 0; k < ADEPTH; ++k) mbar_init(bars_a + 8 * k);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    double dot = 0.0;
+    const int nw = gridDim.x * WPB, w = blockIdx.x * WPB + warp;
+    const int stride = nw * RCHUNK;
+#define NEXT_ROW(r) ((((r) + 1) % RCHUNK) ? ((r) + 1) : ((r) + 1 - RCHUNK + stride))
+    int prow = w * RCHUNK, pnz = 0, pend = 0, pbase = 0, pjl = 0;
+    int qrow = 0, qnz = 0, qend = 0, qjl = 0;
+    while (prow < n && (bmask[prow] || rowptr[prow] == rowptr[prow + 1])) prow = NEXT_ROW(prow);
+    if (prow < n) {
+        pnz = pbase = rowptr[prow];
+        pend = rowptr[prow + 1];
+        pjl = (lane < pend - pbase) ? __ldg(col + pbase + lane) : 0;
+    }
+#define FETCH_NEXT()                                                                     \
+    {                                                                                    \
+        qrow = (prow < n) ? NEXT_ROW(prow) : n;                                          \
+        while (qrow < n && (bmask[qrow] || rowptr[qrow] == rowptr[qrow + 1])) qrow = NEXT_ROW(qrow); \
+        if (qrow < n) {                                                                  \
+            qnz = rowptr[qrow];                                                          \
+            qend = rowptr[qrow + 1];                                                     \
+            qjl = (lane < qend - qnz) ? __ldg(col + qnz + lane) : 0;                     \
+        }                                                                                \
+    }
+    FETCH_NEXT();
+    int sp = 0, sc = 0, inflight = 0;
+    unsigned phase = 0;  // bit k: parity of slot k's next completion
+    // one nonzero into slot sp (nothing once the rows run out)
+#define PRODUCE()                                                                        \
+    {                                                                                    \
+        if (prow < n) {                                                                  \
+            if (pnz - pbase >= 32) {                                                     \
+                pbase = pnz;                                                             \
+                pjl = (lane < pend - pbase) ? __ldg(col + pbase + lane) : 0;             \
+            }                                                                            \
+            const int j_ = __shfl_sync(0xffffffffu, pjl, pnz - pbase);                   \
+            if (lane == 0) {                                                             \
+                const unsigned bar_ = bars_a + 8 * sp;                                   \
+                const unsigned dst_ = ring_a + 4 * SLOTF * sp;                           \
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");             \
+                mbar_expect(bar_, 4 * SLOTF);                                            \
+                bulk_copy(dst_, X + (size_t)j_ * LD, 4 * LD, bar_);                      \
+                bulk_copy(dst_ + 4 * LD, vals + (size_t)pnz * M1P, 4 * M1P, bar_);       \
+            }                                                                            \
+            ++inflight;                                                                  \
+            sp = (sp + 1 == ADEPTH) ? 0 : sp + 1;                                        \
+            if (++pnz == pend) {                                                         \
+                prow = qrow; pnz = pbase = qnz; pend = qend; pjl = qjl;                  \
+                FETCH_NEXT();                                                            \
+            }                                                                            \
+        }                                                                                \
+    }
+    for (int i = 0; i < ADEPTH - 1; ++i) PRODUCE();
+    bool failed = false;
+    for (int row = w * RCHUNK; row < n && !failed; row = NEXT_ROW(row)) {
+        float* yrow = Y + (size_t)row * LD;
+        if (bmask[row]) {
+            for (int c = lane; c < LD; c += 32) yrow[c] = 0.f;
+            continue;
+        }
+        const int nz0 = rowptr[row], nz1 = rowptr[row + 1];
+)";
+    for (int q = 0; q < NS; ++q) {
+        snprintf(buf, sizeof(buf), "        float2 a%d = make_float2(0.f, 0.f);\n", q);
+        s += buf;
+    }
+    s += R"(        for (int t = nz0; t < nz1; ++t) {
+            PRODUCE();
+            if (!mbar_wait(bars_a + 8 * sc, (phase >> sc) & 1u)) {
+                failed = true;
+                break;
+            }
+            phase ^= 1u << sc;
+            --inflight;
+            const float* sl = ring + sc * SLOTF;
+            const float4* cv = reinterpret_cast<const float4*>(sl + LD);
+)";
+    for (int v = 0; v < M1P / 4; ++v) {
+        snprintf(buf, sizeof(buf), "            const float4 c%d = cv[%d];\n", v, v);
+        s += buf;
+    }
+    for (int k = 0; k < KG; ++k) {
+        const int valid = LD - 32 * k;
+        if (valid >= 32)
+            snprintf(buf, sizeof(buf), "            const float u%d = sl[%d + lane];\n", k, 32 * k);
+        else
+            snprintf(buf, sizeof(buf), "            const float u%d = (lane < %d) ? sl[%d + lane] : 0.f;\n", k, valid,
+                     32 * k);
+        s += buf;
+        snprintf(buf, sizeof(buf), "            const float2 w%d = make_float2(u%d, u%d);\n", k, k, k);
+        s += buf;
+    }
+    s += R"(            __syncwarp();  // every lane has read the slot before it is refilled
+            sc = (sc + 1 == ADEPTH) ? 0 : sc + 1;
+)";
+    s += slot_fmas(ctx, "            ");
+    s += "        }\n        if (failed) break;\n";
+    for (int q = 0; q < NS; ++q) {
+        snprintf(buf, sizeof(buf), "        *reinterpret_cast<float2*>(sacc + %d + 2 * lane) = a%d;\n", q * 64, q);
+        s += buf;
+    }
+    s += R"(        __syncwarp();
+        float acc = 0.f;
+#pragma unroll
+        for (int i = 0; i < T; ++i) {
+            const int2 e = stab[i * 32 + lane];
+            acc = fmaf(__int_as_float(e.y), sacc[e.x & 0x1fff], acc);
+            if (e.x >> 28) {
+                ybuf[(e.x >> 13) & 0x7fff] = acc;
+                acc = 0.f;
+            }
+        }
+        __syncwarp();
+        const float* xrow = X + (size_t)row * LD;
+        float rowdot = 0.f;
+        for (int c = lane; c < LD; c += 32) {
+            const float y = (c < P) ? ybuf[c] : 0.f;
+            yrow[c] = y;
+            if (partials) rowdot = fmaf(xrow[c], y, rowdot);
+        }
+        dot += (double)rowdot;
+        __syncwarp();
+    }
+    if (failed) {
+        if (lane == 0) atomicExch(err, 1);
+        // copies still in flight land in this warp's ring: wait for them (bounded) before exiting
+        for (int k = 0; k < inflight; ++k) {
+            mbar_wait(bars_a + 8 * sc, (phase >> sc) & 1u);
+            phase ^= 1u << sc;
+            sc = (sc + 1 == ADEPTH) ? 0 : sc + 1;
+        }
+    }
+    if (partials) {
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
+        if (lane == 0) red[warp] = dot;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t2 = 0.0;
+            for (int w2 = 0; w2 < WPB; ++w2) t2 += red[w2];
+            partials[blockIdx.x] = t2;
+        }
+    }
+}
+)";
+    return s;
+}
+
+// Variant with the column groups split into passes (jit_np > 1): for every row
+// the warp runs over the row's nonzeros once per pass, loading only the pass's X
+// column groups and keeping only the pass's slot accumulators, then folds the
+// pass into ybuf with the pass's part of the combination schedule.  Fewer live
+// accumulators and a smaller slot buffer per warp let more warps share an SM.
+std::string generate_source_passes(const sgfem_context* ctx) {
+    const int LD = (int)ctx->ld, P = (int)ctx->P, M1P = ctx->M1P;
+    const int KG = (int)((P + 31) / 32);
+    const int NP = ctx->jit_np;
+    int maxps = 0;
+    for (int p = 0; p < NP; ++p) maxps = std::max(maxps, ctx->jit_pass_slot0[p + 1] - ctx->jit_pass_slot0[p]);
+    std::string s;
+    char buf[512];
+    snprintf(buf, sizeof(buf),
+             "#define LD %d\n#define P %d\n#define KG %d\n#define M1P %d\n#define NSP %d\n#define WPB %d\n"
+             "#define RCHUNK %d\n#define T %d\n#define MINB %d\n",
+             LD, P, KG, M1P, maxps, JWPB, ctx->jit_rchunk, ctx->jit_T, ctx->jit_minb);
+    s += buf;
+    s += R"(
+#define NV4 (M1P / 4)
+#define CBUF (32 * M1P)
+#define WSMEM (NSP * 64 + 2 * CBUF + LD)   /* floats per warp */
+struct Scal { double rho, pq, alpha, beta, rr, tol2; int done, status, iters, first; };
+
+#define LOAD_VALUES(pv, nz, cnt)                                                        \
+    _Pragma("unroll") for (int i_ = 0; i_ < NV4; ++i_) {                                \
+        const int q_ = lane + 32 * i_;                                                  \
+        pv[i_] = (q_ < (cnt) * NV4) ? __ldg(reinterpret_cast<const float4*>(vals + (size_t)(nz) * M1P) + q_) \
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);                  \
+    }
+#define STORE_VALUES(dst, pv)                                                           \
+    _Pragma("unroll") for (int i_ = 0; i_ < NV4; ++i_)                                  \
+        reinterpret_cast<float4*>(dst)[lane + 32 * i_] = pv[i_];
+
+#if MINB > 0
+extern "C" __global__ void __launch_bounds__(WPB * 32, MINB)
+#else
+extern "C" __global__ void __launch_bounds__(WPB * 32)
+#endif
+sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const float* __restrict__ vals,
+             const float* __restrict__ X, float* __restrict__ Y, int n, const unsigned char* __restrict__ bmask,
+             const int2* __restrict__ jtab, double* __restrict__ partials, const Scal* __restrict__ scal,
+             int* __restrict__ err) {
+    if (scal && scal->done) return;
+    extern __shared__ __align__(16) float smem[];
+    __shared__ double red[WPB];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int2* stab = reinterpret_cast<int2*>(smem);
+    float* wb = smem + 2 * T * 32 + warp * WSMEM;
+    float* sacc = wb;
+    float* cbuf = wb + NSP * 64;
+    float* ybuf = cbuf + 2 * CBUF;
+    for (int i = threadIdx.x; i < T * 32; i += blockDim.x) stab[i] = __ldg(jtab + i);
+    __syncthreads();
+    double dot = 0.0;
+    const int nw = gridDim.x * WPB, w = blockIdx.x * WPB + warp;
+    const int stride = nw * RCHUNK;
+#define NEXT_ROW(r) ((((r) + 1) % RCHUNK) ? ((r) + 1) : ((r) + 1 - RCHUNK + stride))
+    int row = w * RCHUNK;
+    int jn1 = 0, cn1 = 0, b = 0;
+    float4 pv[NV4];
+    if (row < n) {
+        const int a = rowptr[row];
+        cn1 = min(32, rowptr[row + 1] - a);
+        jn1 = (lane < cn1) ? __ldg(col + a + lane) : 0;
+        LOAD_VALUES(pv, a, cn1);
+        STORE_VALUES(cbuf, pv);
+        __syncwarp();
+    }
+    for (; row < n; row = NEXT_ROW(row)) {
+        const int jcur = jn1;
+        const int r1n = NEXT_ROW(row);
+        if (r1n < n) {
+            const int a = __ldg(rowptr + r1n);
+            cn1 = min(32, __ldg(rowptr + r1n + 1) - a);
+            jn1 = (lane < cn1) ? __ldg(col + a + lane) : 0;
+            LOAD_VALUES(pv, a, cn1);
+        }
+        float* yrow = Y + (size_t)row * LD;
+        if (bmask[row]) {
+            for (int c = lane; c < LD; c += 32) yrow[c] = 0.f;
+        } else {
+            const int nz0 = rowptr[row], nz1 = rowptr[row + 1];
+            for (int c = lane; c < LD; c += 32) ybuf[c] = 0.f;
+            const float* cb = cbuf + b * CBUF;
+)";
+    int toff = 0;
+    for (int p = 0; p < NP; ++p) {
+        const int s0 = ctx->jit_pass_slot0[p], s1 = ctx->jit_pass_slot0[p + 1];
+        const int k0 = ctx->jit_pass_k0[p], k1 = ctx->jit_pass_k0[p + 1];
+        // KLE value float4s this pass reads
+        std::vector<char> usev(M1P / 4, 0);
+        for (int q = s0; q < s1; ++q) usev[ctx->jit_slots[q].first / 2] = 1;
+        snprintf(buf, sizeof(buf), "            // ---- pass %d: column groups [%d, %d), slots [%d, %d)\n            {\n", p, k0,
+                 k1, s0, s1);
+        s += buf;
+        for (int q = s0; q < s1; ++q) {
+            snprintf(buf, sizeof(buf), "            float2 a%d = make_float2(0.f, 0.f);\n", q);
+            s += buf;
+        }
+        s += R"(            for (int base = nz0; base < nz1; base += 32) {
+                const int cnt = min(32, nz1 - base);
+                int jl = jcur;
+                if (base != nz0) {  // rows longer than 32 nonzeros: later chunks load synchronously
+                    jl = (lane < cnt) ? __ldg(col + base + lane) : 0;
+                    float4 lv[NV4];
+                    __syncwarp();
+                    LOAD_VALUES(lv, base, cnt);
+                    STORE_VALUES(cbuf + b * CBUF, lv);
+                    __syncwarp();
+                }
+#pragma unroll 2
+                for (int t = 0; t < cnt; ++t) {
+                const int j = __shfl_sync(0xffffffffu, jl, t);
+                const float4* cv = reinterpret_cast<const float4*>(cb + t * M1P);
+                const float* xr = X + (size_t)j * LD + lane;
+)";
+        for (int v = 0; v < M1P / 4; ++v)
+            if (usev[v]) {
+                snprintf(buf, sizeof(buf), "                const float4 c%d = cv[%d];\n", v, v);
+                s += buf;
+            }
+        for (int k = k0; k < k1; ++k) {
+            const int valid = LD - 32 * k;
+            if (valid >= 32)
+                snprintf(buf, sizeof(buf), "                const float u%d = __ldg(xr + %d);\n", k, 32 * k);
+            else
+                snprintf(buf, sizeof(buf), "                const float u%d = (lane < %d) ? __ldg(xr + %d) : 0.f;\n",
+                         k, valid, 32 * k);
+            s += buf;
+            snprintf(buf, sizeof(buf), "                const float2 w%d = make_float2(u%d, u%d);\n", k, k, k);
+            s += buf;
+        }
+        for (int q = s0; q < s1; ++q) {
+            const int pr = ctx->jit_slots[q].first, k = ctx->jit_slots[q].second;
+            const int v = pr / 2;
+            const char* comp = (pr % 2 == 0) ? "x, c%d.y" : "z, c%d.w";
+            char cpair[64];
+            snprintf(cpair, sizeof(cpair), comp, v);
+            snprintf(buf, sizeof(buf), "                a%d = __ffma2_rn(make_float2(c%d.%s), w%d, a%d);\n", q, v, cpair,
+                     k, q);
+            s += buf;
+        }
+        s += "                }\n            }\n";
+        for (int q = s0; q < s1; ++q) {
+            snprintf(buf, sizeof(buf), "            *reinterpret_cast<float2*>(sacc + %d + 2 * lane) = a%d;\n",
+                     (q - s0) * 64, q);
+            s += buf;
+        }
+        snprintf(buf, sizeof(buf), R"(            __syncwarp();
+            {
+                float acc = 0.f;
+#pragma unroll
+                for (int i = 0; i < %d; ++i) {
+                    const int2 e = stab[(%d + i) * 32 + lane];
+                    acc = fmaf(__int_as_float(e.y), sacc[e.x & 0x1fff], acc);
+                    if (e.x >> 28) {
+                        ybuf[(e.x >> 13) & 0x7fff] += acc;
+                        acc = 0.f;
+                    }
+                }
+            }
+            __syncwarp();
+            }
+)",
+                 ctx->jit_pass_T[p], toff);
+        s += buf;
+        toff += ctx->jit_pass_T[p];
+    }
+    s += R"(            const float* xrow = X + (size_t)row * LD;
+            float rowdot = 0.f;
+            for (int c = lane; c < LD; c += 32) {
+                const float y = (c < P) ? ybuf[c] : 0.f;
+                yrow[c] = y;
+                if (partials) rowdot = fmaf(xrow[c], y, rowdot);
+            }
+            dot += (double)rowdot;
+        }
+        if (r1n < n) {  // stage the next row's values
+            __syncwarp();
+            b ^= 1;
+            STORE_VALUES(cbuf + b * CBUF, pv);
+            __syncwarp();
+        }
+    }
+    if (partials) {
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
+        if (lane == 0) red[warp] = dot;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t2 = 0.0;
+            for (int w2 = 0; w2 < WPB; ++w2) t2 += red[w2];
+            partials[blockIdx.x] = t2;
+        }
+    }
+}
+)";
+    return s;
+}
+
 size_t jit_smem_bytes(const sgfem_context* ctx) {
     const int NS = (int)ctx->jit_slots.size();
+    if (ctx->jit_np > 1 && !ctx->jit_async) {
+        int maxps = 0;
+        for (int p = 0; p < ctx->jit_np; ++p)
+            maxps = std::max(maxps, ctx->jit_pass_slot0[p + 1] - ctx->jit_pass_slot0[p]);
+        const size_t wsmem = (size_t)maxps * 64 + 2 * 32 * (size_t)ctx->M1P + ctx->ld;
+        return (2 * (size_t)ctx->jit_T * 32 + JWPB * wsmem) * sizeof(float);
+    }
+    if (ctx->jit_async) {
+        const size_t wsmem = (size_t)ctx->jit_adepth * (ctx->ld + ctx->M1P) + (size_t)NS * 64 + ctx->ld +
+                             (ctx->jit_async == 2 ? 2 * (size_t)ctx->jit_adepth : 0);
+        return (2 * (size_t)ctx->jit_T * 32 + JWPB * wsmem) * sizeof(float);
+    }
     const size_t wsmem = (size_t)NS * 64 + (ctx->jit_stage ? 2 * 32 * ctx->M1P : 0) + ((ctx->ld + 3) & ~3);
     return (2 * (size_t)ctx->jit_T * 32 + JWPB * wsmem) * sizeof(float);
 }
@@ -346,6 +1035,17 @@ void sg_jit_configure(sgfem_context* ctx) {
     ctx->jit_stage = es ? (atoi(es) != 0) : 1;
     ctx->jit_bps_cap = eb ? std::max(1, atoi(eb)) : 8;
     ctx->jit_carveout = ec ? atoi(ec) : -1;
+    const char* ed = getenv("SGFEM_JIT_PFD");
+    ctx->jit_pfd = ed ? std::max(1, std::min(8, atoi(ed))) : 1;
+    const char* ea = getenv("SGFEM_JIT_ASYNC");
+    ctx->jit_async = ea ? std::max(0, std::min(2, atoi(ea))) : 0;
+    const char* eq = getenv("SGFEM_JIT_ADEPTH");
+    ctx->jit_adepth = eq ? std::max(2, std::min(16, atoi(eq))) : 6;
+    const char* en = getenv("SGFEM_JIT_PASSES");
+    ctx->jit_np_req = en ? std::max(1, std::min(8, atoi(en))) : 1;
+    if (ctx->jit_async) ctx->jit_np_req = 1;  // the copy-pipeline variants use one pass
+    const char* em = getenv("SGFEM_JIT_MINB");
+    ctx->jit_minb = em ? std::max(0, std::min(8, atoi(em))) : 0;
 }
 
 int sg_jit_build(sgfem_context* ctx) {
@@ -367,7 +1067,9 @@ int sg_jit_build(sgfem_context* ctx) {
         ctx->jit_log = g_drv.err;
         return SGFEM_ERR_UNSUPPORTED;
     }
-    const std::string src = generate_source(ctx);
+    const std::string src = ctx->jit_async == 2 ? generate_source_bulk(ctx)
+                            : ctx->jit_async ? generate_source_async(ctx)
+                            : ctx->jit_np > 1 ? generate_source_passes(ctx) : generate_source(ctx);
     nvrtcProgram prog = nullptr;
     if (g_nvrtc.create(&prog, src.c_str(), "sgfem_apply_jit.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) {
         ctx->jit_log = "nvrtcCreateProgram failed";
@@ -420,6 +1122,15 @@ int sg_jit_build(sgfem_context* ctx) {
         ctx->jit_log = "occupancy query failed";
         return SGFEM_ERR_UNSUPPORTED;
     }
+    if (!ctx->d_jit_err) {
+        if (cudaMalloc((void**)&ctx->d_jit_err, sizeof(int)) != cudaSuccess ||
+            cudaMemset(ctx->d_jit_err, 0, sizeof(int)) != cudaSuccess) {
+            g_drv.module_unload(mod);
+            ctx->d_jit_err = nullptr;
+            ctx->jit_log = "status word allocation failed";
+            return SGFEM_ERR_UNSUPPORTED;
+        }
+    }
     ctx->jit_blocks_per_sm = std::min(bps, ctx->jit_bps_cap);
     ctx->jit_module = mod;
     ctx->jit_func = fn;
@@ -445,8 +1156,9 @@ int sg_jit_launch(sgfem_context* ctx, const void* X, void* Y, double* partials, 
     int n = (int)ctx->n;
     const unsigned char* bm = ctx->d_bmask;
     const int2* jtab = ctx->d_jtab;
+    int* errp = ctx->d_jit_err;
     void* args[] = {(void*)&rowptr, (void*)&colp, (void*)&vals, (void*)&X, (void*)&Y, (void*)&n, (void*)&bm,
-                    (void*)&jtab, (void*)&partials, (void*)&scal};
+                    (void*)&jtab, (void*)&partials, (void*)&scal, (void*)&errp};
     CUresult r = g_drv.launch_kernel((CUfunction)ctx->jit_func, grid, 1, 1, JWPB * 32, 1, 1, smem,
                                      (CUstream)ctx->stream, args, nullptr);
     if (r != CUDA_SUCCESS) return sg_fail(ctx, SGFEM_ERR_CUDA, "cuLaunchKernel(sg_apply_jit) failed: " + std::to_string((int)r));
@@ -454,7 +1166,20 @@ int sg_jit_launch(sgfem_context* ctx, const void* X, void* Y, double* partials, 
     return SGFEM_OK;
 }
 
+// status word of the specialised kernel (a timed-out copy wait); resets it
+int sg_jit_check(sgfem_context* ctx) {
+    if (!ctx->jit_ok || !ctx->d_jit_err) return SGFEM_OK;
+    int h = 0;
+    SG_CUDA(ctx, cudaMemcpyAsync(&h, ctx->d_jit_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h == 0) return SGFEM_OK;
+    SG_CUDA(ctx, cudaMemsetAsync(ctx->d_jit_err, 0, sizeof(int), ctx->stream));
+    return sg_fail(ctx, SGFEM_ERR_CUDA, "specialised apply: a shared-memory copy did not complete in time");
+}
+
 void sg_jit_release(sgfem_context* ctx) {
+    if (ctx->d_jit_err) cudaFree(ctx->d_jit_err);
+    ctx->d_jit_err = nullptr;
     if (ctx->jit_module && g_drv.loaded) g_drv.module_unload((CUmodule)ctx->jit_module);
     ctx->jit_module = nullptr;
     ctx->jit_func = nullptr;

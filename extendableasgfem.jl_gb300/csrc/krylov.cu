@@ -569,6 +569,7 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
     SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     st->time_ms = ms;
     st->kernel_launches = ctx->launches - launches0;
+    if (low) SG_TRY(sg_jit_check(ctx));
     st->relres = ctx->batched ? colmax : std::sqrt(rr / bb);
     if (status == SGFEM_OK && !(st->relres <= o->rtol)) status = (o->precision == SGFEM_FP32) ? SGFEM_OK : SGFEM_ERR_MAXIT;
     return status_message(ctx, status);

@@ -192,14 +192,26 @@ __device__ __forceinline__ size_t lat_row(int dir, int line, int p, int Nl) {
     return dir == 0 ? (size_t)line * (Nl + 1) + p : (size_t)p * (Nl + 1) + line;
 }
 
+// LAT_UNROLL points per warp are loaded before any is stored, so that many
+// global loads are in flight per warp instead of one
+constexpr int LAT_UNROLL = 8;
+
 template <typename T>
 __device__ void load_line(T* tile, const T* __restrict__ in, int dir, int line, int chunk, LatGeom g) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int mode = chunk * 32 + lane;
-    for (int p = 1 + warp; p < g.Nl; p += LAT_WARPS) {
-        T v = T(0);
-        if (mode < g.ld) v = in[lat_row(dir, line, p, g.Nl) * g.ld + mode];
-        tile[p * 32 + lane] = v;
+    for (int p0 = 1 + warp; p0 < g.Nl; p0 += LAT_WARPS * LAT_UNROLL) {
+        T v[LAT_UNROLL];
+#pragma unroll
+        for (int u = 0; u < LAT_UNROLL; ++u) {
+            const int p = p0 + u * LAT_WARPS;
+            v[u] = (p < g.Nl && mode < g.ld) ? in[lat_row(dir, line, p, g.Nl) * g.ld + mode] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < LAT_UNROLL; ++u) {
+            const int p = p0 + u * LAT_WARPS;
+            if (p < g.Nl) tile[p * 32 + lane] = v[u];
+        }
     }
 }
 
@@ -222,13 +234,24 @@ k_lat_pass_x(const T* __restrict__ in, T* __restrict__ out, const T* __restrict_
     if (m >= g.ld) return;
     T beta = T(0);
     if (mode == 1 && scal && !scal->first) beta = (T)scal->beta;
-    for (int p = 1 + warp; p < g.Nl; p += LAT_WARPS) {
-        const size_t idx = lat_row(0, line, p, g.Nl) * g.ld + m;
-        const T z = tile[p * 32 + lane];
-        if (mode == 1)
-            out[idx] = z + beta * out[idx];
-        else
-            out[idx] = z;
+    for (int p0 = 1 + warp; p0 < g.Nl; p0 += LAT_WARPS * LAT_UNROLL) {
+        T old[LAT_UNROLL];
+        if (mode == 1) {
+#pragma unroll
+            for (int u = 0; u < LAT_UNROLL; ++u) {
+                const int p = p0 + u * LAT_WARPS;
+                old[u] = (p < g.Nl) ? out[lat_row(0, line, p, g.Nl) * g.ld + m] : T(0);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < LAT_UNROLL; ++u) {
+            const int p = p0 + u * LAT_WARPS;
+            if (p < g.Nl) {
+                const size_t idx = lat_row(0, line, p, g.Nl) * g.ld + m;
+                const T z = tile[p * 32 + lane];
+                out[idx] = (mode == 1) ? z + beta * old[u] : z;
+            }
+        }
     }
 }
 
@@ -249,11 +272,22 @@ k_lat_pass_y(T* __restrict__ buf, const T* __restrict__ tab, const T* __restrict
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int N = g.Nl - 1;
     double acc = 0.0;
-    for (int p = 1 + warp; p < g.Nl; p += LAT_WARPS) {
-        const T sc = scale[(size_t)(line - 1) * N + (p - 1)];
-        const T v = tile[p * 32 + lane];
-        acc += (double)v * (double)v * (double)sc;
-        tile[p * 32 + lane] = v * sc;
+    for (int p0 = 1 + warp; p0 < g.Nl; p0 += LAT_WARPS * LAT_UNROLL) {
+        T sc[LAT_UNROLL];
+#pragma unroll
+        for (int u = 0; u < LAT_UNROLL; ++u) {
+            const int p = p0 + u * LAT_WARPS;
+            sc[u] = (p < g.Nl) ? scale[(size_t)(line - 1) * N + (p - 1)] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < LAT_UNROLL; ++u) {
+            const int p = p0 + u * LAT_WARPS;
+            if (p < g.Nl) {
+                const T v = tile[p * 32 + lane];
+                acc += (double)v * (double)v * (double)sc[u];
+                tile[p * 32 + lane] = v * sc[u];
+            }
+        }
     }
     __syncthreads();
     dst_line<T, LGL>(tile, stab);

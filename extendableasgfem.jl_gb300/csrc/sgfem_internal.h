@@ -114,13 +114,23 @@ struct sgfem_context {
     float* d_jg = nullptr;                  // coefficients
     int2* d_jtab = nullptr;                 // lane schedule of the combination, [T][32]
     int jit_T = 0;                          // entries per lane in d_jtab (-1: does not fit)
+    int jit_np_req = 1;                     // passes asked for (SGFEM_JIT_PASSES)
+    int jit_np = 1;                         // passes over the nonzeros of a row (column-group ranges)
+    std::vector<int> jit_pass_k0;           // first column group of pass p (np + 1 entries)
+    std::vector<int> jit_pass_slot0;        // first slot of pass p (np + 1 entries)
+    std::vector<int> jit_pass_T;            // combination entries per lane of pass p
     int jit_rchunk = 8;                     // rows per warp chunk
     int jit_prefetch = 0;
+    int jit_pfd = 1;                        // X prefetch distance in nonzeros (register window)
+    int jit_minb = 0;                       // minimum resident blocks per SM asked of ptxas (0: none)
+    int jit_async = 0;                      // cp.async ring variant of the kernel
+    int jit_adepth = 6;                     // ring slots (nonzeros in flight + 1) per warp
     int jit_stage = 1;                      // KLE values staged in shared memory
     int jit_bps_cap = 8;                    // resident blocks per SM used by the grid
     int jit_carveout = -1;                  // preferred shared-memory carve-out (%), -1 default
     void* jit_module = nullptr;             // CUmodule
     void* jit_func = nullptr;               // CUfunction
+    int* d_jit_err = nullptr;               // status word of the specialised kernel
     bool jit_ok = false;
     bool jit_tried = false;      // the specialised FP32 apply is compiled at its first use
     bool jit_disabled = false;   // SGFEM_APPLY=generic at finalize
@@ -195,6 +205,8 @@ int sg_jit_ensure(sgfem_context* ctx);
 int sg_jit_grid(const sgfem_context* ctx);
 int sg_jit_launch(sgfem_context* ctx, const void* X, void* Y, double* partials, int grid, const KrylovScalars* scal);
 void sg_jit_release(sgfem_context* ctx);
+// error status of the specialised kernel since the last check (resets it)
+int sg_jit_check(sgfem_context* ctx);
 
 // ------------------------------------------------------------------ layout (context.cu)
 int sg_launch_to_device(sgfem_context* ctx, const double* stage, void* X, int precision);
