@@ -553,6 +553,40 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args):
+    """Config 4 batching: the SG problems of the SplitMix64 stream (seed = problem
+    index; n x n P1 mesh with n = 16 + r % 113, M = 4 + r % 13, total degree
+    1 + r % 3), all solved together to 1e-8 by the batched Jacobi-PCG."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    shapes = pkg.config4_problems(args.problems)
+    B = pkg.SGBatch(0)
+    t0 = time.perf_counter()
+    unknowns = 0
+    for N, M, d in shapes:
+        mis = pkg.total_degree_multiindices(M, d)
+        TB = pkg.TensorizedBasis(pkg.LegendrePolynomials, M, d, d + 4, multi_indices=mis)
+        V = pkg.H1Pk(pkg.unit_square_mesh(N), 1)
+        sol = pkg.SGFEVector(V, TB)
+        Ks, b0 = pkg.assemble(pkg.PoissonProblemPrimal, sol, C, rhs=lambda x, y: np.ones_like(x))
+        B.add(V, TB, Ks, b0)
+        unknowns += V.ndofs * TB.nmodes
+    t_setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    B.finalize()
+    t_fin = time.perf_counter() - t0
+    _, st = B.solve(rtol=1e-8, maxit=20000, check_every=16, want_solutions=False)
+    line = {"workload": f"batch: {len(shapes)} SG problems (SplitMix64 shapes), {unknowns} unknowns in total, "
+                        f"Jacobi-PCG to 1e-8 in one launch per phase",
+            "solve_ms": st["time_ms"], "problems_per_s": len(shapes) / (st["time_ms"] * 1e-3),
+            "iterations_max": st["iterations_max"], "converged": st["converged"], "relres_max": st["relres_max"],
+            "graph_replays": st["graph_replays"], "kernel_launches": st["kernel_launches"],
+            "host_setup_s": t_setup, "finalize_s": t_fin, "tuning": B.tuning[:400]}
+    B.close()
+    print(json.dumps(line), flush=True)
+
+
 def ctx_qn(op):
     # pair count P + sum_m nzcols(G_m), from the coupling matrix
     G = op.TB.G.tocsr()
@@ -574,17 +608,18 @@ def main():
     ap.add_argument("--profile", choices=["apply32", "apply64", "solve"], default=None,
                     help="profiling target for ncu: set up the workload, run the kernel(s) a few times, exit")
     ap.add_argument("--mesh", type=int, default=256, help="mesh size for --profile / --workload adjoint")
-    ap.add_argument("--workload", choices=["config2", "config1", "lognormal", "sampling", "adjoint"],
+    ap.add_argument("--workload", choices=["config2", "config1", "lognormal", "sampling", "adjoint", "batch"],
                     default="config2", help="config2 is the headline bench line; the others print their own line")
     ap.add_argument("--samples", type=int, default=100000, help="--workload sampling: number of samples")
     ap.add_argument("--directions", type=int, default=20, help="--workload adjoint: finite-difference directions")
     ap.add_argument("--restart", type=int, default=100, help="--workload lognormal: GMRES restart length")
+    ap.add_argument("--problems", type=int, default=256, help="--workload batch: number of problems")
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)
     if args.workload != "config2":
         return {"config1": run_config1, "lognormal": run_lognormal, "sampling": run_sampling,
-                "adjoint": run_adjoint}[args.workload](args)
+                "adjoint": run_adjoint, "batch": run_batch}[args.workload](args)
     rank, world, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world, pg)

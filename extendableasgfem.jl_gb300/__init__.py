@@ -8,6 +8,7 @@ The directory name follows the Julia package naming; import it through
 from . import _lib
 from ._lib import FP32, FP64, MIXED, PREC_JACOBI, PREC_LATTICE, PREC_NONE, SGError
 from .adjoint import MeanQoI
+from .batch import SGBatch, config4_problems, splitmix64
 from .coefficients import StochasticCoefficientCosinus
 from .estimate import estimate, extension_couplings
 from .fem import (H1Pk, assemble_convection, assemble_laplacian, assemble_pce_rhs, assemble_rhs, assemble_stiffness,
@@ -24,7 +25,8 @@ from .sgfevector import SGFEVector
 from .tensorizedbasis import TensorizedBasis, coupling_matrix
 
 __all__ = [
-    "FP32", "FP64", "MIXED", "PREC_JACOBI", "PREC_LATTICE", "PREC_NONE", "SGError", "MeanQoI",
+    "FP32", "FP64", "MIXED", "PREC_JACOBI", "PREC_LATTICE", "PREC_NONE", "SGError", "MeanQoI", "SGBatch",
+    "config4_problems", "splitmix64",
     "assemble_stiffness_nodal_mean", "box_functional",
     "StochasticCoefficientCosinus", "estimate", "extension_couplings", "H1Pk", "assemble_convection",
     "assemble_laplacian", "assemble_pce_rhs", "assemble_rhs", "assemble_stiffness", "line_rule", "pce_lambda",

@@ -49,6 +49,15 @@ class SolveStats(ctypes.Structure):
 
 
 # name -> (restype, argtypes); every symbol declared in include/sgfem.h
+class BatchStats(ctypes.Structure):
+    _fields_ = [("iterations_max", ctypes.c_int), ("converged", ctypes.c_int), ("graph_replays", ctypes.c_int),
+                ("relres_max", ctypes.c_double), ("time_ms", ctypes.c_double), ("kernel_launches", ctypes.c_longlong)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+
 SIGNATURES = {
     "sgfem_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int]),
     "sgfem_destroy": (ctypes.c_int, [_P]),
@@ -78,6 +87,18 @@ SIGNATURES = {
     "sgfem_solve_gmres": (ctypes.c_int, [_P, _DP, _DP, ctypes.POINTER(SolveOptions), ctypes.c_int,
                                          ctypes.POINTER(SolveStats)]),
     "sgfem_adjoint_gradient": (ctypes.c_int, [_P, _DP, _DP, _DP, _P, _DP]),
+    "sgfem_batch_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int]),
+    "sgfem_batch_destroy": (ctypes.c_int, [_P]),
+    "sgfem_batch_last_error": (ctypes.c_char_p, [_P]),
+    "sgfem_batch_add": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _I64P, _I64P, _DP, _I64P,
+                                       _I64P, _DP, ctypes.c_int64, _I64P, _DP]),
+    "sgfem_batch_count": (ctypes.c_int, [_P]),
+    "sgfem_batch_finalize": (ctypes.c_int, [_P]),
+    "sgfem_batch_tuning": (ctypes.c_char_p, [_P]),
+    "sgfem_batch_solve": (ctypes.c_int, [_P, ctypes.c_double, ctypes.c_int, ctypes.c_int, _DP,
+                                         ctypes.POINTER(BatchStats)]),
+    "sgfem_batch_problem_stats": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                                 ctypes.POINTER(ctypes.c_double)]),
     "sgfem_evaluate_samples": (ctypes.c_int, [_P, _DP, ctypes.c_int64, _P, _DP, ctypes.c_int64, ctypes.c_int64,
                                               ctypes.c_int64, _DP]),
     "sgfem_sampling_error": (ctypes.c_int, [_P, _DP, _P, _P, _DP, _P, _P, _DP, _DP]),

@@ -1,0 +1,139 @@
+"""Batches of independent SG problems on one GPU (host side of K8).
+
+The reference solves one problem per solve! call (src/modelproblems/
+poisson_primal.jl:38-81).  ``SGBatch`` hands many PoissonProblemPrimal systems
+to the library at once (sgfem_batch_*): one Jacobi-preconditioned CG runs all
+of them in lock step, each phase one launch over every problem, iterations
+replayed from a captured CUDA graph.  ``config4_problems`` draws the problem
+shapes from a SplitMix64 stream (seed = problem index):
+n = 16 + r % 113 (n x n P1 mesh), M = 4 + r % 13, total degree 1 + r % 3.
+"""
+import ctypes
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _lib
+
+_MASK64 = (1 << 64) - 1
+
+
+def splitmix64(x):
+    """One output of SplitMix64 for the state x (Steele, Lea, Flood 2014)."""
+    z = (x + 0x9E3779B97F4A7C15) & _MASK64
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _MASK64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _MASK64
+    return z ^ (z >> 31)
+
+
+def config4_problems(count=256, n_lo=16, n_span=113, m_lo=4, m_span=13, deg_span=3):
+    """[(N, M, degree)] for problem indices 0..count-1."""
+    out = []
+    for i in range(count):
+        r = splitmix64(i)
+        out.append((n_lo + r % n_span, m_lo + r % m_span, 1 + r % deg_span))
+    return out
+
+
+def _shared_pattern_values(Ks):
+    """CSC pattern of K_0 and the (M+1) x nnz values of every K_m on it."""
+    K0 = sp.csc_matrix(Ks[0])
+    K0.sort_indices()
+    vals = np.zeros((len(Ks), K0.nnz))
+    for m, K in enumerate(Ks):
+        Kc = sp.csc_matrix(K)
+        Kc.sort_indices()
+        if Kc.nnz == K0.nnz and np.array_equal(Kc.indptr, K0.indptr) and np.array_equal(Kc.indices, K0.indices):
+            vals[m] = Kc.data
+        else:  # values on K_0's pattern (entries outside it would be lost: refuse)
+            extra = abs(Kc) - abs(Kc).multiply(K0 != 0)
+            if extra.nnz and abs(extra).max() > 0:
+                raise ValueError("K_m has entries outside the pattern of K_0")
+            vals[m] = _take(Kc, K0)
+    return K0, vals
+
+
+def _take(Kc, K0):
+    out = np.zeros(K0.nnz)
+    for j in range(K0.shape[1]):
+        rows = K0.indices[K0.indptr[j]:K0.indptr[j + 1]]
+        col = Kc[:, j].toarray().ravel()
+        out[K0.indptr[j]:K0.indptr[j + 1]] = col[rows]
+    return out
+
+
+class SGBatch:
+    def __init__(self, device=0):
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        rc = self.lib.sgfem_batch_create(ctypes.byref(h), int(device))
+        if rc != _lib.OK:
+            raise _lib.SGError(rc, "sgfem_batch_create failed")
+        self.h = h
+        self.shapes = []
+
+    def _check(self, rc, allow=()):
+        if rc != _lib.OK and rc not in allow:
+            raise _lib.SGError(rc, self.lib.sgfem_batch_last_error(self.h).decode())
+
+    def add(self, FES, TB, Ks, b0):
+        """One PoissonProblemPrimal system: K_0..K_M (shared pattern), TB.G, FES boundary dofs, b0."""
+        K0, vals = _shared_pattern_values(Ks)
+        n = K0.shape[0]
+        M = len(Ks) - 1
+        P = TB.nmodes
+        colptr = np.ascontiguousarray(K0.indptr.astype(np.int64) + 1)
+        rowval = np.ascontiguousarray(K0.indices.astype(np.int64) + 1)
+        vals = np.ascontiguousarray(vals)
+        G = sp.csc_matrix(TB.G)
+        G.sort_indices()
+        gcp = np.ascontiguousarray(G.indptr.astype(np.int64) + 1)
+        grv = np.ascontiguousarray(G.indices.astype(np.int64) + 1)
+        gv = np.ascontiguousarray(G.data.astype(np.float64))
+        bd = np.ascontiguousarray(np.asarray(FES.bdofs, dtype=np.int64) + 1)
+        b0 = np.ascontiguousarray(b0, dtype=np.float64)
+        i64 = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        self._check(self.lib.sgfem_batch_add(self.h, n, M, P, i64(colptr), i64(rowval), _lib._dp(vals), i64(gcp),
+                                             i64(grv), _lib._dp(gv), len(bd), i64(bd), _lib._dp(b0)))
+        self.shapes.append((n, P))
+        return len(self.shapes) - 1
+
+    def finalize(self):
+        self._check(self.lib.sgfem_batch_finalize(self.h))
+
+    @property
+    def tuning(self):
+        return self.lib.sgfem_batch_tuning(self.h).decode()
+
+    def solve(self, rtol=1e-8, maxit=20000, check_every=16, allow_maxit=False, want_solutions=True):
+        """Solutions (list of n*P arrays, SGFEVector entries layout) and stats."""
+        total = sum(n * P for n, P in self.shapes)
+        x = np.zeros(total) if want_solutions else None
+        st = _lib.BatchStats()
+        self._check(self.lib.sgfem_batch_solve(self.h, float(rtol), int(maxit), int(check_every),
+                                               _lib._dp(x) if x is not None else None, ctypes.byref(st)),
+                    allow=(_lib.ERR_MAXIT,) if allow_maxit else ())
+        out = []
+        if x is not None:
+            off = 0
+            for n, P in self.shapes:
+                out.append(x[off:off + n * P])
+                off += n * P
+        return out, st.as_dict()
+
+    def problem_stats(self, i):
+        it = ctypes.c_int()
+        rr = ctypes.c_double()
+        self._check(self.lib.sgfem_batch_problem_stats(self.h, int(i), ctypes.byref(it), ctypes.byref(rr)))
+        return it.value, rr.value
+
+    def close(self):
+        if self.h:
+            self.lib.sgfem_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,759 @@
+// K8: many independent SG problems solved together on sm_103a.
+//
+// Each problem is the SG system of solve_primal! (src/modelproblems/
+// solvers_poisson_primal.jl:130-169) on its own mesh, coefficient length M and
+// multi-index set: Y_mu = K_0 X_mu + sum_{m,nu} G[(m-1)P+mu,nu] K_m X_nu with
+// Dirichlet rows zeroed, b = e_1 (x) b0.  All problems advance through one
+// Jacobi-preconditioned CG in lock step: every phase of an iteration (apply,
+// alpha, update, preconditioner, beta, direction) is one launch covering all
+// problems, and a batch of iterations is captured once in a CUDA graph and
+// replayed; converged problems skip their blocks.
+//
+// Work split: problem p owns the contiguous block range [blk0, blk0 + nblk) of
+// every batch kernel (block counts proportional to the problem's apply work),
+// so each block's reduction partial belongs to one problem and the per-problem
+// sums are fixed-order reductions over that range (bitwise reproducible).
+// The apply is the pair-gather of the single-problem generic kernel with the
+// problem's tables read from a descriptor; its launch shape (warps per block,
+// pairs per lane, blocks) is chosen at finalize by timing the candidates
+// (autotuner).  FP64 throughout.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "sgfem_internal.h"
+
+struct BProb {
+    int n, P, ld, M1, Qn;
+    int blk0, nblk;
+    long long voff;               // offset of the problem's vectors (n * ld values)
+    const int* rowptr;
+    const int* col;
+    const double* vals;           // [nnz][M1]
+    const unsigned char* bmask;
+    const double* dinv;           // 0 on Dirichlet rows
+    const int* qtab;              // m << 16 | nu
+    const int* combptr;
+    const int* combq;
+    const double* combg;
+};
+
+struct sgfem_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string err;
+    int num_sms = 0;
+    bool finalized = false;
+    long long launches = 0;
+    // host problems
+    struct HostProb {
+        int n, P, M1, ld;
+        std::vector<int> rowptr, col;
+        std::vector<double> vals, dinv, b0;
+        std::vector<unsigned char> bmask;
+        std::vector<int> qtab, combptr, combq;
+        std::vector<double> combg;
+        double work;
+    };
+    std::vector<HostProb> hp;
+    // device
+    std::vector<void*> owned;
+    BProb* d_probs = nullptr;
+    int* d_bprob = nullptr;
+    KrylovScalars* d_scal = nullptr;
+    double *d_x = nullptr, *d_b = nullptr, *d_r = nullptr, *d_p = nullptr, *d_q = nullptr, *d_part = nullptr;
+    long long total = 0;          // sum of n * ld
+    int blocks = 0, wpb = 4, qt = 4, ldmax = 0, m1max = 0, qnmax = 0;
+    std::string tuning;
+    std::vector<KrylovScalars> h_scal;
+    double rtol = 0.0;            // of the last solve
+};
+
+namespace {
+
+constexpr int BT = 256;  // threads of the vector kernels
+
+int bfail(sgfem_batch* b, int code, const std::string& msg) {
+    b->err = msg;
+    return code;
+}
+#define BCUDA(b, call)                                                                  \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess) return bfail(b, SGFEM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+#define BLAUNCHED(b)                                                                    \
+    do {                                                                                \
+        (b)->launches++;                                                                \
+        cudaError_t e_ = cudaGetLastError();                                            \
+        if (e_ != cudaSuccess) return bfail(b, SGFEM_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+__device__ __forceinline__ void block_sum_store(double v, double* out) {
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+        *out = s;
+    }
+}
+
+// Y = S X for every problem, p'q partials per block
+template <int QT>
+__global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict__ bprob, const double* __restrict__ X,
+                         double* __restrict__ Y, double* __restrict__ partials, const KrylovScalars* __restrict__ scal,
+                         int per_warp) {
+    const int pi = bprob[blockIdx.x];
+    const BProb& d = probs[pi];
+    extern __shared__ double bsm[];
+    const int wpb = blockDim.x >> 5;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (scal && scal[pi].done) {
+        if (threadIdx.x == 0 && partials) partials[blockIdx.x] = 0.0;
+        return;
+    }
+    double* su = bsm + (size_t)warp * per_warp;
+    double* sc = su + d.ld;
+    double* sacc = sc + d.M1 + 1;
+    if (lane == 0) sc[d.M1] = 0.0;
+    const double* Xp = X + d.voff;
+    double* Yp = Y + d.voff;
+    double dot = 0.0;
+    const int lb = blockIdx.x - d.blk0;
+    for (int row = lb * wpb + warp; row < d.n; row += d.nblk * wpb) {
+        double* yrow = Yp + (size_t)row * d.ld;
+        if (d.bmask[row]) {
+            for (int c = lane; c < d.ld; c += 32) yrow[c] = 0.0;
+            continue;
+        }
+        const int nz0 = d.rowptr[row], nz1 = d.rowptr[row + 1];
+        for (int base = 0; base < d.Qn; base += QT * 32) {
+            int om[QT], on[QT];
+            double acc[QT];
+#pragma unroll
+            for (int t = 0; t < QT; ++t) {
+                const int q = base + t * 32 + lane;
+                if (q < d.Qn) {
+                    const int e = d.qtab[q];
+                    om[t] = e >> 16;
+                    on[t] = e & 0xffff;
+                } else {
+                    om[t] = d.M1;
+                    on[t] = 0;
+                }
+                acc[t] = 0.0;
+            }
+            for (int nz = nz0; nz < nz1; ++nz) {
+                const int j = d.col[nz];
+                const double* xs = Xp + (size_t)j * d.ld;
+                for (int c = lane; c < d.ld; c += 32) su[c] = __ldg(xs + c);
+                if (lane < d.M1) sc[lane] = d.vals[(size_t)nz * d.M1 + lane];
+                __syncwarp();
+#pragma unroll
+                for (int t = 0; t < QT; ++t) acc[t] = fma(sc[om[t]], su[on[t]], acc[t]);
+                __syncwarp();
+            }
+#pragma unroll
+            for (int t = 0; t < QT; ++t) {
+                const int q = base + t * 32 + lane;
+                if (q < d.Qn) sacc[q] = acc[t];
+            }
+        }
+        __syncwarp();
+        const double* xrow = Xp + (size_t)row * d.ld;
+        for (int mu = lane; mu < d.ld; mu += 32) {
+            double y = 0.0;
+            if (mu < d.P) {
+                y = sacc[mu];
+                for (int e = d.combptr[mu]; e < d.combptr[mu + 1]; ++e) y = fma(d.combg[e], sacc[d.combq[e]], y);
+            }
+            yrow[mu] = y;
+            dot = fma(xrow[mu], y, dot);
+        }
+        __syncwarp();
+    }
+    if (partials) {
+        __shared__ double red[32];
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
+        if (lane == 0) red[warp] = dot;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0;
+            for (int w = 0; w < wpb; ++w) s += red[w];
+            partials[blockIdx.x] = s;
+        }
+    }
+}
+
+enum BFin { BF_ALPHA = 0, BF_RR = 1, BF_BETA = 2, BF_TOL = 3 };
+
+// one block per problem: sum its block partials in order, update its scalars
+__global__ void k_bfin(const BProb* __restrict__ probs, const double* __restrict__ partials,
+                       KrylovScalars* __restrict__ scal, int mode, double rtol2, int maxit) {
+    const BProb& d = probs[blockIdx.x];
+    KrylovScalars* s = scal + blockIdx.x;
+    __shared__ double red[BT];
+    double v = 0.0;
+    for (int i = threadIdx.x; i < d.nblk; i += BT) v += partials[d.blk0 + i];
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = BT / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    const double sum = red[0];
+    if (mode == BF_TOL) {
+        s->tol2 = rtol2 * sum;
+        s->rr = sum;
+        if (sum == 0.0) s->done = 1;
+        return;
+    }
+    if (s->done) return;
+    if (mode == BF_ALPHA) {
+        s->pq = sum;
+        if (!isfinite(sum)) { s->status = SGFEM_ERR_NONFINITE; s->done = 1; return; }
+        if (!(sum > 0.0)) { s->status = SGFEM_ERR_BREAKDOWN; s->done = 1; return; }
+        s->alpha = s->rho / sum;
+    } else if (mode == BF_RR) {
+        s->rr = sum;
+        if (!s->first) s->iters += 1;
+        if (!isfinite(sum)) { s->status = SGFEM_ERR_NONFINITE; s->done = 1; return; }
+        if (sum <= s->tol2) { s->done = 1; return; }
+        if (s->iters >= maxit) { s->status = SGFEM_ERR_MAXIT; s->done = 1; return; }
+    } else if (mode == BF_BETA) {
+        if (!isfinite(sum)) { s->status = SGFEM_ERR_NONFINITE; s->done = 1; return; }
+        if (!(sum > 0.0)) { s->status = SGFEM_ERR_BREAKDOWN; s->done = 1; return; }
+        s->beta = s->first ? 0.0 : sum / s->rho;
+        s->first = 0;
+        s->rho = sum;
+    }
+}
+
+// element range of block blockIdx.x within its problem's vectors
+#define BRANGE                                                                          \
+    const int pi = bprob[blockIdx.x];                                                   \
+    const BProb& d = probs[pi];                                                         \
+    const long long len = (long long)d.n * d.ld;                                        \
+    const long long t0 = (long long)(blockIdx.x - d.blk0) * BT + threadIdx.x;          \
+    const long long tstep = (long long)d.nblk * BT;
+
+// x += alpha p, r -= alpha q, ||r||^2 partials
+__global__ void __launch_bounds__(BT) k_bupdate(const BProb* __restrict__ probs, const int* __restrict__ bprob,
+                                                double* __restrict__ x, const double* __restrict__ p,
+                                                double* __restrict__ r, const double* __restrict__ q,
+                                                const KrylovScalars* __restrict__ scal, double* __restrict__ partials) {
+    BRANGE;
+    double acc = 0.0;
+    if (!scal[pi].done) {
+        const double a = scal[pi].alpha;
+        for (long long t = t0; t < len; t += tstep) {
+            const long long i = d.voff + t;
+            x[i] = fma(a, p[i], x[i]);
+            const double rn = fma(-a, q[i], r[i]);
+            r[i] = rn;
+            acc = fma(rn, rn, acc);
+        }
+    }
+    block_sum_store(acc, partials + blockIdx.x);
+}
+
+// mode 0: partials of r' D^-1 r ; mode 1: p = D^-1 r + beta p ; mode 2: partials of b'b
+__global__ void __launch_bounds__(BT) k_bjacobi(const BProb* __restrict__ probs, const int* __restrict__ bprob,
+                                                const double* __restrict__ r, double* __restrict__ p,
+                                                const KrylovScalars* __restrict__ scal, double* __restrict__ partials,
+                                                int mode) {
+    BRANGE;
+    double acc = 0.0;
+    if (mode == 2 || !scal[pi].done) {
+        const double beta = (mode == 1) ? scal[pi].beta : 0.0;
+        for (long long t = t0; t < len; t += tstep) {
+            const long long i = d.voff + t;
+            const double rv = r[i];
+            if (mode == 2) {
+                acc = fma(rv, rv, acc);
+                continue;
+            }
+            const double z = d.dinv[t / d.ld] * rv;
+            if (mode == 0)
+                acc = fma(rv, z, acc);
+            else
+                p[i] = fma(beta, p[i], z);
+        }
+    }
+    if (mode != 1) block_sum_store(acc, partials + blockIdx.x);
+}
+
+// b = e_1 (x) b0 (Dirichlet rows zero) in the device layout; x = 0
+__global__ void k_brhs(const double* __restrict__ b0, long long off_b0, double* __restrict__ b, double* __restrict__ x,
+                       long long voff, int n, int ld, const unsigned char* __restrict__ bmask) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < (long long)n * ld;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int row = (int)(t / ld), c = (int)(t % ld);
+        b[voff + t] = (c == 0 && !bmask[row]) ? b0[off_b0 + row] : 0.0;
+        x[voff + t] = 0.0;
+    }
+}
+
+// device layout (n x ld, row-major) -> caller layout (n x P column-major)
+__global__ void k_bout(const double* __restrict__ x, long long voff, int n, int ld, int P, double* __restrict__ out,
+                       long long ooff) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < (long long)n * P;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(t / n), row = (int)(t % n);
+        out[ooff + t] = x[voff + (long long)row * ld + c];
+    }
+}
+
+template <typename Tv>
+int bupload(sgfem_batch* b, const std::vector<Tv>& v, Tv** dst) {
+    void* p = nullptr;
+    BCUDA(b, cudaMalloc(&p, std::max<size_t>(v.size(), 1) * sizeof(Tv)));
+    b->owned.push_back(p);
+    if (!v.empty()) BCUDA(b, cudaMemcpy(p, v.data(), v.size() * sizeof(Tv), cudaMemcpyHostToDevice));
+    *dst = (Tv*)p;
+    return SGFEM_OK;
+}
+
+int balloc(sgfem_batch* b, size_t bytes, void** dst) {
+    BCUDA(b, cudaMalloc(dst, std::max<size_t>(bytes, 8)));
+    b->owned.push_back(*dst);
+    return SGFEM_OK;
+}
+
+size_t apply_smem(const sgfem_batch* b, int wpb) {
+    const size_t per_warp = ((size_t)b->ldmax + b->m1max + 1 + b->qnmax + 1) & ~(size_t)1;
+    return per_warp * sizeof(double) * wpb;
+}
+
+int launch_apply(sgfem_batch* b, int wpb, int qt, const double* X, double* Y, double* partials,
+                 const KrylovScalars* scal) {
+    const int per_warp = (int)(((size_t)b->ldmax + b->m1max + 1 + b->qnmax + 1) & ~(size_t)1);
+    const size_t smem = apply_smem(b, wpb);
+    if (qt == 4)
+        k_bapply<4><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials, scal, per_warp);
+    else
+        k_bapply<8><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials, scal, per_warp);
+    BLAUNCHED(b);
+    return SGFEM_OK;
+}
+
+// block ranges proportional to the problems' work for a given total
+int build_map(sgfem_batch* b, int total_blocks, std::vector<BProb>& probs, std::vector<int>& bprob) {
+    const int B = (int)b->hp.size();
+    double wsum = 0.0;
+    for (auto& h : b->hp) wsum += h.work;
+    std::vector<int> nb(B);
+    int used = 0;
+    for (int i = 0; i < B; ++i) {
+        nb[i] = std::max(1, (int)std::lround(total_blocks * b->hp[i].work / wsum));
+        // no more blocks than rows (apply) or useful vector chunks
+        nb[i] = std::min(nb[i], std::max(1, b->hp[i].n));
+        used += nb[i];
+    }
+    bprob.assign(used, 0);
+    int at = 0;
+    for (int i = 0; i < B; ++i) {
+        probs[i].blk0 = at;
+        probs[i].nblk = nb[i];
+        for (int k = 0; k < nb[i]; ++k) bprob[at + k] = i;
+        at += nb[i];
+    }
+    b->blocks = used;
+    return SGFEM_OK;
+}
+
+}  // namespace
+
+extern "C" int sgfem_batch_create(sgfem_batch** out, int device) {
+    if (!out) return SGFEM_ERR_ARGUMENT;
+    *out = nullptr;
+    sgfem_batch* b = new sgfem_batch();
+    b->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
+        delete b;
+        return SGFEM_ERR_CUDA;
+    }
+    cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, device);
+    *out = b;
+    return SGFEM_OK;
+}
+
+extern "C" int sgfem_batch_destroy(sgfem_batch* b) {
+    if (!b) return SGFEM_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (void* p : b->owned) cudaFree(p);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return SGFEM_OK;
+}
+
+extern "C" const char* sgfem_batch_last_error(const sgfem_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+extern "C" int sgfem_batch_add(sgfem_batch* b, int64_t n, int64_t M, int64_t P, const int64_t* colptr,
+                               const int64_t* rowval, const double* vals, const int64_t* Gcolptr,
+                               const int64_t* Growval, const double* Gval, int64_t nbd, const int64_t* bdofs,
+                               const double* b0) {
+    if (!b) return SGFEM_ERR_ARGUMENT;
+    if (b->finalized) return bfail(b, SGFEM_ERR_STATE, "batch already finalized");
+    if (n <= 0 || n > (1 << 30) || M < 0 || M > 255 || P <= 0 || P > 32767 || !colptr || !rowval || !vals ||
+        !Gcolptr || (nbd > 0 && !bdofs) || !b0)
+        return bfail(b, SGFEM_ERR_ARGUMENT, "sgfem_batch_add: bad arguments (M <= 255, P <= 32767)");
+    sgfem_batch::HostProb h;
+    h.n = (int)n;
+    h.P = (int)P;
+    h.M1 = (int)M + 1;
+    h.ld = (int)((P + 3) / 4 * 4);
+    const int64_t nnz = colptr[n] - 1;
+    if (colptr[0] != 1 || nnz < 0) return bfail(b, SGFEM_ERR_ARGUMENT, "colptr must be 1-based");
+    // CSC (shared pattern) -> CSR; vals is (M+1) x nnz column-major: value of block m at [m * nnz + k]
+    std::vector<int> cnt(n + 1, 0);
+    for (int64_t k = 0; k < nnz; ++k) {
+        const int64_t r = rowval[k] - 1;
+        if (r < 0 || r >= n) return bfail(b, SGFEM_ERR_ARGUMENT, "rowval out of range");
+        cnt[r + 1]++;
+    }
+    for (int64_t i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+    h.rowptr = cnt;
+    h.col.assign(nnz, 0);
+    h.vals.assign((size_t)nnz * h.M1, 0.0);
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (int64_t j = 0; j < n; ++j)
+        for (int64_t k = colptr[j] - 1; k < colptr[j + 1] - 1; ++k) {
+            const int r = (int)(rowval[k] - 1);
+            const int at = fill[r]++;
+            h.col[at] = (int)j;
+            for (int m = 0; m < h.M1; ++m) h.vals[(size_t)at * h.M1 + m] = vals[(size_t)m * nnz + k];
+        }
+    h.bmask.assign(n, 0);
+    for (int64_t t = 0; t < nbd; ++t) {
+        const int64_t d = bdofs[t] - 1;
+        if (d < 0 || d >= n) return bfail(b, SGFEM_ERR_ARGUMENT, "boundary dof out of range");
+        h.bmask[d] = 1;
+    }
+    h.dinv.assign(n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        if (h.bmask[i]) continue;
+        double dg = 0.0;
+        for (int k = h.rowptr[i]; k < h.rowptr[i + 1]; ++k)
+            if (h.col[k] == i) dg += h.vals[(size_t)k * h.M1];
+        if (!(dg > 0.0)) return bfail(b, SGFEM_ERR_ARGUMENT, "K_0 has a non-positive interior diagonal entry");
+        h.dinv[i] = 1.0 / dg;
+    }
+    // coupling: pairs (0, nu) for all nu, then (m, nu) for nonzero columns of G_m; combination lists per mu
+    if (Gcolptr[0] != 1) return bfail(b, SGFEM_ERR_ARGUMENT, "G colptr must be 1-based");
+    std::vector<std::vector<char>> nzc(h.M1, std::vector<char>(P, 0));
+    struct GE { int m, mu, nu; double g; };
+    std::vector<GE> ges;
+    for (int64_t nu = 0; nu < P; ++nu)
+        for (int64_t k = Gcolptr[nu] - 1; k < Gcolptr[nu + 1] - 1; ++k) {
+            const int64_t r = Growval[k] - 1;
+            if (r < 0 || r >= M * P) return bfail(b, SGFEM_ERR_ARGUMENT, "G rowval out of range");
+            if (Gval[k] == 0.0) continue;
+            const int m = (int)(r / P) + 1, mu = (int)(r % P);
+            nzc[m][nu] = 1;
+            ges.push_back({m, mu, (int)nu, Gval[k]});
+        }
+    std::vector<int> qidx((size_t)h.M1 * P, -1);
+    for (int nu = 0; nu < P; ++nu) {
+        qidx[nu] = (int)h.qtab.size();
+        h.qtab.push_back(nu);
+    }
+    for (int m = 1; m < h.M1; ++m)
+        for (int nu = 0; nu < P; ++nu)
+            if (nzc[m][nu]) {
+                qidx[(size_t)m * P + nu] = (int)h.qtab.size();
+                h.qtab.push_back((m << 16) | nu);
+            }
+    h.combptr.assign(P + 1, 0);
+    std::stable_sort(ges.begin(), ges.end(), [](const GE& x, const GE& y) { return x.mu < y.mu; });
+    for (auto& e : ges) {
+        h.combptr[e.mu + 1]++;
+        h.combq.push_back(qidx[(size_t)e.m * P + e.nu]);
+        h.combg.push_back(e.g);
+    }
+    for (int mu = 0; mu < P; ++mu) h.combptr[mu + 1] += h.combptr[mu];
+    h.b0.assign(b0, b0 + n);
+    h.work = (double)nnz * (double)h.qtab.size() + 4.0 * (double)n * h.ld;
+    b->hp.push_back(std::move(h));
+    return SGFEM_OK;
+}
+
+extern "C" int sgfem_batch_count(const sgfem_batch* b) { return b ? (int)b->hp.size() : 0; }
+
+extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
+    if (!b) return SGFEM_ERR_ARGUMENT;
+    if (b->finalized) return bfail(b, SGFEM_ERR_STATE, "batch already finalized");
+    if (b->hp.empty()) return bfail(b, SGFEM_ERR_STATE, "no problems added");
+    BCUDA(b, cudaSetDevice(b->device));
+    const int B = (int)b->hp.size();
+    std::vector<BProb> probs(B);
+    long long voff = 0;
+    for (int i = 0; i < B; ++i) {
+        auto& h = b->hp[i];
+        BProb& d = probs[i];
+        d.n = h.n;
+        d.P = h.P;
+        d.ld = h.ld;
+        d.M1 = h.M1;
+        d.Qn = (int)h.qtab.size();
+        d.voff = voff;
+        voff += (long long)h.n * h.ld;
+        SG_TRY(bupload(b, h.rowptr, (int**)&d.rowptr));
+        SG_TRY(bupload(b, h.col, (int**)&d.col));
+        SG_TRY(bupload(b, h.vals, (double**)&d.vals));
+        SG_TRY(bupload(b, h.bmask, (unsigned char**)&d.bmask));
+        SG_TRY(bupload(b, h.dinv, (double**)&d.dinv));
+        SG_TRY(bupload(b, h.qtab, (int**)&d.qtab));
+        SG_TRY(bupload(b, h.combptr, (int**)&d.combptr));
+        SG_TRY(bupload(b, h.combq, (int**)&d.combq));
+        SG_TRY(bupload(b, h.combg, (double**)&d.combg));
+        b->ldmax = std::max(b->ldmax, h.ld);
+        b->m1max = std::max(b->m1max, h.M1);
+        b->qnmax = std::max(b->qnmax, d.Qn);
+    }
+    b->total = voff;
+    const size_t vb = (size_t)voff * sizeof(double);
+    SG_TRY(balloc(b, vb, (void**)&b->d_x));
+    SG_TRY(balloc(b, vb, (void**)&b->d_b));
+    SG_TRY(balloc(b, vb, (void**)&b->d_r));
+    SG_TRY(balloc(b, vb, (void**)&b->d_p));
+    SG_TRY(balloc(b, vb, (void**)&b->d_q));
+    SG_TRY(balloc(b, (size_t)B * sizeof(KrylovScalars), (void**)&b->d_scal));
+    BCUDA(b, cudaMemset(b->d_x, 0, vb));
+    BCUDA(b, cudaMemset(b->d_p, 0, vb));
+    b->h_scal.assign(B, KrylovScalars{});
+    BCUDA(b, cudaMemset(b->d_scal, 0, (size_t)B * sizeof(KrylovScalars)));
+
+    // ---- autotune the apply: warps per block x pairs per lane x blocks per SM
+    struct Cand { int wpb, qt, bps; };
+    std::vector<Cand> cands;
+    for (int wpb : {2, 4, 8})
+        for (int qt : {4, 8})
+            for (int bps : {4, 8, 16}) cands.push_back({wpb, qt, bps});
+    int dev_smem = 0;
+    cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
+    float best = 1e30f;
+    Cand bestc{0, 0, 0};
+    std::vector<int> bprob;
+    BProb* d_probs = nullptr;
+    SG_TRY(balloc(b, (size_t)B * sizeof(BProb), (void**)&d_probs));
+    b->d_probs = d_probs;
+    int* d_bmap = nullptr;
+    const int max_blocks = b->num_sms * 16 + B;
+    SG_TRY(balloc(b, (size_t)std::max(max_blocks, 1) * 4 * sizeof(int), (void**)&d_bmap));
+    b->d_bprob = d_bmap;
+    SG_TRY(balloc(b, (size_t)std::max(max_blocks, 1) * 4 * sizeof(double), (void**)&b->d_part));
+    std::string log;
+    for (const Cand& c : cands) {
+        const size_t smem = apply_smem(b, c.wpb);
+        if ((int)smem > dev_smem) continue;
+        if (smem > 48 * 1024) {
+            cudaError_t e = (c.qt == 4) ? cudaFuncSetAttribute(k_bapply<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                                        : cudaFuncSetAttribute(k_bapply<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+        }
+        SG_TRY(build_map(b, b->num_sms * c.bps, probs, bprob));
+        if ((int)bprob.size() > max_blocks * 4) continue;
+        BCUDA(b, cudaMemcpy(b->d_probs, probs.data(), (size_t)B * sizeof(BProb), cudaMemcpyHostToDevice));
+        BCUDA(b, cudaMemcpy(b->d_bprob, bprob.data(), bprob.size() * sizeof(int), cudaMemcpyHostToDevice));
+        SG_TRY(launch_apply(b, c.wpb, c.qt, b->d_p, b->d_q, b->d_part, nullptr));  // warm-up
+        BCUDA(b, cudaEventRecord(b->ev0, b->stream));
+        for (int r = 0; r < 3; ++r) SG_TRY(launch_apply(b, c.wpb, c.qt, b->d_p, b->d_q, b->d_part, nullptr));
+        BCUDA(b, cudaEventRecord(b->ev1, b->stream));
+        BCUDA(b, cudaEventSynchronize(b->ev1));
+        float ms = 0.f;
+        BCUDA(b, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+        char buf[96];
+        snprintf(buf, sizeof(buf), "%dw/%dq/%dbps:%.3fms ", c.wpb, c.qt, c.bps, ms / 3);
+        log += buf;
+        if (ms < best) {
+            best = ms;
+            bestc = c;
+        }
+    }
+    if (bestc.wpb == 0) return bfail(b, SGFEM_ERR_UNSUPPORTED, "no apply launch shape fits the shared memory");
+    b->wpb = bestc.wpb;
+    b->qt = bestc.qt;
+    SG_TRY(build_map(b, b->num_sms * bestc.bps, probs, bprob));
+    BCUDA(b, cudaMemcpy(b->d_probs, probs.data(), (size_t)B * sizeof(BProb), cudaMemcpyHostToDevice));
+    BCUDA(b, cudaMemcpy(b->d_bprob, bprob.data(), bprob.size() * sizeof(int), cudaMemcpyHostToDevice));
+    char buf[128];
+    snprintf(buf, sizeof(buf), "chosen %d warps/block, %d pairs/lane, %d blocks; ", b->wpb, b->qt * 32, b->blocks);
+    b->tuning = buf + log;
+    b->finalized = true;
+    return SGFEM_OK;
+}
+
+extern "C" const char* sgfem_batch_tuning(const sgfem_batch* b) { return b ? b->tuning.c_str() : ""; }
+
+namespace {
+
+int batch_iteration(sgfem_batch* b, int maxit) {
+    const int B = (int)b->hp.size();
+    SG_TRY(launch_apply(b, b->wpb, b->qt, b->d_p, b->d_q, b->d_part, b->d_scal));
+    k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_ALPHA, 0.0, maxit);
+    BLAUNCHED(b);
+    k_bupdate<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_x, b->d_p, b->d_r, b->d_q, b->d_scal, b->d_part);
+    BLAUNCHED(b);
+    k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_RR, 0.0, maxit);
+    BLAUNCHED(b);
+    k_bjacobi<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_r, b->d_p, b->d_scal, b->d_part, 0);
+    BLAUNCHED(b);
+    k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_BETA, 0.0, maxit);
+    BLAUNCHED(b);
+    k_bjacobi<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_r, b->d_p, b->d_scal, nullptr, 1);
+    BLAUNCHED(b);
+    return SGFEM_OK;
+}
+
+}  // namespace
+
+extern "C" int sgfem_batch_solve(sgfem_batch* b, double rtol, int maxit, int check_every, double* x_out,
+                                 sgfem_batch_stats* stats) {
+    if (!b) return SGFEM_ERR_ARGUMENT;
+    if (!b->finalized) return bfail(b, SGFEM_ERR_STATE, "batch not finalized");
+    if (!(rtol > 0.0) || maxit <= 0) return bfail(b, SGFEM_ERR_ARGUMENT, "rtol must be > 0 and maxit > 0");
+    check_every = std::max(1, std::min(check_every, 64));
+    BCUDA(b, cudaSetDevice(b->device));
+    const int B = (int)b->hp.size();
+    const long long launches0 = b->launches;
+    b->rtol = rtol;
+    // right-hand sides (upload b0 of every problem, then build b, x = 0)
+    std::vector<double> b0all;
+    std::vector<long long> b0off(B);
+    for (int i = 0; i < B; ++i) {
+        b0off[i] = (long long)b0all.size();
+        b0all.insert(b0all.end(), b->hp[i].b0.begin(), b->hp[i].b0.end());
+    }
+    double* d_b0 = nullptr;
+    BCUDA(b, cudaMalloc((void**)&d_b0, b0all.size() * sizeof(double)));
+    cudaError_t ce = cudaMemcpyAsync(d_b0, b0all.data(), b0all.size() * sizeof(double), cudaMemcpyHostToDevice, b->stream);
+    std::vector<BProb> probs(B);
+    if (ce == cudaSuccess)
+        ce = cudaMemcpy(probs.data(), b->d_probs, (size_t)B * sizeof(BProb), cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) {
+        cudaFree(d_b0);
+        return bfail(b, SGFEM_ERR_CUDA, std::string("upload: ") + cudaGetErrorString(ce));
+    }
+    BCUDA(b, cudaEventRecord(b->ev0, b->stream));
+    for (int i = 0; i < B; ++i) {
+        const int g = (int)std::min<long long>(((long long)probs[i].n * probs[i].ld + 255) / 256, 1024);
+        k_brhs<<<g, 256, 0, b->stream>>>(d_b0, b0off[i], b->d_b, b->d_x, probs[i].voff, probs[i].n, probs[i].ld,
+                                         probs[i].bmask);
+        BLAUNCHED(b);
+    }
+    BCUDA(b, cudaMemcpyAsync(b->d_r, b->d_b, (size_t)b->total * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+    BCUDA(b, cudaMemsetAsync(b->d_p, 0, (size_t)b->total * sizeof(double), b->stream));
+    // scalars: tol2 = rtol^2 ||b||^2 per problem, first = 1
+    for (auto& s : b->h_scal) {
+        std::memset(&s, 0, sizeof(s));
+        s.first = 1;
+    }
+    BCUDA(b, cudaMemcpyAsync(b->d_scal, b->h_scal.data(), (size_t)B * sizeof(KrylovScalars), cudaMemcpyHostToDevice,
+                             b->stream));
+    k_bjacobi<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_r, b->d_p, b->d_scal, b->d_part, 2);
+    BLAUNCHED(b);
+    k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_TOL, rtol * rtol, maxit);
+    BLAUNCHED(b);
+    // first direction: rho = r'Dr, p = D r
+    k_bjacobi<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_r, b->d_p, b->d_scal, b->d_part, 0);
+    BLAUNCHED(b);
+    k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_BETA, 0.0, maxit);
+    BLAUNCHED(b);
+    k_bjacobi<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_r, b->d_p, b->d_scal, nullptr, 1);
+    BLAUNCHED(b);
+    // graph of check_every iterations
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    const long long before = b->launches;
+    int st = SGFEM_OK;
+    for (int k = 0; k < check_every && st == SGFEM_OK; ++k) st = batch_iteration(b, maxit);
+    const long long per_graph = b->launches - before;
+    b->launches = before;
+    ce = cudaStreamEndCapture(b->stream, &graph);
+    if (st != SGFEM_OK || ce != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaFree(d_b0);
+        return st != SGFEM_OK ? st : bfail(b, SGFEM_ERR_CUDA, "graph capture failed");
+    }
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    int replays = 0;
+    int status = SGFEM_OK;
+    while (ce == cudaSuccess) {
+        ce = cudaMemcpyAsync(b->h_scal.data(), b->d_scal, (size_t)B * sizeof(KrylovScalars), cudaMemcpyDeviceToHost,
+                             b->stream);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(b->stream);
+        if (ce != cudaSuccess) break;
+        bool all = true;
+        for (auto& s : b->h_scal) all = all && s.done;
+        if (all) break;
+        ce = cudaGraphLaunch(exec, b->stream);
+        b->launches += per_graph;
+        ++replays;
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    cudaFree(d_b0);
+    if (ce != cudaSuccess) return bfail(b, SGFEM_ERR_CUDA, std::string("batch iteration: ") + cudaGetErrorString(ce));
+    BCUDA(b, cudaEventRecord(b->ev1, b->stream));
+    BCUDA(b, cudaEventSynchronize(b->ev1));
+    float ms = 0.f;
+    BCUDA(b, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    sgfem_batch_stats s{};
+    s.time_ms = ms;
+    s.graph_replays = replays;
+    s.kernel_launches = b->launches - launches0;
+    s.converged = 0;
+    for (int i = 0; i < B; ++i) {
+        const KrylovScalars& k = b->h_scal[i];
+        s.iterations_max = std::max(s.iterations_max, k.iters);
+        const double rel = k.tol2 > 0.0 ? std::sqrt(k.rr * rtol * rtol / k.tol2) : 0.0;
+        s.relres_max = std::max(s.relres_max, rel);
+        if (k.status == SGFEM_OK && k.done) s.converged++;
+        else if (status == SGFEM_OK) status = k.status ? k.status : SGFEM_ERR_MAXIT;
+    }
+    if (stats) *stats = s;
+    if (x_out) {
+        double* d_out = nullptr;
+        long long ototal = 0;
+        for (int i = 0; i < B; ++i) ototal += (long long)probs[i].n * probs[i].P;
+        BCUDA(b, cudaMalloc((void**)&d_out, (size_t)ototal * sizeof(double)));
+        long long oo = 0;
+        for (int i = 0; i < B; ++i) {
+            const int g = (int)std::min<long long>(((long long)probs[i].n * probs[i].P + 255) / 256, 1024);
+            k_bout<<<g, 256, 0, b->stream>>>(b->d_x, probs[i].voff, probs[i].n, probs[i].ld, probs[i].P, d_out, oo);
+            oo += (long long)probs[i].n * probs[i].P;
+        }
+        ce = cudaMemcpyAsync(x_out, d_out, (size_t)ototal * sizeof(double), cudaMemcpyDeviceToHost, b->stream);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(b->stream);
+        cudaFree(d_out);
+        if (ce != cudaSuccess) return bfail(b, SGFEM_ERR_CUDA, std::string("download: ") + cudaGetErrorString(ce));
+    }
+    if (status == SGFEM_ERR_MAXIT) return bfail(b, status, "some problems did not reach the tolerance within maxit");
+    if (status != SGFEM_OK) return bfail(b, status, "a problem broke down (non-finite value or breakdown)");
+    return SGFEM_OK;
+}
+
+extern "C" int sgfem_batch_problem_stats(const sgfem_batch* b, int i, int* iterations, double* relres) {
+    if (!b || i < 0 || i >= (int)b->h_scal.size()) return SGFEM_ERR_ARGUMENT;
+    const KrylovScalars& k = b->h_scal[i];
+    if (iterations) *iterations = k.iters;
+    if (relres) *relres = k.tol2 > 0.0 ? b->rtol * std::sqrt(k.rr / k.tol2) : 0.0;
+    return SGFEM_OK;
+}

@@ -27,9 +27,23 @@ def generate_multiindices(M, deg):
 
 
 def total_degree_multiindices(M, deg):
-    """Total-degree set sum(mu) <= deg: generate_multiindices order, stably
+    """Total-degree set sum(mu) <= deg: generate_multiindices order (the
+    members of the tensor set with sum <= deg, enumerated directly with the
+    running sum pruned instead of filtering (deg+1)^M candidates), stably
     sorted by total degree (the zero index first)."""
-    mis = [mi for mi in generate_multiindices(M, deg) if sum(mi) <= deg]
+    mis = []
+    cur = [0] * M
+
+    def rec(d, rem):
+        if d == M:
+            mis.append(list(cur))
+            return
+        for j in range(min(deg, rem) + 1):
+            cur[d] = j
+            rec(d + 1, rem - j)
+        cur[d] = 0
+
+    rec(0, deg)
     return sorted(mis, key=sum)
 
 

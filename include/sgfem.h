@@ -325,6 +325,43 @@ SGFEM_API int sgfem_precondition_device_static(sgfem_context* ctx, const void* r
 SGFEM_API int sgfem_adjoint_gradient(sgfem_context* ctx, const double* U, const double* Lambda, double* dblocks,
                                      const sgfem_mesh* mesh, double* dalpha);
 
+/*
+ * Batches of independent SG problems (no counterpart in the reference, which
+ * solves one problem per solve! call, poisson_primal.jl:38-81).  Each problem
+ * is the PoissonProblemPrimal system of solve_primal! with b = e_1 (x) b0 and a
+ * zero start: its own n, K_0..K_M on one shared pattern (1-based CSC, values
+ * (M+1) x nnz column-major), coupling G ((M*P) x P, 1-based CSC), boundary dofs
+ * and b0.  sgfem_batch_solve runs Jacobi-preconditioned CG on all problems in
+ * lock step: each phase of an iteration is one launch over every problem, a
+ * batch of check_every iterations is a captured CUDA graph, converged problems
+ * skip their blocks.  The apply's launch shape is chosen at finalize by timing
+ * the candidates (sgfem_batch_tuning reports them).  x_out receives the
+ * solutions, problem after problem, each n x P column-major (may be NULL).
+ * FP64; per-problem reductions in a fixed order.  M <= 255.
+ */
+typedef struct sgfem_batch sgfem_batch;
+typedef struct {
+    int iterations_max;            /* largest iteration count over the problems */
+    int converged;                 /* problems that reached rtol */
+    int graph_replays;
+    double relres_max;             /* largest final ||b - A x|| / ||b|| */
+    double time_ms;                /* device time of the solve (CUDA events) */
+    long long kernel_launches;
+} sgfem_batch_stats;
+SGFEM_API int sgfem_batch_create(sgfem_batch** batch, int device);
+SGFEM_API int sgfem_batch_destroy(sgfem_batch* batch);
+SGFEM_API const char* sgfem_batch_last_error(const sgfem_batch* batch);
+SGFEM_API int sgfem_batch_add(sgfem_batch* batch, int64_t n, int64_t M, int64_t P, const int64_t* colptr,
+                              const int64_t* rowval, const double* vals, const int64_t* Gcolptr,
+                              const int64_t* Growval, const double* Gval, int64_t nbdofs, const int64_t* bdofs,
+                              const double* b0);
+SGFEM_API int sgfem_batch_count(const sgfem_batch* batch);
+SGFEM_API int sgfem_batch_finalize(sgfem_batch* batch);
+SGFEM_API const char* sgfem_batch_tuning(const sgfem_batch* batch);
+SGFEM_API int sgfem_batch_solve(sgfem_batch* batch, double rtol, int maxit, int check_every, double* x_out,
+                                sgfem_batch_stats* stats);
+SGFEM_API int sgfem_batch_problem_stats(const sgfem_batch* batch, int i, int* iterations, double* relres);
+
 /* which FP32 apply kernel a finalized context uses: 1 = specialised to the coupling
    structure (compiled with NVRTC at finalize), 0 = generic; the log says why */
 SGFEM_API int sgfem_apply_variant(const sgfem_context* ctx);

@@ -1,0 +1,53 @@
+"""Batched SG solves (sgfem_batch_*): every problem of a batch with uneven
+mesh sizes, coefficient lengths and multi-index sets against the oracle's
+assembled Kronecker solve (solve_full_primal!, solvers_poisson_primal.jl:
+172-230).  Bar: rtol 1e-10 on the FP64 true residual, solutions within 1e-8."""
+import numpy as np
+import pytest
+
+from oracle import sg as osg
+from tests.problems import build
+
+pytestmark = pytest.mark.gpu
+
+
+def test_batch_matches_kronecker_solves(built_pkg):
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    shapes = [(5, 2, 2), (7, 3, 1), (6, 4, 3), (4, 2, 1), (9, 3, 2), (8, 1, 3), (5, 5, 2), (6, 3, 3)]
+    probs = [build(N, 1, M, pkg.total_degree_multiindices(M, d)) for N, M, d in shapes]
+    probs.append(build(4, 2, 3, pkg.total_degree_multiindices(3, 2)))  # one P2 problem
+    B = pkg.SGBatch(0)
+    for p in probs:
+        B.add(p.V, p.TB, p.Kall, p.b0)
+    B.finalize()
+    assert "chosen" in B.tuning
+    xs, st = B.solve(rtol=1e-10, check_every=8)
+    assert st["converged"] == len(probs)
+    assert st["relres_max"] <= 1e-10
+    for i, (p, x) in enumerate(zip(probs, xs)):
+        ref = osg.kron_direct(p.K0, p.Ks, p.G, p.b0, p.bdofs, p.P)
+        assert np.linalg.norm(x - ref) <= 1e-8 * np.linalg.norm(ref), i
+        it, rr = B.problem_stats(i)
+        assert it > 0 and rr <= 1e-10
+    B.close()
+
+
+def test_batch_equals_single_problem_solver(built_pkg):
+    """A problem solved inside a batch gives the single-problem solver's answer."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    p = build(16, 1, 4, pkg.total_degree_multiindices(4, 2))
+    q = build(12, 1, 3, pkg.total_degree_multiindices(3, 3))
+    B = pkg.SGBatch(0)
+    B.add(p.V, p.TB, p.Kall, p.b0)
+    B.add(q.V, q.TB, q.Kall, q.b0)
+    B.finalize()
+    xs, st = B.solve(rtol=1e-11)
+    for prob, x in ((p, xs[0]), (q, xs[1])):
+        op = pkg.SGOperator(prob.V, prob.TB, prob.Kall, device=0)
+        y = np.zeros(prob.n * prob.P)
+        op.solve_primal(prob.b0, y, rtol=1e-11, precision=pkg.FP64, reference_rhs=False)
+        op.close()
+        assert np.linalg.norm(x - y) <= 1e-8 * np.linalg.norm(y)
+    B.close()

@@ -192,3 +192,21 @@ def test_lognormal_assembly_matches_oracle(pkg):
         b = pkg.assemble_pce_rhs(V, C, mis, lambda x, y: np.ones_like(x), order + 1)
         br = of.assemble_pce_rhs(Vo, Co, mis, f, order + 1)
         assert np.abs(b - br).max() <= 1e-13 * np.abs(br).max()
+
+
+def test_splitmix64_and_config4_stream(pkg):
+    """SplitMix64 (seed 0 gives 0xe220a8397b1dcdaf, the published first output) and
+    the config-4 shapes drawn from it: n in [16, 128], M in [4, 16], degree in {1, 2, 3}."""
+    assert pkg.splitmix64(0) == 0xE220A8397B1DCDAF
+    shapes = pkg.config4_problems(256)
+    assert len(shapes) == 256
+    assert all(16 <= n <= 128 and 4 <= M <= 16 and 1 <= d <= 3 for n, M, d in shapes)
+    assert len(set(shapes)) > 200
+
+
+def test_total_degree_set_equals_filtered_tensor_set(pkg):
+    """The pruned enumeration gives exactly the filtered generate_multiindices list."""
+    for M, d in ((3, 2), (5, 2), (4, 3), (6, 1), (2, 4)):
+        ref = sorted([mi for mi in pkg.generate_multiindices(M, d) if sum(mi) <= d], key=sum)
+        assert pkg.total_degree_multiindices(M, d) == ref
+    assert len(pkg.total_degree_multiindices(16, 3)) == 969
