@@ -243,12 +243,13 @@ struct Owned {
 
 }  // namespace
 
-extern "C" int sgfem_estimate_primal(sgfem_context* ctx, const double* sol, const sgfem_mesh* mesh,
-                                     const sgfem_quadrature* quad, const double* f_qp, const sgfem_cosine* coef,
-                                     const sgfem_extension* ext, double* eta4modes, double* eta4cell) {
+// host geometry, topology, coefficient terms 0..Mcoef and coupling lists -> device (EstArgs)
+static int build_est(sgfem_context* ctx, const double* sol, const sgfem_mesh* mesh, const sgfem_quadrature* quad,
+                     const double* f_qp, const sgfem_cosine* coef, const sgfem_extension* ext, int64_t Mcoef,
+                     Owned& own, EstArgs& a, std::vector<int>& cfaces_out) {
     SG_TRY(sg_check_ready(ctx));
-    if (!sol || !mesh || !quad || !f_qp || !coef || !ext || !eta4modes || !eta4cell)
-        return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "sgfem_estimate_primal: null argument");
+    if (!sol || !mesh || !quad || !f_qp || !coef || !ext)
+        return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "estimator: null argument");
     if (mesh->order != 1 && mesh->order != 2) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "order must be 1 or 2");
     const int nd = mesh->order == 1 ? 3 : 6;
     const int64_t nc = mesh->ncells, nf = mesh->nfaces, nn = mesh->nnodes;
@@ -323,10 +324,11 @@ extern "C" int sgfem_estimate_primal(sgfem_context* ctx, const double* sol, cons
             *loc[s][1] = fb;
         }
     }
-    // coefficient terms 0..M_ext
-    std::vector<double> d(Mext + 1, 0.0);
-    std::vector<int> b1(Mext + 1, 0), b2(Mext + 1, 0);
-    for (int64_t m = 1; m <= Mext; ++m) {
+    // coefficient terms 0..Mcoef (>= M_ext)
+    if (Mcoef < Mext || Mcoef > coef->maxm) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "coefficient terms out of range");
+    std::vector<double> d(Mcoef + 1, 0.0);
+    std::vector<int> b1(Mcoef + 1, 0), b2(Mcoef + 1, 0);
+    for (int64_t m = 1; m <= Mcoef; ++m) {
         d[m] = coef->decay_factors[m - 1];
         b1[m] = (int)coef->b1[m - 1];
         b2[m] = (int)coef->b2[m - 1];
@@ -344,8 +346,7 @@ extern "C" int sgfem_estimate_primal(sgfem_context* ctx, const double* sol, cons
     }
 
     // ---- device data
-    Owned own;
-    EstArgs a{};
+    a = EstArgs{};
     a.order = mesh->order;
     a.nd = nd;
     a.nq = quad->nq;
@@ -375,12 +376,26 @@ extern "C" int sgfem_estimate_primal(sgfem_context* ctx, const double* sol, cons
     a.cg = dcg; a.cdofs = dcd; a.cfaces = dcf; a.fg = dfg; a.xq = dxq; a.wq = dwq; a.tf = dtf; a.wf = dwf; a.fqp = dfq;
     a.lptr = dlp; a.lm = dlm; a.lnu = dln; a.lg = dlg;
     a.coef = Coef{(int)Mext, M_PI * coef->freq, dd, db1, db2, coef->mean};
+    cfaces_out = cfaces;
     // solution in the device layout
     const size_t vb = sg_vec_bytes(ctx, SGFEM_FP64);
     SG_TRY(sg_ensure(ctx, ctx->w_vec[11], vb));
     SG_TRY(sgfem_to_device_layout(ctx, sol, ctx->w_vec[11].p, SGFEM_FP64));
     a.U = (const double*)ctx->w_vec[11].p;
 
+    return SGFEM_OK;
+}
+
+extern "C" int sgfem_estimate_primal(sgfem_context* ctx, const double* sol, const sgfem_mesh* mesh,
+                                     const sgfem_quadrature* quad, const double* f_qp, const sgfem_cosine* coef,
+                                     const sgfem_extension* ext, double* eta4modes, double* eta4cell) {
+    if (!eta4modes || !eta4cell) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "sgfem_estimate_primal: null argument");
+    Owned own;
+    EstArgs a{};
+    std::vector<int> cfh;
+    SG_TRY(build_est(ctx, sol, mesh, quad, f_qp, coef, ext, ext ? ext->M_ext : 0, own, a, cfh));
+    const int64_t nc = a.ncells, nf = a.nfaces, Pext = a.Pext, Mext = a.coef.M;
+    const int* dcf = a.cfaces;
     const int chunk = 64;
     double *d_eta, *d_jumps, *d_vsum, *d_jsum;
     SG_CUDA(ctx, cudaMalloc((void**)&d_eta, (size_t)nc * Pext * sizeof(double)));
@@ -423,5 +438,259 @@ extern "C" int sgfem_estimate_primal(sgfem_context* ctx, const double* sol, cons
                                  ctx->stream));
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     for (int64_t j = 0; j < Pext; ++j) eta4modes[j] = std::sqrt(vsum[j] + jsum[j]);
+    return SGFEM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// estimate(::Type{LogTransformedPoissonProblemPrimal}, sol, C; rhs,
+// bonus_quadorder, tail_extension), src/estimate.jl:70-257.
+//   volume term (:178-214), per cell T, extended mode j, quadrature point q:
+//       r = lambda_j(x_q) f(x_q) [+ Laplace(u_j) for P2 and active j]
+//           + sum_{(m >= 1, nu, g) in list_j} g grad a_m(x_q) . grad u_nu(x_q)
+//       eta_T,j = sum_q w_q r^2 times |T|^2 (active j) or |T| (inactive j)
+//   lambda_j: the interpolant (degree iorder on the cells) of the Hermite chaos
+//   coefficient of exp(-a) (:102-114), given by its values at the interpolation dofs;
+//   data term (:139-156): zeta1 = sum_T sum_q f^2 exp(2 sum_{m<=maxm} a_m^2) w |T|,
+//   zeta2 = sum_T sum_q sum_j lambda_j^2 f^2 w |T|;
+//   jump term (:231-246): for active j, |F| int_F |[[grad u_j]]|^2 on interior faces,
+//   added to the adjacent cells; eta4modes[j] = sqrt(V_j) + sqrt(V_j + J_j).
+namespace {
+
+struct LogArgs {
+    int iorder, ndi, Mext, maxm;
+    const int* idofs;       // ndi per cell, 0-based
+    const double* lamv;     // [j][ndofs_i]
+    long long ndofs_i;
+};
+
+__global__ void __launch_bounds__(EW * 32) k_elog_volume(EstArgs a, LogArgs l, int j0, int j1,
+                                                          double* __restrict__ eta4cell, double* __restrict__ z1,
+                                                          double* __restrict__ z2) {
+    extern __shared__ double esm[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int per = 2 * a.P * a.nq + a.P + 2 * l.Mext * a.nq + a.nq * 6 + a.nq;
+    double* GU = esm + (size_t)warp * per;     // [nu][q][2] grad u_nu
+    double* LU = GU + 2 * a.P * a.nq;          // [nu] Laplace u_nu (P2)
+    double* GA = LU + a.P;                     // [m-1][q][2] grad a_m
+    double* PI = GA + 2 * l.Mext * a.nq;       // [q][ndi] interpolation basis values
+    double* FQ = PI + a.nq * 6;                // [q] f
+    for (int c = blockIdx.x * EW + warp; c < a.ncells; c += gridDim.x * EW) {
+        const CellGeo G = a.cg[c];
+        const double v = G.vol;
+        const int* dofs = a.cdofs + (size_t)c * a.nd;
+        for (int t = lane; t < a.P * a.nq; t += 32) {
+            const int nu = t / a.nq, q = t - nu * a.nq;
+            const double lam[3] = {1.0 - a.xq[2 * q] - a.xq[2 * q + 1], a.xq[2 * q], a.xq[2 * q + 1]};
+            double gg[12];
+            basis_grad(a.order, G.g, lam, gg);
+            double gx = 0.0, gy = 0.0;
+            for (int d = 0; d < a.nd; ++d) {
+                const double u = a.U[(size_t)dofs[d] * a.ld + nu];
+                gx = fma(u, gg[2 * d], gx);
+                gy = fma(u, gg[2 * d + 1], gy);
+            }
+            GU[2 * t] = gx;
+            GU[2 * t + 1] = gy;
+        }
+        if (a.order > 1) {
+            double lap[6];
+            p2_laplacians(G.g, lap);
+            for (int nu = lane; nu < a.P; nu += 32) {
+                double s = 0.0;
+                for (int d = 0; d < a.nd; ++d) s = fma(a.U[(size_t)dofs[d] * a.ld + nu], lap[d], s);
+                LU[nu] = s;
+            }
+        }
+        for (int t = lane; t < l.Mext * a.nq; t += 32) {
+            const int m = 1 + t / a.nq, q = t % a.nq;
+            const double xi = a.xq[2 * q], eta = a.xq[2 * q + 1];
+            const double x = G.x0 + G.j00 * xi + G.j01 * eta, y = G.y0 + G.j10 * xi + G.j11 * eta;
+            // grad a_m = d_m (-b1 w sin(b1 w x) cos(b2 w y), -b2 w cos(b1 w x) sin(b2 w y)), w = freq pi
+            const double w = a.coef.freq_pi, bx = a.coef.b1[m] * w, by = a.coef.b2[m] * w;
+            double sx, cx, sy, cy;
+            sincos(bx * x, &sx, &cx);
+            sincos(by * y, &sy, &cy);
+            GA[2 * t] = -a.coef.d[m] * bx * sx * cy;
+            GA[2 * t + 1] = -a.coef.d[m] * by * cx * sy;
+        }
+        for (int q = lane; q < a.nq; q += 32) {
+            const double lam[3] = {1.0 - a.xq[2 * q] - a.xq[2 * q + 1], a.xq[2 * q], a.xq[2 * q + 1]};
+            double pv[6];
+            sgfem_fe::basis_val(l.iorder, lam, pv);
+            for (int d = 0; d < l.ndi; ++d) PI[q * 6 + d] = pv[d];
+            FQ[q] = a.fqp[(size_t)c * a.nq + q];
+        }
+        __syncwarp();
+        // data term zeta1 (first chunk only): lanes over quadrature points
+        if (j0 == 0) {
+            double zz = 0.0;
+            for (int q = lane; q < a.nq; q += 32) {
+                const double xi = a.xq[2 * q], eta = a.xq[2 * q + 1];
+                const double x = G.x0 + G.j00 * xi + G.j01 * eta, y = G.y0 + G.j10 * xi + G.j11 * eta;
+                double km = 0.0;
+                for (int m = 1; m <= l.maxm; ++m) {
+                    const double am_ = a.coef.d[m] * cos(a.coef.freq_pi * a.coef.b1[m] * x) *
+                                       cos(a.coef.freq_pi * a.coef.b2[m] * y);
+                    km = fma(am_, am_, km);
+                }
+                zz += FQ[q] * FQ[q] * exp(2.0 * km) * a.wq[q] * v;
+            }
+            for (int o = 16; o > 0; o >>= 1) zz += __shfl_down_sync(0xffffffffu, zz, o);
+            if (lane == 0) z1[c] = zz;
+        }
+        const int* idofs = l.idofs + (size_t)c * l.ndi;
+        double zacc = 0.0;
+        for (int j = j0 + lane; j < j1; j += 32) {
+            const double* lj = l.lamv + (size_t)j * l.ndofs_i;
+            double lnode[6];
+            for (int d = 0; d < l.ndi; ++d) lnode[d] = lj[idofs[d]];
+            double acc = 0.0;
+            for (int q = 0; q < a.nq; ++q) {
+                double lam = 0.0;
+                for (int d = 0; d < l.ndi; ++d) lam = fma(PI[q * 6 + d], lnode[d], lam);
+                double r = lam * FQ[q];
+                zacc += lam * lam * FQ[q] * FQ[q] * a.wq[q] * v;
+                if (a.order > 1 && j < a.P) r += LU[j];
+                for (int e = a.lptr[j]; e < a.lptr[j + 1]; ++e) {
+                    const int m = a.lm[e];
+                    if (m == 0) continue;
+                    const double* ga = GA + 2 * ((m - 1) * a.nq + q);
+                    const double* gu = GU + 2 * (a.lnu[e] * a.nq + q);
+                    r = fma(a.lg[e], ga[0] * gu[0] + ga[1] * gu[1], r);
+                }
+                acc = fma(a.wq[q] * r, r, acc);
+            }
+            eta4cell[(size_t)j * a.ncells + c] = acc * (j < a.P ? v * v : v);
+        }
+        for (int o = 16; o > 0; o >>= 1) zacc += __shfl_down_sync(0xffffffffu, zacc, o);
+        if (lane == 0) z2[c] += zacc;
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+extern "C" int sgfem_estimate_logpoisson(sgfem_context* ctx, const double* sol, const sgfem_mesh* mesh,
+                                         const sgfem_quadrature* quad, const double* f_qp, const sgfem_cosine* coef,
+                                         const sgfem_extension* ext, const sgfem_interpolant* lam,
+                                         double* eta4modes, double* eta4cell, double* zeta) {
+    if (!eta4modes || !eta4cell || !zeta || !lam || !lam->values || !lam->cell_dofs)
+        return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "sgfem_estimate_logpoisson: null argument");
+    if (lam->order != 1 && lam->order != 2) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "interpolation degree 1 or 2");
+    Owned own;
+    EstArgs a{};
+    std::vector<int> cfh;
+    SG_TRY(build_est(ctx, sol, mesh, quad, f_qp, coef, ext, coef ? coef->maxm : 0, own, a, cfh));
+    const int64_t nc = a.ncells, nf = a.nfaces, Pext = a.Pext;
+    const int ndi = sgfem_fe::ndofs4cell(lam->order);
+    std::vector<int> idofs((size_t)nc * ndi);
+    for (int64_t c = 0; c < nc; ++c)
+        for (int d = 0; d < ndi; ++d) {
+            const int64_t v = lam->cell_dofs[(size_t)ndi * c + d] - 1;
+            if (v < 0 || v >= lam->ndofs) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "interpolation cell_dofs out of range");
+            idofs[(size_t)c * ndi + d] = (int)v;
+        }
+    for (int64_t t = 0; t < lam->ndofs * Pext; ++t)
+        if (!std::isfinite(lam->values[t])) return sg_fail(ctx, SGFEM_ERR_NONFINITE, "non-finite interpolant value");
+    LogArgs l{};
+    l.iorder = lam->order;
+    l.ndi = ndi;
+    l.Mext = a.coef.M;
+    l.maxm = coef->maxm;
+    l.ndofs_i = lam->ndofs;
+    int* did;
+    double* dlam;
+    SG_TRY(up(ctx, own.p, idofs.data(), idofs.size(), &did));
+    SG_TRY(up(ctx, own.p, lam->values, (size_t)(lam->ndofs * Pext), &dlam));
+    l.idofs = did;
+    l.lamv = dlam;
+    // a.coef.M = M_ext (gradients); the tables d, b1, b2 hold all maxm terms (data term)
+
+    const int chunk = 64;
+    double *d_eta, *d_jumps, *d_vsum, *d_jsum, *d_z1, *d_z2;
+    SG_CUDA(ctx, cudaMalloc((void**)&d_eta, (size_t)nc * Pext * sizeof(double)));
+    own.p.push_back(d_eta);
+    SG_CUDA(ctx, cudaMalloc((void**)&d_jumps, (size_t)nf * chunk * sizeof(double)));
+    own.p.push_back(d_jumps);
+    SG_CUDA(ctx, cudaMalloc((void**)&d_vsum, (size_t)Pext * sizeof(double)));
+    own.p.push_back(d_vsum);
+    SG_CUDA(ctx, cudaMalloc((void**)&d_jsum, (size_t)Pext * sizeof(double)));
+    own.p.push_back(d_jsum);
+    SG_CUDA(ctx, cudaMalloc((void**)&d_z1, (size_t)nc * sizeof(double)));
+    own.p.push_back(d_z1);
+    SG_CUDA(ctx, cudaMalloc((void**)&d_z2, (size_t)nc * sizeof(double)));
+    own.p.push_back(d_z2);
+    SG_CUDA(ctx, cudaMemsetAsync(d_z2, 0, (size_t)nc * sizeof(double), ctx->stream));
+    SG_CUDA(ctx, cudaMemsetAsync(d_jsum, 0, (size_t)Pext * sizeof(double), ctx->stream));
+
+    const size_t smem_v = (size_t)EW * (2 * a.P * a.nq + a.P + 2 * l.Mext * a.nq + a.nq * 6 + a.nq) * sizeof(double);
+    if (smem_v > 220 * 1024)
+        return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "estimator: too many modes or quadrature points for shared memory");
+    if (smem_v > 48 * 1024)
+        SG_CUDA(ctx, cudaFuncSetAttribute(k_elog_volume, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_v));
+    const int gv = (int)std::min<int64_t>((nc + EW - 1) / EW, (int64_t)ctx->num_sms * 16);
+    for (int j0 = 0; j0 < Pext; j0 += chunk) {
+        const int j1 = (int)std::min<int64_t>(Pext, j0 + chunk);
+        k_elog_volume<<<gv, EW * 32, smem_v, ctx->stream>>>(a, l, j0, j1, d_eta, d_z1, d_z2);
+        SG_LAUNCHED(ctx);
+        k_colsum<<<j1 - j0, 256, 0, ctx->stream>>>(d_eta + (size_t)j0 * nc, (size_t)nc, (int)nc, d_vsum + j0);
+        SG_LAUNCHED(ctx);
+    }
+    // jumps of the active modes: unit couplings (0, j, 1), a_0 = 1
+    const int P = a.P;
+    std::vector<int> jp(Pext + 1, 0), jm(P, 0), jn(P);
+    std::vector<double> jg(P, 1.0);
+    for (int j = 0; j < P; ++j) {
+        jp[j + 1] = j + 1;
+        jn[j] = ctx->imode[j];
+    }
+    for (int64_t j = P; j < Pext; ++j) jp[j + 1] = P;
+    int *djp, *djm, *djn;
+    double* djg;
+    SG_TRY(up(ctx, own.p, jp.data(), jp.size(), &djp));
+    SG_TRY(up(ctx, own.p, jm.data(), jm.size(), &djm));
+    SG_TRY(up(ctx, own.p, jn.data(), jn.size(), &djn));
+    SG_TRY(up(ctx, own.p, jg.data(), jg.size(), &djg));
+    EstArgs aj = a;
+    aj.lptr = djp;
+    aj.lm = djm;
+    aj.lnu = djn;
+    aj.lg = djg;
+    aj.coef.M = 0;
+    aj.coef.mean = 1.0;
+    const size_t smem_f = (size_t)EW * (2 * aj.P * aj.nqf + aj.nqf + 2 * aj.nqf * 12) * sizeof(double);
+    if (smem_f > 220 * 1024) return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "estimator: too many modes for the jump term");
+    if (smem_f > 48 * 1024)
+        SG_CUDA(ctx, cudaFuncSetAttribute(k_est_faces, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f));
+    const int gf = (int)std::min<int64_t>((nf + EW - 1) / EW, (int64_t)ctx->num_sms * 16);
+    for (int j0 = 0; j0 < P; j0 += chunk) {
+        const int j1 = std::min(P, j0 + chunk);
+        k_est_faces<<<gf, EW * 32, smem_f, ctx->stream>>>(aj, j0, j1, d_jumps);
+        SG_LAUNCHED(ctx);
+        k_colsum<<<j1 - j0, 256, 0, ctx->stream>>>(d_jumps, (size_t)nf, (int)nf, d_jsum + j0);
+        SG_LAUNCHED(ctx);
+        const int gg = (int)std::min<int64_t>(((int64_t)(j1 - j0) * nc + 255) / 256, (int64_t)ctx->num_sms * 16);
+        k_est_gather<<<gg, 256, 0, ctx->stream>>>(a.cfaces, d_jumps, (int)nc, (int)nf, j0, j1, d_eta);
+        SG_LAUNCHED(ctx);
+    }
+    std::vector<double> vsum(Pext), jsum(Pext), z1(nc), z2(nc);
+    SG_CUDA(ctx, cudaMemcpyAsync(vsum.data(), d_vsum, Pext * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SG_CUDA(ctx, cudaMemcpyAsync(jsum.data(), d_jsum, Pext * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SG_CUDA(ctx, cudaMemcpyAsync(z1.data(), d_z1, nc * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SG_CUDA(ctx, cudaMemcpyAsync(z2.data(), d_z2, nc * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SG_CUDA(ctx, cudaMemcpyAsync(eta4cell, d_eta, (size_t)nc * Pext * sizeof(double), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int64_t j = 0; j < Pext; ++j) {
+        eta4modes[j] = std::sqrt(vsum[j]);
+        if (j < P) eta4modes[j] += std::sqrt(eta4modes[j] * eta4modes[j] + jsum[j]);
+    }
+    double s1 = 0.0, s2 = 0.0;
+    for (int64_t c = 0; c < nc; ++c) {
+        s1 += z1[c];
+        s2 += z2[c];
+    }
+    zeta[0] = s1;
+    zeta[1] = s2;
     return SGFEM_OK;
 }

@@ -18,7 +18,7 @@ import scipy.sparse as sp
 
 from . import _lib
 from .fem import line_rule, triangle_rule
-from .modelproblems import PoissonProblemPrimal
+from .modelproblems import LogTransformedPoissonProblemPrimal, PoissonProblemPrimal
 from .mopcontrol import add_boundary_modes, get_neighbours
 from .tensorizedbasis import coupling_matrix
 
@@ -39,6 +39,11 @@ class _Quad(ctypes.Structure):
 class _Cosine(ctypes.Structure):
     _fields_ = [("maxm", ctypes.c_int), ("mean", ctypes.c_double), ("freq", ctypes.c_double),
                 ("decay_factors", ctypes.c_void_p), ("b1", ctypes.c_void_p), ("b2", ctypes.c_void_p)]
+
+
+class _Interp(ctypes.Structure):
+    _fields_ = [("order", ctypes.c_int), ("ndofs", ctypes.c_int64), ("cell_dofs", ctypes.c_void_p),
+                ("values", ctypes.c_void_p)]
 
 
 class _Ext(ctypes.Structure):
@@ -100,6 +105,8 @@ def estimate(problem, sol, C, rhs=None, bonus_quadorder=1, tail_extension=(10, 2
     ``op``: an SGOperator of the same space and basis to reuse its context.
     ``face_points``: Gauss points per face for the jump term (default quadorder + 1).
     """
+    if problem is LogTransformedPoissonProblemPrimal:
+        return _estimate_log(sol, C, rhs, bonus_quadorder, tail_extension, face_points, device, op)
     if problem is not PoissonProblemPrimal:
         raise NotImplementedError(f"no estimator for {problem}")
     if rhs is None:
@@ -154,3 +161,79 @@ def estimate(problem, sol, C, rhs=None, bonus_quadorder=1, tail_extension=(10, 2
         if op is None:
             ctx.close()
     return eta4modes, eta4cell.T, ext
+
+
+def _mesh_struct(FES, order=None):
+    mesh = FES.mesh
+    keep = dict(
+        coords=np.ascontiguousarray(mesh.coords, dtype=np.float64),
+        cell_nodes=np.ascontiguousarray(mesh.cells + 1, dtype=np.int64),
+        cell_dofs=np.ascontiguousarray(FES.celldofs + 1, dtype=np.int64),
+        face_nodes=np.ascontiguousarray(mesh.face_nodes + 1, dtype=np.int64),
+        face_cells=np.ascontiguousarray(np.where(mesh.face_cells >= 0, mesh.face_cells + 1, 0), dtype=np.int64),
+        cell_faces=np.ascontiguousarray(mesh.cellfaces + 1, dtype=np.int64),
+        cvol=np.ascontiguousarray(mesh.cell_volumes, dtype=np.float64),
+        fvol=np.ascontiguousarray(mesh.face_volumes, dtype=np.float64))
+    m = _Mesh(FES.order if order is None else order, mesh.nnodes, mesh.ncells, mesh.nfaces, _ptr(keep["coords"]),
+              _ptr(keep["cell_nodes"]), _ptr(keep["cell_dofs"]), _ptr(keep["face_nodes"]), _ptr(keep["face_cells"]),
+              _ptr(keep["cell_faces"]), _ptr(keep["cvol"]), _ptr(keep["fvol"]))
+    return m, keep
+
+
+def _estimate_log(sol, C, rhs, bonus_quadorder, tail_extension, face_points, device, op):
+    """estimate(LogTransformedPoissonProblemPrimal, sol, C; rhs, bonus_quadorder,
+    tail_extension), src/estimate.jl:70-257: (eta4modes, eta4cell, ext, zeta).
+    lambda_j is interpolated nodally into the H1Pk space of degree
+    quadorder = 2 (order - 1) + bonus_quadorder (1 or 2)."""
+    from .fem import H1Pk, pce_lambda
+    if rhs is None:
+        raise ValueError("need right-hand side")
+    if isinstance(tail_extension, (int, np.integer)):
+        raise TypeError("tail_extension needs two entries (add_boundary_modes reads tail_extension[2])")
+    FES = sol.FES_space[0]
+    mesh = FES.mesh
+    TB = sol.TB
+    ext, (ptr, ms, nus, gs) = extension_couplings(TB.multi_indices, TB.basis, tail_extension)
+    P_ext, M_ext = len(ext), len(ext[0])
+    if C.maxm() < M_ext:
+        raise ValueError(f"coefficient maxm = {C.maxm()} < extended length {M_ext}")
+    order = FES.order
+    quadorder = 2 * (order - 1) + bonus_quadorder
+    if quadorder not in (1, 2):
+        raise NotImplementedError("interpolation degree 1 or 2 (2 (order - 1) + bonus_quadorder)")
+    pts, wts = triangle_rule(quadorder)
+    tq, tw = line_rule(face_points if face_points is not None else order)
+    X = FES.physical_points(pts)
+    fq = np.ascontiguousarray(np.broadcast_to(np.asarray(rhs(X[..., 0], X[..., 1]), dtype=np.float64), X.shape[:2]))
+    Vi = H1Pk(mesh, quadorder)
+    lamv = np.ascontiguousarray(pce_lambda(C, ext, Vi.dof_coords[:, 0], Vi.dof_coords[:, 1], factor=-1.0))
+    idofs = np.ascontiguousarray(Vi.celldofs + 1, dtype=np.int64)
+    interp = _Interp(quadorder, Vi.ndofs, _ptr(idofs), _ptr(lamv))
+    m, keep = _mesh_struct(FES)
+    xref = np.ascontiguousarray(pts, dtype=np.float64)
+    w = np.ascontiguousarray(wts, dtype=np.float64)
+    tq = np.ascontiguousarray(tq, dtype=np.float64)
+    tw = np.ascontiguousarray(tw, dtype=np.float64)
+    q = _Quad(len(w), _ptr(xref), _ptr(w), len(tw), _ptr(tq), _ptr(tw))
+    dfac = np.ascontiguousarray(C.decay_factors, dtype=np.float64)
+    b1 = np.ascontiguousarray(C.b1, dtype=np.int64)
+    b2 = np.ascontiguousarray(C.b2, dtype=np.int64)
+    c = _Cosine(C.maxm(), C.mean_value, C.freq, _ptr(dfac), _ptr(b1), _ptr(b2))
+    e = _Ext(P_ext, M_ext, _ptr(ptr), _ptr(ms), _ptr(nus), _ptr(gs))
+    eta4modes = np.zeros(P_ext)
+    eta4cell = np.zeros((P_ext, mesh.ncells))
+    zeta = np.zeros(2)
+    ctx = op.ctx if op is not None else _light_context(FES, TB, device)
+    try:
+        solv = np.ascontiguousarray(sol.entries, dtype=np.float64)
+        lib = _lib.load()
+        dp = lambda a_: a_.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        rc = lib.sgfem_estimate_logpoisson(ctx.h, dp(solv), ctypes.byref(m), ctypes.byref(q), dp(fq),
+                                           ctypes.byref(c), ctypes.byref(e), ctypes.byref(interp), dp(eta4modes),
+                                           dp(eta4cell), dp(zeta))
+        ctx._check(rc)
+    finally:
+        if op is None:
+            ctx.close()
+    del keep
+    return eta4modes, eta4cell.T, ext, float(zeta[0] - zeta[1])

@@ -242,6 +242,32 @@ SGFEM_API int sgfem_estimate_primal(sgfem_context* ctx, const double* sol, const
                                     double* eta4cell);
 
 /*
+ * estimate(::Type{LogTransformedPoissonProblemPrimal}, sol, C; rhs,
+ * bonus_quadorder, tail_extension), src/estimate.jl:70-257, for a context whose
+ * operator is the log-transformed one (K_0 = A, K_m = N_m).  mesh, quad, f_qp,
+ * coef and ext as for sgfem_estimate_primal (ext's (0, j, 1) entries are not
+ * used; coef must hold all maxm terms: the data term sums a_m^2 over them).
+ * lam: the interpolant of the Hermite chaos coefficients lambda_j of exp(-a)
+ * (expa_PCE_mop with factor -1, coefficients.jl:219-260) on an H1Pk space of
+ * degree 1 or 2 over the same cells, values P_ext x ndofs (mode j at
+ * [j * ndofs]).  Outputs: eta4modes[P_ext], eta4cell (ncells x P_ext,
+ * column-major) and zeta[2] = (zeta1, zeta2); the reference returns
+ * zeta1 - zeta2.  eta4modes[j] = sqrt(V_j) + sqrt(V_j + J_j) for active j (the
+ * reference's update at :244) and sqrt(V_j) otherwise.
+ */
+typedef struct {
+    int order;                     /* 1 or 2 */
+    int64_t ndofs;
+    const int64_t* cell_dofs;      /* nd x ncells, 1-based */
+    const double* values;          /* ndofs x P_ext column-major */
+} sgfem_interpolant;
+
+SGFEM_API int sgfem_estimate_logpoisson(sgfem_context* ctx, const double* sol, const sgfem_mesh* mesh,
+                                        const sgfem_quadrature* quad, const double* f_qp, const sgfem_cosine* coef,
+                                        const sgfem_extension* ext, const sgfem_interpolant* lam,
+                                        double* eta4modes, double* eta4cell, double* zeta);
+
+/*
  * Evaluation of an SG solution at parameter samples and the sampling error.
  *
  * sgfem_evaluate_samples: batched set_sample!(SGFEV, y[1:m])

@@ -170,3 +170,101 @@ def estimate_primal(space, U, multi_indices, obt, coef, f, bonus_quadorder=1,
         eta4cell[:, j] += jumps[mesh.cellfaces].sum(axis=1)
         eta4modes[j] = np.sqrt(eta4modes[j] ** 2 + jumps.sum())
     return eta4modes, eta4cell, ext
+
+
+def estimate_logpoisson(space, U, multi_indices, obt, coef, f, bonus_quadorder=1, tail_extension=(10, 2),
+                        face_points=None):
+    """estimate(::Type{LogTransformedPoissonProblemPrimal}, sol, C; rhs, bonus_quadorder,
+    tail_extension), src/estimate.jl:70-257, by element loops.
+
+    * lambda_j (the Hermite chaos coefficients of exp(-a), expa_PCE_mop with
+      factor -1, coefficients.jl:219-260) interpolated into the Lagrange space
+      of degree quadorder = 2 (order - 1) + bonus_quadorder (:102-114), here by
+      nodal values (the reference's interpolate! is nodal for P1; its
+      higher-order dofs are UNPINNED);
+    * volume term (:130-214): per cell and extended mode j and quadrature point,
+      f lambda_j (+ Laplace(u_j) for P2 and active j) + sum_m grad a_m . grad of the
+      G-coupled active neighbours, squared and weighted, times |T|^2 (active j)
+      or |T| (inactive j);
+    * data term zeta = zeta1 - zeta2 (:139-156, :248-254);
+    * jumps (:231-246): for active j, int_F |[[grad u_j]]|^2 times |F| on interior
+      faces, added to the adjacent cells; eta4modes[j] += sqrt(eta4modes[j]^2 + sum)
+      (the reference's own update).
+    Returns (eta4modes, eta4cell, ext, zeta).
+    """
+    from .coefficient import pce_lambda
+    from .fem import LagrangeSpace
+    if isinstance(tail_extension, (int, np.integer)):
+        raise TypeError("tail_extension must hold two entries (add_boundary_modes reads tail_extension[2])")
+    mesh = space.mesh
+    nmodes = len(multi_indices)
+    ext = add_boundary_modes(copy.deepcopy([list(m) for m in multi_indices]), tail_extension=tail_extension)
+    M_ext = len(ext[0])
+    next_ = len(ext)
+    G = get_tensor_multiplication_with_ym(obt, ext)
+    plus, minus = get_neighbours(ext)
+    order = space.order
+    quadorder = 2 * (order - 1) + bonus_quadorder
+    if quadorder > 2:
+        raise NotImplementedError("interpolation degree above 2")
+    pts, wts = triangle_rule(quadorder)
+    n = space.ndofs
+    nc = mesh.ncells
+    vol = mesh.cell_volumes
+    Vi = LagrangeSpace(mesh, max(quadorder, 1))
+    lam_nodes = np.zeros((next_, Vi.ndofs))
+    for j in range(next_):
+        for d in range(Vi.ndofs):
+            x, y = Vi.dof_coords[d]
+            lam_nodes[j, d] = pce_lambda(coef, ext[j], x, y, factor=-1.0)
+    Mcoeff = coef.maxm()
+    eta4cell = np.zeros((nc, next_))
+    zeta1 = 0.0
+    zeta2 = 0.0
+    for c in range(nc):
+        p, J, gl = space.cell_geometry(c)
+        _, _, gli = Vi.cell_geometry(c)
+        dofs = space.celldofs[c]
+        idofs = Vi.celldofs[c]
+        lamq = np.zeros((next_, len(wts)))
+        X = []
+        for q, (xi, eta) in enumerate(pts):
+            x = p[0] + J @ np.array([xi, eta])
+            X.append(x)
+            lam = np.array([1 - xi - eta, xi, eta])
+            iv, _, _ = Vi.local_basis(lam, gli)
+            lamq[:, q] = lam_nodes[:, idofs] @ iv
+            kmL2 = sum(float(coef.get_am(x[0], x[1], m)) ** 2 for m in range(1, Mcoeff + 1))
+            fq = f(x[0], x[1])
+            zeta1 += fq ** 2 * np.exp(2 * kmL2) * wts[q] * vol[c]
+            zeta2 += np.sum(lamq[:, q] ** 2) * fq ** 2 * wts[q] * vol[c]
+        for j in range(next_):
+            acc = 0.0
+            for q, (xi, eta) in enumerate(pts):
+                x = X[q]
+                lam = np.array([1 - xi - eta, xi, eta])
+                _, g, lap = space.local_basis(lam, gl)
+                ft = lamq[j, q] * f(x[0], x[1])
+                if order > 1 and j < nmodes:
+                    ft += U[j * n + dofs] @ lap
+                sig = 0.0
+                for m in range(1, M_ext + 1):
+                    ga = np.array([float(t) for t in coef.get_gradam(x[0], x[1], m)])
+                    cv = np.zeros(len(dofs))
+                    cp, cm = plus[m - 1][j], minus[m - 1][j]
+                    if 0 < cp <= nmodes:
+                        cv += U[(cp - 1) * n + dofs] * G[(m - 1) * next_ + j, cp - 1]
+                    if 0 < cm <= nmodes:
+                        cv += U[(cm - 1) * n + dofs] * G[(m - 1) * next_ + j, cm - 1]
+                    sig += cv @ (g @ ga)
+                acc += (ft + sig) ** 2 * wts[q]
+            eta4cell[c, j] = acc * (vol[c] ** 2 if j < nmodes else vol[c])
+    eta4modes = np.sqrt(eta4cell.sum(axis=0))
+    tq, tw = line_rule(face_points if face_points is not None else order)
+    JG, _ = _face_jump_grads(space, U, list(range(nmodes)), tq)
+    fvol = mesh.face_volumes
+    for j in range(nmodes):
+        jumps = fvol * np.sum(tw[None, :] * np.sum(JG[j] ** 2, axis=2), axis=1) * fvol
+        eta4cell[:, j] += jumps[mesh.cellfaces].sum(axis=1)
+        eta4modes[j] += np.sqrt(eta4modes[j] ** 2 + jumps.sum())
+    return eta4modes, eta4cell, ext, zeta1 - zeta2
