@@ -102,14 +102,14 @@ __global__ void __launch_bounds__(VT) k_update(T* __restrict__ x, const T* __res
                                                double* __restrict__ partials) {
     if (s->done) return;
     const T alpha = (T)s->alpha;
-    double acc = 0.0;
+    T acc_t = T(0);  // per-thread partial in the working precision (narrow FP64 pipe)
     for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT) {
         x[i] = fma(alpha, p[i], x[i]);
         const T rn = fma(-alpha, q[i], r[i]);
         r[i] = rn;
-        acc += (double)rn * (double)rn;
+        acc_t = fma(rn, rn, acc_t);
     }
-    block_partial(acc, partials);
+    block_partial((double)acc_t, partials);
 }
 
 // r = b - ax ; partial ||r||^2
@@ -128,23 +128,23 @@ __global__ void __launch_bounds__(VT) k_residual(const double* __restrict__ b, c
 template <typename T>
 __global__ void __launch_bounds__(VT) k_dot(const T* __restrict__ a, const T* __restrict__ b, size_t total,
                                             double* __restrict__ partials) {
-    double acc = 0.0;
+    T acc_t = T(0);
     for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT)
-        acc += (double)a[i] * (double)b[i];
-    block_partial(acc, partials);
+        acc_t = fma(a[i], b[i], acc_t);
+    block_partial((double)acc_t, partials);
 }
 
 // r32 = (float) r64 ; d32 = 0 ; partial ||r32||^2
 __global__ void __launch_bounds__(VT) k_demote(const double* __restrict__ r64, float* __restrict__ r32,
                                                float* __restrict__ d32, size_t total, double* __restrict__ partials) {
-    double acc = 0.0;
+    float acc_t = 0.0f;
     for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT) {
         const float v = (float)r64[i];
         r32[i] = v;
         d32[i] = 0.0f;
-        acc += (double)v * (double)v;
+        acc_t = fmaf(v, v, acc_t);
     }
-    block_partial(acc, partials);
+    block_partial((double)acc_t, partials);
 }
 
 // x64 += (double) d32
@@ -329,7 +329,7 @@ extern "C" void sgfem_default_options(sgfem_solve_options* o) {
     o->preconditioner = SGFEM_PREC_LATTICE;
     o->rtol = 1e-8;
     o->maxit = 2000;
-    o->inner_rtol = 1e-5;
+    o->inner_rtol = 1e-4;  // measured best on the P2 256x256 workload (three refinement steps for 1e-8 either way)
     o->reference_rhs = 1;
     o->check_every = 8;
 }

@@ -271,7 +271,9 @@ k_lat_pass_y(T* __restrict__ buf, const T* __restrict__ tab, const T* __restrict
     dst_line<T, LGL>(tile, stab);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int N = g.Nl - 1;
-    double acc = 0.0;
+    // r'z partial per thread in the working precision (the FP64 pipe is narrow on
+    // this GPU), converted to FP64 once per thread below
+    T acc_t = T(0);
     for (int p0 = 1 + warp; p0 < g.Nl; p0 += LAT_WARPS * LAT_UNROLL) {
         T sc[LAT_UNROLL];
 #pragma unroll
@@ -284,11 +286,13 @@ k_lat_pass_y(T* __restrict__ buf, const T* __restrict__ tab, const T* __restrict
             const int p = p0 + u * LAT_WARPS;
             if (p < g.Nl) {
                 const T v = tile[p * 32 + lane];
-                acc += (double)v * (double)v * (double)sc[u];
-                tile[p * 32 + lane] = v * sc[u];
+                const T vs = v * sc[u];
+                acc_t = fma(v, vs, acc_t);
+                tile[p * 32 + lane] = vs;
             }
         }
     }
+    double acc = (double)acc_t;
     __syncthreads();
     dst_line<T, LGL>(tile, stab);
     const int m = chunk * 32 + lane;
@@ -335,7 +339,7 @@ __global__ void k_jacobi(const T* __restrict__ R, T* __restrict__ out, const T* 
     __shared__ double red[8];
     T beta = T(0);
     if (mode == 1 && scal && !scal->first) beta = (T)scal->beta;
-    double acc = 0.0;
+    T acc_t = T(0);  // per-thread partial in the working precision
     const size_t total = (size_t)n * ld;
     for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
         const int row = (int)(idx / ld);
@@ -344,7 +348,7 @@ __global__ void k_jacobi(const T* __restrict__ R, T* __restrict__ out, const T* 
         const T r = R[idx];
         const T z = d * r;
         if (mode == 2) {
-            acc += (double)r * (double)z;
+            acc_t = fma(r, z, acc_t);
         } else if (mode == 1) {
             if (d != T(0)) out[idx] = z + beta * out[idx];
         } else {
@@ -352,6 +356,7 @@ __global__ void k_jacobi(const T* __restrict__ R, T* __restrict__ out, const T* 
         }
     }
     if (mode == 2) {
+        double acc = (double)acc_t;
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
         __syncthreads();
