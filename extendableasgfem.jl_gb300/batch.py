@@ -2,9 +2,10 @@
 
 The reference solves one problem per solve! call (src/modelproblems/
 poisson_primal.jl:38-81).  ``SGBatch`` hands many PoissonProblemPrimal systems
-to the library at once (sgfem_batch_*): one Jacobi-preconditioned CG runs all
-of them in lock step, each phase one launch over every problem, iterations
-replayed from a captured CUDA graph.  ``config4_problems`` draws the problem
+to the library at once (sgfem_batch_*): one preconditioned CG runs all of them
+in lock step, each phase one launch over every problem, iterations replayed
+from a captured CUDA graph.  P1 problems on the unit-square lattice get the
+mean-based preconditioner (sine transforms), the others Jacobi.  ``config4_problems`` draws the problem
 shapes from a SplitMix64 stream (seed = problem index):
 n = 16 + r % 113 (n x n P1 mesh), M = 4 + r % 13, total degree 1 + r % 3.
 """
@@ -62,6 +63,21 @@ def _take(Kc, K0):
     return out
 
 
+def _lattice_size(FES):
+    """nl if the dofs are the (nl+1)^2 points of a uniform lattice of the unit square in
+    x-fastest order (P1 on unit_square_mesh), else 0."""
+    if getattr(FES, "order", 0) != 1:
+        return 0
+    n = FES.ndofs
+    nl = int(round(np.sqrt(n))) - 1
+    if nl < 2 or nl > 128 or (nl + 1) ** 2 != n:
+        return 0
+    i = np.arange(n) % (nl + 1)
+    j = np.arange(n) // (nl + 1)
+    expect = np.stack([i / nl, j / nl], axis=1)
+    return nl if np.allclose(FES.dof_coords, expect, atol=1e-12) else 0
+
+
 class SGBatch:
     def __init__(self, device=0):
         self.lib = _lib.load()
@@ -96,7 +112,11 @@ class SGBatch:
         self._check(self.lib.sgfem_batch_add(self.h, n, M, P, i64(colptr), i64(rowval), _lib._dp(vals), i64(gcp),
                                              i64(grv), _lib._dp(gv), len(bd), i64(bd), _lib._dp(b0)))
         self.shapes.append((n, P))
-        return len(self.shapes) - 1
+        i = len(self.shapes) - 1
+        nl = _lattice_size(FES)
+        if nl:
+            self._check(self.lib.sgfem_batch_set_lattice(self.h, i, nl))
+        return i
 
     def finalize(self):
         self._check(self.lib.sgfem_batch_finalize(self.h))

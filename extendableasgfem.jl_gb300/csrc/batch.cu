@@ -58,6 +58,8 @@ struct sgfem_batch {
         std::vector<int> qtab, combptr, combq;
         std::vector<double> combg;
         double work;
+        int nl = 0;          // > 0: dofs are the (nl+1)^2 lattice points, x fastest (sine-transform preconditioner)
+        double a0 = 0.0;     // K_0 = a0 * 5-point Laplacian on interior rows
     };
     std::vector<HostProb> hp;
     // device
@@ -66,6 +68,12 @@ struct sgfem_batch {
     int* d_bprob = nullptr;
     KrylovScalars* d_scal = nullptr;
     double *d_x = nullptr, *d_b = nullptr, *d_r = nullptr, *d_p = nullptr, *d_q = nullptr, *d_part = nullptr;
+    double* d_z = nullptr;        // preconditioned residual
+    float* d_t = nullptr;         // sine-transform intermediate
+    int4* d_dstmap = nullptr;     // (problem, line, mode chunk) per block of the transform passes
+    int ndst = 0;
+    int2* d_lat = nullptr;        // per problem: (nl, a0 as float bits); nl = 0: Jacobi
+    size_t dst_smem = 0;
     long long total = 0;          // sum of n * ld
     int blocks = 0, wpb = 4, qt = 4, ldmax = 0, m1max = 0, qnmax = 0;
     std::string tuning;
@@ -312,6 +320,111 @@ __global__ void k_bout(const double* __restrict__ x, long long voff, int n, int 
     }
 }
 
+// z = D^-1 r on the problems without a lattice (Jacobi), Dirichlet rows zero
+__global__ void __launch_bounds__(BT) k_bjz(const BProb* __restrict__ probs, const int* __restrict__ bprob,
+                                            const int2* __restrict__ lat, const double* __restrict__ r,
+                                            double* __restrict__ z, const KrylovScalars* __restrict__ scal) {
+    BRANGE;
+    if (lat[pi].x > 0 || scal[pi].done) return;
+    for (long long t = t0; t < len; t += tstep) z[d.voff + t] = d.dinv[t / d.ld] * r[d.voff + t];
+}
+
+// partials of r'z per block of each problem
+__global__ void __launch_bounds__(BT) k_brz(const BProb* __restrict__ probs, const int* __restrict__ bprob,
+                                            const double* __restrict__ r, const double* __restrict__ z,
+                                            const KrylovScalars* __restrict__ scal, double* __restrict__ partials) {
+    BRANGE;
+    double acc = 0.0;
+    if (!scal[pi].done)
+        for (long long t = t0; t < len; t += tstep) acc = fma(r[d.voff + t], z[d.voff + t], acc);
+    block_sum_store(acc, partials + blockIdx.x);
+}
+
+// p = z + beta p
+__global__ void __launch_bounds__(BT) k_bpz(const BProb* __restrict__ probs, const int* __restrict__ bprob,
+                                            const double* __restrict__ z, double* __restrict__ p,
+                                            const KrylovScalars* __restrict__ scal) {
+    BRANGE;
+    if (scal[pi].done) return;
+    const double beta = scal[pi].beta;
+    for (long long t = t0; t < len; t += tstep) p[d.voff + t] = fma(beta, p[d.voff + t], z[d.voff + t]);
+}
+
+// Mean-based preconditioner of a lattice problem, z = (a0 L)^-1 r on interior rows
+// (L the 5-point Laplacian of the (nl+1)^2 lattice), by the sine transform
+// S_ik = sin(pi i k / nl), i, k = 1..nl-1 (S^2 = (nl/2) I), applied as a dense
+// matrix product along every lattice line: pass 0 (x): t = S r per line j;
+// pass 1 (y): t = S (D .* (S t)) per column, D = (2/nl)^2 / (a0 (lam_kx + lam_ky)),
+// lam_k = 4 sin^2(pi k / (2 nl)); pass 2 (x): z = S t per line.  One block per
+// (problem, line, 32-mode chunk); S and the line tile in shared memory, lanes
+// over modes, FP32 arithmetic.
+__global__ void __launch_bounds__(BT) k_bdst(const BProb* __restrict__ probs, const int4* __restrict__ map,
+                                             const int2* __restrict__ lat, int pass, const double* __restrict__ r,
+                                             float* __restrict__ t, double* __restrict__ z,
+                                             const KrylovScalars* __restrict__ scal) {
+    const int4 e = map[blockIdx.x];
+    const int pi = e.x, line = e.y, chunk = e.z;
+    if (scal[pi].done) return;
+    const BProb& d = probs[pi];
+    const int nl = lat[pi].x, N = nl - 1;
+    const float a0 = __int_as_float(lat[pi].y);
+    extern __shared__ float dsm[];
+    float* S = dsm;                   // N x N
+    float* tile = S + N * N;          // N x 32 (input line)
+    float* out = tile + N * 32;       // N x 32
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
+        const int i = q / N + 1, k = q % N + 1;
+        S[q] = sinpif((float)((i * k) % (2 * nl)) / (float)nl);
+    }
+    const int c = chunk * 32 + lane;
+    const bool live = c < d.ld;
+    const int stride = nl + 1;
+    // lattice point k (1..N) of this line -> row
+    auto row_of = [&](int k) { return (pass == 1) ? k * stride + line : line * stride + k; };
+    for (int k = 1 + warp; k <= N; k += nw) {
+        const long long idx = d.voff + (long long)row_of(k) * d.ld + c;
+        float v = 0.f;
+        if (live) v = (pass == 0) ? (float)r[idx] : t[idx];
+        tile[(k - 1) * 32 + lane] = v;
+    }
+    __syncthreads();
+    for (int i = warp; i < N; i += nw) {
+        float s = 0.f;
+        const float* Si = S + i * N;
+        for (int k = 0; k < N; ++k) s = fmaf(Si[k], tile[k * 32 + lane], s);
+        out[i * 32 + lane] = s;
+    }
+    __syncthreads();
+    if (pass == 1) {
+        // scale by D(kx = line, ky = i + 1) and transform again
+        const float w = 3.14159265358979f / (2.0f * (float)nl);
+        const float sx = sinf(w * (float)line);
+        const float lx = 4.f * sx * sx;
+        const float nrm = 4.f / ((float)nl * (float)nl);
+        for (int i = warp; i < N; i += nw) {
+            const float sy = sinf(w * (float)(i + 1));
+            tile[i * 32 + lane] = out[i * 32 + lane] * (nrm / (a0 * (lx + 4.f * sy * sy)));
+        }
+        __syncthreads();
+        for (int i = warp; i < N; i += nw) {
+            float s = 0.f;
+            const float* Si = S + i * N;
+            for (int k = 0; k < N; ++k) s = fmaf(Si[k], tile[k * 32 + lane], s);
+            out[i * 32 + lane] = s;
+        }
+        __syncthreads();
+    }
+    if (!live) return;
+    for (int k = 1 + warp; k <= N; k += nw) {
+        const long long idx = d.voff + (long long)row_of(k) * d.ld + c;
+        if (pass == 2)
+            z[idx] = (double)out[(k - 1) * 32 + lane];
+        else
+            t[idx] = out[(k - 1) * 32 + lane];
+    }
+}
+
 template <typename Tv>
 int bupload(sgfem_batch* b, const std::vector<Tv>& v, Tv** dst) {
     void* p = nullptr;
@@ -492,6 +605,30 @@ extern "C" int sgfem_batch_add(sgfem_batch* b, int64_t n, int64_t M, int64_t P, 
 
 extern "C" int sgfem_batch_count(const sgfem_batch* b) { return b ? (int)b->hp.size() : 0; }
 
+extern "C" int sgfem_batch_set_lattice(sgfem_batch* b, int i, int64_t nl) {
+    if (!b) return SGFEM_ERR_ARGUMENT;
+    if (b->finalized) return bfail(b, SGFEM_ERR_STATE, "batch already finalized");
+    if (i < 0 || i >= (int)b->hp.size()) return bfail(b, SGFEM_ERR_ARGUMENT, "no such problem");
+    auto& h = b->hp[i];
+    if (nl < 2 || nl > 128 || (int64_t)h.n != (nl + 1) * (nl + 1))
+        return bfail(b, SGFEM_ERR_ARGUMENT, "lattice: n must be (nl + 1)^2 with 2 <= nl <= 128");
+    // interior rows are the lattice interior; a0 = mean interior diagonal / 4
+    double dsum = 0.0;
+    long long cnt = 0;
+    for (int64_t r = 0; r < h.n; ++r) {
+        const int64_t ix = r % (nl + 1), iy = r / (nl + 1);
+        const bool interior = ix > 0 && ix < nl && iy > 0 && iy < nl;
+        if (interior != !h.bmask[r]) return bfail(b, SGFEM_ERR_ARGUMENT, "lattice: Dirichlet rows are not the lattice boundary");
+        if (interior) {
+            dsum += 1.0 / h.dinv[r];
+            ++cnt;
+        }
+    }
+    h.a0 = cnt ? dsum / (4.0 * cnt) : 1.0;
+    h.nl = (int)nl;
+    return SGFEM_OK;
+}
+
 extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
     if (!b) return SGFEM_ERR_ARGUMENT;
     if (b->finalized) return bfail(b, SGFEM_ERR_STATE, "batch already finalized");
@@ -531,6 +668,35 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
     SG_TRY(balloc(b, vb, (void**)&b->d_p));
     SG_TRY(balloc(b, vb, (void**)&b->d_q));
     SG_TRY(balloc(b, (size_t)B * sizeof(KrylovScalars), (void**)&b->d_scal));
+    SG_TRY(balloc(b, vb, (void**)&b->d_z));
+    BCUDA(b, cudaMemset(b->d_z, 0, vb));
+    {
+        // sine-transform preconditioner: per-problem (nl, a0) and one block per (problem, line, chunk)
+        std::vector<int2> lat(B, make_int2(0, 0));
+        std::vector<int4> map;
+        size_t smax = 0;
+        for (int i = 0; i < B; ++i) {
+            const auto& h = b->hp[i];
+            if (h.nl <= 0) continue;
+            float a0f = (float)h.a0;
+            int bits;
+            std::memcpy(&bits, &a0f, sizeof(int));
+            lat[i] = make_int2(h.nl, bits);
+            const int N = h.nl - 1, chunks = (h.ld + 31) / 32;
+            for (int line = 1; line <= N; ++line)
+                for (int c = 0; c < chunks; ++c) map.push_back(make_int4(i, line, c, 0));
+            smax = std::max(smax, ((size_t)N * N + 2 * (size_t)N * 32) * sizeof(float));
+        }
+        SG_TRY(bupload(b, lat, &b->d_lat));
+        b->ndst = (int)map.size();
+        if (b->ndst > 0) {
+            SG_TRY(bupload(b, map, &b->d_dstmap));
+            SG_TRY(balloc(b, (size_t)voff * sizeof(float), (void**)&b->d_t));
+            b->dst_smem = smax;
+            if (smax > 48 * 1024)
+                BCUDA(b, cudaFuncSetAttribute(k_bdst, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
+        }
+    }
     BCUDA(b, cudaMemset(b->d_x, 0, vb));
     BCUDA(b, cudaMemset(b->d_p, 0, vb));
     b->h_scal.assign(B, KrylovScalars{});
@@ -603,6 +769,26 @@ extern "C" const char* sgfem_batch_tuning(const sgfem_batch* b) { return b ? b->
 
 namespace {
 
+// z = B r (sine transform on lattice problems, Jacobi on the others), rho = r'z, beta, p = z + beta p
+int batch_precondition(sgfem_batch* b, int maxit) {
+    const int B = (int)b->hp.size();
+    k_bjz<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_lat, b->d_r, b->d_z, b->d_scal);
+    BLAUNCHED(b);
+    if (b->ndst > 0)
+        for (int pass = 0; pass < 3; ++pass) {
+            k_bdst<<<b->ndst, BT, b->dst_smem, b->stream>>>(b->d_probs, b->d_dstmap, b->d_lat, pass, b->d_r, b->d_t,
+                                                            b->d_z, b->d_scal);
+            BLAUNCHED(b);
+        }
+    k_brz<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_r, b->d_z, b->d_scal, b->d_part);
+    BLAUNCHED(b);
+    k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_BETA, 0.0, maxit);
+    BLAUNCHED(b);
+    k_bpz<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_z, b->d_p, b->d_scal);
+    BLAUNCHED(b);
+    return SGFEM_OK;
+}
+
 int batch_iteration(sgfem_batch* b, int maxit) {
     const int B = (int)b->hp.size();
     SG_TRY(launch_apply(b, b->wpb, b->qt, b->d_p, b->d_q, b->d_part, b->d_scal));
@@ -612,13 +798,7 @@ int batch_iteration(sgfem_batch* b, int maxit) {
     BLAUNCHED(b);
     k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_RR, 0.0, maxit);
     BLAUNCHED(b);
-    k_bjacobi<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_r, b->d_p, b->d_scal, b->d_part, 0);
-    BLAUNCHED(b);
-    k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_BETA, 0.0, maxit);
-    BLAUNCHED(b);
-    k_bjacobi<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_r, b->d_p, b->d_scal, nullptr, 1);
-    BLAUNCHED(b);
-    return SGFEM_OK;
+    return batch_precondition(b, maxit);
 }
 
 }  // namespace
@@ -670,13 +850,9 @@ extern "C" int sgfem_batch_solve(sgfem_batch* b, double rtol, int maxit, int che
     BLAUNCHED(b);
     k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_TOL, rtol * rtol, maxit);
     BLAUNCHED(b);
-    // first direction: rho = r'Dr, p = D r
-    k_bjacobi<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_r, b->d_p, b->d_scal, b->d_part, 0);
-    BLAUNCHED(b);
-    k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_BETA, 0.0, maxit);
-    BLAUNCHED(b);
-    k_bjacobi<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_r, b->d_p, b->d_scal, nullptr, 1);
-    BLAUNCHED(b);
+    // first direction: z = B r, rho = r'z, p = z
+    BCUDA(b, cudaMemsetAsync(b->d_z, 0, (size_t)b->total * sizeof(double), b->stream));
+    SG_TRY(batch_precondition(b, maxit));
     // graph of check_every iterations
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;

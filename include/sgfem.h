@@ -357,7 +357,8 @@ SGFEM_API int sgfem_adjoint_gradient(sgfem_context* ctx, const double* U, const 
  * is the PoissonProblemPrimal system of solve_primal! with b = e_1 (x) b0 and a
  * zero start: its own n, K_0..K_M on one shared pattern (1-based CSC, values
  * (M+1) x nnz column-major), coupling G ((M*P) x P, 1-based CSC), boundary dofs
- * and b0.  sgfem_batch_solve runs Jacobi-preconditioned CG on all problems in
+ * and b0.  sgfem_batch_solve runs preconditioned CG (mean-based by sine transforms on
+ * problems marked with sgfem_batch_set_lattice, Jacobi otherwise) on all problems in
  * lock step: each phase of an iteration is one launch over every problem, a
  * batch of check_every iterations is a captured CUDA graph, converged problems
  * skip their blocks.  The apply's launch shape is chosen at finalize by timing
@@ -382,6 +383,10 @@ SGFEM_API int sgfem_batch_add(sgfem_batch* batch, int64_t n, int64_t M, int64_t 
                               const int64_t* Growval, const double* Gval, int64_t nbdofs, const int64_t* bdofs,
                               const double* b0);
 SGFEM_API int sgfem_batch_count(const sgfem_batch* batch);
+/* problem i's dofs are the (nl+1)^2 points of a uniform lattice, x fastest, Dirichlet rows on its
+   boundary (P1 on the unit square): it gets the mean-based preconditioner (a0 L)^-1 by sine transforms
+   (L the 5-point Laplacian, exact for P1 with a constant mean) instead of Jacobi */
+SGFEM_API int sgfem_batch_set_lattice(sgfem_batch* batch, int i, int64_t nl);
 SGFEM_API int sgfem_batch_finalize(sgfem_batch* batch);
 SGFEM_API const char* sgfem_batch_tuning(const sgfem_batch* batch);
 SGFEM_API int sgfem_batch_solve(sgfem_batch* batch, double rtol, int maxit, int check_every, double* x_out,
