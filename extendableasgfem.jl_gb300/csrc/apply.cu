@@ -166,7 +166,7 @@ int sg_launch_apply(sgfem_context* ctx, int precision, const void* X, void* Y, d
     const size_t smem = per_warp * sg_elem_bytes(precision) * WPB;
     if (smem > 200 * 1024)
         return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "apply: per-row pair list too large for shared memory");
-    if (precision == SGFEM_FP32 && ctx->jit_ok) {
+    if (precision == SGFEM_FP32 && sg_jit_accepts(ctx, X)) {
         const int jgrid = sg_jit_grid(ctx);
         if (nblocks) *nblocks = jgrid;
         return sg_jit_launch(ctx, X, Y, dot_partials, jgrid, skip_if_done);

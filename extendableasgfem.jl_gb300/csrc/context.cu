@@ -230,6 +230,7 @@ static bool detect_lattice(sgfem_context* ctx, std::vector<int32_t>& iperm) {
         iperm[i] = (int32_t)r;
     }
     ctx->Nl = Nl;
+    ctx->lat_np = Nl + 1;
     return true;
 }
 
@@ -369,6 +370,7 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
     // ---- numbering
     std::vector<int32_t> iperm;
     ctx->lattice = detect_lattice(ctx, iperm);
+    ctx->lat_order = ctx->lattice;
     if (!ctx->lattice) {
         iperm.resize(n);
         std::iota(iperm.begin(), iperm.end(), 0);
@@ -461,6 +463,34 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
         }
     }
     ctx->lat_scale = dcount ? dsum / (4.0 * dcount) : 1.0;
+    // lattice reach of the couplings (interior rows), for the window kernel
+    ctx->win_hx = ctx->win_hy = 0;
+    if (ctx->lat_order) {
+        const int np = ctx->lat_np;
+        for (int64_t i = 0; i < n; ++i) {
+            if (ctx->bmask_host[i]) continue;
+            const int iy = (int)(i / np), ix = (int)(i % np);
+            for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+                const int jy = col[k] / np, jx = col[k] % np;
+                ctx->win_hx = std::max(ctx->win_hx, std::abs(jx - ix));
+                ctx->win_hy = std::max(ctx->win_hy, std::abs(jy - iy));
+            }
+        }
+    }
+    // vanishing row sums of every K_m on the interior rows (stiffness and convection
+    // blocks without eliminated boundary columns) allow the difference-form FP32 apply
+    ctx->rowsum_zero = true;
+    for (int64_t i = 0; i < n && ctx->rowsum_zero; ++i) {
+        if (ctx->bmask_host[i]) continue;
+        for (int m = 0; m < M1; ++m) {
+            double sum = 0.0, asum = 0.0;
+            for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+                sum += val64[(size_t)k * M1 + m];
+                asum += fabs(val64[(size_t)k * M1 + m]);
+            }
+            if (fabs(sum) > 1e-10 * asum) { ctx->rowsum_zero = false; break; }
+        }
+    }
 
     if (ctx->batched) {
         // block-diagonal sample operator: identity mode order, per-sample coefficients

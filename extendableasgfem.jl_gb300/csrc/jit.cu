@@ -164,9 +164,10 @@ std::string generate_source(const sgfem_context* ctx) {
     char buf[512];
     snprintf(buf, sizeof(buf),
              "#define LD %d\n#define P %d\n#define KG %d\n#define M1P %d\n#define NS %d\n#define WPB %d\n"
-             "#define RCHUNK %d\n#define PREFETCH %d\n#define T %d\n#define STAGE %d\n#define PFD %d\n#define MINB %d\n",
+             "#define RCHUNK %d\n#define PREFETCH %d\n#define T %d\n#define STAGE %d\n#define PFD %d\n#define MINB %d\n"
+             "#define NBUF %d\n#define DIFF %d\n",
              LD, P, KG, M1P, NS, JWPB, ctx->jit_rchunk, ctx->jit_prefetch, ctx->jit_T, ctx->jit_stage, pfd,
-             ctx->jit_minb);
+             ctx->jit_minb, ctx->jit_nbuf, ctx->jit_diff);
     s += buf;
     s += R"(
 #define NV4 (M1P / 4)                 /* float4 per nonzero */
@@ -175,7 +176,7 @@ std::string generate_source(const sgfem_context* ctx) {
 #else
 #define CBUF 0
 #endif
-#define WSMEM (NS * 64 + 2 * CBUF + ((LD + 3) & ~3))   /* floats per warp */
+#define WSMEM (NS * 64 + NBUF * CBUF + ((LD + 3) & ~3))   /* floats per warp */
 struct Scal { double rho, pq, alpha, beta, rr, tol2; int done, status, iters, first; };
 
 __device__ __forceinline__ void pf_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
@@ -219,7 +220,7 @@ sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const 
     float* wb = smem + 2 * T * 32 + warp * WSMEM;
     float* sacc = wb;
     float* cbuf = wb + NS * 64;
-    float* ybuf = cbuf + 2 * CBUF;
+    float* ybuf = cbuf + NBUF * CBUF;
     for (int i = threadIdx.x; i < T * 32; i += blockDim.x) stab[i] = __ldg(jtab + i);
     __syncthreads();
     double dot = 0.0;
@@ -271,6 +272,16 @@ sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const 
         snprintf(buf, sizeof(buf), "            float2 a%d = make_float2(0.f, 0.f);\n", q);
         s += buf;
     }
+    // difference form: with vanishing row sums K x = sum_j K_ij (x_j - x_i); the own
+    // row's values are subtracted from every gathered row (no cancellation in FP32)
+    for (int k = 0; k < KG; ++k) {
+        const int valid = LD - 32 * k;
+        if (valid >= 32)
+            snprintf(buf, sizeof(buf), "            const float xi%d = DIFF ? __ldg(X + (size_t)row * LD + %d + lane) : 0.f;\n", k, 32 * k);
+        else
+            snprintf(buf, sizeof(buf), "            const float xi%d = (DIFF && lane < %d) ? __ldg(X + (size_t)row * LD + %d + lane) : 0.f;\n", k, valid, 32 * k);
+        s += buf;
+    }
     s += R"(            const int nz0 = rowptr[row], nz1 = rowptr[row + 1];
             if (PREFETCH && r1n < n) prefetch_x(X, jn1, cn1, lane);
             const float* cb = cbuf + b * CBUF;
@@ -305,10 +316,10 @@ sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const 
     for (int k = 0; k < KG; ++k) {
         const int valid = LD - 32 * k;
         if (valid >= 32)
-            snprintf(buf, sizeof(buf), "                const float u%d = __ldg(xr + %d);\n", k, 32 * k);
+            snprintf(buf, sizeof(buf), "                const float u%d = __ldg(xr + %d) - xi%d;\n", k, 32 * k, k);
         else
-            snprintf(buf, sizeof(buf), "                const float u%d = (lane < %d) ? __ldg(xr + %d) : 0.f;\n",
-                     k, valid, 32 * k);
+            snprintf(buf, sizeof(buf), "                const float u%d = (lane < %d) ? __ldg(xr + %d) - xi%d : 0.f;\n",
+                     k, valid, 32 * k, k);
         s += buf;
         snprintf(buf, sizeof(buf), "                const float2 w%d = make_float2(u%d, u%d);\n", k, k, k);
         s += buf;
@@ -338,7 +349,8 @@ sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const 
             s += buf;
         }
         for (int k = 0; k < KG; ++k) {
-            snprintf(buf, sizeof(buf), "                    const float2 w%d = make_float2(x%d_%d, x%d_%d);\n", k, d, k, d, k);
+            snprintf(buf, sizeof(buf), "                    const float2 w%d = make_float2(x%d_%d - xi%d, x%d_%d - xi%d);\n", k, d, k,
+                     k, d, k, k);
             s += buf;
         }
         s += loadx(ctx, d, "t0 + " + std::to_string(d + pfd), "                    ");
@@ -377,7 +389,7 @@ sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const 
 #if STAGE
         if (r1n < n) {  // stage the next row's values
             __syncwarp();
-            b ^= 1;
+            b = (NBUF == 2) ? (b ^ 1) : 0;  // one buffer: the row's reads are done (syncwarp above)
             STORE_VALUES(cbuf + b * CBUF, pv);
             __syncwarp();
         }
@@ -1001,8 +1013,263 @@ sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const 
     return s;
 }
 
+// Variant for operators whose rows are the points of a uniform dof lattice
+// (row = y * NLX + x) with couplings inside |dx| <= HX, |dy| <= HY: the
+// gathered X rows come from a shared-memory window instead of L2.  The
+// lattice is cut into strips of W = WPB * RW columns; a persistent block
+// walks up its share of (strip, line) steps and keeps the X rows of lines
+// y - HY .. y + HY of its strip plus HX halo columns on each side in a ring
+// of WL = 2 HY + 2 line slots (cp.async, 16-byte pieces).  Line y + HY + 1 is
+// copied while line y is computed; one barrier per line.  Warp w computes the
+// RW rows x0 + w RW + r of each line with the packed-FMA slots and the
+// combination of the register-window kernel; KLE values are staged per warp
+// one row ahead, in the storage that holds the accumulators during the
+// combination.  A column outside the window (a pattern that breaks the bounds
+// found at finalize) sets bit 4 of the status word and contributes nothing.
+std::string generate_source_window(const sgfem_context* ctx) {
+    const int LD = (int)ctx->ld, P = (int)ctx->P, M1P = ctx->M1P;
+    const int KG = (int)((P + 31) / 32);
+    const int NS = (int)ctx->jit_slots.size();
+    std::string s;
+    char buf[512];
+    snprintf(buf, sizeof(buf),
+             "#define LD %d\n#define P %d\n#define KG %d\n#define M1P %d\n#define NS %d\n#define WPB %d\n"
+             "#define T %d\n#define DIFF %d\n#define NLX %d\n#define NLY %d\n#define HX %d\n#define HY %d\n#define RW %d\n",
+             LD, P, KG, M1P, NS, ctx->jit_wwpb, ctx->jit_T, ctx->jit_diff, ctx->lat_np, ctx->lat_np, ctx->win_hx,
+             ctx->win_hy, ctx->jit_wrw);
+    s += buf;
+    s += R"(
+#define NV4 (M1P / 4)
+#define W (WPB * RW)                  /* rows of a strip per line */
+#define SW (W + 2 * HX)               /* window columns */
+#define WL (2 * HY + 2)               /* window line slots */
+#define NSTRIP ((NLX + W - 1) / W)
+#define LINES (NSTRIP * NLY)          /* (strip, line) steps */
+#define CBUF (32 * M1P)
+#define AREG (NS * 64 > CBUF ? NS * 64 : CBUF)
+#define WSMEM (AREG + ((LD + 3) & ~3))
+#define WIN (WL * SW * LD)
+struct Scal { double rho, pq, alpha, beta, rr, tol2; int done, status, iters, first; };
+
+__device__ __forceinline__ void cp16(float* dst, const float* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// lattice line ly, columns [max(0, xs), min(NLX, xs + SW)) -> its ring slot
+__device__ __forceinline__ void copy_line(float* win, const float* __restrict__ X, int ly, int xs) {
+    const int cx0 = max(0, xs), cx1 = min(NLX, xs + SW);
+    const int n4 = (cx1 - cx0) * (LD / 4);
+    const float* src = X + ((size_t)ly * NLX + cx0) * LD;
+    float* dst = win + ((ly % WL) * SW + (cx0 - xs)) * LD;
+    for (int i = threadIdx.x; i < n4; i += WPB * 32) cp16(dst + 4 * i, src + 4 * i);
+}
+
+#define LOAD_VALUES(pv, nz, cnt)                                                        \
+    _Pragma("unroll") for (int i_ = 0; i_ < NV4; ++i_) {                                \
+        const int q_ = lane + 32 * i_;                                                  \
+        pv[i_] = (q_ < (cnt) * NV4) ? __ldg(reinterpret_cast<const float4*>(vals + (size_t)(nz) * M1P) + q_) \
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);                  \
+    }
+#define STORE_VALUES(dst, pv)                                                           \
+    _Pragma("unroll") for (int i_ = 0; i_ < NV4; ++i_)                                  \
+        reinterpret_cast<float4*>(dst)[lane + 32 * i_] = pv[i_];
+
+// row of the warp's k-th step in a segment (k = (line - ya) * RW + r), -1 past the lattice edge
+__device__ __forceinline__ int seg_row(int k, int ya, int x0, int warp) {
+    const int x = x0 + warp * RW + k % RW;
+    return x < NLX ? (ya + k / RW) * NLX + x : -1;
+}
+
+extern "C" __global__ void __launch_bounds__(WPB * 32, 1)
+sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const float* __restrict__ vals,
+             const float* __restrict__ X, float* __restrict__ Y, int n, const unsigned char* __restrict__ bmask,
+             const int2* __restrict__ jtab, double* __restrict__ partials, const Scal* __restrict__ scal,
+             int* __restrict__ err) {
+    if (scal && scal->done) return;
+    extern __shared__ __align__(16) float smem[];
+    __shared__ double red[WPB];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int2* stab = reinterpret_cast<int2*>(smem);
+    float* win = smem + 2 * T * 32;
+    float* wb = win + WIN + warp * WSMEM;
+    float* sacc = wb;
+    float* cbuf = wb;
+    float* ybuf = wb + AREG;
+    for (int i = threadIdx.x; i < T * 32; i += blockDim.x) stab[i] = __ldg(jtab + i);
+    double dot = 0.0;
+    int bad = 0;
+    const int g0 = (int)(((long long)blockIdx.x * LINES) / gridDim.x);
+    const int g1 = (int)(((long long)(blockIdx.x + 1) * LINES) / gridDim.x);
+    for (int g = g0; g < g1;) {
+        const int strip = g / NLY, ya = g - strip * NLY;
+        const int yb = min(NLY, ya + (g1 - g));
+        g += yb - ya;
+        const int x0 = strip * W, xs = x0 - HX;
+        __syncthreads();  // every read of the previous segment's window is done
+        for (int ly = max(0, ya - HY); ly <= min(NLY - 1, ya + HY); ++ly) copy_line(win, X, ly, xs);
+        cp_commit();
+        const int KR = (yb - ya) * RW;
+        // the warp's first row: its columns and values
+        int k = 0;
+        while (k < KR && seg_row(k, ya, x0, warp) < 0) ++k;
+        int jn1 = 0, cn1 = 0;
+        float4 pv[NV4];
+        if (k < KR) {
+            const int r0 = seg_row(k, ya, x0, warp);
+            const int a = __ldg(rowptr + r0);
+            cn1 = min(32, __ldg(rowptr + r0 + 1) - a);
+            jn1 = (lane < cn1) ? __ldg(col + a + lane) : 0;
+            LOAD_VALUES(pv, a, cn1);
+            STORE_VALUES(cbuf, pv);
+        }
+        for (int kk = 0; kk < KR; ++kk) {
+            if (kk % RW == 0) {  // new line: its window lines are present, start copying the next one
+                const int y = ya + kk / RW;
+                cp_wait_all();
+                __syncthreads();
+                if (y + HY + 1 < NLY && y + 1 < yb) copy_line(win, X, y + HY + 1, xs);
+                cp_commit();
+            }
+            const int row = seg_row(kk, ya, x0, warp);
+            if (row < 0) continue;  // warp-uniform: past the lattice edge
+            const int y = ya + kk / RW, x = row - y * NLX;
+            const int jcur = jn1, ccur = cn1;
+            int kn = kk + 1;
+            while (kn < KR && seg_row(kn, ya, x0, warp) < 0) ++kn;
+            const int r1n = kn < KR ? seg_row(kn, ya, x0, warp) : -1;
+            if (r1n >= 0) {  // next row: columns and values (first 32 nonzeros) into registers
+                const int a = __ldg(rowptr + r1n);
+                cn1 = min(32, __ldg(rowptr + r1n + 1) - a);
+                jn1 = (lane < cn1) ? __ldg(col + a + lane) : 0;
+                LOAD_VALUES(pv, a, cn1);
+            }
+            float* yrow = Y + (size_t)row * LD;
+            const float* xown = win + ((y % WL) * SW + (x - xs)) * LD;
+            if (bmask[row]) {
+                for (int c = lane; c < LD; c += 32) yrow[c] = 0.f;
+            } else {
+)";
+    for (int q = 0; q < NS; ++q) {
+        snprintf(buf, sizeof(buf), "                float2 a%d = make_float2(0.f, 0.f);\n", q);
+        s += buf;
+    }
+    for (int k = 0; k < KG; ++k) {
+        const int valid = LD - 32 * k;
+        if (valid >= 32)
+            snprintf(buf, sizeof(buf), "                const float xi%d = DIFF ? xown[%d + lane] : 0.f;\n", k, 32 * k);
+        else
+            snprintf(buf, sizeof(buf), "                const float xi%d = (DIFF && lane < %d) ? xown[%d + lane] : 0.f;\n", k,
+                     valid, 32 * k);
+        s += buf;
+    }
+    s += R"(                const int nz0 = __ldg(rowptr + row), nz1 = __ldg(rowptr + row + 1);
+                for (int base = nz0; base < nz1; base += 32) {
+                    const int cnt = min(32, nz1 - base);
+                    int jl = jcur;
+                    if (base != nz0) {  // rows longer than 32 nonzeros: later chunks load synchronously
+                        jl = (lane < cnt) ? __ldg(col + base + lane) : 0;
+                        float4 lv[NV4];
+                        __syncwarp();
+                        LOAD_VALUES(lv, base, cnt);
+                        STORE_VALUES(cbuf, lv);
+                        __syncwarp();
+                    } else {
+                        (void)ccur;
+                    }
+                    // window offset of each lane's nonzero
+                    int off = (int)(xown - win);
+                    if (lane < cnt) {
+                        const int cy = jl / NLX, cx = jl - cy * NLX;
+                        const int dy = cy - y, wx = cx - xs;
+                        if (dy < -HY || dy > HY || wx < 0 || wx >= SW) bad = 1;
+                        else off = ((cy % WL) * SW + wx) * LD;
+                    }
+#pragma unroll 2
+                    for (int t = 0; t < cnt; ++t) {
+                        const float* xr = win + __shfl_sync(0xffffffffu, off, t) + lane;
+                        const float4* cv = reinterpret_cast<const float4*>(cbuf + t * M1P);
+)";
+    for (int v = 0; v < M1P / 4; ++v) {
+        snprintf(buf, sizeof(buf), "                        const float4 c%d = cv[%d];\n", v, v);
+        s += buf;
+    }
+    for (int k = 0; k < KG; ++k) {
+        const int valid = LD - 32 * k;
+        if (valid >= 32)
+            snprintf(buf, sizeof(buf), "                        const float u%d = xr[%d] - xi%d;\n", k, 32 * k, k);
+        else
+            snprintf(buf, sizeof(buf), "                        const float u%d = (lane < %d) ? xr[%d] - xi%d : 0.f;\n", k,
+                     valid, 32 * k, k);
+        s += buf;
+        snprintf(buf, sizeof(buf), "                        const float2 w%d = make_float2(u%d, u%d);\n", k, k, k);
+        s += buf;
+    }
+    s += slot_fmas(ctx, "                        ");
+    s += "                    }\n";
+    s += "                }\n";
+    s += "                __syncwarp();  // staged values read: their storage takes the accumulators\n";
+    for (int q = 0; q < NS; ++q) {
+        snprintf(buf, sizeof(buf), "                *reinterpret_cast<float2*>(sacc + %d + 2 * lane) = a%d;\n", q * 64, q);
+        s += buf;
+    }
+    s += R"(                __syncwarp();
+                float acc = 0.f;
+#pragma unroll
+                for (int i = 0; i < T; ++i) {
+                    const int2 e = stab[i * 32 + lane];
+                    acc = fmaf(__int_as_float(e.y), sacc[e.x & 0x1fff], acc);
+                    if (e.x >> 28) {
+                        ybuf[(e.x >> 13) & 0x7fff] = acc;
+                        acc = 0.f;
+                    }
+                }
+                __syncwarp();
+                float rowdot = 0.f;
+                for (int c = lane; c < LD; c += 32) {
+                    const float yv = (c < P) ? ybuf[c] : 0.f;
+                    yrow[c] = yv;
+                    if (partials) rowdot = fmaf(xown[c], yv, rowdot);
+                }
+                dot += (double)rowdot;
+            }
+            if (r1n >= 0) {  // stage the next row's values (accumulator reads are done)
+                __syncwarp();
+                STORE_VALUES(cbuf, pv);
+                __syncwarp();
+            }
+        }
+    }
+    cp_wait_all();
+    if (bad) atomicOr(err, 4);
+    if (partials) {
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
+        if (lane == 0) red[warp] = dot;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t2 = 0.0;
+            for (int w2 = 0; w2 < WPB; ++w2) t2 += red[w2];
+            partials[blockIdx.x] = t2;
+        }
+    }
+}
+)";
+    return s;
+}
+
+size_t window_smem_bytes(const sgfem_context* ctx, int wpb) {
+    const size_t NS = ctx->jit_slots.size();
+    const size_t W = (size_t)wpb * ctx->jit_wrw, SW = W + 2 * (size_t)ctx->win_hx, WL = 2 * (size_t)ctx->win_hy + 2;
+    const size_t areg = std::max(NS * 64, (size_t)32 * ctx->M1P);
+    const size_t wsmem = areg + ((ctx->ld + 3) & ~(size_t)3);
+    return (2 * (size_t)ctx->jit_T * 32 + WL * SW * ctx->ld + wpb * wsmem) * sizeof(float);
+}
+
 size_t jit_smem_bytes(const sgfem_context* ctx) {
     const int NS = (int)ctx->jit_slots.size();
+    if (ctx->jit_window) return window_smem_bytes(ctx, ctx->jit_wwpb);
     if (ctx->jit_np > 1 && !ctx->jit_async) {
         int maxps = 0;
         for (int p = 0; p < ctx->jit_np; ++p)
@@ -1015,7 +1282,7 @@ size_t jit_smem_bytes(const sgfem_context* ctx) {
                              (ctx->jit_async == 2 ? 2 * (size_t)ctx->jit_adepth : 0);
         return (2 * (size_t)ctx->jit_T * 32 + JWPB * wsmem) * sizeof(float);
     }
-    const size_t wsmem = (size_t)NS * 64 + (ctx->jit_stage ? 2 * 32 * ctx->M1P : 0) + ((ctx->ld + 3) & ~3);
+    const size_t wsmem = (size_t)NS * 64 + (ctx->jit_stage ? (size_t)ctx->jit_nbuf * 32 * ctx->M1P : 0) + ((ctx->ld + 3) & ~3);
     return (2 * (size_t)ctx->jit_T * 32 + JWPB * wsmem) * sizeof(float);
 }
 
@@ -1041,6 +1308,16 @@ void sg_jit_configure(sgfem_context* ctx) {
     ctx->jit_async = ea ? std::max(0, std::min(2, atoi(ea))) : 0;
     const char* eq = getenv("SGFEM_JIT_ADEPTH");
     ctx->jit_adepth = eq ? std::max(2, std::min(16, atoi(eq))) : 6;
+    const char* eb2 = getenv("SGFEM_JIT_NBUF");
+    ctx->jit_nbuf = eb2 ? std::max(1, std::min(2, atoi(eb2))) : 1;
+    const char* ewn = getenv("SGFEM_JIT_WINDOW");
+    ctx->jit_window_req = ewn ? (atoi(ewn) != 0) : 1;
+    const char* eww = getenv("SGFEM_JIT_WWPB");
+    ctx->jit_wwpb = eww ? std::max(1, std::min(32, atoi(eww))) : 12;
+    const char* ewr = getenv("SGFEM_JIT_WRW");
+    ctx->jit_wrw = ewr ? std::max(1, std::min(8, atoi(ewr))) : 2;
+    const char* edf = getenv("SGFEM_JIT_DIFF");
+    ctx->jit_diff_req = edf ? (atoi(edf) != 0) : 1;
     const char* en = getenv("SGFEM_JIT_PASSES");
     ctx->jit_np_req = en ? std::max(1, std::min(8, atoi(en))) : 1;
     if (ctx->jit_async) ctx->jit_np_req = 1;  // the copy-pipeline variants use one pass
@@ -1050,6 +1327,20 @@ void sg_jit_configure(sgfem_context* ctx) {
 
 int sg_jit_build(sgfem_context* ctx) {
     ctx->jit_ok = false;
+    // lattice-window kernel: lattice-ordered rows with short couplings, one pass, and a
+    // window that fits shared memory with at least 4 warps per block
+    ctx->jit_window = 0;
+    if (ctx->jit_window_req && ctx->lat_order && !ctx->jit_async && ctx->jit_np <= 1 && ctx->win_hx <= 4 &&
+        ctx->win_hy <= 4 && ctx->ld % 4 == 0 && ctx->jit_T > 0) {
+        int wpb = ctx->jit_wwpb;
+        while (wpb >= 4 && window_smem_bytes(ctx, wpb) > 220 * 1024) --wpb;
+        if (wpb >= 4) {
+            ctx->jit_wwpb = wpb;
+            ctx->jit_window = 1;
+        }
+    }
+    // the difference form is generated by the single-pass kernels only
+    ctx->jit_diff = (ctx->jit_diff_req && ctx->rowsum_zero && !ctx->jit_async && ctx->jit_np <= 1) ? 1 : 0;
     if (ctx->jit_disabled) {
         ctx->jit_log = "disabled by SGFEM_APPLY=generic";
         return SGFEM_ERR_UNSUPPORTED;
@@ -1067,7 +1358,8 @@ int sg_jit_build(sgfem_context* ctx) {
         ctx->jit_log = g_drv.err;
         return SGFEM_ERR_UNSUPPORTED;
     }
-    const std::string src = ctx->jit_async == 2 ? generate_source_bulk(ctx)
+    const std::string src = ctx->jit_window ? generate_source_window(ctx)
+                            : ctx->jit_async == 2 ? generate_source_bulk(ctx)
                             : ctx->jit_async ? generate_source_async(ctx)
                             : ctx->jit_np > 1 ? generate_source_passes(ctx) : generate_source(ctx);
     nvrtcProgram prog = nullptr;
@@ -1117,7 +1409,8 @@ int sg_jit_build(sgfem_context* ctx) {
     if (ctx->jit_carveout >= 0)
         g_drv.func_set_attribute(fn, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, ctx->jit_carveout);
     int bps = 0;
-    if (g_drv.occupancy(&bps, fn, JWPB * 32, (size_t)smem) != CUDA_SUCCESS || bps < 1) {
+    if (g_drv.occupancy(&bps, fn, (ctx->jit_window ? ctx->jit_wwpb : JWPB) * 32, (size_t)smem) != CUDA_SUCCESS ||
+        bps < 1) {
         g_drv.module_unload(mod);
         ctx->jit_log = "occupancy query failed";
         return SGFEM_ERR_UNSUPPORTED;
@@ -1137,11 +1430,25 @@ int sg_jit_build(sgfem_context* ctx) {
     ctx->jit_ok = true;
     ctx->jit_log = "specialised FP32 apply: " + std::to_string(NS) + " slots, " + std::to_string(bps) +
                    " blocks/SM, rows/chunk " + std::to_string(ctx->jit_rchunk) + ", prefetch " +
-                   std::to_string(ctx->jit_prefetch) + ", staged values " + std::to_string(ctx->jit_stage);
+                   std::to_string(ctx->jit_prefetch) + ", staged values " + std::to_string(ctx->jit_stage) +
+                   (ctx->jit_diff ? ", difference form" : "") +
+                   (ctx->jit_window ? ", lattice window " + std::to_string(ctx->jit_wwpb * ctx->jit_wrw) + " x " +
+                                          std::to_string(2 * ctx->win_hy + 2) + " lines, " +
+                                          std::to_string(ctx->jit_wwpb) + " warps"
+                                    : std::string());
     return SGFEM_OK;
 }
 
+bool sg_jit_accepts(const sgfem_context* ctx, const void* X) {
+    return ctx->jit_ok && (!ctx->jit_window || ((uintptr_t)X % 16) == 0);
+}
+
 int sg_jit_grid(const sgfem_context* ctx) {
+    if (ctx->jit_window) {
+        const int64_t W = (int64_t)ctx->jit_wwpb * ctx->jit_wrw;
+        const int64_t lines = (ctx->lat_np + W - 1) / W * ctx->lat_np;
+        return (int)std::max<int64_t>(1, std::min<int64_t>(lines, (int64_t)ctx->num_sms * std::min(ctx->jit_blocks_per_sm, 8)));
+    }
     // persistent: one wave of resident blocks, each warp a contiguous row range
     const int64_t want = (ctx->n + JWPB - 1) / JWPB;
     const int64_t resident = (int64_t)ctx->num_sms * std::min(ctx->jit_blocks_per_sm, 8);
@@ -1159,7 +1466,8 @@ int sg_jit_launch(sgfem_context* ctx, const void* X, void* Y, double* partials, 
     int* errp = ctx->d_jit_err;
     void* args[] = {(void*)&rowptr, (void*)&colp, (void*)&vals, (void*)&X, (void*)&Y, (void*)&n, (void*)&bm,
                     (void*)&jtab, (void*)&partials, (void*)&scal, (void*)&errp};
-    CUresult r = g_drv.launch_kernel((CUfunction)ctx->jit_func, grid, 1, 1, JWPB * 32, 1, 1, smem,
+    const unsigned threads = (unsigned)(ctx->jit_window ? ctx->jit_wwpb : JWPB) * 32;
+    CUresult r = g_drv.launch_kernel((CUfunction)ctx->jit_func, grid, 1, 1, threads, 1, 1, smem,
                                      (CUstream)ctx->stream, args, nullptr);
     if (r != CUDA_SUCCESS) return sg_fail(ctx, SGFEM_ERR_CUDA, "cuLaunchKernel(sg_apply_jit) failed: " + std::to_string((int)r));
     ctx->launches++;
@@ -1174,6 +1482,7 @@ int sg_jit_check(sgfem_context* ctx) {
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (h == 0) return SGFEM_OK;
     SG_CUDA(ctx, cudaMemsetAsync(ctx->d_jit_err, 0, sizeof(int), ctx->stream));
+    if (h & 4) return sg_fail(ctx, SGFEM_ERR_CUDA, "specialised apply: a column outside the lattice window");
     return sg_fail(ctx, SGFEM_ERR_CUDA, "specialised apply: a shared-memory copy did not complete in time");
 }
 

@@ -40,6 +40,7 @@ struct LatGeom {
     int lg;     // log2(Nl)
     int ld;     // row stride of SG vectors
     int nchunk; // ceil(ld / 32)
+    int async;  // the loaded vector is 16-byte aligned: lines are copied with cp.async
 };
 
 // table layout (length 3*Nl/2 + 1):
@@ -196,8 +197,37 @@ __device__ __forceinline__ size_t lat_row(int dir, int line, int p, int Nl) {
 // global loads are in flight per warp instead of one
 constexpr int LAT_UNROLL = 8;
 
+// the whole tile of a line in flight at once: 16-byte asynchronous copies
+// (the row stride is a multiple of 4 values, so a piece never straddles it)
+template <typename T>
+__device__ void load_line_async(T* tile, const T* __restrict__ in, int dir, int line, int chunk, LatGeom g) {
+    constexpr int EPP = 16 / sizeof(T);  // values per piece
+    constexpr int PPP = 32 / EPP;        // pieces per point
+    const int npieces = (g.Nl - 1) * PPP;
+    for (int i = threadIdx.x; i < npieces; i += blockDim.x) {
+        const int p = 1 + i / PPP, q = i - (i / PPP) * PPP;
+        const int m0 = chunk * 32 + q * EPP;
+        T* dst = tile + p * 32 + q * EPP;
+        if (m0 < g.ld) {
+            const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d),
+                         "l"(in + lat_row(dir, line, p, g.Nl) * g.ld + m0)
+                         : "memory");
+        } else {
+#pragma unroll
+            for (int e = 0; e < EPP; ++e) dst[e] = T(0);
+        }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
 template <typename T>
 __device__ void load_line(T* tile, const T* __restrict__ in, int dir, int line, int chunk, LatGeom g) {
+    if (g.async) {
+        load_line_async(tile, in, dir, line, chunk, g);
+        return;
+    }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int mode = chunk * 32 + lane;
     for (int p0 = 1 + warp; p0 < g.Nl; p0 += LAT_WARPS * LAT_UNROLL) {
@@ -318,6 +348,7 @@ LatGeom geom(const sgfem_context* ctx) {
     g.lg = ctx->lat_log2;
     g.ld = (int)ctx->ld;
     g.nchunk = (int)((ctx->ld + 31) / 32);
+    g.async = 0;
     return g;
 }
 
@@ -457,6 +488,7 @@ PassYFn<T> pass_y_fn(int LGL) {
 template <typename T>
 int launch_x(sgfem_context* ctx, const void* in, void* out, const T* tab, int mode, const KrylovScalars* scal) {
     LatGeom g = geom(ctx);
+    g.async = ((uintptr_t)in % 16) == 0;
     PassXFn<T> fn = pass_x_fn<T>(ctx->lat_log2 - 1);
     if (!fn) return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice size outside the compiled range");
     const int grid = (g.Nl - 1) * g.nchunk;
@@ -469,6 +501,7 @@ template <typename T>
 int launch_y(sgfem_context* ctx, void* buf, const T* tab, const T* scale, double* rz, int* nblocks,
              const KrylovScalars* scal) {
     LatGeom g = geom(ctx);
+    g.async = ((uintptr_t)buf % 16) == 0;
     PassYFn<T> fn = pass_y_fn<T>(ctx->lat_log2 - 1);
     if (!fn) return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice size outside the compiled range");
     const int grid = (g.Nl - 1) * g.nchunk;

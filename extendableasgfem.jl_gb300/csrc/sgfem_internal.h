@@ -122,6 +122,14 @@ struct sgfem_context {
     int jit_rchunk = 8;                     // rows per warp chunk
     int jit_prefetch = 0;
     int jit_pfd = 1;                        // X prefetch distance in nonzeros (register window)
+    int jit_nbuf = 1;                       // KLE value staging buffers per warp (1 or 2)
+    int jit_diff_req = 1;                   // difference form asked for (SGFEM_JIT_DIFF)
+    int jit_diff = 0;                       // difference form in use: FP32 apply as sum_j K_ij (x_j - x_i)
+    bool rowsum_zero = false;               // every row of every K_m sums to zero (up to rounding)
+    int jit_window_req = 1;                 // lattice-window kernel asked for (SGFEM_JIT_WINDOW)
+    int jit_window = 0;                     // lattice-window kernel in use
+    int jit_wwpb = 12;                      // its warps per block
+    int jit_wrw = 2;                        // its rows per warp and lattice line
     int jit_minb = 0;                       // minimum resident blocks per SM asked of ptxas (0: none)
     int jit_async = 0;                      // cp.async ring variant of the kernel
     int jit_adepth = 6;                     // ring slots (nonzeros in flight + 1) per warp
@@ -140,6 +148,9 @@ struct sgfem_context {
     // lattice preconditioner
     bool lattice = false;
     int Nl = 0;                 // lattice intervals per side; points (Nl+1)^2
+    bool lat_order = false;     // device rows are the lattice points, row = y * lat_np + x
+    int lat_np = 0;             // lattice points per line (Nl + 1)
+    int win_hx = 0, win_hy = 0; // largest |dx|, |dy| between an interior row and its columns
     int lat_log2 = 0;           // Nl = 2^lat_log2
     double lat_scale = 1.0;     // a0: K_0 ~ a0 * L on interior rows
     double* d_lat_tab64 = nullptr;  // see lattice.cu
@@ -207,6 +218,8 @@ int sg_jit_launch(sgfem_context* ctx, const void* X, void* Y, double* partials, 
 void sg_jit_release(sgfem_context* ctx);
 // error status of the specialised kernel since the last check (resets it)
 int sg_jit_check(sgfem_context* ctx);
+// whether the specialised kernel takes this X (the window kernel copies 16-byte pieces)
+bool sg_jit_accepts(const sgfem_context* ctx, const void* X);
 
 // ------------------------------------------------------------------ layout (context.cu)
 int sg_launch_to_device(sgfem_context* ctx, const double* stage, void* X, int precision);

@@ -170,3 +170,69 @@ def test_specialised_fp32_apply_active_and_matches_generic(built_pkg, monkeypatc
         op.close()
         opg.close()
 
+
+
+KNOBS = [
+    {},
+    {"SGFEM_JIT_DIFF": "0"},
+    {"SGFEM_JIT_WWPB": "4", "SGFEM_JIT_WRW": "3"},
+    {"SGFEM_JIT_WRW": "1"},
+    {"SGFEM_JIT_WINDOW": "0"},
+    {"SGFEM_JIT_WINDOW": "0", "SGFEM_JIT_DIFF": "0"},
+    {"SGFEM_JIT_WINDOW": "0", "SGFEM_JIT_PFD": "2"},
+    {"SGFEM_JIT_WINDOW": "0", "SGFEM_JIT_NBUF": "2"},
+    {"SGFEM_JIT_WINDOW": "0", "SGFEM_JIT_STAGE": "0"},
+    {"SGFEM_JIT_PASSES": "2"},
+    {"SGFEM_JIT_ASYNC": "1"},
+    {"SGFEM_JIT_ASYNC": "2"},
+    {"SGFEM_JIT_WINDOW": "0", "SGFEM_JIT_RCHUNK": "1", "SGFEM_JIT_PREFETCH": "1"},
+]
+
+
+@pytest.mark.parametrize("knobs", KNOBS, ids=lambda k: ",".join(f"{a[10:]}={b}" for a, b in k.items()) or "default")
+def test_specialised_apply_launch_variants(built_pkg, monkeypatch, knobs):
+    """Every generated form of the specialised FP32 apply (lattice window with
+    its block shapes, register window with its prefetch depth and staging
+    buffers, passes over column groups, cp.async ring, bulk copies with
+    mbarriers) agrees with FP64 to FP32 accuracy."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    p = build(16, 2, 8, pkg.top_weight_multiindices(8, 60, C.decay_factors))
+    for k, v in knobs.items():
+        monkeypatch.setenv(k, v)
+    op = pkg.SGOperator(p.V, p.TB, p.Kall, device=0)
+    x = np.random.default_rng(11).standard_normal(p.n * p.P)
+    y32 = op.mul(x, pkg.FP32)
+    variant, log = op.ctx.apply_variant
+    assert variant == 1, log
+    if knobs in ({}, {"SGFEM_JIT_DIFF": "0"}):
+        assert ("difference form" in log) == (knobs == {}), log
+    windowed = not any(k in knobs for k in ("SGFEM_JIT_WINDOW", "SGFEM_JIT_PASSES", "SGFEM_JIT_ASYNC"))
+    assert ("lattice window" in log) == windowed, log
+    y64 = op.mul(x, pkg.FP64)
+    assert rel(y32, y64) <= 1e-5
+    op.close()
+
+
+def test_difference_form_accuracy_on_smooth_input(built_pkg, monkeypatch):
+    """With vanishing row sums the FP32 apply evaluates sum_j K_ij (x_j - x_i):
+    on a smooth x (where K x is small against |K| |x|: the direct sum cancels
+    to O(h^2) |K| |x|, the differences only to O(h)) its error relative to
+    FP64 is far below that of the direct sum."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    p = config1_like(N=64, order=2)
+    xy = p.V.dof_coords
+    base = np.sin(np.pi * xy[:, 0]) * np.sin(np.pi * xy[:, 1])
+    # FP32-representable input: both forms apply the operator to the same vector
+    x = np.concatenate([base * (0.5 ** k) for k in range(p.P)]).astype(np.float32).astype(np.float64)
+    errs = {}
+    for diff in ("1", "0"):
+        monkeypatch.setenv("SGFEM_JIT_DIFF", diff)
+        op = pkg.SGOperator(p.V, p.TB, p.Kall, device=0)
+        y32 = op.mul(x, pkg.FP32)
+        assert ("difference form" in op.ctx.apply_variant[1]) == (diff == "1")
+        errs[diff] = rel(y32, op.mul(x, pkg.FP64))
+        op.close()
+    assert errs["1"] < 0.2 * errs["0"], errs
