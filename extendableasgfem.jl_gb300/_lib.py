@@ -69,6 +69,7 @@ SIGNATURES = {
     "sgfem_set_dof_coordinates": (ctypes.c_int, [_P, ctypes.c_int64, _DP]),
     "sgfem_finalize": (ctypes.c_int, [_P]),
     "sgfem_has_lattice": (ctypes.c_int, [_P]),
+    "sgfem_lattice_log": (ctypes.c_char_p, [_P]),
     "sgfem_apply": (ctypes.c_int, [_P, _DP, _DP, ctypes.c_int]),
     "sgfem_precondition": (ctypes.c_int, [_P, _DP, _DP, ctypes.c_int, ctypes.c_int]),
     "sgfem_solve": (ctypes.c_int, [_P, _DP, _DP, ctypes.POINTER(SolveOptions), ctypes.POINTER(SolveStats)]),
@@ -232,6 +233,11 @@ class Context:
     @property
     def has_lattice(self):
         return bool(self.lib.sgfem_has_lattice(self.h))
+
+    @property
+    def lattice_log(self):
+        """Which mean-based lattice preconditioner is in use (exact block form or Laplacian), and why."""
+        return self.lib.sgfem_lattice_log(self.h).decode()
 
     def device_layout(self):
         n = ctypes.c_int64()

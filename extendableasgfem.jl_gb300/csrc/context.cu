@@ -86,7 +86,7 @@ extern "C" int sgfem_destroy(sgfem_context* ctx) {
     void* ptrs[] = {ctx->d_rowptr, ctx->d_col, ctx->d_val64, ctx->d_val32, ctx->d_bmask, ctx->d_iperm,
                     ctx->d_dinv64, ctx->d_dinv32, ctx->d_qtab, ctx->d_combptr, ctx->d_combq,
                     ctx->d_combg64, ctx->d_combg32, ctx->d_lat_tab64, ctx->d_lat_tab32,
-                    ctx->d_lat_scale64, ctx->d_lat_scale32, ctx->d_scal, ctx->w_stage.p, ctx->w_partials.p,
+                    ctx->d_lat_scale64, ctx->d_lat_scale32, ctx->d_lat_blk64, ctx->d_lat_blk32, ctx->d_scal, ctx->w_stage.p, ctx->w_partials.p,
                     ctx->d_jptr, ctx->d_joff, ctx->d_jg, ctx->d_jtab, ctx->d_val32p, ctx->d_mode_of_col,
                     ctx->d_y64, ctx->d_y32};
     sg_jit_release(ctx);
@@ -209,6 +209,10 @@ extern "C" int sgfem_set_dof_coordinates(sgfem_context* ctx, int64_t n, const do
 }
 
 extern "C" int sgfem_has_lattice(const sgfem_context* ctx) { return (ctx && ctx->lattice) ? 1 : 0; }
+extern "C" const char* sgfem_lattice_log(const sgfem_context* ctx) {
+    if (!ctx) return "";
+    return ctx->lattice ? ctx->lat_log.c_str() : "no lattice preconditioner";
+}
 
 // lattice detection: every dof at (ix/Nl, iy/Nl), all (Nl+1)^2 points present once
 static bool detect_lattice(sgfem_context* ctx, std::vector<int32_t>& iperm) {
@@ -721,6 +725,7 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
 
     if (ctx->lattice) {
         int s = sg_lattice_setup(ctx);
+        if (s == SGFEM_OK) s = sg_lattice_blocks(ctx, rowptr, col, val64);
         if (s != SGFEM_OK) {
             if (s == SGFEM_ERR_UNSUPPORTED) {
                 ctx->lattice = false;  // e.g. Nl not a power of two: Jacobi only

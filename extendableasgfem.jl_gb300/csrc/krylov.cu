@@ -412,7 +412,7 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
         for (int i = 5; i < 10; ++i) SG_TRY(sg_ensure(ctx, ctx->w_vec[i], n32));
         SG_TRY(sg_jit_ensure(ctx));
     }
-    const int maxblocks = std::max<int>(ctx->num_sms * 8, ctx->lattice ? (ctx->Nl - 1) * (int)((ctx->ld + 31) / 32) : 1);
+    const int maxblocks = std::max<int>(ctx->num_sms * 8, sg_lat_max_blocks(ctx));
     SG_TRY(sg_ensure(ctx, ctx->w_partials, (size_t)(maxblocks + 8) * sizeof(double)));
     double* partials = (double*)ctx->w_partials.p;
     double* b = (double*)ctx->w_vec[0].p;
@@ -500,6 +500,10 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
     // SGFEM_TRACE=1: one line per refinement step on stderr (the reference's @info progress)
     const char* etr = getenv("SGFEM_TRACE");
     const bool trace = etr && atoi(etr) != 0;
+    // smallest reduction asked of one later refinement step (SGFEM_MIXED_FLOOR)
+    const char* efl = getenv("SGFEM_MIXED_FLOOR");
+    const double floor1 = efl ? std::max(1e-10, std::min(1e-2, atof(efl))) : 1e-6;
+    const double floor2 = floor1 * floor1;
     // sample problems: the global residual is driven down until every column
     // meets rtol relative to its own right-hand side
     double tol2e = rtol2;
@@ -544,7 +548,7 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
                 double want;
                 if (o->precision == SGFEM_FP32) want = std::max(in2, 0.25 * tol2e * bb / rr);
                 else if (outer == 0) want = std::max(in2, finish);
-                else want = std::max(finish, 1e-12);
+                else want = std::max(finish, floor2);
                 SG_TRY(S.fin(g, FIN_TOL, FinArgs{want, 0}, nullptr));
                 int it = 0;
                 int s2 = S.pcg<float>(SGFEM_FP32, d32, r32, p32, q32, tmp32, remaining, check_every, &it);

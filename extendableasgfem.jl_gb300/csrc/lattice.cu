@@ -25,7 +25,9 @@
 // in shared memory, every lane works on its own mode, so each global access
 // is a contiguous 32-mode segment of one dof and every shared-memory access
 // is bank-conflict free.
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "sgfem_internal.h"
@@ -342,6 +344,108 @@ k_lat_pass_y(T* __restrict__ buf, const T* __restrict__ tab, const T* __restrict
     }
 }
 
+// Pass Y with the exact mean preconditioner: after pass X the columns kx and
+// Nl - kx of the lattice carry the x-frequencies that K_0 couples (the sine
+// transform of a stencil that repeats with period 2 links k and Nl - k), so a
+// block owns the column pair (i, Nl - i) and 16 modes: lanes 0-15 column i,
+// lanes 16-31 column Nl - i (zero when i = Nl/2), each lane one mode.  After
+// DST_y the four values of (i | Nl-i) x (ky | Nl-ky) get their 4x4 block of
+// (2/Nl)^2 (S K_0 S)^-1, then DST_y again; r'z by Parseval.
+template <typename T>
+__device__ void load_pair(T* tile, const T* __restrict__ in, int i, int chunk, LatGeom g) {
+    const bool self = (2 * i == g.Nl);
+    if (g.async) {
+        constexpr int EPP = 16 / sizeof(T);
+        constexpr int PPH = 16 / EPP;  // pieces per half row of the tile
+        const int npieces = (g.Nl - 1) * 2 * PPH;
+        for (int t = threadIdx.x; t < npieces; t += blockDim.x) {
+            const int p = 1 + t / (2 * PPH), q = t % (2 * PPH), h = q / PPH, qq = q % PPH;
+            const int m0 = chunk * 16 + qq * EPP;
+            T* dst = tile + p * 32 + h * 16 + qq * EPP;
+            if (m0 < g.ld && !(h && self)) {
+                const int col = h ? g.Nl - i : i;
+                const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d),
+                             "l"(in + lat_row(1, col, p, g.Nl) * g.ld + m0)
+                             : "memory");
+            } else {
+#pragma unroll
+                for (int e = 0; e < EPP; ++e) dst[e] = T(0);
+            }
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+    } else {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, h = lane >> 4;
+        const int m = chunk * 16 + (lane & 15), col = h ? g.Nl - i : i;
+        const bool ok = m < g.ld && !(h && self);
+        for (int p = 1 + warp; p < g.Nl; p += LAT_WARPS)
+            tile[p * 32 + lane] = ok ? in[lat_row(1, col, p, g.Nl) * g.ld + m] : T(0);
+    }
+}
+
+template <typename T, int LGL>
+__global__ void __launch_bounds__(LAT_THREADS)
+k_lat_pass_yb(T* __restrict__ buf, const T* __restrict__ tab, const T* __restrict__ blk, LatGeom g,
+              double* __restrict__ rz, const KrylovScalars* __restrict__ scal) {
+    if (scal && scal->done) return;
+    extern __shared__ unsigned char smem_raw[];
+    T* tile = reinterpret_cast<T*>(smem_raw);
+    T* stab = tile + (size_t)g.Nl * 32;
+    __shared__ double red[LAT_WARPS];
+    const int nc16 = (g.ld + 15) / 16;
+    const int i = 1 + blockIdx.x / nc16, chunk = blockIdx.x % nc16;
+    const int H = g.Nl / 2;
+    load_tab(stab, tab, g.Nl);
+    load_pair(tile, buf, i, chunk, g);
+    __syncthreads();
+    dst_line<T, LGL>(tile, stab);
+    T acc_t = T(0);
+    for (int item = threadIdx.x; item < H * 16; item += LAT_THREADS) {
+        const int ky = 1 + item / 16, m = item % 16;
+        const T* q = blk + ((size_t)(i - 1) * H + (ky - 1)) * 10;
+        T* pa = tile + ky * 32 + m;
+        T* pc = tile + (g.Nl - ky) * 32 + m;
+        const T a = pa[0], b = pa[16];
+        if (ky != H) {
+            const T c = pc[0], d = pc[16];
+            const T oa = q[0] * a + q[1] * b + q[2] * c + q[3] * d;
+            const T ob = q[1] * a + q[4] * b + q[5] * c + q[6] * d;
+            const T oc = q[2] * a + q[5] * b + q[7] * c + q[8] * d;
+            const T od = q[3] * a + q[6] * b + q[8] * c + q[9] * d;
+            pa[0] = oa;
+            pa[16] = ob;
+            pc[0] = oc;
+            pc[16] = od;
+            acc_t = fma(a, oa, fma(b, ob, fma(c, oc, fma(d, od, acc_t))));
+        } else {  // ky = Nl - ky: the pair in y collapses
+            const T oa = q[0] * a + q[1] * b;
+            const T ob = q[1] * a + q[4] * b;
+            pa[0] = oa;
+            pa[16] = ob;
+            acc_t = fma(a, oa, fma(b, ob, acc_t));
+        }
+    }
+    double acc = (double)acc_t;
+    __syncthreads();
+    dst_line<T, LGL>(tile, stab);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, h = lane >> 4;
+    const int m = chunk * 16 + (lane & 15), col = h ? g.Nl - i : i;
+    if (m < g.ld && !(h && 2 * i == g.Nl)) {
+        for (int p = 1 + warp; p < g.Nl; p += LAT_WARPS) buf[lat_row(1, col, p, g.Nl) * g.ld + m] = tile[p * 32 + lane];
+    }
+    if (rz) {
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) red[warp] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0;
+            for (int w = 0; w < LAT_WARPS; ++w) s += red[w];
+            rz[blockIdx.x] = s;
+        }
+    }
+}
+
 LatGeom geom(const sgfem_context* ctx) {
     LatGeom g;
     g.Nl = ctx->Nl;
@@ -471,6 +575,20 @@ PassXFn<T> pass_x_fn(int LGL) {
     return nullptr;
 }
 template <typename T>
+PassYFn<T> pass_yb_fn(int LGL) {
+    switch (LGL) {
+        case 1: return k_lat_pass_yb<T, 1>;
+        case 2: return k_lat_pass_yb<T, 2>;
+        case 3: return k_lat_pass_yb<T, 3>;
+        case 4: return k_lat_pass_yb<T, 4>;
+        case 5: return k_lat_pass_yb<T, 5>;
+        case 6: return k_lat_pass_yb<T, 6>;
+        case 7: return k_lat_pass_yb<T, 7>;
+        case 8: return k_lat_pass_yb<T, 8>;
+    }
+    return nullptr;
+}
+template <typename T>
 PassYFn<T> pass_y_fn(int LGL) {
     switch (LGL) {
         case 1: return k_lat_pass_y<T, 1>;
@@ -502,9 +620,9 @@ int launch_y(sgfem_context* ctx, void* buf, const T* tab, const T* scale, double
              const KrylovScalars* scal) {
     LatGeom g = geom(ctx);
     g.async = ((uintptr_t)buf % 16) == 0;
-    PassYFn<T> fn = pass_y_fn<T>(ctx->lat_log2 - 1);
+    PassYFn<T> fn = ctx->lat_block ? pass_yb_fn<T>(ctx->lat_log2 - 1) : pass_y_fn<T>(ctx->lat_log2 - 1);
     if (!fn) return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice size outside the compiled range");
-    const int grid = (g.Nl - 1) * g.nchunk;
+    const int grid = ctx->lat_block ? (g.Nl / 2) * (int)((g.ld + 15) / 16) : (g.Nl - 1) * g.nchunk;
     if (nblocks) *nblocks = grid;
     fn<<<grid, LAT_THREADS, lat_smem(ctx, sizeof(T)), ctx->stream>>>((T*)buf, tab, scale, g, rz, scal);
     SG_LAUNCHED(ctx);
@@ -520,7 +638,14 @@ int sg_lattice_configure(sgfem_context* ctx) {
     SG_TRY(set_smem(ctx, pass_y_fn<double>(LGL), lat_smem(ctx, 8)));
     SG_TRY(set_smem(ctx, pass_x_fn<float>(LGL), lat_smem(ctx, 4)));
     SG_TRY(set_smem(ctx, pass_y_fn<float>(LGL), lat_smem(ctx, 4)));
+    SG_TRY(set_smem(ctx, pass_yb_fn<double>(LGL), lat_smem(ctx, 8)));
+    SG_TRY(set_smem(ctx, pass_yb_fn<float>(LGL), lat_smem(ctx, 4)));
     return SGFEM_OK;
+}
+
+int sg_lat_max_blocks(const sgfem_context* ctx) {
+    if (!ctx->lattice) return 1;
+    return std::max((ctx->Nl - 1) * (int)((ctx->ld + 31) / 32), (ctx->Nl / 2) * (int)((ctx->ld + 15) / 16));
 }
 
 int sg_lat_pass_x(sgfem_context* ctx, int precision, const void* R, void* T, const KrylovScalars* scal) {
@@ -529,8 +654,173 @@ int sg_lat_pass_x(sgfem_context* ctx, int precision, const void* R, void* T, con
 }
 
 int sg_lat_pass_y(sgfem_context* ctx, int precision, void* T, double* rz, int* nblocks, const KrylovScalars* scal) {
-    if (precision == SGFEM_FP64) return launch_y<double>(ctx, T, ctx->d_lat_tab64, ctx->d_lat_scale64, rz, nblocks, scal);
-    return launch_y<float>(ctx, T, ctx->d_lat_tab32, ctx->d_lat_scale32, rz, nblocks, scal);
+    if (precision == SGFEM_FP64)
+        return launch_y<double>(ctx, T, ctx->d_lat_tab64, ctx->lat_block ? ctx->d_lat_blk64 : ctx->d_lat_scale64, rz,
+                                nblocks, scal);
+    return launch_y<float>(ctx, T, ctx->d_lat_tab32, ctx->lat_block ? ctx->d_lat_blk32 : ctx->d_lat_scale32, rz,
+                           nblocks, scal);
+}
+
+// Exact mean preconditioner for lattice operators.  Every interior row of class
+// c = (x % 2, y % 2) must carry the same stencil w_c(d), |d| <= 2, on the interior
+// points (P1 and P2 Lagrange elements on the uniform triangulation with a constant
+// mean coefficient); then the orthonormal 2-D sine transform S maps K_0 (interior
+// rows and columns) to 4x4 blocks on the frequencies {i, Nl-i} x {j, Nl-j}:
+//   B_ab = <phi_a, K_0 phi_b> = sum_c sum_d w_c(d) X_c,dx(a_x, b_x) Y_c,dy(a_y, b_y),
+//   X_c,dx(k, l) = sum_{x = c_x mod 2, 1 <= x, x + dx <= Nl - 1} s_k(x) s_l(x + dx),
+// s_k(x) = sqrt(2/Nl) sin(pi k x / Nl).  The table holds (2/Nl)^2 B^-1 (upper
+// triangle, frequency pairs that collapse for i or j = Nl/2 left out), so that
+// pass Y applies K_0^-1 = (2/Nl)^2 T B^-1 T with the unnormalised transforms T.
+// This is the reference's LU(K_0) solve (solvers_poisson_primal.jl:23-78) on
+// interior rows.  Anything else keeps the 5-point Laplacian scaled by the mean.
+int sg_lattice_blocks(sgfem_context* ctx, const std::vector<int64_t>& rowptr, const std::vector<int32_t>& col,
+                      const std::vector<double>& val64) {
+    ctx->lat_block = false;
+    const int Nl = ctx->Nl, np = Nl + 1, M1 = ctx->M1;
+    constexpr int R = 2;
+    const char* ev = getenv("SGFEM_LAT_BLOCK");
+    if (ev && atoi(ev) == 0) {
+        ctx->lat_log = "5-point Laplacian (SGFEM_LAT_BLOCK=0)";
+        return SGFEM_OK;
+    }
+    if (Nl < 8 || !ctx->lat_order || ctx->win_hx > R || ctx->win_hy > R) {
+        ctx->lat_log = "5-point Laplacian (lattice too small or couplings too long for the block form)";
+        return SGFEM_OK;
+    }
+    auto boundary = [&](int x, int y) { return x == 0 || y == 0 || x == Nl || y == Nl; };
+    for (int64_t r = 0; r < (int64_t)np * np; ++r)
+        if ((ctx->bmask_host[r] != 0) != boundary((int)(r % np), (int)(r / np))) {
+            ctx->lat_log = "5-point Laplacian (Dirichlet dofs are not the lattice boundary)";
+            return SGFEM_OK;
+        }
+    auto value = [&](int64_t r, int32_t c) -> double {
+        auto b = col.begin() + rowptr[r], e = col.begin() + rowptr[r + 1];
+        auto it = std::lower_bound(b, e, c);
+        return (it != e && *it == c) ? val64[(size_t)(it - col.begin()) * M1] : 0.0;
+    };
+    double w[2][2][2 * R + 1][2 * R + 1];
+    double wmax = 0.0;
+    for (int cy = 0; cy < 2; ++cy)
+        for (int cx = 0; cx < 2; ++cx) {
+            const int x0 = Nl / 2 + cx, y0 = Nl / 2 + cy;
+            for (int dy = -R; dy <= R; ++dy)
+                for (int dx = -R; dx <= R; ++dx) {
+                    const double v = value((int64_t)y0 * np + x0, (y0 + dy) * np + x0 + dx);
+                    w[cy][cx][dy + R][dx + R] = v;
+                    wmax = std::max(wmax, std::fabs(v));
+                }
+        }
+    const double tol = 1e-11 * wmax;
+    for (int y = 1; y < Nl; ++y)
+        for (int x = 1; x < Nl; ++x) {
+            const int64_t r = (int64_t)y * np + x;
+            const int cx = x & 1, cy = y & 1;
+            double seen = 0.0, want = 0.0;
+            for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+                const int jx = col[k] % np, jy = col[k] / np;
+                if (boundary(jx, jy)) continue;
+                const int dx = jx - x, dy = jy - y;
+                const double v = val64[(size_t)k * M1];
+                if (std::abs(dx) > R || std::abs(dy) > R || std::fabs(v - w[cy][cx][dy + R][dx + R]) > tol) {
+                    ctx->lat_log = "5-point Laplacian (K_0 is not translation invariant on the lattice)";
+                    return SGFEM_OK;
+                }
+                seen += std::fabs(v);
+            }
+            for (int dy = -R; dy <= R; ++dy)
+                for (int dx = -R; dx <= R; ++dx)
+                    if (!boundary(x + dx, y + dy) && x + dx >= 0 && y + dy >= 0 && x + dx <= Nl && y + dy <= Nl)
+                        want += std::fabs(w[cy][cx][dy + R][dx + R]);
+            if (std::fabs(seen - want) > 1e-10 * want) {
+                ctx->lat_log = "5-point Laplacian (K_0 is not translation invariant on the lattice)";
+                return SGFEM_OK;
+            }
+        }
+    // one-dimensional sums X_c,d(a, b) for the frequency pair (i, Nl - i), i = 1..H
+    const int H = Nl / 2;
+    const double pi = 3.14159265358979323846;
+    std::vector<double> sn(2 * Nl);
+    for (int m = 0; m < 2 * Nl; ++m) sn[m] = std::sqrt(2.0 / Nl) * std::sin(pi * m / Nl);
+    auto sv = [&](int k, int x) { return sn[(size_t)((int64_t)k * x % (2 * Nl))]; };
+    std::vector<double> A((size_t)(H + 1) * 2 * (2 * R + 1) * 4, 0.0);
+    auto aidx = [&](int i, int c, int d, int a, int b) { return ((((size_t)i * 2 + c) * (2 * R + 1) + d + R) * 2 + a) * 2 + b; };
+    for (int i = 1; i <= H; ++i) {
+        const int f[2] = {i, Nl - i};
+        for (int c = 0; c < 2; ++c)
+            for (int d = -R; d <= R; ++d)
+                for (int a = 0; a < 2; ++a)
+                    for (int b = 0; b < 2; ++b) {
+                        double sum = 0.0;
+                        for (int x = c; x < Nl; x += 2)
+                            if (x >= 1 && x + d >= 1 && x + d <= Nl - 1) sum += sv(f[a], x) * sv(f[b], x + d);
+                        A[aidx(i, c, d, a, b)] = sum;
+                    }
+    }
+    const double norm = 4.0 / ((double)Nl * (double)Nl);
+    std::vector<double> blk((size_t)H * H * 10);
+    for (int i = 1; i <= H; ++i)
+        for (int j = 1; j <= H; ++j) {
+            double B[4][4] = {};
+            for (int cy = 0; cy < 2; ++cy)
+                for (int cx = 0; cx < 2; ++cx)
+                    for (int dy = -R; dy <= R; ++dy)
+                        for (int dx = -R; dx <= R; ++dx) {
+                            const double wv = w[cy][cx][dy + R][dx + R];
+                            if (wv == 0.0) continue;
+                            for (int a = 0; a < 4; ++a)
+                                for (int b = 0; b < 4; ++b)
+                                    B[a][b] += wv * A[aidx(i, cx, dx, a & 1, b & 1)] * A[aidx(j, cy, dy, a >> 1, b >> 1)];
+                        }
+            // distinct frequencies: index a = 2 ay + ax, ax < nx, ay < ny
+            const int nx = (i == H) ? 1 : 2, ny = (j == H) ? 1 : 2;
+            int id[4], k = 0;
+            for (int ay = 0; ay < ny; ++ay)
+                for (int ax = 0; ax < nx; ++ax) id[k++] = 2 * ay + ax;
+            // Gauss-Jordan inverse of the k x k block (symmetric positive definite)
+            double Mx[4][8] = {};
+            for (int r = 0; r < k; ++r) {
+                for (int c = 0; c < k; ++c) Mx[r][c] = B[id[r]][id[c]];
+                Mx[r][k + r] = 1.0;
+            }
+            for (int c = 0; c < k; ++c) {
+                int pr = c;
+                for (int r = c + 1; r < k; ++r)
+                    if (std::fabs(Mx[r][c]) > std::fabs(Mx[pr][c])) pr = r;
+                if (!(std::fabs(Mx[pr][c]) > 1e-14 * wmax)) {
+                    ctx->lat_log = "5-point Laplacian (singular sine-transform block)";
+                    return SGFEM_OK;
+                }
+                for (int t = 0; t < 2 * k; ++t) std::swap(Mx[c][t], Mx[pr][t]);
+                const double piv = Mx[c][c];
+                for (int t = 0; t < 2 * k; ++t) Mx[c][t] /= piv;
+                for (int r = 0; r < k; ++r)
+                    if (r != c) {
+                        const double f = Mx[r][c];
+                        for (int t = 0; t < 2 * k; ++t) Mx[r][t] -= f * Mx[c][t];
+                    }
+            }
+            double Bi[4][4] = {};
+            for (int r = 0; r < k; ++r)
+                for (int c = 0; c < k; ++c) Bi[id[r]][id[c]] = norm * 0.5 * (Mx[r][k + c] + Mx[c][k + r]);
+            for (int r = 0; r < 4; ++r)
+                if (Bi[r][r] < 0.0) {
+                    ctx->lat_log = "5-point Laplacian (sine-transform block not positive definite)";
+                    return SGFEM_OK;
+                }
+            double* o = &blk[((size_t)(i - 1) * H + (j - 1)) * 10];
+            o[0] = Bi[0][0]; o[1] = Bi[0][1]; o[2] = Bi[0][2]; o[3] = Bi[0][3];
+            o[4] = Bi[1][1]; o[5] = Bi[1][2]; o[6] = Bi[1][3];
+            o[7] = Bi[2][2]; o[8] = Bi[2][3];
+            o[9] = Bi[3][3];
+        }
+    std::vector<float> blk32(blk.begin(), blk.end());
+    SG_CUDA(ctx, cudaMalloc(&ctx->d_lat_blk64, blk.size() * sizeof(double)));
+    SG_CUDA(ctx, cudaMemcpy(ctx->d_lat_blk64, blk.data(), blk.size() * sizeof(double), cudaMemcpyHostToDevice));
+    SG_CUDA(ctx, cudaMalloc(&ctx->d_lat_blk32, blk32.size() * sizeof(float)));
+    SG_CUDA(ctx, cudaMemcpy(ctx->d_lat_blk32, blk32.data(), blk32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    ctx->lat_block = true;
+    ctx->lat_log = "exact K_0^-1: 4x4 blocks of the 2-D sine transform";
+    return SGFEM_OK;
 }
 
 int sg_lat_pass_xinv(sgfem_context* ctx, int precision, const void* T, void* out, int mode, const KrylovScalars* scal) {

@@ -157,6 +157,10 @@ struct sgfem_context {
     float* d_lat_tab32 = nullptr;
     double* d_lat_scale64 = nullptr;  // per (kx, ky) scale, (Nl-1)^2
     float* d_lat_scale32 = nullptr;
+    bool lat_block = false;         // exact K_0^-1 by 4x4 blocks of the sine transform (pass Y)
+    double* d_lat_blk64 = nullptr;  // per (kx, ky) in [1, Nl/2]^2: 10 values of a symmetric 4x4 block
+    float* d_lat_blk32 = nullptr;
+    std::string lat_log;            // which mean-based preconditioner is in use, and why
 
     // workspaces (lazily sized)
     DeviceBuf w_stage;         // host-layout staging (n*P doubles)
@@ -227,6 +231,12 @@ int sg_launch_from_device(sgfem_context* ctx, const void* X, double* stage, int 
 
 // ------------------------------------------------------------------ preconditioners (lattice.cu)
 int sg_lattice_setup(sgfem_context* ctx);
+// largest block count of a lattice pass (size of the reduction partials)
+int sg_lat_max_blocks(const sgfem_context* ctx);
+// exact mean preconditioner: K_0 restricted to interior lattice points is translation invariant
+// per parity class (x % 2, y % 2); rowptr/col in device numbering, val64 (nnz x M1, K_0 at m = 0)
+int sg_lattice_blocks(sgfem_context* ctx, const std::vector<int64_t>& rowptr, const std::vector<int32_t>& col,
+                      const std::vector<double>& val64);
 // pass 1: T = DST_x(R) on interior rows
 int sg_lat_pass_x(sgfem_context* ctx, int precision, const void* R, void* T,
                   const KrylovScalars* skip_if_done);

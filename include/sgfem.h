@@ -98,6 +98,11 @@ SGFEM_API int sgfem_set_dof_coordinates(sgfem_context* ctx, int64_t n, const dou
 SGFEM_API int sgfem_finalize(sgfem_context* ctx);
 /* 1 if the lattice preconditioner is available after finalize */
 SGFEM_API int sgfem_has_lattice(const sgfem_context* ctx);
+/* which mean-based lattice preconditioner a finalized context applies: the exact
+   K_0^-1 (4x4 blocks of the 2-D sine transform; K_0 translation invariant on the
+   lattice, as for P1/P2 with a constant mean) or the 5-point Laplacian scaled by
+   the mean diagonal, with the reason */
+SGFEM_API const char* sgfem_lattice_log(const sgfem_context* ctx);
 
 /*
  * mul!(Ax, S::MySystemPrimal, x), solvers_poisson_primal.jl:86-124:

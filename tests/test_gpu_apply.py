@@ -84,28 +84,10 @@ def test_preconditioner(case):
     for mu in range(p.P):
         b[mu * p.n + p.bdofs] = 0.0
     inner = np.setdiff1d(np.arange(p.n), p.bdofs)
-    if p.V.order == 1:
-        ref = osg.MeanPreconditioner(p.K0, p.bdofs, p.P).ldiv(b)
-    else:
-        # lattice Laplacian on the P2 dofs (vertices + edge midpoints)
-        Nl = int(round(np.sqrt(p.n))) - 1
-        ij = np.rint(p.V.dof_coords * Nl).astype(int)
-        pos = {(a, c): k for k, (a, c) in enumerate(ij)}
-        rows, cols, vals = [], [], []
-        for k, (a, c) in enumerate(ij):
-            rows.append(k); cols.append(k); vals.append(4.0)
-            for da, dc in ((1, 0), (-1, 0), (0, 1), (0, -1)):
-                j = pos.get((a + da, c + dc))
-                if j is not None:
-                    rows.append(k); cols.append(j); vals.append(-1.0)
-        L = sp.csr_matrix((vals, (rows, cols)), shape=(p.n, p.n))
-        d = p.K0.diagonal()[inner]
-        a0 = d.sum() / (4 * len(inner))
-        lu = spla.splu((a0 * L[inner][:, inner]).tocsc())
-        ref = np.zeros_like(b)
-        for mu in range(p.P):
-            ref[mu * p.n + inner] = lu.solve(b[mu * p.n + inner])
+    # the reference's preconditioner: LU(K_0) on interior rows, every mode
+    ref = osg.MeanPreconditioner(p.K0, p.bdofs, p.P).ldiv(b)
     if op.has_lattice:
+        assert "exact" in op.ctx.lattice_log, op.ctx.lattice_log
         y = op.ldiv(b, pkg.PREC_LATTICE, pkg.FP64)
         mask = osg.interior_mask(p.n, p.P, p.bdofs)
         assert rel(y[mask], ref[mask]) <= 1e-10
@@ -116,6 +98,66 @@ def test_preconditioner(case):
     dj = np.zeros(p.n)
     dj[inner] = 1.0 / p.K0.diagonal()[inner]
     assert rel(yj, b * np.tile(dj, p.P)) <= 1e-14
+
+
+def lattice_laplacian_solve(p, b):
+    """(a0 L)^-1 on interior rows, L the 5-point Laplacian of the dof lattice, a0 the
+    mean interior diagonal of K_0 over 4."""
+    Nl = int(round(np.sqrt(p.n))) - 1
+    ij = np.rint(p.V.dof_coords * Nl).astype(int)
+    pos = {(a, c): k for k, (a, c) in enumerate(ij)}
+    rows, cols, vals = [], [], []
+    for k, (a, c) in enumerate(ij):
+        rows.append(k); cols.append(k); vals.append(4.0)
+        for da, dc in ((1, 0), (-1, 0), (0, 1), (0, -1)):
+            j = pos.get((a + da, c + dc))
+            if j is not None:
+                rows.append(k); cols.append(j); vals.append(-1.0)
+    L = sp.csr_matrix((vals, (rows, cols)), shape=(p.n, p.n))
+    inner = np.setdiff1d(np.arange(p.n), p.bdofs)
+    a0 = p.K0.diagonal()[inner].sum() / (4 * len(inner))
+    lu = spla.splu((a0 * L[inner][:, inner]).tocsc())
+    ref = np.zeros_like(b)
+    for mu in range(p.P):
+        ref[mu * p.n + inner] = lu.solve(b[mu * p.n + inner])
+    return ref
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_laplacian_lattice_preconditioner(built_pkg, monkeypatch, order):
+    """With the block form switched off (or K_0 not translation invariant) the
+    lattice preconditioner is (a0 L)^-1 with the 5-point Laplacian."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    p = build(16, order, 3, pkg.total_degree_multiindices(3, 2))
+    monkeypatch.setenv("SGFEM_LAT_BLOCK", "0")
+    op = pkg.SGOperator(p.V, p.TB, p.Kall, device=0)
+    assert op.has_lattice and "Laplacian" in op.ctx.lattice_log
+    b = np.random.default_rng(5).standard_normal(p.n * p.P)
+    for mu in range(p.P):
+        b[mu * p.n + p.bdofs] = 0.0
+    ref = lattice_laplacian_solve(p, b)
+    mask = osg.interior_mask(p.n, p.P, p.bdofs)
+    for prec, tol in ((pkg.FP64, 1e-10), (pkg.FP32, 1e-4)):
+        y = op.ldiv(b, pkg.PREC_LATTICE, prec)
+        assert rel(y[mask], ref[mask]) <= tol
+    op.close()
+
+
+def test_block_preconditioner_needs_translation_invariance(built_pkg):
+    """A mean coefficient that varies in space makes K_0 non-invariant: the
+    Laplacian form is used and the log says why."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    p = build(16, 1, 2, pkg.total_degree_multiindices(2, 1))
+    K0 = p.Kall[0].tolil()
+    n1 = int(round(np.sqrt(p.n)))
+    r = (n1 // 2) * n1 + n1 // 2  # one interior row scaled: no longer a repeating stencil
+    K0[r, :] = K0[r, :] * 1.5
+    Kall = [K0.tocsc()] + list(p.Kall[1:])
+    op = pkg.SGOperator(p.V, p.TB, Kall, device=0)
+    assert op.has_lattice and "not translation invariant" in op.ctx.lattice_log, op.ctx.lattice_log
+    op.close()
 
 
 def test_lattice_detection(case):

@@ -112,3 +112,57 @@ def test_adjoint_oracle_matches_finite_differences():
         fd = (Q.value(theta + h * dt, alpha + h * da) - Q.value(theta - h * dt, alpha - h * da)) / (2 * h)
         an = gt @ dt + ga @ da
         assert abs(fd - an) <= 1e-6 * abs(an)
+
+
+@pytest.mark.parametrize("order,N", [(1, 8), (2, 4), (2, 8)])
+def test_sine_transform_blocks_of_lattice_stiffness(order, N):
+    """The exact lattice preconditioner rests on this: the orthonormal 2-D sine
+    transform S maps the interior stiffness K_0 of P1/P2 on the uniform
+    triangulation to 4x4 blocks on the frequencies {i, Nl-i} x {j, Nl-j}, and the
+    blocks equal the separable sums over the stencil of each parity class,
+      B_ab = sum_c sum_d w_c(d) X_c,dx(a_x, b_x) X_c,dy(a_y, b_y)."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    from tests.problems import build
+    p = build(N, order, 1, [[0]])
+    K = p.K0.toarray()
+    Nl = N * order
+    xy = np.rint(p.V.dof_coords * Nl).astype(int)
+    idx = {(x, y): i for i, (x, y) in enumerate(xy)}
+    interior = [(x, y) for y in range(1, Nl) for x in range(1, Nl)]
+    I = [idx[q] for q in interior]
+    j = np.arange(1, Nl)
+    S1 = np.sqrt(2.0 / Nl) * np.sin(np.pi * np.outer(j, j) / Nl)
+    T = np.kron(S1, S1) @ K[np.ix_(I, I)] @ np.kron(S1, S1)
+    pos = lambda kx, ky: (ky - 1) * (Nl - 1) + kx - 1
+    R = 2
+    w = np.zeros((2, 2, 2 * R + 1, 2 * R + 1))
+    for cy in range(2):
+        for cx in range(2):
+            x0, y0 = Nl // 2 + cx, Nl // 2 + cy
+            for dy in range(-R, R + 1):
+                for dx in range(-R, R + 1):
+                    w[cy, cx, dy + R, dx + R] = K[idx[(x0, y0)], idx[(x0 + dx, y0 + dy)]]
+    s = lambda k, x: np.sqrt(2.0 / Nl) * np.sin(np.pi * k * x / Nl)
+
+    def X(i, c, d, a, b):
+        f = (i, Nl - i)
+        return sum(s(f[a], x) * s(f[b], x + d) for x in range(c, Nl, 2) if 1 <= x and 1 <= x + d <= Nl - 1)
+
+    H = Nl // 2
+    for kx in range(1, Nl):
+        for ky in range(1, Nl):
+            row = T[pos(kx, ky)]
+            alias = {pos(a, b) for a in (kx, Nl - kx) for b in (ky, Nl - ky)}
+            assert np.all(np.abs(np.delete(row, sorted(alias))) <= 1e-12)
+    for i in range(1, H + 1):
+        for jy in range(1, H + 1):
+            fx, fy = (i, Nl - i), (jy, Nl - jy)
+            for a in range(4):
+                for b in range(4):
+                    if (i == H and (a % 2 or b % 2)) or (jy == H and (a // 2 or b // 2)):
+                        continue
+                    B = sum(w[cy, cx, dy + R, dx + R] * X(i, cx, dx, a % 2, b % 2) * X(jy, cy, dy, a // 2, b // 2)
+                            for cy in range(2) for cx in range(2) for dy in range(-R, R + 1) for dx in range(-R, R + 1)
+                            if w[cy, cx, dy + R, dx + R] != 0.0)
+                    assert abs(B - T[pos(fx[a % 2], fy[a // 2]), pos(fx[b % 2], fy[b // 2])]) <= 1e-12
