@@ -329,7 +329,8 @@ def run_ours(args, rank, world, local, pg):
 
 def run_profile(args):
     """Small, bounded launches for ncu: `apply32` / `apply64` launch the apply 1+3
-    times; `solve` runs one mixed solve."""
+    times; `precond32` / `precond64` apply the lattice preconditioner 1+2 times
+    (three pass kernels each); `solve` runs one mixed solve."""
     import __graft_entry__ as ge
     pkg = ge.load_package()
     V, TB, Ks, b0 = setup_workload(pkg, N=args.mesh)
@@ -338,6 +339,10 @@ def run_profile(args):
         prec = pkg.FP32 if args.profile == "apply32" else pkg.FP64
         ms = op.ctx.time_apply(prec, 3)
         print(json.dumps({"profile": args.profile, "ms_per_apply": ms}))
+    elif args.profile in ("precond32", "precond64"):
+        prec = pkg.FP32 if args.profile == "precond32" else pkg.FP64
+        ms = op.ctx.time_precondition(prec, 2)
+        print(json.dumps({"profile": args.profile, "ms_per_application": ms, "form": op.ctx.lattice_log}))
     else:
         x = np.zeros(V.ndofs * TB.nmodes)
         st = op.solve_primal(b0, x, rtol=1e-8, precision=pkg.MIXED)
@@ -606,7 +611,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile", choices=["apply32", "apply64", "solve"], default=None,
+    ap.add_argument("--profile", choices=["apply32", "apply64", "precond32", "precond64", "solve"], default=None,
                     help="profiling target for ncu: set up the workload, run the kernel(s) a few times, exit")
     ap.add_argument("--mesh", type=int, default=256, help="mesh size for --profile / --workload adjoint")
     ap.add_argument("--workload", choices=["config2", "config1", "lognormal", "sampling", "adjoint", "batch"],

@@ -97,16 +97,20 @@ __device__ __forceinline__ void block_partial(double acc, double* partials) {
     }
 }
 
-// x += alpha p ; r -= alpha q ; partial ||r||^2
-template <typename T>
-__global__ void __launch_bounds__(VT) k_update(T* __restrict__ x, const T* __restrict__ p, T* __restrict__ r,
+// x += alpha p ; r -= alpha q ; partial ||r||^2.  TX = double with T = float: the
+// solution of an FP32 PCG accumulates in FP64 (stored in FP32 its rounding errors
+// are rough vectors that A amplifies by its condition number, ~1/h^2, and the true
+// residual then stalls near kappa * 2^-24 whatever the recurrence says)
+template <typename T, typename TX = T>
+__global__ void __launch_bounds__(VT) k_update(TX* __restrict__ x, const T* __restrict__ p, T* __restrict__ r,
                                                const T* __restrict__ q, size_t total, const KrylovScalars* __restrict__ s,
                                                double* __restrict__ partials) {
     if (s->done) return;
     const T alpha = (T)s->alpha;
+    const TX alpha_x = (TX)s->alpha;
     T acc_t = T(0);  // per-thread partial in the working precision (narrow FP64 pipe)
     for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT) {
-        x[i] = fma(alpha, p[i], x[i]);
+        x[i] = fma(alpha_x, (TX)p[i], x[i]);
         const T rn = fma(-alpha, q[i], r[i]);
         r[i] = rn;
         acc_t = fma(rn, rn, acc_t);
@@ -138,20 +142,36 @@ __global__ void __launch_bounds__(VT) k_dot(const T* __restrict__ a, const T* __
 
 // r32 = (float) r64 ; d32 = 0 ; partial ||r32||^2
 __global__ void __launch_bounds__(VT) k_demote(const double* __restrict__ r64, float* __restrict__ r32,
-                                               float* __restrict__ d32, size_t total, double* __restrict__ partials) {
+                                               double* __restrict__ d64, size_t total, double* __restrict__ partials) {
     float acc_t = 0.0f;
     for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT) {
         const float v = (float)r64[i];
         r32[i] = v;
-        d32[i] = 0.0f;
+        d64[i] = 0.0;
         acc_t = fmaf(v, v, acc_t);
     }
     block_partial((double)acc_t, partials);
 }
 
-// x64 += (double) d32
-__global__ void __launch_bounds__(VT) k_promote_add(double* __restrict__ x, const float* __restrict__ d, size_t total) {
-    for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT) x[i] += (double)d[i];
+// partial ||r - q||^2 with r in FP64 and q in FP32 (refinement diagnostics)
+__global__ void __launch_bounds__(VT) k_diffnorm(const double* __restrict__ r, const float* __restrict__ q, size_t total,
+                                                 double* __restrict__ partials) {
+    double acc = 0.0;
+    for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT) {
+        const double d = r[i] - (double)q[i];
+        acc = fma(d, d, acc);
+    }
+    block_partial(acc, partials);
+}
+
+// x64 += d64
+__global__ void __launch_bounds__(VT) k_add64(double* __restrict__ x, const double* __restrict__ d, size_t total) {
+    for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT) x[i] += d[i];
+}
+
+// d32 = (float) d64 (refinement diagnostics)
+__global__ void __launch_bounds__(VT) k_to_f32(const double* __restrict__ d, float* __restrict__ o, size_t total) {
+    for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT) o[i] = (float)d[i];
 }
 
 // b = (x0 or 0) + e_1 (x) b0, Dirichlet rows zeroed.  b0 in caller order.
@@ -238,15 +258,15 @@ struct Solver {
         return SGFEM_OK;
     }
 
-    template <typename T>
-    int iteration(int precision, T* x, T* r, T* p, T* q, T* tmp, int maxit) {
+    template <typename T, typename TX = T>
+    int iteration(int precision, TX* x, T* r, T* p, T* q, T* tmp, int maxit) {
         int nb = 0;
         FinArgs fa{0.0, maxit};
         SG_TRY(sg_launch_apply(ctx, precision, p, q, partials, &nb, s));
         SG_TRY(fin(nb, FIN_ALPHA, fa));
         const size_t total = (size_t)ctx->n * ctx->ld;
         const int g = vgrid(ctx);
-        k_update<T><<<g, VT, 0, ctx->stream>>>(x, p, r, q, total, s, partials);
+        k_update<T, TX><<<g, VT, 0, ctx->stream>>>(x, p, r, q, total, s, partials);
         SG_LAUNCHED(ctx);
         SG_TRY(fin(g, FIN_RR, fa));
         SG_TRY(precond_block<T>(precision, r, p, tmp, maxit));
@@ -255,8 +275,8 @@ struct Solver {
 
     // PCG on A x = b given r = b - A x on entry, stopping when ||r||^2 <= s->tol2
     // (set by the caller).  Returns the status; iterations in *iters.
-    template <typename T>
-    int pcg(int precision, T* x, T* r, T* p, T* q, T* tmp, int maxit, int check_every, int* iters) {
+    template <typename T, typename TX = T>
+    int pcg(int precision, TX* x, T* r, T* p, T* q, T* tmp, int maxit, int check_every, int* iters) {
         const size_t vb = (size_t)ctx->n * ctx->ld * sizeof(T);
         SG_CUDA(ctx, cudaMemsetAsync(p, 0, vb, ctx->stream));
         // initial residual norm and flags
@@ -283,7 +303,7 @@ struct Solver {
         SG_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
         int st = SGFEM_OK;
         const long long before = ctx->launches;
-        for (int k = 0; k < check_every && st == SGFEM_OK; ++k) st = iteration<T>(precision, x, r, p, q, tmp, maxit);
+        for (int k = 0; k < check_every && st == SGFEM_OK; ++k) st = iteration<T, TX>(precision, x, r, p, q, tmp, maxit);
         const long long per_graph = ctx->launches - before;  // kernel nodes per replay
         ctx->launches = before;
         cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
@@ -499,7 +519,7 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
     int remaining = o->maxit;
     // SGFEM_TRACE=1: one line per refinement step on stderr (the reference's @info progress)
     const char* etr = getenv("SGFEM_TRACE");
-    const bool trace = etr && atoi(etr) != 0;
+    const int trace = etr ? atoi(etr) : 0;  // 2: also the recurrence and FP32-operator residuals
     // smallest reduction asked of one later refinement step (SGFEM_MIXED_FLOOR)
     const char* efl = getenv("SGFEM_MIXED_FLOOR");
     const double floor1 = efl ? std::max(1e-10, std::min(1e-2, atof(efl))) : 1e-6;
@@ -528,6 +548,7 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
             }
         } else {
             float* d32 = (float*)ctx->w_vec[5].p;
+            double* d64 = q;  // the FP32 PCG's solution, accumulated in FP64
             float* r32 = (float*)ctx->w_vec[6].p;
             float* p32 = (float*)ctx->w_vec[7].p;
             float* q32 = (float*)ctx->w_vec[8].p;
@@ -537,13 +558,12 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
                 if (!std::isfinite(rr)) { status = SGFEM_ERR_NONFINITE; break; }
                 if (rr <= tol2e * bb) break;
                 if (remaining <= 0) { status = SGFEM_ERR_MAXIT; break; }
-                k_demote<<<g, VT, 0, ctx->stream>>>(r, r32, d32, total, partials);
+                k_demote<<<g, VT, 0, ctx->stream>>>(r, r32, d64, total, partials);
                 SG_LAUNCHED(ctx);
-                // inner target (squared reduction of ||r||).  First step: inner_rtol; the FP32
-                // operator's error on the smooth first correction (rounding amplified by the
-                // O(1/h) cancellation of K d) bounds what this step achieves in FP64 anyway.
-                // Later steps correct rough residuals, where FP32 PCG is accurate: aim to end
-                // the solve with a margin of 3, asking at most a 1e-6 reduction per step.
+                // inner target (squared reduction of ||r||).  First step: inner_rtol.  Later
+                // steps aim to end the solve with a margin of 3, asking at most a 1e-6
+                // reduction of one FP32 PCG (about what its recurrence tracks in FP64 with
+                // the solution accumulated in FP64; SGFEM_TRACE=2 prints both per step).
                 const double finish = 0.1 * tol2e * bb / rr;
                 double want;
                 if (o->precision == SGFEM_FP32) want = std::max(in2, 0.25 * tol2e * bb / rr);
@@ -551,17 +571,36 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
                 else want = std::max(finish, floor2);
                 SG_TRY(S.fin(g, FIN_TOL, FinArgs{want, 0}, nullptr));
                 int it = 0;
-                int s2 = S.pcg<float>(SGFEM_FP32, d32, r32, p32, q32, tmp32, remaining, check_every, &it);
+                int s2 = S.pcg<float, double>(SGFEM_FP32, d64, r32, p32, q32, tmp32, remaining, check_every, &it);
                 st->iterations += it;
                 st->outer_iterations += 1;
                 remaining -= it;
                 if (s2 == SGFEM_ERR_BREAKDOWN || s2 == SGFEM_ERR_NONFINITE) { status = s2; break; }
-                k_promote_add<<<g, VT, 0, ctx->stream>>>(x64, d32, total);
+                double rec = 0.0, tr32 = 0.0;
+                if (trace >= 2) {  // recurrence ||r32|| and FP32-operator residual ||r - A32 d|| (one extra apply)
+                    k_dot<float><<<g, VT, 0, ctx->stream>>>(r32, r32, total, partials);
+                    SG_LAUNCHED(ctx);
+                    SG_TRY(S.fin(g, FIN_SUM, FinArgs{0.0, 0}, d_sum));
+                    SG_CUDA(ctx, cudaMemcpyAsync(&rec, d_sum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+                    k_to_f32<<<g, VT, 0, ctx->stream>>>(d64, d32, total);
+                    SG_LAUNCHED(ctx);
+                    SG_TRY(sg_launch_apply(ctx, SGFEM_FP32, d32, q32, nullptr, nullptr, nullptr));
+                    k_diffnorm<<<g, VT, 0, ctx->stream>>>(r, q32, total, partials);
+                    SG_LAUNCHED(ctx);
+                    SG_TRY(S.fin(g, FIN_SUM, FinArgs{0.0, 0}, d_sum));
+                    SG_CUDA(ctx, cudaMemcpyAsync(&tr32, d_sum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+                    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+                }
+                const double rr_in = rr;
+                k_add64<<<g, VT, 0, ctx->stream>>>(x64, d64, total);
                 SG_LAUNCHED(ctx);
                 SG_TRY(true_residual(&rr));
                 if (trace)
                     fprintf(stderr, "sgfem: refinement step %d: inner target %.3g, %d FP32 iterations, relres %.3e\n",
                             outer + 1, std::sqrt(want), it, std::sqrt(rr / bb));
+                if (trace >= 2)
+                    fprintf(stderr, "sgfem:   reduction: recurrence %.3e, FP32 operator %.3e, FP64 %.3e\n",
+                            std::sqrt(rec / rr_in), std::sqrt(tr32 / rr_in), std::sqrt(rr / rr_in));
                 if (o->precision == SGFEM_FP32) break;  // plain FP32 PCG: no refinement
             }
         }
