@@ -93,6 +93,7 @@ extern "C" int sgfem_destroy(sgfem_context* ctx) {
     for (void* p : ptrs) free_dev(p);
     for (int i = 0; i < SG_NBUF; ++i) free_dev(ctx->w_vec[i].p);
     free_dev(ctx->w_basis.p);
+    free_dev(ctx->w_zbasis.p);
     free_dev(ctx->w_gsmall.p);
     if (ctx->h_scal) cudaFreeHost(ctx->h_scal);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);

@@ -85,6 +85,20 @@ __global__ void __launch_bounds__(GT) k_lincomb(T* __restrict__ w, const T* __re
     }
 }
 
+// x64 += sum_i c_i Z_i (FP64 accumulation of FP32 vectors)
+template <typename T>
+__global__ void __launch_bounds__(GT) k_lincomb_add64(double* __restrict__ x, const T* __restrict__ Z, size_t total,
+                                                      int k, const double* __restrict__ c) {
+    __shared__ double cs[KMAX];
+    for (int i = threadIdx.x; i < k; i += GT) cs[i] = c[i];
+    __syncthreads();
+    for (size_t t = (size_t)blockIdx.x * GT + threadIdx.x; t < total; t += (size_t)gridDim.x * GT) {
+        double a = x[t];
+        for (int i = 0; i < k; ++i) a = fma(cs[i], (double)Z[(size_t)i * total + t], a);
+        x[t] = a;
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(GT) k_scale(T* __restrict__ dst, const T* __restrict__ src, size_t total, double s) {
     for (size_t t = (size_t)blockIdx.x * GT + threadIdx.x; t < total; t += (size_t)gridDim.x * GT)
@@ -169,9 +183,14 @@ struct Gm {
     // Restarted right-preconditioned GMRES on A x = b in precision T.  x holds the
     // start (x_zero: zero); stops when ||b - A x|| <= tol_abs (true residual in
     // precision T, FP64 sums) or after maxit Arnoldi steps.  z's Dirichlet rows zero.
+    // Flexible form (Z != nullptr, one cycle from a zero start): the preconditioned
+    // basis vectors z_k are kept and the cycle ends with x64 += Z y in FP64, so the
+    // correction is exactly the combination the Arnoldi relation A Z = V H holds for
+    // (x = B (V y) recomputed in FP32 differs from Z y by rough rounding errors that
+    // A amplifies by its condition number); *res is the GMRES residual estimate.
     template <typename T>
     int run(int precision, T* x, const T* b, T* V, T* z, T* w, T* tmp, int restart, double tol_abs, int maxit,
-            bool x_zero, int* iters, double* res) {
+            bool x_zero, int* iters, double* res, T* Z = nullptr, double* x64 = nullptr) {
         T* v0 = V;
         if (x_zero) {
             SG_CUDA(ctx, cudaMemcpyAsync(v0, b, total * sizeof(T), cudaMemcpyDeviceToDevice, ctx->stream));
@@ -199,8 +218,9 @@ struct Gm {
             for (int k = 0; k < m; ++k) {
                 T* vk = V + (size_t)k * total;
                 T* vn = V + (size_t)(k + 1) * total;
-                SG_TRY(precond<T>(precision, vk, z, tmp));
-                SG_TRY(apply<T>(precision, z, w));
+                T* zk = Z ? Z + (size_t)k * total : z;
+                SG_TRY(precond<T>(precision, vk, zk, tmp));
+                SG_TRY(apply<T>(precision, zk, w));
                 // CGS2
                 SG_TRY(dots<T>(V, k + 1, w, h.data()));
                 for (int i = 0; i <= k; ++i) h[i] = -h[i];
@@ -245,6 +265,13 @@ struct Gm {
                 y[i] = s / Hat(i, i);
             }
             SG_CUDA(ctx, cudaMemcpyAsync(d_h, y.data(), (size_t)kk * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+            if (Z) {
+                k_lincomb_add64<T><<<grid, GT, 0, ctx->stream>>>(x64, Z, total, kk, d_h);
+                SG_LAUNCHED(ctx);
+                *res = std::fabs(g[kk]);
+                *iters = it;
+                return SGFEM_OK;
+            }
             k_lincomb<T><<<grid, GT, 0, ctx->stream>>>(w, V, total, kk, d_h, 0.0);
             SG_LAUNCHED(ctx);
             SG_TRY(precond<T>(precision, w, z, tmp));
@@ -295,6 +322,7 @@ extern "C" int sgfem_solve_gmres(sgfem_context* ctx, const double* b0, double* x
         SG_TRY(sg_jit_ensure(ctx));
     }
     SG_TRY(sg_ensure(ctx, ctx->w_basis, (size_t)(restart + 1) * total * esz));
+    if (low) SG_TRY(sg_ensure(ctx, ctx->w_zbasis, (size_t)restart * total * sizeof(float)));
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)((total + GT * 4 - 1) / (GT * 4)),
                                                                  (int64_t)ctx->num_sms * 8));
     const int nbx = std::min(grid, ctx->num_sms * 4);
@@ -361,21 +389,29 @@ extern "C" int sgfem_solve_gmres(sgfem_context* ctx, const double* b0, double* x
             if (o.precision == SGFEM_FP32 && outer > 0) break;  // plain FP32 solve: one pass
             k_demote<<<grid, GT, 0, ctx->stream>>>(b32, r64, total);
             SG_LAUNCHED(ctx);
-            SG_CUDA(ctx, cudaMemsetAsync(d32, 0, n32, ctx->stream));
-            // one FP32 restart cycle per refinement step (FP32 GMRES stagnates near its
-            // attainable accuracy; the FP64 residual drives the outer loop)
-            // FP32 GMRES reliably reaches about 1e-4 of its right-hand side on these operators
-            const double inner = o.precision == SGFEM_FP32 ? o.rtol : std::max(o.inner_rtol, 1e-4);
-            const int inner_max = o.precision == SGFEM_FP32 ? o.maxit - total_it : std::min(restart, o.maxit - total_it);
             int its = 0;
             double rin = 0.0;
-            int rc = G.run<float>(SGFEM_FP32, d32, b32, V32, z32, w32, tmp32, restart, inner * res, inner_max, true,
-                                  &its, &rin);
-            if (rc != SGFEM_OK && rc != SGFEM_ERR_MAXIT) return rc;
+            int rc;
+            if (o.precision == SGFEM_FP32) {
+                SG_CUDA(ctx, cudaMemsetAsync(d32, 0, n32, ctx->stream));
+                rc = G.run<float>(SGFEM_FP32, d32, b32, V32, z32, w32, tmp32, restart, o.rtol * res, o.maxit - total_it,
+                                  true, &its, &rin);
+                if (rc != SGFEM_OK && rc != SGFEM_ERR_MAXIT) return rc;
+                k_add<double, float><<<grid, GT, 0, ctx->stream>>>(x64, d32, total);
+                SG_LAUNCHED(ctx);
+            } else {
+                // one flexible FP32 cycle per refinement step, its correction accumulated in
+                // FP64; first step to inner_rtol, later steps aim to end the solve (margin 3,
+                // at most a 1e-6 reduction per cycle)
+                const double finish = 0.3 * tol / res;
+                const double inner = outer == 0 ? std::max(o.inner_rtol, finish) : std::max(finish, 1e-6);
+                rc = G.run<float>(SGFEM_FP32, d32, b32, V32, z32, w32, tmp32, restart, inner * res,
+                                  std::min(restart, o.maxit - total_it), true, &its, &rin,
+                                  (float*)ctx->w_zbasis.p, x64);
+                if (rc != SGFEM_OK && rc != SGFEM_ERR_MAXIT) return rc;
+            }
             total_it += its;
             ++outer;
-            k_add<double, float><<<grid, GT, 0, ctx->stream>>>(x64, d32, total);
-            SG_LAUNCHED(ctx);
             if (its == 0) {  // FP32 cannot reduce the residual further
                 status = SGFEM_ERR_MAXIT;
                 break;

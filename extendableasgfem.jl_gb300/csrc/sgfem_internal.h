@@ -167,6 +167,7 @@ struct sgfem_context {
     DeviceBuf w_vec[SG_NBUF];  // SG vectors
     DeviceBuf w_partials;      // per-block reduction partials (double)
     DeviceBuf w_basis;         // GMRES Krylov basis (restart + 1 vectors)
+    DeviceBuf w_zbasis;        // flexible GMRES: preconditioned basis vectors (restart, FP32)
     DeviceBuf w_gsmall;        // GMRES multi-dot partials and coefficients
     KrylovScalars* d_scal = nullptr;
     KrylovScalars* h_scal = nullptr;  // pinned
