@@ -49,11 +49,29 @@ struct LatGeom {
 //   [0, Nl/2)          cos(2 pi k / Nl)
 //   [Nl/2, Nl)         sin(2 pi k / Nl)
 //   [Nl, 3Nl/2 + 1)    sin(pi j / Nl), j = 0..Nl/2
+// cos(pi m / 8), m = 0..8: the roots of unity of order 16 used inside a group
+__device__ __forceinline__ constexpr double cos_pi8(int m) {
+    return m == 0 ? 1.0
+         : m == 1 ? 0.92387953251128675613
+         : m == 2 ? 0.70710678118654752440
+         : m == 3 ? 0.38268343236508977173
+         : m == 4 ? 0.0
+         : m == 5 ? -0.38268343236508977173
+         : m == 6 ? -0.70710678118654752440
+         : m == 7 ? -0.92387953251128675613
+                  : -1.0;
+}
+
 // Radix-2 DIF FFT of the L = 2^LGL complex slots of every line of the tile,
 // sign +.  Stages are done in chunks of up to 4 bits: each thread loads the
 // 16 points of one group (indices differing only in the chunk's bits) into
 // registers, runs the chunk's stages there and writes back, so a 256-point
-// transform takes two shared-memory round trips instead of eight.
+// transform takes two shared-memory round trips instead of eight.  The
+// twiddle of stage b (span h = 2^b) at t = bl + k' 2^lo (bl = the group's bits
+// below the chunk, k' = the point's chunk bits below b) factors as
+//   exp(i pi t / h) = omega^(2^(hi-b)) * exp(i pi k' / 2^(b-lo)),
+// omega = exp(i pi bl / 2^hi) read once per group (and squared from stage to
+// stage), the second factor a compile-time root of unity of order <= 16.
 template <typename T, int LGL>
 __device__ __forceinline__ void fft_dif(T* tile, const T* cs, const T* sn, int lane, int warp) {
     constexpr int L = 1 << LGL;
@@ -74,23 +92,36 @@ __device__ __forceinline__ void fft_dif(T* tile, const T* cs, const T* sn, int l
                     re[k] = tile[(2 * idx) * 32 + lane];
                     im[k] = tile[(2 * idx + 1) * 32 + lane];
                 }
+            T omr = T(1), omi = T(0);
+            if (lo > 0) {
+                const int j = (g & ((1 << lo) - 1)) << (LGL - hi);
+                omr = cs[j];
+                omi = sn[j];
+            }
 #pragma unroll
             for (int bb = RB - 1; bb >= 0; --bb) {
                 if (bb >= nb) continue;
-                const int b = lo + bb;
+                if (bb != nb - 1) {  // omega^(2^(hi-b)) from the previous stage's power
+                    const T sr = omr * omr - omi * omi, si = T(2) * omr * omi;
+                    omr = sr;
+                    omi = si;
+                }
                 const int hs = 1 << bb;
-                const int h = 1 << b;
-                const int tstep = (2 * L) >> (b + 1);  // Nl / (2h)
 #pragma unroll
                 for (int k = 0; k < (1 << RB); ++k)
                     if (k < G && !(k & hs)) {
                         const int k2 = k | hs;
-                        const int t = (base | (k << lo)) & (h - 1);
                         const T ar = re[k], ai = im[k], cr = re[k2], ci = im[k2];
                         re[k] = ar + cr;
                         im[k] = ai + ci;
                         const T dr = ar - cr, di = ai - ci;
-                        const T wr = cs[t * tstep], wi = sn[t * tstep];
+                        const int m = (k & (hs - 1)) << (3 - bb);  // compile-time after unrolling
+                        T wr = omr, wi = omi;
+                        if (m != 0) {
+                            const T c = (T)cos_pi8(m), sgn = (T)cos_pi8(m > 4 ? m - 4 : 4 - m);
+                            wr = omr * c - omi * sgn;
+                            wi = omr * sgn + omi * c;
+                        }
                         re[k2] = dr * wr - di * wi;
                         im[k2] = dr * wi + di * wr;
                     }
