@@ -80,6 +80,7 @@ SIGNATURES = {
     "sgfem_from_device_layout": (ctypes.c_int, [_P, _P, _DP, ctypes.c_int]),
     "sgfem_solve_device": (ctypes.c_int, [_P, _DP, _P, ctypes.POINTER(SolveOptions), ctypes.POINTER(SolveStats)]),
     "sgfem_time_apply": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _DP]),
+    "sgfem_time_residual": (ctypes.c_int, [_P, ctypes.c_int, _DP, ctypes.POINTER(ctypes.c_int)]),
     "sgfem_kernel_launches": (ctypes.c_longlong, [_P]),
     "sgfem_time_precondition": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _DP]),
     "sgfem_estimate_primal": (ctypes.c_int, [_P, _DP, _P, _P, _DP, _P, _P, _DP, _DP]),
@@ -324,6 +325,13 @@ class Context:
         ms = ctypes.c_double()
         self._check(self.lib.sgfem_time_precondition(self.h, int(precision), int(reps), ctypes.byref(ms)))
         return ms.value
+
+    def time_residual(self, reps=10):
+        """(ms per refinement residual, 'double-FP32' or 'FP64')."""
+        ms = ctypes.c_double()
+        kind = ctypes.c_int()
+        self._check(self.lib.sgfem_time_residual(self.h, int(reps), ctypes.byref(ms), ctypes.byref(kind)))
+        return ms.value, ("double-FP32" if kind.value else "FP64")
 
     def time_apply(self, precision=FP64, reps=10):
         ms = ctypes.c_double()

@@ -169,6 +169,11 @@ __global__ void __launch_bounds__(VT) k_add64(double* __restrict__ x, const doub
     for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT) x[i] += d[i];
 }
 
+// r64 = (double) r32 (refinement diagnostics)
+__global__ void __launch_bounds__(VT) k_to_f64(const float* __restrict__ r, double* __restrict__ o, size_t total) {
+    for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT) o[i] = (double)r[i];
+}
+
 // d32 = (float) d64 (refinement diagnostics)
 __global__ void __launch_bounds__(VT) k_to_f32(const double* __restrict__ d, float* __restrict__ o, size_t total) {
     for (size_t i = (size_t)blockIdx.x * VT + threadIdx.x; i < total; i += (size_t)gridDim.x * VT) o[i] = (float)d[i];
@@ -501,6 +506,30 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
 
     int status = SGFEM_OK;
     double rr = 0.0;
+    // refinement residuals in double-FP32 arithmetic (residual_df.cu) when the operator
+    // allows the difference form: x and b as (hi, lo) float pairs, r straight to FP32
+    const bool df = low && sg_residual_df_usable(ctx);
+    void* xs = nullptr;
+    void* bs = nullptr;
+    bool r32_ready = false;
+    float* r32 = low ? (float*)ctx->w_vec[6].p : nullptr;
+    auto residual_df = [&](double* rr_out) -> int {
+        int nb = 0;
+        SG_TRY(sg_residual_df(ctx, xs, bs, r32, partials, &nb));
+        SG_TRY(S.fin(nb, FIN_SUM, FinArgs{0.0, 0}, d_sum));
+        SG_CUDA(ctx, cudaMemcpyAsync(rr_out, d_sum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        r32_ready = true;
+        return SGFEM_OK;
+    };
+    if (df) {
+        SG_TRY(sg_residual_df_prepare(ctx));
+        SG_TRY(sg_ensure(ctx, ctx->w_vec[12], n64));
+        SG_TRY(sg_ensure(ctx, ctx->w_vec[13], n64));
+        xs = ctx->w_vec[12].p;
+        bs = ctx->w_vec[13].p;
+        SG_TRY(sg_split_df(ctx, b, nullptr, bs, 0));
+    }
     {
         // initial residual: with a zero warm start r = b and no FP64 apply is needed
         k_dot<double><<<g, VT, 0, ctx->stream>>>(x64, x64, total, partials);
@@ -512,6 +541,9 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
         if (xx == 0.0) {
             SG_CUDA(ctx, cudaMemcpyAsync(r, b, n64, cudaMemcpyDeviceToDevice, ctx->stream));
             rr = bb;
+        } else if (df) {
+            SG_TRY(sg_split_df(ctx, x64, nullptr, xs, 0));
+            SG_TRY(residual_df(&rr));
         } else {
             SG_TRY(true_residual(&rr));
         }
@@ -549,7 +581,6 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
         } else {
             float* d32 = (float*)ctx->w_vec[5].p;
             double* d64 = q;  // the FP32 PCG's solution, accumulated in FP64
-            float* r32 = (float*)ctx->w_vec[6].p;
             float* p32 = (float*)ctx->w_vec[7].p;
             float* q32 = (float*)ctx->w_vec[8].p;
             float* tmp32 = (float*)ctx->w_vec[9].p;
@@ -558,8 +589,18 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
                 if (!std::isfinite(rr)) { status = SGFEM_ERR_NONFINITE; break; }
                 if (rr <= tol2e * bb) break;
                 if (remaining <= 0) { status = SGFEM_ERR_MAXIT; break; }
-                k_demote<<<g, VT, 0, ctx->stream>>>(r, r32, d64, total, partials);
-                SG_LAUNCHED(ctx);
+                if (r32_ready) {  // the double-FP32 residual already wrote the FP32 right-hand side
+                    SG_CUDA(ctx, cudaMemsetAsync(d64, 0, n64, ctx->stream));
+                    k_dot<float><<<g, VT, 0, ctx->stream>>>(r32, r32, total, partials);  // for FIN_TOL below
+                    SG_LAUNCHED(ctx);
+                    if (trace >= 2) {  // the diagnostics compare against r in FP64
+                        k_to_f64<<<g, VT, 0, ctx->stream>>>(r32, r, total);
+                        SG_LAUNCHED(ctx);
+                    }
+                } else {
+                    k_demote<<<g, VT, 0, ctx->stream>>>(r, r32, d64, total, partials);
+                    SG_LAUNCHED(ctx);
+                }
                 // inner target (squared reduction of ||r||).  First step: inner_rtol.  Later
                 // steps aim to end the solve with a margin of 3, asking at most a 1e-6
                 // reduction of one FP32 PCG (about what its recurrence tracks in FP64 with
@@ -592,15 +633,21 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
                     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
                 }
                 const double rr_in = rr;
-                k_add64<<<g, VT, 0, ctx->stream>>>(x64, d64, total);
-                SG_LAUNCHED(ctx);
-                SG_TRY(true_residual(&rr));
+                if (df) {
+                    SG_TRY(sg_split_df(ctx, x64, d64, xs, 1));  // x += d, then x as (hi, lo)
+                    SG_TRY(residual_df(&rr));
+                } else {
+                    k_add64<<<g, VT, 0, ctx->stream>>>(x64, d64, total);
+                    SG_LAUNCHED(ctx);
+                    SG_TRY(true_residual(&rr));
+                }
                 if (trace)
                     fprintf(stderr, "sgfem: refinement step %d: inner target %.3g, %d FP32 iterations, relres %.3e\n",
                             outer + 1, std::sqrt(want), it, std::sqrt(rr / bb));
                 if (trace >= 2)
-                    fprintf(stderr, "sgfem:   reduction: recurrence %.3e, FP32 operator %.3e, FP64 %.3e\n",
-                            std::sqrt(rec / rr_in), std::sqrt(tr32 / rr_in), std::sqrt(rr / rr_in));
+                    fprintf(stderr, "sgfem:   reduction: recurrence %.3e, FP32 operator %.3e, %s %.3e\n",
+                            std::sqrt(rec / rr_in), std::sqrt(tr32 / rr_in), df ? "double-FP32" : "FP64",
+                            std::sqrt(rr / rr_in));
                 if (o->precision == SGFEM_FP32) break;  // plain FP32 PCG: no refinement
             }
         }

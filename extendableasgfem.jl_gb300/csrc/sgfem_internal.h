@@ -48,7 +48,7 @@ struct DeviceBuf {
     size_t bytes = 0;
 };
 
-enum { SG_NBUF = 12 };
+enum { SG_NBUF = 14 };
 
 struct sgfem_context {
     int device = 0;
@@ -98,6 +98,8 @@ struct sgfem_context {
     double* d_combg64 = nullptr;
     float* d_combg32 = nullptr;
     int ncomb = 0;
+    float2* d_valdf = nullptr;     // K_m values as (hi, lo) float pairs (double-FP32 residual)
+    float2* d_combgdf = nullptr;   // G combination coefficients as (hi, lo)
 
     // device column order of the modes
     std::vector<int32_t> mode_of_col;  // device column -> caller mode
@@ -223,6 +225,12 @@ int sg_jit_launch(sgfem_context* ctx, const void* X, void* Y, double* partials, 
 void sg_jit_release(sgfem_context* ctx);
 // error status of the specialised kernel since the last check (resets it)
 int sg_jit_check(sgfem_context* ctx);
+// double-FP32 refinement residual (residual_df.cu): usable when every K_m has vanishing
+// row sums (difference form); xs/bs are (hi, lo) float2 vectors in the device layout
+bool sg_residual_df_usable(const sgfem_context* ctx);
+int sg_residual_df_prepare(sgfem_context* ctx);
+int sg_split_df(sgfem_context* ctx, double* x, const double* d, void* xs, int add);
+int sg_residual_df(sgfem_context* ctx, const void* xs, const void* bs, float* r32, double* partials, int* nblocks);
 // whether the specialised kernel takes this X (the window kernel copies 16-byte pieces)
 bool sg_jit_accepts(const sgfem_context* ctx, const void* X);
 

@@ -162,6 +162,11 @@ SGFEM_API int sgfem_solve_device(sgfem_context* ctx, const double* b0, void* x_d
 
 /* time (ms, CUDA events on the context stream) of `reps` back-to-back device applies */
 SGFEM_API int sgfem_time_apply(sgfem_context* ctx, int precision, int reps, double* ms_per_apply);
+/* device time of the residual r = b - A x that ends every mixed refinement step:
+   double-FP32 arithmetic (difference form, error-free products and sums on the
+   FP32 pipe) when every K_m has vanishing row sums, else the FP64 apply plus
+   the subtraction; *kind = 1 for the double-FP32 form, 0 for FP64 */
+SGFEM_API int sgfem_time_residual(sgfem_context* ctx, int reps, double* ms_per_residual, int* kind);
 /* the same for the lattice preconditioner (three passes per application) */
 SGFEM_API int sgfem_time_precondition(sgfem_context* ctx, int precision, int reps, double* ms_per_application);
 /*

@@ -146,3 +146,33 @@ def test_package_solve_entry_point(built_pkg):
     assert rel(p.sol.entries, oracle_solution(p)) <= 1e-9
     with pytest.raises(ValueError):
         pkg.solve(pkg.PoissonProblemPrimal, p.sol, p.C, rhs=None)
+
+
+@pytest.mark.parametrize("order,N", [(1, 32), (2, 16)])
+def test_mixed_residual_certificate(built_pkg, monkeypatch, order, N):
+    """The mixed solver's refinement residuals are evaluated in double-FP32
+    arithmetic (difference form, error-free products and sums); the relres it
+    reports equals the FP64 residual of the returned solution, and it agrees
+    with the FP64-residual mode (SGFEM_RESIDUAL=fp64)."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    p = build(N, order, 6, pkg.top_weight_multiindices(6, 30, C.decay_factors))
+    b = osg.reference_rhs(np.zeros(p.n * p.P), p.b0, p.bdofs, p.P)
+    out = {}
+    for mode in ("default", "fp64"):
+        if mode == "fp64":
+            monkeypatch.setenv("SGFEM_RESIDUAL", "fp64")
+        op = pkg.SGOperator(p.V, p.TB, p.Kall, device=0)
+        for rtol in (1e-8, 1e-11):
+            x = np.zeros(p.n * p.P)
+            st = op.solve_primal(p.b0, x, rtol=rtol, precision=pkg.MIXED)
+            r = b - osg.apply_fast(x, p.K0, p.Ks, p.G, p.bdofs, p.P)
+            host = np.linalg.norm(r) / np.linalg.norm(b)
+            assert st["relres"] <= rtol and host <= 1.01 * rtol, (mode, rtol, st["relres"], host)
+            assert abs(st["relres"] - host) <= 0.02 * host + 1e-14, (mode, rtol, st["relres"], host)
+            out[(mode, rtol)] = x
+            assert (st["fp64_applies"] == 0) == (mode == "default")
+        op.close()
+    for rtol in (1e-8, 1e-11):
+        assert rel(out[("default", rtol)], out[("fp64", rtol)]) <= 1e3 * rtol
