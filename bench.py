@@ -330,7 +330,8 @@ def run_ours(args, rank, world, local, pg):
 def run_profile(args):
     """Small, bounded launches for ncu: `apply32` / `apply64` launch the apply 1+3
     times; `precond32` / `precond64` apply the lattice preconditioner 1+2 times
-    (three pass kernels each); `solve` runs one mixed solve."""
+    (three pass kernels each); `residual` evaluates the mixed refinement residual
+    1+2 times; `solve` runs one mixed solve."""
     import __graft_entry__ as ge
     pkg = ge.load_package()
     V, TB, Ks, b0 = setup_workload(pkg, N=args.mesh)
@@ -339,6 +340,9 @@ def run_profile(args):
         prec = pkg.FP32 if args.profile == "apply32" else pkg.FP64
         ms = op.ctx.time_apply(prec, 3)
         print(json.dumps({"profile": args.profile, "ms_per_apply": ms}))
+    elif args.profile == "residual":
+        ms, kind = op.ctx.time_residual(2)
+        print(json.dumps({"profile": "residual", "ms_per_residual": ms, "kind": kind}))
     elif args.profile in ("precond32", "precond64"):
         prec = pkg.FP32 if args.profile == "precond32" else pkg.FP64
         ms = op.ctx.time_precondition(prec, 2)
@@ -611,7 +615,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile", choices=["apply32", "apply64", "precond32", "precond64", "solve"], default=None,
+    ap.add_argument("--profile", choices=["apply32", "apply64", "precond32", "precond64", "residual", "solve"], default=None,
                     help="profiling target for ncu: set up the workload, run the kernel(s) a few times, exit")
     ap.add_argument("--mesh", type=int, default=256, help="mesh size for --profile / --workload adjoint")
     ap.add_argument("--workload", choices=["config2", "config1", "lognormal", "sampling", "adjoint", "batch"],

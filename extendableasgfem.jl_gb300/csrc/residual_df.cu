@@ -27,6 +27,7 @@
 namespace {
 
 constexpr int DWPB = 4;  // warps per block
+constexpr int DMINB = 4;  // resident blocks per SM the register budget is fitted to
 
 struct DF {
     float h, l;
@@ -69,8 +70,10 @@ __global__ void k_add_split(double* __restrict__ x, const double* __restrict__ d
     }
 }
 
+constexpr int DCOL = 5;  // columns per lane staged from registers (ld <= 160); larger ld loads in place
+
 template <int QT>
-__global__ void __launch_bounds__(DWPB * 32)
+__global__ void __launch_bounds__(DWPB * 32, DMINB)
 k_residual_df(const int* __restrict__ rowptr, const int* __restrict__ col, const float2* __restrict__ vals, int M1,
               const float2* __restrict__ xs, const float2* __restrict__ bs, float* __restrict__ r32, int n, int P,
               int ld, const unsigned char* __restrict__ bmask, const int* __restrict__ qtab, int Qn,
@@ -112,17 +115,50 @@ k_residual_df(const int* __restrict__ rowptr, const int* __restrict__ col, const
             DF acc[QT];
 #pragma unroll
             for (int t = 0; t < QT; ++t) acc[t] = {0.f, 0.f};
-            for (int nz = nz0; nz < nz1; ++nz) {
-                const int j = col[nz];
-                const float2* xj = xs + (size_t)j * ld;
-                __syncwarp();
-                for (int c = lane; c < ld; c += 32) {
-                    const float2 a = xj[c], b = sx[c];
-                    const DF s = two_sum(a.x, -b.x);
-                    sd[c] = make_float2(s.h, __fadd_rn(s.l, __fsub_rn(a.y, b.y)));
+            // the next nonzero's X row and values are loaded while the current one is used
+            const bool reg = ld <= 32 * DCOL;
+            float2 xn[DCOL];
+            float2 vn = make_float2(0.f, 0.f);
+            if (nz0 < nz1) {
+                const float2* xj = xs + (size_t)col[nz0] * ld;
+#pragma unroll
+                for (int u = 0; u < DCOL; ++u) {
+                    const int c = lane + 32 * u;
+                    xn[u] = (reg && c < ld) ? xj[c] : make_float2(0.f, 0.f);
                 }
-                if (lane < M1) sc[lane] = vals[(size_t)nz * M1 + lane];
+                if (lane < M1) vn = vals[(size_t)nz0 * M1 + lane];
+            }
+            for (int nz = nz0; nz < nz1; ++nz) {
                 __syncwarp();
+                if (reg) {
+#pragma unroll
+                    for (int u = 0; u < DCOL; ++u) {
+                        const int c = lane + 32 * u;
+                        if (c < ld) {
+                            const float2 a = xn[u], b = sx[c];
+                            const DF s = two_sum(a.x, -b.x);
+                            sd[c] = make_float2(s.h, __fadd_rn(s.l, __fsub_rn(a.y, b.y)));
+                        }
+                    }
+                } else {
+                    const float2* xj = xs + (size_t)col[nz] * ld;
+                    for (int c = lane; c < ld; c += 32) {
+                        const float2 a = xj[c], b = sx[c];
+                        const DF s = two_sum(a.x, -b.x);
+                        sd[c] = make_float2(s.h, __fadd_rn(s.l, __fsub_rn(a.y, b.y)));
+                    }
+                }
+                if (lane < M1) sc[lane] = vn;
+                __syncwarp();
+                if (nz + 1 < nz1) {
+                    const float2* xj = xs + (size_t)col[nz + 1] * ld;
+#pragma unroll
+                    for (int u = 0; u < DCOL; ++u) {
+                        const int c = lane + 32 * u;
+                        if (reg && c < ld) xn[u] = xj[c];
+                    }
+                    if (lane < M1) vn = vals[(size_t)(nz + 1) * M1 + lane];
+                }
 #pragma unroll
                 for (int t = 0; t < QT; ++t) df_fma(acc[t], sc[om[t]], sd[on[t]]);
             }
