@@ -89,6 +89,8 @@ extern "C" int sgfem_destroy(sgfem_context* ctx) {
                     ctx->d_lat_scale64, ctx->d_lat_scale32, ctx->d_lat_blk64, ctx->d_lat_blk32, ctx->d_scal, ctx->w_stage.p, ctx->w_partials.p,
                     ctx->d_jptr, ctx->d_joff, ctx->d_jg, ctx->d_jtab, ctx->d_val32p, ctx->d_mode_of_col,
                     ctx->d_y64, ctx->d_y32, ctx->d_valdf, ctx->d_combgdf};
+    if (ctx->pcg_exec) cudaGraphExecDestroy(ctx->pcg_exec);
+    if (ctx->pcg_graph) cudaGraphDestroy(ctx->pcg_graph);
     sg_jit_release(ctx);
     for (void* p : ptrs) free_dev(p);
     for (int i = 0; i < SG_NBUF; ++i) free_dev(ctx->w_vec[i].p);
