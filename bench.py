@@ -292,9 +292,9 @@ def run_ours(args, rank, world, local, pg):
             traffic = None
     line = {
         "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "precision": "mixed (FP32 inner PCG, FP64 refinement)",
+        "config": {"workload": WORKLOAD, "precision": "mixed (FP32 PCG with FP64 solution accumulation, double-FP32 refinement residual, FP64 result)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (operator + vectors ~0.8 GB)"},
         "fp64_solve_ms": fp64_ms, "mixed_speedup_vs_fp64": fp64_ms / ms,
@@ -312,6 +312,9 @@ def run_ours(args, rank, world, local, pg):
         "precondition_ms": {"fp32": ctx.time_precondition(pkg.FP32, 10), "fp64": ctx.time_precondition(pkg.FP64, 5)},
         "apply_fp64": {"ms_per_launch": t64, "GB/s": B64 / (t64 * 1e-3) / 1e9,
                        "GFLOP/s": algorithmic_flops(n, P, nnz, ctx_qn(op), TB.G.nnz) / (t64 * 1e-3) / 1e9},
+        "refinement_residual": dict(zip(("ms", "arithmetic"), ctx.time_residual(5))),
+        "solve_structure": {"fp32_iterations": statistics.median(iters), "refinement_steps": st.outer_iterations,
+                            "fp64_applies": st.fp64_applies, "lattice_preconditioner": ctx.lattice_log},
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:
