@@ -50,12 +50,43 @@ __device__ __forceinline__ void df_fma(DF& acc, float2 k, float2 d) {
     acc.h = s.h;
 }
 
+// (hi, lo) = (fl32(v), fl32(v - fl32(v))) by integer operations on the bit pattern
+// (GB300's FP64 conversions and subtraction run at the FP64 rate): hi keeps the top
+// 24 bits of the 53-bit significand rounded to nearest even, lo is the signed
+// remainder (< 2^29 units of the last place) times 2^(e - 1075).  Magnitudes
+// outside [2^-74, 2^126] (where the scale or hi would leave the normal float
+// range) take the FP64 path; zero and subnormal doubles give (0, 0).
+__device__ __forceinline__ float2 split_f64(double v) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((u >> 52) & 0x7FF);
+    if (e == 0) return make_float2(0.f, 0.f);
+    if (e < 949 || e > 1149) {
+        const float h = __double2float_rn(v);
+        return make_float2(h, __double2float_rn(v - (double)h));
+    }
+    const unsigned long long mant = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    unsigned int q = (unsigned int)(mant >> 29);
+    int rem = (int)(mant & 0x1FFFFFFFull);
+    if (rem > (1 << 28) || (rem == (1 << 28) && (q & 1u))) {
+        q += 1u;
+        rem -= (1 << 29);
+    }
+    int fe = e - 1023 + 127;
+    if (q == (1u << 24)) {
+        q >>= 1;
+        fe += 1;
+    }
+    const unsigned int sign = (unsigned int)(u >> 63) << 31;
+    const float hi = __uint_as_float(sign | ((unsigned int)fe << 23) | (q & 0x7FFFFFu));
+    const float scale = __uint_as_float((unsigned int)(e - 948) << 23);  // 2^(e - 1075)
+    const float lo = __fmul_rn(__int2float_rn(rem), scale);
+    return make_float2(hi, sign ? -lo : lo);
+}
+
 // hi/lo split of FP64 values
 __global__ void k_split_pairs(const double* __restrict__ src, float2* __restrict__ dst, size_t count) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
-        const double v = src[i];
-        const float h = (float)v;
-        dst[i] = make_float2(h, (float)(v - (double)h));
+        dst[i] = split_f64(src[i]);
     }
 }
 
@@ -65,8 +96,7 @@ __global__ void k_add_split(double* __restrict__ x, const double* __restrict__ d
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         const double v = add ? x[i] + d[i] : x[i];
         if (add) x[i] = v;
-        const float h = (float)v;
-        xs[i] = make_float2(h, (float)(v - (double)h));
+        xs[i] = split_f64(v);
     }
 }
 
