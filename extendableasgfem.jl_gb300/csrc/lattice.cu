@@ -76,15 +76,24 @@ template <typename T, int LGL>
 __device__ __forceinline__ void fft_dif(T* tile, const T* cs, const T* sn, int lane, int warp) {
     constexpr int L = 1 << LGL;
     constexpr int RB = LGL < 4 ? LGL : 4;
+    // the last chunk (lo = 0) keeps all of a thread's groups in registers and stores
+    // them to their bit-reversed slots, so the output is in natural order
+    constexpr int NBL = (LGL - 1) % RB + 1;
+    constexpr int NGW = ((L >> NBL) + LAT_WARPS - 1) / LAT_WARPS;
+    T rel[NGW][1 << RB], iml[NGW][1 << RB];
 #pragma unroll
     for (int hi = LGL - 1; hi >= 0; hi -= RB) {
         const int lo = hi - RB + 1 > 0 ? hi - RB + 1 : 0;
         const int nb = hi - lo + 1;
         const int G = 1 << nb;
         const int ngroups = L >> nb;
-        for (int g = warp; g < ngroups; g += LAT_WARPS) {
+#pragma unroll
+        for (int w = 0; w < (lo == 0 ? NGW : (L >> nb) / LAT_WARPS + 1); ++w) {
+            const int g = warp + w * LAT_WARPS;
+            if (g >= ngroups) break;
             const int base = ((g >> lo) << (hi + 1)) | (g & ((1 << lo) - 1));
-            T re[1 << RB], im[1 << RB];
+            T* re = rel[lo == 0 ? w : 0];
+            T* im = iml[lo == 0 ? w : 0];
 #pragma unroll
             for (int k = 0; k < (1 << RB); ++k)
                 if (k < G) {
@@ -126,13 +135,31 @@ __device__ __forceinline__ void fft_dif(T* tile, const T* cs, const T* sn, int l
                         im[k2] = dr * wi + di * wr;
                     }
             }
+            if (lo != 0) {
 #pragma unroll
-            for (int k = 0; k < (1 << RB); ++k)
-                if (k < G) {
-                    const int idx = base | (k << lo);
-                    tile[(2 * idx) * 32 + lane] = re[k];
-                    tile[(2 * idx + 1) * 32 + lane] = im[k];
-                }
+                for (int k = 0; k < (1 << RB); ++k)
+                    if (k < G) {
+                        const int idx = base | (k << lo);
+                        tile[(2 * idx) * 32 + lane] = re[k];
+                        tile[(2 * idx + 1) * 32 + lane] = im[k];
+                    }
+            }
+        }
+        if (lo == 0) {
+            __syncthreads();  // every input of the last chunk is in registers
+#pragma unroll
+            for (int w = 0; w < NGW; ++w) {
+                const int g = warp + w * LAT_WARPS;
+                if (g >= ngroups) break;
+#pragma unroll
+                for (int k = 0; k < (1 << RB); ++k)
+                    if (k < G) {
+                        const int idx = g * G + k;
+                        const int r = (int)(__brev((unsigned)idx) >> (32 - LGL));
+                        tile[(2 * r) * 32 + lane] = rel[w][k];
+                        tile[(2 * r + 1) * 32 + lane] = iml[w][k];
+                    }
+            }
         }
         __syncthreads();
     }
@@ -141,7 +168,6 @@ __device__ __forceinline__ void fft_dif(T* tile, const T* cs, const T* sn, int l
 template <typename T, int LGL>
 __device__ void dst_line(T* tile, const T* tab) {
     constexpr int Nl = 2 << LGL;
-    constexpr int lg = LGL + 1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     constexpr int L = Nl >> 1;
     const T* cs = tab;
@@ -159,21 +185,7 @@ __device__ void dst_line(T* tile, const T* tab) {
     if (warp == 0) tile[lane] = T(0);
     __syncthreads();
     // complex FFT (sign +) of z_k = (y_2k, y_2k+1), k < L, decimation in frequency
-    fft_dif<T, LGL>(tile, cs, sn, lane, warp);
-    // bit reversal of the L complex slots
-    for (int k = warp; k < L; k += LAT_WARPS) {
-        const int r = (int)(__brev((unsigned)k) >> (32 - (lg - 1)));
-        if (k < r) {
-            T* a = tile + 2 * k * 32 + lane;
-            T* c = tile + 2 * r * 32 + lane;
-            const T t0 = a[0], t1 = a[32];
-            a[0] = c[0];
-            a[32] = c[32];
-            c[0] = t0;
-            c[32] = t1;
-        }
-    }
-    __syncthreads();
+    fft_dif<T, LGL>(tile, cs, sn, lane, warp);  // output in natural order
     // unpack F_k = E_k + w^k O_k for the pair (k, L-k); write X_2k = Im F_k at 2k,
     // Re F_k at 2k+1 (prefix-summed below)
     for (int k = warp; k <= (L >> 1); k += LAT_WARPS) {
