@@ -582,7 +582,7 @@ def run_batch(args):
         TB = pkg.TensorizedBasis(pkg.LegendrePolynomials, M, d, d + 4, multi_indices=mis)
         V = pkg.H1Pk(pkg.unit_square_mesh(N), 1)
         sol = pkg.SGFEVector(V, TB)
-        Ks, b0 = pkg.assemble(pkg.PoissonProblemPrimal, sol, C, rhs=lambda x, y: np.ones_like(x))
+        Ks, b0 = pkg.assemble(pkg.PoissonProblemPrimal, sol, C, rhs=lambda x, y: np.ones_like(x), device=0)
         B.add(V, TB, Ks, b0)
         unknowns += V.ndofs * TB.nmodes
     t_setup = time.perf_counter() - t0
@@ -611,6 +611,29 @@ def ctx_qn(op):
     return q
 
 
+def run_assembly(args):
+    """K_0..K_20 of the headline workload (P2 256x256, cosine coefficient, order-4
+    cell rule): host assembly (the caller-side restatement) vs sgfem_assemble_stiffness
+    (wall time including the pattern and gather lists built on the host)."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    V = pkg.H1Pk(pkg.unit_square_mesh(args.mesh), 2)
+    ms = list(range(21))
+    pkg.assemble_stiffness_gpu(V, C, [0], 4)  # context and library warm-up
+    t = time.perf_counter()
+    Kg = pkg.assemble_stiffness_gpu(V, C, ms, 4)
+    t_gpu = (time.perf_counter() - t) * 1e3
+    t = time.perf_counter()
+    Kh = pkg.assemble_stiffness(V, C, ms, 4)
+    t_host = (time.perf_counter() - t) * 1e3
+    err = max(float(np.abs(a.data - b.data).max() / np.abs(a.data).max()) for a, b in zip(Kh, Kg))
+    line = {"workload": f"assembly: K_0..K_20 of P2 {args.mesh}x{args.mesh} ({V.ndofs} dofs, {Kg[0].nnz} nonzeros), "
+                        f"cosine coefficient, order-4 cell rule",
+            "gpu_ms_wall": t_gpu, "host_ms_wall": t_host, "speedup": t_host / t_gpu, "max_rel_diff": err}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -621,7 +644,8 @@ def main():
     ap.add_argument("--profile", choices=["apply32", "apply64", "precond32", "precond64", "residual", "solve"], default=None,
                     help="profiling target for ncu: set up the workload, run the kernel(s) a few times, exit")
     ap.add_argument("--mesh", type=int, default=256, help="mesh size for --profile / --workload adjoint")
-    ap.add_argument("--workload", choices=["config2", "config1", "lognormal", "sampling", "adjoint", "batch"],
+    ap.add_argument("--workload", choices=["config2", "config1", "lognormal", "sampling", "adjoint", "batch",
+                                           "assembly"],
                     default="config2", help="config2 is the headline bench line; the others print their own line")
     ap.add_argument("--samples", type=int, default=100000, help="--workload sampling: number of samples")
     ap.add_argument("--directions", type=int, default=20, help="--workload adjoint: finite-difference directions")
@@ -632,7 +656,7 @@ def main():
         return run_profile(args)
     if args.workload != "config2":
         return {"config1": run_config1, "lognormal": run_lognormal, "sampling": run_sampling,
-                "adjoint": run_adjoint, "batch": run_batch}[args.workload](args)
+                "adjoint": run_adjoint, "batch": run_batch, "assembly": run_assembly}[args.workload](args)
     rank, world, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world, pg)

@@ -12,6 +12,7 @@ from .batch import SGBatch, config4_problems, splitmix64
 from .coefficients import StochasticCoefficientCosinus
 from .estimate import estimate, extension_couplings
 from .fem import (H1Pk, assemble_convection, assemble_laplacian, assemble_pce_rhs, assemble_rhs, assemble_stiffness,
+                  assemble_stiffness_gpu,
                   assemble_stiffness_nodal_mean, box_functional, line_rule, pce_lambda, triangle_rule,
                   unit_square_mesh)
 from .modelproblems import (AbstractModelProblem, LogTransformedPoissonProblemPrimal, PoissonProblemPrimal, SGOperator,
@@ -27,7 +28,7 @@ from .tensorizedbasis import TensorizedBasis, coupling_matrix
 __all__ = [
     "FP32", "FP64", "MIXED", "PREC_JACOBI", "PREC_LATTICE", "PREC_NONE", "SGError", "MeanQoI", "SGBatch",
     "config4_problems", "splitmix64",
-    "assemble_stiffness_nodal_mean", "box_functional",
+    "assemble_stiffness_nodal_mean", "assemble_stiffness_gpu", "box_functional",
     "StochasticCoefficientCosinus", "estimate", "extension_couplings", "H1Pk", "assemble_convection",
     "assemble_laplacian", "assemble_pce_rhs", "assemble_rhs", "assemble_stiffness", "line_rule", "pce_lambda",
     "triangle_rule", "unit_square_mesh", "AbstractModelProblem", "LogTransformedPoissonProblemPrimal",

@@ -321,3 +321,45 @@ def box_functional(space, box, quadorder=None):
     x0, x1, y0, y1 = box
     ind = lambda x, y: ((x >= x0) & (x <= x1) & (y >= y0) & (y <= y1)).astype(np.float64)
     return assemble_rhs(space, ind, space.order + 1 if quadorder is None else quadorder)
+
+
+def assemble_stiffness_gpu(space, coef, ms, quadorder, device=0, ctx=None):
+    """assemble_stiffness on the GPU (sgfem_assemble_stiffness): the same CSR
+    matrices (pattern of `space.pattern()`, values summed cell by cell), with the
+    quadrature-point work and the per-nonzero sums on the device.  `ms` must be a
+    contiguous range of terms."""
+    import ctypes
+    from . import _lib
+    from .estimate import _Cosine, _Quad, _mesh_struct, _ptr
+    from .sampling_error import _FESpace
+    ms = list(ms)
+    m0, m1 = ms[0], ms[-1]
+    if ms != list(range(m0, m1 + 1)):
+        raise ValueError("assemble_stiffness_gpu: terms must be a contiguous range")
+    pts, wts = triangle_rule(quadorder)
+    indptr, col, _ = space.pattern()
+    n = space.ndofs
+    colptr = np.ascontiguousarray(indptr + 1, dtype=np.int64)   # the pattern is symmetric: CSR = CSC
+    rowval = np.ascontiguousarray(col + 1, dtype=np.int64)
+    nnz = len(col)
+    mesh, keep = _mesh_struct(space)
+    xref = np.ascontiguousarray(pts, dtype=np.float64)
+    w = np.ascontiguousarray(wts, dtype=np.float64)
+    q = _Quad(len(w), _ptr(xref), _ptr(w), 0, None, None)
+    dfac = np.ascontiguousarray(coef.decay_factors, dtype=np.float64)
+    b1 = np.ascontiguousarray(coef.b1, dtype=np.int64)
+    b2 = np.ascontiguousarray(coef.b2, dtype=np.int64)
+    c = _Cosine(coef.maxm(), coef.mean_value, coef.freq, _ptr(dfac), _ptr(b1), _ptr(b2))
+    cd = np.ascontiguousarray(space.celldofs + 1, dtype=np.int64)
+    fs = _FESpace(space.order, n, cd.ctypes.data)
+    vals = np.zeros((m1 - m0 + 1, nnz))
+    own = ctx is None
+    ctx = _lib.Context(device) if own else ctx
+    try:
+        ctx._check(ctx.lib.sgfem_assemble_stiffness(ctx.h, ctypes.byref(mesh), ctypes.byref(fs), ctypes.byref(c), m0,
+                                                    m1, ctypes.byref(q), nnz, _lib._i64p(colptr), _lib._i64p(rowval),
+                                                    _lib._dp(vals)))
+    finally:
+        if own:
+            ctx.close()
+    return [sp.csr_matrix((vals[i], col, indptr), shape=(n, n)) for i in range(m1 - m0 + 1)]

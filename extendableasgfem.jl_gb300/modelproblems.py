@@ -20,7 +20,8 @@ boundary, ExtendableFEM in the reference) and moves arrays across the C ABI.
 import numpy as np
 
 from . import _lib
-from .fem import assemble_convection, assemble_laplacian, assemble_pce_rhs, assemble_rhs, assemble_stiffness
+from .fem import (assemble_convection, assemble_laplacian, assemble_pce_rhs, assemble_rhs, assemble_stiffness,
+                  assemble_stiffness_gpu)
 
 
 class AbstractModelProblem:
@@ -94,9 +95,10 @@ class SGOperator:
         self.ctx.close()
 
 
-def assemble(problem, sol, C, rhs, bonus_quadorder_a=2, bonus_quadorder_f=0):
+def assemble(problem, sol, C, rhs, bonus_quadorder_a=2, bonus_quadorder_f=0, device=None):
     """Spatial blocks: poisson_primal.jl:55-68 ([K_0..K_M], b = (f, v)) or
-    logpoisson_primal.jl:97-131 ([A, N_1..N_M], b_mu = (lambda_mu f, v) for all modes)."""
+    logpoisson_primal.jl:97-131 ([A, N_1..N_M], b_mu = (lambda_mu f, v) for all modes).
+    device=k assembles the K_m of PoissonProblemPrimal on GPU k (sgfem_assemble_stiffness)."""
     if problem is not PoissonProblemPrimal and problem is not LogTransformedPoissonProblemPrimal:
         raise NotImplementedError(f"no assembly for {problem}")
     if rhs is None:
@@ -109,7 +111,10 @@ def assemble(problem, sol, C, rhs, bonus_quadorder_a=2, bonus_quadorder_f=0):
         Ns = assemble_convection(FES, C, list(range(1, M + 1)), p + (p - 1) + bonus_quadorder_a)
         b = assemble_pce_rhs(FES, C, [sol.TB.multi_indices[k] for k in sol.active_modes], rhs, p + bonus_quadorder_f)
         return [A] + Ns, b
-    Ks = assemble_stiffness(FES, C, list(range(M + 1)), 2 * (p - 1) + bonus_quadorder_a)
+    if device is None:
+        Ks = assemble_stiffness(FES, C, list(range(M + 1)), 2 * (p - 1) + bonus_quadorder_a)
+    else:
+        Ks = assemble_stiffness_gpu(FES, C, list(range(M + 1)), 2 * (p - 1) + bonus_quadorder_a, device=device)
     b0 = assemble_rhs(FES, rhs, p + bonus_quadorder_f)
     return Ks, b0
 

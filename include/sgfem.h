@@ -403,6 +403,22 @@ SGFEM_API int sgfem_batch_solve(sgfem_batch* batch, double rtol, int maxit, int 
                                 sgfem_batch_stats* stats);
 SGFEM_API int sgfem_batch_problem_stats(const sgfem_batch* batch, int i, int* iterations, double* relres);
 
+/*
+ * Stiffness matrices of the cosine coefficient assembled on the GPU (the
+ * reference assembles them on the host with ExtendableFEM, poisson_primal.jl:
+ * 56-68): K_m = (a_m grad u, grad v) for m = m0..m1 (a_0 = coef->mean) on the
+ * H1Pk space `space` (order 1 or 2) of `mesh` (coords, cell_nodes and
+ * cell_volumes are used), with the cell rule of `quad` (weights summing to
+ * one).  The sparsity pattern is the caller's CSC (1-based colptr[n + 1],
+ * rowval[nnz], every cell coupling present); values receives the nonzeros of
+ * K_m0..K_m1 in that pattern, (m1 - m0 + 1) x nnz column-major.  Each nonzero
+ * sums its cells' contributions in increasing cell order (no atomics).  ctx only
+ * names the GPU, the stream and the error message; it need not be finalized.
+ */
+SGFEM_API int sgfem_assemble_stiffness(sgfem_context* ctx, const sgfem_mesh* mesh, const sgfem_fe_space* space,
+                                       const sgfem_cosine* coef, int m0, int m1, const sgfem_quadrature* quad,
+                                       int64_t nnz, const int64_t* colptr, const int64_t* rowval, double* values);
+
 /* which FP32 apply kernel a finalized context uses: 1 = specialised to the coupling
    structure (compiled with NVRTC at finalize), 0 = generic; the log says why */
 SGFEM_API int sgfem_apply_variant(const sgfem_context* ctx);
