@@ -69,6 +69,7 @@ SIGNATURES = {
     "sgfem_set_dof_coordinates": (ctypes.c_int, [_P, ctypes.c_int64, _DP]),
     "sgfem_finalize": (ctypes.c_int, [_P]),
     "sgfem_has_lattice": (ctypes.c_int, [_P]),
+    "sgfem_update_coupling": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int64, _I64P, _I64P, _DP]),
     "sgfem_lattice_log": (ctypes.c_char_p, [_P]),
     "sgfem_apply": (ctypes.c_int, [_P, _DP, _DP, ctypes.c_int]),
     "sgfem_precondition": (ctypes.c_int, [_P, _DP, _DP, ctypes.c_int, ctypes.c_int]),
@@ -200,6 +201,13 @@ class Context:
     def set_coupling(self, G, P, M):
         colptr, rowval, nzval = _csc_arrays(G)
         self._check(self.lib.sgfem_set_coupling(self.h, int(P), int(M), _i64p(colptr), _i64p(rowval), _dp(nzval)))
+        self.P = P
+
+    def update_coupling(self, G, P, M):
+        """New modes on a finalized context (sgfem_update_coupling)."""
+        colptr, rowval, nzval = _csc_arrays(G)
+        self._check(self.lib.sgfem_update_coupling(self.h, int(P), int(M), _i64p(colptr), _i64p(rowval),
+                                                   _dp(nzval)))
         self.P = P
 
     def set_samples(self, y):

@@ -146,10 +146,8 @@ extern "C" int sgfem_set_spatial_matrix(sgfem_context* ctx, int m, int64_t n, co
     return SGFEM_OK;
 }
 
-extern "C" int sgfem_set_coupling(sgfem_context* ctx, int64_t P, int64_t M, const int64_t* colptr,
-                                  const int64_t* rowval, const double* nzval) {
-    if (!ctx) return SGFEM_ERR_ARGUMENT;
-    SG_TRY(invalidate(ctx));
+static int parse_coupling(sgfem_context* ctx, int64_t P, int64_t M, const int64_t* colptr, const int64_t* rowval,
+                          const double* nzval) {
     if (P <= 0 || P > 32767 || M < 0 || M > 4095 || !colptr || (!rowval && colptr[P] > 1))
         return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "sgfem_set_coupling: bad sizes (P <= 32767, M <= 4095)");
     int64_t nnz = colptr[P] - 1;
@@ -167,6 +165,13 @@ extern "C" int sgfem_set_coupling(sgfem_context* ctx, int64_t P, int64_t M, cons
     ctx->M = M;
     ctx->has_G = true;
     return SGFEM_OK;
+}
+
+extern "C" int sgfem_set_coupling(sgfem_context* ctx, int64_t P, int64_t M, const int64_t* colptr,
+                                  const int64_t* rowval, const double* nzval) {
+    if (!ctx) return SGFEM_ERR_ARGUMENT;
+    SG_TRY(invalidate(ctx));
+    return parse_coupling(ctx, P, M, colptr, rowval, nzval);
 }
 
 static int upload_samples(sgfem_context* ctx);
@@ -353,6 +358,233 @@ static int upload_samples(sgfem_context* ctx) {
 }
 
 
+// row stride of SG vectors in the device layout: P rounded up to `align` values
+static void set_ld(sgfem_context* ctx) {
+    const char* ea = getenv("SGFEM_LD_ALIGN");
+    int align = ea ? atoi(ea) : 4;
+    if (align != 4 && align != 8 && align != 16 && align != 32) align = 4;
+    ctx->ld = (ctx->P + align - 1) / align * align;
+}
+
+// Coupling-dependent state of a finalized context (everything that depends on G
+// and P): device column order, pair list and combination tables, slot tables
+// and lane schedule of the specialised FP32 apply.  val64 (nnz x M1) is given at
+// finalize to build the padded FP32 values; a coupling update passes nullptr and
+// keeps them.
+static int build_coupling(sgfem_context* ctx, const std::vector<double>* val64, int64_t nnz) {
+        const int64_t M = ctx->M, P = ctx->P;
+    // ---- coupling structure from G ((M*P) x P, CSC): entry (row = m'*P + mu, col = nu), m = m'+1
+        std::vector<std::vector<char>> nzcol(M + 1, std::vector<char>(P, 0));
+        struct GE { int m; int mu; int nu; double g; };
+        std::vector<GE> ges;
+        for (int64_t nu = 0; nu < P; ++nu)
+            for (int64_t k = ctx->G_colptr[nu]; k < ctx->G_colptr[nu + 1]; ++k) {
+                double g = ctx->G_val[k];
+                if (g == 0.0) continue;  // the reference skips zero couplings (solvers_poisson_primal.jl:111)
+                int64_t r = ctx->G_rowval[k];
+                int m = (int)(r / P) + 1;
+                int mu = (int)(r % P);
+                nzcol[m][nu] = 1;
+                ges.push_back({m, mu, (int)nu, g});
+            }
+    
+        // ---- device column order of the modes (sg_mode_order): packs the coupled
+        // columns of each pair of KLE terms into few 32-column groups
+        std::vector<int32_t> mode_of_col;  // device column -> caller mode
+        sg_mode_order(ctx, nzcol, mode_of_col);
+        ctx->imode.assign(P, 0);
+        for (int64_t c = 0; c < P; ++c) ctx->imode[mode_of_col[c]] = (int32_t)c;
+        const std::vector<int32_t>& imode = ctx->imode;
+    
+        // pair list Q in device columns: (0, c) for all c, then (m, c) for nonzero columns of G_m
+        std::vector<int32_t> qtab;
+        std::map<std::pair<int, int>, int> qidx;
+        for (int64_t c = 0; c < P; ++c) {
+            qidx[{0, (int)c}] = (int)qtab.size();
+            qtab.push_back((int32_t)c);
+        }
+        for (int64_t m = 1; m <= M; ++m)
+            for (int64_t c = 0; c < P; ++c)
+                if (nzcol[m][mode_of_col[c]]) {
+                    qidx[{(int)m, (int)c}] = (int)qtab.size();
+                    qtab.push_back((int32_t)((m << 16) | c));
+                }
+        ctx->Qn = (int)qtab.size();
+        for (GE& e : ges) {
+            e.mu = imode[e.mu];
+            e.nu = imode[e.nu];
+        }
+        std::sort(ges.begin(), ges.end(), [](const GE& a, const GE& b) {
+            if (a.mu != b.mu) return a.mu < b.mu;
+            if (a.m != b.m) return a.m < b.m;
+            return a.nu < b.nu;
+        });
+        std::vector<int32_t> combptr(P + 1, 0), combq;
+        std::vector<double> combg;
+        for (const GE& e : ges) {
+            combptr[e.mu + 1]++;
+            combq.push_back(qidx[{e.m, e.nu}]);
+            combg.push_back(e.g);
+        }
+        for (int64_t mu = 0; mu < P; ++mu) combptr[mu + 1] += combptr[mu];
+        ctx->ncomb = (int)combq.size();
+        std::vector<float> combg32(combg.begin(), combg.end());
+    
+        // ---- slot tables of the specialised FP32 apply: slot (pair p = m/2, group k = c/32)
+        // exists if some column of group k couples to K_2p or K_2p+1 (K_0 couples to all).
+        // The column groups are split into jit_np passes (contiguous group ranges with
+        // balanced slot counts); a pass keeps only its own slots' accumulators.  Slots are
+        // numbered pass by pass; jit_pass_slot0[p] is the first slot of pass p.
+        sg_jit_configure(ctx);
+        const int KG = (int)((P + 31) / 32);
+        const int NPAIR = (ctx->M1 + 1) / 2;
+        ctx->M1P = (ctx->M1 + 3) / 4 * 4;
+        std::vector<std::vector<char>> needs(NPAIR, std::vector<char>(KG, 0));
+        std::vector<int> slots_in_group(KG, 0);
+        for (int pr = 0; pr < NPAIR; ++pr)
+            for (int k = 0; k < KG; ++k) {
+                bool need = false;
+                for (int c = 32 * k; c < std::min<int64_t>(P, 32 * k + 32) && !need; ++c)
+                    for (int m = 2 * pr; m <= std::min<int64_t>(M, 2 * pr + 1) && !need; ++m)
+                        need = (m == 0) || nzcol[m][mode_of_col[c]];
+                needs[pr][k] = need;
+                slots_in_group[k] += need;
+            }
+        const int np = std::max(1, std::min(ctx->jit_np_req, KG));
+        ctx->jit_pass_k0.assign(np + 1, KG);
+        {
+            int total = 0;
+            for (int k = 0; k < KG; ++k) total += slots_in_group[k];
+            int p = 0, acc = 0;
+            ctx->jit_pass_k0[0] = 0;
+            for (int k = 0; k < KG; ++k) {
+                // close pass p once it holds its share and groups remain for the others
+                if (p + 1 < np && acc > 0 && acc + slots_in_group[k] / 2 > (long long)total * (p + 1) / np &&
+                    KG - k >= np - p - 1) {
+                    ctx->jit_pass_k0[++p] = k;
+                }
+                acc += slots_in_group[k];
+            }
+            for (int q = p + 1; q <= np; ++q) ctx->jit_pass_k0[q] = KG;
+            ctx->jit_np = p + 1;
+            ctx->jit_pass_k0.resize(ctx->jit_np + 1);
+            ctx->jit_pass_k0[ctx->jit_np] = KG;
+        }
+        std::vector<int> pass_of_k(KG, 0);
+        for (int p = 0; p < ctx->jit_np; ++p)
+            for (int k = ctx->jit_pass_k0[p]; k < ctx->jit_pass_k0[p + 1]; ++k) pass_of_k[k] = p;
+        ctx->jit_slot_of.assign((size_t)NPAIR * KG, -1);
+        ctx->jit_slots.clear();
+        ctx->jit_pass_slot0.assign(ctx->jit_np + 1, 0);
+        for (int p = 0; p < ctx->jit_np; ++p) {
+            ctx->jit_pass_slot0[p] = (int)ctx->jit_slots.size();
+            for (int pr = 0; pr < NPAIR; ++pr)
+                for (int k = ctx->jit_pass_k0[p]; k < ctx->jit_pass_k0[p + 1]; ++k)
+                    if (needs[pr][k]) {
+                        ctx->jit_slot_of[(size_t)pr * KG + k] = (int)ctx->jit_slots.size();
+                        ctx->jit_slots.push_back({pr, k});
+                    }
+        }
+        ctx->jit_pass_slot0[ctx->jit_np] = (int)ctx->jit_slots.size();
+        // sacc offset of F(m, c) within its pass's accumulator block
+        auto slot_off = [&](int m, int c) {
+            const int sl = ctx->jit_slot_of[(size_t)(m / 2) * KG + c / 32];
+            const int ls = sl - ctx->jit_pass_slot0[pass_of_k[c / 32]];
+            return ls * 64 + 2 * (c % 32) + (m % 2);
+        };
+        auto pass_of = [&](int c) { return pass_of_k[c / 32]; };
+        // combination list per output column: (1, acc(0, c)) then (g, acc(m, nu)); jpass is
+        // the pass whose accumulators hold the entry
+        std::vector<int32_t> jptr(P + 1, 0), joff, jpass;
+        std::vector<float> jg;
+        for (int64_t c = 0; c < P; ++c) {
+            joff.push_back(slot_off(0, (int)c));
+            jpass.push_back(pass_of((int)c));
+            jg.push_back(1.0f);
+            for (int32_t e = combptr[c]; e < combptr[c + 1]; ++e) {
+                int q = combq[e];
+                int m = qtab[q] >> 16, nu = qtab[q] & 0xffff;
+                joff.push_back(slot_off(m, nu));
+                jpass.push_back(pass_of(nu));
+                jg.push_back((float)combg[e]);
+            }
+            jptr[c + 1] = (int32_t)joff.size();
+        }
+        std::vector<float> val32p;
+        if (val64) {  // the padded FP32 values depend on the K_m only: kept by a coupling update
+            val32p.assign((size_t)nnz * ctx->M1P, 0.0f);
+            for (int64_t k = 0; k < nnz; ++k)
+                for (int m = 0; m < ctx->M1; ++m)
+                    val32p[(size_t)k * ctx->M1P + m] = (float)(*val64)[(size_t)k * ctx->M1 + m];
+        }
+        SG_TRY(upload(ctx, &ctx->d_jptr, jptr.data(), jptr.size()));
+        SG_TRY(upload(ctx, &ctx->d_joff, joff.data(), joff.size()));
+        SG_TRY(upload(ctx, &ctx->d_jg, jg.data(), jg.size()));
+        // lane schedule of the combination: columns assigned to the 32 lanes longest
+        // first (each to the least loaded lane); per lane its columns' entries in
+        // sequence, padded to a common length T; entry (i, lane) at [i * 32 + lane]
+        // x = sacc offset | column << 13 | (last entry of the column) << 28, y = g bits
+        {
+            std::vector<int> order(P);
+            std::iota(order.begin(), order.end(), 0);
+            std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+                return (jptr[a + 1] - jptr[a]) > (jptr[b + 1] - jptr[b]);
+            });
+            const int NPS = ctx->jit_np;
+            // lanes[p][l]: lane l's entries of pass p; a column stays on one lane in every pass
+            std::vector<std::vector<std::vector<int2>>> lanes(NPS, std::vector<std::vector<int2>>(32));
+            std::vector<size_t> load(32, 0);
+            for (int c : order) {
+                int best = 0;
+                for (int l = 1; l < 32; ++l)
+                    if (load[l] < load[best]) best = l;
+                load[best] += jptr[c + 1] - jptr[c];
+                for (int p = 0; p < NPS; ++p) {
+                    int lastp = -1;
+                    for (int32_t e = jptr[c]; e < jptr[c + 1]; ++e)
+                        if (jpass[e] == p) lastp = e;
+                    for (int32_t e = jptr[c]; e < jptr[c + 1]; ++e) {
+                        if (jpass[e] != p) continue;
+                        int bits;
+                        std::memcpy(&bits, &jg[e], sizeof(int));
+                        const bool last = (e == lastp);
+                        lanes[p][best].push_back(make_int2(joff[e] | (int)(c << 13) | ((last ? 1 : 0) << 28), bits));
+                    }
+                }
+            }
+            ctx->jit_pass_T.assign(NPS, 0);
+            size_t T = 0;
+            for (int p = 0; p < NPS; ++p) {
+                size_t tp = 0;
+                for (auto& l : lanes[p]) tp = std::max(tp, l.size());
+                ctx->jit_pass_T[p] = (int)tp;
+                T += tp;
+            }
+            ctx->jit_T = (int)T;
+            std::vector<int2> jtab(std::max<size_t>(T, 1) * 32, make_int2(0, 0));
+            size_t off = 0;
+            for (int p = 0; p < NPS; ++p) {
+                for (int l = 0; l < 32; ++l)
+                    for (size_t i = 0; i < lanes[p][l].size(); ++i) jtab[(off + i) * 32 + l] = lanes[p][l][i];
+                off += ctx->jit_pass_T[p];
+            }
+            int maxps = 0;
+            for (int p = 0; p < NPS; ++p) maxps = std::max(maxps, ctx->jit_pass_slot0[p + 1] - ctx->jit_pass_slot0[p]);
+            const bool fits = ((size_t)maxps * 64 <= 8192) && P <= 32767;
+            if (!fits) ctx->jit_T = -1;
+            SG_TRY(upload(ctx, &ctx->d_jtab, jtab.data(), jtab.size()));
+        }
+        if (val64) SG_TRY(upload(ctx, &ctx->d_val32p, val32p.data(), val32p.size()));
+        ctx->mode_of_col = mode_of_col;
+        SG_TRY(upload(ctx, &ctx->d_mode_of_col, mode_of_col.data(), mode_of_col.size()));
+        SG_TRY(upload(ctx, &ctx->d_qtab, qtab.data(), qtab.size()));
+        SG_TRY(upload(ctx, &ctx->d_combptr, combptr.data(), combptr.size()));
+        SG_TRY(upload(ctx, &ctx->d_combq, combq.data(), combq.size()));
+        SG_TRY(upload(ctx, &ctx->d_combg64, combg.data(), combg.size()));
+        SG_TRY(upload(ctx, &ctx->d_combg32, combg32.data(), combg32.size()));
+    return SGFEM_OK;
+}
+
 extern "C" int sgfem_finalize(sgfem_context* ctx) {
     if (!ctx) return SGFEM_ERR_ARGUMENT;
     SG_TRY(invalidate(ctx));
@@ -364,13 +596,7 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
     for (int64_t m = 0; m <= M; ++m)
         if (!ctx->mats[m].set) return sg_fail(ctx, SGFEM_ERR_STATE, "spatial matrix K_" + std::to_string(m) + " not set");
     ctx->M1 = (int)(M + 1);
-    {
-        // row stride of SG vectors in the device layout: P rounded up to `align` values
-        const char* ea = getenv("SGFEM_LD_ALIGN");
-        int align = ea ? atoi(ea) : 4;
-        if (align != 4 && align != 8 && align != 16 && align != 32) align = 4;
-        ctx->ld = (P + align - 1) / align * align;
-    }
+    set_ld(ctx);
     for (int64_t b : ctx->bdofs)
         if (b < 0 || b >= n) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "boundary dof out of range");
 
@@ -509,211 +735,7 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
         SG_TRY(upload_samples(ctx));
         ctx->Qn = 0;
     } else {
-    // ---- coupling structure from G ((M*P) x P, CSC): entry (row = m'*P + mu, col = nu), m = m'+1
-        std::vector<std::vector<char>> nzcol(M + 1, std::vector<char>(P, 0));
-        struct GE { int m; int mu; int nu; double g; };
-        std::vector<GE> ges;
-        for (int64_t nu = 0; nu < P; ++nu)
-            for (int64_t k = ctx->G_colptr[nu]; k < ctx->G_colptr[nu + 1]; ++k) {
-                double g = ctx->G_val[k];
-                if (g == 0.0) continue;  // the reference skips zero couplings (solvers_poisson_primal.jl:111)
-                int64_t r = ctx->G_rowval[k];
-                int m = (int)(r / P) + 1;
-                int mu = (int)(r % P);
-                nzcol[m][nu] = 1;
-                ges.push_back({m, mu, (int)nu, g});
-            }
-    
-        // ---- device column order of the modes (sg_mode_order): packs the coupled
-        // columns of each pair of KLE terms into few 32-column groups
-        std::vector<int32_t> mode_of_col;  // device column -> caller mode
-        sg_mode_order(ctx, nzcol, mode_of_col);
-        ctx->imode.assign(P, 0);
-        for (int64_t c = 0; c < P; ++c) ctx->imode[mode_of_col[c]] = (int32_t)c;
-        const std::vector<int32_t>& imode = ctx->imode;
-    
-        // pair list Q in device columns: (0, c) for all c, then (m, c) for nonzero columns of G_m
-        std::vector<int32_t> qtab;
-        std::map<std::pair<int, int>, int> qidx;
-        for (int64_t c = 0; c < P; ++c) {
-            qidx[{0, (int)c}] = (int)qtab.size();
-            qtab.push_back((int32_t)c);
-        }
-        for (int64_t m = 1; m <= M; ++m)
-            for (int64_t c = 0; c < P; ++c)
-                if (nzcol[m][mode_of_col[c]]) {
-                    qidx[{(int)m, (int)c}] = (int)qtab.size();
-                    qtab.push_back((int32_t)((m << 16) | c));
-                }
-        ctx->Qn = (int)qtab.size();
-        for (GE& e : ges) {
-            e.mu = imode[e.mu];
-            e.nu = imode[e.nu];
-        }
-        std::sort(ges.begin(), ges.end(), [](const GE& a, const GE& b) {
-            if (a.mu != b.mu) return a.mu < b.mu;
-            if (a.m != b.m) return a.m < b.m;
-            return a.nu < b.nu;
-        });
-        std::vector<int32_t> combptr(P + 1, 0), combq;
-        std::vector<double> combg;
-        for (const GE& e : ges) {
-            combptr[e.mu + 1]++;
-            combq.push_back(qidx[{e.m, e.nu}]);
-            combg.push_back(e.g);
-        }
-        for (int64_t mu = 0; mu < P; ++mu) combptr[mu + 1] += combptr[mu];
-        ctx->ncomb = (int)combq.size();
-        std::vector<float> combg32(combg.begin(), combg.end());
-    
-        // ---- slot tables of the specialised FP32 apply: slot (pair p = m/2, group k = c/32)
-        // exists if some column of group k couples to K_2p or K_2p+1 (K_0 couples to all).
-        // The column groups are split into jit_np passes (contiguous group ranges with
-        // balanced slot counts); a pass keeps only its own slots' accumulators.  Slots are
-        // numbered pass by pass; jit_pass_slot0[p] is the first slot of pass p.
-        sg_jit_configure(ctx);
-        const int KG = (int)((P + 31) / 32);
-        const int NPAIR = (ctx->M1 + 1) / 2;
-        ctx->M1P = (ctx->M1 + 3) / 4 * 4;
-        std::vector<std::vector<char>> needs(NPAIR, std::vector<char>(KG, 0));
-        std::vector<int> slots_in_group(KG, 0);
-        for (int pr = 0; pr < NPAIR; ++pr)
-            for (int k = 0; k < KG; ++k) {
-                bool need = false;
-                for (int c = 32 * k; c < std::min<int64_t>(P, 32 * k + 32) && !need; ++c)
-                    for (int m = 2 * pr; m <= std::min<int64_t>(M, 2 * pr + 1) && !need; ++m)
-                        need = (m == 0) || nzcol[m][mode_of_col[c]];
-                needs[pr][k] = need;
-                slots_in_group[k] += need;
-            }
-        const int np = std::max(1, std::min(ctx->jit_np_req, KG));
-        ctx->jit_pass_k0.assign(np + 1, KG);
-        {
-            int total = 0;
-            for (int k = 0; k < KG; ++k) total += slots_in_group[k];
-            int p = 0, acc = 0;
-            ctx->jit_pass_k0[0] = 0;
-            for (int k = 0; k < KG; ++k) {
-                // close pass p once it holds its share and groups remain for the others
-                if (p + 1 < np && acc > 0 && acc + slots_in_group[k] / 2 > (long long)total * (p + 1) / np &&
-                    KG - k >= np - p - 1) {
-                    ctx->jit_pass_k0[++p] = k;
-                }
-                acc += slots_in_group[k];
-            }
-            for (int q = p + 1; q <= np; ++q) ctx->jit_pass_k0[q] = KG;
-            ctx->jit_np = p + 1;
-            ctx->jit_pass_k0.resize(ctx->jit_np + 1);
-            ctx->jit_pass_k0[ctx->jit_np] = KG;
-        }
-        std::vector<int> pass_of_k(KG, 0);
-        for (int p = 0; p < ctx->jit_np; ++p)
-            for (int k = ctx->jit_pass_k0[p]; k < ctx->jit_pass_k0[p + 1]; ++k) pass_of_k[k] = p;
-        ctx->jit_slot_of.assign((size_t)NPAIR * KG, -1);
-        ctx->jit_slots.clear();
-        ctx->jit_pass_slot0.assign(ctx->jit_np + 1, 0);
-        for (int p = 0; p < ctx->jit_np; ++p) {
-            ctx->jit_pass_slot0[p] = (int)ctx->jit_slots.size();
-            for (int pr = 0; pr < NPAIR; ++pr)
-                for (int k = ctx->jit_pass_k0[p]; k < ctx->jit_pass_k0[p + 1]; ++k)
-                    if (needs[pr][k]) {
-                        ctx->jit_slot_of[(size_t)pr * KG + k] = (int)ctx->jit_slots.size();
-                        ctx->jit_slots.push_back({pr, k});
-                    }
-        }
-        ctx->jit_pass_slot0[ctx->jit_np] = (int)ctx->jit_slots.size();
-        // sacc offset of F(m, c) within its pass's accumulator block
-        auto slot_off = [&](int m, int c) {
-            const int sl = ctx->jit_slot_of[(size_t)(m / 2) * KG + c / 32];
-            const int ls = sl - ctx->jit_pass_slot0[pass_of_k[c / 32]];
-            return ls * 64 + 2 * (c % 32) + (m % 2);
-        };
-        auto pass_of = [&](int c) { return pass_of_k[c / 32]; };
-        // combination list per output column: (1, acc(0, c)) then (g, acc(m, nu)); jpass is
-        // the pass whose accumulators hold the entry
-        std::vector<int32_t> jptr(P + 1, 0), joff, jpass;
-        std::vector<float> jg;
-        for (int64_t c = 0; c < P; ++c) {
-            joff.push_back(slot_off(0, (int)c));
-            jpass.push_back(pass_of((int)c));
-            jg.push_back(1.0f);
-            for (int32_t e = combptr[c]; e < combptr[c + 1]; ++e) {
-                int q = combq[e];
-                int m = qtab[q] >> 16, nu = qtab[q] & 0xffff;
-                joff.push_back(slot_off(m, nu));
-                jpass.push_back(pass_of(nu));
-                jg.push_back((float)combg[e]);
-            }
-            jptr[c + 1] = (int32_t)joff.size();
-        }
-        std::vector<float> val32p((size_t)nnz * ctx->M1P, 0.0f);
-        for (int64_t k = 0; k < nnz; ++k)
-            for (int m = 0; m < ctx->M1; ++m) val32p[(size_t)k * ctx->M1P + m] = (float)val64[(size_t)k * ctx->M1 + m];
-        SG_TRY(upload(ctx, &ctx->d_jptr, jptr.data(), jptr.size()));
-        SG_TRY(upload(ctx, &ctx->d_joff, joff.data(), joff.size()));
-        SG_TRY(upload(ctx, &ctx->d_jg, jg.data(), jg.size()));
-        // lane schedule of the combination: columns assigned to the 32 lanes longest
-        // first (each to the least loaded lane); per lane its columns' entries in
-        // sequence, padded to a common length T; entry (i, lane) at [i * 32 + lane]
-        // x = sacc offset | column << 13 | (last entry of the column) << 28, y = g bits
-        {
-            std::vector<int> order(P);
-            std::iota(order.begin(), order.end(), 0);
-            std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-                return (jptr[a + 1] - jptr[a]) > (jptr[b + 1] - jptr[b]);
-            });
-            const int NPS = ctx->jit_np;
-            // lanes[p][l]: lane l's entries of pass p; a column stays on one lane in every pass
-            std::vector<std::vector<std::vector<int2>>> lanes(NPS, std::vector<std::vector<int2>>(32));
-            std::vector<size_t> load(32, 0);
-            for (int c : order) {
-                int best = 0;
-                for (int l = 1; l < 32; ++l)
-                    if (load[l] < load[best]) best = l;
-                load[best] += jptr[c + 1] - jptr[c];
-                for (int p = 0; p < NPS; ++p) {
-                    int lastp = -1;
-                    for (int32_t e = jptr[c]; e < jptr[c + 1]; ++e)
-                        if (jpass[e] == p) lastp = e;
-                    for (int32_t e = jptr[c]; e < jptr[c + 1]; ++e) {
-                        if (jpass[e] != p) continue;
-                        int bits;
-                        std::memcpy(&bits, &jg[e], sizeof(int));
-                        const bool last = (e == lastp);
-                        lanes[p][best].push_back(make_int2(joff[e] | (int)(c << 13) | ((last ? 1 : 0) << 28), bits));
-                    }
-                }
-            }
-            ctx->jit_pass_T.assign(NPS, 0);
-            size_t T = 0;
-            for (int p = 0; p < NPS; ++p) {
-                size_t tp = 0;
-                for (auto& l : lanes[p]) tp = std::max(tp, l.size());
-                ctx->jit_pass_T[p] = (int)tp;
-                T += tp;
-            }
-            ctx->jit_T = (int)T;
-            std::vector<int2> jtab(std::max<size_t>(T, 1) * 32, make_int2(0, 0));
-            size_t off = 0;
-            for (int p = 0; p < NPS; ++p) {
-                for (int l = 0; l < 32; ++l)
-                    for (size_t i = 0; i < lanes[p][l].size(); ++i) jtab[(off + i) * 32 + l] = lanes[p][l][i];
-                off += ctx->jit_pass_T[p];
-            }
-            int maxps = 0;
-            for (int p = 0; p < NPS; ++p) maxps = std::max(maxps, ctx->jit_pass_slot0[p + 1] - ctx->jit_pass_slot0[p]);
-            const bool fits = ((size_t)maxps * 64 <= 8192) && P <= 32767;
-            if (!fits) ctx->jit_T = -1;
-            SG_TRY(upload(ctx, &ctx->d_jtab, jtab.data(), jtab.size()));
-        }
-        SG_TRY(upload(ctx, &ctx->d_val32p, val32p.data(), val32p.size()));
-        ctx->mode_of_col = mode_of_col;
-        SG_TRY(upload(ctx, &ctx->d_mode_of_col, mode_of_col.data(), mode_of_col.size()));
-        SG_TRY(upload(ctx, &ctx->d_qtab, qtab.data(), qtab.size()));
-        SG_TRY(upload(ctx, &ctx->d_combptr, combptr.data(), combptr.size()));
-        SG_TRY(upload(ctx, &ctx->d_combq, combq.data(), combq.size()));
-        SG_TRY(upload(ctx, &ctx->d_combg64, combg.data(), combg.size()));
-        SG_TRY(upload(ctx, &ctx->d_combg32, combg32.data(), combg32.size()));
+        SG_TRY(build_coupling(ctx, &val64, nnz));
     }
 
     // ---- upload
@@ -752,7 +774,44 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
     return SGFEM_OK;
 }
 
-// ------------------------------------------------------------------ layout kernels
+// New modes (the adaptive loop appends multi-indices, scripts/poisson.jl:341-420,
+// mopcontrol.jl:60-132) change G and P but not the K_m: rebuild only the
+// coupling-dependent state of a finalized context.  M may not exceed the number
+// of K_m the context holds.
+extern "C" int sgfem_update_coupling(sgfem_context* ctx, int64_t P, int64_t M, const int64_t* colptr,
+                                     const int64_t* rowval, const double* nzval) {
+    if (!ctx) return SGFEM_ERR_ARGUMENT;
+    if (!ctx->finalized || ctx->batched)
+        return sg_fail(ctx, SGFEM_ERR_STATE, "sgfem_update_coupling: needs a finalized SG (not samples) context");
+    if (M > ctx->M1 - 1)
+        return sg_fail(ctx, SGFEM_ERR_STATE,
+                       "sgfem_update_coupling: more KLE terms than the context holds (finalize a new context)");
+    SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    SG_TRY(parse_coupling(ctx, P, M, colptr, rowval, nzval));
+    void** tabs[] = {(void**)&ctx->d_mode_of_col, (void**)&ctx->d_qtab, (void**)&ctx->d_combptr,
+                     (void**)&ctx->d_combq, (void**)&ctx->d_combg64, (void**)&ctx->d_combg32,
+                     (void**)&ctx->d_jptr, (void**)&ctx->d_joff, (void**)&ctx->d_jg, (void**)&ctx->d_jtab,
+                     (void**)&ctx->d_combgdf};
+    for (void** t : tabs) {
+        free_dev(*t);
+        *t = nullptr;
+    }
+    sg_jit_release(ctx);
+    ctx->jit_tried = false;
+    if (ctx->pcg_exec) cudaGraphExecDestroy(ctx->pcg_exec);
+    if (ctx->pcg_graph) cudaGraphDestroy(ctx->pcg_graph);
+    ctx->pcg_exec = nullptr;
+    ctx->pcg_graph = nullptr;
+    ctx->samples_x_valid = false;
+    set_ld(ctx);
+    SG_TRY(build_coupling(ctx, nullptr, ctx->nnz));
+    SG_TRY(sg_apply_configure(ctx));
+    ctx->jit_log = "not compiled yet (at the first FP32 apply)";
+    return SGFEM_OK;
+}
+
+// ------------------------------------------------------------------ layout kernels// ------------------------------------------------------------------ layout kernels
 // stage: caller layout, FP64, column-major n x P.  X: device layout (T), n x ld.
 // tile of 32 dofs x 32 device columns; column c holds caller mode mode_of_col[c]
 // (pad columns c >= P are written as zero)

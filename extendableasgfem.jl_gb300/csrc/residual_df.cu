@@ -264,13 +264,15 @@ bool sg_residual_df_usable(const sgfem_context* ctx) {
 }
 
 int sg_residual_df_prepare(sgfem_context* ctx) {
-    if (ctx->d_valdf) return SGFEM_OK;
-    const size_t nv = (size_t)ctx->nnz * ctx->M1;
-    SG_CUDA(ctx, cudaMalloc(&ctx->d_valdf, nv * sizeof(float2)));
-    SG_CUDA(ctx, cudaMalloc(&ctx->d_combgdf, std::max<size_t>(1, (size_t)ctx->ncomb) * sizeof(float2)));
+    if (ctx->d_valdf && ctx->d_combgdf) return SGFEM_OK;
     const int grid = ctx->num_sms * 8;
-    k_split_pairs<<<grid, 256, 0, ctx->stream>>>(ctx->d_val64, (float2*)ctx->d_valdf, nv);
-    SG_LAUNCHED(ctx);
+    if (!ctx->d_valdf) {  // the K_m (kept across coupling updates)
+        const size_t nv = (size_t)ctx->nnz * ctx->M1;
+        SG_CUDA(ctx, cudaMalloc(&ctx->d_valdf, nv * sizeof(float2)));
+        k_split_pairs<<<grid, 256, 0, ctx->stream>>>(ctx->d_val64, (float2*)ctx->d_valdf, nv);
+        SG_LAUNCHED(ctx);
+    }
+    SG_CUDA(ctx, cudaMalloc(&ctx->d_combgdf, std::max<size_t>(1, (size_t)ctx->ncomb) * sizeof(float2)));
     if (ctx->ncomb > 0) {
         k_split_pairs<<<grid, 256, 0, ctx->stream>>>(ctx->d_combg64, (float2*)ctx->d_combgdf, (size_t)ctx->ncomb);
         SG_LAUNCHED(ctx);

@@ -61,6 +61,20 @@ class SGOperator:
     def has_lattice(self):
         return self.ctx.has_lattice
 
+    def update_basis(self, TB):
+        """The adaptive loop appended modes: switch to the TensorizedBasis TB (same
+        spatial blocks; TB's multi-index length may not exceed len(Ks) - 1).  The
+        K_m, the dof numbering and the lattice preconditioner stay on the GPU."""
+        M = TB.maxlength_multiindices()
+        if M > self.M:
+            raise ValueError("update_basis: TB needs more KLE terms than this operator holds")
+        G = TB.G
+        if G.shape != (M * TB.nmodes, TB.nmodes):
+            raise ValueError("G must be (M*P) x P")
+        self.ctx.update_coupling(G, TB.nmodes, M)
+        self.TB = TB
+        self.P = TB.nmodes
+
     def mul(self, x, precision=_lib.FP64):
         """mul!(Ax, S, x) on SGFEVector.entries."""
         return self.ctx.apply(x, precision)

@@ -96,6 +96,15 @@ SGFEM_API int sgfem_set_boundary_dofs(sgfem_context* ctx, int64_t count, const i
    and the device numbering follows the lattice. */
 SGFEM_API int sgfem_set_dof_coordinates(sgfem_context* ctx, int64_t n, const double* xy);
 SGFEM_API int sgfem_finalize(sgfem_context* ctx);
+/* the adaptive loop appended modes (scripts/poisson.jl:341-420): new coupling G
+   ((M*P) x P, 1-based CSC as for sgfem_set_coupling) on a finalized context.  Only
+   the coupling-dependent state is rebuilt (device column order, pair and
+   combination tables, the specialised FP32 apply); the K_m, the dof numbering and
+   the lattice preconditioner stay resident.  M must not exceed the number of K_m
+   set before finalize minus one.  Device vectors of the old layout are invalid
+   afterwards. */
+SGFEM_API int sgfem_update_coupling(sgfem_context* ctx, int64_t P, int64_t M, const int64_t* colptr,
+                                    const int64_t* rowval, const double* nzval);
 /* 1 if the lattice preconditioner is available after finalize */
 SGFEM_API int sgfem_has_lattice(const sgfem_context* ctx);
 /* which mean-based lattice preconditioner a finalized context applies: the exact
