@@ -30,7 +30,8 @@ constexpr int KMAX = 128;  // largest restart + 1
 
 template <typename T>
 __global__ void __launch_bounds__(GT) k_mdot(const T* __restrict__ V, size_t total, int k, const T* __restrict__ w,
-                                             double* __restrict__ partials) {
+                                             double* __restrict__ partials, const KrylovScalars* __restrict__ scal) {
+    if (scal && scal->done) return;
     __shared__ double red[GT / 32][8];
     const int i0 = blockIdx.y * 8;
     double acc[8];
@@ -71,10 +72,91 @@ __global__ void __launch_bounds__(GT) k_mdot_fin(const double* __restrict__ part
     if (threadIdx.x == 0) h[blockIdx.x] = red[0];
 }
 
+// device-side Arnoldi bookkeeping: the step's Hessenberg column, the rotations,
+// the residual estimate and the stop flag live in device memory, so a step needs
+// no host round trip (the host reads the state every few steps)
+struct ArnState {
+    double res;      // |g[k+1]| after the last completed step
+    double inv_nrm;  // 1 / ||w|| of the last step (scales the next basis vector)
+    int kk;          // completed steps of this cycle
+    int flag;        // 0 running, 1 converged or happy breakdown, 2 singular, 3 non-finite
+};
+
+// hneg[i] = -sum_b partials[i * nb + b]; hcol[i] (+)= the sum (CGS2 accumulates both rounds)
+__global__ void __launch_bounds__(GT) k_mdot_fin_neg(const double* __restrict__ partials, int nb, double* __restrict__ hneg,
+                                                     double* __restrict__ hcol, int accumulate,
+                                                     const KrylovScalars* __restrict__ scal) {
+    if (scal->done) return;
+    __shared__ double red[GT];
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nb; b += GT) v += partials[(size_t)blockIdx.x * nb + b];
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = GT / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        hneg[blockIdx.x] = -red[0];
+        hcol[blockIdx.x] = accumulate ? hcol[blockIdx.x] + red[0] : red[0];
+    }
+}
+
+// one thread: column k of the Hessenberg matrix from hcol and ||w||^2 = *nrm2,
+// rotations of the earlier steps, the new rotation, the residual estimate
+__global__ void k_givens(int k, const double* __restrict__ hcol, const double* __restrict__ nrm2, double* __restrict__ H,
+                         int ldh, double* __restrict__ cs, double* __restrict__ sn, double* __restrict__ g,
+                         ArnState* __restrict__ st, KrylovScalars* __restrict__ scal, double tol_abs) {
+    if (scal->done) return;
+    const double nrm = sqrt(*nrm2);
+    double* col = H + (size_t)k * ldh;
+    for (int i = 0; i <= k; ++i) col[i] = hcol[i];
+    for (int i = 0; i < k; ++i) {
+        const double a = col[i], c2 = col[i + 1];
+        col[i] = cs[i] * a + sn[i] * c2;
+        col[i + 1] = -sn[i] * a + cs[i] * c2;
+    }
+    const double r = hypot(col[k], nrm);
+    if (!isfinite(r)) {
+        st->flag = 3;
+        scal->done = 1;
+        return;
+    }
+    if (r == 0.0) {
+        st->flag = 2;
+        scal->done = 1;
+        return;
+    }
+    cs[k] = col[k] / r;
+    sn[k] = nrm / r;
+    col[k] = r;
+    col[k + 1] = 0.0;
+    g[k + 1] = -sn[k] * g[k];
+    g[k] = cs[k] * g[k];
+    st->res = fabs(g[k + 1]);
+    st->kk = k + 1;
+    st->inv_nrm = nrm > 0.0 ? 1.0 / nrm : 0.0;
+    if (st->res <= tol_abs || nrm == 0.0) {
+        st->flag = 1;
+        scal->done = 1;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(GT) k_scale_dev(T* __restrict__ dst, const T* __restrict__ src, size_t total,
+                                                  const ArnState* __restrict__ st, const KrylovScalars* __restrict__ scal) {
+    if (scal->done) return;
+    const double s = st->inv_nrm;
+    for (size_t t = (size_t)blockIdx.x * GT + threadIdx.x; t < total; t += (size_t)gridDim.x * GT)
+        dst[t] = (T)((double)src[t] * s);
+}
+
 // w = beta * w + sum_i c_i V_i   (beta = 0: w = V c)
 template <typename T>
 __global__ void __launch_bounds__(GT) k_lincomb(T* __restrict__ w, const T* __restrict__ V, size_t total, int k,
-                                                const double* __restrict__ c, double beta) {
+                                                const double* __restrict__ c, double beta,
+                                                const KrylovScalars* __restrict__ scal = nullptr) {
+    if (scal && scal->done) return;
     __shared__ double cs[KMAX];
     for (int i = threadIdx.x; i < k; i += GT) cs[i] = c[i];
     __syncthreads();
@@ -146,7 +228,7 @@ struct Gm {
     template <typename T>
     int dots(const T* V, int k, const T* w, double* out) {
         dim3 g((unsigned)nbx, (unsigned)((k + 7) / 8));
-        k_mdot<T><<<g, GT, 0, ctx->stream>>>(V, total, k, w, d_part);
+        k_mdot<T><<<g, GT, 0, ctx->stream>>>(V, total, k, w, d_part, nullptr);
         SG_LAUNCHED(ctx);
         k_mdot_fin<<<k, GT, 0, ctx->stream>>>(d_part, nbx, d_h);
         SG_LAUNCHED(ctx);
@@ -165,19 +247,19 @@ struct Gm {
 
     // z = B v (z's Dirichlet rows are left as they are: zero)
     template <typename T>
-    int precond(int precision, const T* v, T* z, T* tmp) {
+    int precond(int precision, const T* v, T* z, T* tmp, const KrylovScalars* scal = nullptr) {
         if (prec_kind == SGFEM_PREC_LATTICE) {
-            SG_TRY(sg_lat_pass_x(ctx, precision, v, tmp, nullptr));
-            SG_TRY(sg_lat_pass_y(ctx, precision, tmp, nullptr, nullptr, nullptr));
-            return sg_lat_pass_xinv(ctx, precision, tmp, z, 0, nullptr);
+            SG_TRY(sg_lat_pass_x(ctx, precision, v, tmp, scal));
+            SG_TRY(sg_lat_pass_y(ctx, precision, tmp, nullptr, nullptr, scal));
+            return sg_lat_pass_xinv(ctx, precision, tmp, z, 0, scal);
         }
-        return sg_jacobi(ctx, precision, v, z, 0, prec_kind == SGFEM_PREC_NONE ? 1 : 0, nullptr, nullptr, nullptr);
+        return sg_jacobi(ctx, precision, v, z, 0, prec_kind == SGFEM_PREC_NONE ? 1 : 0, nullptr, nullptr, scal);
     }
 
     template <typename T>
-    int apply(int precision, const T* x, T* y) {
+    int apply(int precision, const T* x, T* y, const KrylovScalars* scal = nullptr) {
         if (precision == SGFEM_FP64) applies64++;
-        return sg_launch_apply(ctx, precision, x, y, nullptr, nullptr, nullptr);
+        return sg_launch_apply(ctx, precision, x, y, nullptr, nullptr, scal);
     }
 
     // Restarted right-preconditioned GMRES on A x = b in precision T.  x holds the
@@ -206,58 +288,73 @@ struct Gm {
         if (!std::isfinite(beta)) return sg_fail(ctx, SGFEM_ERR_NONFINITE, "non-finite residual");
         if (beta <= tol_abs) return SGFEM_OK;
         const int m = restart;
-        std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), h(m + 1), h2(m + 1), y(m);
+        std::vector<double> H((size_t)(m + 1) * m, 0.0), g(m + 1), y(m);
         auto Hat = [&](int i, int j) -> double& { return H[(size_t)j * (m + 1) + i]; };
+        // device state of the Arnoldi steps
+        KrylovScalars* scal = ctx->d_scal;
+        double* d_hcol = d_h + KMAX;
+        double* d_H = d_hcol + KMAX;
+        double* d_cs = d_H + (size_t)(KMAX + 1) * KMAX;
+        double* d_sn = d_cs + KMAX;
+        double* d_g = d_sn + KMAX;
+        double* d_nrm2 = d_g + KMAX + 1;
+        ArnState* d_st = reinterpret_cast<ArnState*>(d_nrm2 + 1);
+        constexpr int CHK = 4;  // steps between host checks of the stop flag
         int it = 0;
         for (;;) {
             k_scale<T><<<grid, GT, 0, ctx->stream>>>(v0, v0, total, 1.0 / beta);
             SG_LAUNCHED(ctx);
             std::fill(g.begin(), g.end(), 0.0);
             g[0] = beta;
-            int kk = 0;
-            for (int k = 0; k < m; ++k) {
+            ArnState hs{beta, 0.0, 0, 0};
+            SG_CUDA(ctx, cudaMemcpyAsync(d_g, g.data(), (size_t)(m + 1) * sizeof(double), cudaMemcpyHostToDevice,
+                                         ctx->stream));
+            SG_CUDA(ctx, cudaMemcpyAsync(d_st, &hs, sizeof(ArnState), cudaMemcpyHostToDevice, ctx->stream));
+            SG_CUDA(ctx, cudaMemsetAsync(scal, 0, sizeof(KrylovScalars), ctx->stream));
+            const int kmax = std::min(m, maxit - it);
+            for (int k = 0; k < kmax; ++k) {
                 T* vk = V + (size_t)k * total;
                 T* vn = V + (size_t)(k + 1) * total;
                 T* zk = Z ? Z + (size_t)k * total : z;
-                SG_TRY(precond<T>(precision, vk, zk, tmp));
-                SG_TRY(apply<T>(precision, zk, w));
-                // CGS2
-                SG_TRY(dots<T>(V, k + 1, w, h.data()));
-                for (int i = 0; i <= k; ++i) h[i] = -h[i];
-                SG_CUDA(ctx, cudaMemcpyAsync(d_h, h.data(), (size_t)(k + 1) * sizeof(double), cudaMemcpyHostToDevice,
-                                             ctx->stream));
-                k_lincomb<T><<<grid, GT, 0, ctx->stream>>>(w, V, total, k + 1, d_h, 1.0);
-                SG_LAUNCHED(ctx);
-                SG_TRY(dots<T>(V, k + 1, w, h2.data()));
-                for (int i = 0; i <= k; ++i) h2[i] = -h2[i];
-                SG_CUDA(ctx, cudaMemcpyAsync(d_h, h2.data(), (size_t)(k + 1) * sizeof(double), cudaMemcpyHostToDevice,
-                                             ctx->stream));
-                k_lincomb<T><<<grid, GT, 0, ctx->stream>>>(w, V, total, k + 1, d_h, 1.0);
-                SG_LAUNCHED(ctx);
-                double nrm = 0.0;
-                SG_TRY(norm<T>(w, &nrm));
-                for (int i = 0; i <= k; ++i) Hat(i, k) = -(h[i] + h2[i]);
-                Hat(k + 1, k) = nrm;
-                for (int i = 0; i < k; ++i) {
-                    const double a = Hat(i, k), c2 = Hat(i + 1, k);
-                    Hat(i, k) = cs[i] * a + sn[i] * c2;
-                    Hat(i + 1, k) = -sn[i] * a + cs[i] * c2;
+                SG_TRY(precond<T>(precision, vk, zk, tmp, scal));
+                SG_TRY(apply<T>(precision, zk, w, scal));
+                // CGS2: twice w -= V (V^T w), the column accumulating both projections
+                for (int round = 0; round < 2; ++round) {
+                    dim3 gd((unsigned)nbx, (unsigned)((k + 1 + 7) / 8));
+                    k_mdot<T><<<gd, GT, 0, ctx->stream>>>(V, total, k + 1, w, d_part, scal);
+                    SG_LAUNCHED(ctx);
+                    k_mdot_fin_neg<<<k + 1, GT, 0, ctx->stream>>>(d_part, nbx, d_h, d_hcol, round, scal);
+                    SG_LAUNCHED(ctx);
+                    k_lincomb<T><<<grid, GT, 0, ctx->stream>>>(w, V, total, k + 1, d_h, 1.0, scal);
+                    SG_LAUNCHED(ctx);
                 }
-                const double r = std::hypot(Hat(k, k), nrm);
-                if (!std::isfinite(r)) return sg_fail(ctx, SGFEM_ERR_NONFINITE, "non-finite value in a GMRES iterate");
-                if (r == 0.0) return sg_fail(ctx, SGFEM_ERR_BREAKDOWN, "GMRES breakdown (singular Hessenberg column)");
-                cs[k] = Hat(k, k) / r;
-                sn[k] = nrm / r;
-                Hat(k, k) = r;
-                Hat(k + 1, k) = 0.0;
-                g[k + 1] = -sn[k] * g[k];
-                g[k] = cs[k] * g[k];
-                ++it;
-                kk = k + 1;
-                if (std::fabs(g[k + 1]) <= tol_abs || nrm == 0.0 || it >= maxit) break;
-                k_scale<T><<<grid, GT, 0, ctx->stream>>>(vn, w, total, 1.0 / nrm);
+                k_mdot<T><<<dim3((unsigned)nbx, 1), GT, 0, ctx->stream>>>(w, total, 1, w, d_part, scal);
                 SG_LAUNCHED(ctx);
+                k_mdot_fin<<<1, GT, 0, ctx->stream>>>(d_part, nbx, d_nrm2);
+                SG_LAUNCHED(ctx);
+                k_givens<<<1, 1, 0, ctx->stream>>>(k, d_hcol, d_nrm2, d_H, m + 1, d_cs, d_sn, d_g, d_st, scal, tol_abs);
+                SG_LAUNCHED(ctx);
+                k_scale_dev<T><<<grid, GT, 0, ctx->stream>>>(vn, w, total, d_st, scal);
+                SG_LAUNCHED(ctx);
+                if ((k + 1) % CHK == 0 || k + 1 == kmax) {
+                    SG_CUDA(ctx, cudaMemcpyAsync(&hs, d_st, sizeof(ArnState), cudaMemcpyDeviceToHost, ctx->stream));
+                    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+                    if (hs.flag) break;
+                }
             }
+            if (hs.flag == 2) return sg_fail(ctx, SGFEM_ERR_BREAKDOWN, "GMRES breakdown (singular Hessenberg column)");
+            if (hs.flag == 3) return sg_fail(ctx, SGFEM_ERR_NONFINITE, "non-finite value in a GMRES iterate");
+            const int kk = hs.kk;
+            it += kk;
+            if (kk == 0) {
+                *iters = it;
+                return SGFEM_ERR_MAXIT;
+            }
+            SG_CUDA(ctx, cudaMemcpyAsync(H.data(), d_H, (size_t)(m + 1) * kk * sizeof(double), cudaMemcpyDeviceToHost,
+                                         ctx->stream));
+            SG_CUDA(ctx, cudaMemcpyAsync(g.data(), d_g, (size_t)(kk + 1) * sizeof(double), cudaMemcpyDeviceToHost,
+                                         ctx->stream));
+            SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
             // y = H^-1 g, x += B (V y)
             for (int i = kk - 1; i >= 0; --i) {
                 double s = g[i];
@@ -326,7 +423,9 @@ extern "C" int sgfem_solve_gmres(sgfem_context* ctx, const double* b0, double* x
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)((total + GT * 4 - 1) / (GT * 4)),
                                                                  (int64_t)ctx->num_sms * 8));
     const int nbx = std::min(grid, ctx->num_sms * 4);
-    SG_TRY(sg_ensure(ctx, ctx->w_gsmall, ((size_t)KMAX * nbx + KMAX) * sizeof(double)));
+    // partials | h | Hessenberg column | H | cs | sn | g | ||w||^2 | Arnoldi state
+    SG_TRY(sg_ensure(ctx, ctx->w_gsmall,
+                     ((size_t)KMAX * nbx + 2 * KMAX + (size_t)(KMAX + 1) * KMAX + 3 * KMAX + 1 + 1 + 8) * sizeof(double)));
     Gm G{ctx, o.preconditioner, total, nbx, (double*)ctx->w_gsmall.p, (double*)ctx->w_gsmall.p + (size_t)KMAX * nbx,
          grid};
 
