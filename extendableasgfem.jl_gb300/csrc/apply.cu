@@ -94,6 +94,7 @@ k_apply(const int* __restrict__ rowptr, const int* __restrict__ col, const T* __
         }
         __syncwarp();
         const T* xrow = X + (size_t)row * ld;
+        T rowdot = T(0);  // per-row products in the working precision, rows summed in FP64
         for (int mu = lane; mu < ld; mu += 32) {
             T y = T(0);
             if (mu < P) {
@@ -101,8 +102,9 @@ k_apply(const int* __restrict__ rowptr, const int* __restrict__ col, const T* __
                 for (int e = combptr[mu]; e < combptr[mu + 1]; ++e) y = fma(combg[e], sacc[combq[e]], y);
             }
             yrow[mu] = y;
-            if (partials) dot += (double)xrow[mu] * (double)y;
+            if (partials) rowdot = fma(xrow[mu], y, rowdot);
         }
+        dot += (double)rowdot;
         __syncwarp();
     }
     if (partials) {

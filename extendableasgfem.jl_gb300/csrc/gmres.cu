@@ -34,19 +34,21 @@ __global__ void __launch_bounds__(GT) k_mdot(const T* __restrict__ V, size_t tot
     if (scal && scal->done) return;
     __shared__ double red[GT / 32][8];
     const int i0 = blockIdx.y * 8;
-    double acc[8];
+    // per-thread partials in the vectors' precision (GB300's FP64 rate is 1/64 of
+    // FP32), block and grid sums in FP64
+    T acc[8];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) acc[i] = 0.0;
+    for (int i = 0; i < 8; ++i) acc[i] = T(0);
     for (size_t t = (size_t)blockIdx.x * GT + threadIdx.x; t < total; t += (size_t)gridDim.x * GT) {
-        const double wv = (double)w[t];
+        const T wv = w[t];
 #pragma unroll
         for (int i = 0; i < 8; ++i)
-            if (i0 + i < k) acc[i] = fma((double)V[(size_t)(i0 + i) * total + t], wv, acc[i]);
+            if (i0 + i < k) acc[i] = fma(V[(size_t)(i0 + i) * total + t], wv, acc[i]);
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-        double a = acc[i];
+        double a = (double)acc[i];
         for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
         if (lane == 0) red[warp][i] = a;
     }
@@ -157,13 +159,14 @@ __global__ void __launch_bounds__(GT) k_lincomb(T* __restrict__ w, const T* __re
                                                 const double* __restrict__ c, double beta,
                                                 const KrylovScalars* __restrict__ scal = nullptr) {
     if (scal && scal->done) return;
-    __shared__ double cs[KMAX];
-    for (int i = threadIdx.x; i < k; i += GT) cs[i] = c[i];
+    __shared__ T cs[KMAX];  // coefficients in the vectors' precision
+    for (int i = threadIdx.x; i < k; i += GT) cs[i] = (T)c[i];
     __syncthreads();
+    const T bt = (T)beta;
     for (size_t t = (size_t)blockIdx.x * GT + threadIdx.x; t < total; t += (size_t)gridDim.x * GT) {
-        double a = beta == 0.0 ? 0.0 : beta * (double)w[t];
-        for (int i = 0; i < k; ++i) a = fma(cs[i], (double)V[(size_t)i * total + t], a);
-        w[t] = (T)a;
+        T a = beta == 0.0 ? T(0) : bt * w[t];
+        for (int i = 0; i < k; ++i) a = fma(cs[i], V[(size_t)i * total + t], a);
+        w[t] = a;
     }
 }
 
