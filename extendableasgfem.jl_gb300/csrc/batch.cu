@@ -39,7 +39,20 @@ struct BProb {
     const int* combptr;
     const int* combq;
     const double* combg;
+    const float* vals32;          // FP32 copies for the inner PCG of the mixed solve
+    const float* combg32;
+    const float* dinv32;
 };
+
+template <typename T> __device__ __forceinline__ const T* bvals(const BProb& d);
+template <> __device__ __forceinline__ const double* bvals<double>(const BProb& d) { return d.vals; }
+template <> __device__ __forceinline__ const float* bvals<float>(const BProb& d) { return d.vals32; }
+template <typename T> __device__ __forceinline__ const T* bcombg(const BProb& d);
+template <> __device__ __forceinline__ const double* bcombg<double>(const BProb& d) { return d.combg; }
+template <> __device__ __forceinline__ const float* bcombg<float>(const BProb& d) { return d.combg32; }
+template <typename T> __device__ __forceinline__ const T* bdinv(const BProb& d);
+template <> __device__ __forceinline__ const double* bdinv<double>(const BProb& d) { return d.dinv; }
+template <> __device__ __forceinline__ const float* bdinv<float>(const BProb& d) { return d.dinv32; }
 
 struct sgfem_batch {
     int device = 0;
@@ -69,6 +82,10 @@ struct sgfem_batch {
     KrylovScalars* d_scal = nullptr;
     double *d_x = nullptr, *d_b = nullptr, *d_r = nullptr, *d_p = nullptr, *d_q = nullptr, *d_part = nullptr;
     double* d_z = nullptr;        // preconditioned residual
+    // mixed solve: FP32 inner PCG vectors and the FP64 correction accumulator
+    float *d_r32 = nullptr, *d_p32 = nullptr, *d_q32 = nullptr, *d_z32 = nullptr;
+    double* d_d64 = nullptr;
+    double* d_want = nullptr;     // per-problem squared inner reduction target
     float* d_t = nullptr;         // sine-transform intermediate
     int4* d_dstmap = nullptr;     // (problem, line, mode chunk) per block of the transform passes
     int ndst = 0;
@@ -76,9 +93,12 @@ struct sgfem_batch {
     size_t dst_smem = 0;
     long long total = 0;          // sum of n * ld
     int blocks = 0, wpb = 4, qt = 4, ldmax = 0, m1max = 0, qnmax = 0;
+    int wpb32 = 4, qt32 = 8;      // launch shape of the FP32 apply (mixed solve)
     std::string tuning;
     std::vector<KrylovScalars> h_scal;
     double rtol = 0.0;            // of the last solve
+    std::vector<int> h_iters;     // per problem, last solve: PCG iterations (all refinement steps)
+    std::vector<double> h_relres; //   and the final ||b - A x|| / ||b|| (FP64)
 };
 
 namespace {
@@ -114,37 +134,40 @@ __device__ __forceinline__ void block_sum_store(double v, double* out) {
 }
 
 // Y = S X for every problem, p'q partials per block
-template <int QT>
-__global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict__ bprob, const double* __restrict__ X,
-                         double* __restrict__ Y, double* __restrict__ partials, const KrylovScalars* __restrict__ scal,
+template <typename T, int QT>
+__global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict__ bprob, const T* __restrict__ X,
+                         T* __restrict__ Y, double* __restrict__ partials, const KrylovScalars* __restrict__ scal,
                          int per_warp) {
     const int pi = bprob[blockIdx.x];
     const BProb& d = probs[pi];
-    extern __shared__ double bsm[];
+    extern __shared__ __align__(16) unsigned char bsm_raw[];
+    T* bsm = reinterpret_cast<T*>(bsm_raw);
+    const T* vals = bvals<T>(d);
+    const T* combg = bcombg<T>(d);
     const int wpb = blockDim.x >> 5;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (scal && scal[pi].done) {
         if (threadIdx.x == 0 && partials) partials[blockIdx.x] = 0.0;
         return;
     }
-    double* su = bsm + (size_t)warp * per_warp;
-    double* sc = su + d.ld;
-    double* sacc = sc + d.M1 + 1;
-    if (lane == 0) sc[d.M1] = 0.0;
-    const double* Xp = X + d.voff;
-    double* Yp = Y + d.voff;
+    T* su = bsm + (size_t)warp * per_warp;
+    T* sc = su + d.ld;
+    T* sacc = sc + d.M1 + 1;
+    if (lane == 0) sc[d.M1] = T(0);
+    const T* Xp = X + d.voff;
+    T* Yp = Y + d.voff;
     double dot = 0.0;
     const int lb = blockIdx.x - d.blk0;
     for (int row = lb * wpb + warp; row < d.n; row += d.nblk * wpb) {
-        double* yrow = Yp + (size_t)row * d.ld;
+        T* yrow = Yp + (size_t)row * d.ld;
         if (d.bmask[row]) {
-            for (int c = lane; c < d.ld; c += 32) yrow[c] = 0.0;
+            for (int c = lane; c < d.ld; c += 32) yrow[c] = T(0);
             continue;
         }
         const int nz0 = d.rowptr[row], nz1 = d.rowptr[row + 1];
         for (int base = 0; base < d.Qn; base += QT * 32) {
             int om[QT], on[QT];
-            double acc[QT];
+            T acc[QT];
 #pragma unroll
             for (int t = 0; t < QT; ++t) {
                 const int q = base + t * 32 + lane;
@@ -156,13 +179,13 @@ __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict_
                     om[t] = d.M1;
                     on[t] = 0;
                 }
-                acc[t] = 0.0;
+                acc[t] = T(0);
             }
             for (int nz = nz0; nz < nz1; ++nz) {
                 const int j = d.col[nz];
-                const double* xs = Xp + (size_t)j * d.ld;
+                const T* xs = Xp + (size_t)j * d.ld;
                 for (int c = lane; c < d.ld; c += 32) su[c] = __ldg(xs + c);
-                if (lane < d.M1) sc[lane] = d.vals[(size_t)nz * d.M1 + lane];
+                if (lane < d.M1) sc[lane] = vals[(size_t)nz * d.M1 + lane];
                 __syncwarp();
 #pragma unroll
                 for (int t = 0; t < QT; ++t) acc[t] = fma(sc[om[t]], su[on[t]], acc[t]);
@@ -175,16 +198,18 @@ __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict_
             }
         }
         __syncwarp();
-        const double* xrow = Xp + (size_t)row * d.ld;
+        const T* xrow = Xp + (size_t)row * d.ld;
+        T rowdot = T(0);  // per-row products in the working precision, rows summed in FP64
         for (int mu = lane; mu < d.ld; mu += 32) {
-            double y = 0.0;
+            T y = T(0);
             if (mu < d.P) {
                 y = sacc[mu];
-                for (int e = d.combptr[mu]; e < d.combptr[mu + 1]; ++e) y = fma(d.combg[e], sacc[d.combq[e]], y);
+                for (int e = d.combptr[mu]; e < d.combptr[mu + 1]; ++e) y = fma(combg[e], sacc[d.combq[e]], y);
             }
             yrow[mu] = y;
-            dot = fma(xrow[mu], y, dot);
+            rowdot = fma(xrow[mu], y, rowdot);
         }
+        dot += (double)rowdot;
         __syncwarp();
     }
     if (partials) {
@@ -200,11 +225,13 @@ __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict_
     }
 }
 
-enum BFin { BF_ALPHA = 0, BF_RR = 1, BF_BETA = 2, BF_TOL = 3 };
+enum BFin { BF_ALPHA = 0, BF_RR = 1, BF_BETA = 2, BF_TOL = 3, BF_NORM = 4 };
 
 // one block per problem: sum its block partials in order, update its scalars
+// (BF_TOL: tol2 = rtol2 * sum, rtol2 per problem when want != nullptr; BF_NORM: rr = sum)
 __global__ void k_bfin(const BProb* __restrict__ probs, const double* __restrict__ partials,
-                       KrylovScalars* __restrict__ scal, int mode, double rtol2, int maxit) {
+                       KrylovScalars* __restrict__ scal, int mode, double rtol2, int maxit,
+                       const double* __restrict__ want = nullptr) {
     const BProb& d = probs[blockIdx.x];
     KrylovScalars* s = scal + blockIdx.x;
     __shared__ double red[BT];
@@ -219,9 +246,13 @@ __global__ void k_bfin(const BProb* __restrict__ probs, const double* __restrict
     if (threadIdx.x != 0) return;
     const double sum = red[0];
     if (mode == BF_TOL) {
-        s->tol2 = rtol2 * sum;
+        s->tol2 = (want ? want[blockIdx.x] : rtol2) * sum;
         s->rr = sum;
         if (sum == 0.0) s->done = 1;
+        return;
+    }
+    if (mode == BF_NORM) {
+        s->rr = sum;
         return;
     }
     if (s->done) return;
@@ -253,50 +284,91 @@ __global__ void k_bfin(const BProb* __restrict__ probs, const double* __restrict
     const long long t0 = (long long)(blockIdx.x - d.blk0) * BT + threadIdx.x;          \
     const long long tstep = (long long)d.nblk * BT;
 
-// x += alpha p, r -= alpha q, ||r||^2 partials
+// x += alpha p, r -= alpha q, ||r||^2 partials (TX = double with T = float: the FP32
+// PCG's solution accumulates in FP64; partials per thread in T)
+template <typename T, typename TX>
 __global__ void __launch_bounds__(BT) k_bupdate(const BProb* __restrict__ probs, const int* __restrict__ bprob,
-                                                double* __restrict__ x, const double* __restrict__ p,
-                                                double* __restrict__ r, const double* __restrict__ q,
-                                                const KrylovScalars* __restrict__ scal, double* __restrict__ partials) {
+                                                TX* __restrict__ x, const T* __restrict__ p, T* __restrict__ r,
+                                                const T* __restrict__ q, const KrylovScalars* __restrict__ scal,
+                                                double* __restrict__ partials) {
     BRANGE;
-    double acc = 0.0;
+    T acc = T(0);
     if (!scal[pi].done) {
-        const double a = scal[pi].alpha;
+        const T a = (T)scal[pi].alpha;
+        const TX ax = (TX)scal[pi].alpha;
         for (long long t = t0; t < len; t += tstep) {
             const long long i = d.voff + t;
-            x[i] = fma(a, p[i], x[i]);
-            const double rn = fma(-a, q[i], r[i]);
+            x[i] = fma(ax, (TX)p[i], x[i]);
+            const T rn = fma(-a, q[i], r[i]);
             r[i] = rn;
             acc = fma(rn, rn, acc);
         }
+    }
+    block_sum_store((double)acc, partials + blockIdx.x);
+}
+
+// mixed solve: r32 = (float) r, d = 0, partials of ||r32||^2 (problems with done set skip)
+__global__ void __launch_bounds__(BT) k_bdemote(const BProb* __restrict__ probs, const int* __restrict__ bprob,
+                                                const double* __restrict__ r, float* __restrict__ r32,
+                                                double* __restrict__ dx, double* __restrict__ partials) {
+    BRANGE;
+    float acc = 0.f;
+    for (long long t = t0; t < len; t += tstep) {
+        const long long i = d.voff + t;
+        const float v = (float)r[i];
+        r32[i] = v;
+        dx[i] = 0.0;
+        acc = fmaf(v, v, acc);
+    }
+    block_sum_store((double)acc, partials + blockIdx.x);
+}
+
+// mixed solve: x += d, r = b - q (q = A x from the FP64 apply), partials of ||r||^2
+__global__ void __launch_bounds__(BT) k_badd(const BProb* __restrict__ probs, const int* __restrict__ bprob,
+                                             double* __restrict__ x, const double* __restrict__ dx) {
+    BRANGE;
+    for (long long t = t0; t < len; t += tstep) x[d.voff + t] += dx[d.voff + t];
+}
+__global__ void __launch_bounds__(BT) k_bresid(const BProb* __restrict__ probs, const int* __restrict__ bprob,
+                                               const double* __restrict__ b, const double* __restrict__ q,
+                                               double* __restrict__ r, double* __restrict__ partials) {
+    BRANGE;
+    double acc = 0.0;
+    for (long long t = t0; t < len; t += tstep) {
+        const long long i = d.voff + t;
+        const double rv = b[i] - q[i];
+        r[i] = rv;
+        acc = fma(rv, rv, acc);
     }
     block_sum_store(acc, partials + blockIdx.x);
 }
 
 // mode 0: partials of r' D^-1 r ; mode 1: p = D^-1 r + beta p ; mode 2: partials of b'b
+template <typename T>
 __global__ void __launch_bounds__(BT) k_bjacobi(const BProb* __restrict__ probs, const int* __restrict__ bprob,
-                                                const double* __restrict__ r, double* __restrict__ p,
+                                                const T* __restrict__ r, T* __restrict__ p,
                                                 const KrylovScalars* __restrict__ scal, double* __restrict__ partials,
                                                 int mode) {
     BRANGE;
-    double acc = 0.0;
+    T acc = T(0);
+    const T* dinv = bdinv<T>(d);
     if (mode == 2 || !scal[pi].done) {
-        const double beta = (mode == 1) ? scal[pi].beta : 0.0;
+        const T beta = (mode == 1) ? (T)scal[pi].beta : T(0);
         for (long long t = t0; t < len; t += tstep) {
             const long long i = d.voff + t;
-            const double rv = r[i];
+            const T rv = r[i];
             if (mode == 2) {
                 acc = fma(rv, rv, acc);
                 continue;
             }
-            const double z = d.dinv[t / d.ld] * rv;
+            const T z = dinv[t / d.ld] * rv;
             if (mode == 0)
                 acc = fma(rv, z, acc);
             else
                 p[i] = fma(beta, p[i], z);
         }
     }
-    if (mode != 1) block_sum_store(acc, partials + blockIdx.x);
+    if (mode != 1) block_sum_store((double)acc, partials + blockIdx.x);
 }
 
 // b = e_1 (x) b0 (Dirichlet rows zero) in the device layout; x = 0
@@ -321,32 +393,36 @@ __global__ void k_bout(const double* __restrict__ x, long long voff, int n, int 
 }
 
 // z = D^-1 r on the problems without a lattice (Jacobi), Dirichlet rows zero
+template <typename T>
 __global__ void __launch_bounds__(BT) k_bjz(const BProb* __restrict__ probs, const int* __restrict__ bprob,
-                                            const int2* __restrict__ lat, const double* __restrict__ r,
-                                            double* __restrict__ z, const KrylovScalars* __restrict__ scal) {
+                                            const int2* __restrict__ lat, const T* __restrict__ r,
+                                            T* __restrict__ z, const KrylovScalars* __restrict__ scal) {
     BRANGE;
     if (lat[pi].x > 0 || scal[pi].done) return;
-    for (long long t = t0; t < len; t += tstep) z[d.voff + t] = d.dinv[t / d.ld] * r[d.voff + t];
+    const T* dinv = bdinv<T>(d);
+    for (long long t = t0; t < len; t += tstep) z[d.voff + t] = dinv[t / d.ld] * r[d.voff + t];
 }
 
 // partials of r'z per block of each problem
+template <typename T>
 __global__ void __launch_bounds__(BT) k_brz(const BProb* __restrict__ probs, const int* __restrict__ bprob,
-                                            const double* __restrict__ r, const double* __restrict__ z,
+                                            const T* __restrict__ r, const T* __restrict__ z,
                                             const KrylovScalars* __restrict__ scal, double* __restrict__ partials) {
     BRANGE;
-    double acc = 0.0;
+    T acc = T(0);
     if (!scal[pi].done)
         for (long long t = t0; t < len; t += tstep) acc = fma(r[d.voff + t], z[d.voff + t], acc);
-    block_sum_store(acc, partials + blockIdx.x);
+    block_sum_store((double)acc, partials + blockIdx.x);
 }
 
 // p = z + beta p
+template <typename T>
 __global__ void __launch_bounds__(BT) k_bpz(const BProb* __restrict__ probs, const int* __restrict__ bprob,
-                                            const double* __restrict__ z, double* __restrict__ p,
+                                            const T* __restrict__ z, T* __restrict__ p,
                                             const KrylovScalars* __restrict__ scal) {
     BRANGE;
     if (scal[pi].done) return;
-    const double beta = scal[pi].beta;
+    const T beta = (T)scal[pi].beta;
     for (long long t = t0; t < len; t += tstep) p[d.voff + t] = fma(beta, p[d.voff + t], z[d.voff + t]);
 }
 
@@ -358,9 +434,10 @@ __global__ void __launch_bounds__(BT) k_bpz(const BProb* __restrict__ probs, con
 // lam_k = 4 sin^2(pi k / (2 nl)); pass 2 (x): z = S t per line.  One block per
 // (problem, line, 32-mode chunk); S and the line tile in shared memory, lanes
 // over modes, FP32 arithmetic.
+template <typename T>
 __global__ void __launch_bounds__(BT) k_bdst(const BProb* __restrict__ probs, const int4* __restrict__ map,
-                                             const int2* __restrict__ lat, int pass, const double* __restrict__ r,
-                                             float* __restrict__ t, double* __restrict__ z,
+                                             const int2* __restrict__ lat, int pass, const T* __restrict__ r,
+                                             float* __restrict__ t, T* __restrict__ z,
                                              const KrylovScalars* __restrict__ scal) {
     const int4 e = map[blockIdx.x];
     const int pi = e.x, line = e.y, chunk = e.z;
@@ -419,7 +496,7 @@ __global__ void __launch_bounds__(BT) k_bdst(const BProb* __restrict__ probs, co
     for (int k = 1 + warp; k <= N; k += nw) {
         const long long idx = d.voff + (long long)row_of(k) * d.ld + c;
         if (pass == 2)
-            z[idx] = (double)out[(k - 1) * 32 + lane];
+            z[idx] = (T)out[(k - 1) * 32 + lane];
         else
             t[idx] = out[(k - 1) * 32 + lane];
     }
@@ -441,19 +518,28 @@ int balloc(sgfem_batch* b, size_t bytes, void** dst) {
     return SGFEM_OK;
 }
 
+template <typename T = double>
 size_t apply_smem(const sgfem_batch* b, int wpb) {
-    const size_t per_warp = ((size_t)b->ldmax + b->m1max + 1 + b->qnmax + 1) & ~(size_t)1;
-    return per_warp * sizeof(double) * wpb;
+    const size_t per_warp = ((size_t)b->ldmax + b->m1max + 1 + b->qnmax + 3) & ~(size_t)3;
+    return per_warp * sizeof(T) * wpb;
 }
 
-int launch_apply(sgfem_batch* b, int wpb, int qt, const double* X, double* Y, double* partials,
-                 const KrylovScalars* scal) {
-    const int per_warp = (int)(((size_t)b->ldmax + b->m1max + 1 + b->qnmax + 1) & ~(size_t)1);
-    const size_t smem = apply_smem(b, wpb);
+template <typename T>
+int launch_apply(sgfem_batch* b, int wpb, int qt, const T* X, T* Y, double* partials, const KrylovScalars* scal) {
+    const int per_warp = (int)(((size_t)b->ldmax + b->m1max + 1 + b->qnmax + 3) & ~(size_t)3);
+    const size_t smem = apply_smem<T>(b, wpb);
     if (qt == 4)
-        k_bapply<4><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials, scal, per_warp);
+        k_bapply<T, 4><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials, scal,
+                                                                  per_warp);
+    else if (qt == 8)
+        k_bapply<T, 8><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials, scal,
+                                                                  per_warp);
+    else if (qt == 16)
+        k_bapply<T, 16><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials, scal,
+                                                                   per_warp);
     else
-        k_bapply<8><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials, scal, per_warp);
+        k_bapply<T, 32><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials, scal,
+                                                                   per_warp);
     BLAUNCHED(b);
     return SGFEM_OK;
 }
@@ -656,6 +742,13 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
         SG_TRY(bupload(b, h.combptr, (int**)&d.combptr));
         SG_TRY(bupload(b, h.combq, (int**)&d.combq));
         SG_TRY(bupload(b, h.combg, (double**)&d.combg));
+        {
+            const std::vector<float> v32(h.vals.begin(), h.vals.end()), g32(h.combg.begin(), h.combg.end()),
+                d32(h.dinv.begin(), h.dinv.end());
+            SG_TRY(bupload(b, v32, (float**)&d.vals32));
+            SG_TRY(bupload(b, g32, (float**)&d.combg32));
+            SG_TRY(bupload(b, d32, (float**)&d.dinv32));
+        }
         b->ldmax = std::max(b->ldmax, h.ld);
         b->m1max = std::max(b->m1max, h.M1);
         b->qnmax = std::max(b->qnmax, d.Qn);
@@ -670,6 +763,13 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
     SG_TRY(balloc(b, (size_t)B * sizeof(KrylovScalars), (void**)&b->d_scal));
     SG_TRY(balloc(b, vb, (void**)&b->d_z));
     BCUDA(b, cudaMemset(b->d_z, 0, vb));
+    const size_t vb32 = (size_t)voff * sizeof(float);
+    SG_TRY(balloc(b, vb32, (void**)&b->d_r32));
+    SG_TRY(balloc(b, vb32, (void**)&b->d_p32));
+    SG_TRY(balloc(b, vb32, (void**)&b->d_q32));
+    SG_TRY(balloc(b, vb32, (void**)&b->d_z32));
+    SG_TRY(balloc(b, vb, (void**)&b->d_d64));
+    SG_TRY(balloc(b, (size_t)B * sizeof(double), (void**)&b->d_want));
     {
         // sine-transform preconditioner: per-problem (nl, a0) and one block per (problem, line, chunk)
         std::vector<int2> lat(B, make_int2(0, 0));
@@ -693,8 +793,10 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
             SG_TRY(bupload(b, map, &b->d_dstmap));
             SG_TRY(balloc(b, (size_t)voff * sizeof(float), (void**)&b->d_t));
             b->dst_smem = smax;
-            if (smax > 48 * 1024)
-                BCUDA(b, cudaFuncSetAttribute(k_bdst, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
+            if (smax > 48 * 1024) {
+                BCUDA(b, cudaFuncSetAttribute(k_bdst<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
+                BCUDA(b, cudaFuncSetAttribute(k_bdst<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
+            }
         }
     }
     BCUDA(b, cudaMemset(b->d_x, 0, vb));
@@ -726,20 +828,26 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
         const size_t smem = apply_smem(b, c.wpb);
         if ((int)smem > dev_smem) continue;
         if (smem > 48 * 1024) {
-            cudaError_t e = (c.qt == 4) ? cudaFuncSetAttribute(k_bapply<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                                        : cudaFuncSetAttribute(k_bapply<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaError_t e = (c.qt == 4) ? cudaFuncSetAttribute(k_bapply<double, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                                        : cudaFuncSetAttribute(k_bapply<double, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) {
                 cudaGetLastError();
                 continue;
             }
+            // the FP32 apply of the same shape needs half of it
+            if (c.qt == 4)
+                cudaFuncSetAttribute(k_bapply<float, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            else
+                cudaFuncSetAttribute(k_bapply<float, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaGetLastError();
         }
         SG_TRY(build_map(b, b->num_sms * c.bps, probs, bprob));
         if ((int)bprob.size() > max_blocks * 4) continue;
         BCUDA(b, cudaMemcpy(b->d_probs, probs.data(), (size_t)B * sizeof(BProb), cudaMemcpyHostToDevice));
         BCUDA(b, cudaMemcpy(b->d_bprob, bprob.data(), bprob.size() * sizeof(int), cudaMemcpyHostToDevice));
-        SG_TRY(launch_apply(b, c.wpb, c.qt, b->d_p, b->d_q, b->d_part, nullptr));  // warm-up
+        SG_TRY(launch_apply<double>(b, c.wpb, c.qt, b->d_p, b->d_q, b->d_part, nullptr));  // warm-up
         BCUDA(b, cudaEventRecord(b->ev0, b->stream));
-        for (int r = 0; r < 3; ++r) SG_TRY(launch_apply(b, c.wpb, c.qt, b->d_p, b->d_q, b->d_part, nullptr));
+        for (int r = 0; r < 3; ++r) SG_TRY(launch_apply<double>(b, c.wpb, c.qt, b->d_p, b->d_q, b->d_part, nullptr));
         BCUDA(b, cudaEventRecord(b->ev1, b->stream));
         BCUDA(b, cudaEventSynchronize(b->ev1));
         float ms = 0.f;
@@ -758,9 +866,43 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
     SG_TRY(build_map(b, b->num_sms * bestc.bps, probs, bprob));
     BCUDA(b, cudaMemcpy(b->d_probs, probs.data(), (size_t)B * sizeof(BProb), cudaMemcpyHostToDevice));
     BCUDA(b, cudaMemcpy(b->d_bprob, bprob.data(), bprob.size() * sizeof(int), cudaMemcpyHostToDevice));
-    char buf[128];
-    snprintf(buf, sizeof(buf), "chosen %d warps/block, %d pairs/lane, %d blocks; ", b->wpb, b->qt * 32, b->blocks);
-    b->tuning = buf + log;
+    // FP32 apply of the mixed solve on the same block map: more pairs per pass amortise
+    // the staging of each X row (LSU-bound rather than FP64-bound)
+    std::string log32;
+    float best32 = 1e30f;
+    for (int wpb : {4, 8})
+        for (int qt : {8, 16, 32}) {
+            const size_t smem = apply_smem<float>(b, wpb);
+            if ((int)smem > dev_smem) continue;
+            if (smem > 48 * 1024) {
+                cudaError_t e = qt == 8 ? cudaFuncSetAttribute(k_bapply<float, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                              : qt == 16 ? cudaFuncSetAttribute(k_bapply<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                                         : cudaFuncSetAttribute(k_bapply<float, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (e != cudaSuccess) {
+                    cudaGetLastError();
+                    continue;
+                }
+            }
+            SG_TRY(launch_apply<float>(b, wpb, qt, b->d_p32, b->d_q32, b->d_part, nullptr));
+            BCUDA(b, cudaEventRecord(b->ev0, b->stream));
+            for (int r = 0; r < 2; ++r) SG_TRY(launch_apply<float>(b, wpb, qt, b->d_p32, b->d_q32, b->d_part, nullptr));
+            BCUDA(b, cudaEventRecord(b->ev1, b->stream));
+            BCUDA(b, cudaEventSynchronize(b->ev1));
+            float ms = 0.f;
+            BCUDA(b, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+            char buf32[96];
+            snprintf(buf32, sizeof(buf32), "%dw/%dq:%.3fms ", wpb, qt, ms / 2);
+            log32 += buf32;
+            if (ms < best32) {
+                best32 = ms;
+                b->wpb32 = wpb;
+                b->qt32 = qt;
+            }
+        }
+    char buf[192];
+    snprintf(buf, sizeof(buf), "chosen %d warps/block, %d pairs/lane, %d blocks (FP32: %d warps/block, %d pairs/lane); ",
+             b->wpb, b->qt * 32, b->blocks, b->wpb32, b->qt32 * 32);
+    b->tuning = buf + log + "FP32 " + log32;
     b->finalized = true;
     return SGFEM_OK;
 }
@@ -770,35 +912,95 @@ extern "C" const char* sgfem_batch_tuning(const sgfem_batch* b) { return b ? b->
 namespace {
 
 // z = B r (sine transform on lattice problems, Jacobi on the others), rho = r'z, beta, p = z + beta p
-int batch_precondition(sgfem_batch* b, int maxit) {
+// the PCG vectors of one precision: FP64 (x, r, p, q, z) or the FP32 inner set with the FP64 accumulator
+template <typename T, typename TX>
+struct BVecs {
+    TX* x;
+    T *r, *p, *q, *z;
+};
+
+template <typename T, typename TX>
+int batch_precondition(sgfem_batch* b, const BVecs<T, TX>& v, int maxit) {
     const int B = (int)b->hp.size();
-    k_bjz<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_lat, b->d_r, b->d_z, b->d_scal);
+    k_bjz<T><<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_lat, v.r, v.z, b->d_scal);
     BLAUNCHED(b);
     if (b->ndst > 0)
         for (int pass = 0; pass < 3; ++pass) {
-            k_bdst<<<b->ndst, BT, b->dst_smem, b->stream>>>(b->d_probs, b->d_dstmap, b->d_lat, pass, b->d_r, b->d_t,
-                                                            b->d_z, b->d_scal);
+            k_bdst<T><<<b->ndst, BT, b->dst_smem, b->stream>>>(b->d_probs, b->d_dstmap, b->d_lat, pass, v.r, b->d_t,
+                                                               v.z, b->d_scal);
             BLAUNCHED(b);
         }
-    k_brz<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_r, b->d_z, b->d_scal, b->d_part);
+    k_brz<T><<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, v.r, v.z, b->d_scal, b->d_part);
     BLAUNCHED(b);
     k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_BETA, 0.0, maxit);
     BLAUNCHED(b);
-    k_bpz<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_z, b->d_p, b->d_scal);
+    k_bpz<T><<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, v.z, v.p, b->d_scal);
     BLAUNCHED(b);
     return SGFEM_OK;
 }
 
-int batch_iteration(sgfem_batch* b, int maxit) {
+template <typename T, typename TX>
+int batch_iteration(sgfem_batch* b, const BVecs<T, TX>& v, int maxit) {
     const int B = (int)b->hp.size();
-    SG_TRY(launch_apply(b, b->wpb, b->qt, b->d_p, b->d_q, b->d_part, b->d_scal));
+    const bool f32 = sizeof(T) == 4;
+    SG_TRY(launch_apply<T>(b, f32 ? b->wpb32 : b->wpb, f32 ? b->qt32 : b->qt, v.p, v.q, b->d_part, b->d_scal));
     k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_ALPHA, 0.0, maxit);
     BLAUNCHED(b);
-    k_bupdate<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_x, b->d_p, b->d_r, b->d_q, b->d_scal, b->d_part);
+    k_bupdate<T, TX><<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, v.x, v.p, v.r, v.q, b->d_scal,
+                                                      b->d_part);
     BLAUNCHED(b);
     k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_RR, 0.0, maxit);
     BLAUNCHED(b);
-    return batch_precondition(b, maxit);
+    return batch_precondition<T, TX>(b, v, maxit);
+}
+
+// PCG on all problems from the residual in v.r (x = 0 in v.x for the problems that run):
+// scalars reset (done kept for problems marked done in h_scal), tolerances from
+// BF_TOL over the Jacobi partials of ||r||^2 (want per problem, or rtol2), then
+// check_every iterations per graph replay until every problem is done.
+template <typename T, typename TX>
+int batch_pcg(sgfem_batch* b, const BVecs<T, TX>& v, const double* want, double rtol2, int maxit, int check_every,
+              int* replays) {
+    const int B = (int)b->hp.size();
+    BCUDA(b, cudaMemcpyAsync(b->d_scal, b->h_scal.data(), (size_t)B * sizeof(KrylovScalars), cudaMemcpyHostToDevice,
+                             b->stream));
+    k_bjacobi<T><<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, v.r, v.p, b->d_scal, b->d_part, 2);
+    BLAUNCHED(b);
+    k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_TOL, rtol2, maxit, want);
+    BLAUNCHED(b);
+    BCUDA(b, cudaMemsetAsync(v.p, 0, (size_t)b->total * sizeof(T), b->stream));
+    BCUDA(b, cudaMemsetAsync(v.z, 0, (size_t)b->total * sizeof(T), b->stream));
+    SG_TRY((batch_precondition<T, TX>(b, v, maxit)));
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    const long long before = b->launches;
+    int st = SGFEM_OK;
+    for (int k = 0; k < check_every && st == SGFEM_OK; ++k) st = batch_iteration<T, TX>(b, v, maxit);
+    const long long per_graph = b->launches - before;
+    b->launches = before;
+    cudaError_t ce = cudaStreamEndCapture(b->stream, &graph);
+    if (st != SGFEM_OK || ce != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return st != SGFEM_OK ? st : bfail(b, SGFEM_ERR_CUDA, "graph capture failed");
+    }
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    while (ce == cudaSuccess) {
+        ce = cudaMemcpyAsync(b->h_scal.data(), b->d_scal, (size_t)B * sizeof(KrylovScalars), cudaMemcpyDeviceToHost,
+                             b->stream);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(b->stream);
+        if (ce != cudaSuccess) break;
+        bool all = true;
+        for (auto& s : b->h_scal) all = all && s.done;
+        if (all) break;
+        ce = cudaGraphLaunch(exec, b->stream);
+        b->launches += per_graph;
+        ++*replays;
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return bfail(b, SGFEM_ERR_CUDA, std::string("batch iteration: ") + cudaGetErrorString(ce));
+    return SGFEM_OK;
 }
 
 }  // namespace
@@ -837,56 +1039,90 @@ extern "C" int sgfem_batch_solve(sgfem_batch* b, double rtol, int maxit, int che
                                          probs[i].bmask);
         BLAUNCHED(b);
     }
-    BCUDA(b, cudaMemcpyAsync(b->d_r, b->d_b, (size_t)b->total * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
-    BCUDA(b, cudaMemsetAsync(b->d_p, 0, (size_t)b->total * sizeof(double), b->stream));
-    // scalars: tol2 = rtol^2 ||b||^2 per problem, first = 1
-    for (auto& s : b->h_scal) {
-        std::memset(&s, 0, sizeof(s));
-        s.first = 1;
-    }
-    BCUDA(b, cudaMemcpyAsync(b->d_scal, b->h_scal.data(), (size_t)B * sizeof(KrylovScalars), cudaMemcpyHostToDevice,
-                             b->stream));
-    k_bjacobi<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_r, b->d_p, b->d_scal, b->d_part, 2);
-    BLAUNCHED(b);
-    k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_TOL, rtol * rtol, maxit);
-    BLAUNCHED(b);
-    // first direction: z = B r, rho = r'z, p = z
-    BCUDA(b, cudaMemsetAsync(b->d_z, 0, (size_t)b->total * sizeof(double), b->stream));
-    SG_TRY(batch_precondition(b, maxit));
-    // graph of check_every iterations
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    const long long before = b->launches;
-    int st = SGFEM_OK;
-    for (int k = 0; k < check_every && st == SGFEM_OK; ++k) st = batch_iteration(b, maxit);
-    const long long per_graph = b->launches - before;
-    b->launches = before;
-    ce = cudaStreamEndCapture(b->stream, &graph);
-    if (st != SGFEM_OK || ce != cudaSuccess) {
-        if (graph) cudaGraphDestroy(graph);
-        cudaFree(d_b0);
-        return st != SGFEM_OK ? st : bfail(b, SGFEM_ERR_CUDA, "graph capture failed");
-    }
-    ce = cudaGraphInstantiate(&exec, graph, 0);
     int replays = 0;
     int status = SGFEM_OK;
-    while (ce == cudaSuccess) {
-        ce = cudaMemcpyAsync(b->h_scal.data(), b->d_scal, (size_t)B * sizeof(KrylovScalars), cudaMemcpyDeviceToHost,
-                             b->stream);
-        if (ce == cudaSuccess) ce = cudaStreamSynchronize(b->stream);
-        if (ce != cudaSuccess) break;
-        bool all = true;
-        for (auto& s : b->h_scal) all = all && s.done;
-        if (all) break;
-        ce = cudaGraphLaunch(exec, b->stream);
-        b->launches += per_graph;
-        ++replays;
+    std::vector<int> iters(B, 0);
+    std::vector<double> bb(B, 0.0), rr(B, 0.0);
+    auto reset_scalars = [&](const std::vector<char>* active) {
+        for (int i = 0; i < B; ++i) {
+            KrylovScalars& s0 = b->h_scal[i];
+            std::memset(&s0, 0, sizeof(s0));
+            s0.first = 1;
+            s0.done = (active && !(*active)[i]) ? 1 : 0;
+        }
+    };
+    // per-problem squared norms of an FP64 vector (b or r) into h
+    auto norms64 = [&](const double* v, std::vector<double>& h) -> int {
+        for (auto& s0 : b->h_scal) std::memset(&s0, 0, sizeof(s0));
+        BCUDA(b, cudaMemcpyAsync(b->d_scal, b->h_scal.data(), (size_t)B * sizeof(KrylovScalars), cudaMemcpyHostToDevice,
+                                 b->stream));
+        k_bjacobi<double><<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, v, nullptr, b->d_scal, b->d_part, 2);
+        BLAUNCHED(b);
+        k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_NORM, 0.0, maxit);
+        BLAUNCHED(b);
+        BCUDA(b, cudaMemcpyAsync(b->h_scal.data(), b->d_scal, (size_t)B * sizeof(KrylovScalars), cudaMemcpyDeviceToHost,
+                                 b->stream));
+        BCUDA(b, cudaStreamSynchronize(b->stream));
+        for (int i = 0; i < B; ++i) h[i] = b->h_scal[i].rr;
+        return SGFEM_OK;
+    };
+    const char* ep = getenv("SGFEM_BATCH_PRECISION");
+    const bool fp64 = ep && std::string(ep) == "fp64";
+    SG_TRY(norms64(b->d_b, bb));
+    if (fp64) {
+        // FP64 PCG on every problem
+        BCUDA(b, cudaMemcpyAsync(b->d_r, b->d_b, (size_t)b->total * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+        reset_scalars(nullptr);
+        const BVecs<double, double> v{b->d_x, b->d_r, b->d_p, b->d_q, b->d_z};
+        SG_TRY((batch_pcg<double, double>(b, v, nullptr, rtol * rtol, maxit, check_every, &replays)));
+        for (int i = 0; i < B; ++i) {
+            iters[i] = b->h_scal[i].iters;
+            rr[i] = b->h_scal[i].rr;
+            if (b->h_scal[i].status != SGFEM_OK && status == SGFEM_OK) status = b->h_scal[i].status;
+        }
+    } else {
+        // mixed: FP32 PCG on the correction of every unconverged problem, solution and
+        // residual in FP64 (FP64 apply); first step to 1e-4, later steps aim to end the
+        // solve (margin 3, at most a 1e-6 reduction per step)
+        BCUDA(b, cudaMemcpyAsync(b->d_r, b->d_b, (size_t)b->total * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+        rr = bb;
+        const BVecs<float, double> v{b->d_d64, b->d_r32, b->d_p32, b->d_q32, b->d_z32};
+        std::vector<double> want(B, 0.0);
+        for (int outer = 0; outer < 16; ++outer) {
+            std::vector<char> active(B, 0);
+            bool any = false;
+            for (int i = 0; i < B; ++i) {
+                active[i] = bb[i] > 0.0 && rr[i] > rtol * rtol * bb[i];
+                any = any || active[i];
+                const double finish = 0.1 * rtol * rtol * bb[i] / std::max(rr[i], 1e-300);
+                want[i] = outer == 0 ? std::max(1e-8, finish) : std::max(finish, 1e-12);
+            }
+            if (!any) break;
+            k_bdemote<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_r, b->d_r32, b->d_d64, b->d_part);
+            BLAUNCHED(b);
+            BCUDA(b, cudaMemcpyAsync(b->d_want, want.data(), (size_t)B * sizeof(double), cudaMemcpyHostToDevice,
+                                     b->stream));
+            reset_scalars(&active);
+            SG_TRY((batch_pcg<float, double>(b, v, b->d_want, 0.0, maxit, check_every, &replays)));
+            for (int i = 0; i < B; ++i) {
+                iters[i] += b->h_scal[i].iters;
+                const int st0 = b->h_scal[i].status;
+                if (st0 == SGFEM_ERR_BREAKDOWN || st0 == SGFEM_ERR_NONFINITE) status = st0;
+            }
+            if (status != SGFEM_OK) break;
+            // x += d; r = b - A x (FP64)
+            k_badd<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_x, b->d_d64);
+            BLAUNCHED(b);
+            SG_TRY(launch_apply<double>(b, b->wpb, b->qt, b->d_x, b->d_q, b->d_part, nullptr));
+            k_bresid<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_b, b->d_q, b->d_r, b->d_part);
+            BLAUNCHED(b);
+            SG_TRY(norms64(b->d_r, rr));
+            if (*std::max_element(iters.begin(), iters.end()) >= maxit) break;
+        }
     }
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
     cudaFree(d_b0);
-    if (ce != cudaSuccess) return bfail(b, SGFEM_ERR_CUDA, std::string("batch iteration: ") + cudaGetErrorString(ce));
+    cudaError_t ce2 = cudaSuccess;
+    if (ce2 != cudaSuccess) return bfail(b, SGFEM_ERR_CUDA, std::string("batch iteration: ") + cudaGetErrorString(ce2));
     BCUDA(b, cudaEventRecord(b->ev1, b->stream));
     BCUDA(b, cudaEventSynchronize(b->ev1));
     float ms = 0.f;
@@ -896,13 +1132,15 @@ extern "C" int sgfem_batch_solve(sgfem_batch* b, double rtol, int maxit, int che
     s.graph_replays = replays;
     s.kernel_launches = b->launches - launches0;
     s.converged = 0;
+    b->h_iters = iters;
+    b->h_relres.assign(B, 0.0);
     for (int i = 0; i < B; ++i) {
-        const KrylovScalars& k = b->h_scal[i];
-        s.iterations_max = std::max(s.iterations_max, k.iters);
-        const double rel = k.tol2 > 0.0 ? std::sqrt(k.rr * rtol * rtol / k.tol2) : 0.0;
+        s.iterations_max = std::max(s.iterations_max, iters[i]);
+        const double rel = bb[i] > 0.0 ? std::sqrt(rr[i] / bb[i]) : 0.0;
+        b->h_relres[i] = rel;
         s.relres_max = std::max(s.relres_max, rel);
-        if (k.status == SGFEM_OK && k.done) s.converged++;
-        else if (status == SGFEM_OK) status = k.status ? k.status : SGFEM_ERR_MAXIT;
+        if (rel <= rtol) s.converged++;
+        else if (status == SGFEM_OK) status = SGFEM_ERR_MAXIT;
     }
     if (stats) *stats = s;
     if (x_out) {
@@ -927,9 +1165,8 @@ extern "C" int sgfem_batch_solve(sgfem_batch* b, double rtol, int maxit, int che
 }
 
 extern "C" int sgfem_batch_problem_stats(const sgfem_batch* b, int i, int* iterations, double* relres) {
-    if (!b || i < 0 || i >= (int)b->h_scal.size()) return SGFEM_ERR_ARGUMENT;
-    const KrylovScalars& k = b->h_scal[i];
-    if (iterations) *iterations = k.iters;
-    if (relres) *relres = k.tol2 > 0.0 ? b->rtol * std::sqrt(k.rr / k.tol2) : 0.0;
+    if (!b || i < 0 || i >= (int)b->h_iters.size()) return SGFEM_ERR_ARGUMENT;
+    if (iterations) *iterations = b->h_iters[i];
+    if (relres) *relres = b->h_relres[i];
     return SGFEM_OK;
 }

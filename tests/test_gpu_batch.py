@@ -51,3 +51,26 @@ def test_batch_equals_single_problem_solver(built_pkg):
         op.close()
         assert np.linalg.norm(x - y) <= 1e-8 * np.linalg.norm(y)
     B.close()
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_batch_precisions_agree(built_pkg, monkeypatch, precision):
+    """The default mixed solve (FP32 inner PCG, FP64 residuals and solution) and
+    the plain FP64 PCG (SGFEM_BATCH_PRECISION=fp64) both meet rtol on the FP64
+    residual and agree with the single-problem FP64 solve."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    if precision == "fp64":
+        monkeypatch.setenv("SGFEM_BATCH_PRECISION", "fp64")
+    probs = [build(16, 1, 4, pkg.total_degree_multiindices(4, 2)), build(8, 2, 3, pkg.total_degree_multiindices(3, 2)),
+             build(11, 1, 5, pkg.total_degree_multiindices(5, 1))]
+    B = pkg.SGBatch(0)
+    for p in probs:
+        B.add(p.V, p.TB, p.Kall, p.b0)
+    B.finalize()
+    xs, st = B.solve(rtol=1e-9)
+    assert st["converged"] == len(probs) and st["relres_max"] <= 1e-9
+    for p, x in zip(probs, xs):
+        ref = osg.kron_direct(p.K0, p.Ks, p.G, p.b0, p.bdofs, p.P)
+        assert np.linalg.norm(x - ref) <= 1e-7 * np.linalg.norm(ref)
+    B.close()
