@@ -12,7 +12,8 @@ from .batch import SGBatch, config4_problems, splitmix64
 from .coefficients import StochasticCoefficientCosinus
 from .estimate import estimate, extension_couplings
 from .fem import (H1Pk, assemble_convection, assemble_laplacian, assemble_pce_rhs, assemble_rhs, assemble_stiffness,
-                  assemble_stiffness_gpu,
+                  assemble_stiffness_gpu, assemble_rhs_gpu, assemble_pce_rhs_gpu, assemble_laplacian_gpu,
+                  assemble_convection_gpu,
                   assemble_stiffness_nodal_mean, box_functional, line_rule, pce_lambda, triangle_rule,
                   unit_square_mesh)
 from .modelproblems import (AbstractModelProblem, LogTransformedPoissonProblemPrimal, PoissonProblemPrimal, SGOperator,

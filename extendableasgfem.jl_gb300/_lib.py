@@ -87,6 +87,11 @@ SIGNATURES = {
     "sgfem_estimate_primal": (ctypes.c_int, [_P, _DP, _P, _P, _DP, _P, _P, _DP, _DP]),
     "sgfem_assemble_stiffness": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int64,
                                                 _I64P, _I64P, _DP]),
+    "sgfem_assemble_convection": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int64,
+                                                 _I64P, _I64P, _DP]),
+    "sgfem_assemble_rhs": (ctypes.c_int, [_P, _P, _P, _P, _DP, _DP]),
+    "sgfem_assemble_pce_rhs": (ctypes.c_int, [_P, _P, _P, _P, _DP, _P, ctypes.c_int64, ctypes.c_int64,
+                                              ctypes.POINTER(ctypes.c_int32), ctypes.c_double, ctypes.c_int64, _DP]),
     "sgfem_estimate_logpoisson": (ctypes.c_int, [_P, _DP, _P, _P, _DP, _P, _P, _P, _DP, _DP, _DP]),
     "sgfem_set_samples": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int64, _DP]),
     "sgfem_solve_samples": (ctypes.c_int, [_P, _DP, _DP, ctypes.POINTER(SolveOptions), ctypes.POINTER(SolveStats)]),

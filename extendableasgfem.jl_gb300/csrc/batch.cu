@@ -807,9 +807,10 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
     // ---- autotune the apply: warps per block x pairs per lane x blocks per SM
     struct Cand { int wpb, qt, bps; };
     std::vector<Cand> cands;
-    for (int wpb : {2, 4, 8})
-        for (int qt : {4, 8})
-            for (int bps : {4, 8, 16}) cands.push_back({wpb, qt, bps});
+    // 2 warps/block, 4 pairs per lane and 4 blocks per SM lost on every batch measured
+    for (int wpb : {4, 8})
+        for (int qt : {8, 16})
+            for (int bps : {8, 16}) cands.push_back({wpb, qt, bps});
     int dev_smem = 0;
     cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
     float best = 1e30f;
@@ -828,18 +829,12 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
         const size_t smem = apply_smem(b, c.wpb);
         if ((int)smem > dev_smem) continue;
         if (smem > 48 * 1024) {
-            cudaError_t e = (c.qt == 4) ? cudaFuncSetAttribute(k_bapply<double, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                                        : cudaFuncSetAttribute(k_bapply<double, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaError_t e = c.qt == 8 ? cudaFuncSetAttribute(k_bapply<double, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                                      : cudaFuncSetAttribute(k_bapply<double, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) {
                 cudaGetLastError();
                 continue;
             }
-            // the FP32 apply of the same shape needs half of it
-            if (c.qt == 4)
-                cudaFuncSetAttribute(k_bapply<float, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            else
-                cudaFuncSetAttribute(k_bapply<float, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            cudaGetLastError();
         }
         SG_TRY(build_map(b, b->num_sms * c.bps, probs, bprob));
         if ((int)bprob.size() > max_blocks * 4) continue;
@@ -847,13 +842,13 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
         BCUDA(b, cudaMemcpy(b->d_bprob, bprob.data(), bprob.size() * sizeof(int), cudaMemcpyHostToDevice));
         SG_TRY(launch_apply<double>(b, c.wpb, c.qt, b->d_p, b->d_q, b->d_part, nullptr));  // warm-up
         BCUDA(b, cudaEventRecord(b->ev0, b->stream));
-        for (int r = 0; r < 3; ++r) SG_TRY(launch_apply<double>(b, c.wpb, c.qt, b->d_p, b->d_q, b->d_part, nullptr));
+        SG_TRY(launch_apply<double>(b, c.wpb, c.qt, b->d_p, b->d_q, b->d_part, nullptr));
         BCUDA(b, cudaEventRecord(b->ev1, b->stream));
         BCUDA(b, cudaEventSynchronize(b->ev1));
         float ms = 0.f;
         BCUDA(b, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
         char buf[96];
-        snprintf(buf, sizeof(buf), "%dw/%dq/%dbps:%.3fms ", c.wpb, c.qt, c.bps, ms / 3);
+        snprintf(buf, sizeof(buf), "%dw/%dq/%dbps:%.3fms ", c.wpb, c.qt, c.bps, ms);
         log += buf;
         if (ms < best) {
             best = ms;
@@ -871,12 +866,11 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
     std::string log32;
     float best32 = 1e30f;
     for (int wpb : {4, 8})
-        for (int qt : {8, 16, 32}) {
+        for (int qt : {16, 32}) {
             const size_t smem = apply_smem<float>(b, wpb);
             if ((int)smem > dev_smem) continue;
             if (smem > 48 * 1024) {
-                cudaError_t e = qt == 8 ? cudaFuncSetAttribute(k_bapply<float, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                              : qt == 16 ? cudaFuncSetAttribute(k_bapply<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                cudaError_t e = qt == 16 ? cudaFuncSetAttribute(k_bapply<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
                                          : cudaFuncSetAttribute(k_bapply<float, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
                 if (e != cudaSuccess) {
                     cudaGetLastError();

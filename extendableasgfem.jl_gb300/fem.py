@@ -323,11 +323,7 @@ def box_functional(space, box, quadorder=None):
     return assemble_rhs(space, ind, space.order + 1 if quadorder is None else quadorder)
 
 
-def assemble_stiffness_gpu(space, coef, ms, quadorder, device=0, ctx=None):
-    """assemble_stiffness on the GPU (sgfem_assemble_stiffness): the same CSR
-    matrices (pattern of `space.pattern()`, values summed cell by cell), with the
-    quadrature-point work and the per-nonzero sums on the device.  `ms` must be a
-    contiguous range of terms."""
+def _bilinear_gpu(entry, space, coef, ms, quadorder, device, ctx):
     import ctypes
     from . import _lib
     from .estimate import _Cosine, _Quad, _mesh_struct, _ptr
@@ -335,7 +331,7 @@ def assemble_stiffness_gpu(space, coef, ms, quadorder, device=0, ctx=None):
     ms = list(ms)
     m0, m1 = ms[0], ms[-1]
     if ms != list(range(m0, m1 + 1)):
-        raise ValueError("assemble_stiffness_gpu: terms must be a contiguous range")
+        raise ValueError(f"{entry}: terms must be a contiguous range")
     pts, wts = triangle_rule(quadorder)
     indptr, col, _ = space.pattern()
     n = space.ndofs
@@ -353,13 +349,101 @@ def assemble_stiffness_gpu(space, coef, ms, quadorder, device=0, ctx=None):
     cd = np.ascontiguousarray(space.celldofs + 1, dtype=np.int64)
     fs = _FESpace(space.order, n, cd.ctypes.data)
     vals = np.zeros((m1 - m0 + 1, nnz))
+    _with_ctx(device, ctx, lambda cx: getattr(cx.lib, entry)(
+        cx.h, ctypes.byref(mesh), ctypes.byref(fs), ctypes.byref(c), m0, m1, ctypes.byref(q), nnz,
+        _lib._i64p(colptr), _lib._i64p(rowval), _lib._dp(vals)))
+    # values[k] is the entry (rowval[k], column) of the CSC pattern
+    return [sp.csc_matrix((vals[i], col, indptr), shape=(n, n)).tocsr() for i in range(m1 - m0 + 1)]
+
+
+def assemble_stiffness_gpu(space, coef, ms, quadorder, device=0, ctx=None):
+    """assemble_stiffness on the GPU (sgfem_assemble_stiffness): the same CSR
+    matrices (pattern of `space.pattern()`, values summed cell by cell), with the
+    quadrature-point work and the per-nonzero sums on the device.  `ms` must be a
+    contiguous range of terms."""
+    return _bilinear_gpu("sgfem_assemble_stiffness", space, coef, ms, quadorder, device, ctx)
+
+
+def assemble_convection_gpu(space, coef, ms, quadorder, device=0, ctx=None):
+    """assemble_convection on the GPU (sgfem_assemble_convection):
+    N_m[i, j] = -(grad a_m . grad phi_j, phi_i) for a contiguous range of terms."""
+    return _bilinear_gpu("sgfem_assemble_convection", space, coef, ms, quadorder, device, ctx)
+
+
+class _UnitMean:
+    """a = 1: the coefficient of the Laplacian A = (grad u, grad v)."""
+    mean_value = 1.0
+    freq = 1.0
+    decay_factors = b1 = b2 = ()
+
+    @staticmethod
+    def maxm():
+        return 0
+
+
+def assemble_laplacian_gpu(space, quadorder=None, device=0, ctx=None):
+    """assemble_laplacian on the GPU (sgfem_assemble_stiffness with a = 1)."""
+    q = 2 * (space.order - 1) if quadorder is None else quadorder
+    return assemble_stiffness_gpu(space, _UnitMean, [0], q, device, ctx)[0]
+
+
+def _gpu_rhs_args(space, f, quadorder):
+    from .estimate import _Quad, _mesh_struct, _ptr
+    from .sampling_error import _FESpace
+    pts, wts = triangle_rule(quadorder)
+    X = space.physical_points(pts)
+    fqp = np.ascontiguousarray(np.broadcast_to(np.asarray(f(X[..., 0], X[..., 1]), dtype=np.float64), X.shape[:2]))
+    mesh, keep = _mesh_struct(space)
+    xref = np.ascontiguousarray(pts, dtype=np.float64)
+    w = np.ascontiguousarray(wts, dtype=np.float64)
+    q = _Quad(len(w), _ptr(xref), _ptr(w), 0, None, None)
+    cd = np.ascontiguousarray(space.celldofs + 1, dtype=np.int64)
+    fs = _FESpace(space.order, space.ndofs, cd.ctypes.data)
+    return mesh, q, fs, fqp, (keep, xref, w, cd)
+
+
+def _with_ctx(device, ctx, call):
+    from . import _lib
     own = ctx is None
     ctx = _lib.Context(device) if own else ctx
     try:
-        ctx._check(ctx.lib.sgfem_assemble_stiffness(ctx.h, ctypes.byref(mesh), ctypes.byref(fs), ctypes.byref(c), m0,
-                                                    m1, ctypes.byref(q), nnz, _lib._i64p(colptr), _lib._i64p(rowval),
-                                                    _lib._dp(vals)))
+        ctx._check(call(ctx))
     finally:
         if own:
             ctx.close()
-    return [sp.csr_matrix((vals[i], col, indptr), shape=(n, n)) for i in range(m1 - m0 + 1)]
+
+
+def assemble_rhs_gpu(space, f, quadorder, device=0, ctx=None):
+    """assemble_rhs on the GPU (sgfem_assemble_rhs): b = (f, v) with f evaluated
+    on the host at the quadrature points and the cell sums on the device."""
+    import ctypes
+    from . import _lib
+    mesh, q, fs, fqp, keep = _gpu_rhs_args(space, f, quadorder)
+    b = np.zeros(space.ndofs)
+    _with_ctx(device, ctx, lambda c: c.lib.sgfem_assemble_rhs(c.h, ctypes.byref(mesh), ctypes.byref(fs),
+                                                              ctypes.byref(q), _lib._dp(fqp), _lib._dp(b)))
+    return b
+
+
+def assemble_pce_rhs_gpu(space, coef, multi_indices, f, quadorder, factor=-1.0, N_truncate=None, device=0, ctx=None):
+    """assemble_pce_rhs on the GPU (sgfem_assemble_pce_rhs): b_mu = (lambda_mu f, v)
+    for every multi-index, flattened mode-major (SGFEVector layout)."""
+    import ctypes
+    from . import _lib
+    from .estimate import _Cosine, _ptr
+    mesh, q, fs, fqp, keep = _gpu_rhs_args(space, f, quadorder)
+    P = len(multi_indices)
+    M = max(len(mi) for mi in multi_indices)
+    mis = np.zeros((P, M), dtype=np.int32)
+    for k, mi in enumerate(multi_indices):
+        mis[k, :len(mi)] = mi
+    N = coef.maxm() if N_truncate is None else N_truncate
+    dfac = np.ascontiguousarray(coef.decay_factors, dtype=np.float64)
+    b1 = np.ascontiguousarray(coef.b1, dtype=np.int64)
+    b2 = np.ascontiguousarray(coef.b2, dtype=np.int64)
+    c = _Cosine(coef.maxm(), coef.meanvalue(), coef.freq, _ptr(dfac), _ptr(b1), _ptr(b2))
+    b = np.zeros((P, space.ndofs))
+    _with_ctx(device, ctx, lambda cx: cx.lib.sgfem_assemble_pce_rhs(
+        cx.h, ctypes.byref(mesh), ctypes.byref(fs), ctypes.byref(q), _lib._dp(fqp), ctypes.byref(c), M, P,
+        mis.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), float(factor), int(N), _lib._dp(b)))
+    return b.ravel()

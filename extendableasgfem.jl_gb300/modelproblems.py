@@ -21,7 +21,8 @@ import numpy as np
 
 from . import _lib
 from .fem import (assemble_convection, assemble_laplacian, assemble_pce_rhs, assemble_rhs, assemble_stiffness,
-                  assemble_stiffness_gpu)
+                  assemble_stiffness_gpu, assemble_rhs_gpu, assemble_pce_rhs_gpu, assemble_laplacian_gpu,
+                  assemble_convection_gpu)
 
 
 class AbstractModelProblem:
@@ -112,7 +113,9 @@ class SGOperator:
 def assemble(problem, sol, C, rhs, bonus_quadorder_a=2, bonus_quadorder_f=0, device=None):
     """Spatial blocks: poisson_primal.jl:55-68 ([K_0..K_M], b = (f, v)) or
     logpoisson_primal.jl:97-131 ([A, N_1..N_M], b_mu = (lambda_mu f, v) for all modes).
-    device=k assembles the K_m of PoissonProblemPrimal on GPU k (sgfem_assemble_stiffness)."""
+    device=k assembles on GPU k: the K_m (sgfem_assemble_stiffness), b (sgfem_assemble_rhs),
+    and A, N_m, b_mu of the lognormal problem (sgfem_assemble_stiffness with a = 1,
+    sgfem_assemble_convection, sgfem_assemble_pce_rhs)."""
     if problem is not PoissonProblemPrimal and problem is not LogTransformedPoissonProblemPrimal:
         raise NotImplementedError(f"no assembly for {problem}")
     if rhs is None:
@@ -121,15 +124,25 @@ def assemble(problem, sol, C, rhs, bonus_quadorder_a=2, bonus_quadorder_f=0, dev
     p = FES.order
     M = sol.TB.maxlength_multiindices()
     if problem is LogTransformedPoissonProblemPrimal:
-        A = assemble_laplacian(FES)
-        Ns = assemble_convection(FES, C, list(range(1, M + 1)), p + (p - 1) + bonus_quadorder_a)
-        b = assemble_pce_rhs(FES, C, [sol.TB.multi_indices[k] for k in sol.active_modes], rhs, p + bonus_quadorder_f)
+        mis = [sol.TB.multi_indices[k] for k in sol.active_modes]
+        qa = p + (p - 1) + bonus_quadorder_a
+        if device is None:
+            A = assemble_laplacian(FES)
+            Ns = assemble_convection(FES, C, list(range(1, M + 1)), qa)
+            b = assemble_pce_rhs(FES, C, mis, rhs, p + bonus_quadorder_f)
+        else:
+            A = assemble_laplacian_gpu(FES, device=device)
+            Ns = assemble_convection_gpu(FES, C, list(range(1, M + 1)), qa, device=device)
+            b = assemble_pce_rhs_gpu(FES, C, mis, rhs, p + bonus_quadorder_f, device=device)
         return [A] + Ns, b
     if device is None:
         Ks = assemble_stiffness(FES, C, list(range(M + 1)), 2 * (p - 1) + bonus_quadorder_a)
     else:
         Ks = assemble_stiffness_gpu(FES, C, list(range(M + 1)), 2 * (p - 1) + bonus_quadorder_a, device=device)
-    b0 = assemble_rhs(FES, rhs, p + bonus_quadorder_f)
+    if device is None:
+        b0 = assemble_rhs(FES, rhs, p + bonus_quadorder_f)
+    else:
+        b0 = assemble_rhs_gpu(FES, rhs, p + bonus_quadorder_f, device=device)
     return Ks, b0
 
 

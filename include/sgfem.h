@@ -383,7 +383,12 @@ SGFEM_API int sgfem_adjoint_gradient(sgfem_context* ctx, const double* U, const 
  * skip their blocks.  The apply's launch shape is chosen at finalize by timing
  * the candidates (sgfem_batch_tuning reports them).  x_out receives the
  * solutions, problem after problem, each n x P column-major (may be NULL).
- * FP64; per-problem reductions in a fixed order.  M <= 255.
+ * Mixed precision by default: iterative refinement whose residuals are FP64
+ * applies of every unconverged problem, with an FP32 PCG (FP32 operator and
+ * preconditioner tables, FP64 solution accumulation) as the correction solve;
+ * stats report the FP64 residuals.  SGFEM_BATCH_PRECISION=fp64 in the
+ * environment selects the plain FP64 PCG.  Per-problem reductions run in a
+ * fixed order.  M <= 255.
  */
 typedef struct sgfem_batch sgfem_batch;
 typedef struct {
@@ -427,6 +432,37 @@ SGFEM_API int sgfem_batch_problem_stats(const sgfem_batch* batch, int i, int* it
 SGFEM_API int sgfem_assemble_stiffness(sgfem_context* ctx, const sgfem_mesh* mesh, const sgfem_fe_space* space,
                                        const sgfem_cosine* coef, int m0, int m1, const sgfem_quadrature* quad,
                                        int64_t nnz, const int64_t* colptr, const int64_t* rowval, double* values);
+/* the convection blocks of solve!(LogTransformedPoissonProblemPrimal),
+   N_m[i, j] = -(grad a_m . grad phi_j, phi_i) for m = m0..m1 (logpoisson_primal.jl:
+   101-107; N_0 = 0), same arguments and layout as sgfem_assemble_stiffness (row i
+   of the CSC pattern tests with phi_i, column j is the ansatz) */
+SGFEM_API int sgfem_assemble_convection(sgfem_context* ctx, const sgfem_mesh* mesh, const sgfem_fe_space* space,
+                                        const sgfem_cosine* coef, int m0, int m1, const sgfem_quadrature* quad,
+                                        int64_t nnz, const int64_t* colptr, const int64_t* rowval, double* values);
+
+/*
+ * Right-hand sides assembled on the GPU (the reference assembles them on the
+ * host with ExtendableFEM's LinearOperator).  f_qp: the caller's f at the points
+ * of the cell rule `quad`, nq x ncells (f_qp[c * nq + q]), as for the
+ * estimators.  Each dof sums its cells in increasing cell order (no atomics).
+ * sgfem_assemble_rhs: b = (f, v), b[ndofs], of solve!(PoissonProblemPrimal)
+ *   (poisson_primal.jl:65-68).
+ * sgfem_assemble_pce_rhs: b[:, k] = (lambda_k f, v) for the P multi-indices of
+ *   solve!(LogTransformedPoissonProblemPrimal) (logpoisson_primal.jl:109-131),
+ *   lambda_mu(x) = exp(sum_{m <= N_truncate} a_m(x)^2 / 2) exp(factor a_0)
+ *   prod_d a_d(x)^mu_d / (sqrt(prod_d mu_d!) factor^|mu|) (lambda_mu of
+ *   expa_PCE_mop, coefficients.jl:219-260; the reference passes factor = -1 and
+ *   N_truncate = maxm).  multi_indices: M x P column-major (entry d of mode k at
+ *   [k * M + d]), M, N_truncate <= coef->maxm; b: ndofs x P column-major
+ *   (SGFEVector entries).
+ * ctx only names the GPU, the stream and the error message.
+ */
+SGFEM_API int sgfem_assemble_rhs(sgfem_context* ctx, const sgfem_mesh* mesh, const sgfem_fe_space* space,
+                                 const sgfem_quadrature* quad, const double* f_qp, double* b);
+SGFEM_API int sgfem_assemble_pce_rhs(sgfem_context* ctx, const sgfem_mesh* mesh, const sgfem_fe_space* space,
+                                     const sgfem_quadrature* quad, const double* f_qp, const sgfem_cosine* coef,
+                                     int64_t M, int64_t P, const int32_t* multi_indices, double factor,
+                                     int64_t N_truncate, double* b);
 
 /* which FP32 apply kernel a finalized context uses: 1 = specialised to the coupling
    structure (compiled with NVRTC at finalize), 0 = generic; the log says why */

@@ -2,7 +2,10 @@
 (sgfem_assemble_stiffness) against the host assembly (the caller-side
 restatement of ExtendableFEM's BilinearOperator assembly, poisson_primal.jl:
 56-68): same pattern, values within 1e-13 of the largest entry, bitwise
-reproducible, and a solve on GPU-assembled blocks matches one on host blocks."""
+reproducible, and a solve on GPU-assembled blocks matches one on host blocks.
+Right-hand sides (sgfem_assemble_rhs, sgfem_assemble_pce_rhs) against the host
+LinearOperator restatement (poisson_primal.jl:65-68, logpoisson_primal.jl:
+109-131 with lambda_mu of coefficients.jl:219-260)."""
 import numpy as np
 import pytest
 
@@ -40,7 +43,7 @@ def test_solve_on_gpu_assembled_blocks(built_pkg):
     f = lambda x, y: np.ones_like(x)
     Kh, b0 = pkg.assemble(pkg.PoissonProblemPrimal, sol, C, rhs=f)
     Kg, b0g = pkg.assemble(pkg.PoissonProblemPrimal, sol, C, rhs=f, device=0)
-    assert np.array_equal(b0, b0g)
+    assert np.abs(b0 - b0g).max() <= 1e-14 * np.abs(b0).max()
     xs = []
     for Ks in (Kh, Kg):
         op = pkg.SGOperator(V, TB, Ks, device=0)
@@ -61,3 +64,86 @@ def test_assembly_argument_errors(built_pkg):
         pkg.assemble_stiffness_gpu(V, C, [0, 2], 2)  # not a contiguous range of terms
     with pytest.raises(pkg.SGError):
         pkg.assemble_stiffness_gpu(V, C, list(range(0, 12)), 2)  # beyond maxm = 10
+
+
+@pytest.mark.parametrize("order,N,qo", [(1, 16, 1), (2, 12, 2), (2, 8, 4)])
+def test_gpu_rhs_matches_host(built_pkg, order, N, qo):
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    V = pkg.H1Pk(pkg.unit_square_mesh(N), order)
+    f = lambda x, y: np.sin(3 * x) * (1 + y * y) - 0.5
+    host = pkg.assemble_rhs(V, f, qo)
+    gpu = pkg.assemble_rhs_gpu(V, f, qo)
+    assert np.abs(host - gpu).max() <= 1e-14 * np.abs(host).max()
+    assert np.array_equal(gpu, pkg.assemble_rhs_gpu(V, f, qo))
+
+
+@pytest.mark.parametrize("order,N,M,deg,factor,ntrunc", [(1, 16, 4, 2, -1.0, None), (2, 8, 6, 3, -1.0, 8),
+                                                         (1, 8, 3, 3, 0.5, 3)])
+def test_gpu_pce_rhs_matches_host(built_pkg, order, N, M, deg, factor, ntrunc):
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=0.3, maxm=20)
+    V = pkg.H1Pk(pkg.unit_square_mesh(N), order)
+    mis = pkg.total_degree_multiindices(M, deg)
+    f = lambda x, y: 1.0 + x * y
+    qo = order + 1
+    host = pkg.assemble_pce_rhs(V, C, mis, f, qo, factor=factor, N_truncate=ntrunc)
+    gpu = pkg.assemble_pce_rhs_gpu(V, C, mis, f, qo, factor=factor, N_truncate=ntrunc)
+    n = V.ndofs
+    for k in range(len(mis)):
+        h, g = host[k * n:(k + 1) * n], gpu[k * n:(k + 1) * n]
+        assert np.abs(h - g).max() <= 1e-13 * max(np.abs(h).max(), 1e-300), (k, mis[k])
+
+
+def test_lognormal_solve_on_gpu_rhs(built_pkg):
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=0.0, maxm=150)
+    V = pkg.H1Pk(pkg.unit_square_mesh(16), 1)
+    mis = pkg.total_degree_multiindices(4, 2)
+    TB = pkg.TensorizedBasis(pkg.HermitePolynomials, 4, 2, 6, multi_indices=mis)
+    sol = pkg.SGFEVector(V, TB)
+    f = lambda x, y: np.ones_like(x)
+    Kh, bh = pkg.assemble(pkg.LogTransformedPoissonProblemPrimal, sol, C, rhs=f)
+    Kg, bg = pkg.assemble(pkg.LogTransformedPoissonProblemPrimal, sol, C, rhs=f, device=0)
+    assert np.abs(bh - bg).max() <= 1e-13 * np.abs(bh).max()
+    for m, (A, B) in enumerate(zip(Kh, Kg)):
+        assert abs(A - B).max() <= 1e-13 * abs(A).max(), m
+    xs = []
+    for Ks, b in ((Kh, bh), (Kg, bg)):
+        op = pkg.SGOperator(V, TB, Ks, device=0)
+        x = np.zeros(V.ndofs * TB.nmodes)
+        st = op.solve_logpoisson(b, x, rtol=1e-10, precision=pkg.FP64)
+        assert st["relres"] <= 1e-10
+        xs.append(x)
+        op.close()
+    assert np.linalg.norm(xs[0] - xs[1]) <= 1e-10 * np.linalg.norm(xs[0])
+
+
+@pytest.mark.parametrize("order,N,M", [(1, 16, 5), (2, 8, 4)])
+def test_gpu_convection_matches_host(built_pkg, order, N, M):
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=0.0, maxm=20)
+    V = pkg.H1Pk(pkg.unit_square_mesh(N), order)
+    qa = 2 * order - 1 + 2
+    host = pkg.assemble_convection(V, C, list(range(1, M + 1)), qa)
+    gpu = pkg.assemble_convection_gpu(V, C, list(range(1, M + 1)), qa)
+    for m, (A, B) in enumerate(zip(host, gpu)):
+        assert abs(A - B).max() <= 1e-13 * abs(A).max(), m
+        assert abs(B - B.T).max() > 1e-3 * abs(B).max()   # non-symmetric: the orientation is checked
+    lap = pkg.assemble_laplacian_gpu(V)
+    assert abs(lap - pkg.assemble_laplacian(V)).max() <= 1e-13 * abs(lap).max()
+
+
+def test_rhs_argument_errors(built_pkg):
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=0.0, maxm=3)
+    V = pkg.H1Pk(pkg.unit_square_mesh(4), 1)
+    f = lambda x, y: np.ones_like(x)
+    with pytest.raises(pkg.SGError):
+        pkg.assemble_pce_rhs_gpu(V, C, pkg.total_degree_multiindices(4, 1), f, 2)  # M = 4 > maxm = 3
+    with pytest.raises(pkg.SGError):
+        pkg.assemble_pce_rhs_gpu(V, C, [[0, 1, 0]], f, 2, factor=0.0)
