@@ -427,6 +427,54 @@ def run_config1(args):
     print(json.dumps(line), flush=True)
 
 
+def run_equilibration(args):
+    """Equilibration estimator (sgfem_estimate_equilibration) on the config 1 basis
+    (M=5, total degree 2, P=21) for P1 meshes of 32x32 and 128x128 and a P2 64x64
+    mesh, on the solved SG system; the oracle (pure Python, one thread) on the P1
+    8x8 mesh is the CPU rate, compared per (cell, extended mode)."""
+    import __graft_entry__ as ge
+    from oracle import basis as ob
+    from oracle import coefficient as oc
+    from oracle import equilibration as oq
+    from oracle import fem as of
+    pkg = ge.load_package()
+    f = lambda x, y: np.ones_like(x)
+    cases = []
+    for N, order in ((32, 1), (128, 1), (64, 2)):
+        C, V, TB, sol, Ks, b0 = config1_problem(pkg, N=N)
+        if order == 2:
+            V = pkg.H1Pk(pkg.unit_square_mesh(N), 2)
+            sol = pkg.SGFEVector(V, TB)
+            Ks, b0 = pkg.assemble(pkg.PoissonProblemPrimal, sol, C, rhs=f)
+        op = pkg.SGOperator(V, TB, Ks, device=0)
+        op.solve_primal(b0, sol.entries, rtol=1e-10, precision=pkg.FP64)
+        pkg.estimate_equilibration(pkg.PoissonProblemPrimal, sol, C, rhs=f, op=op)
+        ts = []
+        for _ in range(max(1, args.steps)):
+            (em, ec, ext), t = _timed(lambda: pkg.estimate_equilibration(pkg.PoissonProblemPrimal, sol, C, rhs=f,
+                                                                         op=op))
+            ts.append(t)
+        op.close()
+        cases.append({"mesh": f"P{order} {N}x{N}", "ncells": V.mesh.ncells, "P_ext": len(ext),
+                      "gpu_ms_wall": statistics.median(ts),
+                      "us_per_cell_mode": statistics.median(ts) * 1e3 / (V.mesh.ncells * len(ext))})
+    C, V, TB, sol, Ks, b0 = config1_problem(pkg, N=8)
+    Vo = of.LagrangeSpace(of.StructuredMesh(8), 1)
+    Co = oc.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    U = np.random.default_rng(3).standard_normal(V.ndofs * TB.nmodes)
+    t = time.perf_counter()
+    _, oec, oext = oq.estimate_equilibration(Vo, U, TB.multi_indices, ob.LEGENDRE, Co, lambda x, y: 1.0 + 0 * x)
+    t_cpu = (time.perf_counter() - t) * 1e3
+    cpu_rate = t_cpu * 1e3 / (Vo.mesh.ncells * len(oext))
+    line = {"workload": "equilibration estimator: config 1 basis (M=5, total degree 2, P=21), RT_k patch problems on "
+                        "every node, div penalty 1e5",
+            "cases": cases,
+            "cpu_baseline": {"kind": "port", "cores": 1, "sample": "oracle on P1 8x8 (128 cells)",
+                             "ms": t_cpu, "us_per_cell_mode": cpu_rate},
+            "speedup_per_cell_mode_vs_cpu": cpu_rate / cases[1]["us_per_cell_mode"]}
+    print(json.dumps(line), flush=True)
+
+
 def run_lognormal(args):
     """Config 3 lognormal variant: LogTransformedPoissonProblemPrimal, Hermite,
     P1 128x128 (16641 dofs), M=10, 80 top-weight multi-indices, mean 0, tau=0.9;
@@ -645,7 +693,7 @@ def main():
                     help="profiling target for ncu: set up the workload, run the kernel(s) a few times, exit")
     ap.add_argument("--mesh", type=int, default=256, help="mesh size for --profile / --workload adjoint")
     ap.add_argument("--workload", choices=["config2", "config1", "lognormal", "sampling", "adjoint", "batch",
-                                           "assembly"],
+                                           "assembly", "equilibration"],
                     default="config2", help="config2 is the headline bench line; the others print their own line")
     ap.add_argument("--samples", type=int, default=100000, help="--workload sampling: number of samples")
     ap.add_argument("--directions", type=int, default=20, help="--workload adjoint: finite-difference directions")
@@ -656,7 +704,8 @@ def main():
         return run_profile(args)
     if args.workload != "config2":
         return {"config1": run_config1, "lognormal": run_lognormal, "sampling": run_sampling,
-                "adjoint": run_adjoint, "batch": run_batch, "assembly": run_assembly}[args.workload](args)
+                "adjoint": run_adjoint, "batch": run_batch, "assembly": run_assembly,
+                "equilibration": run_equilibration}[args.workload](args)
     rank, world, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world, pg)

@@ -10,7 +10,7 @@ from ._lib import FP32, FP64, MIXED, PREC_JACOBI, PREC_LATTICE, PREC_NONE, SGErr
 from .adjoint import MeanQoI
 from .batch import SGBatch, config4_problems, splitmix64
 from .coefficients import StochasticCoefficientCosinus
-from .estimate import estimate, extension_couplings
+from .estimate import estimate, estimate_equilibration, extension_couplings
 from .fem import (H1Pk, assemble_convection, assemble_laplacian, assemble_pce_rhs, assemble_rhs, assemble_stiffness,
                   assemble_stiffness_gpu, assemble_rhs_gpu, assemble_pce_rhs_gpu, assemble_laplacian_gpu,
                   assemble_convection_gpu,

@@ -237,3 +237,57 @@ def _estimate_log(sol, C, rhs, bonus_quadorder, tail_extension, face_points, dev
             ctx.close()
     del keep
     return eta4modes, eta4cell.T, ext, float(zeta[0] - zeta[1])
+
+
+def estimate_equilibration(problem, sol, C, rhs=None, tail_extension=(10, 2), bonus_quadorder=0, FETypeDual=None,
+                           div_penalty=1.0e5, quadorder=None, device=0, op=None):
+    """estimate_equilibration(PoissonProblemPrimal, sol, C; rhs, tail_extension)
+    (src/estimate.jl:607-954) on the GPU (sgfem_estimate_equilibration): local
+    RT_k flux equilibration on every node patch, k the order of the space.
+    Returns (eta4modes, eta4cell, multi_indices_extended), eta4cell (ncells, P_ext).
+    The cell rule has order 2 (k + 1) like the reference's (``quadorder``
+    overrides it); ``bonus_quadorder`` is accepted and unused, as in the reference.
+    The reference's default tail_extension = 5 cannot reach add_boundary_modes,
+    which reads tail_extension[2]; a pair is required."""
+    if problem is not PoissonProblemPrimal:
+        raise NotImplementedError(f"no equilibration estimator for {problem}")
+    if rhs is None:
+        raise ValueError("need right-hand side")
+    if FETypeDual is not None:
+        raise NotImplementedError("the flux space is RT_k with k the order of the H1Pk space")
+    if isinstance(tail_extension, (int, np.integer)):
+        raise TypeError("tail_extension needs two entries (add_boundary_modes reads tail_extension[2])")
+    FES = sol.FES_space[0]
+    mesh = FES.mesh
+    TB = sol.TB
+    ext, (ptr, ms, nus, gs) = extension_couplings(TB.multi_indices, TB.basis, tail_extension)
+    P_ext, M_ext = len(ext), len(ext[0])
+    if C.maxm() < M_ext:
+        raise ValueError(f"coefficient maxm = {C.maxm()} < extended length {M_ext}")
+    pts, wts = triangle_rule(2 * (FES.order + 1) if quadorder is None else quadorder)
+    X = FES.physical_points(pts)
+    fq = np.ascontiguousarray(np.broadcast_to(np.asarray(rhs(X[..., 0], X[..., 1]), dtype=np.float64), X.shape[:2]))
+    m, keep = _mesh_struct(FES)
+    xref = np.ascontiguousarray(pts, dtype=np.float64)
+    w = np.ascontiguousarray(wts, dtype=np.float64)
+    q = _Quad(len(w), _ptr(xref), _ptr(w), 0, None, None)
+    dfac = np.ascontiguousarray(C.decay_factors, dtype=np.float64)
+    b1 = np.ascontiguousarray(C.b1, dtype=np.int64)
+    b2 = np.ascontiguousarray(C.b2, dtype=np.int64)
+    c = _Cosine(C.maxm(), C.mean_value, C.freq, _ptr(dfac), _ptr(b1), _ptr(b2))
+    e = _Ext(P_ext, M_ext, _ptr(ptr), _ptr(ms), _ptr(nus), _ptr(gs))
+    eta4modes = np.zeros(P_ext)
+    eta4cell = np.zeros((P_ext, mesh.ncells))
+    ctx = op.ctx if op is not None else _light_context(FES, TB, device)
+    try:
+        solv = np.ascontiguousarray(sol.entries, dtype=np.float64)
+        dp = lambda a_: a_.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        rc = _lib.load().sgfem_estimate_equilibration(ctx.h, dp(solv), ctypes.byref(m), ctypes.byref(q), dp(fq),
+                                                      ctypes.byref(c), ctypes.byref(e), float(div_penalty),
+                                                      dp(eta4modes), dp(eta4cell))
+        ctx._check(rc)
+    finally:
+        if op is None:
+            ctx.close()
+    del keep
+    return eta4modes, eta4cell.T, ext

@@ -287,6 +287,27 @@ SGFEM_API int sgfem_estimate_logpoisson(sgfem_context* ctx, const double* sol, c
                                         double* eta4modes, double* eta4cell, double* zeta);
 
 /*
+ * estimate_equilibration(::Type{PoissonProblemPrimal}, sol, C; rhs,
+ * tail_extension), src/estimate.jl:607-954: for every node z and extended mode
+ * j the flux sigma_{z,j} in RT_k (k = mesh->order, HDIVRTk{2, k}) on the node
+ * patch that minimises ||sigma - phi_z F_j||^2 + sum_T div_penalty sqrt|T|
+ * ||div sigma - (F_j . grad phi_z - f phi_z [j = 1])||_T^2 with zero normal flux
+ * on the edges the patch shares with outside cells, F_j = sum over ext's list j
+ * of g a_m grad u_nu; then eta4cell[c + j ncells] = sum_q w_q |T| (|F_j -
+ * sigma_j|^2 + (f [j = 1] + div sigma_j)^2 / pi^2), sigma_j = sum_z sigma_{z,j},
+ * eta4modes[j] = sqrt(sum_c eta4cell[c + j ncells]).  The reference's penalty is
+ * div_penalty = 1e5 and its cell rule has order 2 (k + 1).  mesh: coords,
+ * cell_nodes, cell_dofs, cell_faces, face_nodes, face_cells, cell_volumes;
+ * quad: the cell rule (the face rule is not used); f_qp: nq x ncells.  Each
+ * node patch is solved on its own (the reference groups disjoint patches
+ * into one system, NodePatchGroups).  A patch may hold at most 120 flux dofs.
+ */
+SGFEM_API int sgfem_estimate_equilibration(sgfem_context* ctx, const double* sol, const sgfem_mesh* mesh,
+                                           const sgfem_quadrature* quad, const double* f_qp,
+                                           const sgfem_cosine* coef, const sgfem_extension* ext, double div_penalty,
+                                           double* eta4modes, double* eta4cell);
+
+/*
  * Evaluation of an SG solution at parameter samples and the sampling error.
  *
  * sgfem_evaluate_samples: batched set_sample!(SGFEV, y[1:m])

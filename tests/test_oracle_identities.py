@@ -166,3 +166,51 @@ def test_sine_transform_blocks_of_lattice_stiffness(order, N):
                             for cy in range(2) for cx in range(2) for dy in range(-R, R + 1) for dx in range(-R, R + 1)
                             if w[cy, cx, dy + R, dx + R] != 0.0)
                     assert abs(B - T[pos(fx[a % 2], fy[a // 2]), pos(fx[b % 2], fy[b // 2])]) <= 1e-12
+
+
+@pytest.mark.parametrize("k", [1, 2])
+def test_equilibration_rt_space_is_conforming(k):
+    """The oracle's RT_k basis (per physical cell, dual to normal-flux point
+    values on each edge and interior moments): the normal flux of a face dof
+    agrees from both sides of the face, every other basis function of the two
+    cells has zero normal flux there, and div maps onto P_k (piecewise)."""
+    from oracle import equilibration as oq
+    from oracle import fem as of
+    m = of.StructuredMesh(3)
+    rt = oq.RTSpace(m, k)
+    worst = 0.0
+    for f in range(m.nfaces):
+        c0, c1 = m.face_cells[f]
+        if c1 < 0:
+            continue
+        A, B = sorted(m.face_nodes[f])
+        pa, pb = m.coords[A], m.coords[B]
+        nrm = np.array([pb[1] - pa[1], -(pb[0] - pa[0])])
+        for t in (0.11, 0.5, 0.83):
+            x = pa + t * (pb - pa)
+            flux = {}
+            for c in (c0, c1):
+                v, _ = rt.eval(c, x)
+                for i, dof in enumerate(rt.celldofs[c]):
+                    on_face = (k + 1) * f <= dof < (k + 1) * (f + 1)
+                    if on_face:
+                        flux.setdefault(dof, []).append(v[i] @ nrm)
+                    else:
+                        worst = max(worst, abs(v[i] @ nrm))
+            for vals in flux.values():
+                assert len(vals) == 2
+                worst = max(worst, abs(vals[0] - vals[1]))
+    assert worst <= 1e-10
+
+
+def test_equilibration_oracle_vanishes_for_zero_data():
+    """u_h = 0 and f = 0: every local flux and the estimate vanish."""
+    from oracle import basis as ob
+    from oracle import coefficient as oc
+    from oracle import equilibration as oq
+    from oracle import fem as of
+    V = of.LagrangeSpace(of.StructuredMesh(3), 1)
+    C = oc.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=40)
+    mis = [[0, 0], [1, 0], [0, 1]]
+    em, ec, ext = oq.estimate_equilibration(V, np.zeros(V.ndofs * 3), mis, ob.LEGENDRE, C, lambda x, y: 0.0 * x)
+    assert np.all(em == 0.0) and np.all(ec == 0.0)
