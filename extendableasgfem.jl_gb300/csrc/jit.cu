@@ -1187,7 +1187,7 @@ sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const 
                         if (dy < -HY || dy > HY || wx < 0 || wx >= SW) bad = 1;
                         else off = ((cy % WL) * SW + wx) * LD;
                     }
-#pragma unroll 2
+#pragma unroll UNROLL
                     for (int t = 0; t < cnt; ++t) {
                         const float* xr = win + __shfl_sync(0xffffffffu, off, t) + lane;
                         const float4* cv = reinterpret_cast<const float4*>(cbuf + t * M1P);
@@ -1256,6 +1256,9 @@ sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const 
     }
 }
 )";
+    const std::string pu = "#pragma unroll UNROLL";
+    const size_t at = s.find(pu);
+    if (at != std::string::npos) s.replace(at, pu.size(), "#pragma unroll " + std::to_string(ctx->jit_unroll));
     return s;
 }
 
@@ -1316,6 +1319,8 @@ void sg_jit_configure(sgfem_context* ctx) {
     ctx->jit_wwpb = eww ? std::max(1, std::min(32, atoi(eww))) : 12;
     const char* ewr = getenv("SGFEM_JIT_WRW");
     ctx->jit_wrw = ewr ? std::max(1, std::min(8, atoi(ewr))) : 2;
+    const char* eun = getenv("SGFEM_JIT_UNROLL");
+    ctx->jit_unroll = eun ? std::max(1, std::min(4, atoi(eun))) : 1;
     const char* edf = getenv("SGFEM_JIT_DIFF");
     ctx->jit_diff_req = edf ? (atoi(edf) != 0) : 1;
     const char* en = getenv("SGFEM_JIT_PASSES");

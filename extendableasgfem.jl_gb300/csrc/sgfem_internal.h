@@ -134,6 +134,7 @@ struct sgfem_context {
     int jit_window = 0;                     // lattice-window kernel in use
     int jit_wwpb = 12;                      // its warps per block
     int jit_wrw = 2;                        // its rows per warp and lattice line
+    int jit_unroll = 1;                     // its unroll of the nonzero loop (SGFEM_JIT_UNROLL)
     int jit_minb = 0;                       // minimum resident blocks per SM asked of ptxas (0: none)
     int jit_async = 0;                      // cp.async ring variant of the kernel
     int jit_adepth = 6;                     // ring slots (nonzeros in flight + 1) per warp

@@ -219,6 +219,8 @@ KNOBS = [
     {"SGFEM_JIT_DIFF": "0"},
     {"SGFEM_JIT_WWPB": "4", "SGFEM_JIT_WRW": "3"},
     {"SGFEM_JIT_WRW": "1"},
+    {"SGFEM_JIT_UNROLL": "2"},
+    {"SGFEM_JIT_UNROLL": "4"},
     {"SGFEM_JIT_WINDOW": "0"},
     {"SGFEM_JIT_WINDOW": "0", "SGFEM_JIT_DIFF": "0"},
     {"SGFEM_JIT_WINDOW": "0", "SGFEM_JIT_PFD": "2"},
