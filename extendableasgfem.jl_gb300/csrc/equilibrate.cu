@@ -34,8 +34,11 @@
 // Device, per chunk of modes: (1) a warp per cell evaluates F_j at its
 // quadrature points (lanes over modes); (2) once, a block per patch assembles
 // the patch matrix (mass + div-div, the same for all modes) in shared memory
-// and factors it (Cholesky); (3) a block per patch solves every mode of the
-// chunk, a warp per mode (right-hand side, two triangular solves); (4) a warp
+// and factors it (Cholesky); (3) blocks per patch solve the modes of the
+// chunk, a thread per mode (the right-hand side is linear in F_j: per-slot
+// coefficient tables in shared memory; then two triangular solves), because
+// on GB300 every FP64 warp instruction costs the FP64 pipe 16 cycles and a
+// warp per mode left most lanes idle; (4) a warp
 // per cell adds sigma from its three vertex patches and integrates the
 // estimate (lanes over modes).  Fixed summation orders, no atomics: results are
 // bitwise reproducible.  FP64 throughout.
@@ -54,7 +57,6 @@ constexpr int QW = 4;        // warps per block of the per-cell kernels
 constexpr int QMAX = 16;     // largest cell rule
 constexpr int NBMAX = 15;    // RT_2 dofs per cell
 constexpr int PMAX = 120;    // largest patch system
-constexpr int SW = 8;        // warps per block of the patch solves
 
 struct QCell {
     double x0, y0, j00, j10, j01, j11, g[6], vol, det;
@@ -234,79 +236,100 @@ __global__ void k_eq_factor(EqArgs a) {
         __syncthreads();
     }
     double* Lz = a.L + a.lofs[z];
-    for (int t = threadIdx.x; t < n * n; t += blockDim.x) Lz[t] = A[t];
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) Lz[t] = (t % (n + 1) == 0) ? 1.0 / A[t] : A[t];
 }
 
-// (3) the modes of the chunk on one patch: a warp per mode
-__global__ void __launch_bounds__(SW * 32) k_eq_solve(EqArgs a, int j0, int nj, int ns_max) {
+// (3) the modes of the chunk on one patch, a thread per mode.  The right-hand side
+// is linear in F: b_i = sum_{s,q} C[s,q,i] . F_j(s,q) - [j = 0] sum_{s,q} pen_w f phi_z div phi_i
+// with C = w phi_z phi_i + pen_w div phi_i grad phi_z (pen_w = pen sqrt|T| w |T|), so
+// the block builds C of one slot at a time in shared memory and every thread
+// accumulates its own mode's b, then solves L L^T x = b with the factor in
+// shared memory (its diagonal stored inverted).  Block (z, g) takes the modes
+// g * blockDim.x .. of the chunk.
+__global__ void k_eq_solve(EqArgs a, int j0, int nj) {
     extern __shared__ double ssm[];
     const int z = blockIdx.x;
     const int n = a.pn[z];
     if (n == 0) return;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int s0 = a.pptr[z], ns = a.pptr[z + 1] - s0;
-    double* L = ssm;
-    double* bv = L + (size_t)n * n;                          // ns x nq x nb x 2
-    double* bd = bv + (size_t)ns_max * a.nq * a.nb * 2;      // ns x nq x nb
-    double* rb = bd + (size_t)ns_max * a.nq * a.nb;          // SW x n
+    const int nt = blockDim.x;
+    double* L = ssm;                              // n x n
+    double* C = L + (size_t)n * n;                // nq x nb x 2 (one slot)
+    double* D = C + (size_t)a.nq * a.nb * 2;      // nb: the f term of one slot
+    double* B = D + a.nb;                         // n x nt: b of each thread's mode
+    __shared__ int smap[NBMAX];
     const double* Lz = a.L + a.lofs[z];
-    for (int t = threadIdx.x; t < n * n; t += blockDim.x) L[t] = Lz[t];
+    for (int t = threadIdx.x; t < n * n; t += nt) L[t] = Lz[t];
+    for (int t = threadIdx.x; t < n * nt; t += nt) B[t] = 0.0;
     for (int s = 0; s < ns; ++s) {
         const int c = a.pcell[s0 + s];
-        eq_cell_basis(a, c, a.cg[c], bv + (size_t)s * a.nq * a.nb * 2, bd + (size_t)s * a.nq * a.nb, threadIdx.x,
-                      blockDim.x);
-    }
-    __syncthreads();
-    double* b = rb + (size_t)warp * n;
-    for (int jj = warp; jj < nj; jj += SW) {
-        const int j = j0 + jj;
-        for (int p = lane; p < n; p += 32) b[p] = 0.0;
-        __syncwarp();
-        for (int s = 0; s < ns; ++s) {
-            const int c = a.pcell[s0 + s];
-            const int loc = a.ploc[s0 + s];
-            const QCell G = a.cg[c];
-            const double gzx = G.g[2 * loc], gzy = G.g[2 * loc + 1];
-            const double sv = sqrt(G.vol);
-            const int p = lane < a.nb ? a.pmap[(size_t)(s0 + s) * a.nb + lane] : -1;
-            const double* bvs = bv + (size_t)s * a.nq * a.nb * 2;
-            const double* bds = bd + (size_t)s * a.nq * a.nb;
-            double acc = 0.0;
+        const int loc = a.ploc[s0 + s];
+        const QCell G = a.cg[c];
+        const double inv = 1.0 / G.det, sv = sqrt(G.vol);
+        const short* map = a.pmap + (size_t)(s0 + s) * a.nb;
+        __syncthreads();  // the previous slot's tables are no longer read
+        for (int i = threadIdx.x; i < a.nb; i += nt) smap[i] = map[i];
+        for (int t = threadIdx.x; t < a.nq * a.nb; t += nt) {
+            const int q = t / a.nb, i = t - q * a.nb;
+            const double sg = a.csign[(size_t)c * a.nb + i] * inv;
+            const double r0 = a.rtv[2 * t], r1 = a.rtv[2 * t + 1];
+            const double vx = sg * (G.j00 * r0 + G.j01 * r1), vy = sg * (G.j10 * r0 + G.j11 * r1);
+            const double dv = sg * a.rtd[t];
+            const double xi = a.xq[2 * q], eta = a.xq[2 * q + 1];
+            const double phiz = loc == 0 ? 1.0 - xi - eta : (loc == 1 ? xi : eta);
+            const double w = a.wq[q] * G.vol;
+            const double pw = a.pen * sv * w * dv;
+            C[2 * t] = w * phiz * vx + pw * G.g[2 * loc];
+            C[2 * t + 1] = w * phiz * vy + pw * G.g[2 * loc + 1];
+        }
+        if (j0 == 0 && blockIdx.y == 0)  // the f term of mode 0, in quadrature-point order
+            for (int i = threadIdx.x; i < a.nb; i += nt) {
+                double acc = 0.0;
+                for (int q = 0; q < a.nq; ++q) {
+                    const int t = q * a.nb + i;
+                    const double dv = a.csign[(size_t)c * a.nb + i] * inv * a.rtd[t];
+                    const double xi = a.xq[2 * q], eta = a.xq[2 * q + 1];
+                    const double phiz = loc == 0 ? 1.0 - xi - eta : (loc == 1 ? xi : eta);
+                    const double w = a.wq[q] * G.vol;
+                    acc += a.pen * sv * w * dv * a.fqp[(size_t)c * a.nq + q] * phiz;
+                }
+                D[i] = acc;
+            }
+        __syncthreads();
+        const int jj = blockIdx.y * nt + threadIdx.x;
+        if (jj < nj) {
+            double* b = B + threadIdx.x;
+            const double* fl = a.FL + ((size_t)c * a.nq * nj + jj) * 2;
             for (int q = 0; q < a.nq; ++q) {
-                const double xi = a.xq[2 * q], eta = a.xq[2 * q + 1];
-                const double phiz = loc == 0 ? 1.0 - xi - eta : (loc == 1 ? xi : eta);
-                const double* fl = a.FL + (((size_t)c * a.nq + q) * nj + jj) * 2;
-                const double flx = fl[0], fly = fl[1];
-                const double w = a.wq[q] * G.vol;
-                double r = flx * gzx + fly * gzy;
-                if (j == 0) r -= a.fqp[(size_t)c * a.nq + q] * phiz;
-                if (p >= 0) {
-                    const double* vi = bvs + (q * a.nb + lane) * 2;
-                    acc += (flx * vi[0] + fly * vi[1]) * phiz * w;
-                    acc += a.pen * sv * w * r * bds[q * a.nb + lane];
+                const double fx = fl[(size_t)q * nj * 2], fy = fl[(size_t)q * nj * 2 + 1];
+                const double* Cq = C + (size_t)q * a.nb * 2;
+                for (int i = 0; i < a.nb; ++i) {
+                    const int p = smap[i];
+                    if (p >= 0) b[(size_t)p * nt] = fma(Cq[2 * i], fx, fma(Cq[2 * i + 1], fy, b[(size_t)p * nt]));
                 }
             }
-            if (p >= 0) b[p] += acc;
-            __syncwarp();
+            if (j0 + jj == 0)
+                for (int i = 0; i < a.nb; ++i)
+                    if (smap[i] >= 0) b[(size_t)smap[i] * nt] -= D[i];
         }
-        // L y = b, then L^T x = y
-        for (int k = 0; k < n; ++k) {
-            const double xk = b[k] / L[k * n + k];
-            for (int i = k + 1 + lane; i < n; i += 32) b[i] -= L[i * n + k] * xk;
-            __syncwarp();
-            if (lane == 0) b[k] = xk;
-            __syncwarp();
+    }
+    __syncthreads();
+    double* Sz = a.S + (size_t)a.sofs[z] * nj;
+    const int jj = blockIdx.y * nt + threadIdx.x;
+    if (jj < nj) {
+        double* b = B + threadIdx.x;
+        // L y = b, then L^T x = y (diagonal stored inverted)
+        for (int i = 0; i < n; ++i) {
+            double v = b[(size_t)i * nt];
+            for (int k = 0; k < i; ++k) v = fma(-L[i * n + k], b[(size_t)k * nt], v);
+            b[(size_t)i * nt] = v * L[i * n + i];
         }
-        for (int k = n - 1; k >= 0; --k) {
-            const double xk = b[k] / L[k * n + k];
-            for (int i = lane; i < k; i += 32) b[i] -= L[k * n + i] * xk;
-            __syncwarp();
-            if (lane == 0) b[k] = xk;
-            __syncwarp();
+        for (int i = n - 1; i >= 0; --i) {
+            double v = b[(size_t)i * nt];
+            for (int k = i + 1; k < n; ++k) v = fma(-L[k * n + i], b[(size_t)k * nt], v);
+            b[(size_t)i * nt] = v * L[i * n + i];
         }
-        double* Sz = a.S + (size_t)a.sofs[z] * nj;
-        for (int p = lane; p < n; p += 32) Sz[(size_t)p * nj + jj] = b[p];
-        __syncwarp();
+        for (int p = 0; p < n; ++p) Sz[(size_t)p * nj + jj] = b[(size_t)p * nt];
     }
 }
 
@@ -635,9 +658,8 @@ extern "C" int sgfem_estimate_equilibration(sgfem_context* ctx, const double* so
     std::vector<short> pmap((size_t)nslots * nb, -1);
     std::vector<int> pn(nn, 0);
     std::vector<long long> lofs(nn + 1, 0), sofs(nn + 1, 0);
-    int ns_max = 0, n_max = 0;
+    int n_max = 0;
     for (int64_t z = 0; z < nn; ++z) {
-        ns_max = std::max(ns_max, pptr[z + 1] - pptr[z]);
         std::vector<std::pair<int, int>> shared_edges;  // (face * 4 + l, patch dof)
         int cnt = 0;
         for (int s = pptr[z]; s < pptr[z + 1]; ++s) {
@@ -699,7 +721,10 @@ extern "C" int sgfem_estimate_equilibration(sgfem_context* ctx, const double* so
     cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
     const size_t smem_flux = (size_t)QW * ((Mext + 1) * nq + nq * nd * 2) * sizeof(double);
     const size_t smem_fac = ((size_t)n_max * n_max + (size_t)nq * nb * 3) * sizeof(double);
-    const size_t smem_sol = ((size_t)n_max * n_max + (size_t)ns_max * nq * nb * 3 + (size_t)SW * n_max) * sizeof(double);
+    int st = 128;  // threads (modes) per patch-solve block
+    auto sol_bytes = [&](int t) { return ((size_t)n_max * n_max + (size_t)nq * nb * 2 + nb + (size_t)n_max * t) * sizeof(double); };
+    while (st > 32 && (int64_t)sol_bytes(st) > dev_smem) st /= 2;
+    const size_t smem_sol = sol_bytes(st);
     const size_t smem_vol = (size_t)QW * nq * nb * 3 * sizeof(double);
     if ((int64_t)std::max({smem_flux, smem_fac, smem_sol, smem_vol}) > dev_smem)
         return fail(SGFEM_ERR_UNSUPPORTED, "node patches or coefficient terms too large for shared memory");
@@ -777,7 +802,7 @@ extern "C" int sgfem_estimate_equilibration(sgfem_context* ctx, const double* so
         const int nj = (int)std::min<int64_t>(CH, Pext - j0);
         k_eq_flux<<<gc, QW * 32, smem_flux, ctx->stream>>>(a, (int)j0, nj);
         SG_LAUNCHED(ctx);
-        k_eq_solve<<<(unsigned)nn, SW * 32, smem_sol, ctx->stream>>>(a, (int)j0, nj, ns_max);
+        k_eq_solve<<<dim3((unsigned)nn, (unsigned)((nj + st - 1) / st)), st, smem_sol, ctx->stream>>>(a, (int)j0, nj);
         SG_LAUNCHED(ctx);
         k_eq_volume<<<gc, QW * 32, smem_vol, ctx->stream>>>(a, (int)j0, nj, deta);
         SG_LAUNCHED(ctx);
