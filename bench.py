@@ -427,6 +427,33 @@ def run_config1(args):
     print(json.dumps(line), flush=True)
 
 
+def run_estimate(args):
+    """Config 2's estimator pass: estimate(PoissonProblemPrimal) of the mixed
+    solution of the headline workload (P2 256x256, M=20, P=150), default
+    bonus_quadorder = 1 and tail_extension = (10, 2); wall time of the whole call
+    (host extension of the multi-index set, argument setup, kernels)."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    V, TB, Ks, b0 = setup_workload(pkg, N=args.mesh)
+    op = pkg.SGOperator(V, TB, Ks, device=0)
+    sol = pkg.SGFEVector(V, TB)
+    st = op.solve_primal(b0, sol.entries, rtol=1e-8, precision=pkg.MIXED)
+    f = lambda x, y: np.ones_like(x)
+    pkg.estimate(pkg.PoissonProblemPrimal, sol, C, rhs=f, op=op)
+    ts = []
+    for _ in range(max(1, args.steps)):
+        (em, ec, ext), t = _timed(lambda: pkg.estimate(pkg.PoissonProblemPrimal, sol, C, rhs=f, op=op))
+        ts.append(t)
+    op.close()
+    line = {"workload": f"config 2 estimator pass: P2 {args.mesh}x{args.mesh} ({V.ndofs} dofs), M=20, P=150, "
+                        f"bonus_quadorder 1, tail_extension (10, 2)",
+            "estimate_ms_wall": statistics.median(ts), "P_ext": len(ext), "M_ext": len(ext[0]),
+            "ncells": V.mesh.ncells, "solve_relres": st["relres"],
+            "eta_total": float(np.sqrt(np.sum(em ** 2)))}
+    print(json.dumps(line), flush=True)
+
+
 def run_equilibration(args):
     """Equilibration estimator (sgfem_estimate_equilibration) on the config 1 basis
     (M=5, total degree 2, P=21) for P1 meshes of 32x32 and 128x128 and a P2 64x64
@@ -693,7 +720,7 @@ def main():
                     help="profiling target for ncu: set up the workload, run the kernel(s) a few times, exit")
     ap.add_argument("--mesh", type=int, default=256, help="mesh size for --profile / --workload adjoint")
     ap.add_argument("--workload", choices=["config2", "config1", "lognormal", "sampling", "adjoint", "batch",
-                                           "assembly", "equilibration"],
+                                           "assembly", "equilibration", "estimate"],
                     default="config2", help="config2 is the headline bench line; the others print their own line")
     ap.add_argument("--samples", type=int, default=100000, help="--workload sampling: number of samples")
     ap.add_argument("--directions", type=int, default=20, help="--workload adjoint: finite-difference directions")
@@ -705,7 +732,7 @@ def main():
     if args.workload != "config2":
         return {"config1": run_config1, "lognormal": run_lognormal, "sampling": run_sampling,
                 "adjoint": run_adjoint, "batch": run_batch, "assembly": run_assembly,
-                "equilibration": run_equilibration}[args.workload](args)
+                "equilibration": run_equilibration, "estimate": run_estimate}[args.workload](args)
     rank, world, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world, pg)

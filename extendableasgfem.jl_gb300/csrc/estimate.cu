@@ -224,6 +224,14 @@ __global__ void k_colsum(const double* __restrict__ src, size_t stride, int len,
     if (threadIdx.x == 0) out[blockIdx.x] = red[0];
 }
 
+// extended modes per pass: the per-face gradient jumps and the a_m at the
+// quadrature points are computed once per pass, so one pass covers every mode
+// unless the face buffer (nfaces x chunk doubles) would exceed ~2 GB
+int est_chunk(int64_t nfaces, int64_t Pext) {
+    const int64_t cap = std::max<int64_t>(64, ((int64_t)2 << 30) / (8 * std::max<int64_t>(nfaces, 1)));
+    return (int)std::max<int64_t>(1, std::min(Pext, cap));
+}
+
 template <typename T>
 int up(sgfem_context* ctx, std::vector<void*>& owned, const T* src, size_t n, T** dst) {
     void* p = nullptr;
@@ -396,7 +404,7 @@ extern "C" int sgfem_estimate_primal(sgfem_context* ctx, const double* sol, cons
     SG_TRY(build_est(ctx, sol, mesh, quad, f_qp, coef, ext, ext ? ext->M_ext : 0, own, a, cfh));
     const int64_t nc = a.ncells, nf = a.nfaces, Pext = a.Pext, Mext = a.coef.M;
     const int* dcf = a.cfaces;
-    const int chunk = 64;
+    const int chunk = est_chunk(nf, Pext);
     double *d_eta, *d_jumps, *d_vsum, *d_jsum;
     SG_CUDA(ctx, cudaMalloc((void**)&d_eta, (size_t)nc * Pext * sizeof(double)));
     own.p.push_back(d_eta);
@@ -606,7 +614,7 @@ extern "C" int sgfem_estimate_logpoisson(sgfem_context* ctx, const double* sol, 
     l.lamv = dlam;
     // a.coef.M = M_ext (gradients); the tables d, b1, b2 hold all maxm terms (data term)
 
-    const int chunk = 64;
+    const int chunk = est_chunk(nf, Pext);
     double *d_eta, *d_jumps, *d_vsum, *d_jsum, *d_z1, *d_z2;
     SG_CUDA(ctx, cudaMalloc((void**)&d_eta, (size_t)nc * Pext * sizeof(double)));
     own.p.push_back(d_eta);
