@@ -234,6 +234,54 @@ k_apply_samples(const int* __restrict__ rowptr, const int* __restrict__ col, con
     }
 }
 
+// the same with K(y_s) precomputed ([nz][ld]): per nonzero one coefficient load
+// (contiguous over the warp's samples) and one FMA
+template <typename T>
+__global__ void __launch_bounds__(128)
+k_apply_samples_pre(const int* __restrict__ rowptr, const int* __restrict__ col, const T* __restrict__ kval,
+                    const T* __restrict__ X, T* __restrict__ Y, int n, int ld, const unsigned char* __restrict__ bmask,
+                    double* __restrict__ partials, const KrylovScalars* __restrict__ scal) {
+    if (scal && scal->done) return;
+    __shared__ double red[4];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nchunk = (ld + 31) / 32;
+    const long long items = (long long)n * nchunk;
+    double dot = 0.0;
+    for (long long it = (long long)blockIdx.x * 4 + warp; it < items; it += (long long)gridDim.x * 4) {
+        const int row = (int)(it / nchunk), ch = (int)(it - (long long)row * nchunk);
+        const int s = ch * 32 + lane;
+        if (s >= ld) continue;
+        T acc = T(0);
+        if (!bmask[row])
+            for (int nz = rowptr[row]; nz < rowptr[row + 1]; ++nz)
+                acc = fma(kval[(size_t)nz * ld + s], X[(size_t)col[nz] * ld + s], acc);
+        Y[(size_t)row * ld + s] = acc;
+        if (partials) dot += (double)X[(size_t)row * ld + s] * (double)acc;
+    }
+    if (partials) {
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
+        if (lane == 0) red[warp] = dot;
+        __syncthreads();
+        if (threadIdx.x == 0) partials[blockIdx.x] = red[0] + red[1] + red[2] + red[3];
+    }
+}
+
+// K(y_s)[nz] = sum_m y_{s,m} K_m[nz] in FP64, in the order the on-the-fly kernel sums
+// (so the FP64 apply is unchanged bit for bit); the FP32 copy rounds the FP64 sum
+__global__ void k_combine_samples(const double* __restrict__ vals, int M1, const double* __restrict__ y, long long nnz,
+                                  int S, int ld, double* __restrict__ k64, float* __restrict__ k32) {
+    const long long total = nnz * ld;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        const long long nz = t / ld;
+        const int s = (int)(t - nz * ld);
+        double c = 0.0;
+        if (s < S)
+            for (int m = 0; m < M1; ++m) c = fma(y[(size_t)s * M1 + m], vals[(size_t)nz * M1 + m], c);
+        k64[t] = c;
+        k32[t] = (float)c;
+    }
+}
+
 template <typename T, int MMAX>
 int launch_samples_t(sgfem_context* ctx, const T* vals, const T* y, const void* X, void* Y, double* partials,
                      int grid, const KrylovScalars* scal) {
@@ -257,12 +305,41 @@ int launch_samples(sgfem_context* ctx, const T* vals, const T* y, const void* X,
 
 }  // namespace
 
+int sg_samples_combine(sgfem_context* ctx) {
+    if (!ctx->batched || !ctx->d_val64 || !ctx->d_y64) return SGFEM_OK;
+    const size_t count = (size_t)ctx->nnz * ctx->ld;
+    if (count * (sizeof(double) + sizeof(float)) > ((size_t)4 << 30)) return SGFEM_OK;
+    if (!ctx->d_kval64) {
+        SG_CUDA(ctx, cudaMalloc((void**)&ctx->d_kval64, std::max<size_t>(count, 1) * sizeof(double)));
+        SG_CUDA(ctx, cudaMalloc((void**)&ctx->d_kval32, std::max<size_t>(count, 1) * sizeof(float)));
+    }
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)count + 255) / 256, (int64_t)ctx->num_sms * 16));
+    k_combine_samples<<<grid, 256, 0, ctx->stream>>>(ctx->d_val64, ctx->M1, ctx->d_y64, (long long)ctx->nnz,
+                                                     (int)ctx->P, (int)ctx->ld, ctx->d_kval64, ctx->d_kval32);
+    SG_LAUNCHED(ctx);
+    return SGFEM_OK;
+}
+
 int sg_launch_apply_samples(sgfem_context* ctx, int precision, const void* X, void* Y, double* dot_partials,
                             int* nblocks, const KrylovScalars* skip_if_done) {
     const int64_t items = ctx->n * ((ctx->ld + 31) / 32);
     int grid = (int)std::min<int64_t>((items + 3) / 4, (int64_t)ctx->num_sms * 8);
     if (grid < 1) grid = 1;
     if (nblocks) *nblocks = grid;
+    if (ctx->d_kval64) {
+        if (precision == SGFEM_FP64)
+            k_apply_samples_pre<double><<<grid, 128, 0, ctx->stream>>>(ctx->d_rowptr, ctx->d_col, ctx->d_kval64,
+                                                                       (const double*)X, (double*)Y, (int)ctx->n,
+                                                                       (int)ctx->ld, ctx->d_bmask, dot_partials,
+                                                                       skip_if_done);
+        else
+            k_apply_samples_pre<float><<<grid, 128, 0, ctx->stream>>>(ctx->d_rowptr, ctx->d_col, ctx->d_kval32,
+                                                                      (const float*)X, (float*)Y, (int)ctx->n,
+                                                                      (int)ctx->ld, ctx->d_bmask, dot_partials,
+                                                                      skip_if_done);
+        SG_LAUNCHED(ctx);
+        return SGFEM_OK;
+    }
     if (precision == SGFEM_FP64)
         return launch_samples<double>(ctx, ctx->d_val64, ctx->d_y64, X, Y, dot_partials, grid, skip_if_done);
     return launch_samples<float>(ctx, ctx->d_val32, ctx->d_y32, X, Y, dot_partials, grid, skip_if_done);

@@ -88,7 +88,7 @@ extern "C" int sgfem_destroy(sgfem_context* ctx) {
                     ctx->d_combg64, ctx->d_combg32, ctx->d_lat_tab64, ctx->d_lat_tab32,
                     ctx->d_lat_scale64, ctx->d_lat_scale32, ctx->d_lat_blk64, ctx->d_lat_blk32, ctx->d_scal, ctx->w_stage.p, ctx->w_partials.p,
                     ctx->d_jptr, ctx->d_joff, ctx->d_jg, ctx->d_jtab, ctx->d_val32p, ctx->d_mode_of_col,
-                    ctx->d_y64, ctx->d_y32, ctx->d_valdf, ctx->d_combgdf};
+                    ctx->d_y64, ctx->d_y32, ctx->d_valdf, ctx->d_combgdf, ctx->d_kval64, ctx->d_kval32};
     if (ctx->pcg_exec) cudaGraphExecDestroy(ctx->pcg_exec);
     if (ctx->pcg_graph) cudaGraphDestroy(ctx->pcg_graph);
     sg_jit_release(ctx);
@@ -354,6 +354,7 @@ static int upload_samples(sgfem_context* ctx) {
         SG_CUDA(ctx, cudaMemcpy(ctx->d_y32, y32.data(), y32.size() * sizeof(float), cudaMemcpyHostToDevice));
     }
     ctx->samples_x_valid = false;
+    if (ctx->d_val64) SG_TRY(sg_samples_combine(ctx));  // next batch of a finalized context
     return SGFEM_OK;
 }
 
@@ -743,6 +744,7 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
     SG_TRY(upload(ctx, &ctx->d_col, col.data(), col.size()));
     SG_TRY(upload(ctx, &ctx->d_val64, val64.data(), val64.size()));
     SG_TRY(upload(ctx, &ctx->d_val32, val32.data(), val32.size()));
+    if (ctx->batched) SG_TRY(sg_samples_combine(ctx));
     SG_TRY(upload(ctx, &ctx->d_bmask, ctx->bmask_host.data(), ctx->bmask_host.size()));
     SG_TRY(upload(ctx, &ctx->d_iperm, ctx->iperm.data(), ctx->iperm.size()));
     SG_TRY(upload(ctx, &ctx->d_dinv64, dinv.data(), dinv.size()));

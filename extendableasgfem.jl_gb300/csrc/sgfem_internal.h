@@ -70,6 +70,8 @@ struct sgfem_context {
     std::vector<double> ysamp;   // M x S
     double* d_y64 = nullptr;     // [S][M1] coefficients, y_{s,0} = 1
     float* d_y32 = nullptr;
+    double* d_kval64 = nullptr;  // [nnz][ld]: K(y_s) = sum_m y_{s,m} K_m per sample (nullptr: combined on the fly)
+    float* d_kval32 = nullptr;
     bool samples_x_valid = false;  // w_vec[10] holds the solutions of the current samples
     std::vector<int64_t> bdofs;  // 0-based caller numbering
     bool has_bdofs = false;
@@ -250,6 +252,9 @@ int sg_launch_from_device(sgfem_context* ctx, const void* X, double* stage, int 
 int sg_lattice_setup(sgfem_context* ctx);
 // largest block count of a lattice pass (size of the reduction partials)
 int sg_lat_max_blocks(const sgfem_context* ctx);
+// K(y_s) of every sample of a samples context into d_kval64/32 (after the values and
+// the samples are on the device); leaves them null above a 4 GB budget
+int sg_samples_combine(sgfem_context* ctx);
 // exact mean preconditioner: K_0 restricted to interior lattice points is translation invariant
 // per parity class (x % 2, y % 2); rowptr/col in device numbering, val64 (nnz x M1, K_0 at m = 0)
 int sg_lattice_blocks(sgfem_context* ctx, const std::vector<int64_t>& rowptr, const std::vector<int32_t>& col,
