@@ -80,7 +80,7 @@ k_apply(const int* __restrict__ rowptr, const int* __restrict__ col, const T* __
                 const V* xs = reinterpret_cast<const V*>(X + (size_t)j * ld);
                 V* sv = reinterpret_cast<V*>(su);
                 for (int c = lane; c < nvec; c += 32) sv[c] = __ldg(xs + c);
-                if (lane < M1) sc[lane] = vals[(size_t)nz * M1 + lane];
+                for (int m = lane; m < M1; m += 32) sc[m] = vals[(size_t)nz * M1 + m];
                 __syncwarp();
 #pragma unroll
                 for (int t = 0; t < QT; ++t) acc[t] = fma(sc[om[t]], su[on[t]], acc[t]);

@@ -185,7 +185,7 @@ __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict_
                 const int j = d.col[nz];
                 const T* xs = Xp + (size_t)j * d.ld;
                 for (int c = lane; c < d.ld; c += 32) su[c] = __ldg(xs + c);
-                if (lane < d.M1) sc[lane] = vals[(size_t)nz * d.M1 + lane];
+                for (int m = lane; m < d.M1; m += 32) sc[m] = vals[(size_t)nz * d.M1 + m];
                 __syncwarp();
 #pragma unroll
                 for (int t = 0; t < QT; ++t) acc[t] = fma(sc[om[t]], su[on[t]], acc[t]);

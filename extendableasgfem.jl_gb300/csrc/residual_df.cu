@@ -256,7 +256,8 @@ int launch_df_qt(sgfem_context* ctx, const float2* xs, const float2* bs, float* 
 }  // namespace
 
 bool sg_residual_df_usable(const sgfem_context* ctx) {
-    if (ctx->batched || !ctx->rowsum_zero || ctx->Qn <= 0) return false;
+    // one KLE value per lane is staged per nonzero: M + 1 <= 32 terms
+    if (ctx->batched || !ctx->rowsum_zero || ctx->Qn <= 0 || ctx->M1 > 32) return false;
     const size_t smem = (size_t)(2 * ctx->ld + ctx->M1 + 1 + ctx->Qn) * sizeof(float2) * DWPB;
     if (smem > 200 * 1024) return false;
     const char* e = getenv("SGFEM_RESIDUAL");

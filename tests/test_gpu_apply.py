@@ -31,6 +31,8 @@ def problems():
         "hermite_full": lambda: build(8, 1, 3, pkg.generate_multiindices(3, 2), basis="hermite", mean=2.0),
         "p1_odd_mesh": lambda: build(12, 1, 4, pkg.total_degree_multiindices(4, 2)),
         "single_mode": lambda: build(8, 1, 2, [[0, 0]]),
+        # 41 KLE terms: every K_m reaches the apply (the mean mode couples to each e_m)
+        "many_terms": lambda: build(6, 1, 40, [[0] * 40] + [[int(k == m) for k in range(40)] for m in range(40)]),
     }
 
 

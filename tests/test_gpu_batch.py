@@ -74,3 +74,22 @@ def test_batch_precisions_agree(built_pkg, monkeypatch, precision):
         ref = osg.kron_direct(p.K0, p.Ks, p.G, p.b0, p.bdofs, p.P)
         assert np.linalg.norm(x - ref) <= 1e-7 * np.linalg.norm(ref)
     B.close()
+
+
+def test_batch_many_kle_terms(built_pkg):
+    """A problem with 41 KLE terms (every K_m coupled through the mean mode) next
+    to a small one: all M + 1 values of a nonzero reach the batch apply."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    units = [[0] * 40] + [[int(k == m) for k in range(40)] for m in range(40)]
+    probs = [build(6, 1, 40, units), build(5, 1, 2, pkg.total_degree_multiindices(2, 2))]
+    B = pkg.SGBatch(0)
+    for p in probs:
+        B.add(p.V, p.TB, p.Kall, p.b0)
+    B.finalize()
+    xs, st = B.solve(rtol=1e-10)
+    assert st["converged"] == len(probs) and st["relres_max"] <= 1e-10
+    for p, x in zip(probs, xs):
+        ref = osg.kron_direct(p.K0, p.Ks, p.G, p.b0, p.bdofs, p.P)
+        assert np.linalg.norm(x - ref) <= 1e-8 * np.linalg.norm(ref)
+    B.close()
