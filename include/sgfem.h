@@ -39,7 +39,7 @@ extern "C" {
 #define SGFEM_ERR_NONFINITE 4   /* NaN/Inf met in an input or an iterate */
 #define SGFEM_ERR_BREAKDOWN 5   /* Krylov breakdown (p'Ap <= 0 or r'z <= 0) */
 #define SGFEM_ERR_MAXIT 6       /* tolerance not reached within maxit */
-#define SGFEM_ERR_UNSUPPORTED 7 /* configuration not handled by this build */
+#define SGFEM_ERR_UNSUPPORTED 7 /* configuration the library does not handle */
 
 #define SGFEM_FP64 0            /* all arithmetic in FP64 */
 #define SGFEM_FP32 1            /* FP32 operator values, vectors and accumulation */
