@@ -94,6 +94,7 @@ struct sgfem_batch {
     long long total = 0;          // sum of n * ld
     int blocks = 0, wpb = 4, qt = 4, ldmax = 0, m1max = 0, qnmax = 0;
     int wpb32 = 4, qt32 = 8;      // launch shape of the FP32 apply (mixed solve)
+    int pf32 = 0;                 // 1: the FP32 apply prefetches the next nonzero into registers
     std::string tuning;
     std::vector<KrylovScalars> h_scal;
     double rtol = 0.0;            // of the last solve
@@ -133,8 +134,13 @@ __device__ __forceinline__ void block_sum_store(double v, double* out) {
     }
 }
 
-// Y = S X for every problem, p'q partials per block
-template <typename T, int QT>
+// Y = S X for every problem, p'q partials per block.  PF: the next nonzero's X row
+// (up to 32 columns per lane, ld <= 1024) and values are loaded into registers
+// while the current nonzero's pair FMAs run
+constexpr int BPC = 32;  // X columns per lane held for the prefetch
+constexpr int BPV = 8;   // KLE values per lane held for the prefetch (M + 1 <= 256)
+
+template <typename T, int QT, bool PF = false>
 __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict__ bprob, const T* __restrict__ X,
                          T* __restrict__ Y, double* __restrict__ partials, const KrylovScalars* __restrict__ scal,
                          int per_warp) {
@@ -181,15 +187,47 @@ __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict_
                 }
                 acc[t] = T(0);
             }
-            for (int nz = nz0; nz < nz1; ++nz) {
-                const int j = d.col[nz];
-                const T* xs = Xp + (size_t)j * d.ld;
-                for (int c = lane; c < d.ld; c += 32) su[c] = __ldg(xs + c);
-                for (int m = lane; m < d.M1; m += 32) sc[m] = vals[(size_t)nz * d.M1 + m];
-                __syncwarp();
+            if constexpr (PF) {
+                T xr[BPC], vr[BPV];
+                auto fetch = [&](int nz) {
+                    const T* xs = Xp + (size_t)d.col[nz] * d.ld;
 #pragma unroll
-                for (int t = 0; t < QT; ++t) acc[t] = fma(sc[om[t]], su[on[t]], acc[t]);
+                    for (int u = 0; u < BPC; ++u) {
+                        const int c = lane + 32 * u;
+                        xr[u] = c < d.ld ? __ldg(xs + c) : T(0);
+                    }
+#pragma unroll
+                    for (int u = 0; u < BPV; ++u) {
+                        const int m = lane + 32 * u;
+                        vr[u] = m < d.M1 ? vals[(size_t)nz * d.M1 + m] : T(0);
+                    }
+                };
+                if (nz0 < nz1) fetch(nz0);
+                for (int nz = nz0; nz < nz1; ++nz) {
+                    __syncwarp();  // the previous nonzero's FMAs have read su and sc
+#pragma unroll
+                    for (int u = 0; u < BPC; ++u)
+                        if (lane + 32 * u < d.ld) su[lane + 32 * u] = xr[u];
+#pragma unroll
+                    for (int u = 0; u < BPV; ++u)
+                        if (lane + 32 * u < d.M1) sc[lane + 32 * u] = vr[u];
+                    __syncwarp();
+                    if (nz + 1 < nz1) fetch(nz + 1);
+#pragma unroll
+                    for (int t = 0; t < QT; ++t) acc[t] = fma(sc[om[t]], su[on[t]], acc[t]);
+                }
                 __syncwarp();
+            } else {
+                for (int nz = nz0; nz < nz1; ++nz) {
+                    const int j = d.col[nz];
+                    const T* xs = Xp + (size_t)j * d.ld;
+                    for (int c = lane; c < d.ld; c += 32) su[c] = __ldg(xs + c);
+                    for (int m = lane; m < d.M1; m += 32) sc[m] = vals[(size_t)nz * d.M1 + m];
+                    __syncwarp();
+#pragma unroll
+                    for (int t = 0; t < QT; ++t) acc[t] = fma(sc[om[t]], su[on[t]], acc[t]);
+                    __syncwarp();
+                }
             }
 #pragma unroll
             for (int t = 0; t < QT; ++t) {
@@ -525,9 +563,20 @@ size_t apply_smem(const sgfem_batch* b, int wpb) {
 }
 
 template <typename T>
-int launch_apply(sgfem_batch* b, int wpb, int qt, const T* X, T* Y, double* partials, const KrylovScalars* scal) {
+int launch_apply(sgfem_batch* b, int wpb, int qt, const T* X, T* Y, double* partials, const KrylovScalars* scal,
+                 int pf = 0) {
     const int per_warp = (int)(((size_t)b->ldmax + b->m1max + 1 + b->qnmax + 3) & ~(size_t)3);
     const size_t smem = apply_smem<T>(b, wpb);
+    if (pf) {  // prefetching variant (tuned for the FP32 apply, 16 or 32 pairs per lane)
+        if (qt == 16)
+            k_bapply<T, 16, true><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials,
+                                                                            scal, per_warp);
+        else
+            k_bapply<T, 32, true><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials,
+                                                                            scal, per_warp);
+        BLAUNCHED(b);
+        return SGFEM_OK;
+    }
     if (qt == 4)
         k_bapply<T, 4><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials, scal,
                                                                   per_warp);
@@ -865,37 +914,57 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
     // the staging of each X row (LSU-bound rather than FP64-bound)
     std::string log32;
     float best32 = 1e30f;
-    for (int wpb : {4, 8})
-        for (int qt : {16, 32}) {
-            const size_t smem = apply_smem<float>(b, wpb);
-            if ((int)smem > dev_smem) continue;
-            if (smem > 48 * 1024) {
-                cudaError_t e = qt == 16 ? cudaFuncSetAttribute(k_bapply<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                                         : cudaFuncSetAttribute(k_bapply<float, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                if (e != cudaSuccess) {
-                    cudaGetLastError();
-                    continue;
+    for (int pf : {0, 1})
+        for (int wpb : {4, 8})
+            for (int qt : {16, 32}) {
+                if (pf && (b->ldmax > 32 * BPC || b->m1max > 32 * BPV)) continue;
+                const size_t smem = apply_smem<float>(b, wpb);
+                if ((int)smem > dev_smem) continue;
+                {  // the register budget of the variant must allow the block size
+                    cudaFuncAttributes fa{};
+                    const cudaError_t ea = pf ? (qt == 16 ? cudaFuncGetAttributes(&fa, k_bapply<float, 16, true>)
+                                                          : cudaFuncGetAttributes(&fa, k_bapply<float, 32, true>))
+                                              : (qt == 16 ? cudaFuncGetAttributes(&fa, k_bapply<float, 16>)
+                                                          : cudaFuncGetAttributes(&fa, k_bapply<float, 32>));
+                    if (ea != cudaSuccess || fa.maxThreadsPerBlock < wpb * 32) {
+                        cudaGetLastError();
+                        continue;
+                    }
+                }
+                if (smem > 48 * 1024) {
+                    cudaError_t e;
+                    if (pf)
+                        e = qt == 16 ? cudaFuncSetAttribute(k_bapply<float, 16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                                     : cudaFuncSetAttribute(k_bapply<float, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                    else
+                        e = qt == 16 ? cudaFuncSetAttribute(k_bapply<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                                     : cudaFuncSetAttribute(k_bapply<float, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                    if (e != cudaSuccess) {
+                        cudaGetLastError();
+                        continue;
+                    }
+                }
+                SG_TRY(launch_apply<float>(b, wpb, qt, b->d_p32, b->d_q32, b->d_part, nullptr, pf));
+                BCUDA(b, cudaEventRecord(b->ev0, b->stream));
+                for (int r = 0; r < 2; ++r)
+                    SG_TRY(launch_apply<float>(b, wpb, qt, b->d_p32, b->d_q32, b->d_part, nullptr, pf));
+                BCUDA(b, cudaEventRecord(b->ev1, b->stream));
+                BCUDA(b, cudaEventSynchronize(b->ev1));
+                float ms = 0.f;
+                BCUDA(b, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+                char buf32[96];
+                snprintf(buf32, sizeof(buf32), "%s%dw/%dq:%.3fms ", pf ? "prefetch " : "", wpb, qt, ms / 2);
+                log32 += buf32;
+                if (ms < best32) {
+                    best32 = ms;
+                    b->wpb32 = wpb;
+                    b->qt32 = qt;
+                    b->pf32 = pf;
                 }
             }
-            SG_TRY(launch_apply<float>(b, wpb, qt, b->d_p32, b->d_q32, b->d_part, nullptr));
-            BCUDA(b, cudaEventRecord(b->ev0, b->stream));
-            for (int r = 0; r < 2; ++r) SG_TRY(launch_apply<float>(b, wpb, qt, b->d_p32, b->d_q32, b->d_part, nullptr));
-            BCUDA(b, cudaEventRecord(b->ev1, b->stream));
-            BCUDA(b, cudaEventSynchronize(b->ev1));
-            float ms = 0.f;
-            BCUDA(b, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
-            char buf32[96];
-            snprintf(buf32, sizeof(buf32), "%dw/%dq:%.3fms ", wpb, qt, ms / 2);
-            log32 += buf32;
-            if (ms < best32) {
-                best32 = ms;
-                b->wpb32 = wpb;
-                b->qt32 = qt;
-            }
-        }
     char buf[192];
-    snprintf(buf, sizeof(buf), "chosen %d warps/block, %d pairs/lane, %d blocks (FP32: %d warps/block, %d pairs/lane); ",
-             b->wpb, b->qt * 32, b->blocks, b->wpb32, b->qt32 * 32);
+    snprintf(buf, sizeof(buf), "chosen %d warps/block, %d pairs/lane, %d blocks (FP32: %s%d warps/block, %d pairs/lane); ",
+             b->wpb, b->qt * 32, b->blocks, b->pf32 ? "prefetch, " : "", b->wpb32, b->qt32 * 32);
     b->tuning = buf + log + "FP32 " + log32;
     b->finalized = true;
     return SGFEM_OK;
@@ -937,7 +1006,8 @@ template <typename T, typename TX>
 int batch_iteration(sgfem_batch* b, const BVecs<T, TX>& v, int maxit) {
     const int B = (int)b->hp.size();
     const bool f32 = sizeof(T) == 4;
-    SG_TRY(launch_apply<T>(b, f32 ? b->wpb32 : b->wpb, f32 ? b->qt32 : b->qt, v.p, v.q, b->d_part, b->d_scal));
+    SG_TRY(launch_apply<T>(b, f32 ? b->wpb32 : b->wpb, f32 ? b->qt32 : b->qt, v.p, v.q, b->d_part, b->d_scal,
+                           f32 ? b->pf32 : 0));
     k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_ALPHA, 0.0, maxit);
     BLAUNCHED(b);
     k_bupdate<T, TX><<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, v.x, v.p, v.r, v.q, b->d_scal,
