@@ -94,6 +94,7 @@ SIGNATURES = {
                                               ctypes.POINTER(ctypes.c_int32), ctypes.c_double, ctypes.c_int64, _DP]),
     "sgfem_estimate_logpoisson": (ctypes.c_int, [_P, _DP, _P, _P, _DP, _P, _P, _P, _DP, _DP, _DP]),
     "sgfem_estimate_equilibration": (ctypes.c_int, [_P, _DP, _P, _P, _DP, _P, _P, ctypes.c_double, _DP, _DP]),
+    "sgfem_rt_reference_basis": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP, _DP, _DP]),
     "sgfem_set_samples": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int64, _DP]),
     "sgfem_solve_samples": (ctypes.c_int, [_P, _DP, _DP, ctypes.POINTER(SolveOptions), ctypes.POINTER(SolveStats)]),
     "sgfem_solve_gmres": (ctypes.c_int, [_P, _DP, _DP, ctypes.POINTER(SolveOptions), ctypes.c_int,

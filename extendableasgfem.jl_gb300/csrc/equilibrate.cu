@@ -567,6 +567,15 @@ struct EqOwned {
 
 }  // namespace
 
+extern "C" int sgfem_rt_reference_basis(int k, int np, const double* pts, double* values, double* divs) {
+    if ((k != 1 && k != 2) || np < 0 || (np > 0 && (!pts || !values || !divs))) return SGFEM_ERR_ARGUMENT;
+    std::vector<double> v, dv;
+    if (!rt_basis(k, np, pts, v, dv)) return SGFEM_ERR_UNSUPPORTED;
+    std::copy(v.begin(), v.end(), values);
+    std::copy(dv.begin(), dv.end(), divs);
+    return SGFEM_OK;
+}
+
 extern "C" int sgfem_estimate_equilibration(sgfem_context* ctx, const double* sol, const sgfem_mesh* mesh,
                                             const sgfem_quadrature* quad, const double* f_qp,
                                             const sgfem_cosine* coef, const sgfem_extension* ext, double div_penalty,

@@ -306,6 +306,14 @@ SGFEM_API int sgfem_estimate_equilibration(sgfem_context* ctx, const double* sol
                                            const sgfem_quadrature* quad, const double* f_qp,
                                            const sgfem_cosine* coef, const sgfem_extension* ext, double div_penalty,
                                            double* eta4modes, double* eta4cell);
+/* the RT_k basis of the reference cell that sgfem_estimate_equilibration maps to
+   every cell (k = 1 or 2): dual to the edge moments int_0^1 sigma(x(t)) . R x'(t)
+   L_l(2t - 1) dt on the edges (v0,v1), (v1,v2), (v2,v0) of the reference cell
+   (R the rotation by -90 degrees, L_l Legendre, l = 0..k; dofs e (k + 1) + l)
+   and the interior moments int sigma_c q, q in {1} (k = 1) or {1, xi, eta}
+   (k = 2; dofs 3 (k + 1) + c * nq + iq).  At np points (xi, eta): values
+   np x nb x 2, divs np x nb, nb = 8 (k = 1) or 15 (k = 2).  Host only. */
+SGFEM_API int sgfem_rt_reference_basis(int k, int np, const double* pts, double* values, double* divs);
 
 /*
  * Evaluation of an SG solution at parameter samples and the sampling error.
