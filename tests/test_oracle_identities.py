@@ -214,3 +214,36 @@ def test_equilibration_oracle_vanishes_for_zero_data():
     mis = [[0, 0], [1, 0], [0, 1]]
     em, ec, ext = oq.estimate_equilibration(V, np.zeros(V.ndofs * 3), mis, ob.LEGENDRE, C, lambda x, y: 0.0 * x)
     assert np.all(em == 0.0) and np.all(ec == 0.0)
+
+
+def test_equilibration_oracle_is_basis_independent(monkeypatch):
+    """The estimate does not depend on the RT_k basis: the oracle with its edge
+    functionals at other points along each edge (another basis of the same
+    constrained spaces) agrees to the conditioning of the penalised patch
+    systems (div penalty 1e5: 1e-7 per element, 1e-8 for eta4modes)."""
+    import numpy as np
+    from oracle import basis as ob
+    from oracle import coefficient as oc
+    from oracle import equilibration as oq
+    from oracle import fem as of
+    V = of.LagrangeSpace(of.StructuredMesh(4), 2)
+    C = oc.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=40)
+    mis = [[0, 0, 0], [1, 0, 0], [0, 1, 0], [2, 0, 0], [0, 0, 1]]
+    U = np.random.default_rng(11).standard_normal(V.ndofs * len(mis))
+    f = lambda x, y: 1.0 + x * y
+    a = oq.estimate_equilibration(V, U, mis, ob.LEGENDRE, C, f)
+    orig = oq.RTSpace.__init__
+
+    def other_points(self, mesh, k):
+        gauss = np.polynomial.legendre.leggauss
+        np.polynomial.legendre.leggauss = lambda n: (np.linspace(-0.8, 0.8, n), np.ones(n))
+        try:
+            orig(self, mesh, k)
+        finally:
+            np.polynomial.legendre.leggauss = gauss
+
+    monkeypatch.setattr(oq.RTSpace, "__init__", other_points)
+    b = oq.estimate_equilibration(V, U, mis, ob.LEGENDRE, C, f)
+    assert a[2] == b[2]
+    assert np.max(np.abs(a[0] - b[0]) / a[0]) <= 1e-8
+    assert np.max(np.abs(a[1] - b[1]) / np.abs(a[1]).max(axis=0)) <= 1e-7
