@@ -6,6 +6,7 @@ CMake, no torch extension machinery: the library is plain C ABI.
 """
 import concurrent.futures
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -31,6 +32,13 @@ def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
+def _toolchain_stamp():
+    """nvcc version, target architecture, flags and host machine: a change of
+    any of them invalidates every object (x86 objects never link on Arm)."""
+    v = subprocess.run([nvcc(), "--version"], capture_output=True, text=True).stdout.strip()
+    return "\n".join([v, " ".join(ARCH), " ".join(FLAGS), platform.machine()])
+
+
 def _stale(target, deps):
     if not os.path.exists(target):
         return True
@@ -40,6 +48,14 @@ def _stale(target, deps):
 
 def build(verbose=False, ptxas_verbose=False, force=False):
     os.makedirs(BUILD, exist_ok=True)
+    stamp_path = os.path.join(BUILD, "toolchain.stamp")
+    stamp = _toolchain_stamp()
+    try:
+        old = open(stamp_path).read()
+    except OSError:
+        old = None
+    if old != stamp:
+        force = True
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
     headers.append(os.path.join(HERE, "..", "include", "sgfem.h"))
     objs = []
@@ -58,6 +74,7 @@ def build(verbose=False, ptxas_verbose=False, force=False):
                 sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
             if r.returncode != 0:
                 raise RuntimeError("nvcc failed for " + cmd[-3])
+    linked = False
     if force or jobs or _stale(OUT, objs):
         tmp = OUT + ".tmp"
         cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-ldl"]
@@ -66,6 +83,11 @@ def build(verbose=False, ptxas_verbose=False, force=False):
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link failed")
         os.replace(tmp, OUT)
+        linked = True
+    with open(stamp_path, "w") as f:
+        f.write(stamp)
+    sys.stderr.write(f"libsgfem build: {len(jobs)} of {len(objs)} units compiled, "
+                     f"{'linked' if linked else 'up to date'} ({platform.machine()})\n")
     return OUT
 
 

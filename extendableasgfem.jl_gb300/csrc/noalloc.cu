@@ -9,6 +9,7 @@
 // output vectors (device layout, see sgfem_device_layout); the intermediate
 // buffer of the three sine-transform passes lives in the array below, which
 // every GPU that loads the library holds until the process exits.
+#include <atomic>
 #include <string>
 
 #include "sgfem_internal.h"
@@ -21,20 +22,22 @@ static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBy
 namespace {
 
 constexpr int kMaxDevices = 64;
-// device address of g_static_scratch, looked up once per device
-void* g_scratch_addr[kMaxDevices] = {nullptr};
+// device address of g_static_scratch, looked up once per device; host threads
+// that make their first call on one device at the same time may both look it
+// up, and both store the same address
+std::atomic<void*> g_scratch_addr[kMaxDevices];
 
 int scratch_address(sgfem_context* ctx, void** out) {
     if (ctx->device < 0 || ctx->device >= kMaxDevices)
         return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "static scratch: device index out of range");
-    if (!g_scratch_addr[ctx->device]) {
+    void* p = g_scratch_addr[ctx->device].load(std::memory_order_acquire);
+    if (!p) {
         // the device is current (set by the caller of this function)
-        void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
         if (e != cudaSuccess) return sg_cuda_fail(ctx, e, "cudaGetSymbolAddress(g_static_scratch)");
-        g_scratch_addr[ctx->device] = p;
+        g_scratch_addr[ctx->device].store(p, std::memory_order_release);
     }
-    *out = g_scratch_addr[ctx->device];
+    *out = p;
     return SGFEM_OK;
 }
 

@@ -374,10 +374,15 @@ SGFEM_API int sgfem_sampling_error(sgfem_context* ctx, const double* det_solutio
  * in the device layout (sgfem_device_layout).  The intermediate buffer is a
  * static device array of SGFEM_STATIC_SCRATCH_BYTES that every GPU loading the
  * library holds until the process exits; a vector needing more than that
- * (n_dev * ld * element size) is rejected with SGFEM_ERR_ARGUMENT.  The first
- * call on a device looks up the array's device address, so make that first
- * call before any stream capture.  All calls share the one array: calls that
- * overlap on the same GPU (from other contexts or host threads) race on it.
+ * (n_dev * ld * element size) is rejected with SGFEM_ERR_ARGUMENT.  The work
+ * runs on the context's own stream, which does not wait for other streams:
+ * finish every write to r_dev and z_dev (e.g. synchronise the stream that
+ * made them) before the call.  The call is synchronous: it returns after the
+ * result is in z_dev.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  All calls share the one array and it keeps the last call's
+ * contents: calls that overlap on the same GPU (from other contexts or host
+ * threads) race on it.
  */
 #define SGFEM_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
 SGFEM_API int sgfem_precondition_device_static(sgfem_context* ctx, const void* r_dev, void* z_dev, int precision);

@@ -16,6 +16,7 @@
  * the reference.
  */
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
 #include <omp.h>
@@ -57,4 +58,99 @@ int oracle_max_threads(void) {
 #else
     return 1;
 #endif
+}
+
+/*
+ * ldiv!(y, P, b) of solvers_poisson_primal.jl:47-78 with the LU factors of
+ * K_0 (1e60 on the boundary diagonals) computed once by SuperLU:
+ * Pr A Pc = L U, L unit lower and U upper triangular, both CSC (0-based,
+ * int64 indices), perm_r / perm_c as returned by SciPy's splu
+ * (Pr[perm_r[i], i] = 1, Pc[i, perm_c[i]] = 1, so x = Pc U^-1 L^-1 Pr b).  Every mode mu of the
+ * column-major n x P block B is solved independently, as the reference does
+ * one LU solve per mode; with OpenMP the modes are split over host threads in
+ * groups of RB right-hand sides that share one pass over the factors.
+ */
+#define RB 8
+void oracle_lu_solve_modes(int64_t n, int64_t P, const int64_t* Lp, const int64_t* Li, const double* Lx,
+                           const int64_t* Up, const int64_t* Ui, const double* Ux, const int64_t* perm_r,
+                           const int64_t* perm_c, const double* B, double* X, int nthreads) {
+    const int64_t ngroups = (P + RB - 1) / RB;
+#ifdef _OPENMP
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel num_threads(nthreads)
+#endif
+    {
+        double* w = (double*)malloc(sizeof(double) * (size_t)n * RB);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+        for (int64_t g = 0; g < ngroups; ++g) {
+            const int64_t m0 = g * RB;
+            const int64_t nr = (P - m0 < RB) ? (P - m0) : RB;
+            /* w = Pr b, interleaved [row][rhs] */
+            for (int64_t r = 0; r < nr; ++r) {
+                const double* b = B + (m0 + r) * n;
+                for (int64_t i = 0; i < n; ++i) w[perm_r[i] * RB + r] = b[i];
+            }
+            /* L z = w (unit diagonal; the diagonal entry of each column is skipped) */
+            for (int64_t j = 0; j < n; ++j) {
+                double* wj = w + j * RB;
+                for (int64_t p = Lp[j]; p < Lp[j + 1]; ++p) {
+                    const int64_t i = Li[p];
+                    if (i <= j) continue;
+                    const double l = Lx[p];
+                    double* wi = w + i * RB;
+                    for (int64_t r = 0; r < nr; ++r) wi[r] -= l * wj[r];
+                }
+            }
+            /* U v = z (column-oriented back substitution) */
+            for (int64_t j = n - 1; j >= 0; --j) {
+                double* wj = w + j * RB;
+                double d = 0.0;
+                for (int64_t p = Up[j]; p < Up[j + 1]; ++p)
+                    if (Ui[p] == j) d = Ux[p];
+                for (int64_t r = 0; r < nr; ++r) wj[r] /= d;
+                for (int64_t p = Up[j]; p < Up[j + 1]; ++p) {
+                    const int64_t i = Ui[p];
+                    if (i >= j) continue;
+                    const double u = Ux[p];
+                    double* wi = w + i * RB;
+                    for (int64_t r = 0; r < nr; ++r) wi[r] -= u * wj[r];
+                }
+            }
+            /* x = Pc v */
+            for (int64_t r = 0; r < nr; ++r) {
+                double* x = X + (m0 + r) * n;
+                for (int64_t i = 0; i < n; ++i) x[i] = w[perm_c[i] * RB + r];
+            }
+        }
+        free(w);
+    }
+}
+
+/* BLAS-1 helpers of the Krylov loop (Krylov.jl calls BLAS dot / axpy) */
+double oracle_dot(int64_t n, const double* x, const double* y, int nthreads) {
+    double s = 0.0;
+#ifdef _OPENMP
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for reduction(+ : s) schedule(static) num_threads(nthreads)
+#endif
+    for (int64_t i = 0; i < n; ++i) s += x[i] * y[i];
+    return s;
+}
+
+void oracle_axpy(int64_t n, double a, const double* x, double* y, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+    for (int64_t i = 0; i < n; ++i) y[i] += a * x[i];
+}
+
+void oracle_scale_copy(int64_t n, double a, const double* x, double* y, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+    for (int64_t i = 0; i < n; ++i) y[i] = a * x[i];
 }

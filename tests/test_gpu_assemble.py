@@ -31,6 +31,30 @@ def test_gpu_stiffness_matches_host(built_pkg, order, N, M):
     assert all(np.array_equal(a.data, b.data) for a, b in zip(part, gpu[3:6]))
 
 
+@pytest.mark.parametrize("order,N", [(1, 16), (2, 8)])
+def test_gpu_stiffness_and_rhs_match_oracle(built_pkg, order, N):
+    """The GPU-assembled K_m and b directly against the oracle's element loops
+    (oracle/fem.py: the same structured mesh, dof numbering and triangle rules)."""
+    import __graft_entry__ as ge
+    from oracle import coefficient as oc
+    from oracle import fem as of
+    pkg = ge.load_package()
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.3, maxm=150)
+    Co = oc.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.3, maxm=150)
+    V = pkg.H1Pk(pkg.unit_square_mesh(N), order)
+    Vo = of.LagrangeSpace(of.StructuredMesh(N), order)
+    ms = list(range(7))
+    qo = 2 * (order - 1) + 2
+    gpu = pkg.assemble_stiffness_gpu(V, C, ms, qo)
+    ref = of.assemble_stiffness(Vo, Co, ms, qo)
+    for m, A, R in zip(ms, gpu, ref):
+        d = (A - R).toarray()
+        assert np.abs(d).max() <= 1e-13 * np.abs(R.toarray()).max(), m
+    bg = pkg.assemble_rhs_gpu(V, lambda x, y: np.ones_like(x), order)
+    bo = of.assemble_rhs(Vo, lambda x, y: 1.0, order)
+    assert np.abs(bg - bo).max() <= 1e-14 * np.abs(bo).max()
+
+
 def test_solve_on_gpu_assembled_blocks(built_pkg):
     import __graft_entry__ as ge
     pkg = ge.load_package()

@@ -1,10 +1,14 @@
 """Appending modes to a finalized operator (sgfem_update_coupling, the
-adaptive loop of scripts/poisson.jl:341-420): the updated operator applies,
-preconditions and solves exactly like an operator finalized from scratch with
-the new basis, while the K_m stay on the GPU."""
+adaptive loop of scripts/poisson.jl:341-420): the updated operator applies
+the oracle's mul! for the new basis (solvers_poisson_primal.jl:86-124, 1e-12
+relative), its solve meets the FP64 residual on the host and matches the
+oracle's Kronecker solve, and it applies, preconditions and solves exactly
+like an operator finalized from scratch with the new basis, while the K_m
+stay on the GPU."""
 import numpy as np
 import pytest
 
+from oracle import sg as osg
 from tests.problems import build
 
 pytestmark = pytest.mark.gpu
@@ -30,6 +34,11 @@ def test_update_matches_fresh_operator(built_pkg, order, N):
     op.solve_primal(p.b0, x0, rtol=1e-10, precision=pkg.MIXED)  # the old basis, kernels compiled
     op.update_basis(TB2)
     x = np.random.default_rng(3).standard_normal(p.n * TB2.nmodes)
+    G2 = TB2.G.toarray()
+    yref = osg.mul_literal(x, p.K0, p.Ks, G2, p.bdofs, TB2.nmodes)
+    y = op.mul(x, pkg.FP64)
+    assert np.linalg.norm(y - yref) <= 1e-12 * np.linalg.norm(yref)
+    assert np.linalg.norm(op.mul(x, pkg.FP32) - yref) <= 1e-5 * np.linalg.norm(yref)
     for prec in (pkg.FP64, pkg.FP32):
         assert np.array_equal(op.mul(x, prec), fresh.mul(x, prec))
     if op.has_lattice:
@@ -40,6 +49,8 @@ def test_update_matches_fresh_operator(built_pkg, order, N):
         sa = op.solve_primal(p.b0, xa, rtol=1e-10, precision=prec)
         sb = fresh.solve_primal(p.b0, xb, rtol=1e-10, precision=prec)
         assert sa["iterations"] == sb["iterations"] and np.array_equal(xa, xb)
+        ref = osg.kron_direct(p.K0, p.Ks, G2, p.b0, p.bdofs, TB2.nmodes)
+        assert np.linalg.norm(xa - ref) <= 1e-8 * np.linalg.norm(ref)
     op.close()
     fresh.close()
 
@@ -56,6 +67,8 @@ def test_update_to_shorter_multi_indices_and_errors(built_pkg):
     fresh = pkg.SGOperator(p.V, TB4, p.Kall[:5], device=0)
     x = np.random.default_rng(4).standard_normal(p.n * TB4.nmodes)
     assert np.array_equal(op.mul(x, pkg.FP64), fresh.mul(x, pkg.FP64))
+    yref = osg.mul_literal(x, p.K0, p.Ks[:4], TB4.G.toarray(), p.bdofs, TB4.nmodes)
+    assert np.linalg.norm(op.mul(x, pkg.FP64) - yref) <= 1e-12 * np.linalg.norm(yref)
     xa = np.zeros(p.n * TB4.nmodes)
     xb = np.zeros(p.n * TB4.nmodes)
     op.solve_primal(p.b0, xa, rtol=1e-10, precision=pkg.MIXED)

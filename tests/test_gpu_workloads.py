@@ -1,0 +1,171 @@
+"""Parity at the benchmarked sizes: the workloads that bench.py times, checked
+against the oracle at their full size.
+
+* Config 2 (P2 256x256, 263 169 dofs, M = 20, P = 150, the bench's operator):
+  - the FP64 apply against the oracle's C restatement of mul!
+    (solvers_poisson_primal.jl:86-124), 1e-12 relative in the 2-norm;
+  - the FP32 apply in its default generated form (the one the bench times)
+    against the FP64 apply, 1e-5;
+  - the mixed-precision solve to 1e-8: the FP64 residual of the returned
+    solution recomputed on the host with the oracle's mul! and the reference
+    right-hand side (solvers_poisson_primal.jl:149-155) is <= 1.01e-8, and the
+    solution is within 1e-6 of the FP64 GPU solve.
+* Config 3 lognormal (Hermite, P1 128x128, M = 10, P = 80): the FP64 apply
+  against the oracle's literal mul! (solvers_logpoisson_primal.jl:87-127),
+  1e-12; GMRES (FP64 and mixed) to 1e-8 with the host FP64 residual <= 1.01e-8.
+* Config 1 estimator at N = 32 (P1, M = 5, total degree 2) against the
+  oracle's estimate (estimate.jl:260-418), 1e-10 per element.
+* The first 32 problems of the config-4 stream (SplitMix64 shapes, up to
+  10.5 M unknowns each) solved in one batch: every problem's FP64 residual
+  recomputed on the host with the oracle's apply is <= 1.01e-8, and the
+  small ones match the oracle's Kronecker solve (solve_full_primal!,
+  solvers_poisson_primal.jl:172-230) to 1e-7.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import cbuild
+from oracle import sg as osg
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module")
+def config2(built_pkg):
+    import bench
+    pkg = built_pkg
+    V, TB, Ks, b0 = bench.setup_workload(pkg)
+    op = pkg.SGOperator(V, TB, Ks, device=0)
+    cop = cbuild.COperator(Ks, TB.G.toarray(), V.bdofs, TB.nmodes)
+    yield pkg, V, TB, Ks, b0, op, cop
+    op.close()
+
+
+def test_config2_fp64_apply_matches_oracle(config2):
+    pkg, V, TB, Ks, b0, op, cop = config2
+    n, P = V.ndofs, TB.nmodes
+    assert (n, P, len(Ks)) == (263169, 150, 21)
+    x = np.random.default_rng(0).standard_normal(n * P)
+    y = op.mul(x, pkg.FP64)
+    yref = cop.mul(x, nthreads=os.cpu_count())
+    assert rel(y, yref) <= 1e-12
+    Y = y.reshape(P, n)
+    assert np.all(Y[:, V.bdofs] == 0.0)
+
+
+def test_config2_fp32_default_apply(config2):
+    """The FP32 apply the bench times (the lattice-window form generated for
+    this coupling structure) agrees with FP64 to FP32 accuracy."""
+    pkg, V, TB, Ks, b0, op, cop = config2
+    variant, log = op.ctx.apply_variant
+    assert variant == 1 and "lattice window" in log, log
+    x = np.random.default_rng(1).standard_normal(V.ndofs * TB.nmodes)
+    y64 = op.mul(x, pkg.FP64)
+    y32 = op.mul(x, pkg.FP32)
+    assert rel(y32, y64) <= 1e-5
+
+
+def test_config2_mixed_solve_host_residual(config2):
+    pkg, V, TB, Ks, b0, op, cop = config2
+    n, P = V.ndofs, TB.nmodes
+    x = np.zeros(n * P)
+    st = op.solve_primal(b0, x, rtol=1e-8, precision=pkg.MIXED)
+    b = osg.reference_rhs(np.zeros(n * P), b0, V.bdofs, P)
+    r = b - cop.mul(x, nthreads=os.cpu_count())
+    relres = np.linalg.norm(r) / np.linalg.norm(b)
+    assert relres <= 1.01e-8, (relres, st)
+    # the solver's own residual certificate agrees with the host's
+    assert abs(st["relres"] - relres) <= 0.05 * relres + 1e-12, (st["relres"], relres)
+    x64 = np.zeros(n * P)
+    st64 = op.solve_primal(b0, x64, rtol=1e-8, precision=pkg.FP64)
+    assert st64["relres"] <= 1e-8
+    assert rel(x, x64) <= 1e-6
+
+
+def _lognormal_config3(pkg):
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=0.0, maxm=150)
+    M, P = 10, 80
+    mis = pkg.top_weight_multiindices(M, P, C.decay_factors)
+    deg = max(max(m) for m in mis)
+    V = pkg.H1Pk(pkg.unit_square_mesh(128), 1)
+    TB = pkg.TensorizedBasis(pkg.HermitePolynomials, M, deg, deg + 4, multi_indices=mis)
+    sol = pkg.SGFEVector(V, TB)
+    Ks, b = pkg.assemble(pkg.LogTransformedPoissonProblemPrimal, sol, C, rhs=lambda x, y: np.ones_like(x))
+    return V, TB, Ks, b
+
+
+def test_config3_lognormal_apply_and_gmres(built_pkg):
+    pkg = built_pkg
+    V, TB, Ks, b = _lognormal_config3(pkg)
+    n, P = V.ndofs, TB.nmodes
+    assert (n, P) == (16641, 80)
+    G = TB.G.toarray()
+    op = pkg.SGOperator(V, TB, Ks, device=0)
+    try:
+        x = np.random.default_rng(2).standard_normal(n * P)
+        yref = osg.mul_literal(x, Ks[0], Ks[1:], G, V.bdofs, P)
+        assert rel(op.mul(x, pkg.FP64), yref) <= 1e-12
+        assert rel(op.mul(x, pkg.FP32), yref) <= 1e-5
+        bb = b.copy()
+        for mu in range(P):
+            bb[mu * n + V.bdofs] = 0.0
+        sols = {}
+        for name, prec in (("fp64", pkg.FP64), ("mixed", pkg.MIXED)):
+            xs = np.zeros(n * P)
+            st = op.solve_logpoisson(b, xs, rtol=1e-8, precision=prec, restart=100, maxit=3000)
+            r = bb - osg.apply_fast(xs, Ks[0], Ks[1:], G, V.bdofs, P)
+            relres = np.linalg.norm(r) / np.linalg.norm(bb)
+            assert relres <= 1.01e-8, (name, relres, st)
+            sols[name] = xs
+        assert rel(sols["mixed"], sols["fp64"]) <= 1e-6
+    finally:
+        op.close()
+
+
+def test_config1_estimator_n32(built_pkg):
+    from tests.problems import config1_like
+    from tests.test_gpu_estimate import check, run_both
+    p = config1_like(N=32)
+    assert (p.n, p.P) == (1089, 21)
+    check(*run_both(p, bonus=2, tail=(10, 2)))
+
+
+def test_config4_stream_first_32_problems(built_pkg):
+    pkg = built_pkg
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    shapes = pkg.config4_problems(32)
+    B = pkg.SGBatch(0)
+    probs = []
+    try:
+        for N, M, d in shapes:
+            mis = pkg.total_degree_multiindices(M, d)
+            TB = pkg.TensorizedBasis(pkg.LegendrePolynomials, M, d, d + 4, multi_indices=mis)
+            V = pkg.H1Pk(pkg.unit_square_mesh(N), 1)
+            sol = pkg.SGFEVector(V, TB)
+            Ks, b0 = pkg.assemble(pkg.PoissonProblemPrimal, sol, C, rhs=lambda x, y: np.ones_like(x), device=0)
+            B.add(V, TB, Ks, b0)
+            probs.append((V, TB, Ks, b0))
+        B.finalize()
+        xs, st = B.solve(rtol=1e-8, maxit=20000, check_every=16)
+        assert st["converged"] == len(shapes)
+        for i, ((V, TB, Ks, b0), x) in enumerate(zip(probs, xs)):
+            n, P = V.ndofs, TB.nmodes
+            G = TB.G.toarray()
+            b = np.zeros(n * P)
+            b[:n] = b0
+            for mu in range(P):
+                b[mu * n + V.bdofs] = 0.0
+            r = b - osg.apply_fast(x, Ks[0], Ks[1:], G, V.bdofs, P)
+            relres = np.linalg.norm(r) / np.linalg.norm(b)
+            assert relres <= 1.01e-8, (i, shapes[i], relres)
+            if n * P <= 20000:
+                ref = osg.kron_direct(Ks[0], Ks[1:], G, b0, V.bdofs, P)
+                assert rel(x, ref) <= 1e-7, (i, shapes[i])
+    finally:
+        B.close()

@@ -44,6 +44,8 @@ def test_static_matches_allocating_entry_point(setup, precision):
         ref = op.ldiv(b, p.pkg.PREC_LATTICE, prec)
         r_dev = torch.empty(n_dev * ld, dtype=dtype, device="cuda:0")
         z_dev = torch.full((n_dev * ld,), float("nan"), dtype=dtype, device="cuda:0")
+        # the library works on its own stream: torch's fill must be done first
+        torch.cuda.synchronize()
         ctx.to_device_layout(b, r_dev.data_ptr(), prec)
         ctx.precondition_device_static(r_dev.data_ptr(), z_dev.data_ptr(), prec)
         z = np.empty(p.n * p.P)
@@ -63,6 +65,7 @@ def test_static_rejects_vectors_beyond_the_maximum(built_pkg):
     assert n_dev * ld * 8 > STATIC_BYTES
     r = torch.zeros(n_dev * ld, dtype=torch.float64, device="cuda:0")
     z = torch.zeros_like(r)
+    torch.cuda.synchronize()
     with pytest.raises(pkg.SGError) as e:
         op.ctx.precondition_device_static(r.data_ptr(), z.data_ptr(), pkg.FP64)
     assert e.value.code == 1 and "static maximum" in str(e.value)
