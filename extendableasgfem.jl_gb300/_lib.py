@@ -27,6 +27,7 @@ MIXED = 2
 PREC_NONE = 0
 PREC_LATTICE = 1
 PREC_JACOBI = 2
+PREC_CHOLESKY = 3
 
 _P = ctypes.c_void_p
 _I64P = ctypes.POINTER(ctypes.c_int64)
@@ -71,6 +72,9 @@ SIGNATURES = {
     "sgfem_has_lattice": (ctypes.c_int, [_P]),
     "sgfem_update_coupling": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int64, _I64P, _I64P, _DP]),
     "sgfem_lattice_log": (ctypes.c_char_p, [_P]),
+    "sgfem_cholesky_log": (ctypes.c_char_p, [_P]),
+    "sgfem_cholesky_host_solve": (ctypes.c_int, [ctypes.c_int64, _I64P, _I64P, _DP, ctypes.c_int64, _I64P,
+                                                 ctypes.c_int64, _DP, _DP, ctypes.c_char_p, ctypes.c_int]),
     "sgfem_apply": (ctypes.c_int, [_P, _DP, _DP, ctypes.c_int]),
     "sgfem_precondition": (ctypes.c_int, [_P, _DP, _DP, ctypes.c_int, ctypes.c_int]),
     "sgfem_solve": (ctypes.c_int, [_P, _DP, _DP, ctypes.POINTER(SolveOptions), ctypes.POINTER(SolveStats)]),
@@ -153,6 +157,24 @@ def _dp(a):
 
 def _i64p(a):
     return a.ctypes.data_as(_I64P)
+
+
+def cholesky_host_solve(K0, bdofs, B):
+    """sgfem_cholesky_host_solve: K_0^-1 B (B column-major n x P, SGFEVector layout) by
+    the SGFEM_PREC_CHOLESKY factorisation and schedule, on the host; returns (Z, summary)."""
+    lib = load()
+    n = K0.shape[0]
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    P = len(B) // n
+    cp, rv, nz = _csc_arrays(K0)
+    bd = np.ascontiguousarray(np.asarray(bdofs, dtype=np.int64) + 1)
+    Z = np.zeros_like(B)
+    msg = ctypes.create_string_buffer(512)
+    rc = lib.sgfem_cholesky_host_solve(n, _i64p(cp), _i64p(rv), _dp(nz), len(bd), _i64p(bd), P, _dp(B), _dp(Z),
+                                       msg, 512)
+    if rc != OK:
+        raise SGError(rc, msg.value.decode())
+    return Z, msg.value.decode()
 
 
 def _csc_arrays(A):
@@ -251,6 +273,11 @@ class Context:
     @property
     def has_lattice(self):
         return bool(self.lib.sgfem_has_lattice(self.h))
+
+    @property
+    def cholesky_log(self):
+        """The sparse-Cholesky mean preconditioner: its factor size, or 'not factored yet'."""
+        return self.lib.sgfem_cholesky_log(self.h).decode()
 
     @property
     def lattice_log(self):

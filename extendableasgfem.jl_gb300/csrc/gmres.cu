@@ -256,6 +256,7 @@ struct Gm {
             SG_TRY(sg_lat_pass_y(ctx, precision, tmp, nullptr, nullptr, scal));
             return sg_lat_pass_xinv(ctx, precision, tmp, z, 0, scal);
         }
+        if (prec_kind == SGFEM_PREC_CHOLESKY) return sg_chol_apply(ctx, precision, v, z, scal);
         return sg_jacobi(ctx, precision, v, z, 0, prec_kind == SGFEM_PREC_NONE ? 1 : 0, nullptr, nullptr, scal);
     }
 
@@ -406,10 +407,15 @@ extern "C" int sgfem_solve_gmres(sgfem_context* ctx, const double* b0, double* x
         return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad precision");
     if (o.preconditioner == SGFEM_PREC_LATTICE && !ctx->lattice)
         return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice preconditioner unavailable (dofs do not form a power-of-two lattice)");
-    if (o.preconditioner != SGFEM_PREC_LATTICE && o.preconditioner != SGFEM_PREC_JACOBI && o.preconditioner != SGFEM_PREC_NONE)
+    if (o.preconditioner != SGFEM_PREC_LATTICE && o.preconditioner != SGFEM_PREC_JACOBI && o.preconditioner != SGFEM_PREC_NONE &&
+        o.preconditioner != SGFEM_PREC_CHOLESKY)
         return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad preconditioner kind");
     if (!(o.rtol > 0.0) || o.maxit <= 0) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "rtol must be > 0 and maxit > 0");
     SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (o.preconditioner == SGFEM_PREC_CHOLESKY) {
+        SG_TRY(sg_chol_ensure(ctx));
+        SG_TRY(sg_chol_workspace(ctx, SGFEM_FP64));
+    }
     ctx->samples_x_valid = false;
     const size_t total = (size_t)ctx->n * ctx->ld;
     const size_t n64 = total * sizeof(double), n32 = total * sizeof(float);

@@ -254,6 +254,11 @@ struct Solver {
             SG_TRY(sg_lat_pass_y(ctx, precision, tmp, partials, &nb, s));
             SG_TRY(fin(nb, FIN_BETA, fa));
             SG_TRY(sg_lat_pass_xinv(ctx, precision, tmp, p, 1, s));
+        } else if (prec_kind == SGFEM_PREC_CHOLESKY) {
+            SG_TRY(sg_chol_apply(ctx, precision, r, tmp, s));
+            SG_TRY(sg_chol_finish(ctx, precision, r, tmp, p, 2, partials, &nb, s));
+            SG_TRY(fin(nb, FIN_BETA, fa));
+            SG_TRY(sg_chol_finish(ctx, precision, r, tmp, p, 1, nullptr, nullptr, s));
         } else {
             const int identity = prec_kind == SGFEM_PREC_NONE ? 1 : 0;
             SG_TRY(sg_jacobi(ctx, precision, r, p, 2, identity, partials, &nb, s));
@@ -386,9 +391,13 @@ extern "C" int sgfem_precondition(sgfem_context* ctx, const double* b, double* y
     if (precision != SGFEM_FP64 && precision != SGFEM_FP32) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad precision");
     if (kind == SGFEM_PREC_LATTICE && !ctx->lattice)
         return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice preconditioner unavailable (dofs do not form a power-of-two lattice)");
-    if (kind != SGFEM_PREC_LATTICE && kind != SGFEM_PREC_JACOBI && kind != SGFEM_PREC_NONE)
+    if (kind != SGFEM_PREC_LATTICE && kind != SGFEM_PREC_JACOBI && kind != SGFEM_PREC_NONE && kind != SGFEM_PREC_CHOLESKY)
         return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad preconditioner kind");
     SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (kind == SGFEM_PREC_CHOLESKY) {
+        SG_TRY(sg_chol_ensure(ctx));
+        SG_TRY(sg_chol_workspace(ctx, SGFEM_FP64));
+    }
     const size_t vb = sg_vec_bytes(ctx, precision);
     for (int i = 0; i < 3; ++i) SG_TRY(sg_ensure(ctx, ctx->w_vec[i], vb));
     SG_TRY(sgfem_to_device_layout(ctx, b, ctx->w_vec[0].p, precision));
@@ -397,6 +406,8 @@ extern "C" int sgfem_precondition(sgfem_context* ctx, const double* b, double* y
         SG_TRY(sg_lat_pass_x(ctx, precision, ctx->w_vec[0].p, ctx->w_vec[2].p, nullptr));
         SG_TRY(sg_lat_pass_y(ctx, precision, ctx->w_vec[2].p, nullptr, nullptr, nullptr));
         SG_TRY(sg_lat_pass_xinv(ctx, precision, ctx->w_vec[2].p, ctx->w_vec[1].p, 0, nullptr));
+    } else if (kind == SGFEM_PREC_CHOLESKY) {
+        SG_TRY(sg_chol_apply(ctx, precision, ctx->w_vec[0].p, ctx->w_vec[1].p, nullptr));
     } else if (kind == SGFEM_PREC_JACOBI) {
         SG_TRY(sg_jacobi(ctx, precision, ctx->w_vec[0].p, ctx->w_vec[1].p, 0, 0, nullptr, nullptr, nullptr));
     } else {
@@ -409,12 +420,16 @@ extern "C" int sgfem_time_precondition(sgfem_context* ctx, int precision, int re
     SG_TRY(sg_check_ready(ctx));
     if (reps <= 0 || !ms_per_application) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad reps");
     if (precision != SGFEM_FP64 && precision != SGFEM_FP32) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad precision");
-    if (!ctx->lattice) return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice preconditioner unavailable");
     SG_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (!ctx->lattice) {
+        SG_TRY(sg_chol_ensure(ctx));
+        SG_TRY(sg_chol_workspace(ctx, SGFEM_FP64));
+    }
     const size_t vb = sg_vec_bytes(ctx, precision);
     for (int i = 0; i < 3; ++i) SG_TRY(sg_ensure(ctx, ctx->w_vec[i], vb));
     SG_CUDA(ctx, cudaMemsetAsync(ctx->w_vec[0].p, 0, vb, ctx->stream));
     auto once = [&]() -> int {
+        if (!ctx->lattice) return sg_chol_apply(ctx, precision, ctx->w_vec[0].p, ctx->w_vec[1].p, nullptr);
         SG_TRY(sg_lat_pass_x(ctx, precision, ctx->w_vec[0].p, ctx->w_vec[2].p, nullptr));
         SG_TRY(sg_lat_pass_y(ctx, precision, ctx->w_vec[2].p, nullptr, nullptr, nullptr));
         return sg_lat_pass_xinv(ctx, precision, ctx->w_vec[2].p, ctx->w_vec[1].p, 0, nullptr);
@@ -439,9 +454,14 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
     int prec_kind = o->preconditioner;
     if (prec_kind == SGFEM_PREC_LATTICE && !ctx->lattice)
         return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice preconditioner unavailable (dofs do not form a power-of-two lattice)");
-    if (prec_kind != SGFEM_PREC_LATTICE && prec_kind != SGFEM_PREC_JACOBI && prec_kind != SGFEM_PREC_NONE)
+    if (prec_kind != SGFEM_PREC_LATTICE && prec_kind != SGFEM_PREC_JACOBI && prec_kind != SGFEM_PREC_NONE &&
+        prec_kind != SGFEM_PREC_CHOLESKY)
         return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "bad preconditioner kind");
     if (!(o->rtol > 0.0) || o->maxit <= 0) return sg_fail(ctx, SGFEM_ERR_ARGUMENT, "rtol must be > 0 and maxit > 0");
+    if (prec_kind == SGFEM_PREC_CHOLESKY) {  // factor and size its workspace before any capture
+        SG_TRY(sg_chol_ensure(ctx));
+        SG_TRY(sg_chol_workspace(ctx, SGFEM_FP64));
+    }
     const int check_every = std::max(1, std::min(o->check_every, 64));
     const size_t n64 = sg_vec_bytes(ctx, SGFEM_FP64), n32 = sg_vec_bytes(ctx, SGFEM_FP32);
     const size_t total = (size_t)ctx->n * ctx->ld;

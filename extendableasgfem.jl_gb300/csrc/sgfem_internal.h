@@ -52,6 +52,8 @@ struct DeviceBuf {
 
 enum { SG_NBUF = 14 };
 
+struct MeanChol;  // sparse-Cholesky mean preconditioner (meanchol.cu)
+
 struct sgfem_context {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -168,6 +170,7 @@ struct sgfem_context {
     double* d_lat_blk64 = nullptr;  // per (kx, ky) in [1, Nl/2]^2: 10 values of a symmetric 4x4 block
     float* d_lat_blk32 = nullptr;
     std::string lat_log;            // which mean-based preconditioner is in use, and why
+    MeanChol* chol = nullptr;       // exact K_0^-1 on any mesh (factored at the first use)
 
     // workspaces (lazily sized)
     DeviceBuf w_stage;         // host-layout staging (n*P doubles)
@@ -272,6 +275,19 @@ int sg_lat_pass_xinv(sgfem_context* ctx, int precision, const void* T, void* out
 // mode 1: out = D^-1 R + beta*out on interior rows ; mode 2: r'z partials only
 int sg_jacobi(sgfem_context* ctx, int precision, const void* R, void* out, int mode, int identity,
               double* rz, int* nblocks, const KrylovScalars* scal);
+// mean-based preconditioner on any mesh by sparse Cholesky (meanchol.cu): K_0 of the
+// interior rows is kept at finalize, factored at the first use (never inside a capture)
+int sg_chol_prepare(sgfem_context* ctx, const std::vector<int64_t>& rowptr, const std::vector<int32_t>& col,
+                    const std::vector<double>& val64);
+int sg_chol_ensure(sgfem_context* ctx);
+int sg_chol_workspace(sgfem_context* ctx, int precision);
+// Z = K_0^-1 R on interior rows, boundary rows of Z zero
+int sg_chol_apply(sgfem_context* ctx, int precision, const void* R, void* Z, const KrylovScalars* scal);
+// mode 2: r'z partials; mode 1: P = Z + beta P (interior rows)
+int sg_chol_finish(sgfem_context* ctx, int precision, const void* R, const void* Z, void* P, int mode, double* rz,
+                   int* nblocks, const KrylovScalars* scal);
+const char* sg_chol_log(const sgfem_context* ctx);
+void sg_chol_release(sgfem_context* ctx);
 // set the dynamic shared-memory limits once (before any graph capture)
 int sg_lattice_configure(sgfem_context* ctx);
 int sg_apply_configure(sgfem_context* ctx);

@@ -102,6 +102,22 @@ def unit_square_mesh(N):
     return Mesh(coords, cells)
 
 
+def perturbed_unit_square_mesh(N, delta=0.2, seed=0):
+    """unit_square_mesh(N) with every interior vertex moved by a uniform random
+    offset of at most delta * h in each direction (h = 1/N; delta < 0.25 keeps every
+    triangle positively oriented, at 0.25 two corners can meet): a non-uniform mesh
+    whose dofs form no lattice, standing in for the locally refined meshes of the
+    adaptive loop."""
+    if not (0.0 <= delta < 0.25):
+        raise ValueError("delta in [0, 0.25)")
+    m = unit_square_mesh(N)
+    p = m.coords.copy()
+    inner = np.nonzero((p[:, 0] > 0) & (p[:, 0] < 1) & (p[:, 1] > 0) & (p[:, 1] < 1))[0]
+    rng = np.random.default_rng(seed)
+    p[inner] += rng.uniform(-delta / N, delta / N, size=(len(inner), 2))
+    return Mesh(p, m.cells)
+
+
 class H1Pk:
     def __init__(self, mesh, order):
         if order not in (1, 2):

@@ -62,6 +62,13 @@ class SGOperator:
     def has_lattice(self):
         return self.ctx.has_lattice
 
+    @property
+    def mean_preconditioner(self):
+        """The exact mean-based preconditioner (the reference's LU(K_0) solve): the
+        sine-transform form on power-of-two dof lattices, the sparse Cholesky of K_0
+        on every other mesh."""
+        return _lib.PREC_LATTICE if self.has_lattice else _lib.PREC_CHOLESKY
+
     def update_basis(self, TB):
         """The adaptive loop appended modes: switch to the TensorizedBasis TB (same
         spatial blocks; TB's multi-index length may not exceed len(Ks) - 1).  The
@@ -83,14 +90,14 @@ class SGOperator:
     def ldiv(self, b, kind=None, precision=_lib.FP64):
         """ldiv!(y, P, b): mean-based preconditioner on every mode."""
         if kind is None:
-            kind = _lib.PREC_LATTICE if self.has_lattice else _lib.PREC_JACOBI
+            kind = self.mean_preconditioner
         return self.ctx.precondition(b, kind, precision)
 
     def solve_primal(self, b0, x, rtol=1e-12, precision=_lib.MIXED, preconditioner=None, maxit=5000,
                      inner_rtol=1e-4, reference_rhs=True, check_every=8, allow_maxit=False):
         """solve_primal!: x (SGFEVector.entries) is the warm start and receives the solution."""
         if preconditioner is None:
-            preconditioner = _lib.PREC_LATTICE if self.has_lattice else _lib.PREC_JACOBI
+            preconditioner = self.mean_preconditioner
         o = self.ctx.default_options(precision=precision, preconditioner=preconditioner, rtol=rtol, maxit=maxit,
                                      inner_rtol=inner_rtol, reference_rhs=1 if reference_rhs else 0,
                                      check_every=check_every)
@@ -101,7 +108,7 @@ class SGOperator:
         """solve_logpoisson_primal!: GMRES for the non-symmetric operator; b_full holds
         the n x P right-hand side blocks, x the warm start (receives the solution)."""
         if preconditioner is None:
-            preconditioner = _lib.PREC_LATTICE if self.has_lattice else _lib.PREC_JACOBI
+            preconditioner = self.mean_preconditioner
         o = self.ctx.default_options(precision=precision, preconditioner=preconditioner, rtol=rtol, maxit=maxit,
                                      inner_rtol=inner_rtol, reference_rhs=1 if reference_rhs else 0)
         return self.ctx.solve_gmres(b_full, x, o, restart=restart, allow_maxit=allow_maxit).as_dict()

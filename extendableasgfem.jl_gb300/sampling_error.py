@@ -22,7 +22,7 @@ import numpy as np
 
 from . import _lib
 from .estimate import _Mesh, _Quad
-from .fem import H1Pk, assemble_rhs, assemble_stiffness, triangle_rule
+from .fem import H1Pk, assemble_rhs, assemble_stiffness_gpu, triangle_rule
 from .modelproblems import PoissonProblemPrimal
 
 
@@ -119,7 +119,7 @@ class SampleProblems:
         self.ctx.set_samples(samples)
 
     def options(self, rtol=1e-10, precision=_lib.MIXED, maxit=5000, check_every=8):
-        prec = _lib.PREC_LATTICE if self.ctx.has_lattice else _lib.PREC_JACOBI
+        prec = _lib.PREC_LATTICE if self.ctx.has_lattice else _lib.PREC_CHOLESKY
         return self.ctx.default_options(precision=precision, preconditioner=prec, rtol=rtol, maxit=maxit,
                                         reference_rhs=0, check_every=check_every)
 
@@ -210,7 +210,7 @@ def calculate_sampling_error(sol, C, problem=PoissonProblemPrimal, bonus_quadord
     if Ms < M:
         raise ValueError("Msamples below the multi-index length")
     Vd = H1Pk(FES.mesh, order)
-    Kd = assemble_stiffness(Vd, C, list(range(Ms + 1)), 2 * (order - 1) + bonus_quadorder_a)
+    Kd = assemble_stiffness_gpu(Vd, C, list(range(Ms + 1)), 2 * (order - 1) + bonus_quadorder_a, device=device)
     bd = assemble_rhs(Vd, rhs, order + bonus_quadorder_f)
     B = min(batch, S)
     errH1 = np.zeros((M + 1, S))

@@ -48,6 +48,9 @@ extern "C" {
 #define SGFEM_PREC_NONE 0
 #define SGFEM_PREC_LATTICE 1    /* mean-based I (x) (a0 L)^-1, L = 5-point lattice Laplacian */
 #define SGFEM_PREC_JACOBI 2     /* I (x) diag(K_0)^-1 */
+#define SGFEM_PREC_CHOLESKY 3   /* mean-based I (x) K_0^-1 on any mesh: sparse Cholesky of K_0 on the
+                                   interior dofs (nested-dissection order), factored at the first use;
+                                   the reference's LU(K_0) solve, solvers_poisson_primal.jl:23-78 */
 
 typedef struct sgfem_context sgfem_context;
 
@@ -112,6 +115,21 @@ SGFEM_API int sgfem_has_lattice(const sgfem_context* ctx);
    lattice, as for P1/P2 with a constant mean) or the 5-point Laplacian scaled by
    the mean diagonal, with the reason */
 SGFEM_API const char* sgfem_lattice_log(const sgfem_context* ctx);
+/* the sparse-Cholesky mean preconditioner (SGFEM_PREC_CHOLESKY) of a finalized
+   context: "not factored yet" before its first use, then the factor's size (nodes
+   and heights of the nested-dissection tree, nnz(L)) or why the factorisation
+   failed.  Replaces the reference's lu(A0.cscmatrix), solvers_poisson_primal.jl:41. */
+SGFEM_API const char* sgfem_cholesky_log(const sgfem_context* ctx);
+/* Host-only (no GPU needed): the SGFEM_PREC_CHOLESKY factorisation of K_0
+   (1-based CSC, n x n, boundary dofs 1-based) and both triangular solves in the
+   device kernels' order of summation, applied to B (column-major n x P) into Z:
+   Z = K_0^-1 B on the interior rows, zero on the boundary rows, as ldiv! of
+   solvers_poisson_primal.jl:47-78 with the LU of K_0 (1e60 on the boundary
+   diagonals, :30-44).  msg (msglen bytes) receives the factor summary or the
+   error.  For checking the ordering and factorisation on a CPU. */
+SGFEM_API int sgfem_cholesky_host_solve(int64_t n, const int64_t* colptr, const int64_t* rowval,
+                                        const double* nzval, int64_t nb, const int64_t* bdofs, int64_t P,
+                                        const double* B, double* Z, char* msg, int msglen);
 
 /*
  * mul!(Ax, S::MySystemPrimal, x), solvers_poisson_primal.jl:86-124:
