@@ -584,6 +584,10 @@ static int build_coupling(sgfem_context* ctx, const std::vector<double>* val64, 
         SG_TRY(upload(ctx, &ctx->d_combq, combq.data(), combq.size()));
         SG_TRY(upload(ctx, &ctx->d_combg64, combg.data(), combg.size()));
         SG_TRY(upload(ctx, &ctx->d_combg32, combg32.data(), combg32.size()));
+        ctx->h_qtab = qtab;
+        ctx->h_combptr = combptr;
+        ctx->h_combq = combq;
+        ctx->h_combg = combg;
     return SGFEM_OK;
 }
 
@@ -648,6 +652,8 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
     }
     for (int64_t i = 0; i < n; ++i) rowptr[i + 1] = rowptr[i] + rowcount[i + 1];
     const int64_t nnz = rowptr[n];
+    ctx->row_nnz_max = 0;
+    for (int64_t i = 0; i < n; ++i) ctx->row_nnz_max = std::max<int>(ctx->row_nnz_max, (int)rowcount[i + 1]);
     if (nnz > (int64_t)INT32_MAX) return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "more than 2^31 nonzeros");
     ctx->nnz = nnz;
     if (same) {

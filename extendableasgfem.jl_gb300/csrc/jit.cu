@@ -1271,6 +1271,7 @@ size_t window_smem_bytes(const sgfem_context* ctx, int wpb) {
 }
 
 size_t jit_smem_bytes(const sgfem_context* ctx) {
+    if (ctx->jit_split) return sg_split_smem(ctx, ctx->jit_wwpb);
     const int NS = (int)ctx->jit_slots.size();
     if (ctx->jit_window) return window_smem_bytes(ctx, ctx->jit_wwpb);
     if (ctx->jit_np > 1 && !ctx->jit_async) {
@@ -1326,6 +1327,8 @@ void sg_jit_configure(sgfem_context* ctx) {
     const char* en = getenv("SGFEM_JIT_PASSES");
     ctx->jit_np_req = en ? std::max(1, std::min(8, atoi(en))) : 1;
     if (ctx->jit_async) ctx->jit_np_req = 1;  // the copy-pipeline variants use one pass
+    const char* esp = getenv("SGFEM_JIT_SPLIT");
+    ctx->jit_split_req = esp ? (atoi(esp) != 0) : 1;
     const char* em = getenv("SGFEM_JIT_MINB");
     ctx->jit_minb = em ? std::max(0, std::min(8, atoi(em))) : 0;
 }
@@ -1335,13 +1338,38 @@ int sg_jit_build(sgfem_context* ctx) {
     // lattice-window kernel: lattice-ordered rows with short couplings, one pass, and a
     // window that fits shared memory with at least 4 warps per block
     ctx->jit_window = 0;
+    ctx->jit_split = 0;
+    std::string split_why;
     if (ctx->jit_window_req && ctx->lat_order && !ctx->jit_async && ctx->jit_np <= 1 && ctx->win_hx <= 4 &&
         ctx->win_hy <= 4 && ctx->ld % 4 == 0 && ctx->jit_T > 0) {
-        int wpb = ctx->jit_wwpb;
-        while (wpb >= 4 && window_smem_bytes(ctx, wpb) > 220 * 1024) --wpb;
-        if (wpb >= 4) {
-            ctx->jit_wwpb = wpb;
-            ctx->jit_window = 1;
+        // split-slot form first (jit_split.cu), else the pair-slot window form
+        if (ctx->jit_split_req && sg_split_plan(ctx, split_why) == SGFEM_OK) {
+            if (sg_split_upload(ctx) != SGFEM_OK) split_why = "split tables: device allocation failed";
+            // block shape of the split form: 16 warps of one row per lattice line unless asked otherwise
+            if (!getenv("SGFEM_JIT_WWPB")) ctx->jit_wwpb = 16;
+            if (!getenv("SGFEM_JIT_WRW")) ctx->jit_wrw = 1;
+            int wpb = ctx->jit_wwpb;
+            while (wpb >= 4 && sg_split_smem(ctx, wpb) > 220 * 1024) --wpb;
+            if (!split_why.empty()) {
+                sg_split_release(ctx);
+            } else if (wpb >= 4) {
+                ctx->jit_wwpb = wpb;
+                ctx->jit_window = 1;
+                ctx->jit_split = 1;
+            } else {
+                sg_split_release(ctx);
+                split_why = "window does not fit shared memory";
+            }
+        }
+        if (!ctx->jit_split) {
+            if (!getenv("SGFEM_JIT_WWPB")) ctx->jit_wwpb = 12;
+            if (!getenv("SGFEM_JIT_WRW")) ctx->jit_wrw = 2;
+            int wpb = ctx->jit_wwpb;
+            while (wpb >= 4 && window_smem_bytes(ctx, wpb) > 220 * 1024) --wpb;
+            if (wpb >= 4) {
+                ctx->jit_wwpb = wpb;
+                ctx->jit_window = 1;
+            }
         }
     }
     // the difference form is generated by the single-pass kernels only
@@ -1363,7 +1391,8 @@ int sg_jit_build(sgfem_context* ctx) {
         ctx->jit_log = g_drv.err;
         return SGFEM_ERR_UNSUPPORTED;
     }
-    const std::string src = ctx->jit_window ? generate_source_window(ctx)
+    const std::string src = ctx->jit_split ? sg_split_source(ctx)
+                            : ctx->jit_window ? generate_source_window(ctx)
                             : ctx->jit_async == 2 ? generate_source_bulk(ctx)
                             : ctx->jit_async ? generate_source_async(ctx)
                             : ctx->jit_np > 1 ? generate_source_passes(ctx) : generate_source(ctx);
@@ -1440,7 +1469,9 @@ int sg_jit_build(sgfem_context* ctx) {
                    (ctx->jit_window ? ", lattice window " + std::to_string(ctx->jit_wwpb * ctx->jit_wrw) + " x " +
                                           std::to_string(2 * ctx->win_hy + 2) + " lines, " +
                                           std::to_string(ctx->jit_wwpb) + " warps"
-                                    : std::string());
+                                    : std::string()) +
+                   (ctx->jit_split ? ", " + sg_split_summary(ctx)
+                                   : (split_why.empty() ? std::string() : " (split form not used: " + split_why + ")"));
     return SGFEM_OK;
 }
 
@@ -1471,9 +1502,17 @@ int sg_jit_launch(sgfem_context* ctx, const void* X, void* Y, double* partials, 
     int* errp = ctx->d_jit_err;
     void* args[] = {(void*)&rowptr, (void*)&colp, (void*)&vals, (void*)&X, (void*)&Y, (void*)&n, (void*)&bm,
                     (void*)&jtab, (void*)&partials, (void*)&scal, (void*)&errp};
+    const int2* sjtab = nullptr;
+    const int* lanetab = nullptr;
+    void* sargs[] = {(void*)&rowptr, (void*)&colp, (void*)&vals, (void*)&X, (void*)&Y, (void*)&n, (void*)&bm,
+                     (void*)&sjtab, (void*)&lanetab, (void*)&partials, (void*)&scal, (void*)&errp};
+    if (ctx->jit_split) {
+        sjtab = sg_split_jtab(ctx);
+        lanetab = sg_split_lanetab(ctx);
+    }
     const unsigned threads = (unsigned)(ctx->jit_window ? ctx->jit_wwpb : JWPB) * 32;
     CUresult r = g_drv.launch_kernel((CUfunction)ctx->jit_func, grid, 1, 1, threads, 1, 1, smem,
-                                     (CUstream)ctx->stream, args, nullptr);
+                                     (CUstream)ctx->stream, ctx->jit_split ? sargs : args, nullptr);
     if (r != CUDA_SUCCESS) return sg_fail(ctx, SGFEM_ERR_CUDA, "cuLaunchKernel(sg_apply_jit) failed: " + std::to_string((int)r));
     ctx->launches++;
     return SGFEM_OK;
@@ -1492,6 +1531,8 @@ int sg_jit_check(sgfem_context* ctx) {
 }
 
 void sg_jit_release(sgfem_context* ctx) {
+    sg_split_release(ctx);
+    ctx->jit_split = 0;
     if (ctx->d_jit_err) cudaFree(ctx->d_jit_err);
     ctx->d_jit_err = nullptr;
     if (ctx->jit_module && g_drv.loaded) g_drv.module_unload((CUmodule)ctx->jit_module);

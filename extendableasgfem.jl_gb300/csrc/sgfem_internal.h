@@ -107,6 +107,14 @@ struct sgfem_context {
     float2* d_valdf = nullptr;     // K_m values as (hi, lo) float pairs (double-FP32 residual)
     float2* d_combgdf = nullptr;   // G combination coefficients as (hi, lo)
 
+    // host copies of the pair list and the per-column combination lists (device columns)
+    std::vector<int32_t> h_qtab, h_combptr, h_combq;
+    std::vector<double> h_combg;
+    struct SplitApply* split = nullptr;  // split-slot form of the specialised FP32 apply (jit_split.cu)
+    int jit_split_req = 1;               // asked for (SGFEM_JIT_SPLIT)
+    int jit_split = 0;                   // in use
+    int row_nnz_max = -1;                // longest row of the union pattern (set at finalize)
+
     // device column order of the modes
     std::vector<int32_t> mode_of_col;  // device column -> caller mode
     std::vector<int32_t> imode;        // caller mode -> device column
@@ -244,6 +252,16 @@ bool sg_residual_df_usable(const sgfem_context* ctx);
 int sg_residual_df_prepare(sgfem_context* ctx);
 int sg_split_df(sgfem_context* ctx, double* x, const double* d, void* xs, int add);
 int sg_residual_df(sgfem_context* ctx, const void* xs, const void* bs, float* r32, double* partials, int* nblocks);
+// split-slot form of the lattice-window FP32 apply (jit_split.cu): plan and tables at the
+// first FP32 use (needs the lattice window); source for NVRTC; shared memory; release
+int sg_split_plan(sgfem_context* ctx, std::string& why);  // host only
+int sg_split_upload(sgfem_context* ctx);
+std::string sg_split_source(const sgfem_context* ctx);
+size_t sg_split_smem(const sgfem_context* ctx, int wpb);
+const int* sg_split_lanetab(const sgfem_context* ctx);
+const int2* sg_split_jtab(const sgfem_context* ctx);
+std::string sg_split_summary(const sgfem_context* ctx);
+void sg_split_release(sgfem_context* ctx);
 // whether the specialised kernel takes this X (the window kernel copies 16-byte pieces)
 bool sg_jit_accepts(const sgfem_context* ctx, const void* X);
 

@@ -219,6 +219,9 @@ def test_specialised_fp32_apply_active_and_matches_generic(built_pkg, monkeypatc
 KNOBS = [
     {},
     {"SGFEM_JIT_DIFF": "0"},
+    {"SGFEM_JIT_SPLIT": "0"},
+    {"SGFEM_JIT_SPLIT": "0", "SGFEM_JIT_DIFF": "0"},
+    {"SGFEM_JIT_WWPB": "8", "SGFEM_JIT_WRW": "2"},
     {"SGFEM_JIT_WWPB": "4", "SGFEM_JIT_WRW": "3"},
     {"SGFEM_JIT_WRW": "1"},
     {"SGFEM_JIT_UNROLL": "2"},
@@ -237,8 +240,9 @@ KNOBS = [
 
 @pytest.mark.parametrize("knobs", KNOBS, ids=lambda k: ",".join(f"{a[10:]}={b}" for a, b in k.items()) or "default")
 def test_specialised_apply_launch_variants(built_pkg, monkeypatch, knobs):
-    """Every generated form of the specialised FP32 apply (lattice window with
-    its block shapes, register window with its prefetch depth and staging
+    """Every generated form of the specialised FP32 apply (lattice window in its
+    split-slot and pair-slot forms with their block shapes, register window with
+    its prefetch depth and staging
     buffers, passes over column groups, cp.async ring, bulk copies with
     mbarriers) agrees with FP64 to FP32 accuracy."""
     import __graft_entry__ as ge
@@ -256,6 +260,7 @@ def test_specialised_apply_launch_variants(built_pkg, monkeypatch, knobs):
         assert ("difference form" in log) == (knobs == {}), log
     windowed = not any(k in knobs for k in ("SGFEM_JIT_WINDOW", "SGFEM_JIT_PASSES", "SGFEM_JIT_ASYNC"))
     assert ("lattice window" in log) == windowed, log
+    assert ("split slots" in log) == (windowed and knobs.get("SGFEM_JIT_SPLIT") != "0"), log
     y64 = op.mul(x, pkg.FP64)
     assert rel(y32, y64) <= 1e-5
     op.close()
