@@ -383,9 +383,10 @@ def config1_problem(pkg, N=32, M=5, deg=2):
 
 
 def run_config1(args):
-    """Config 1 (P1 32x32, M=5, total degree 2, P=21): FP64 PCG to 1e-10 and one
-    estimator pass; config 3's mixed-precision errors against FP64 (solution,
-    energy norm, estimator)."""
+    """Config 1 (P1 32x32, M=5, total degree 2, P=21): FP64 PCG and mixed PCG to
+    --rtol (default 1e-10; 1e-8 is the mixed-vs-FP64 target) and one estimator
+    pass; config 3's mixed-precision errors against FP64 (solution, energy norm,
+    estimator)."""
     import __graft_entry__ as ge
     pkg = ge.load_package()
     C, V, TB, sol, Ks, b0 = config1_problem(pkg)
@@ -397,7 +398,7 @@ def run_config1(args):
         ts = []
         for k in range(args.warmup + args.steps):
             x = np.zeros(n * P)
-            st = op.solve_primal(b0, x, rtol=1e-10, precision=prec)
+            st = op.solve_primal(b0, x, rtol=args.rtol, precision=prec)
             if k >= args.warmup:
                 ts.append(st["time_ms"])
         res[name] = (x, st, statistics.median(ts))
@@ -414,8 +415,9 @@ def run_config1(args):
     sol.entries[:] = xm
     etam, ecm, _ = pkg.estimate(pkg.PoissonProblemPrimal, sol, C, rhs=f, bonus_quadorder=2, tail_extension=(10, 2),
                                 op=op)
-    line = {"workload": "config1: P1 32x32 (1089 dofs), M=5, total degree 2 (P=21), PCG to 1e-10 + estimator",
+    line = {"workload": f"config1: P1 32x32 (1089 dofs), M=5, total degree 2 (P=21), PCG to {args.rtol:g} + estimator",
             "fp64_solve_ms": res["fp64"][2], "fp64_iterations": res["fp64"][1]["iterations"],
+            "mixed_speedup_vs_fp64": res["fp64"][2] / res["mixed"][2],
             "mixed_solve_ms": res["mixed"][2], "mixed_iterations": res["mixed"][1]["iterations"],
             "mixed_outer": res["mixed"][1]["outer_iterations"],
             "estimate_ms_wall": statistics.median(tes), "P_ext": len(ext),
@@ -727,6 +729,7 @@ def main():
     ap.add_argument("--directions", type=int, default=20, help="--workload adjoint: finite-difference directions")
     ap.add_argument("--restart", type=int, default=100, help="--workload lognormal: GMRES restart length")
     ap.add_argument("--problems", type=int, default=256, help="--workload batch: number of problems")
+    ap.add_argument("--rtol", type=float, default=1e-10, help="--workload config1: solve tolerance")
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)

@@ -17,8 +17,12 @@
 // problem's tables read from a descriptor; its launch shape (warps per block,
 // pairs per lane, blocks) is chosen at finalize by timing the candidates
 // (autotuner).  FP64 throughout.
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <string>
@@ -618,6 +622,69 @@ int build_map(sgfem_batch* b, int total_blocks, std::vector<BProb>& probs, std::
     return SGFEM_OK;
 }
 
+// ---- on-disk tuning cache: the launch shapes chosen for a set of problem shapes on a
+// device model, so that a later finalize of the same batch skips the timing sweep.
+// One line per entry: "<key hash> wpb qt bps wpb32 qt32 pf32"; the file is
+// SGFEM_TUNE_CACHE, else $XDG_CACHE_HOME/extendableasgfem_gb300/batch_tuning.txt, else
+// $HOME/.cache/extendableasgfem_gb300/batch_tuning.txt ("off" disables it).
+struct TuneEntry {
+    int wpb, qt, bps, wpb32, qt32, pf32;
+};
+
+std::string tune_path() {
+    const char* e = getenv("SGFEM_TUNE_CACHE");
+    if (e) return std::string(e) == "off" ? std::string() : std::string(e);
+    std::string dir;
+    if (const char* x = getenv("XDG_CACHE_HOME")) dir = x;
+    else if (const char* h = getenv("HOME")) dir = std::string(h) + "/.cache";
+    else return std::string();
+    mkdir(dir.c_str(), 0755);  // may exist already
+    dir += "/extendableasgfem_gb300";
+    mkdir(dir.c_str(), 0755);
+    return dir + "/batch_tuning.txt";
+}
+
+std::string tune_key(const sgfem_batch* b) {
+    cudaDeviceProp pr{};
+    cudaGetDeviceProperties(&pr, b->device);
+    std::string k = std::string(pr.name) + "|" + std::to_string(pr.multiProcessorCount) + "|v1";
+    for (const auto& h : b->hp)
+        k += "|" + std::to_string(h.n) + "," + std::to_string(h.P) + "," + std::to_string(h.M1) + "," +
+             std::to_string(h.col.size()) + "," + std::to_string(h.qtab.size()) + "," + std::to_string(h.nl);
+    uint64_t f = 1469598103934665603ull;  // FNV-1a
+    for (unsigned char c : k) {
+        f ^= c;
+        f *= 1099511628211ull;
+    }
+    char buf[48];
+    snprintf(buf, sizeof(buf), "%016llx-%zu", (unsigned long long)f, b->hp.size());
+    return buf;
+}
+
+bool tune_lookup(const std::string& path, const std::string& key, TuneEntry& e) {
+    if (path.empty()) return false;
+    FILE* f = fopen(path.c_str(), "r");
+    if (!f) return false;
+    char k[64];
+    TuneEntry t{};
+    bool found = false;
+    while (fscanf(f, "%63s %d %d %d %d %d %d", k, &t.wpb, &t.qt, &t.bps, &t.wpb32, &t.qt32, &t.pf32) == 7)
+        if (key == k) {
+            e = t;
+            found = true;  // the last entry for a key wins
+        }
+    fclose(f);
+    return found;
+}
+
+void tune_store(const std::string& path, const std::string& key, const TuneEntry& e) {
+    if (path.empty()) return;
+    FILE* f = fopen(path.c_str(), "a");
+    if (!f) return;
+    fprintf(f, "%s %d %d %d %d %d %d\n", key.c_str(), e.wpb, e.qt, e.bps, e.wpb32, e.qt32, e.pf32);
+    fclose(f);
+}
+
 }  // namespace
 
 extern "C" int sgfem_batch_create(sgfem_batch** out, int device) {
@@ -874,7 +941,42 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
     b->d_bprob = d_bmap;
     SG_TRY(balloc(b, (size_t)std::max(max_blocks, 1) * 4 * sizeof(double), (void**)&b->d_part));
     std::string log;
+    // tuning cache: a batch of the same shapes on the same device model was tuned before
+    const std::string tpath = tune_path(), tkey = tune_key(b);
+    TuneEntry te{};
+    bool hit = tune_lookup(tpath, tkey, te);
+    if (hit) {
+        const bool ok64 = (te.wpb == 4 || te.wpb == 8) && (te.qt == 8 || te.qt == 16) && te.bps >= 1 &&
+                          te.bps <= 16 && (int)apply_smem(b, te.wpb) <= dev_smem;
+        const bool ok32 = (te.wpb32 == 4 || te.wpb32 == 8) && (te.qt32 == 16 || te.qt32 == 32) &&
+                          (te.pf32 == 0 || (te.pf32 == 1 && b->ldmax <= 32 * BPC && b->m1max <= 32 * BPV)) &&
+                          (int)apply_smem<float>(b, te.wpb32) <= dev_smem;
+        hit = ok64 && ok32;
+    }
+    if (hit) {
+        const size_t sm64 = apply_smem(b, te.wpb), sm32 = apply_smem<float>(b, te.wpb32);
+        if (sm64 > 48 * 1024)
+            BCUDA(b, te.qt == 8 ? cudaFuncSetAttribute(k_bapply<double, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm64)
+                                : cudaFuncSetAttribute(k_bapply<double, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm64));
+        if (sm32 > 48 * 1024) {
+            cudaError_t e32;
+            if (te.pf32)
+                e32 = te.qt32 == 16 ? cudaFuncSetAttribute(k_bapply<float, 16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm32)
+                                    : cudaFuncSetAttribute(k_bapply<float, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm32);
+            else
+                e32 = te.qt32 == 16 ? cudaFuncSetAttribute(k_bapply<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm32)
+                                    : cudaFuncSetAttribute(k_bapply<float, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm32);
+            BCUDA(b, e32);
+        }
+        best = 0.f;
+        bestc = Cand{te.wpb, te.qt, te.bps};
+        b->wpb32 = te.wpb32;
+        b->qt32 = te.qt32;
+        b->pf32 = te.pf32;
+        log = "from the tuning cache " + tpath + "; ";
+    }
     for (const Cand& c : cands) {
+        if (hit) break;
         const size_t smem = apply_smem(b, c.wpb);
         if ((int)smem > dev_smem) continue;
         if (smem > 48 * 1024) {
@@ -917,6 +1019,7 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
     for (int pf : {0, 1})
         for (int wpb : {4, 8})
             for (int qt : {16, 32}) {
+                if (hit) break;
                 if (pf && (b->ldmax > 32 * BPC || b->m1max > 32 * BPV)) continue;
                 const size_t smem = apply_smem<float>(b, wpb);
                 if ((int)smem > dev_smem) continue;
@@ -962,6 +1065,7 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
                     b->pf32 = pf;
                 }
             }
+    if (!hit) tune_store(tpath, tkey, TuneEntry{b->wpb, b->qt, bestc.bps, b->wpb32, b->qt32, b->pf32});
     char buf[192];
     snprintf(buf, sizeof(buf), "chosen %d warps/block, %d pairs/lane, %d blocks (FP32: %s%d warps/block, %d pairs/lane); ",
              b->wpb, b->qt * 32, b->blocks, b->pf32 ? "prefetch, " : "", b->wpb32, b->qt32 * 32);

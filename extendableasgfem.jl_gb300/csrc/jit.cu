@@ -1328,7 +1328,7 @@ void sg_jit_configure(sgfem_context* ctx) {
     ctx->jit_np_req = en ? std::max(1, std::min(8, atoi(en))) : 1;
     if (ctx->jit_async) ctx->jit_np_req = 1;  // the copy-pipeline variants use one pass
     const char* esp = getenv("SGFEM_JIT_SPLIT");
-    ctx->jit_split_req = esp ? (atoi(esp) != 0) : 1;
+    ctx->jit_split_req = esp ? (atoi(esp) != 0) : 0;  // measured slower than the pair-slot form
     const char* em = getenv("SGFEM_JIT_MINB");
     ctx->jit_minb = em ? std::max(0, std::min(8, atoi(em))) : 0;
 }

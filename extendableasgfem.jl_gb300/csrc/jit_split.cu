@@ -482,9 +482,11 @@ sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const 
             cp_commit();
         }
         for (int kk = 0; kk < KR; ++kk) {
+            // this row's staged values and (at a line start) the window lines it needs; the
+            // copies issued below (the next line, the next row's values) stay in flight
+            cp_wait_all();
             if (kk % RW == 0) {
                 const int y = ya + kk / RW;
-                cp_wait_all();
                 __syncthreads();
                 if (y + HY + 1 < NLY && y + 1 < yb) copy_line(win, X, y + HY + 1, xs);
                 cp_commit();
@@ -493,7 +495,6 @@ sg_apply_jit(const int* __restrict__ rowptr, const int* __restrict__ col, const 
             if (row < 0) continue;
             const int y = ya + kk / RW, x = row - y * NLX;
             const int jcur = jn1, cnt = cn1;
-            cp_wait_all();  // this row's staged values
             float* kb = kbs + cur * KB;
             if ((cnt & 1) && lane < M1) kb[lane * KSTR + cnt] = 0.f;  // complete the last pair
             int kn = kk + 1;

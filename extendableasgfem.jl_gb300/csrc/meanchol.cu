@@ -329,7 +329,9 @@ int host_factor(int64_t n, const std::vector<int64_t>& krowptr, const std::vecto
                 const int32_t j = iidx[kcol[q]];
                 if (j < 0) continue;
                 const int32_t pj = pos[j];
-                if (pj <= k) rowbuf.emplace_back(pj, kval[q]);
+                // exact zeros (e.g. the diagonal edges of P1 on right triangles) are left out
+                // here as in the dissection graph: the factor's pattern must be the graph's
+                if (pj <= k && (kval[q] != 0.0 || pj == k)) rowbuf.emplace_back(pj, kval[q]);
             }
             std::sort(rowbuf.begin(), rowbuf.end());
             for (auto& e : rowbuf) {
@@ -485,6 +487,14 @@ int host_factor(int64_t n, const std::vector<int64_t>& krowptr, const std::vecto
         for (int r = 0; r < s; ++r)
             for (int c = 0; c < s; ++c) Dt[(size_t)c * s + r] = D[(size_t)r * s + c];
     }
+    // ---- the schedule's premise: every gathered entry of a row lies in a strictly lower
+    // node (forward) / strictly higher node (backward) of the dissection tree
+    for (int64_t k = 0; k < ni; ++k)
+        for (int p = fptr[k]; p < fptr[k + 1]; ++p)
+            if (nodes[node_of[fcol[p]]].height >= nodes[node_of[k]].height) {
+                f.err = "mean Cholesky: an entry of L couples two nodes that are not in descent";
+                return SGFEM_ERR_UNSUPPORTED;
+            }
     // ---- schedule by height
     int H = 0;
     for (auto& nd_ : nodes) H = std::max(H, nd_.height + 1);

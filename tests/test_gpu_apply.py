@@ -219,9 +219,10 @@ def test_specialised_fp32_apply_active_and_matches_generic(built_pkg, monkeypatc
 KNOBS = [
     {},
     {"SGFEM_JIT_DIFF": "0"},
-    {"SGFEM_JIT_SPLIT": "0"},
-    {"SGFEM_JIT_SPLIT": "0", "SGFEM_JIT_DIFF": "0"},
-    {"SGFEM_JIT_WWPB": "8", "SGFEM_JIT_WRW": "2"},
+    {"SGFEM_JIT_SPLIT": "1"},
+    {"SGFEM_JIT_SPLIT": "1", "SGFEM_JIT_DIFF": "0"},
+    {"SGFEM_JIT_SPLIT": "1", "SGFEM_JIT_WWPB": "8", "SGFEM_JIT_WRW": "2"},
+    {"SGFEM_JIT_SPLIT": "1", "SGFEM_JIT_WWPB": "16", "SGFEM_JIT_WRW": "1"},
     {"SGFEM_JIT_WWPB": "4", "SGFEM_JIT_WRW": "3"},
     {"SGFEM_JIT_WRW": "1"},
     {"SGFEM_JIT_UNROLL": "2"},
@@ -260,7 +261,7 @@ def test_specialised_apply_launch_variants(built_pkg, monkeypatch, knobs):
         assert ("difference form" in log) == (knobs == {}), log
     windowed = not any(k in knobs for k in ("SGFEM_JIT_WINDOW", "SGFEM_JIT_PASSES", "SGFEM_JIT_ASYNC"))
     assert ("lattice window" in log) == windowed, log
-    assert ("split slots" in log) == (windowed and knobs.get("SGFEM_JIT_SPLIT") != "0"), log
+    assert ("split slots" in log) == (windowed and knobs.get("SGFEM_JIT_SPLIT") == "1"), log
     y64 = op.mul(x, pkg.FP64)
     assert rel(y32, y64) <= 1e-5
     op.close()

@@ -93,3 +93,28 @@ def test_batch_many_kle_terms(built_pkg):
         ref = osg.kron_direct(p.K0, p.Ks, p.G, p.b0, p.bdofs, p.P)
         assert np.linalg.norm(x - ref) <= 1e-8 * np.linalg.norm(ref)
     B.close()
+
+
+def test_batch_tuning_cache(built_pkg, monkeypatch, tmp_path):
+    """The launch shapes tuned at finalize go to the on-disk cache; a batch of
+    the same shapes finalized again takes them from there (no timing sweep) and
+    solves to the same answer."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    cache = tmp_path / "tuning.txt"
+    monkeypatch.setenv("SGFEM_TUNE_CACHE", str(cache))
+    probs = [build(12, 1, 3, pkg.total_degree_multiindices(3, 2)), build(6, 1, 2, pkg.total_degree_multiindices(2, 3))]
+    out = []
+    for attempt in range(2):
+        B = pkg.SGBatch(0)
+        for p in probs:
+            B.add(p.V, p.TB, p.Kall, p.b0)
+        B.finalize()
+        assert ("from the tuning cache" in B.tuning) == (attempt == 1), B.tuning
+        xs, st = B.solve(rtol=1e-10)
+        assert st["converged"] == len(probs) and st["relres_max"] <= 1e-10
+        out.append(xs)
+        B.close()
+    assert cache.exists() and len(cache.read_text().splitlines()) == 1
+    for a, b in zip(*out):
+        assert np.linalg.norm(a - b) <= 1e-9 * np.linalg.norm(b)

@@ -161,3 +161,27 @@ def test_sample_solves_on_perturbed_mesh(built_pkg, precision):
         ref = osm.deterministic_solve(Ks, b0, V.bdofs, y[:, s])
         assert np.linalg.norm(U[:, s] - ref) <= 1e-8 * np.linalg.norm(ref)
     sp_.close()
+
+
+def test_precision_switch_on_one_context(built_pkg):
+    """FP64 then FP32 and mixed solves with the Cholesky form on one context of a
+    structured P1 mesh (exact zeros in K_0): the shared work vectors hold the
+    previous precision's data, which no application may read before writing."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    p = build(12, 1, 6, pkg.top_weight_multiindices(6, 20, C.decay_factors))
+    op = pkg.SGOperator(p.V, p.TB, p.Kall, device=0)
+    assert op.mean_preconditioner == pkg.PREC_CHOLESKY
+    b = np.random.default_rng(4).standard_normal(p.n * p.P)
+    mask = osg.interior_mask(p.n, p.P, p.bdofs)
+    b[~mask] = 0.0
+    ref = osg.MeanPreconditioner(p.K0, p.bdofs, p.P).ldiv(b)
+    for prec, tol, pt in ((pkg.FP64, 1e-10, 1e-10), (pkg.FP32, 1e-6, 1e-4), (pkg.MIXED, 1e-10, 1e-4),
+                          (pkg.FP64, 1e-10, 1e-10)):
+        x = np.zeros(p.n * p.P)
+        st = op.solve_primal(p.b0, x, rtol=tol, precision=prec)
+        assert st["relres"] <= tol, (prec, st)
+        y = op.ldiv(b, pkg.PREC_CHOLESKY, pkg.FP32 if prec != pkg.FP64 else pkg.FP64)
+        assert rel(y[mask], ref[mask]) <= pt, prec
+    op.close()

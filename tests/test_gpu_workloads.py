@@ -60,24 +60,25 @@ def test_config2_fp64_apply_matches_oracle(config2):
 
 
 def test_config2_fp32_default_apply(config2):
-    """The FP32 apply the bench times (the split-slot lattice-window form
+    """The FP32 apply the bench times (the pair-slot lattice-window form
     generated for this coupling structure) agrees with FP64 to FP32 accuracy."""
     pkg, V, TB, Ks, b0, op, cop = config2
     variant, log = op.ctx.apply_variant
-    assert variant == 1 and "lattice window" in log and "split slots" in log, log
+    assert variant == 1 and "lattice window" in log and "split slots" not in log, log
     x = np.random.default_rng(1).standard_normal(V.ndofs * TB.nmodes)
     y64 = op.mul(x, pkg.FP64)
     y32 = op.mul(x, pkg.FP32)
     assert rel(y32, y64) <= 1e-5
 
 
-def test_config2_fp32_pair_slot_form(config2, monkeypatch):
+def test_config2_fp32_split_slot_form(config2, monkeypatch):
+    """The split-slot window form (SGFEM_JIT_SPLIT=1) on the same operator."""
     pkg, V, TB, Ks, b0, op, cop = config2
-    monkeypatch.setenv("SGFEM_JIT_SPLIT", "0")
+    monkeypatch.setenv("SGFEM_JIT_SPLIT", "1")
     op2 = pkg.SGOperator(V, TB, Ks, device=0)
     try:
         variant, log = op2.ctx.apply_variant
-        assert variant == 1 and "lattice window" in log and "split slots" not in log, log
+        assert variant == 1 and "lattice window" in log and "split slots" in log, log
         x = np.random.default_rng(1).standard_normal(V.ndofs * TB.nmodes)
         assert rel(op2.mul(x, pkg.FP32), op.mul(x, pkg.FP64)) <= 1e-5
     finally:
