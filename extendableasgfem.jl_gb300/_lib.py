@@ -73,6 +73,7 @@ SIGNATURES = {
     "sgfem_update_coupling": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int64, _I64P, _I64P, _DP]),
     "sgfem_lattice_log": (ctypes.c_char_p, [_P]),
     "sgfem_cholesky_log": (ctypes.c_char_p, [_P]),
+    "sgfem_small_solve_log": (ctypes.c_char_p, [_P]),
     "sgfem_cholesky_host_solve": (ctypes.c_int, [ctypes.c_int64, _I64P, _I64P, _DP, ctypes.c_int64, _I64P,
                                                  ctypes.c_int64, _DP, _DP, ctypes.c_char_p, ctypes.c_int]),
     "sgfem_apply": (ctypes.c_int, [_P, _DP, _DP, ctypes.c_int]),
@@ -273,6 +274,11 @@ class Context:
     @property
     def has_lattice(self):
         return bool(self.lib.sgfem_has_lattice(self.h))
+
+    @property
+    def small_solve_log(self):
+        """Whether mixed solves run the inner FP32 PCG as one cluster launch, or why not."""
+        return self.lib.sgfem_small_solve_log(self.h).decode()
 
     @property
     def cholesky_log(self):

@@ -93,6 +93,7 @@ extern "C" int sgfem_destroy(sgfem_context* ctx) {
     if (ctx->pcg_graph) cudaGraphDestroy(ctx->pcg_graph);
     sg_jit_release(ctx);
     sg_chol_release(ctx);
+    sg_small_release(ctx);
     for (void* p : ptrs) free_dev(p);
     for (int i = 0; i < SG_NBUF; ++i) free_dev(ctx->w_vec[i].p);
     free_dev(ctx->w_basis.p);
@@ -771,6 +772,8 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
     }
     // exact mean preconditioner for any mesh: K_0 of the interior rows kept, factored at the first use
     SG_TRY(sg_chol_prepare(ctx, rowptr, col, val64));
+    // one-cluster inner PCG for small P1 lattice problems (mixed solves)
+    if (!ctx->batched) SG_TRY(sg_small_prepare(ctx, rowptr, col, val64));
     if (!ctx->batched) SG_TRY(sg_apply_configure(ctx));
     if (ctx->lattice) SG_TRY(sg_lattice_configure(ctx));
     // specialised FP32 apply; on failure the generic kernel stays in use (reason in the variant log)
@@ -809,6 +812,7 @@ extern "C" int sgfem_update_coupling(sgfem_context* ctx, int64_t P, int64_t M, c
         *t = nullptr;
     }
     sg_jit_release(ctx);
+    sg_small_invalidate(ctx);
     ctx->jit_tried = false;
     if (ctx->pcg_exec) cudaGraphExecDestroy(ctx->pcg_exec);
     if (ctx->pcg_graph) cudaGraphDestroy(ctx->pcg_graph);

@@ -624,6 +624,8 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
             float* q32 = (float*)ctx->w_vec[8].p;
             float* tmp32 = (float*)ctx->w_vec[9].p;
             const double in2 = o->precision == SGFEM_FP32 ? tol2e : o->inner_rtol * o->inner_rtol;
+            // small P1 lattice problems: the inner FP32 PCG in one cluster launch (SGFEM_SMALL=0 disables)
+            const bool use_small = prec_kind == SGFEM_PREC_LATTICE && !ctx->batched && sg_small_usable(ctx);
             for (int outer = 0; outer < 64; ++outer) {
                 if (!std::isfinite(rr)) { status = SGFEM_ERR_NONFINITE; break; }
                 if (rr <= tol2e * bb) break;
@@ -651,7 +653,14 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
                 else want = std::max(finish, floor2);
                 SG_TRY(S.fin(g, FIN_TOL, FinArgs{want, 0}, nullptr));
                 int it = 0;
-                int s2 = S.pcg<float, double>(SGFEM_FP32, d64, r32, p32, q32, tmp32, remaining, check_every, &it);
+                int s2 = SGFEM_OK;
+                if (use_small) {  // the whole FP32 PCG in one cluster launch (small.cu)
+                    SG_CUDA(ctx, cudaMemsetAsync(d64, 0, n64, ctx->stream));
+                    SG_TRY(sg_small_pcg(ctx, r32, d64, remaining, &it, &s2));
+                    if (s2 == SGFEM_ERR_MAXIT) s2 = SGFEM_OK;  // the outer loop reports it
+                } else {
+                    s2 = S.pcg<float, double>(SGFEM_FP32, d64, r32, p32, q32, tmp32, remaining, check_every, &it);
+                }
                 st->iterations += it;
                 st->outer_iterations += 1;
                 remaining -= it;

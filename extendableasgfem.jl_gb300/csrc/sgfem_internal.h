@@ -53,6 +53,7 @@ struct DeviceBuf {
 enum { SG_NBUF = 14 };
 
 struct MeanChol;  // sparse-Cholesky mean preconditioner (meanchol.cu)
+struct SmallPCG;  // one-cluster FP32 PCG for small lattice problems (small.cu)
 
 struct sgfem_context {
     int device = 0;
@@ -179,6 +180,7 @@ struct sgfem_context {
     float* d_lat_blk32 = nullptr;
     std::string lat_log;            // which mean-based preconditioner is in use, and why
     MeanChol* chol = nullptr;       // exact K_0^-1 on any mesh (factored at the first use)
+    SmallPCG* small = nullptr;      // one-cluster inner PCG of the mixed solve (small lattice problems)
 
     // workspaces (lazily sized)
     DeviceBuf w_stage;         // host-layout staging (n*P doubles)
@@ -305,6 +307,15 @@ int sg_chol_apply(sgfem_context* ctx, int precision, const void* R, void* Z, con
 int sg_chol_finish(sgfem_context* ctx, int precision, const void* R, const void* Z, void* P, int mode, double* rz,
                    int* nblocks, const KrylovScalars* scal);
 const char* sg_chol_log(const sgfem_context* ctx);
+// one-cluster FP32 inner PCG (small.cu): eligibility and tables at finalize, coupling
+// tables at the first use (again after a coupling update)
+int sg_small_prepare(sgfem_context* ctx, const std::vector<int64_t>& rowptr, const std::vector<int32_t>& col,
+                     const std::vector<double>& val64);
+bool sg_small_usable(sgfem_context* ctx);
+int sg_small_pcg(sgfem_context* ctx, const float* r32, double* d64, int maxit, int* iters, int* status);
+const char* sg_small_log(const sgfem_context* ctx);
+void sg_small_invalidate(sgfem_context* ctx);
+void sg_small_release(sgfem_context* ctx);
 void sg_chol_release(sgfem_context* ctx);
 // set the dynamic shared-memory limits once (before any graph capture)
 int sg_lattice_configure(sgfem_context* ctx);
