@@ -90,9 +90,13 @@ def test_small_other_shapes_and_update(built_pkg, monkeypatch, N, M, deg, cl):
 def test_small_not_used_where_it_does_not_apply(built_pkg):
     import __graft_entry__ as ge
     pkg = ge.load_package()
-    p2 = build(16, 2, 3, pkg.total_degree_multiindices(3, 2))  # P2: the lattice holds edge midpoints
+    p2 = build(16, 2, 3, pkg.total_degree_multiindices(3, 2))  # P2: K_0 is no 5-point Laplacian
     op = pkg.SGOperator(p2.V, p2.TB, p2.Kall, device=0)
-    assert "P1 dof lattice" in op.ctx.small_solve_log
+    assert "5-point Laplacian" in op.ctx.small_solve_log, op.ctx.small_solve_log
+    op.close()
+    odd = build(12, 1, 3, pkg.total_degree_multiindices(3, 2))  # 12 intervals: no power-of-two lattice
+    op = pkg.SGOperator(odd.V, odd.TB, odd.Kall, device=0)
+    assert "power-of-two P1 dof lattice" in op.ctx.small_solve_log, op.ctx.small_solve_log
     op.close()
     big = build(16, 1, 6, pkg.total_degree_multiindices(6, 2))  # 28 modes: fits; 7 terms
     op = pkg.SGOperator(big.V, big.TB, big.Kall, device=0)
