@@ -16,19 +16,25 @@
 //
 // Layout: CTA b of the cluster owns the lattice lines [lo(b), lo(b+1)) (all
 // modes; lane = device column, ld <= 32), its rows of r, p, q, z in shared
-// memory.  Apply: a warp per row, the X rows of neighbouring lines read from the
-// owning CTA's shared memory; per row w_m = sum_j K_m[i,j] (p_j - p_i)
-// (difference form) for every KLE term, then q_mu = w_0[mu] + sum g w_m[nu] with
-// nu fetched by warp shuffles from the lane that owns it.  Preconditioner:
-// x-transform of the CTA's lines, then CTA b transforms the columns kx of its
-// share along y (scale, back along y), then the x-transform back of its lines;
-// the two changes of ownership read the other CTAs' shared memory.  Dot
-// products: per-CTA FP64 partials, summed by every CTA in rank order (all CTAs
-// take identical decisions).  The FP64 solution correction accumulates in
-// global memory (x += alpha p in FP64, as in the multi-launch solve).
+// memory, p with one halo line on each side.  Apply: a warp per row, all
+// operands in shared memory; per row w_m = sum_j K_m[i,j] (p_j - p_i)
+// (difference form, the diagonal left out) for every KLE term, then
+// q_mu = w_0[mu] + sum g w_m[nu] with nu fetched by warp shuffles from the lane
+// that owns it.  Preconditioner: x-transform of the CTA's lines, then CTA b
+// transforms the columns kx of its share along y (scale, back along y), then the
+// x-transform back of its lines; the two changes of ownership read the other
+// CTAs' shared memory.  Dot products: per-warp partials, which every warp of
+// every CTA sums in one fixed order (all CTAs take identical decisions).  The
+// halo lines of p = z + beta p are formed by each CTA from the owners' z, so an
+// iteration has four cluster barriers: the p'q sum, the two transposes of the
+// preconditioner and the joint r'r, r'z sum.  The FP64 solution correction
+// accumulates in shared memory (x += alpha p in FP64, as in the multi-launch
+// solve) and is written out at the end.
 #include <cooperative_groups.h>
 
+#include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -42,28 +48,156 @@ constexpr int SM_THREADS = 512;
 constexpr int SM_WARPS = SM_THREADS / 32;
 constexpr int SM_MAXM1 = 16;   // KLE terms (M + 1) the kernel holds per row
 constexpr int SM_MAXSLOT = 4;  // couplings per (term, output mode)
+constexpr int SM_R = 4;        // transform outputs per warp item (they share the lane-strided loads)
 
 struct SmallGeom {
     int NP;      // lattice points per line (Nl + 1)
     int N;       // interior points per line (Nl - 1)
     int NS;      // row stride of the sine matrix (N rounded up to 4)
     int ld, M1, M1P;
+    int KS;      // stride of a staged nonzero's KLE values (M1 rounded up to 2)
     int CL;      // CTAs in the cluster
     int MAXL;    // lines per CTA (most)
     int MAXK;    // transform columns per CTA (most)
+    int TMAX;    // staged nonzeros per row (most; the diagonal is left out in difference form)
     int diff;
 };
 
 struct SmallTabs {
     const float* S;       // N x NS, S[k][x] (symmetric)
     const float* scale;   // N x N, 1 / (a0 (lam_ky + lam_kx)), [ky][kx]
-    const int* nslot;     // [M1]: couplings per output mode for term m (max over modes)
-    const int* src;       // [M1][SM_MAXSLOT][32]: source lane (device column)
-    const float* g;       // [M1][SM_MAXSLOT][32]: coefficient (0 for padding)
+    const int* nslot;     // [1]: couplings per (term, output mode), most over all terms and modes
+    const int2* cg;       // [SM_MAXSLOT][M1][32]: {source lane, bits of g} (g = 0 for padding)
 };
 
-__device__ __forceinline__ int line_lo(int b, const SmallGeom& G) { return (int)(((long long)b * G.NP) / G.CL); }
-__device__ __forceinline__ int col_lo(int b, const SmallGeom& G) { return (int)(((long long)b * G.N) / G.CL); }
+// float offsets of the shared-memory arrays, each start 16-byte aligned
+struct SmallLayout {
+    int xh, xl, pe, r, q, z, T, Tl, V, sc, S, kv, own, cown, cj, cg, red, total;
+};
+
+__host__ __device__ inline int small_take(int& o, int nfloats) {
+    const int at = o;
+    o += (nfloats + 3) & ~3;
+    return at;
+}
+
+__host__ __device__ inline SmallLayout small_layout(const SmallGeom& G) {
+    SmallLayout L{};
+    int o = 0;
+    const int RMAX = G.MAXL * G.NP;
+    L.xh = small_take(o, RMAX * G.ld);               // [RMAX][ld]: the correction of my rows, high part
+    L.xl = small_take(o, RMAX * G.ld);               // and low part (x = xh + xl)
+    L.pe = small_take(o, (RMAX + 2 * G.NP) * 32);     // p, lines l0 - 1 .. l0 + MAXL
+    L.r = small_take(o, RMAX * 32);
+    L.q = small_take(o, RMAX * 32);
+    L.z = small_take(o, RMAX * 32);
+    L.T = small_take(o, G.MAXL * G.N * 32);           // [MAXL][N][32]: x-transform of my lines
+    L.Tl = small_take(o, G.N * G.MAXK * 32);          // [N][MAXK][32]: my columns, all lines
+    L.V = small_take(o, G.N * G.MAXK * 32);           // [N][MAXK][32]: my columns after y and scale
+    L.sc = small_take(o, G.N * G.MAXK);               // [N][MAXK]: preconditioner scale of my columns
+    L.S = small_take(o, G.N * G.NS);                  // [N][NS]
+    L.kv = small_take(o, RMAX * G.TMAX * G.KS);       // [RMAX][TMAX][KS]: my rows' KLE values
+    L.own = small_take(o, G.NP);                      // [NP]: owner CTA << 16 | line index in the owner
+    L.cown = small_take(o, G.N);                      // [N]: the same for transform columns
+    L.cj = small_take(o, RMAX * G.TMAX);              // [RMAX][TMAX]: row of pe of each nonzero (-1: boundary row)
+    L.cg = small_take(o, SM_MAXSLOT * G.M1 * 32 * 2); // int2 [SM_MAXSLOT][M1][32]
+    L.red = small_take(o, 3 * SM_WARPS);              // [3][SM_WARPS]: p'q, r'r, r'z partials
+    L.total = o;
+    return L;
+}
+
+// out[r] = sum_k S[kr + r][k] * b[k * bs] for r < SM_R (rows clamped to N - 1: their outputs are
+// not stored), S rows 16-byte aligned and broadcast, b lane-strided and shared by the SM_R sums
+__device__ __forceinline__ void dotR(const float* __restrict__ S_s, int NS, int kr, int N,
+                                     const float* __restrict__ b, int bs, float out[SM_R]) {
+    const float* a[SM_R];
+#pragma unroll
+    for (int r = 0; r < SM_R; ++r) {
+        a[r] = S_s + min(kr + r, N - 1) * NS;
+        out[r] = 0.f;
+    }
+    int k = 0;
+    for (; k + 4 <= N; k += 4) {
+        const float b0 = b[k * bs], b1 = b[(k + 1) * bs], b2 = b[(k + 2) * bs], b3 = b[(k + 3) * bs];
+#pragma unroll
+        for (int r = 0; r < SM_R; ++r) {
+            const float4 av = *reinterpret_cast<const float4*>(a[r] + k);
+            out[r] = fmaf(av.x, b0, out[r]);
+            out[r] = fmaf(av.y, b1, out[r]);
+            out[r] = fmaf(av.z, b2, out[r]);
+            out[r] = fmaf(av.w, b3, out[r]);
+        }
+    }
+    for (; k < N; ++k) {
+        const float bk = b[k * bs];
+#pragma unroll
+        for (int r = 0; r < SM_R; ++r) out[r] = fmaf(a[r][k], bk, out[r]);
+    }
+}
+
+// (xh, xl) += (ph, pl) in double-FP32 arithmetic (Knuth's TwoSum of the high parts, then
+// the low parts, renormalised)
+__device__ __forceinline__ void df_add(float& xh, float& xl, float ph, float pl) {
+    const float s = xh + ph;
+    const float bv = s - xh;
+    const float e = (xh - (s - bv)) + (ph - bv);
+    const float t = e + (xl + pl);
+    xh = s + t;
+    xl = t - (xh - s);
+}
+
+// first line / transform column of CTA b (b <= CL; the products stay far below 2^31)
+__device__ __forceinline__ int line_lo(int b, const SmallGeom& G) { return b * G.NP / G.CL; }
+__device__ __forceinline__ int col_lo(int b, const SmallGeom& G) { return b * G.N / G.CL; }
+
+// q = A p on my rows for M1 KLE terms (w_m in registers); returns this thread's p'q partial.
+// Rows are padded to TMAX nonzeros with zero values (no data-dependent exit), couplings to
+// nsl slots per term with g = 0.
+template <int M1>
+__device__ __forceinline__ float apply_rows(const int* __restrict__ cj_s, const float* __restrict__ kv_s,
+                                            const float* __restrict__ pe_s, const float* __restrict__ p_s,
+                                            float* __restrict__ q_s, const int2* __restrict__ cg_s, int nsl,
+                                            int nrow, int warp, int lane, const SmallGeom& G) {
+    constexpr int KS = (M1 + 1) & ~1;
+    const bool lv = lane < G.ld;
+    float part = 0.f;
+    for (int li = warp; li < nrow; li += SM_WARPS) {
+        float qv = 0.f;
+        const int* cr = cj_s + li * G.TMAX;
+        const float pi_ = p_s[li * 32 + lane];
+        if (cr[0] >= 0) {  // warp-uniform: not a boundary row
+            float w[M1];
+#pragma unroll
+            for (int m = 0; m < M1; ++m) w[m] = 0.f;
+            const float* kv = kv_s + (size_t)li * G.TMAX * KS;
+#pragma unroll 2
+            for (int t = 0; t < G.TMAX; ++t) {
+                const float pj = pe_s[cr[t] * 32 + lane];
+                const float u = G.diff ? pj - pi_ : pj;
+#pragma unroll
+                for (int m = 0; m + 1 < M1; m += 2) {
+                    const float2 v = *reinterpret_cast<const float2*>(kv + t * KS + m);
+                    w[m] = fmaf(v.x, u, w[m]);
+                    w[m + 1] = fmaf(v.y, u, w[m + 1]);
+                }
+                if (M1 & 1) w[M1 - 1] = fmaf(kv[t * KS + M1 - 1], u, w[M1 - 1]);
+            }
+            qv = w[0];
+            for (int sl = 0; sl < nsl; ++sl) {  // warp-uniform count; the terms of a slot are independent
+#pragma unroll
+                for (int m = 1; m < M1; ++m) {
+                    const int2 e = cg_s[(sl * M1 + m) * 32 + lane];
+                    const float v = __shfl_sync(0xffffffffu, w[m], e.x);
+                    qv = fmaf(__int_as_float(e.y), v, qv);
+                }
+            }
+            if (!lv) qv = 0.f;
+        }
+        q_s[li * 32 + lane] = qv;
+        part = fmaf(pi_, qv, part);
+    }
+    return part;
+}
 
 __global__ void __launch_bounds__(SM_THREADS, 1)
 k_small_pcg(const int* __restrict__ rowptr, const int* __restrict__ col, const float* __restrict__ vals,
@@ -73,226 +207,275 @@ k_small_pcg(const int* __restrict__ rowptr, const int* __restrict__ col, const f
     const int me = (int)cluster.block_rank();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     extern __shared__ __align__(16) float sm[];
+    const SmallLayout L = small_layout(G);
     const int RMAX = G.MAXL * G.NP;
-    float* r_s = sm;
-    float* p_s = r_s + RMAX * 32;
-    float* q_s = p_s + RMAX * 32;
-    float* z_s = q_s + RMAX * 32;
-    float* T_s = z_s + RMAX * 32;                 // [MAXL][N][32]: x-transform of my lines
-    float* Tl_s = T_s + G.MAXL * G.N * 32;        // [N][MAXK][32]: my columns, all lines
-    float* V_s = Tl_s + G.N * G.MAXK * 32;        // [N][MAXK][32]: my columns after y, scale, y
-    float* Vl_s = V_s + G.N * G.MAXK * 32;        // [MAXL][N][32]: all columns of my lines
-    float* S_s = Vl_s + G.MAXL * G.N * 32;        // [N][NS]
-    int* owner_s = reinterpret_cast<int*>(S_s + G.N * G.NS);  // [NP]
-    int* src_s = owner_s + ((G.NP + 3) & ~3);                   // [M1][SM_MAXSLOT][32]
-    float* g_s = reinterpret_cast<float*>(src_s + G.M1 * SM_MAXSLOT * 32);
-    double* red_s = reinterpret_cast<double*>(g_s + ((G.M1 * SM_MAXSLOT * 32 + 1) & ~1));  // [3]: pq, rr, rz
-    __shared__ double wred[SM_WARPS];
-    __shared__ int nslot_s[SM_MAXM1];
+    float* xh_s = sm + L.xh;
+    float* xl_s = sm + L.xl;
+    float* pe_s = sm + L.pe;
+    float* p_s = pe_s + G.NP * 32;  // my rows; halo line l0 - 1 before, l1 after
+    float* r_s = sm + L.r;
+    float* q_s = sm + L.q;
+    float* z_s = sm + L.z;
+    float* T_s = sm + L.T;
+    float* Tl_s = sm + L.Tl;
+    float* V_s = sm + L.V;
+    // all columns of my lines; shares T_s's storage (T_s is read by the other CTAs only
+    // before the second barrier of an application, Vl_s written after it)
+    float* Vl_s = T_s;
+    float* sc_s = sm + L.sc;
+    float* S_s = sm + L.S;
+    float* kv_s = sm + L.kv;
+    int* owner_s = reinterpret_cast<int*>(sm + L.own);
+    int* cown_s = reinterpret_cast<int*>(sm + L.cown);
+    int* cj_s = reinterpret_cast<int*>(sm + L.cj);
+    int2* cg_s = reinterpret_cast<int2*>(sm + L.cg);
+    float* red_s = sm + L.red;
 
     const int l0 = line_lo(me, G), l1 = line_lo(me + 1, G);
-    const int nrow = (l1 - l0) * G.NP;
+    const int nl = l1 - l0;
+    const int nrow = nl * G.NP;
     const int row0 = l0 * G.NP;
     const int k0 = col_lo(me, G), k1 = col_lo(me + 1, G);
     const int nk = k1 - k0;
+    const int ng = (G.N + SM_R - 1) / SM_R;  // groups of SM_R transform outputs along a line
     const bool lv = lane < G.ld;
+    const int nsl = tb.nslot[0];
     for (int i = threadIdx.x; i < G.N * G.NS; i += SM_THREADS) S_s[i] = tb.S[i];
+    for (int i = threadIdx.x; i < G.N * nk; i += SM_THREADS) {
+        const int ky = i / nk, kk = i - ky * nk;
+        sc_s[ky * G.MAXK + kk] = tb.scale[ky * G.N + k0 + kk];
+    }
+    for (int i = threadIdx.x; i < RMAX * G.ld; i += SM_THREADS) {
+        xh_s[i] = 0.f;
+        xl_s[i] = 0.f;
+    }
     for (int y = threadIdx.x; y < G.NP; y += SM_THREADS) {
         int o = 0;
         while (o + 1 < G.CL && line_lo(o + 1, G) <= y) ++o;
-        owner_s[y] = o;
+        owner_s[y] = o << 16 | (y - line_lo(o, G));
     }
+    for (int kx = threadIdx.x; kx < G.N; kx += SM_THREADS) {
+        int o = 0;
+        while (o + 1 < G.CL && col_lo(o + 1, G) <= kx) ++o;
+        cown_s[kx] = o << 16 | (kx - col_lo(o, G));
+    }
+    for (int i = threadIdx.x; i < (RMAX + 2 * G.NP) * 32; i += SM_THREADS) pe_s[i] = 0.f;
     for (int i = threadIdx.x; i < RMAX * 32; i += SM_THREADS) {
         const int li = i >> 5, c = i & 31;
-        const float v = (li < nrow && c < G.ld) ? rin[(size_t)(row0 + li) * G.ld + c] : 0.f;
-        r_s[i] = v;
-        p_s[i] = 0.f;
+        r_s[i] = (li < nrow && c < G.ld) ? rin[(size_t)(row0 + li) * G.ld + c] : 0.f;
         q_s[i] = 0.f;
         z_s[i] = 0.f;
     }
-    // coupling tables of the apply (per term m, slot s and output lane: source lane, g)
-    for (int i = threadIdx.x; i < G.M1 * SM_MAXSLOT * 32; i += SM_THREADS) {
-        src_s[i] = tb.src[i];
-        g_s[i] = tb.g[i];
+    // my rows' nonzeros, one thread per row: their row in the halo-extended p (lines
+    // l0 - 1 .. l1) and KLE values, in difference form without the diagonal; padded to
+    // TMAX with zero values (at row 0 of p); a boundary row is marked by -1
+    for (int li = threadIdx.x; li < RMAX; li += SM_THREADS) {
+        int cnt = 0;
+        const bool interior = li < nrow && !bmask[row0 + li];
+        if (interior) {
+            const int gi = row0 + li;
+            for (int k = rowptr[gi]; k < rowptr[gi + 1] && cnt < G.TMAX; ++k) {
+                const int j = col[k];
+                if (G.diff && j == gi) continue;
+                const int at = li * G.TMAX + cnt;
+                cj_s[at] = (j / G.NP - (l0 - 1)) * G.NP + j % G.NP;
+                for (int m = 0; m < G.KS; ++m) kv_s[(size_t)at * G.KS + m] = m < G.M1 ? vals[(size_t)k * G.M1P + m] : 0.f;
+                ++cnt;
+            }
+        }
+        for (; cnt < G.TMAX; ++cnt) {
+            const int at = li * G.TMAX + cnt;
+            cj_s[at] = (interior || cnt > 0) ? 0 : -1;
+            for (int m = 0; m < G.KS; ++m) kv_s[(size_t)at * G.KS + m] = 0.f;
+        }
     }
-    if (threadIdx.x < SM_MAXM1) nslot_s[threadIdx.x] = threadIdx.x < G.M1 ? tb.nslot[threadIdx.x] : 0;
+    for (int i = threadIdx.x; i < SM_MAXSLOT * G.M1 * 32; i += SM_THREADS) cg_s[i] = tb.cg[i];
     __syncthreads();
-    const double tol2 = scal->tol2;
+    const float tol2 = (float)scal->tol2;
+    const int nred = G.CL * SM_WARPS;
 
-    // cluster-wide sum of one FP64 value per thread: warp, then CTA, then the CTAs in rank order
-    auto csum = [&](double v, int slot) -> double {
+    // cluster-wide FP32 sums of per-thread values: warp sums into red_s, one cluster barrier,
+    // then every warp adds the CL x SM_WARPS partials in one fixed order (lane e sums
+    // entries e, e + 32, ...; then a butterfly), so every thread of every CTA holds the
+    // same totals.  A slot is written again only after a later cluster barrier.
+    auto wsum = [&](float v) {
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) wred[warp] = v;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double t = 0.0;
-            for (int w = 0; w < SM_WARPS; ++w) t += wred[w];
-            red_s[slot] = t;
+        return v;
+    };
+    auto gather = [&](int slot) {
+        float t = 0.f;
+        for (int e = lane; e < nred; e += 32)
+            t += *cluster.map_shared_rank(red_s + slot * SM_WARPS + (e & (SM_WARPS - 1)), e / SM_WARPS);
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        return t;
+    };
+    auto csum1 = [&](float v, int slot) -> float {
+        v = wsum(v);
+        if (lane == 0) red_s[slot * SM_WARPS + warp] = v;
+        cluster.sync();
+        return gather(slot);
+    };
+    auto csum2 = [&](float a, float b, float& ta, float& tb2) {
+        a = wsum(a);
+        b = wsum(b);
+        if (lane == 0) {
+            red_s[1 * SM_WARPS + warp] = a;
+            red_s[2 * SM_WARPS + warp] = b;
         }
         cluster.sync();
-        double tot = 0.0;
-        for (int o = 0; o < G.CL; ++o) tot += *cluster.map_shared_rank(red_s + slot, o);
-        return tot;
+        ta = gather(1);
+        tb2 = gather(2);
     };
 
     // z = K_0^-1 r on interior points (lanes over modes), boundary rows of z stay zero
     auto precondition = [&]() {
+        float o4[SM_R];
         // x-transform of my interior lines: T[y][kx] = sum_x S[kx][x] r[y][x]
-        for (int it = warp; it < (l1 - l0) * G.N; it += SM_WARPS) {
-            const int ly = it / G.N, kx = it - ly * G.N;
+        for (int it = warp; it < nl * ng; it += SM_WARPS) {
+            const int ly = it / ng, kx = (it - ly * ng) * SM_R;
             const int y = l0 + ly;
-            float acc = 0.f;
-            if (y >= 1 && y <= G.N) {
-                const float* rr = r_s + (ly * G.NP + 1) * 32 + lane;
-                const float* sr = S_s + kx * G.NS;
-                for (int x = 0; x < G.N; ++x) acc = fmaf(sr[x], rr[x * 32], acc);
-            }
-            T_s[(ly * G.N + kx) * 32 + lane] = acc;
+            if (y >= 1 && y <= G.N) dotR(S_s, G.NS, kx, G.N, r_s + (ly * G.NP + 1) * 32 + lane, 32, o4);
+            else for (int r = 0; r < SM_R; ++r) o4[r] = 0.f;
+#pragma unroll
+            for (int r = 0; r < SM_R; ++r)
+                if (kx + r < G.N) T_s[(ly * G.N + kx + r) * 32 + lane] = o4[r];
         }
         cluster.sync();
         // my columns kx in [k0, k1) from the owners of every interior line
         for (int it = warp; it < G.N * nk; it += SM_WARPS) {
             const int y1 = it / nk, kk = it - y1 * nk;  // interior line y1 + 1
-            const int y = y1 + 1, o = owner_s[y];
-            const float* src = cluster.map_shared_rank(T_s, o);
-            Tl_s[(y1 * G.MAXK + kk) * 32 + lane] = src[((y - line_lo(o, G)) * G.N + k0 + kk) * 32 + lane];
+            const int ow = owner_s[y1 + 1];
+            const float* src = cluster.map_shared_rank(T_s, ow >> 16);
+            Tl_s[(y1 * G.MAXK + kk) * 32 + lane] = src[((ow & 0xffff) * G.N + k0 + kk) * 32 + lane];
         }
         __syncthreads();
         // U[ky][kx] = scale * sum_y S[ky][y] Tl[y][kx] ; V[y][kx] = sum_ky S[y][ky] U[ky][kx]
-        for (int it = warp; it < G.N * nk; it += SM_WARPS) {
-            const int ky = it / nk, kk = it - ky * nk;
-            const float* sr = S_s + ky * G.NS;
-            float acc = 0.f;
-            for (int y1 = 0; y1 < G.N; ++y1) acc = fmaf(sr[y1], Tl_s[(y1 * G.MAXK + kk) * 32 + lane], acc);
-            V_s[(ky * G.MAXK + kk) * 32 + lane] = acc * tb.scale[ky * G.N + k0 + kk];
+        for (int it = warp; it < ng * nk; it += SM_WARPS) {
+            const int kg = it / nk, kk = it - kg * nk, ky = kg * SM_R;
+            dotR(S_s, G.NS, ky, G.N, Tl_s + kk * 32 + lane, G.MAXK * 32, o4);
+#pragma unroll
+            for (int r = 0; r < SM_R; ++r)
+                if (ky + r < G.N) V_s[((ky + r) * G.MAXK + kk) * 32 + lane] = o4[r] * sc_s[(ky + r) * G.MAXK + kk];
         }
         __syncthreads();
-        for (int it = warp; it < G.N * nk; it += SM_WARPS) {  // back along y, into Tl
-            const int y1 = it / nk, kk = it - y1 * nk;
-            const float* sr = S_s + y1 * G.NS;
-            float acc = 0.f;
-            for (int ky = 0; ky < G.N; ++ky) acc = fmaf(sr[ky], V_s[(ky * G.MAXK + kk) * 32 + lane], acc);
-            Tl_s[(y1 * G.MAXK + kk) * 32 + lane] = acc;
+        for (int it = warp; it < ng * nk; it += SM_WARPS) {  // back along y, into Tl
+            const int yg = it / nk, kk = it - yg * nk, y1 = yg * SM_R;
+            dotR(S_s, G.NS, y1, G.N, V_s + kk * 32 + lane, G.MAXK * 32, o4);
+#pragma unroll
+            for (int r = 0; r < SM_R; ++r)
+                if (y1 + r < G.N) Tl_s[((y1 + r) * G.MAXK + kk) * 32 + lane] = o4[r];
         }
         cluster.sync();
         // all columns of my interior lines from their owners, then back along x
-        for (int it = warp; it < (l1 - l0) * G.N; it += SM_WARPS) {
+        for (int it = warp; it < nl * G.N; it += SM_WARPS) {
             const int ly = it / G.N, kx = it - ly * G.N;
             const int y = l0 + ly;
             float v = 0.f;
             if (y >= 1 && y <= G.N) {
-                int o = 0;
-                while (o + 1 < G.CL && col_lo(o + 1, G) <= kx) ++o;
-                const float* src = cluster.map_shared_rank(Tl_s, o);
-                v = src[((y - 1) * G.MAXK + (kx - col_lo(o, G))) * 32 + lane];
+                const int ow = cown_s[kx];
+                const float* src = cluster.map_shared_rank(Tl_s, ow >> 16);
+                v = src[((y - 1) * G.MAXK + (ow & 0xffff)) * 32 + lane];
             }
             Vl_s[(ly * G.N + kx) * 32 + lane] = v;
         }
         __syncthreads();
-        for (int it = warp; it < (l1 - l0) * G.N; it += SM_WARPS) {
-            const int ly = it / G.N, x1 = it - ly * G.N;
+        for (int it = warp; it < nl * ng; it += SM_WARPS) {
+            const int ly = it / ng, x1 = (it - ly * ng) * SM_R;
             const int y = l0 + ly;
             if (y < 1 || y > G.N) continue;
-            const float* sr = S_s + x1 * G.NS;
-            const float* vr = Vl_s + ly * G.N * 32 + lane;
-            float acc = 0.f;
-            for (int kx = 0; kx < G.N; ++kx) acc = fmaf(sr[kx], vr[kx * 32], acc);
-            z_s[(ly * G.NP + x1 + 1) * 32 + lane] = lv ? acc : 0.f;
+            dotR(S_s, G.NS, x1, G.N, Vl_s + ly * G.N * 32 + lane, 32, o4);
+#pragma unroll
+            for (int r = 0; r < SM_R; ++r)
+                if (x1 + r < G.N) z_s[(ly * G.NP + x1 + r + 1) * 32 + lane] = lv ? o4[r] : 0.f;
         }
         __syncthreads();
     };
 
-    // q = A p on my rows
-    auto apply = [&]() -> double {
-        double part = 0.0;
-        for (int li = warp; li < nrow; li += SM_WARPS) {
-            const int gi = row0 + li;
-            float qv = 0.f;
-            if (!bmask[gi]) {
-                const float pi_ = p_s[li * 32 + lane];
-                float w[SM_MAXM1];
-#pragma unroll
-                for (int m = 0; m < SM_MAXM1; ++m) w[m] = 0.f;
-                for (int k = rowptr[gi]; k < rowptr[gi + 1]; ++k) {
-                    const int j = col[k];
-                    const int jy = j / G.NP, o = owner_s[jy];
-                    const int lj = j - line_lo(o, G) * G.NP;
-                    const float* pp = (o == me) ? p_s : cluster.map_shared_rank(p_s, o);
-                    const float pj = pp[lj * 32 + lane];
-                    const float u = G.diff ? pj - pi_ : pj;
-                    const float* kv = vals + (size_t)k * G.M1P;
-#pragma unroll
-                    for (int m = 0; m < SM_MAXM1; ++m)
-                        if (m < G.M1) w[m] = fmaf(__ldg(kv + m), u, w[m]);
-                }
-                qv = w[0];
-#pragma unroll
-                for (int m = 1; m < SM_MAXM1; ++m) {
-                    if (m >= G.M1) break;
-                    for (int sl = 0; sl < nslot_s[m]; ++sl) {  // warp-uniform count
-                        const int at = (m * SM_MAXSLOT + sl) * 32 + lane;
-                        const float v = __shfl_sync(0xffffffffu, w[m], src_s[at]);
-                        qv = fmaf(g_s[at], v, qv);
-                    }
-                }
-                if (!lv) qv = 0.f;
-            }
-            q_s[li * 32 + lane] = qv;
-            part += (double)(p_s[li * 32 + lane] * qv);
+    // p = z + bf p on my rows and on the halo lines l0 - 1 and l1, whose z comes from the
+    // owners: complete since the last cluster barrier, and not rewritten before the owner's
+    // next preconditioner, which starts after the next cluster barrier
+    const int hy0 = l0 - 1, hy1 = l1;
+    const bool h0 = nrow > 0 && hy0 >= 0, h1 = nrow > 0 && hy1 < G.NP;
+    const float* hz0 = h0 ? cluster.map_shared_rank(z_s, owner_s[hy0] >> 16) + (size_t)(owner_s[hy0] & 0xffff) * G.NP * 32 : nullptr;
+    const float* hz1 = h1 ? cluster.map_shared_rank(z_s, owner_s[hy1] >> 16) + (size_t)(owner_s[hy1] & 0xffff) * G.NP * 32 : nullptr;
+    float* hp1 = pe_s + (size_t)(hy1 - hy0) * G.NP * 32;
+    auto update_p = [&](float bf) {
+        for (int i = threadIdx.x; i < nrow * 32; i += SM_THREADS) p_s[i] = fmaf(bf, p_s[i], z_s[i]);
+#pragma unroll 4
+        for (int i = threadIdx.x; i < G.NP * 32; i += SM_THREADS) {
+            const float z0 = h0 ? hz0[i] : 0.f, z1 = h1 ? hz1[i] : 0.f;
+            if (h0) pe_s[i] = fmaf(bf, pe_s[i], z0);
+            if (h1) hp1[i] = fmaf(bf, hp1[i], z1);
         }
-        return part;
+    };
+
+    auto apply = [&]() -> float {
+        switch (G.M1) {
+#define SM_APPLY(k) \
+    case k: return apply_rows<k>(cj_s, kv_s, pe_s, p_s, q_s, cg_s, nsl, nrow, warp, lane, G);
+            SM_APPLY(1) SM_APPLY(2) SM_APPLY(3) SM_APPLY(4) SM_APPLY(5) SM_APPLY(6) SM_APPLY(7) SM_APPLY(8)
+            SM_APPLY(9) SM_APPLY(10) SM_APPLY(11) SM_APPLY(12) SM_APPLY(13) SM_APPLY(14) SM_APPLY(15) SM_APPLY(16)
+#undef SM_APPLY
+            default: return 0.f;
+        }
     };
 
     // z = M^-1 r, rho = r'z, p = z
     precondition();
-    double rz_loc = 0.0;
-    for (int i = threadIdx.x; i < nrow * 32; i += SM_THREADS) {
-        rz_loc += (double)(r_s[i] * z_s[i]);
-        p_s[i] = z_s[i];
-    }
-    double rho = csum(rz_loc, 2);
-    int iters = 0, status = SGFEM_OK;
-    double rr = 0.0;
+    float rr = 0.f, rho = 0.f;
     {
-        double rl = 0.0;
-        for (int i = threadIdx.x; i < nrow * 32; i += SM_THREADS) rl += (double)(r_s[i] * r_s[i]);
-        rr = csum(rl, 1);
+        float rl = 0.f, zl = 0.f;
+        for (int i = threadIdx.x; i < nrow * 32; i += SM_THREADS) {
+            rl = fmaf(r_s[i], r_s[i], rl);
+            zl = fmaf(r_s[i], z_s[i], zl);
+        }
+        csum2(rl, zl, rr, rho);
     }
-    if (!isfinite(rho)) status = SGFEM_ERR_NONFINITE;
-    else if (!(rho > 0.0) && rr > tol2) status = SGFEM_ERR_BREAKDOWN;
+    int iters = 0, status = SGFEM_OK;
+    float bf = 0.f;  // p = z + 0 p (p and its halo start at zero)
+    if (!isfinite(rho) || !isfinite(rr)) status = SGFEM_ERR_NONFINITE;
+    else if (!(rho > 0.f) && rr > tol2) status = SGFEM_ERR_BREAKDOWN;
     while (status == SGFEM_OK && rr > tol2) {
         if (iters >= maxit) {
             status = SGFEM_ERR_MAXIT;
             break;
         }
-        cluster.sync();  // p complete in every CTA before the halo reads
-        const double pq = csum(apply(), 0);
+        update_p(bf);
+        __syncthreads();
+        const float pq = csum1(apply(), 0);
         if (!isfinite(pq)) { status = SGFEM_ERR_NONFINITE; break; }
-        if (!(pq > 0.0)) { status = SGFEM_ERR_BREAKDOWN; break; }
-        const double alpha = rho / pq;
-        const float af = (float)alpha;
-        double rl = 0.0;
+        if (!(pq > 0.f)) { status = SGFEM_ERR_BREAKDOWN; break; }
+        const float af = rho / pq;
         for (int i = threadIdx.x; i < nrow * 32; i += SM_THREADS) {
-            const int li = i >> 5, c = i & 31;
-            if (c < G.ld) x64[(size_t)(row0 + li) * G.ld + c] += alpha * (double)p_s[i];
-            const float rv = fmaf(-af, q_s[i], r_s[i]);
-            r_s[i] = rv;
-            rl += (double)(rv * rv);
+            const float pv = p_s[i];
+            r_s[i] = fmaf(-af, q_s[i], r_s[i]);
+            const int c = i & 31;
+            if (c < G.ld) {  // x += af p with the product's rounding error kept (FMA), in double-FP32
+                const int at = (i >> 5) * G.ld + c;
+                const float ph = af * pv;
+                df_add(xh_s[at], xl_s[at], ph, fmaf(af, pv, -ph));
+            }
         }
-        rr = csum(rl, 1);
+        __syncthreads();
+        // z for the next direction (wasted once, at convergence), then r'r and r'z in one sum
+        precondition();
+        float rl = 0.f, zl = 0.f;
+        for (int i = threadIdx.x; i < nrow * 32; i += SM_THREADS) {
+            rl = fmaf(r_s[i], r_s[i], rl);
+            zl = fmaf(r_s[i], z_s[i], zl);
+        }
+        float rho_new;
+        csum2(rl, zl, rr, rho_new);
         ++iters;
         if (!isfinite(rr)) { status = SGFEM_ERR_NONFINITE; break; }
         if (rr <= tol2) break;
-        precondition();
-        double zl = 0.0;
-        for (int i = threadIdx.x; i < nrow * 32; i += SM_THREADS) zl += (double)(r_s[i] * z_s[i]);
-        const double rho_new = csum(zl, 2);
         if (!isfinite(rho_new)) { status = SGFEM_ERR_NONFINITE; break; }
-        if (!(rho_new > 0.0)) { status = SGFEM_ERR_BREAKDOWN; break; }
-        const float bf = (float)(rho_new / rho);
+        if (!(rho_new > 0.f)) { status = SGFEM_ERR_BREAKDOWN; break; }
+        bf = rho_new / rho;
         rho = rho_new;
-        for (int i = threadIdx.x; i < nrow * 32; i += SM_THREADS) p_s[i] = fmaf(bf, p_s[i], z_s[i]);
     }
+    for (int i = threadIdx.x; i < nrow * G.ld; i += SM_THREADS)
+        x64[(size_t)row0 * G.ld + i] = (double)xh_s[i] + (double)xl_s[i];
     cluster.sync();  // no CTA leaves while another may still read its shared memory
     if (me == 0 && threadIdx.x == 0) {
         scal->iters = iters;
@@ -312,19 +495,18 @@ struct SmallPCG {
     float* d_S = nullptr;
     float* d_scale = nullptr;
     int* d_nslot = nullptr;
-    int* d_src = nullptr;
-    float* d_g = nullptr;
+    int* d_cg = nullptr;  // int2 {source lane, bits of g}
     bool tables = false;  // coupling tables for the current G
     size_t smem = 0;
+    long long launches = 0;
+    std::string log;
 };
 
 static void small_free_tables(SmallPCG* s) {
     if (s->d_nslot) cudaFree(s->d_nslot);
-    if (s->d_src) cudaFree(s->d_src);
-    if (s->d_g) cudaFree(s->d_g);
+    if (s->d_cg) cudaFree(s->d_cg);
     s->d_nslot = nullptr;
-    s->d_src = nullptr;
-    s->d_g = nullptr;
+    s->d_cg = nullptr;
     s->tables = false;
 }
 
@@ -342,15 +524,15 @@ void sg_small_invalidate(sgfem_context* ctx) {
     if (ctx->small) small_free_tables(ctx->small);
 }
 
-const char* sg_small_log(const sgfem_context* ctx) { return ctx->small ? ctx->small->why.c_str() : "not prepared"; }
-
-static size_t small_smem(const SmallGeom& G) {
-    const size_t RMAX = (size_t)G.MAXL * G.NP;
-    size_t f = 4 * RMAX * 32 + (size_t)G.MAXL * G.N * 32 + 2 * (size_t)G.N * G.MAXK * 32 +
-               (size_t)G.MAXL * G.N * 32 + (size_t)G.N * G.NS + ((G.NP + 3) & ~3) +
-               (size_t)G.M1 * SM_MAXSLOT * 32 + (((size_t)G.M1 * SM_MAXSLOT * 32 + 1) & ~(size_t)1);
-    return f * sizeof(float) + 4 * sizeof(double);
+const char* sg_small_log(const sgfem_context* ctx) {
+    SmallPCG* s = ctx->small;
+    if (!s) return "not prepared";
+    s->log = s->why;
+    if (s->ok) s->log += "; launches: " + std::to_string(s->launches);
+    return s->log.c_str();
 }
+
+static size_t small_smem(const SmallGeom& G) { return (size_t)small_layout(G).total * sizeof(float); }
 
 // at finalize (rowptr/col/val64 in device numbering): is K_0 on the interior rows a0 times
 // the 5-point Laplacian of a power-of-two P1 lattice, with few enough modes and terms?
@@ -371,6 +553,10 @@ int sg_small_prepare(sgfem_context* ctx, const std::vector<int64_t>& rowptr, con
     }
     if (ctx->ld > 32 || ctx->M1 > SM_MAXM1) {
         s->why = "more than 32 modes or 16 KLE terms";
+        return SGFEM_OK;
+    }
+    if (ctx->win_hy > 1) {  // the apply reads one halo line on each side
+        s->why = "couplings beyond the neighbouring lattice lines";
         return SGFEM_OK;
     }
     const int M1 = ctx->M1;
@@ -413,7 +599,20 @@ int sg_small_prepare(sgfem_context* ctx, const std::vector<int64_t>& rowptr, con
     G.ld = (int)ctx->ld;
     G.M1 = M1;
     G.M1P = ctx->M1P;
+    G.KS = (M1 + 1) & ~1;
     G.diff = ctx->rowsum_zero ? 1 : 0;
+    // staged nonzeros per interior row: in difference form the diagonal contributes nothing
+    G.TMAX = 1;
+    for (int64_t i = 0; i < ctx->n; ++i) {
+        if (ctx->bmask_host[i]) continue;
+        int c = 0;
+        for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k) c += !(G.diff && col[k] == i);
+        G.TMAX = std::max(G.TMAX, c);
+    }
+    if (G.TMAX > 16) {
+        s->why = "rows with more than 16 nonzeros";
+        return SGFEM_OK;
+    }
     // the largest cluster the device runs (16 non-portable, else 8) whose share fits
     size_t smem = 0;
     int CL = 0;
@@ -427,7 +626,7 @@ int sg_small_prepare(sgfem_context* ctx, const std::vector<int64_t>& rowptr, con
         t.MAXK = (N + c - 1) / c;
         if (t.MAXL < 1 || t.MAXK < 1) continue;
         const size_t b = small_smem(t);
-        if (b > 200 * 1024) continue;
+        if (b > 220 * 1024) continue;
         if (cudaFuncSetAttribute(k_small_pcg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b) != cudaSuccess ||
             (c > 8 && cudaFuncSetAttribute(k_small_pcg, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
                           cudaSuccess)) {
@@ -491,32 +690,44 @@ static int small_tables(sgfem_context* ctx, SmallPCG* s) {
             const int m = q >> 16, nu = q & 0xffff;
             lst[m][mu].push_back({nu, (float)ctx->h_combg[e]});
         }
-    std::vector<int> nslot(M1, 0), src((size_t)M1 * SM_MAXSLOT * 32), gmax;
-    std::vector<float> g((size_t)M1 * SM_MAXSLOT * 32, 0.f);
+    // slot-major [SM_MAXSLOT][M1][32]; the kernel runs the most slots any term m >= 1 needs.
+    // The lists hold the terms m >= 1 only: K_0 acts on every mode alone (q = w_0 + ...)
+    std::vector<int> nslot(1, 0), cgt((size_t)SM_MAXSLOT * M1 * 32 * 2);
     for (int m = 0; m < M1; ++m)
         for (int L = 0; L < 32; ++L) {
             if ((int)lst[m][L].size() > SM_MAXSLOT) return SGFEM_ERR_UNSUPPORTED;
-            nslot[m] = std::max(nslot[m], (int)lst[m][L].size());
+            if (m > 0) nslot[0] = std::max(nslot[0], (int)lst[m][L].size());
             for (int t = 0; t < SM_MAXSLOT; ++t) {
-                const size_t at = ((size_t)m * SM_MAXSLOT + t) * 32 + L;
-                src[at] = t < (int)lst[m][L].size() ? lst[m][L][t].first : L;
-                g[at] = t < (int)lst[m][L].size() ? lst[m][L][t].second : 0.f;
+                const size_t at = ((size_t)t * M1 + m) * 32 + L;
+                const float g = t < (int)lst[m][L].size() ? lst[m][L][t].second : 0.f;
+                cgt[2 * at] = t < (int)lst[m][L].size() ? lst[m][L][t].first : L;
+                std::memcpy(&cgt[2 * at + 1], &g, sizeof(float));
             }
         }
     if (cudaMalloc((void**)&s->d_nslot, nslot.size() * sizeof(int)) != cudaSuccess ||
         cudaMemcpy(s->d_nslot, nslot.data(), nslot.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMalloc((void**)&s->d_src, src.size() * sizeof(int)) != cudaSuccess ||
-        cudaMemcpy(s->d_src, src.data(), src.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMalloc((void**)&s->d_g, g.size() * sizeof(float)) != cudaSuccess ||
-        cudaMemcpy(s->d_g, g.data(), g.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+        cudaMalloc((void**)&s->d_cg, cgt.size() * sizeof(int)) != cudaSuccess ||
+        cudaMemcpy(s->d_cg, cgt.data(), cgt.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
         return SGFEM_ERR_CUDA;
     s->tables = true;
     return SGFEM_OK;
 }
 
+// the shared memory of a launch for the context's current mode count (the x rows are ld wide)
+static size_t small_launch_smem(const sgfem_context* ctx, const SmallPCG* s) {
+    SmallGeom G = s->geom;
+    G.ld = (int)ctx->ld;
+    return small_smem(G);
+}
+
 bool sg_small_usable(sgfem_context* ctx) {
     SmallPCG* s = ctx->small;
     if (!s || !s->ok || ctx->ld > 32 || ctx->M1 > SM_MAXM1) return false;
+    if (small_launch_smem(ctx, s) > 220 * 1024) {  // the mode count grew past the shared memory
+        s->ok = false;
+        s->why = "no cluster shape fits the grown mode count";
+        return false;
+    }
     if (small_tables(ctx, s) != SGFEM_OK) {
         s->ok = false;
         s->why = "couplings outside the one-cluster PCG's tables";
@@ -531,9 +742,13 @@ int sg_small_pcg(sgfem_context* ctx, const float* r32, double* d64, int maxit, i
     SmallPCG* s = ctx->small;
     SmallGeom G = s->geom;
     G.ld = (int)ctx->ld;
-    SmallTabs tb{s->d_S, s->d_scale, s->d_nslot, s->d_src, s->d_g};
+    SmallTabs tb{s->d_S, s->d_scale, s->d_nslot, reinterpret_cast<const int2*>(s->d_cg)};
+    // sized for the geometry passed below (the layout the kernel computes from it)
+    const size_t smem = small_smem(G);
+    if (smem != small_launch_smem(ctx, s) || smem > 220 * 1024)
+        return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "small PCG: shared memory does not fit the mode count");
     // the function attributes are per process: set this context's shared-memory size
-    SG_CUDA(ctx, cudaFuncSetAttribute(k_small_pcg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem));
+    SG_CUDA(ctx, cudaFuncSetAttribute(k_small_pcg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (G.CL > 8) SG_CUDA(ctx, cudaFuncSetAttribute(k_small_pcg, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     cudaLaunchConfig_t cfg{};
     cudaLaunchAttribute at[1];
@@ -543,7 +758,7 @@ int sg_small_pcg(sgfem_context* ctx, const float* r32, double* d64, int maxit, i
     at[0].val.clusterDim.z = 1;
     cfg.gridDim = dim3(G.CL);
     cfg.blockDim = dim3(SM_THREADS);
-    cfg.dynamicSmemBytes = s->smem;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = ctx->stream;
     cfg.attrs = at;
     cfg.numAttrs = 1;
@@ -551,6 +766,7 @@ int sg_small_pcg(sgfem_context* ctx, const float* r32, double* d64, int maxit, i
                                     (const float*)ctx->d_val32p, (const unsigned char*)ctx->d_bmask, r32, d64,
                                     ctx->d_scal, tb, G, maxit));
     ctx->launches++;
+    s->launches++;
     KrylovScalars* h = ctx->h_scal;
     SG_CUDA(ctx, cudaMemcpyAsync(h, ctx->d_scal, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, ctx->stream));
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

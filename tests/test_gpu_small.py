@@ -7,6 +7,8 @@ Bars: the mixed solve meets rtol on the FP64 residual, matches the oracle's
 GMRES solution (the reference solve) to 100 * rtol, and agrees with the
 multi-launch inner PCG (SGFEM_SMALL=0) to 1e-8 with the same iteration count
 to within two."""
+import re
+
 import numpy as np
 import pytest
 
@@ -18,6 +20,12 @@ pytestmark = pytest.mark.gpu
 
 def rel(a, b):
     return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def launches(op):
+    """One-cluster PCG launches on the context so far (parsed from its log)."""
+    m = re.search(r"launches: (\d+)", op.ctx.small_solve_log)
+    return int(m.group(1)) if m else -1
 
 
 def oracle_solution(p):
@@ -41,6 +49,7 @@ def test_small_mixed_solve_config1(built_pkg, monkeypatch, rtol):
     ref = oracle_solution(p)
     xs, xm = np.zeros(p.n * p.P), np.zeros(p.n * p.P)
     ss = op.solve_primal(p.b0, xs, rtol=rtol, precision=pkg.MIXED)
+    assert launches(op) == ss["outer_iterations"] > 0, (op.ctx.small_solve_log, ss)
     sm = op_ml.solve_primal(p.b0, xm, rtol=rtol, precision=pkg.MIXED)
     assert ss["relres"] <= rtol and sm["relres"] <= rtol
     assert rel(xs, ref) <= 100 * rtol
@@ -73,6 +82,7 @@ def test_small_other_shapes_and_update(built_pkg, monkeypatch, N, M, deg, cl):
         assert f"{cl} CTAs" in op.ctx.small_solve_log
     x = np.zeros(p.n * p.P)
     st = op.solve_primal(p.b0, x, rtol=1e-10, precision=pkg.MIXED)
+    assert launches(op) == st["outer_iterations"] > 0, (op.ctx.small_solve_log, st)
     ref = osg.kron_direct(p.K0, p.Ks, p.G, p.b0, p.bdofs, p.P) if p.n * p.P < 30000 else oracle_solution(p)
     assert st["relres"] <= 1e-10 and rel(x, ref) <= 1e-8
     mis2 = pkg.total_degree_multiindices(M, deg + 1)
@@ -80,7 +90,9 @@ def test_small_other_shapes_and_update(built_pkg, monkeypatch, N, M, deg, cl):
     if TB2.nmodes <= 32:
         op.update_basis(TB2)
         x2 = np.zeros(p.n * TB2.nmodes)
+        n0 = launches(op)
         st2 = op.solve_primal(p.b0, x2, rtol=1e-10, precision=pkg.MIXED)
+        assert launches(op) - n0 == st2["outer_iterations"] > 0, (op.ctx.small_solve_log, st2)
         b = osg.reference_rhs(np.zeros(p.n * TB2.nmodes), p.b0, p.bdofs, TB2.nmodes)
         r = b - osg.apply_fast(x2, p.K0, p.Ks, TB2.G.toarray(), p.bdofs, TB2.nmodes)
         assert st2["relres"] <= 1e-10 and np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(b)
@@ -90,9 +102,9 @@ def test_small_other_shapes_and_update(built_pkg, monkeypatch, N, M, deg, cl):
 def test_small_not_used_where_it_does_not_apply(built_pkg):
     import __graft_entry__ as ge
     pkg = ge.load_package()
-    p2 = build(16, 2, 3, pkg.total_degree_multiindices(3, 2))  # P2: K_0 is no 5-point Laplacian
+    p2 = build(16, 2, 3, pkg.total_degree_multiindices(3, 2))  # P2: rows couple lines two apart
     op = pkg.SGOperator(p2.V, p2.TB, p2.Kall, device=0)
-    assert "5-point Laplacian" in op.ctx.small_solve_log, op.ctx.small_solve_log
+    assert "beyond the neighbouring lattice lines" in op.ctx.small_solve_log, op.ctx.small_solve_log
     op.close()
     odd = build(12, 1, 3, pkg.total_degree_multiindices(3, 2))  # 12 intervals: no power-of-two lattice
     op = pkg.SGOperator(odd.V, odd.TB, odd.Kall, device=0)
