@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <type_traits>
 #include <vector>
 
 #include "sgfem_internal.h"
@@ -35,6 +36,7 @@
 namespace {
 
 constexpr int LAT_THREADS = 256;
+constexpr bool kLatScalarFFT = false;  // true: the scalar FFT for FP32 lines too
 constexpr int LAT_WARPS = LAT_THREADS / 32;
 
 struct LatGeom {
@@ -165,6 +167,153 @@ __device__ __forceinline__ void fft_dif(T* tile, const T* cs, const T* sn, int l
     }
 }
 
+// The same transform for FP32 lines whose length is a power of 16 (4-bit chunks
+// only), with packed FP32x2 arithmetic: a group's 16 points are held as 8
+// register pairs (point j, point j + 8) of real and of imaginary parts.  The
+// span-8 stage combines the two halves of each pair (scalar); in the span-4, 2,
+// 1 stages the butterflies k and k + 8 share their twiddle, so one packed
+// add / subtract / complex multiply serves both.  Twiddles as in fft_dif:
+// omega^(2^(3-b)) times a root of unity of order 16; in the last chunk omega = 1
+// and the trivial factors (1, i) cost no multiplication.
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float sin_pi8(int m) { return (float)cos_pi8(m <= 4 ? 4 - m : m - 4); }
+
+// the four stages of one group; TRIV: omega = 1 (last chunk, all twiddles constant)
+template <bool TRIV>
+__device__ __forceinline__ void bfly16_packed(float2 (&PR)[8], float2 (&PI)[8], float omr, float omi) {
+    // span 8: point j with point j + 8, twiddle omega * r16^j
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const float ar = PR[j].x, cr = PR[j].y, ai = PI[j].x, ci = PI[j].y;
+        const float dr = ar - cr, di = ai - ci;
+        PR[j].x = ar + cr;
+        PI[j].x = ai + ci;
+        if (TRIV && j == 0) {
+            PR[j].y = dr;
+            PI[j].y = di;
+        } else if (TRIV && j == 4) {  // times i
+            PR[j].y = -di;
+            PI[j].y = dr;
+        } else {
+            float wr = omr, wi = omi;
+            if (TRIV) {
+                wr = (float)cos_pi8(j);
+                wi = sin_pi8(j);
+            } else if (j != 0) {
+                const float c = (float)cos_pi8(j), sg = sin_pi8(j);
+                wr = omr * c - omi * sg;
+                wi = omr * sg + omi * c;
+            }
+            PR[j].y = dr * wr - di * wi;
+            PI[j].y = dr * wi + di * wr;
+        }
+    }
+#pragma unroll
+    for (int bb = 2; bb >= 0; --bb) {
+        if (!TRIV) {  // omega^(2^(3-b))
+            const float sr = omr * omr - omi * omi, si = 2.f * omr * omi;
+            omr = sr;
+            omi = si;
+        }
+        const int hs = 1 << bb;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            if (k & hs) continue;
+            const int k2 = k | hs;
+            const int m = (k & (hs - 1)) << (3 - bb);
+            const float2 A = PR[k], C = PR[k2], Ai = PI[k], Ci = PI[k2];
+            PR[k] = __fadd2_rn(A, C);
+            PI[k] = __fadd2_rn(Ai, Ci);
+            const float2 D = sub2(A, C), Di = sub2(Ai, Ci);
+            if (TRIV && m == 0) {
+                PR[k2] = D;
+                PI[k2] = Di;
+            } else if (TRIV && m == 4) {  // times i
+                PR[k2] = __fmul2_rn(Di, f2(-1.f));
+                PI[k2] = D;
+            } else {
+                float wr = omr, wi = omi;
+                if (TRIV) {
+                    wr = (float)cos_pi8(m);
+                    wi = sin_pi8(m);
+                } else if (m != 0) {
+                    const float c = (float)cos_pi8(m), sg = sin_pi8(m);
+                    wr = omr * c - omi * sg;
+                    wi = omr * sg + omi * c;
+                }
+                PR[k2] = __ffma2_rn(Di, f2(-wi), __fmul2_rn(D, f2(wr)));
+                PI[k2] = __ffma2_rn(Di, f2(wr), __fmul2_rn(D, f2(wi)));
+            }
+        }
+    }
+}
+
+template <int LGL>
+__device__ __forceinline__ void fft_dif_packed(float* tile, const float* cs, const float* sn, int lane, int warp) {
+    static_assert(LGL % 4 == 0 && LGL >= 4 && LGL <= 8, "4-bit chunks");
+    constexpr int L = 1 << LGL;
+    constexpr int NG = L >> 4;                                // groups per chunk
+    constexpr int NGW = (NG + LAT_WARPS - 1) / LAT_WARPS;     // groups per warp
+    if constexpr (LGL == 8) {  // chunk of bits 7..4 (lo = 4): group data back in place
+#pragma unroll
+        for (int w = 0; w < NGW; ++w) {
+            const int g = warp + w * LAT_WARPS;
+            if (g >= NG) break;
+            const int base = ((g >> 4) << 8) | (g & 15);
+            float2 PR[8], PI[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int i0 = base | (j << 4), i1 = base | ((j + 8) << 4);
+                PR[j] = make_float2(tile[(2 * i0) * 32 + lane], tile[(2 * i1) * 32 + lane]);
+                PI[j] = make_float2(tile[(2 * i0 + 1) * 32 + lane], tile[(2 * i1 + 1) * 32 + lane]);
+            }
+            const int jt = (g & 15) << (LGL - 7);
+            bfly16_packed<false>(PR, PI, cs[jt], sn[jt]);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int i0 = base | (j << 4), i1 = base | ((j + 8) << 4);
+                tile[(2 * i0) * 32 + lane] = PR[j].x;
+                tile[(2 * i1) * 32 + lane] = PR[j].y;
+                tile[(2 * i0 + 1) * 32 + lane] = PI[j].x;
+                tile[(2 * i1 + 1) * 32 + lane] = PI[j].y;
+            }
+        }
+        __syncthreads();
+    }
+    // last chunk (bits 3..0, omega = 1): every group of the warp in registers, then the
+    // bit-reversed stores (natural order out)
+    float2 PR[NGW][8], PI[NGW][8];
+#pragma unroll
+    for (int w = 0; w < NGW; ++w) {
+        const int g = warp + w * LAT_WARPS;
+        if (g >= NG) break;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int i0 = g * 16 + j, i1 = g * 16 + j + 8;
+            PR[w][j] = make_float2(tile[(2 * i0) * 32 + lane], tile[(2 * i1) * 32 + lane]);
+            PI[w][j] = make_float2(tile[(2 * i0 + 1) * 32 + lane], tile[(2 * i1 + 1) * 32 + lane]);
+        }
+        bfly16_packed<true>(PR[w], PI[w], 1.f, 0.f);
+    }
+    __syncthreads();  // every input of the last chunk is in registers
+#pragma unroll
+    for (int w = 0; w < NGW; ++w) {
+        const int g = warp + w * LAT_WARPS;
+        if (g >= NG) break;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int r0 = (int)(__brev((unsigned)(g * 16 + j)) >> (32 - LGL));
+            const int r1 = (int)(__brev((unsigned)(g * 16 + j + 8)) >> (32 - LGL));
+            tile[(2 * r0) * 32 + lane] = PR[w][j].x;
+            tile[(2 * r0 + 1) * 32 + lane] = PI[w][j].x;
+            tile[(2 * r1) * 32 + lane] = PR[w][j].y;
+            tile[(2 * r1 + 1) * 32 + lane] = PI[w][j].y;
+        }
+    }
+    __syncthreads();
+}
+
 template <typename T, int LGL>
 __device__ void dst_line(T* tile, const T* tab) {
     constexpr int Nl = 2 << LGL;
@@ -185,7 +334,10 @@ __device__ void dst_line(T* tile, const T* tab) {
     if (warp == 0) tile[lane] = T(0);
     __syncthreads();
     // complex FFT (sign +) of z_k = (y_2k, y_2k+1), k < L, decimation in frequency
-    fft_dif<T, LGL>(tile, cs, sn, lane, warp);  // output in natural order
+    if constexpr (std::is_same<T, float>::value && LGL % 4 == 0 && LGL <= 8 && !kLatScalarFFT)
+        fft_dif_packed<LGL>(tile, cs, sn, lane, warp);  // output in natural order
+    else
+        fft_dif<T, LGL>(tile, cs, sn, lane, warp);  // output in natural order
     // unpack F_k = E_k + w^k O_k for the pair (k, L-k); write X_2k = Im F_k at 2k,
     // Re F_k at 2k+1 (prefix-summed below)
     for (int k = warp; k <= (L >> 1); k += LAT_WARPS) {
