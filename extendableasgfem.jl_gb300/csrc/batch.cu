@@ -83,6 +83,8 @@ struct sgfem_batch {
     std::vector<void*> owned;
     BProb* d_probs = nullptr;
     int* d_bprob = nullptr;
+    int* d_vorder = nullptr;      // work-queue order of the virtual blocks (persistent apply)
+    int* d_wq = nullptr;          // work-queue counter
     KrylovScalars* d_scal = nullptr;
     double *d_x = nullptr, *d_b = nullptr, *d_r = nullptr, *d_p = nullptr, *d_q = nullptr, *d_part = nullptr;
     double* d_z = nullptr;        // preconditioned residual
@@ -98,7 +100,8 @@ struct sgfem_batch {
     long long total = 0;          // sum of n * ld
     int blocks = 0, wpb = 4, qt = 4, ldmax = 0, m1max = 0, qnmax = 0;
     int wpb32 = 4, qt32 = 8;      // launch shape of the FP32 apply (mixed solve)
-    int pf32 = 0;                 // 1: the FP32 apply prefetches the next nonzero into registers
+    int pf32 = 0;                 // bit 0: the FP32 apply prefetches the next nonzero into registers;
+                                  // bit 1: persistent grid over the work queue
     std::string tuning;
     std::vector<KrylovScalars> h_scal;
     double rtol = 0.0;            // of the last solve
@@ -144,21 +147,44 @@ __device__ __forceinline__ void block_sum_store(double v, double* out) {
 constexpr int BPC = 32;  // X columns per lane held for the prefetch
 constexpr int BPV = 8;   // KLE values per lane held for the prefetch (M + 1 <= 256)
 
+//
+// Work items are the virtual blocks of the block map (problem bprob[v], local index
+// v - blk0, partial in partials[v]).  wq == nullptr: one item per launched block
+// (v = blockIdx.x).  Otherwise a persistent grid of resident blocks takes items from
+// the queue counter *wq (zero at launch) in the order vorder (descending cost) until
+// all nvb are taken; the partials land where the plain launch puts them, so the
+// per-problem sums stay fixed-order.
 template <typename T, int QT, bool PF = false>
 __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict__ bprob, const T* __restrict__ X,
                          T* __restrict__ Y, double* __restrict__ partials, const KrylovScalars* __restrict__ scal,
-                         int per_warp) {
-    const int pi = bprob[blockIdx.x];
-    const BProb& d = probs[pi];
+                         int per_warp, const int* __restrict__ vorder, int* __restrict__ wq, int nvb) {
+    __shared__ int s_item;
     extern __shared__ __align__(16) unsigned char bsm_raw[];
     T* bsm = reinterpret_cast<T*>(bsm_raw);
-    const T* vals = bvals<T>(d);
-    const T* combg = bcombg<T>(d);
     const int wpb = blockDim.x >> 5;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int round = 0;; ++round) {
+    int vb;
+    if (wq) {
+        __syncthreads();  // the previous item is finished by every warp (shared area, s_item)
+        if (threadIdx.x == 0) {
+            const int k = atomicAdd(wq, 1);
+            s_item = k < nvb ? vorder[k] : -1;
+        }
+        __syncthreads();
+        vb = s_item;
+        if (vb < 0) break;
+    } else {
+        if (round > 0) break;
+        vb = blockIdx.x;
+    }
+    const int pi = bprob[vb];
+    const BProb& d = probs[pi];
+    const T* vals = bvals<T>(d);
+    const T* combg = bcombg<T>(d);
     if (scal && scal[pi].done) {
-        if (threadIdx.x == 0 && partials) partials[blockIdx.x] = 0.0;
-        return;
+        if (threadIdx.x == 0 && partials) partials[vb] = 0.0;
+        continue;
     }
     T* su = bsm + (size_t)warp * per_warp;
     T* sc = su + d.ld;
@@ -167,7 +193,7 @@ __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict_
     const T* Xp = X + d.voff;
     T* Yp = Y + d.voff;
     double dot = 0.0;
-    const int lb = blockIdx.x - d.blk0;
+    const int lb = vb - d.blk0;
     for (int row = lb * wpb + warp; row < d.n; row += d.nblk * wpb) {
         T* yrow = Yp + (size_t)row * d.ld;
         if (d.bmask[row]) {
@@ -262,8 +288,10 @@ __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict_
         if (threadIdx.x == 0) {
             double s = 0.0;
             for (int w = 0; w < wpb; ++w) s += red[w];
-            partials[blockIdx.x] = s;
+            partials[vb] = s;
         }
+        __syncthreads();  // red is free before the next item
+    }
     }
 }
 
@@ -566,34 +594,41 @@ size_t apply_smem(const sgfem_batch* b, int wpb) {
     return per_warp * sizeof(T) * wpb;
 }
 
+// pf bit 0: the prefetching variant (FP32, 16 or 32 pairs per lane); bit 1: persistent
+// grid over the work queue (resident blocks only, queue counter reset before the launch)
 template <typename T>
 int launch_apply(sgfem_batch* b, int wpb, int qt, const T* X, T* Y, double* partials, const KrylovScalars* scal,
                  int pf = 0) {
     const int per_warp = (int)(((size_t)b->ldmax + b->m1max + 1 + b->qnmax + 3) & ~(size_t)3);
     const size_t smem = apply_smem<T>(b, wpb);
-    if (pf) {  // prefetching variant (tuned for the FP32 apply, 16 or 32 pairs per lane)
-        if (qt == 16)
-            k_bapply<T, 16, true><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials,
-                                                                            scal, per_warp);
-        else
-            k_bapply<T, 32, true><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials,
-                                                                            scal, per_warp);
-        BLAUNCHED(b);
-        return SGFEM_OK;
+    using KF = void (*)(const BProb*, const int*, const T*, T*, double*, const KrylovScalars*, int, const int*, int*, int);
+    KF kf;
+    if (pf & 1) kf = qt == 16 ? k_bapply<T, 16, true> : k_bapply<T, 32, true>;
+    else kf = qt == 4 ? k_bapply<T, 4> : qt == 8 ? k_bapply<T, 8> : qt == 16 ? k_bapply<T, 16> : k_bapply<T, 32>;
+    int grid = b->blocks;
+    int* wq = nullptr;
+    if (pf & 2) {
+        int per_sm = 0;
+        BCUDA(b, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kf, wpb * 32, smem));
+        grid = std::min(b->blocks, std::max(1, per_sm) * b->num_sms);
+        BCUDA(b, cudaMemsetAsync(b->d_wq, 0, sizeof(int), b->stream));
+        wq = b->d_wq;
     }
-    if (qt == 4)
-        k_bapply<T, 4><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials, scal,
-                                                                  per_warp);
-    else if (qt == 8)
-        k_bapply<T, 8><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials, scal,
-                                                                  per_warp);
-    else if (qt == 16)
-        k_bapply<T, 16><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials, scal,
-                                                                   per_warp);
-    else
-        k_bapply<T, 32><<<b->blocks, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials, scal,
-                                                                   per_warp);
+    kf<<<grid, wpb * 32, smem, b->stream>>>(b->d_probs, b->d_bprob, X, Y, partials, scal, per_warp, b->d_vorder, wq,
+                                            b->blocks);
     BLAUNCHED(b);
+    return SGFEM_OK;
+}
+
+// the block map and the work-queue order (virtual blocks by descending rows x pairs each) to the device
+int upload_map(sgfem_batch* b, const std::vector<BProb>& probs, const std::vector<int>& bprob) {
+    std::vector<int> order(bprob.size());
+    std::iota(order.begin(), order.end(), 0);
+    auto cost = [&](int v) { return b->hp[bprob[v]].work / probs[bprob[v]].nblk; };
+    std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return cost(u) > cost(v); });
+    BCUDA(b, cudaMemcpy(b->d_probs, probs.data(), probs.size() * sizeof(BProb), cudaMemcpyHostToDevice));
+    BCUDA(b, cudaMemcpy(b->d_bprob, bprob.data(), bprob.size() * sizeof(int), cudaMemcpyHostToDevice));
+    BCUDA(b, cudaMemcpy(b->d_vorder, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice));
     return SGFEM_OK;
 }
 
@@ -939,6 +974,8 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
     const int max_blocks = b->num_sms * 16 + B;
     SG_TRY(balloc(b, (size_t)std::max(max_blocks, 1) * 4 * sizeof(int), (void**)&d_bmap));
     b->d_bprob = d_bmap;
+    SG_TRY(balloc(b, (size_t)std::max(max_blocks, 1) * 4 * sizeof(int), (void**)&b->d_vorder));
+    SG_TRY(balloc(b, sizeof(int), (void**)&b->d_wq));
     SG_TRY(balloc(b, (size_t)std::max(max_blocks, 1) * 4 * sizeof(double), (void**)&b->d_part));
     std::string log;
     // tuning cache: a batch of the same shapes on the same device model was tuned before
@@ -949,7 +986,8 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
         const bool ok64 = (te.wpb == 4 || te.wpb == 8) && (te.qt == 8 || te.qt == 16) && te.bps >= 1 &&
                           te.bps <= 16 && (int)apply_smem(b, te.wpb) <= dev_smem;
         const bool ok32 = (te.wpb32 == 4 || te.wpb32 == 8) && (te.qt32 == 16 || te.qt32 == 32) &&
-                          (te.pf32 == 0 || (te.pf32 == 1 && b->ldmax <= 32 * BPC && b->m1max <= 32 * BPV)) &&
+                          te.pf32 >= 0 && te.pf32 <= 3 &&
+                          (!(te.pf32 & 1) || (b->ldmax <= 32 * BPC && b->m1max <= 32 * BPV)) &&
                           (int)apply_smem<float>(b, te.wpb32) <= dev_smem;
         hit = ok64 && ok32;
     }
@@ -960,7 +998,7 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
                                 : cudaFuncSetAttribute(k_bapply<double, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm64));
         if (sm32 > 48 * 1024) {
             cudaError_t e32;
-            if (te.pf32)
+            if (te.pf32 & 1)
                 e32 = te.qt32 == 16 ? cudaFuncSetAttribute(k_bapply<float, 16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm32)
                                     : cudaFuncSetAttribute(k_bapply<float, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm32);
             else
@@ -989,8 +1027,7 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
         }
         SG_TRY(build_map(b, b->num_sms * c.bps, probs, bprob));
         if ((int)bprob.size() > max_blocks * 4) continue;
-        BCUDA(b, cudaMemcpy(b->d_probs, probs.data(), (size_t)B * sizeof(BProb), cudaMemcpyHostToDevice));
-        BCUDA(b, cudaMemcpy(b->d_bprob, bprob.data(), bprob.size() * sizeof(int), cudaMemcpyHostToDevice));
+        SG_TRY(upload_map(b, probs, bprob));
         SG_TRY(launch_apply<double>(b, c.wpb, c.qt, b->d_p, b->d_q, b->d_part, nullptr));  // warm-up
         BCUDA(b, cudaEventRecord(b->ev0, b->stream));
         SG_TRY(launch_apply<double>(b, c.wpb, c.qt, b->d_p, b->d_q, b->d_part, nullptr));
@@ -1010,22 +1047,21 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
     b->wpb = bestc.wpb;
     b->qt = bestc.qt;
     SG_TRY(build_map(b, b->num_sms * bestc.bps, probs, bprob));
-    BCUDA(b, cudaMemcpy(b->d_probs, probs.data(), (size_t)B * sizeof(BProb), cudaMemcpyHostToDevice));
-    BCUDA(b, cudaMemcpy(b->d_bprob, bprob.data(), bprob.size() * sizeof(int), cudaMemcpyHostToDevice));
+    SG_TRY(upload_map(b, probs, bprob));
     // FP32 apply of the mixed solve on the same block map: more pairs per pass amortise
     // the staging of each X row (LSU-bound rather than FP64-bound)
     std::string log32;
     float best32 = 1e30f;
-    for (int pf : {0, 1})
+    for (int pf : {0, 1, 2, 3})
         for (int wpb : {4, 8})
             for (int qt : {16, 32}) {
                 if (hit) break;
-                if (pf && (b->ldmax > 32 * BPC || b->m1max > 32 * BPV)) continue;
+                if ((pf & 1) && (b->ldmax > 32 * BPC || b->m1max > 32 * BPV)) continue;
                 const size_t smem = apply_smem<float>(b, wpb);
                 if ((int)smem > dev_smem) continue;
                 {  // the register budget of the variant must allow the block size
                     cudaFuncAttributes fa{};
-                    const cudaError_t ea = pf ? (qt == 16 ? cudaFuncGetAttributes(&fa, k_bapply<float, 16, true>)
+                    const cudaError_t ea = (pf & 1) ? (qt == 16 ? cudaFuncGetAttributes(&fa, k_bapply<float, 16, true>)
                                                           : cudaFuncGetAttributes(&fa, k_bapply<float, 32, true>))
                                               : (qt == 16 ? cudaFuncGetAttributes(&fa, k_bapply<float, 16>)
                                                           : cudaFuncGetAttributes(&fa, k_bapply<float, 32>));
@@ -1036,7 +1072,7 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
                 }
                 if (smem > 48 * 1024) {
                     cudaError_t e;
-                    if (pf)
+                    if (pf & 1)
                         e = qt == 16 ? cudaFuncSetAttribute(k_bapply<float, 16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
                                      : cudaFuncSetAttribute(k_bapply<float, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
                     else
@@ -1056,7 +1092,8 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
                 float ms = 0.f;
                 BCUDA(b, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
                 char buf32[96];
-                snprintf(buf32, sizeof(buf32), "%s%dw/%dq:%.3fms ", pf ? "prefetch " : "", wpb, qt, ms / 2);
+                snprintf(buf32, sizeof(buf32), "%s%s%dw/%dq:%.3fms ", (pf & 2) ? "queue " : "", (pf & 1) ? "prefetch " : "",
+                         wpb, qt, ms / 2);
                 log32 += buf32;
                 if (ms < best32) {
                     best32 = ms;
@@ -1066,9 +1103,12 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
                 }
             }
     if (!hit) tune_store(tpath, tkey, TuneEntry{b->wpb, b->qt, bestc.bps, b->wpb32, b->qt32, b->pf32});
-    char buf[192];
+    if (const char* q = getenv("SGFEM_BATCH_QUEUE"))  // 1 / 0: the FP32 apply over the work queue or not
+        b->pf32 = atoi(q) ? (b->pf32 | 2) : (b->pf32 & 1);
+    char buf[256];
     snprintf(buf, sizeof(buf), "chosen %d warps/block, %d pairs/lane, %d blocks (FP32: %s%d warps/block, %d pairs/lane); ",
-             b->wpb, b->qt * 32, b->blocks, b->pf32 ? "prefetch, " : "", b->wpb32, b->qt32 * 32);
+             b->wpb, b->qt * 32, b->blocks, b->pf32 == 3 ? "work queue, prefetch, " : b->pf32 == 2 ? "work queue, " : b->pf32 ? "prefetch, " : "",
+             b->wpb32, b->qt32 * 32);
     b->tuning = buf + log + "FP32 " + log32;
     b->finalized = true;
     return SGFEM_OK;

@@ -118,3 +118,32 @@ def test_batch_tuning_cache(built_pkg, monkeypatch, tmp_path):
     assert cache.exists() and len(cache.read_text().splitlines()) == 1
     for a, b in zip(*out):
         assert np.linalg.norm(a - b) <= 1e-9 * np.linalg.norm(b)
+
+
+def test_batch_work_queue_apply_is_bitwise_the_block_map(built_pkg, monkeypatch):
+    """The FP32 apply over the persistent work queue (SGFEM_BATCH_QUEUE=1: resident
+    blocks take the block map's items in descending-cost order) computes every item
+    as the one-block-per-item launch does and leaves each partial in the same
+    slot, so the mixed solves are bitwise equal and meet rtol."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    shapes = [(9, 3, 2), (5, 2, 2), (12, 4, 2), (6, 5, 1), (7, 2, 3), (16, 3, 2)]
+    probs = [build(N, 1, M, pkg.total_degree_multiindices(M, d)) for N, M, d in shapes]
+    monkeypatch.setenv("SGFEM_TUNE_CACHE", "off")
+    out = {}
+    for q in ("0", "1"):
+        monkeypatch.setenv("SGFEM_BATCH_QUEUE", q)
+        B = pkg.SGBatch(0)
+        for p in probs:
+            B.add(p.V, p.TB, p.Kall, p.b0)
+        B.finalize()
+        assert ("work queue" in B.tuning.split(";")[0]) == (q == "1"), B.tuning
+        xs, st = B.solve(rtol=1e-10, check_every=8)
+        assert st["converged"] == len(probs) and st["relres_max"] <= 1e-10
+        out[q] = xs
+        B.close()
+    for a, b in zip(out["0"], out["1"]):
+        assert np.array_equal(a, b)
+    for p, x in zip(probs, out["1"]):
+        ref = osg.kron_direct(p.K0, p.Ks, p.G, p.b0, p.bdofs, p.P)
+        assert np.linalg.norm(x - ref) <= 1e-8 * np.linalg.norm(ref)
