@@ -3,8 +3,9 @@
 Mirrors src/sgfevector.jl of ExtendableASGFEM.jl (one unknown): ``entries``
 is a flat Float64 vector holding the column-major n x P block matrix, mode mu
 at entries[mu*n:(mu+1)*n] (sgfevector.jl:86-106).  ``set_sample`` evaluates
-sum_k H_k(y) U[:, k] (sgfevector.jl:43-69) on the host for single samples;
-batched evaluation on the GPU is ``evaluate_samples`` in sampling_error.py.
+sum_k H_k(y) U[:, k] (sgfevector.jl:43-69) on the GPU: the batched evaluation
+``evaluate_samples`` (sampling_error.py, sgfem_evaluate_samples) with one
+sample, on a light context the vector keeps for later samples.
 """
 import numpy as np
 
@@ -20,6 +21,7 @@ class SGFEVector:
         self.entries = np.zeros(n * P)
         self.last_sample = np.zeros(TB.maxlength_multiindices())
         self.FEV = np.zeros(n)
+        self._eval_ctx = None  # device context of set_sample (created at the first call)
 
     @property
     def ndofs(self):
@@ -40,16 +42,20 @@ class SGFEVector:
         """n x P column view of the entries."""
         return self.entries.reshape(self.num_multiindices(), self.ndofs).T
 
-    def set_sample(self, S):
+    def set_sample(self, S, device=0):
+        """set_sample!(SolutionSGFEM, S) (sgfevector.jl:43-69): keeps S, sets the
+        basis sample (tensorizedbasis.jl:226-252; dimensions beyond len(S) take
+        p_0 = 1, p_k = 0) and evaluates FEV = sum_k H_k(S) U[:, k] on the GPU."""
+        from .sampling_error import _light_samples_context, evaluate_samples
+        S = np.asarray(S, dtype=np.float64).ravel()
         self.last_sample[:] = 0.0
         k = min(len(S), len(self.last_sample))
         self.last_sample[:k] = S[:k]
-        self.TB.set_sample(S[:len(self.TB.vals)], normalize=True)
-        self.FEV[:] = 0.0
-        for j, mode in enumerate(self.active_modes):
-            r = self.TB.evaluate(mode)
-            if r != 0:
-                self.FEV += r * self[j]
+        x = S[:len(self.TB.vals)]
+        self.TB.set_sample(x, normalize=True)
+        if self._eval_ctx is None:
+            self._eval_ctx = _light_samples_context(self.FES_space[0], device)
+        self.FEV[:] = evaluate_samples(self, x[:, None], m=len(x), ctx=self._eval_ctx)[:, 0]
         return self.FEV
 
     def norms(self, p=2):

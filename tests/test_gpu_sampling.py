@@ -81,6 +81,22 @@ def test_evaluate_samples_matches_oracle(built_pkg, basis):
         assert np.max(np.abs(out - ref)) <= 1e-13 * np.max(np.abs(ref))
 
 
+@pytest.mark.parametrize("basis", ["legendre", "hermite"])
+def test_set_sample_on_the_gpu_matches_oracle(built_pkg, basis):
+    """SGFEVector.set_sample (set_sample!, sgfevector.jl:43-69) evaluates on the
+    GPU: FEV against the oracle for samples shorter than, equal to and longer than
+    the multi-index length (and empty), and the stored sample."""
+    pkg, p, TBo = sg_case(M=4, deg=3, basis=basis, solve=False)
+    rng = np.random.default_rng(21)
+    for L in (0, 2, 4, 7):
+        S = rng.uniform(-1, 1, L) if basis == "legendre" else rng.standard_normal(L)
+        fev = p.sol.set_sample(S).copy()
+        ref = osm.sg_evaluate(p.sol.entries, p.n, TBo, S[:p.M])
+        assert np.max(np.abs(fev - ref)) <= 1e-13 * np.max(np.abs(ref)), L
+        assert np.array_equal(p.sol.last_sample[:min(L, p.M)], S[:min(L, p.M)])
+        assert not np.any(p.sol.last_sample[min(L, p.M):])
+
+
 def det_oracle(p, Ms, order=2, bonus_a=10):
     N = int(round(np.sqrt(p.V.mesh.ncells / 2)))
     mesh = of.StructuredMesh(N)
