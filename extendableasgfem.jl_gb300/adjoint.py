@@ -19,7 +19,7 @@ import numpy as np
 
 from . import _lib
 from .estimate import _Mesh
-from .fem import assemble_rhs, assemble_stiffness, assemble_stiffness_nodal_mean, box_functional
+from .fem import assemble_rhs_gpu, assemble_stiffness_gpu, assemble_stiffness_nodal_mean, box_functional
 from .modelproblems import SGOperator
 
 
@@ -33,8 +33,8 @@ class MeanQoI:
         self.n = FES.ndofs
         p = FES.order
         self.quadorder_a = 2 * (p - 1) + bonus_quadorder_a
-        self.Km = assemble_stiffness(FES, C, list(range(1, self.M + 1)), self.quadorder_a)
-        self.b0 = assemble_rhs(FES, rhs, p + bonus_quadorder_f)
+        self.Km = assemble_stiffness_gpu(FES, C, list(range(1, self.M + 1)), self.quadorder_a, device=device)
+        self.b0 = assemble_rhs_gpu(FES, rhs, p + bonus_quadorder_f, device=device)
         self.l = box_functional(FES, box)
         mesh = FES.mesh
         self._coords = np.ascontiguousarray(mesh.coords, dtype=np.float64)

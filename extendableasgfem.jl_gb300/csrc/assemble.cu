@@ -31,7 +31,8 @@
 
 namespace {
 
-constexpr int AQ = 16;  // largest cell rule
+constexpr int AQ = 16;      // quadrature points per chunk of the gather (one chunk up to 16 points)
+constexpr int AQMAX = 1024; // largest cell rule
 
 struct AGeo {
     double x0, y0, j00, j10, j01, j11, g[6], vol;
@@ -94,27 +95,32 @@ __global__ void k_gather(AArgs a, double* __restrict__ values) {
             const int la = ab / a.nd, lb = ab - la * a.nd;
             const AGeo& G = a.geo[c];
             const int W = a.kind == 0 ? 1 : 2;
-            double gd[2 * AQ];
-            for (int q = 0; q < a.nq; ++q) {
-                const double lam[3] = {1.0 - a.xq[2 * q] - a.xq[2 * q + 1], a.xq[2 * q], a.xq[2 * q + 1]};
-                double gr[12];
-                sgfem_fe::basis_grad(a.order, G.g, lam, gr);
-                const double wv = a.wq[q] * G.vol;
-                if (a.kind == 0) {
-                    gd[q] = wv * (gr[2 * la] * gr[2 * lb] + gr[2 * la + 1] * gr[2 * lb + 1]);
-                } else {
-                    // row la tests with phi_la, column lb is the ansatz grad phi_lb
-                    double v[6];
-                    sgfem_fe::basis_val(a.order, lam, v);
-                    gd[2 * q] = -wv * v[la] * gr[2 * lb];
-                    gd[2 * q + 1] = -wv * v[la] * gr[2 * lb + 1];
+            // the rule in chunks of AQ points (the per-point geometric factors in registers)
+            for (int q0 = 0; q0 < a.nq; q0 += AQ) {
+                const int nqc = min(AQ, a.nq - q0);
+                double gd[2 * AQ];
+                for (int qq = 0; qq < nqc; ++qq) {
+                    const int q = q0 + qq;
+                    const double lam[3] = {1.0 - a.xq[2 * q] - a.xq[2 * q + 1], a.xq[2 * q], a.xq[2 * q + 1]};
+                    double gr[12];
+                    sgfem_fe::basis_grad(a.order, G.g, lam, gr);
+                    const double wv = a.wq[q] * G.vol;
+                    if (a.kind == 0) {
+                        gd[qq] = wv * (gr[2 * la] * gr[2 * lb] + gr[2 * la + 1] * gr[2 * lb + 1]);
+                    } else {
+                        // row la tests with phi_la, column lb is the ansatz grad phi_lb
+                        double v[6];
+                        sgfem_fe::basis_val(a.order, lam, v);
+                        gd[2 * qq] = -wv * v[la] * gr[2 * lb];
+                        gd[2 * qq + 1] = -wv * v[la] * gr[2 * lb + 1];
+                    }
                 }
-            }
-            for (int mi = 0; mi < a.nterms; ++mi) {
-                const double* Ac = a.A + ((size_t)mi * a.nc + c) * a.nq * W;
-                double s = 0.0;
-                for (int q = 0; q < a.nq * W; ++q) s = fma(Ac[q], gd[q], s);
-                values[(size_t)mi * a.nnz + k] += s;
+                for (int mi = 0; mi < a.nterms; ++mi) {
+                    const double* Ac = a.A + ((size_t)mi * a.nc + c) * a.nq * W + (size_t)q0 * W;
+                    double s = 0.0;
+                    for (int q = 0; q < nqc * W; ++q) s = fma(Ac[q], gd[q], s);
+                    values[(size_t)mi * a.nnz + k] += s;
+                }
             }
         }
     }
@@ -193,7 +199,7 @@ int assemble_bilinear(sgfem_context* ctx, const char* who, int kind, const sgfem
     if (!mesh || !space || !coef || !quad || !colptr || !rowval || !values) return fail("null pointer");
     if (space->order != 1 && space->order != 2) return fail("order must be 1 or 2");
     if (m0 < 0 || m1 < m0 || m1 > coef->maxm) return fail("terms outside 0..maxm");
-    if (quad->nq < 1 || quad->nq > AQ) return fail("cell rule must have 1..16 points");
+    if (quad->nq < 1 || quad->nq > AQMAX) return fail("cell rule must have 1..1024 points");
     const int nd = sgfem_fe::ndofs4cell(space->order);
     const int64_t nc = mesh->ncells, n = space->ndofs;
     if (nc <= 0 || n <= 0 || nnz <= 0 || colptr[n] - 1 != nnz) return fail("bad sizes");
@@ -391,7 +397,7 @@ int assemble_rhs(sgfem_context* ctx, const char* who, const sgfem_mesh* mesh, co
     };
     if (!mesh || !space || !quad || !f_qp || !b) return fail("null pointer");
     if (space->order != 1 && space->order != 2) return fail("order must be 1 or 2");
-    if (quad->nq < 1 || quad->nq > AQ) return fail("cell rule must have 1..16 points");
+    if (quad->nq < 1 || quad->nq > AQMAX) return fail("cell rule must have 1..1024 points");
     const int nd = sgfem_fe::ndofs4cell(space->order);
     const int64_t nc = mesh->ncells, n = space->ndofs;
     if (nc <= 0 || n <= 0 || nc > INT32_MAX || P < 1 || M < 0) return fail("bad sizes");

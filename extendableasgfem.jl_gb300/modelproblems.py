@@ -155,14 +155,15 @@ def assemble(problem, sol, C, rhs, bonus_quadorder_a=2, bonus_quadorder_f=0, dev
 
 def solve(problem, sol, C, rhs=None, bonus_quadorder_a=2, bonus_quadorder_f=0, use_iterative_solver=True,
           device=0, **solver_kwargs):
-    """solve!(problem, sol, C; rhs, ...): solves on the GPU, writes sol.entries,
-    returns the (0-based) boundary dofs like the reference returns bdofs.
+    """solve!(problem, sol, C; rhs, ...): assembles (poisson_primal.jl:55-68) and
+    solves on GPU ``device``, writes sol.entries, returns the (0-based) boundary
+    dofs like the reference returns bdofs.
     ``solver_kwargs`` go to SGOperator.solve_primal (rtol, precision, ...)."""
     if not issubclass(problem, AbstractModelProblem) or problem is AbstractModelProblem:
         raise NotImplementedError("This model problem seems to have no solver implemented!")
     if not use_iterative_solver:
         raise NotImplementedError("the GPU path has no assembled Kronecker solver; use_iterative_solver=True")
-    Ks, b0 = assemble(problem, sol, C, rhs, bonus_quadorder_a, bonus_quadorder_f)
+    Ks, b0 = assemble(problem, sol, C, rhs, bonus_quadorder_a, bonus_quadorder_f, device=device)
     op = SGOperator(sol.FES_space[0], sol.TB, Ks, device=device)
     try:
         if problem is LogTransformedPoissonProblemPrimal:

@@ -22,7 +22,7 @@ import numpy as np
 
 from . import _lib
 from .estimate import _Mesh, _Quad
-from .fem import H1Pk, assemble_rhs, assemble_stiffness, assemble_stiffness_gpu, triangle_rule
+from .fem import H1Pk, assemble_rhs_gpu, assemble_stiffness_gpu, triangle_rule
 from .modelproblems import PoissonProblemPrimal
 
 
@@ -211,11 +211,8 @@ def calculate_sampling_error(sol, C, problem=PoissonProblemPrimal, bonus_quadord
         raise ValueError("Msamples below the multi-index length")
     Vd = H1Pk(FES.mesh, order)
     qa = 2 * (order - 1) + bonus_quadorder_a
-    if len(triangle_rule(qa)[1]) <= 16:  # the GPU assembly takes cell rules of up to 16 points
-        Kd = assemble_stiffness_gpu(Vd, C, list(range(Ms + 1)), qa, device=device)
-    else:
-        Kd = assemble_stiffness(Vd, C, list(range(Ms + 1)), qa)
-    bd = assemble_rhs(Vd, rhs, order + bonus_quadorder_f)
+    Kd = assemble_stiffness_gpu(Vd, C, list(range(Ms + 1)), qa, device=device)
+    bd = assemble_rhs_gpu(Vd, rhs, order + bonus_quadorder_f, device=device)
     B = min(batch, S)
     errH1 = np.zeros((M + 1, S))
     errL2 = np.zeros((M + 1, S))

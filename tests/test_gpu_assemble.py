@@ -171,3 +171,31 @@ def test_rhs_argument_errors(built_pkg):
         pkg.assemble_pce_rhs_gpu(V, C, pkg.total_degree_multiindices(4, 1), f, 2)  # M = 4 > maxm = 3
     with pytest.raises(pkg.SGError):
         pkg.assemble_pce_rhs_gpu(V, C, [[0, 1, 0]], f, 2, factor=0.0)
+
+
+@pytest.mark.parametrize("qo", [12, 14])
+def test_gpu_assembly_with_rules_beyond_16_points(built_pkg, qo):
+    """Cell rules of 49 and 64 points (the gather runs the rule in chunks of 16):
+    K_m, the convection blocks N_m and b against the oracle's element loops."""
+    import __graft_entry__ as ge
+    from oracle import coefficient as oc
+    from oracle import fem as of
+    pkg = ge.load_package()
+    assert len(pkg.triangle_rule(qo)[1]) > 16
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.3, maxm=150)
+    Co = oc.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.3, maxm=150)
+    for order, N in ((1, 8), (2, 6)):
+        V = pkg.H1Pk(pkg.unit_square_mesh(N), order)
+        Vo = of.LagrangeSpace(of.StructuredMesh(N), order)
+        ms = list(range(5))
+        gpu = pkg.assemble_stiffness_gpu(V, C, ms, qo)
+        ref = of.assemble_stiffness(Vo, Co, ms, qo)
+        for m, A, R in zip(ms, gpu, ref):
+            assert np.abs((A - R).toarray()).max() <= 1e-13 * np.abs(R.toarray()).max(), (order, m)
+        host = pkg.assemble_convection(V, C, [1, 2, 3], qo)
+        dev = pkg.assemble_convection_gpu(V, C, [1, 2, 3], qo)
+        for A, B in zip(host, dev):
+            assert np.abs((A - B).toarray()).max() <= 1e-13 * np.abs(A.toarray()).max()
+        bg = pkg.assemble_rhs_gpu(V, lambda x, y: np.ones_like(x) + x * y, qo)
+        bo = of.assemble_rhs(Vo, lambda x, y: 1.0 + x * y, qo)
+        assert np.abs(bg - bo).max() <= 1e-14 * np.abs(bo).max()
