@@ -519,13 +519,17 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
     }
 
     Solver S{ctx, prec_kind, partials, ctx->d_scal};
-    // ||b||^2 -> host
+    // ||b||^2 and ||x0||^2 -> host in one copy (a zero warm start needs no FP64 apply)
     k_dot<double><<<g, VT, 0, ctx->stream>>>(b, b, total, partials);
     double* d_sum = partials + maxblocks + 2;
     SG_TRY(S.fin(g, FIN_SUM, FinArgs{0.0, 0}, d_sum));
-    double bb = 0.0;
-    SG_CUDA(ctx, cudaMemcpyAsync(&bb, d_sum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    k_dot<double><<<g, VT, 0, ctx->stream>>>(x64, x64, total, partials);
+    SG_LAUNCHED(ctx);
+    SG_TRY(S.fin(g, FIN_SUM, FinArgs{0.0, 0}, d_sum + 1));
+    double bbxx[2] = {0.0, 0.0};
+    SG_CUDA(ctx, cudaMemcpyAsync(bbxx, d_sum, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const double bb = bbxx[0], xx = bbxx[1];
     st->iterations = 0;
     st->outer_iterations = 0;
     st->fp64_applies = 0;
@@ -583,12 +587,6 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
     }
     {
         // initial residual: with a zero warm start r = b and no FP64 apply is needed
-        k_dot<double><<<g, VT, 0, ctx->stream>>>(x64, x64, total, partials);
-        SG_LAUNCHED(ctx);
-        SG_TRY(S.fin(g, FIN_SUM, FinArgs{0.0, 0}, d_sum));
-        double xx = 0.0;
-        SG_CUDA(ctx, cudaMemcpyAsync(&xx, d_sum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-        SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         if (xx == 0.0) {
             SG_CUDA(ctx, cudaMemcpyAsync(r, b, n64, cudaMemcpyDeviceToDevice, ctx->stream));
             rr = bb;
@@ -666,17 +664,17 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
                 SG_TRY(S.fin(g, FIN_TOL, FinArgs{want, 0}, nullptr));
                 int it = 0;
                 int s2 = SGFEM_OK;
-                if (use_small) {  // the whole FP32 PCG in one cluster launch (small.cu)
+                if (use_small) {  // the whole FP32 PCG in one cluster launch (small.cu), no host wait:
+                    // iterations and status are read with the refinement residual below
                     SG_CUDA(ctx, cudaMemsetAsync(d64, 0, n64, ctx->stream));
-                    SG_TRY(sg_small_pcg(ctx, r32, d64, remaining, &it, &s2));
-                    if (s2 == SGFEM_ERR_MAXIT) s2 = SGFEM_OK;  // the outer loop reports it
+                    SG_TRY(sg_small_pcg_launch(ctx, r32, d64, remaining));
                 } else {
                     s2 = S.pcg<float, double>(SGFEM_FP32, d64, r32, p32, q32, tmp32, remaining, check_every, &it);
+                    st->iterations += it;
+                    st->outer_iterations += 1;
+                    remaining -= it;
+                    if (s2 == SGFEM_ERR_BREAKDOWN || s2 == SGFEM_ERR_NONFINITE) { status = s2; break; }
                 }
-                st->iterations += it;
-                st->outer_iterations += 1;
-                remaining -= it;
-                if (s2 == SGFEM_ERR_BREAKDOWN || s2 == SGFEM_ERR_NONFINITE) { status = s2; break; }
                 double rec = 0.0, tr32 = 0.0;
                 if (trace >= 2) {  // recurrence ||r32|| and FP32-operator residual ||r - A32 d|| (one extra apply)
                     k_dot<float><<<g, VT, 0, ctx->stream>>>(r32, r32, total, partials);
@@ -700,6 +698,15 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
                     k_add64<<<g, VT, 0, ctx->stream>>>(x64, d64, total);
                     SG_LAUNCHED(ctx);
                     SG_TRY(true_residual(&rr));
+                }
+                if (use_small) {  // the residual's synchronisation also brought the scalars
+                    sg_small_pcg_result(ctx, &it, &s2);
+                    if (s2 == SGFEM_ERR_MAXIT) s2 = SGFEM_OK;  // the outer loop reports it
+                    st->iterations += it;
+                    st->outer_iterations += 1;
+                    remaining -= it;
+                    // a failed inner solve returned d = 0: x and r are the previous step's
+                    if (s2 == SGFEM_ERR_BREAKDOWN || s2 == SGFEM_ERR_NONFINITE) { status = s2; break; }
                 }
                 if (trace)
                     fprintf(stderr, "sgfem: refinement step %d: inner target %.3g, %d FP32 iterations, relres %.3e\n",

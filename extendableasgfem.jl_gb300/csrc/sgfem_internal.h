@@ -316,7 +316,8 @@ const char* sg_chol_log(const sgfem_context* ctx);
 int sg_small_prepare(sgfem_context* ctx, const std::vector<int64_t>& rowptr, const std::vector<int32_t>& col,
                      const std::vector<double>& val64);
 bool sg_small_usable(sgfem_context* ctx);
-int sg_small_pcg(sgfem_context* ctx, const float* r32, double* d64, int maxit, int* iters, int* status);
+int sg_small_pcg_launch(sgfem_context* ctx, const float* r32, double* d64, int maxit);
+void sg_small_pcg_result(const sgfem_context* ctx, int* iters, int* status);  // after a stream synchronisation
 const char* sg_small_log(const sgfem_context* ctx);
 void sg_small_invalidate(sgfem_context* ctx);
 void sg_small_release(sgfem_context* ctx);

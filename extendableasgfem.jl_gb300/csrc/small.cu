@@ -474,8 +474,11 @@ k_small_pcg(const int* __restrict__ rowptr, const int* __restrict__ col, const f
         bf = rho_new / rho;
         rho = rho_new;
     }
+    // a failed solve (breakdown, non-finite values) returns a zero correction, so the
+    // caller's iterate and residual stay those of the previous refinement step
+    const bool keep = status == SGFEM_OK || status == SGFEM_ERR_MAXIT;
     for (int i = threadIdx.x; i < nrow * G.ld; i += SM_THREADS)
-        x64[(size_t)row0 * G.ld + i] = (double)xh_s[i] + (double)xl_s[i];
+        x64[(size_t)row0 * G.ld + i] = keep ? (double)xh_s[i] + (double)xl_s[i] : 0.0;
     cluster.sync();  // no CTA leaves while another may still read its shared memory
     if (me == 0 && threadIdx.x == 0) {
         scal->iters = iters;
@@ -737,8 +740,10 @@ bool sg_small_usable(sgfem_context* ctx) {
 }
 
 // FP32 PCG on A d = r32 from d = 0 to ||r||^2 <= scal->tol2 (set before), d accumulated in
-// FP64 into d64 (zero on entry); iterations and status come back in scal
-int sg_small_pcg(sgfem_context* ctx, const float* r32, double* d64, int maxit, int* iters, int* status) {
+// FP64 into d64 (zero on entry; zero again if the solve fails).  The launch and the copy of
+// the scalars to the host are queued on the context's stream without a wait: the caller
+// reads iterations and status with sg_small_pcg_result after its next synchronisation.
+int sg_small_pcg_launch(sgfem_context* ctx, const float* r32, double* d64, int maxit) {
     SmallPCG* s = ctx->small;
     SmallGeom G = s->geom;
     G.ld = (int)ctx->ld;
@@ -767,12 +772,13 @@ int sg_small_pcg(sgfem_context* ctx, const float* r32, double* d64, int maxit, i
                                     ctx->d_scal, tb, G, maxit));
     ctx->launches++;
     s->launches++;
-    KrylovScalars* h = ctx->h_scal;
-    SG_CUDA(ctx, cudaMemcpyAsync(h, ctx->d_scal, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, ctx->stream));
-    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    *iters = h->iters;
-    *status = h->status;
+    SG_CUDA(ctx, cudaMemcpyAsync(ctx->h_scal, ctx->d_scal, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, ctx->stream));
     return SGFEM_OK;
+}
+
+void sg_small_pcg_result(const sgfem_context* ctx, int* iters, int* status) {
+    *iters = ctx->h_scal->iters;
+    *status = ctx->h_scal->status;
 }
 
 extern "C" const char* sgfem_small_solve_log(const sgfem_context* ctx) {
