@@ -20,7 +20,6 @@ from . import _lib
 from .fem import line_rule, triangle_rule
 from .modelproblems import LogTransformedPoissonProblemPrimal, PoissonProblemPrimal
 from .mopcontrol import add_boundary_modes, get_neighbours
-from .tensorizedbasis import coupling_matrix
 
 
 class _Mesh(ctypes.Structure):
@@ -63,8 +62,10 @@ def extension_couplings(multi_indices, basis, tail_extension=(10, 2)):
     ext = add_boundary_modes(copy.deepcopy([list(m) for m in multi_indices]), tail_extension=tail_extension)
     P_ext = len(ext)
     M_ext = len(ext[0])
-    G = coupling_matrix(basis, ext).tocsr()
     plus, minus = get_neighbours(ext)
+    # G_ext[(m-1) P_ext + j, nu] for nu = j + e_m / j - e_m is the up / down value of the
+    # one-dimensional coupling at degree ext[j][m-1] (the entry coupling_matrix stores)
+    cpl = {}
     ptr = [0]
     ms, nus, gs = [], [], []
     for j in range(P_ext):
@@ -73,11 +74,15 @@ def extension_couplings(multi_indices, basis, tail_extension=(10, 2)):
             nus.append(j)
             gs.append(1.0)
         for m in range(1, M_ext + 1):
-            for nb in (plus[m - 1][j], minus[m - 1][j]):
+            k = ext[j][m - 1]
+            if k not in cpl:
+                cpl[k] = basis.coupling(k)
+            up, down = cpl[k]
+            for nb, g in ((plus[m - 1][j], up), (minus[m - 1][j], down)):
                 if 0 < nb <= nmodes:
                     ms.append(m)
                     nus.append(nb - 1)
-                    gs.append(G[(m - 1) * P_ext + j, nb - 1])
+                    gs.append(g)
         ptr.append(len(ms))
     return ext, (np.array(ptr, dtype=np.int64), np.array(ms, dtype=np.int32), np.array(nus, dtype=np.int32),
                  np.array(gs, dtype=np.float64))

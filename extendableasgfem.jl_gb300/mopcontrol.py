@@ -154,15 +154,14 @@ def get_neighbours(mis):
         index[tuple(mi)] = k + 1  # the reference keeps the last match
     plus = [[0] * n for _ in range(M)]
     minus = [[0] * n for _ in range(M)]
+    get = index.get
     for j, mi in enumerate(mis):
+        t = tuple(mi)
         for m in range(M):
-            up = list(mi)
-            up[m] += 1
-            plus[m][j] = index.get(tuple(up), 0)
-            if mi[m] > 0:
-                dn = list(mi)
-                dn[m] -= 1
-                minus[m][j] = index.get(tuple(dn), 0)
+            head, k, tail = t[:m], t[m], t[m + 1:]
+            plus[m][j] = get(head + (k + 1,) + tail, 0)
+            if k > 0:
+                minus[m][j] = get(head + (k - 1,) + tail, 0)
     return plus, minus
 
 
