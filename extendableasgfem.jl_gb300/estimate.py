@@ -19,7 +19,7 @@ import scipy.sparse as sp
 from . import _lib
 from .fem import line_rule, triangle_rule
 from .modelproblems import LogTransformedPoissonProblemPrimal, PoissonProblemPrimal
-from .mopcontrol import add_boundary_modes, get_neighbours
+from .mopcontrol import add_boundary_modes
 
 
 class _Mesh(ctypes.Structure):
@@ -57,35 +57,63 @@ def _ptr(a):
 def extension_couplings(multi_indices, basis, tail_extension=(10, 2)):
     """Extended set and, per extended mode j, its couplings to active modes:
     (0, j, 1) if j is active, (m, nu, G_ext[(m-1)P_ext + j, nu]) for active
-    neighbours nu = j +/- e_m (estimate.jl:343-353, :385-393)."""
+    neighbours nu = j +/- e_m (estimate.jl:343-353, :385-393), in that order
+    (m ascending, the j + e_m neighbour before j - e_m).  G_ext at a neighbour is
+    the up / down value of the one-dimensional coupling at degree ext[j][m-1]
+    (the entry coupling_matrix stores); neighbours are found by mixed-radix keys
+    (the last of equal multi-indices wins, as in get_neighbours)."""
     nmodes = len(multi_indices)
     ext = add_boundary_modes(copy.deepcopy([list(m) for m in multi_indices]), tail_extension=tail_extension)
     P_ext = len(ext)
     M_ext = len(ext[0])
-    plus, minus = get_neighbours(ext)
-    # G_ext[(m-1) P_ext + j, nu] for nu = j + e_m / j - e_m is the up / down value of the
-    # one-dimensional coupling at degree ext[j][m-1] (the entry coupling_matrix stores)
-    cpl = {}
-    ptr = [0]
-    ms, nus, gs = [], [], []
-    for j in range(P_ext):
-        if j < nmodes:
-            ms.append(0)
-            nus.append(j)
-            gs.append(1.0)
-        for m in range(1, M_ext + 1):
-            k = ext[j][m - 1]
-            if k not in cpl:
-                cpl[k] = basis.coupling(k)
-            up, down = cpl[k]
-            for nb, g in ((plus[m - 1][j], up), (minus[m - 1][j], down)):
-                if 0 < nb <= nmodes:
-                    ms.append(m)
-                    nus.append(nb - 1)
-                    gs.append(g)
-        ptr.append(len(ms))
-    return ext, (np.array(ptr, dtype=np.int64), np.array(ms, dtype=np.int32), np.array(nus, dtype=np.int32),
-                 np.array(gs, dtype=np.float64))
+    A = np.asarray(ext, dtype=np.int64)                    # P_ext x M_ext degrees
+    radix = [int(r) + 2 for r in A.max(axis=0)]            # per dimension: a degree + 1 stays below it
+    w_py = [1] * M_ext
+    for d in range(M_ext - 2, -1, -1):
+        w_py[d] = w_py[d + 1] * radix[d + 1]
+    exact = w_py[0] * radix[0] < 2 ** 62
+    w = np.array(w_py, dtype=np.int64 if exact else object)  # object ints only if int64 would overflow
+    keys = (A.astype(object) if not exact else A) @ w
+    # last occurrence of each key -> its 1-based index
+    order = np.argsort(keys, kind="stable")
+    sk = keys[order]
+    last = np.r_[sk[1:] != sk[:-1], True]
+    uk, ui = sk[last], order[last] + 1
+    def lookup(q):
+        pos = np.searchsorted(uk, q)
+        pos_c = np.minimum(pos, len(uk) - 1)
+        hit = (pos < len(uk)) & (uk[pos_c] == q)
+        return np.where(hit, ui[pos_c], 0)
+    wm = np.asarray(w)[None, :]
+    plus = lookup(keys[:, None] + wm)                       # P_ext x M_ext, 1-based, 0: none
+    minus = np.where(A > 0, lookup(keys[:, None] - wm), 0)
+    maxdeg = int(A.max())
+    tab = np.array([basis.coupling(k) for k in range(maxdeg + 1)], dtype=np.float64)  # (up, down) per degree
+    up, down = tab[A, 0], tab[A, 1]
+    # per mode j: the self term, then for m = 1..M_ext the plus and the minus neighbour
+    act_self = np.arange(P_ext) < nmodes
+    valid = np.zeros((P_ext, 1 + 2 * M_ext), dtype=bool)
+    mcol = np.zeros((P_ext, 1 + 2 * M_ext), dtype=np.int32)
+    nucol = np.zeros((P_ext, 1 + 2 * M_ext), dtype=np.int64)
+    gcol = np.zeros((P_ext, 1 + 2 * M_ext), dtype=np.float64)
+    valid[:, 0] = act_self
+    nucol[:, 0] = np.arange(P_ext)
+    gcol[:, 0] = 1.0
+    mm = np.arange(1, M_ext + 1, dtype=np.int32)[None, :]
+    valid[:, 1::2] = (plus > 0) & (plus <= nmodes)
+    valid[:, 2::2] = (minus > 0) & (minus <= nmodes)
+    mcol[:, 1::2] = mm
+    mcol[:, 2::2] = mm
+    nucol[:, 1::2] = plus - 1
+    nucol[:, 2::2] = minus - 1
+    gcol[:, 1::2] = up
+    gcol[:, 2::2] = down
+    ptr = np.r_[0, np.cumsum(valid.sum(axis=1))].astype(np.int64)
+    flat = valid.ravel()
+    ms = mcol.ravel()[flat].astype(np.int32)
+    nus = nucol.ravel()[flat].astype(np.int32)
+    gs = gcol.ravel()[flat].astype(np.float64)
+    return ext, (ptr, ms, nus, gs)
 
 
 def _light_context(FES, TB, device):
