@@ -164,9 +164,15 @@ class H1Pk:
         return v, g, lap
 
     def physical_points(self, pts):
-        """(nc, nq, 2) physical coordinates of reference points."""
+        """(nc, nq, 2) physical coordinates of reference points: p0 + J xi per cell
+        (broadcast products, summed as (J_i0 xi_0 + J_i1 xi_1) before adding p0)."""
         p0 = self.mesh.coords[self.mesh.cells[:, 0]]
-        return p0[:, None, :] + np.einsum("cij,qj->cqi", self.mesh.J, pts)
+        J = self.mesh.J
+        pts = np.asarray(pts, dtype=np.float64)
+        out = np.empty((len(p0), len(pts), 2))
+        for i in range(2):
+            out[:, :, i] = p0[:, i:i + 1] + (J[:, i, 0:1] * pts[None, :, 0] + J[:, i, 1:2] * pts[None, :, 1])
+        return out
 
     def pattern(self):
         """CSR pattern of the cell connectivity and the scatter map cell-entry -> nnz."""
