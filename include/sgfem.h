@@ -123,10 +123,12 @@ SGFEM_API const char* sgfem_cholesky_log(const sgfem_context* ctx);
 /* Whether the mixed-precision solve of a finalized context runs its inner FP32 PCG
    (the iterations of solve_primal!, solvers_poisson_primal.jl:130-169, on the
    refinement residual) as ONE thread-block-cluster launch per refinement step:
-   "one-cluster FP32 PCG: ..." for small P1 problems on a power-of-two dof lattice
-   (K_0 = a0 x 5-point Laplacian, at most 32 modes and 16 KLE terms, the vectors in
-   the cluster's shared memory), else the reason it does not (then one launch per
-   phase).  SGFEM_SMALL=0 at finalize disables it. */
+   "one-cluster FP32 PCG: <CTAs> CTAs, <KB> KB shared memory each; launches: <n>"
+   for small P1 problems on a power-of-two dof lattice (K_0 = a0 x 5-point
+   Laplacian, at most 32 modes and 16 KLE terms, couplings to neighbouring lines
+   only, the vectors in the cluster's shared memory; n counts the launches so far),
+   else the reason it does not (then one launch per phase).  SGFEM_SMALL=0 at
+   finalize disables it. */
 SGFEM_API const char* sgfem_small_solve_log(const sgfem_context* ctx);
 /* Host-only (no GPU needed): the SGFEM_PREC_CHOLESKY factorisation of K_0
    (1-based CSC, n x n, boundary dofs 1-based) and both triangular solves in the
