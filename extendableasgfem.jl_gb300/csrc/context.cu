@@ -776,10 +776,7 @@ extern "C" int sgfem_finalize(sgfem_context* ctx) {
     if (!ctx->batched) SG_TRY(sg_small_prepare(ctx, rowptr, col, val64));
     if (!ctx->batched) SG_TRY(sg_apply_configure(ctx));
     if (ctx->lattice) SG_TRY(sg_lattice_configure(ctx));
-    {
-        const char* e = getenv("SGFEM_LAT_FUSE");
-        ctx->lat_fuse = e && atoi(e) != 0;
-    }
+
     // specialised FP32 apply; on failure the generic kernel stays in use (reason in the variant log)
     ctx->jit_log = ctx->batched ? "block-diagonal sample operator" : "not compiled yet (at the first FP32 apply)";
     // host copies of the pattern are no longer needed

@@ -25,8 +25,6 @@
 #include <cstdlib>
 #include <cstring>
 
-#include <type_traits>
-
 #include "sgfem_internal.h"
 
 namespace {
@@ -276,16 +274,6 @@ struct Solver {
         FinArgs fa{0.0, maxit};
         SG_TRY(sg_launch_apply(ctx, precision, p, q, partials, &nb, s));
         SG_TRY(fin(nb, FIN_ALPHA, fa));
-        if (prec_kind == SGFEM_PREC_LATTICE && ctx->lat_fuse && std::is_same<TX, double>::value) {
-            // the update inside pass X, then the rest of the preconditioner
-            int nbx = 0;
-            SG_TRY(sg_lat_pass_xu(ctx, precision, r, tmp, q, p, (double*)x, partials, &nbx, s));
-            SG_TRY(fin(nbx, FIN_RR, fa));
-            SG_TRY(sg_lat_pass_y(ctx, precision, tmp, partials, &nb, s));
-            SG_TRY(fin(nb, FIN_BETA, fa));
-            SG_TRY(sg_lat_pass_xinv(ctx, precision, tmp, p, 1, s));
-            return SGFEM_OK;
-        }
         const size_t total = (size_t)ctx->n * ctx->ld;
         const int g = vgrid(ctx);
         k_update<T, TX><<<g, VT, 0, ctx->stream>>>(x, p, r, q, total, s, partials);

@@ -482,82 +482,6 @@ k_lat_pass_x(const T* __restrict__ in, T* __restrict__ out, const T* __restrict_
     }
 }
 
-// The PCG step update fused into pass X (SGFEM_LAT_FUSE=1; one launch and one read
-// of r fewer per iteration than the separate update kernel):  x += alpha p (x in
-// FP64), r -= alpha q, block partials of ||r||^2, then T = DST_x(r) of the new r.  The
-// same arithmetic per element as the separate update; boundary rows of r, p and x
-// stay zero (the solve keeps them so), so the interior points of the interior lines
-// are all there is.  Measured slower than the separate streaming update on the P2
-// 256x256 solve (37.9 against 36.3 ms): the register loads of four streams and the
-// FP64 updates sit in front of each block's transform, where the plain pass copies
-// its line with cp.async.
-template <typename T, int LGL>
-__global__ void __launch_bounds__(LAT_THREADS)
-k_lat_pass_xu(T* __restrict__ r, T* __restrict__ out, const T* __restrict__ tab, LatGeom g, const T* __restrict__ q,
-              const T* __restrict__ p, double* __restrict__ x, double* __restrict__ partials,
-              const KrylovScalars* __restrict__ scal) {
-    if (scal->done) return;  // the partials are not read once done
-    extern __shared__ unsigned char smem_raw[];
-    T* tile = reinterpret_cast<T*>(smem_raw);
-    T* stab = tile + (size_t)g.Nl * 32;
-    __shared__ double red[LAT_WARPS];
-    const int line = 1 + blockIdx.x / g.nchunk, chunk = blockIdx.x % g.nchunk;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int m = chunk * 32 + lane;
-    const bool mv = m < g.ld;
-    const T alpha = (T)scal->alpha;
-    const double alpha_x = scal->alpha;
-    load_tab(stab, tab, g.Nl);
-    T acc_t = T(0);
-    for (int p0 = 1 + warp; p0 < g.Nl; p0 += LAT_WARPS * LAT_UNROLL) {
-        T rv[LAT_UNROLL], qv[LAT_UNROLL], pv[LAT_UNROLL];
-        double xv[LAT_UNROLL];
-#pragma unroll
-        for (int u = 0; u < LAT_UNROLL; ++u) {
-            const int pt = p0 + u * LAT_WARPS;
-            if (pt < g.Nl && mv) {
-                const size_t idx = lat_row(0, line, pt, g.Nl) * g.ld + m;
-                rv[u] = r[idx];
-                qv[u] = q[idx];
-                pv[u] = p[idx];
-                xv[u] = x[idx];
-            } else {
-                rv[u] = qv[u] = pv[u] = T(0);
-                xv[u] = 0.0;
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < LAT_UNROLL; ++u) {
-            const int pt = p0 + u * LAT_WARPS;
-            if (pt >= g.Nl) continue;
-            T rn = T(0);
-            if (mv) {
-                const size_t idx = lat_row(0, line, pt, g.Nl) * g.ld + m;
-                x[idx] = fma(alpha_x, (double)pv[u], xv[u]);
-                rn = fma(-alpha, qv[u], rv[u]);
-                r[idx] = rn;
-                acc_t = fma(rn, rn, acc_t);
-            }
-            tile[pt * 32 + lane] = rn;
-        }
-    }
-    __syncthreads();
-    dst_line<T, LGL>(tile, stab);
-    if (mv) {
-        for (int pt = 1 + warp; pt < g.Nl; pt += LAT_WARPS)
-            out[lat_row(0, line, pt, g.Nl) * g.ld + m] = tile[pt * 32 + lane];
-    }
-    double acc = (double)acc_t;
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (lane == 0) red[warp] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t2 = 0.0;
-        for (int w = 0; w < LAT_WARPS; ++w) t2 += red[w];
-        partials[blockIdx.x] = t2;
-    }
-}
-
 template <typename T, int LGL>
 __global__ void __launch_bounds__(LAT_THREADS)
 k_lat_pass_y(T* __restrict__ buf, const T* __restrict__ tab, const T* __restrict__ scale, LatGeom g,
@@ -829,24 +753,6 @@ template <typename T>
 using PassXFn = void (*)(const T*, T*, const T*, LatGeom, int, const KrylovScalars*);
 template <typename T>
 using PassYFn = void (*)(T*, const T*, const T*, LatGeom, double*, const KrylovScalars*);
-template <typename T>
-using PassXUFn = void (*)(T*, T*, const T*, LatGeom, const T*, const T*, double*, double*, const KrylovScalars*);
-
-template <typename T>
-PassXUFn<T> pass_xu_fn(int LGL) {
-    switch (LGL) {
-        case 1: return k_lat_pass_xu<T, 1>;
-        case 2: return k_lat_pass_xu<T, 2>;
-        case 3: return k_lat_pass_xu<T, 3>;
-        case 4: return k_lat_pass_xu<T, 4>;
-        case 5: return k_lat_pass_xu<T, 5>;
-        case 6: return k_lat_pass_xu<T, 6>;
-        case 7: return k_lat_pass_xu<T, 7>;
-        case 8: return k_lat_pass_xu<T, 8>;
-    }
-    return nullptr;
-}
-
 // instantiations for L = Nl/2 = 2^LGL complex points, Nl = 4 .. 512
 template <typename T>
 PassXFn<T> pass_x_fn(int LGL) {
@@ -904,21 +810,6 @@ int launch_x(sgfem_context* ctx, const void* in, void* out, const T* tab, int mo
 }
 
 template <typename T>
-int launch_xu(sgfem_context* ctx, void* r, void* out, const T* tab, const void* q, const void* p, double* x,
-              double* partials, int* nblocks, const KrylovScalars* scal) {
-    LatGeom g = geom(ctx);
-    g.async = 0;
-    PassXUFn<T> fn = pass_xu_fn<T>(ctx->lat_log2 - 1);
-    if (!fn) return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "lattice size outside the compiled range");
-    const int grid = (g.Nl - 1) * g.nchunk;
-    if (nblocks) *nblocks = grid;
-    fn<<<grid, LAT_THREADS, lat_smem(ctx, sizeof(T)), ctx->stream>>>((T*)r, (T*)out, tab, g, (const T*)q, (const T*)p, x,
-                                                                     partials, scal);
-    SG_LAUNCHED(ctx);
-    return SGFEM_OK;
-}
-
-template <typename T>
 int launch_y(sgfem_context* ctx, void* buf, const T* tab, const T* scale, double* rz, int* nblocks,
              const KrylovScalars* scal) {
     LatGeom g = geom(ctx);
@@ -943,8 +834,6 @@ int sg_lattice_configure(sgfem_context* ctx) {
     SG_TRY(set_smem(ctx, pass_y_fn<float>(LGL), lat_smem(ctx, 4)));
     SG_TRY(set_smem(ctx, pass_yb_fn<double>(LGL), lat_smem(ctx, 8)));
     SG_TRY(set_smem(ctx, pass_yb_fn<float>(LGL), lat_smem(ctx, 4)));
-    SG_TRY(set_smem(ctx, pass_xu_fn<double>(LGL), lat_smem(ctx, 8)));
-    SG_TRY(set_smem(ctx, pass_xu_fn<float>(LGL), lat_smem(ctx, 4)));
     return SGFEM_OK;
 }
 
@@ -956,13 +845,6 @@ int sg_lat_max_blocks(const sgfem_context* ctx) {
 int sg_lat_pass_x(sgfem_context* ctx, int precision, const void* R, void* T, const KrylovScalars* scal) {
     if (precision == SGFEM_FP64) return launch_x<double>(ctx, R, T, ctx->d_lat_tab64, 0, scal);
     return launch_x<float>(ctx, R, T, ctx->d_lat_tab32, 0, scal);
-}
-
-int sg_lat_pass_xu(sgfem_context* ctx, int precision, void* r, void* T, const void* q, const void* p, double* x,
-                   double* partials, int* nblocks, const KrylovScalars* scal) {
-    if (precision == SGFEM_FP64)
-        return launch_xu<double>(ctx, r, T, ctx->d_lat_tab64, q, p, x, partials, nblocks, scal);
-    return launch_xu<float>(ctx, r, T, ctx->d_lat_tab32, q, p, x, partials, nblocks, scal);
 }
 
 int sg_lat_pass_y(sgfem_context* ctx, int precision, void* T, double* rz, int* nblocks, const KrylovScalars* scal) {

@@ -176,7 +176,6 @@ struct sgfem_context {
     double* d_lat_scale64 = nullptr;  // per (kx, ky) scale, (Nl-1)^2
     float* d_lat_scale32 = nullptr;
     bool lat_block = false;         // exact K_0^-1 by 4x4 blocks of the sine transform (pass Y)
-    bool lat_fuse = false;          // PCG step update inside pass X (SGFEM_LAT_FUSE=1; measured slower)
     double* d_lat_blk64 = nullptr;  // per (kx, ky) in [1, Nl/2]^2: 10 values of a symmetric 4x4 block
     float* d_lat_blk32 = nullptr;
     std::string lat_log;            // which mean-based preconditioner is in use, and why
@@ -287,9 +286,6 @@ int sg_lattice_blocks(sgfem_context* ctx, const std::vector<int64_t>& rowptr, co
 int sg_lat_pass_x(sgfem_context* ctx, int precision, const void* R, void* T,
                   const KrylovScalars* skip_if_done);
 // pass 2: T <- DST_y(scale .* DST_y(T)); rz partials (Parseval) if rz != nullptr
-// x += alpha p, r -= alpha q, partials of ||r||^2, then pass X of the new r (x in FP64)
-int sg_lat_pass_xu(sgfem_context* ctx, int precision, void* r, void* T, const void* q, const void* p, double* x,
-                   double* partials, int* nblocks, const KrylovScalars* scal);
 int sg_lat_pass_y(sgfem_context* ctx, int precision, void* T, double* rz, int* nblocks,
                   const KrylovScalars* skip_if_done);
 // pass 3: z = DST_x(T); mode 0: out = z (boundary rows untouched), mode 1: out = z + beta*out

@@ -177,29 +177,3 @@ def test_mixed_residual_certificate(built_pkg, monkeypatch, order, N):
     for rtol in (1e-8, 1e-11):
         assert rel(out[("default", rtol)], out[("fp64", rtol)]) <= 1e3 * rtol
 
-
-@pytest.mark.parametrize("precision", ["FP64", "MIXED"])
-def test_fused_lattice_update_matches_separate_kernel(built_pkg, monkeypatch, precision):
-    """The PCG step update fused into the sine-transform pass X (SGFEM_LAT_FUSE=1:
-    x += alpha p, r -= alpha q and ||r||^2 in the pass that reads r) and the
-    separate update kernel (the default) take the same iterations, reach rtol on
-    the host FP64 residual, and agree with the oracle's solution."""
-    import __graft_entry__ as ge
-    pkg = ge.load_package()
-    p = build(32, 2, 4, pkg.total_degree_multiindices(4, 2))  # P2 lattice: not the one-cluster path
-    prec = getattr(pkg, precision)
-    b = osg.reference_rhs(np.zeros(p.n * p.P), p.b0, p.bdofs, p.P)
-    out = {}
-    for fuse in ("1", "0"):
-        monkeypatch.setenv("SGFEM_LAT_FUSE", fuse)
-        op = pkg.SGOperator(p.V, p.TB, p.Kall, device=0)
-        assert op.has_lattice
-        x = np.zeros(p.n * p.P)
-        st = op.solve_primal(p.b0, x, rtol=1e-10, precision=prec)
-        op.close()
-        r = b - osg.apply_fast(x, p.K0, p.Ks, p.G, p.bdofs, p.P)
-        assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(b), (fuse, st)
-        out[fuse] = (x, st)
-    assert abs(out["1"][1]["iterations"] - out["0"][1]["iterations"]) <= 1
-    assert rel(out["1"][0], out["0"][0]) <= 1e-8
-    assert rel(out["1"][0], oracle_solution(p)) <= 1e-8
