@@ -56,7 +56,7 @@ def build(verbose=False, ptxas_verbose=False, force=False):
         old = None
     if old != stamp:
         force = True
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(HERE, "..", "include", "sgfem.h"))
     objs = []
     jobs = []
