@@ -202,6 +202,11 @@ __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict_
         }
         const int nz0 = d.rowptr[row], nz1 = d.rowptr[row + 1];
         for (int base = 0; base < d.Qn; base += QT * 32) {
+            // the pass's pairs are ordered by column: only columns [c0, c1) of each X row
+            // are staged (su[c - c0]); padding lanes read su[0] with a zero value
+            const int c0 = d.qtab[base] & 0xffff;
+            const int c1 = (d.qtab[min(base + QT * 32, d.Qn) - 1] & 0xffff) + 1;
+            const int nc = c1 - c0;
             int om[QT], on[QT];
             T acc[QT];
 #pragma unroll
@@ -210,7 +215,7 @@ __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict_
                 if (q < d.Qn) {
                     const int e = d.qtab[q];
                     om[t] = e >> 16;
-                    on[t] = e & 0xffff;
+                    on[t] = (e & 0xffff) - c0;
                 } else {
                     om[t] = d.M1;
                     on[t] = 0;
@@ -220,11 +225,12 @@ __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict_
             if constexpr (PF) {
                 T xr[BPC], vr[BPV];
                 auto fetch = [&](int nz) {
-                    const T* xs = Xp + (size_t)d.col[nz] * d.ld;
+                    const T* xs = Xp + (size_t)d.col[nz] * d.ld + c0;
 #pragma unroll
                     for (int u = 0; u < BPC; ++u) {
+                        if (32 * u >= nc) break;
                         const int c = lane + 32 * u;
-                        xr[u] = c < d.ld ? __ldg(xs + c) : T(0);
+                        xr[u] = c < nc ? __ldg(xs + c) : T(0);
                     }
 #pragma unroll
                     for (int u = 0; u < BPV; ++u) {
@@ -236,8 +242,10 @@ __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict_
                 for (int nz = nz0; nz < nz1; ++nz) {
                     __syncwarp();  // the previous nonzero's FMAs have read su and sc
 #pragma unroll
-                    for (int u = 0; u < BPC; ++u)
-                        if (lane + 32 * u < d.ld) su[lane + 32 * u] = xr[u];
+                    for (int u = 0; u < BPC; ++u) {
+                        if (32 * u >= nc) break;
+                        if (lane + 32 * u < nc) su[lane + 32 * u] = xr[u];
+                    }
 #pragma unroll
                     for (int u = 0; u < BPV; ++u)
                         if (lane + 32 * u < d.M1) sc[lane + 32 * u] = vr[u];
@@ -250,8 +258,8 @@ __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict_
             } else {
                 for (int nz = nz0; nz < nz1; ++nz) {
                     const int j = d.col[nz];
-                    const T* xs = Xp + (size_t)j * d.ld;
-                    for (int c = lane; c < d.ld; c += 32) su[c] = __ldg(xs + c);
+                    const T* xs = Xp + (size_t)j * d.ld + c0;
+                    for (int c = lane; c < nc; c += 32) su[c] = __ldg(xs + c);
                     for (int m = lane; m < d.M1; m += 32) sc[m] = vals[(size_t)nz * d.M1 + m];
                     __syncwarp();
 #pragma unroll
@@ -270,10 +278,8 @@ __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict_
         T rowdot = T(0);  // per-row products in the working precision, rows summed in FP64
         for (int mu = lane; mu < d.ld; mu += 32) {
             T y = T(0);
-            if (mu < d.P) {
-                y = sacc[mu];
+            if (mu < d.P)  // the first entry is the mode's K_0 pair with g = 1
                 for (int e = d.combptr[mu]; e < d.combptr[mu + 1]; ++e) y = fma(combg[e], sacc[d.combq[e]], y);
-            }
             yrow[mu] = y;
             rowdot = fma(xrow[mu], y, rowdot);
         }
@@ -815,23 +821,28 @@ extern "C" int sgfem_batch_add(sgfem_batch* b, int64_t n, int64_t M, int64_t P, 
             nzc[m][nu] = 1;
             ges.push_back({m, mu, (int)nu, Gval[k]});
         }
+    // pairs ordered by column nu, then term m: a pass of the apply over consecutive
+    // pairs reads a narrow column range of each X row
     std::vector<int> qidx((size_t)h.M1 * P, -1);
-    for (int nu = 0; nu < P; ++nu) {
-        qidx[nu] = (int)h.qtab.size();
-        h.qtab.push_back(nu);
-    }
-    for (int m = 1; m < h.M1; ++m)
-        for (int nu = 0; nu < P; ++nu)
-            if (nzc[m][nu]) {
+    for (int nu = 0; nu < P; ++nu)
+        for (int m = 0; m < h.M1; ++m)
+            if (m == 0 || nzc[m][nu]) {
                 qidx[(size_t)m * P + nu] = (int)h.qtab.size();
                 h.qtab.push_back((m << 16) | nu);
             }
+    // per output mode mu: its K_0 pair with g = 1 first, then the G entries in their order
     h.combptr.assign(P + 1, 0);
     std::stable_sort(ges.begin(), ges.end(), [](const GE& x, const GE& y) { return x.mu < y.mu; });
-    for (auto& e : ges) {
-        h.combptr[e.mu + 1]++;
-        h.combq.push_back(qidx[(size_t)e.m * P + e.nu]);
-        h.combg.push_back(e.g);
+    size_t e0 = 0;
+    for (int mu = 0; mu < P; ++mu) {
+        h.combptr[mu + 1]++;
+        h.combq.push_back(qidx[mu]);
+        h.combg.push_back(1.0);
+        for (; e0 < ges.size() && ges[e0].mu == mu; ++e0) {
+            h.combptr[mu + 1]++;
+            h.combq.push_back(qidx[(size_t)ges[e0].m * P + ges[e0].nu]);
+            h.combg.push_back(ges[e0].g);
+        }
     }
     for (int mu = 0; mu < P; ++mu) h.combptr[mu + 1] += h.combptr[mu];
     h.b0.assign(b0, b0 + n);
