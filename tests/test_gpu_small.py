@@ -122,3 +122,30 @@ def test_small_not_used_where_it_does_not_apply(built_pkg):
     op = pkg.SGOperator(large.V, large.TB, large.Kall, device=0)
     assert "no cluster shape fits" in op.ctx.small_solve_log
     op.close()
+
+
+def test_small_reports_breakdown_like_the_multi_launch_path(built_pkg, monkeypatch):
+    """An indefinite SG operator (mean 0.05 against KLE amplitudes summing to ~1.3;
+    the oracle's PCG meets p'Ap < 0 at its second iteration): the one-cluster inner
+    PCG returns SGFEM_ERR_BREAKDOWN (with a zero correction) like the multi-launch
+    FP32 PCG, through the same error of sgfem_solve."""
+    import sys
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    lib = sys.modules[pkg.__name__ + "._lib"]
+    ERR_BREAKDOWN, SGError = lib.ERR_BREAKDOWN, lib.SGError
+    p = build(32, 1, 5, pkg.total_degree_multiindices(5, 2), mean=0.05)
+    codes = {}
+    for small in ("1", "0"):
+        monkeypatch.setenv("SGFEM_SMALL", small)
+        op = pkg.SGOperator(p.V, p.TB, p.Kall, device=0)
+        assert ("one-cluster" in op.ctx.small_solve_log) == (small == "1"), op.ctx.small_solve_log
+        x = np.zeros(p.n * p.P)
+        with pytest.raises(SGError) as e:
+            op.solve_primal(p.b0, x, rtol=1e-8, precision=pkg.MIXED)
+        codes[small] = e.value.code
+        if small == "1":
+            assert launches(op) == 1
+        assert np.all(np.isfinite(x))
+        op.close()
+    assert codes["1"] == codes["0"] == ERR_BREAKDOWN, codes
