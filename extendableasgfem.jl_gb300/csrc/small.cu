@@ -199,6 +199,55 @@ __device__ __forceinline__ float apply_rows(const int* __restrict__ cj_s, const 
     return part;
 }
 
+// the same for any M1 <= SM_MAXM1 at run time (the term loops run to SM_MAXM1 behind a
+// warp-uniform guard): one code body for the counts above those specialised
+__device__ __forceinline__ float apply_rows_any(const int* __restrict__ cj_s, const float* __restrict__ kv_s,
+                                                const float* __restrict__ pe_s, const float* __restrict__ p_s,
+                                                float* __restrict__ q_s, const int2* __restrict__ cg_s, int nsl,
+                                                int nrow, int warp, int lane, const SmallGeom& G) {
+    const int M1 = G.M1, KS = G.KS;
+    const bool lv = lane < G.ld;
+    float part = 0.f;
+    for (int li = warp; li < nrow; li += SM_WARPS) {
+        float qv = 0.f;
+        const int* cr = cj_s + li * G.TMAX;
+        const float pi_ = p_s[li * 32 + lane];
+        if (cr[0] >= 0) {  // warp-uniform: not a boundary row
+            float w[SM_MAXM1];
+#pragma unroll
+            for (int m = 0; m < SM_MAXM1; ++m) w[m] = 0.f;
+            const float* kv = kv_s + (size_t)li * G.TMAX * KS;
+            for (int t = 0; t < G.TMAX; ++t) {
+                const float pj = pe_s[cr[t] * 32 + lane];
+                const float u = G.diff ? pj - pi_ : pj;
+#pragma unroll
+                for (int m = 0; m < SM_MAXM1; m += 2) {
+                    if (m < M1) {  // KS is even and the staged values are zero beyond M1
+                        const float2 v = *reinterpret_cast<const float2*>(kv + t * KS + m);
+                        w[m] = fmaf(v.x, u, w[m]);
+                        w[m + 1] = fmaf(v.y, u, w[m + 1]);
+                    }
+                }
+            }
+            qv = w[0];
+            for (int sl = 0; sl < nsl; ++sl) {
+#pragma unroll
+                for (int m = 1; m < SM_MAXM1; ++m) {
+                    if (m < M1) {
+                        const int2 e = cg_s[(sl * M1 + m) * 32 + lane];
+                        const float v = __shfl_sync(0xffffffffu, w[m], e.x);
+                        qv = fmaf(__int_as_float(e.y), v, qv);
+                    }
+                }
+            }
+            if (!lv) qv = 0.f;
+        }
+        q_s[li * 32 + lane] = qv;
+        part = fmaf(pi_, qv, part);
+    }
+    return part;
+}
+
 __global__ void __launch_bounds__(SM_THREADS, 1)
 k_small_pcg(const int* __restrict__ rowptr, const int* __restrict__ col, const float* __restrict__ vals,
             const unsigned char* __restrict__ bmask, const float* __restrict__ rin, double* __restrict__ x64,
@@ -414,9 +463,8 @@ k_small_pcg(const int* __restrict__ rowptr, const int* __restrict__ col, const f
 #define SM_APPLY(k) \
     case k: return apply_rows<k>(cj_s, kv_s, pe_s, p_s, q_s, cg_s, nsl, nrow, warp, lane, G);
             SM_APPLY(1) SM_APPLY(2) SM_APPLY(3) SM_APPLY(4) SM_APPLY(5) SM_APPLY(6) SM_APPLY(7) SM_APPLY(8)
-            SM_APPLY(9) SM_APPLY(10) SM_APPLY(11) SM_APPLY(12) SM_APPLY(13) SM_APPLY(14) SM_APPLY(15) SM_APPLY(16)
 #undef SM_APPLY
-            default: return 0.f;
+            default: return apply_rows_any(cj_s, kv_s, pe_s, p_s, q_s, cg_s, nsl, nrow, warp, lane, G);
         }
     };
 

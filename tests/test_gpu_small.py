@@ -66,11 +66,13 @@ def test_small_mixed_solve_config1(built_pkg, monkeypatch, rtol):
     op_ml.close()
 
 
-@pytest.mark.parametrize("N,M,deg,cl", [(16, 3, 2, None), (32, 4, 2, "8"), (8, 6, 1, None), (32, 5, 2, "8")])
+@pytest.mark.parametrize("N,M,deg,cl", [(16, 3, 2, None), (32, 4, 2, "8"), (8, 6, 1, None), (32, 5, 2, "8"),
+                                         (16, 10, 1, None)])
 def test_small_other_shapes_and_update(built_pkg, monkeypatch, N, M, deg, cl):
-    """Other lattice sizes (cluster shares of 0 to 5 lines), term counts, both
-    cluster sizes (16 CTAs, and the portable 8), and a coupling update (new
-    tables for the grown multi-index set)."""
+    """Other lattice sizes (cluster shares of 0 to 5 lines), term counts (4 to 7
+    with the specialised applies, 11 with the run-time one), both cluster sizes
+    (16 CTAs, and the portable 8), and a coupling update (new tables for the
+    grown multi-index set)."""
     import __graft_entry__ as ge
     pkg = ge.load_package()
     if cl:
