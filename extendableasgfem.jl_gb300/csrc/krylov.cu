@@ -13,9 +13,9 @@
 //   z = B r (three lattice passes, r'z by Parseval) -> finalize: beta
 //   p = z + beta p (fused into the last preconditioner pass)
 // Reductions are per-block FP64 partials summed by one block in a fixed
-// order, so results are bitwise reproducible run to run.  A batch of
-// iterations is captured once in a CUDA graph and replayed; kernels return
-// immediately once the convergence flag is set.
+// order, so results are bitwise reproducible run to run.  The iterations run
+// as a device-side loop (a CUDA graph conditional WHILE node) that stops when
+// the convergence flag is set; kernels return immediately once it is.
 // SGFEM_MIXED: FP64 x, b and true residual r = b - A x; each refinement step
 // solves A d = r with FP32 PCG (FP32 operator values, vectors and
 // accumulation; FP64 inner products) to inner_rtol and adds d to x in FP64.
@@ -36,30 +36,12 @@ enum FinMode { FIN_ALPHA = 0, FIN_RR = 1, FIN_BETA = 2, FIN_TOL = 3, FIN_SUM = 4
 struct FinArgs {
     double rtol2;  // FIN_TOL: tol2 = rtol2 * sum
     int maxit;
+    int loop;      // 1: last finalize of a device-loop body, sets the loop condition
+    cudaGraphConditionalHandle handle;
 };
 
-__global__ void k_finalize(const double* __restrict__ partials, int nb, KrylovScalars* __restrict__ s, int mode,
-                           FinArgs fa, double* __restrict__ out_sum) {
-    __shared__ double red[VT];
-    double v = 0.0;
-    for (int i = threadIdx.x; i < nb; i += VT) v += partials[i];
-    red[threadIdx.x] = v;
-    __syncthreads();
-    for (int w = VT / 2; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-        __syncthreads();
-    }
-    if (threadIdx.x != 0) return;
-    const double sum = red[0];
-    if (mode == FIN_SUM) {
-        *out_sum = sum;
-        return;
-    }
-    if (mode == FIN_TOL) {
-        s->tol2 = fa.rtol2 * sum;
-        if (out_sum) *out_sum = sum;
-        return;
-    }
+// one finalize step of the PCG scalars; sticky done flag
+__device__ void fin_step(KrylovScalars* s, int mode, double sum) {
     if (s->done) return;
     if (mode == FIN_ALPHA) {
         s->pq = sum;
@@ -83,6 +65,46 @@ __global__ void k_finalize(const double* __restrict__ partials, int nb, KrylovSc
         }
         s->rho = sum;
     }
+}
+
+__global__ void k_finalize(const double* __restrict__ partials, int nb, KrylovScalars* __restrict__ s, int mode,
+                           FinArgs fa, double* __restrict__ out_sum) {
+    __shared__ double red[VT];
+    double v = 0.0;
+    for (int i = threadIdx.x; i < nb; i += VT) v += partials[i];
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = VT / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    const double sum = red[0];
+    if (mode == FIN_SUM) {
+        *out_sum = sum;
+        return;
+    }
+    if (mode == FIN_TOL) {
+        s->tol2 = fa.rtol2 * sum;
+        if (out_sum) *out_sum = sum;
+        return;
+    }
+    fin_step(s, mode, sum);
+    if (fa.loop) {
+        // the device loop runs another body while the solve goes on; the body count
+        // is capped at maxit + 1 (every body not stopped by the flag is an iteration)
+        const int bodies = ++s->loops;
+        cudaGraphSetConditional(fa.handle, (!s->done && bodies <= s->maxit + 1) ? 1u : 0u);
+    }
+}
+
+// scalars of a new PCG run: everything zero but tol2 (set by the caller)
+__global__ void k_pcg_reset(KrylovScalars* s, int maxit) {
+    const double tol2 = s->tol2;
+    *s = KrylovScalars{};
+    s->tol2 = tol2;
+    s->first = 1;
+    s->maxit = maxit;
 }
 
 __device__ __forceinline__ void block_partial(double acc, double* partials) {
@@ -238,7 +260,14 @@ struct Solver {
     double* partials;
     KrylovScalars* s;
 
-    int fin(int nb, int mode, FinArgs fa = FinArgs{0.0, 0}, double* out = nullptr) {
+    int loop = 0;  // set while the last iteration of a device-loop body is captured
+    cudaGraphConditionalHandle loop_handle = 0;
+
+    int fin(int nb, int mode, FinArgs fa = FinArgs{0.0, 0, 0, 0}, double* out = nullptr) {
+        if (mode == FIN_BETA && loop) {
+            fa.loop = 1;
+            fa.handle = loop_handle;
+        }
         k_finalize<<<1, VT, 0, ctx->stream>>>(partials, nb, s, mode, fa, out);
         SG_LAUNCHED(ctx);
         return SGFEM_OK;
@@ -248,7 +277,7 @@ struct Solver {
     template <typename T>
     int precond_block(int precision, T* r, T* p, T* tmp, int maxit) {
         int nb = 0;
-        FinArgs fa{0.0, maxit};
+        FinArgs fa{0.0, maxit, 0, 0};
         if (prec_kind == SGFEM_PREC_LATTICE) {
             SG_TRY(sg_lat_pass_x(ctx, precision, r, tmp, s));
             SG_TRY(sg_lat_pass_y(ctx, precision, tmp, partials, &nb, s));
@@ -271,7 +300,7 @@ struct Solver {
     template <typename T, typename TX = T>
     int iteration(int precision, TX* x, T* r, T* p, T* q, T* tmp, int maxit) {
         int nb = 0;
-        FinArgs fa{0.0, maxit};
+        FinArgs fa{0.0, maxit, 0, 0};
         SG_TRY(sg_launch_apply(ctx, precision, p, q, partials, &nb, s));
         SG_TRY(fin(nb, FIN_ALPHA, fa));
         const size_t total = (size_t)ctx->n * ctx->ld;
@@ -285,33 +314,26 @@ struct Solver {
 
     // PCG on A x = b given r = b - A x on entry, stopping when ||r||^2 <= s->tol2
     // (set by the caller).  Returns the status; iterations in *iters.
+    // The iterations run as one CUDA graph launch: a conditional WHILE node whose
+    // body is check_every iterations; the last FIN_BETA finalize of the body clears
+    // the loop condition once the done flag is set, so the convergence test costs
+    // no host round trip and at most check_every - 1 iterations of early returns.
     template <typename T, typename TX = T>
     int pcg(int precision, TX* x, T* r, T* p, T* q, T* tmp, int maxit, int check_every, int* iters) {
         const size_t vb = (size_t)ctx->n * ctx->ld * sizeof(T);
         SG_CUDA(ctx, cudaMemsetAsync(p, 0, vb, ctx->stream));
-        // initial residual norm and flags
-        {
-            // reset everything except tol2
-            KrylovScalars* h = ctx->h_scal;
-            SG_CUDA(ctx, cudaMemcpyAsync(h, s, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, ctx->stream));
-            SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-            double tol2 = h->tol2;
-            std::memset(h, 0, sizeof(KrylovScalars));
-            h->tol2 = tol2;
-            h->first = 1;
-            h->maxit = maxit;
-            SG_CUDA(ctx, cudaMemcpyAsync(s, h, sizeof(KrylovScalars), cudaMemcpyHostToDevice, ctx->stream));
-        }
+        k_pcg_reset<<<1, 1, 0, ctx->stream>>>(s, maxit);
+        SG_LAUNCHED(ctx);
         const size_t total = (size_t)ctx->n * ctx->ld;
         const int g = vgrid(ctx);
         k_dot<T><<<g, VT, 0, ctx->stream>>>(r, r, total, partials);
         SG_LAUNCHED(ctx);
-        SG_TRY(fin(g, FIN_RR, FinArgs{0.0, maxit}));
+        SG_TRY(fin(g, FIN_RR, FinArgs{0.0, maxit, 0, 0}));
         SG_TRY(precond_block<T>(precision, r, p, tmp, maxit));
 
-        // the graph of check_every iterations depends only on the buffers, the kernel
-        // choice and the block counts (the iteration cap lives in the device scalars), so
-        // the instantiated graph of the previous run on the same buffers is replayed
+        // the graph depends only on the buffers, the kernel choice and the block
+        // counts (the iteration cap lives in the device scalars), so the instantiated
+        // graph of the previous run on the same buffers is replayed
         const uint64_t key[12] = {(uint64_t)precision, (uint64_t)sizeof(T), (uint64_t)sizeof(TX), (uint64_t)(uintptr_t)x,
                                   (uint64_t)(uintptr_t)r, (uint64_t)(uintptr_t)p, (uint64_t)(uintptr_t)q,
                                   (uint64_t)(uintptr_t)tmp, (uint64_t)check_every, (uint64_t)prec_kind,
@@ -322,19 +344,39 @@ struct Solver {
             ctx->pcg_exec = nullptr;
             ctx->pcg_graph = nullptr;
             cudaGraph_t graph = nullptr;
-            SG_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            SG_CUDA(ctx, cudaGraphCreate(&graph, 0));
+            cudaGraphConditionalHandle h = 0;
+            cudaError_t ce = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+            cudaGraphNodeParams np{};
+            np.type = cudaGraphNodeTypeConditional;
+            np.conditional.handle = h;
+            np.conditional.type = cudaGraphCondTypeWhile;
+            np.conditional.size = 1;
+            cudaGraphNode_t node = nullptr;
+            if (ce == cudaSuccess) ce = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np);
+            cudaGraph_t body = ce == cudaSuccess ? np.conditional.phGraph_out[0] : nullptr;
+            if (ce == cudaSuccess)
+                ce = cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0,
+                                                   cudaStreamCaptureModeThreadLocal);
+            if (ce != cudaSuccess) {
+                cudaGraphDestroy(graph);
+                return sg_cuda_fail(ctx, ce, "PCG device loop");
+            }
             int st = SGFEM_OK;
             const long long before = ctx->launches;
-            for (int k = 0; k < check_every && st == SGFEM_OK; ++k)
+            loop_handle = h;
+            for (int k = 0; k < check_every && st == SGFEM_OK; ++k) {
+                loop = k == check_every - 1;
                 st = iteration<T, TX>(precision, x, r, p, q, tmp, maxit);
-            const long long per_graph = ctx->launches - before;  // kernel nodes per replay
-            ctx->launches = before;
-            cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
-            if (st != SGFEM_OK) {
-                if (graph) cudaGraphDestroy(graph);
-                return st;
             }
-            SG_CUDA(ctx, ce);
+            loop = 0;
+            const long long per_body = ctx->launches - before;  // kernel nodes per loop body
+            ctx->launches = before;
+            ce = cudaStreamEndCapture(ctx->stream, &body);
+            if (st != SGFEM_OK || ce != cudaSuccess) {
+                cudaGraphDestroy(graph);
+                return st != SGFEM_OK ? st : sg_cuda_fail(ctx, ce, "PCG device loop capture");
+            }
             cudaGraphExec_t ex = nullptr;
             cudaError_t ie = cudaGraphInstantiate(&ex, graph, 0);
             if (ie != cudaSuccess) {
@@ -343,25 +385,18 @@ struct Solver {
             }
             ctx->pcg_graph = graph;
             ctx->pcg_exec = ex;
-            ctx->pcg_per_graph = per_graph;
+            ctx->pcg_per_graph = per_body;
             std::memcpy(ctx->pcg_key, key, sizeof(key));
         }
-        cudaGraphExec_t exec = ctx->pcg_exec;
-        const long long per_graph = ctx->pcg_per_graph;
-        int status = SGFEM_OK;
-        for (;;) {
-            SG_CUDA(ctx, cudaMemcpyAsync(ctx->h_scal, s, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, ctx->stream));
-            SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-            if (ctx->h_scal->done) {
-                status = ctx->h_scal->status;
-                break;
-            }
-            cudaError_t le = cudaGraphLaunch(exec, ctx->stream);
-            ctx->launches += per_graph;
-            if (le != cudaSuccess) return sg_cuda_fail(ctx, le, "cudaGraphLaunch");
-        }
-        *iters = ctx->h_scal->iters;
-        return status;
+        cudaError_t le = cudaGraphLaunch(ctx->pcg_exec, ctx->stream);
+        if (le != cudaSuccess) return sg_cuda_fail(ctx, le, "cudaGraphLaunch");
+        SG_CUDA(ctx, cudaMemcpyAsync(ctx->h_scal, s, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, ctx->stream));
+        SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        const KrylovScalars* hs = ctx->h_scal;
+        ctx->launches += ctx->pcg_per_graph * hs->loops;
+        *iters = hs->iters;
+        if (!hs->done) return sg_fail(ctx, SGFEM_ERR_MAXIT, "PCG device loop ended before the done flag");
+        return hs->status;
     }
 };
 
@@ -382,7 +417,7 @@ extern "C" void sgfem_default_options(sgfem_solve_options* o) {
     o->maxit = 2000;
     o->inner_rtol = 1e-4;  // measured best on the P2 256x256 workload
     o->reference_rhs = 1;
-    o->check_every = 8;
+    o->check_every = 4;  // device-loop body length: measured best on the P2 256x256 and sampling workloads
 }
 
 extern "C" int sgfem_precondition(sgfem_context* ctx, const double* b, double* y, int kind, int precision) {

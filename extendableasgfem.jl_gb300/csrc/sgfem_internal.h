@@ -42,7 +42,7 @@ struct KrylovScalars {
     int iters;       // iterations completed
     int first;       // 1 before the first preconditioner application (beta = 0)
     int maxit;       // iteration cap of the current PCG run
-    int pad_;
+    int loops;       // device-loop bodies run by the current PCG run
 };
 
 struct DeviceBuf {
@@ -188,11 +188,12 @@ struct sgfem_context {
     DeviceBuf w_partials;      // per-block reduction partials (double)
     DeviceBuf w_basis;         // GMRES Krylov basis (restart + 1 vectors)
     DeviceBuf w_zbasis;        // flexible GMRES: preconditioned basis vectors (restart, FP32)
-    // PCG graph of check_every iterations, kept for the next run on the same buffers
+    // PCG graph (a device loop of check_every iterations per body), kept for the next
+    // run on the same buffers
     cudaGraph_t pcg_graph = nullptr;
     cudaGraphExec_t pcg_exec = nullptr;
     uint64_t pcg_key[12] = {};
-    long long pcg_per_graph = 0;
+    long long pcg_per_graph = 0;  // kernel launches per loop body
     DeviceBuf w_gsmall;        // GMRES multi-dot partials and coefficients
     KrylovScalars* d_scal = nullptr;
     KrylovScalars* h_scal = nullptr;  // pinned

@@ -94,7 +94,7 @@ class SGOperator:
         return self.ctx.precondition(b, kind, precision)
 
     def solve_primal(self, b0, x, rtol=1e-12, precision=_lib.MIXED, preconditioner=None, maxit=5000,
-                     inner_rtol=1e-4, reference_rhs=True, check_every=8, allow_maxit=False):
+                     inner_rtol=1e-4, reference_rhs=True, check_every=4, allow_maxit=False):
         """solve_primal!: x (SGFEVector.entries) is the warm start and receives the solution."""
         if preconditioner is None:
             preconditioner = self.mean_preconditioner

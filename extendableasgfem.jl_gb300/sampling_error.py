@@ -118,12 +118,12 @@ class SampleProblems:
             raise ValueError("batch shape differs")
         self.ctx.set_samples(samples)
 
-    def options(self, rtol=1e-10, precision=_lib.MIXED, maxit=5000, check_every=8):
+    def options(self, rtol=1e-10, precision=_lib.MIXED, maxit=5000, check_every=4):
         prec = _lib.PREC_LATTICE if self.ctx.has_lattice else _lib.PREC_CHOLESKY
         return self.ctx.default_options(precision=precision, preconditioner=prec, rtol=rtol, maxit=maxit,
                                         reference_rhs=0, check_every=check_every)
 
-    def solve(self, b0, rtol=1e-10, precision=_lib.MIXED, maxit=5000, check_every=8, keep_on_device=False):
+    def solve(self, b0, rtol=1e-10, precision=_lib.MIXED, maxit=5000, check_every=4, keep_on_device=False):
         """Solutions as an (n, S) array (None with keep_on_device: they stay in the
         context for sampling_error)."""
         o = self.options(rtol, precision, maxit, check_every)

@@ -62,7 +62,10 @@ typedef struct {
     double inner_rtol;  /* MIXED: relative reduction asked of each FP32 inner solve */
     int reference_rhs;  /* 1: b = x0 + e_1 (x) b0 as solvers_poisson_primal.jl:149-150 does;
                            0: b = e_1 (x) b0.  Boundary rows of b are zeroed either way. */
-    int check_every;    /* iterations between host-side convergence checks (>= 1) */
+    int check_every;    /* PCG iterations per body of the device-side loop (1..64, default 4): the
+                           whole PCG is one CUDA graph launch whose conditional WHILE node runs
+                           bodies until the device-side convergence flag is set; iterations of a
+                           body after convergence return at once */
 } sgfem_solve_options;
 
 typedef struct {

@@ -103,6 +103,34 @@ def test_maxit_reports_status(c1):
     assert st["iterations"] <= 2 + 8
 
 
+@pytest.mark.parametrize("precision", ["FP64", "MIXED"])
+def test_device_loop_body_length(c1, monkeypatch, precision):
+    """The PCG runs as a device-side WHILE loop of check_every iterations per
+    body: every body length gives the same iterates bit for bit (iterations of a
+    body after convergence return at once) and the same iteration count; the cap
+    maxit stops the loop at exactly maxit iterations."""
+    p, op, ref = c1
+    monkeypatch.setenv("SGFEM_SMALL", "0")  # the mixed solve's inner PCG through the device loop
+    op_ml = p.pkg.SGOperator(p.V, p.TB, p.Kall, device=0)
+    prec = getattr(p.pkg, precision)
+    xs, sts = [], []
+    for ce in (1, 3, 4, 64):
+        x = np.zeros(p.n * p.P)
+        sts.append(op_ml.solve_primal(p.b0, x, rtol=1e-10, precision=prec, check_every=ce))
+        xs.append(x)
+    for x, st in zip(xs[1:], sts[1:]):
+        assert np.array_equal(x, xs[0])
+        assert st["iterations"] == sts[0]["iterations"] and st["relres"] == sts[0]["relres"]
+    assert sts[0]["relres"] <= 1e-10 and rel(xs[0], ref) <= 1e-8
+    assert sts[-1]["kernel_launches"] > sts[0]["kernel_launches"]  # the early-return iterations count
+    for ce in (1, 4, 64):
+        x = np.zeros(p.n * p.P)
+        st = op_ml.solve_primal(p.b0, x, rtol=1e-14, precision=p.pkg.FP64, maxit=5, check_every=ce,
+                                allow_maxit=True)
+        assert st["iterations"] == 5, (ce, st)
+    op_ml.close()
+
+
 @pytest.mark.parametrize("order,N,M,P", [(2, 8, 4, 12), (2, 16, 6, 30)])
 def test_solve_p2_mixed(built_pkg, order, N, M, P):
     import __graft_entry__ as ge
