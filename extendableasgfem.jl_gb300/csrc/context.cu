@@ -102,6 +102,10 @@ extern "C" int sgfem_destroy(sgfem_context* ctx) {
     if (ctx->h_scal) cudaFreeHost(ctx->h_scal);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->side) cudaStreamSynchronize(ctx->side);
+    if (ctx->ev_spec_x) cudaEventDestroy(ctx->ev_spec_x);
+    if (ctx->ev_spec) cudaEventDestroy(ctx->ev_spec);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return SGFEM_OK;

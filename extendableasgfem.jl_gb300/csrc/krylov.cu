@@ -582,6 +582,23 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
         return SGFEM_OK;
     };
 
+    // the solution to the caller's pinned host buffer, overlapped with the convergence
+    // check that follows: converted on the main stream (one pass over x), copied on the
+    // side stream; the host waits for it when the solve returns (sgfem_solve)
+    auto spec_out = [&]() -> int {
+        if (!ctx->spec_host) return SGFEM_OK;
+        if (ctx->spec_pending) SG_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_spec, 0));  // staging free
+        SG_TRY(sg_launch_from_device(ctx, x64, (double*)ctx->w_stage.p, SGFEM_FP64));
+        SG_CUDA(ctx, cudaEventRecord(ctx->ev_spec_x, ctx->stream));
+        SG_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_spec_x, 0));
+        SG_CUDA(ctx, cudaMemcpyAsync(ctx->spec_host, ctx->w_stage.p, (size_t)ctx->n * ctx->P * sizeof(double),
+                                     cudaMemcpyDeviceToHost, ctx->side));
+        SG_CUDA(ctx, cudaEventRecord(ctx->ev_spec, ctx->side));
+        ctx->spec_pending = true;
+        ctx->spec_valid = true;
+        return SGFEM_OK;
+    };
+
     int status = SGFEM_OK;
     double rr = 0.0;
     // refinement residuals in double-FP32 arithmetic (residual_df.cu) when the operator
@@ -643,10 +660,12 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
                 h.tol2 = tol2e * bb;
                 SG_CUDA(ctx, cudaMemcpyAsync(ctx->d_scal, &h, sizeof(KrylovScalars), cudaMemcpyHostToDevice, ctx->stream));
                 int it = 0;
+                ctx->spec_valid = false;
                 status = S.pcg<double>(SGFEM_FP64, x64, r, t, q, tmp, remaining, check_every, &it);
                 st->iterations += it;
                 st->outer_iterations += 1;
                 remaining -= it;
+                if (status == SGFEM_OK) SG_TRY(spec_out());  // the recurrence met the target
                 SG_TRY(true_residual(&rr));
                 if (status != SGFEM_OK) break;
             }
@@ -714,12 +733,18 @@ static int solve_core(sgfem_context* ctx, const double* b0, double* x64, const s
                     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
                 }
                 const double rr_in = rr;
+                // a step whose target reduction reaches the final tolerance (or the single FP32
+                // solve) is expected to end the solve
+                const bool last = o->precision == SGFEM_FP32 || rr * want <= tol2e * bb;
+                ctx->spec_valid = false;
                 if (df) {
                     SG_TRY(sg_split_df(ctx, x64, d64, xs, 1));  // x += d, then x as (hi, lo)
+                    if (last) SG_TRY(spec_out());
                     SG_TRY(residual_df(&rr));
                 } else {
                     k_add64<<<g, VT, 0, ctx->stream>>>(x64, d64, total);
                     SG_LAUNCHED(ctx);
+                    if (last) SG_TRY(spec_out());
                     SG_TRY(true_residual(&rr));
                 }
                 if (use_small) {  // the residual's synchronisation also brought the scalars
@@ -793,7 +818,31 @@ extern "C" int sgfem_solve(sgfem_context* ctx, const double* b0, double* x_inout
     SG_TRY(sg_ensure(ctx, ctx->w_vec[10], n64));
     ctx->samples_x_valid = false;
     SG_TRY(sgfem_to_device_layout(ctx, x_inout, ctx->w_vec[10].p, SGFEM_FP64));
+    // pinned x_inout: the solution's copy overlaps the last convergence check
+    // (SGFEM_OVERLAP_COPY=0 turns this off); pageable memory takes the copy below
+    cudaPointerAttributes pa{};
+    const bool pinned = cudaPointerGetAttributes(&pa, x_inout) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+    const char* eov = getenv("SGFEM_OVERLAP_COPY");
+    if (pinned && !(eov && atoi(eov) == 0)) {
+        if (!ctx->side) SG_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+        if (!ctx->ev_spec_x) SG_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_spec_x, cudaEventDisableTiming));
+        if (!ctx->ev_spec) SG_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_spec, cudaEventDisableTiming));
+        ctx->spec_host = x_inout;
+    }
+    ctx->spec_pending = false;
+    ctx->spec_valid = false;
     int rc = sgfem_solve_device(ctx, b0, ctx->w_vec[10].p, opts, stats);
+    ctx->spec_host = nullptr;
+    if (ctx->spec_pending) {  // a copy into x_inout may still run: wait for it on every return
+        ctx->spec_pending = false;
+        const cudaError_t e = cudaEventSynchronize(ctx->ev_spec);
+        if (e != cudaSuccess) return sg_cuda_fail(ctx, e, "solution copy");
+        if (ctx->spec_valid && (rc == SGFEM_OK || rc == SGFEM_ERR_MAXIT)) {
+            if (getenv("SGFEM_TRACE")) fprintf(stderr, "sgfem: solution copy overlapped with the convergence check\n");
+            return rc;  // x_inout holds the final solution
+        }
+    }
     if (rc != SGFEM_OK && rc != SGFEM_ERR_MAXIT) return rc;
     std::string keep = ctx->err;
     int rc2 = sgfem_from_device_layout(ctx, ctx->w_vec[10].p, x_inout, SGFEM_FP64);

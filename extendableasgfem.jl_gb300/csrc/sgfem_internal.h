@@ -198,6 +198,14 @@ struct sgfem_context {
     KrylovScalars* d_scal = nullptr;
     KrylovScalars* h_scal = nullptr;  // pinned
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // sgfem_solve into pinned host memory: the solution of a refinement step expected
+    // to end the solve goes to the host on a side stream while the convergence check
+    // (the FP64 / double-FP32 residual) runs
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_spec_x = nullptr, ev_spec = nullptr;  // x converted; copy done
+    double* spec_host = nullptr;  // destination while a solve runs, else null
+    bool spec_pending = false;    // a copy was issued (ev_spec marks its end)
+    bool spec_valid = false;      // the last copy holds the current solution
     long long launches = 0;    // kernels launched by this context (graph replays included)
 };
 

@@ -163,6 +163,11 @@ SGFEM_API int sgfem_precondition(sgfem_context* ctx, const double* b, double* y,
  * solves S x = b with b built from b0 (n doubles, the assembled (f, v)) and the
  * warm start x_inout (SGFEVector.entries, in/out).  Uses PCG (the SG operator of
  * PoissonProblemPrimal is SPD on interior dofs) instead of the reference's GMRES.
+ * x_inout receives the solution on SGFEM_OK and SGFEM_ERR_MAXIT.  When x_inout is
+ * pinned host memory (cudaHostAlloc / cudaHostRegister), the solution of a step
+ * expected to end the solve is copied to it while the final convergence check runs;
+ * after an error other than SGFEM_ERR_MAXIT it may then hold that last iterate.
+ * The call returns only once every copy into x_inout has ended.
  */
 SGFEM_API int sgfem_solve(sgfem_context* ctx, const double* b0, double* x_inout,
                 const sgfem_solve_options* opts, sgfem_solve_stats* stats);

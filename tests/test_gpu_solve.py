@@ -104,6 +104,37 @@ def test_maxit_reports_status(c1):
 
 
 @pytest.mark.parametrize("precision", ["FP64", "MIXED"])
+def test_pinned_solution_copy_overlaps_the_last_check(c1, monkeypatch, capfd, precision):
+    """sgfem_solve into pinned host memory copies the solution of the step expected
+    to end the solve during the final convergence check: the caller gets the same
+    bits as through pageable memory (copy after the solve), also with a warm start
+    and after a step that did not end the solve (rtol 1e-12 forces a later step)."""
+    torch = pytest.importorskip("torch")
+    p, op, ref = c1
+    prec = getattr(p.pkg, precision)
+    monkeypatch.setenv("SGFEM_TRACE", "1")
+    rng = np.random.default_rng(5)
+    x0 = 0.1 * rng.standard_normal(p.n * p.P)
+    for rtol in (1e-10, 1e-12):
+        for start in (np.zeros(p.n * p.P), x0):
+            xa = start.copy()
+            sa = op.solve_primal(p.b0, xa, rtol=rtol, precision=prec)
+            capfd.readouterr()
+            xp = torch.zeros(p.n * p.P, dtype=torch.float64, pin_memory=True).numpy()
+            xp[:] = start
+            sp = op.solve_primal(p.b0, xp, rtol=rtol, precision=prec)
+            err = capfd.readouterr().err
+            assert "solution copy overlapped" in err, err
+            assert np.array_equal(xa, xp)
+            assert sa["iterations"] == sp["iterations"] and sa["relres"] == sp["relres"] <= rtol
+    monkeypatch.setenv("SGFEM_OVERLAP_COPY", "0")
+    xq = torch.zeros(p.n * p.P, dtype=torch.float64, pin_memory=True).numpy()
+    op.solve_primal(p.b0, xq, rtol=1e-10, precision=prec)
+    assert "solution copy overlapped" not in capfd.readouterr().err
+    assert rel(xq, ref) <= 1e-8
+
+
+@pytest.mark.parametrize("precision", ["FP64", "MIXED"])
 def test_device_loop_body_length(c1, monkeypatch, precision):
     """The PCG runs as a device-side WHILE loop of check_every iterations per
     body: every body length gives the same iterates bit for bit (iterations of a
