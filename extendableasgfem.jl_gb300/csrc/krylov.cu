@@ -331,13 +331,18 @@ struct Solver {
         SG_TRY(fin(g, FIN_RR, FinArgs{0.0, maxit, 0, 0}));
         SG_TRY(precond_block<T>(precision, r, p, tmp, maxit));
 
+        // SGFEM_PCG_LOOP=host: the graph is check_every plain iterations, replayed by a
+        // host loop that reads the scalars between replays (for tools that do not
+        // profile the kernels of conditional graph bodies, and drivers without them)
+        const char* elp = getenv("SGFEM_PCG_LOOP");
+        const bool host_loop = elp && std::strcmp(elp, "host") == 0;
         // the graph depends only on the buffers, the kernel choice and the block
         // counts (the iteration cap lives in the device scalars), so the instantiated
         // graph of the previous run on the same buffers is replayed
-        const uint64_t key[12] = {(uint64_t)precision, (uint64_t)sizeof(T), (uint64_t)sizeof(TX), (uint64_t)(uintptr_t)x,
+        const uint64_t key[13] = {(uint64_t)precision, (uint64_t)sizeof(T), (uint64_t)sizeof(TX), (uint64_t)(uintptr_t)x,
                                   (uint64_t)(uintptr_t)r, (uint64_t)(uintptr_t)p, (uint64_t)(uintptr_t)q,
                                   (uint64_t)(uintptr_t)tmp, (uint64_t)check_every, (uint64_t)prec_kind,
-                                  (uint64_t)(uintptr_t)partials, (uint64_t)(uintptr_t)s};
+                                  (uint64_t)(uintptr_t)partials, (uint64_t)(uintptr_t)s, (uint64_t)host_loop};
         if (!ctx->pcg_exec || std::memcmp(key, ctx->pcg_key, sizeof(key)) != 0) {
             if (ctx->pcg_exec) cudaGraphExecDestroy(ctx->pcg_exec);
             if (ctx->pcg_graph) cudaGraphDestroy(ctx->pcg_graph);
@@ -345,16 +350,20 @@ struct Solver {
             ctx->pcg_graph = nullptr;
             cudaGraph_t graph = nullptr;
             SG_CUDA(ctx, cudaGraphCreate(&graph, 0));
+            cudaGraph_t body = graph;  // host loop: the iterations are the graph itself
+            cudaError_t ce = cudaSuccess;
             cudaGraphConditionalHandle h = 0;
-            cudaError_t ce = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
-            cudaGraphNodeParams np{};
-            np.type = cudaGraphNodeTypeConditional;
-            np.conditional.handle = h;
-            np.conditional.type = cudaGraphCondTypeWhile;
-            np.conditional.size = 1;
-            cudaGraphNode_t node = nullptr;
-            if (ce == cudaSuccess) ce = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np);
-            cudaGraph_t body = ce == cudaSuccess ? np.conditional.phGraph_out[0] : nullptr;
+            if (!host_loop) {
+                ce = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+                cudaGraphNodeParams np{};
+                np.type = cudaGraphNodeTypeConditional;
+                np.conditional.handle = h;
+                np.conditional.type = cudaGraphCondTypeWhile;
+                np.conditional.size = 1;
+                cudaGraphNode_t node = nullptr;
+                if (ce == cudaSuccess) ce = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np);
+                body = ce == cudaSuccess ? np.conditional.phGraph_out[0] : nullptr;
+            }
             if (ce == cudaSuccess)
                 ce = cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0,
                                                    cudaStreamCaptureModeThreadLocal);
@@ -366,7 +375,7 @@ struct Solver {
             const long long before = ctx->launches;
             loop_handle = h;
             for (int k = 0; k < check_every && st == SGFEM_OK; ++k) {
-                loop = k == check_every - 1;
+                loop = !host_loop && k == check_every - 1;
                 st = iteration<T, TX>(precision, x, r, p, q, tmp, maxit);
             }
             loop = 0;
@@ -388,12 +397,23 @@ struct Solver {
             ctx->pcg_per_graph = per_body;
             std::memcpy(ctx->pcg_key, key, sizeof(key));
         }
-        cudaError_t le = cudaGraphLaunch(ctx->pcg_exec, ctx->stream);
-        if (le != cudaSuccess) return sg_cuda_fail(ctx, le, "cudaGraphLaunch");
-        SG_CUDA(ctx, cudaMemcpyAsync(ctx->h_scal, s, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, ctx->stream));
-        SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         const KrylovScalars* hs = ctx->h_scal;
-        ctx->launches += ctx->pcg_per_graph * hs->loops;
+        if (host_loop) {
+            for (;;) {
+                SG_CUDA(ctx, cudaMemcpyAsync(ctx->h_scal, s, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, ctx->stream));
+                SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+                if (hs->done) break;
+                cudaError_t le = cudaGraphLaunch(ctx->pcg_exec, ctx->stream);
+                if (le != cudaSuccess) return sg_cuda_fail(ctx, le, "cudaGraphLaunch");
+                ctx->launches += ctx->pcg_per_graph;
+            }
+        } else {
+            cudaError_t le = cudaGraphLaunch(ctx->pcg_exec, ctx->stream);
+            if (le != cudaSuccess) return sg_cuda_fail(ctx, le, "cudaGraphLaunch");
+            SG_CUDA(ctx, cudaMemcpyAsync(ctx->h_scal, s, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, ctx->stream));
+            SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            ctx->launches += ctx->pcg_per_graph * hs->loops;
+        }
         *iters = hs->iters;
         if (!hs->done) return sg_fail(ctx, SGFEM_ERR_MAXIT, "PCG device loop ended before the done flag");
         return hs->status;

@@ -192,7 +192,7 @@ struct sgfem_context {
     // run on the same buffers
     cudaGraph_t pcg_graph = nullptr;
     cudaGraphExec_t pcg_exec = nullptr;
-    uint64_t pcg_key[12] = {};
+    uint64_t pcg_key[13] = {};
     long long pcg_per_graph = 0;  // kernel launches per loop body
     DeviceBuf w_gsmall;        // GMRES multi-dot partials and coefficients
     KrylovScalars* d_scal = nullptr;

@@ -154,6 +154,16 @@ def test_device_loop_body_length(c1, monkeypatch, precision):
         assert st["iterations"] == sts[0]["iterations"] and st["relres"] == sts[0]["relres"]
     assert sts[0]["relres"] <= 1e-10 and rel(xs[0], ref) <= 1e-8
     assert sts[-1]["kernel_launches"] > sts[0]["kernel_launches"]  # the early-return iterations count
+    # the host-checked replay loop (SGFEM_PCG_LOOP=host) runs the same iterations
+    monkeypatch.setenv("SGFEM_PCG_LOOP", "host")
+    for ce in (1, 4):
+        x = np.zeros(p.n * p.P)
+        st = op_ml.solve_primal(p.b0, x, rtol=1e-10, precision=prec, check_every=ce)
+        assert np.array_equal(x, xs[0]) and st["iterations"] == sts[0]["iterations"]
+    x = np.zeros(p.n * p.P)
+    st = op_ml.solve_primal(p.b0, x, rtol=1e-14, precision=p.pkg.FP64, maxit=5, check_every=4, allow_maxit=True)
+    assert st["iterations"] == 5
+    monkeypatch.delenv("SGFEM_PCG_LOOP")
     for ce in (1, 4, 64):
         x = np.zeros(p.n * p.P)
         st = op_ml.solve_primal(p.b0, x, rtol=1e-14, precision=p.pkg.FP64, maxit=5, check_every=ce,
