@@ -74,6 +74,7 @@ SIGNATURES = {
     "sgfem_lattice_log": (ctypes.c_char_p, [_P]),
     "sgfem_cholesky_log": (ctypes.c_char_p, [_P]),
     "sgfem_small_solve_log": (ctypes.c_char_p, [_P]),
+    "sgfem_sampling_error_log": (ctypes.c_char_p, [_P]),
     "sgfem_cholesky_host_solve": (ctypes.c_int, [ctypes.c_int64, _I64P, _I64P, _DP, ctypes.c_int64, _I64P,
                                                  ctypes.c_int64, _DP, _DP, ctypes.c_char_p, ctypes.c_int]),
     "sgfem_apply": (ctypes.c_int, [_P, _DP, _DP, ctypes.c_int]),
@@ -274,6 +275,11 @@ class Context:
     @property
     def has_lattice(self):
         return bool(self.lib.sgfem_has_lattice(self.h))
+
+    @property
+    def sampling_error_log(self):
+        """The form of the last sampling-error call: quadratic forms or quadrature points."""
+        return self.lib.sgfem_sampling_error_log(self.h).decode()
 
     @property
     def small_solve_log(self):

@@ -26,6 +26,7 @@
 //                    partials that a second kernel adds in group order, so the
 //                    result is bitwise reproducible.  FP64 throughout.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <numeric>
 #include <string>
@@ -231,6 +232,118 @@ __global__ void __launch_bounds__(SW * 32) k_sampling_error(ErrArgs a) {
     }
 }
 
+// The same sums as quadratic forms, where the SG space embeds in the deterministic one
+// (P1 in P2, equal orders): psi_j = sum_i E_ij phi_i with E_ij = psi_j(node_i), so on
+// every cell e = u_s - u_sg,m = sum_i c_i phi_i with c = d - E us, and with matrices
+// built from the caller's rule
+//   sum_q w_q e(x_q)^2        = c' Mq c,     Mq_ij  = sum_q w_q phi_i phi_j,
+//   sum_q w_q |grad e(x_q)|^2 = c' K_T c,    K_T_ij = sum_{k,l} (g_k . g_l) R^kl_ij,
+//   R^kl_ij = sum_q w_q (dphi_i/dlam_k)(dphi_j/dlam_l),
+// the quadrature sums of k_sampling_error up to rounding, for any rule.  K_T
+// annihilates constants, so the gradient form takes c_i - c_0 (a nearly constant error
+// does not cancel).  Per (cell, sample, level): NDD NDS + ~2 NDD^2 FMAs instead of
+// nq (3 NDS + 4), and no quadrature pass over u_s per cell.
+__host__ __device__ constexpr int ut_index(int i, int j, int n) { return i * n - i * (i - 1) / 2 + (j - i); }
+
+struct QfArgs {
+    int ncells, S, ld, M, nsg, groups, lds;
+    const double* vol;   // ncells
+    const double* KT;    // ncells x NDD(NDD+1)/2, upper triangle row by row
+    const double* E;     // NDD x NDS
+    const double* Mq;    // NDD(NDD+1)/2
+    const int* ddofs;
+    const int* sdofs;
+    const double* D;
+    const double* U;
+    const double* psi;
+    const int* kptr;
+    double* part;
+};
+
+template <int NDD, int NDS>
+__global__ void __launch_bounds__(SW * 32) k_sampling_error_qf(QfArgs a) {
+    constexpr int NT = NDD * (NDD + 1) / 2;
+    extern __shared__ double ssm[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* sE = ssm;                                          // NDD x NDS
+    double* sM = sE + NDD * NDS;                               // NT
+    double* acc = sM + NT + (size_t)warp * (a.M + 1) * 2 * 32;  // [m][2][32]
+    for (int t = threadIdx.x; t < NDD * NDS; t += blockDim.x) sE[t] = a.E[t];
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) sM[t] = a.Mq[t];
+    for (int t = 0; t <= a.M; ++t) {
+        acc[(2 * t) * 32 + lane] = 0.0;
+        acc[(2 * t + 1) * 32 + lane] = 0.0;
+    }
+    __syncthreads();
+    const int chunks = (a.S + 31) / 32;
+    const int wid = blockIdx.x * SW + warp;
+    const int chunk = wid % chunks, group = wid / chunks;
+    if (group >= a.groups) return;
+    const int s = chunk * 32 + lane;
+    const bool live = s < a.S;
+    for (int c = group; c < a.ncells; c += a.groups) {
+        double K[NT];
+#pragma unroll
+        for (int t = 0; t < NT; ++t) K[t] = __ldg(a.KT + (size_t)c * NT + t);
+        const double vol = __ldg(a.vol + c);
+        double d[NDD];
+#pragma unroll
+        for (int i = 0; i < NDD; ++i) d[i] = live ? a.D[(size_t)a.ddofs[(size_t)c * NDD + i] * a.ld + s] : 0.0;
+        int sd[NDS];
+        double us[NDS];
+#pragma unroll
+        for (int i = 0; i < NDS; ++i) {
+            sd[i] = a.sdofs[(size_t)c * NDS + i];
+            us[i] = 0.0;
+        }
+        for (int m = 0; m <= a.M; ++m) {
+            const int k1 = a.kptr[m + 1];
+            for (int k = a.kptr[m]; k < k1; ++k) {
+                const double ps = live ? a.psi[(size_t)k * a.lds + s] : 0.0;
+                const double* Uk = a.U + (size_t)k * a.nsg;
+#pragma unroll
+                for (int i = 0; i < NDS; ++i) us[i] = fma(__ldg(Uk + sd[i]), ps, us[i]);
+            }
+            double e[NDD];
+#pragma unroll
+            for (int i = 0; i < NDD; ++i) {
+                double v = d[i];
+#pragma unroll
+                for (int j = 0; j < NDS; ++j) v = fma(-sE[i * NDS + j], us[j], v);
+                e[i] = v;
+            }
+            double el = 0.0;
+#pragma unroll
+            for (int i = 0; i < NDD; ++i) {
+                double off = 0.0;
+#pragma unroll
+                for (int j = i + 1; j < NDD; ++j) off = fma(sM[ut_index(i, j, NDD)], e[j], off);
+                el = fma(e[i], fma(2.0, off, sM[ut_index(i, i, NDD)] * e[i]), el);
+            }
+            double f[NDD];
+#pragma unroll
+            for (int i = 1; i < NDD; ++i) f[i] = e[i] - e[0];
+            double eh = 0.0;
+#pragma unroll
+            for (int i = 1; i < NDD; ++i) {
+                double off = 0.0;
+#pragma unroll
+                for (int j = i + 1; j < NDD; ++j) off = fma(K[ut_index(i, j, NDD)], f[j], off);
+                eh = fma(f[i], fma(2.0, off, K[ut_index(i, i, NDD)] * f[i]), eh);
+            }
+            acc[(2 * m) * 32 + lane] += vol * eh;
+            acc[(2 * m + 1) * 32 + lane] += vol * el;
+        }
+    }
+    if (live) {
+        double* out = a.part + (size_t)group * (a.M + 1) * 2 * a.S;
+        for (int m = 0; m <= a.M; ++m) {
+            out[(size_t)(2 * m) * a.S + s] = acc[(2 * m) * 32 + lane];
+            out[(size_t)(2 * m + 1) * a.S + s] = acc[(2 * m + 1) * 32 + lane];
+        }
+    }
+}
+
 // errH1/errL2[s * (M+1) + m] = sum over groups in order
 __global__ void k_sampling_reduce(const double* __restrict__ part, int groups, int M, int S, double* __restrict__ eh,
                                   double* __restrict__ el) {
@@ -293,6 +406,84 @@ int launch_psi(sgfem_context* ctx, const sgfem_sg_basis* b, const int* d_mi, con
     const int blocks = (int)((total + 255) / 256);
     k_psi<<<blocks, 256, 0, ctx->stream>>>((int)b->P, (int)b->M, S, d_mi, d_rec, d_norms, d_y, ys, yoff, mtrunc, d_psi,
                                           lds);
+    SG_LAUNCHED(ctx);
+    return SGFEM_OK;
+}
+
+// d phi_i / d lam_k (k = 0..2) of the P1 / P2 basis at barycentric lam, out[i * 3 + k]
+void basis_dlam(int order, const double* lam, double* out) {
+    std::fill(out, out + 18, 0.0);
+    if (order == 1) {
+        for (int i = 0; i < 3; ++i) out[i * 3 + i] = 1.0;
+        return;
+    }
+    const int ea[3] = {0, 1, 2}, eb[3] = {1, 2, 0};
+    for (int i = 0; i < 3; ++i) out[i * 3 + i] = 4.0 * lam[i] - 1.0;
+    for (int e = 0; e < 3; ++e) {
+        out[(3 + e) * 3 + ea[e]] = 4.0 * lam[eb[e]];
+        out[(3 + e) * 3 + eb[e]] = 4.0 * lam[ea[e]];
+    }
+}
+
+// Quadratic-form data of k_sampling_error_qf from the cell rule: E (SG basis in the
+// deterministic one, false when it does not embed), Mq and the six symmetric
+// combinations Rs[(k,l), k <= l] of R^kl (R^kl + R^lk off the diagonal).
+bool quadform_tables(int od, int os, int nq, const double* xq, const double* wq, std::vector<double>& E,
+                     std::vector<double>& Mq, std::vector<double>& Rs) {
+    const int ndd = sgfem_fe::ndofs4cell(od), nds = sgfem_fe::ndofs4cell(os), nt = ndd * (ndd + 1) / 2;
+    // nodes of the deterministic basis: vertices, then the midpoints of (0,1), (1,2), (2,0)
+    const double nodes[6][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0.5, 0.5, 0}, {0, 0.5, 0.5}, {0.5, 0, 0.5}};
+    E.assign((size_t)ndd * nds, 0.0);
+    double v[6], w6[6];
+    for (int i = 0; i < ndd; ++i) {
+        sgfem_fe::basis_val(os, nodes[i], v);
+        for (int j = 0; j < nds; ++j) E[(size_t)i * nds + j] = v[j];
+    }
+    // the embedding holds where sum_i E_ij phi_i = psi_j on a set that determines quadratics
+    std::vector<std::array<double, 3>> pts;
+    for (int q = 0; q < nq; ++q) pts.push_back({1.0 - xq[2 * q] - xq[2 * q + 1], xq[2 * q], xq[2 * q + 1]});
+    for (auto& nd : nodes) pts.push_back({nd[0], nd[1], nd[2]});
+    pts.push_back({1.0 / 3, 1.0 / 3, 1.0 / 3});
+    pts.push_back({0.2, 0.3, 0.5});
+    pts.push_back({0.6, 0.1, 0.3});
+    for (auto& lam : pts) {
+        sgfem_fe::basis_val(od, lam.data(), w6);
+        sgfem_fe::basis_val(os, lam.data(), v);
+        for (int j = 0; j < nds; ++j) {
+            double t = 0.0;
+            for (int i = 0; i < ndd; ++i) t += E[(size_t)i * nds + j] * w6[i];
+            if (std::fabs(t - v[j]) > 1e-13) return false;
+        }
+    }
+    Mq.assign(nt, 0.0);
+    Rs.assign((size_t)6 * nt, 0.0);
+    const int kk[6] = {0, 1, 2, 0, 0, 1}, ll[6] = {0, 1, 2, 1, 2, 2};
+    double dl[18];
+    for (int q = 0; q < nq; ++q) {
+        const double lam[3] = {1.0 - xq[2 * q] - xq[2 * q + 1], xq[2 * q], xq[2 * q + 1]};
+        sgfem_fe::basis_val(od, lam, w6);
+        basis_dlam(od, lam, dl);
+        for (int i = 0; i < ndd; ++i)
+            for (int j = i; j < ndd; ++j) {
+                const int t = ut_index(i, j, ndd);
+                Mq[t] += wq[q] * w6[i] * w6[j];
+                for (int r = 0; r < 6; ++r) {
+                    const int k = kk[r], l = ll[r];
+                    double g = dl[i * 3 + k] * dl[j * 3 + l];
+                    if (k != l) g += dl[i * 3 + l] * dl[j * 3 + k];
+                    Rs[(size_t)r * nt + t] += wq[q] * g;
+                }
+            }
+    }
+    return true;
+}
+
+template <int NDD, int NDS>
+int launch_error_qf(sgfem_context* ctx, const QfArgs& a, int blocks, size_t smem) {
+    if (smem > 48 * 1024)
+        SG_CUDA(ctx, cudaFuncSetAttribute(k_sampling_error_qf<NDD, NDS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+    k_sampling_error_qf<NDD, NDS><<<blocks, SW * 32, smem, ctx->stream>>>(a);
     SG_LAUNCHED(ctx);
     return SGFEM_OK;
 }
@@ -426,7 +617,6 @@ extern "C" int sgfem_sampling_error(sgfem_context* ctx, const double* det_soluti
     sorted.multi_indices = mi.data();
 
     Owned o;
-    ErrArgs a{};
     const int lds = (int)((S + 31) / 32 * 32);
     int *d_mi, *d_kptr, *d_dd, *d_sd;
     double *d_rec, *d_norms, *d_U, *d_psi, *d_xq, *d_wq, *d_part, *d_eh, *d_el;
@@ -450,44 +640,106 @@ extern "C" int sgfem_sampling_error(sgfem_context* ctx, const double* det_soluti
     const int groups = (int)std::max<int64_t>(1, std::min<int64_t>(nc, (target + chunks - 1) / chunks));
     const int64_t warps = (int64_t)groups * chunks;
     const int blocks = (int)((warps + SW - 1) / SW);
-    const size_t smem = sizeof(double) * ((size_t)nq * (ndd + nds + 1) +
-                                          (size_t)SW * (nq * 2 * (ndd + nds) + nq * 3 * 32 + (M + 1) * 2 * 32));
-    if (smem > 227 * 1024)
-        return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED, "sampling error: too many truncation levels or quadrature points for shared memory");
     const size_t per = (size_t)(M + 1) * 2 * S;
     SG_TRY(scratch(ctx, o, per * groups, &d_part));
     SG_TRY(scratch(ctx, o, (size_t)(M + 1) * S, &d_eh));
     SG_TRY(scratch(ctx, o, (size_t)(M + 1) * S, &d_el));
-    a.od = mesh->order;
-    a.os = sg_space->order;
-    a.nq = nq;
-    a.ncells = (int)nc;
-    a.S = (int)S;
-    a.ld = (int)ctx->ld;
-    a.M = (int)M;
-    a.nsg = (int)nsg;
-    a.groups = groups;
-    a.lds = lds;
-    a.cg = d_cg;
-    a.ddofs = d_dd;
-    a.sdofs = d_sd;
-    a.D = (const double*)ctx->w_vec[10].p;
-    a.U = d_U;
-    a.psi = d_psi;
-    a.kptr = d_kptr;
-    a.xq = d_xq;
-    a.wq = d_wq;
-    a.part = d_part;
-    int rc;
-    if (ndd == 6 && nds == 3) rc = launch_error<6, 3>(ctx, a, blocks, smem);
-    else if (ndd == 6) rc = launch_error<6, 6>(ctx, a, blocks, smem);
-    else if (nds == 3) rc = launch_error<3, 3>(ctx, a, blocks, smem);
-    else rc = launch_error<3, 6>(ctx, a, blocks, smem);
-    SG_TRY(rc);
+    // quadratic forms where the SG space embeds in the deterministic one (SGFEM_SAMPLING_QF=0:
+    // the quadrature kernel always)
+    std::vector<double> E, Mq, Rs;
+    const char* eqf = getenv("SGFEM_SAMPLING_QF");
+    const bool qf = !(eqf && atoi(eqf) == 0) && quadform_tables(mesh->order, sg_space->order, nq, quad->xref, quad->w,
+                                                                 E, Mq, Rs);
+    const size_t smem_qf = sizeof(double) * ((size_t)ndd * nds + Mq.size() + (size_t)SW * (M + 1) * 2 * 32);
+    if (qf && smem_qf <= 227 * 1024) {
+        const int nt = ndd * (ndd + 1) / 2;
+        const int kk[6] = {0, 1, 2, 0, 0, 1}, ll[6] = {0, 1, 2, 1, 2, 2};
+        std::vector<double> KT((size_t)nc * nt), vol(nc);
+        for (int64_t c = 0; c < nc; ++c) {
+            const double* g = cg[c].g;
+            double G[6];
+            for (int r = 0; r < 6; ++r) G[r] = g[2 * kk[r]] * g[2 * ll[r]] + g[2 * kk[r] + 1] * g[2 * ll[r] + 1];
+            for (int t = 0; t < nt; ++t) {
+                double v = 0.0;
+                for (int r = 0; r < 6; ++r) v += G[r] * Rs[(size_t)r * nt + t];
+                KT[(size_t)c * nt + t] = v;
+            }
+            vol[c] = cg[c].vol;
+        }
+        double *d_KT, *d_vol, *d_E, *d_Mq;
+        SG_TRY(up(ctx, o, KT.data(), KT.size(), &d_KT));
+        SG_TRY(up(ctx, o, vol.data(), vol.size(), &d_vol));
+        SG_TRY(up(ctx, o, E.data(), E.size(), &d_E));
+        SG_TRY(up(ctx, o, Mq.data(), Mq.size(), &d_Mq));
+        QfArgs b{};
+        b.ncells = (int)nc;
+        b.S = (int)S;
+        b.ld = (int)ctx->ld;
+        b.M = (int)M;
+        b.nsg = (int)nsg;
+        b.groups = groups;
+        b.lds = lds;
+        b.vol = d_vol;
+        b.KT = d_KT;
+        b.E = d_E;
+        b.Mq = d_Mq;
+        b.ddofs = d_dd;
+        b.sdofs = d_sd;
+        b.D = (const double*)ctx->w_vec[10].p;
+        b.U = d_U;
+        b.psi = d_psi;
+        b.kptr = d_kptr;
+        b.part = d_part;
+        int rc;
+        if (ndd == 6 && nds == 3) rc = launch_error_qf<6, 3>(ctx, b, blocks, smem_qf);
+        else if (ndd == 6) rc = launch_error_qf<6, 6>(ctx, b, blocks, smem_qf);
+        else rc = launch_error_qf<3, 3>(ctx, b, blocks, smem_qf);
+        SG_TRY(rc);
+        ctx->sampling_form = 1;
+    } else {
+        ctx->sampling_form = 2;
+        const size_t smem = sizeof(double) * ((size_t)nq * (ndd + nds + 1) +
+                                              (size_t)SW * (nq * 2 * (ndd + nds) + nq * 3 * 32 + (M + 1) * 2 * 32));
+        if (smem > 227 * 1024)
+            return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED,
+                           "sampling error: too many truncation levels or quadrature points for shared memory");
+        ErrArgs a{};
+        a.od = mesh->order;
+        a.os = sg_space->order;
+        a.nq = nq;
+        a.ncells = (int)nc;
+        a.S = (int)S;
+        a.ld = (int)ctx->ld;
+        a.M = (int)M;
+        a.nsg = (int)nsg;
+        a.groups = groups;
+        a.lds = lds;
+        a.cg = d_cg;
+        a.ddofs = d_dd;
+        a.sdofs = d_sd;
+        a.D = (const double*)ctx->w_vec[10].p;
+        a.U = d_U;
+        a.psi = d_psi;
+        a.kptr = d_kptr;
+        a.xq = d_xq;
+        a.wq = d_wq;
+        a.part = d_part;
+        int rc;
+        if (ndd == 6 && nds == 3) rc = launch_error<6, 3>(ctx, a, blocks, smem);
+        else if (ndd == 6) rc = launch_error<6, 6>(ctx, a, blocks, smem);
+        else if (nds == 3) rc = launch_error<3, 3>(ctx, a, blocks, smem);
+        else rc = launch_error<3, 6>(ctx, a, blocks, smem);
+        SG_TRY(rc);
+    }
     k_sampling_reduce<<<(int)((per + 255) / 256), 256, 0, ctx->stream>>>(d_part, groups, (int)M, (int)S, d_eh, d_el);
     SG_LAUNCHED(ctx);
     SG_CUDA(ctx, cudaMemcpyAsync(errH1, d_eh, (size_t)(M + 1) * S * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     SG_CUDA(ctx, cudaMemcpyAsync(errL2, d_el, (size_t)(M + 1) * S * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return SGFEM_OK;
+}
+
+extern "C" const char* sgfem_sampling_error_log(const sgfem_context* ctx) {
+    if (!ctx) return "no context";
+    return ctx->sampling_form == 1 ? "quadratic forms" : ctx->sampling_form == 2 ? "quadrature points" : "none";
 }

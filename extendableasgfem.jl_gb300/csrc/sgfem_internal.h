@@ -76,6 +76,7 @@ struct sgfem_context {
     double* d_kval64 = nullptr;  // [nnz][ld]: K(y_s) = sum_m y_{s,m} K_m per sample (nullptr: combined on the fly)
     float* d_kval32 = nullptr;
     bool samples_x_valid = false;  // w_vec[10] holds the solutions of the current samples
+    int sampling_form = 0;         // last sgfem_sampling_error: 0 none, 1 quadratic forms, 2 quadrature points
     std::vector<int64_t> bdofs;  // 0-based caller numbering
     bool has_bdofs = false;
     std::vector<double> dof_xy;  // 2 x n column-major

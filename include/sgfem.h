@@ -377,6 +377,11 @@ SGFEM_API int sgfem_rt_reference_basis(int k, int np, const double* pts, double*
  * The SG part is evaluated with Psi_k at the full sample (m = M); for modes
  * active at truncation m this differs from the reference's truncated product
  * only by the factors 1/||p_0|| of the dimensions m..M-1 (1 up to rounding).
+ * Where the SG space embeds in the deterministic one (P1 in P2, equal orders)
+ * the rule's sums are evaluated as quadratic forms in the local coefficients of
+ * the error, with matrices built from the same rule (equal up to rounding);
+ * otherwise point by point.  sgfem_sampling_error_log names the form of the
+ * last call; SGFEM_SAMPLING_QF=0 keeps the point-by-point form.
  */
 typedef struct {                   /* TensorizedBasis + ONBasis, src/tensorizedbasis.jl:28-34, onbasis.jl:13-18 */
     int64_t P;                     /* multi-indices */
@@ -398,6 +403,9 @@ SGFEM_API int sgfem_evaluate_samples(sgfem_context* ctx, const double* U, int64_
 SGFEM_API int sgfem_sampling_error(sgfem_context* ctx, const double* det_solutions, const sgfem_mesh* mesh,
                                    const sgfem_fe_space* sg_space, const double* U, const sgfem_sg_basis* basis,
                                    const sgfem_quadrature* quad, double* errH1, double* errL2);
+/* "quadratic forms", "quadrature points" or "none" (no call yet): the form of the
+   last sgfem_sampling_error on this context. */
+SGFEM_API const char* sgfem_sampling_error_log(const sgfem_context* ctx);
 
 /*
  * No counterpart in the reference package.  Applies the mean-based lattice

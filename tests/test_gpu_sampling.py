@@ -129,6 +129,48 @@ def test_sampling_error_integrals_match_oracle(built_pkg):
             assert abs(el[m, s] - l2) <= 1e-11 * l2
 
 
+@pytest.mark.parametrize("sg_order,det_order", [(1, 2), (2, 2), (1, 1), (2, 1)])
+def test_sampling_error_forms_match_oracle(built_pkg, monkeypatch, sg_order, det_order):
+    """The error sums as quadratic forms in the error's local coefficients (the SG
+    space embeds in the deterministic one: P1 in P2, equal orders) and point by point
+    (no embedding, or SGFEM_SAMPLING_QF=0): both against the oracle's point-by-point
+    sums (1e-11 per (m, s)) and against each other (1e-12), for 4- and 6-point rules."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    M, N, Ms, S = 3, 8, 5, 37
+    p = build(N, sg_order, M, pkg.total_degree_multiindices(M, 2))
+    rng = np.random.default_rng(21)
+    p.sol.entries[:] = rng.standard_normal(len(p.sol.entries))
+    maxdeg = max(max(mi) for mi in p.mis)
+    TBo = ob.TensorizedBasis(ob.LEGENDRE, M, maxdeg, maxdeg + 4, multi_indices=p.mis)
+    y = rng.uniform(-1, 1, (Ms, S))
+    Vd = pkg.H1Pk(p.V.mesh, det_order)
+    Kd = pkg.assemble_stiffness(Vd, p.C, list(range(Ms + 1)), 6)
+    D = rng.standard_normal((Vd.ndofs, S))
+    mesh = of.StructuredMesh(N)
+    Vo_det, Vo_sg = of.LagrangeSpace(mesh, det_order), of.LagrangeSpace(mesh, sg_order)
+    embeds = sg_order <= det_order
+    sp_ = pkg.SampleProblems(Vd, Kd, y)
+    for quadorder in (2, 4):
+        res = {}
+        for qf in ("1", "0"):
+            monkeypatch.setenv("SGFEM_SAMPLING_QF", qf)
+            res[qf] = sp_.sampling_error(p.sol, quadorder, det_solutions=D)
+            want = "quadratic forms" if (qf == "1" and embeds) else "quadrature points"
+            assert sp_.ctx.sampling_error_log == want, sp_.ctx.sampling_error_log
+        for k in range(2):
+            a, b = res["1"][k], res["0"][k]
+            assert np.max(np.abs(a - b) / np.abs(b)) <= 1e-12
+        eh, el = res["1"]
+        for s in (0, 13, 36):
+            for m in range(M + 1):
+                us = osm.sg_evaluate(p.sol.entries, p.n, TBo, y[:m, s])
+                h1, l2 = osm.error_integrals(Vo_det, D[:, s], Vo_sg, us, quadorder)
+                assert abs(eh[m, s] - h1) <= 1e-11 * h1
+                assert abs(el[m, s] - l2) <= 1e-11 * l2
+    sp_.close()
+
+
 def test_calculate_sampling_error_matches_oracle(built_pkg):
     """The whole driver: batched device solves (3 batches, last one padded) and
     the weighted / uniform means against the oracle's direct solves."""
