@@ -20,6 +20,7 @@
 // for phase 2.  Per-block FP64 partials of X .* Y (the p'Ap of CG) are fused
 // into the epilogue.
 #include <algorithm>
+#include <cstring>
 
 #include "sgfem_internal.h"
 
@@ -266,6 +267,58 @@ k_apply_samples_pre(const int* __restrict__ rowptr, const int* __restrict__ col,
     }
 }
 
+// the same with V consecutive samples per lane (16-byte loads: float4 / double2; ld is
+// a multiple of 4): four times the bytes in flight per load instruction.  Per sample
+// the nonzeros are summed in the same order as above.
+template <typename T, int V> struct SampleVec;
+template <> struct SampleVec<float, 4> { using type = float4; };
+template <> struct SampleVec<double, 2> { using type = double2; };
+
+template <typename T, int V>
+__global__ void __launch_bounds__(128)
+k_apply_samples_pre_v(const int* __restrict__ rowptr, const int* __restrict__ col, const T* __restrict__ kval,
+                      const T* __restrict__ X, T* __restrict__ Y, int n, int ld, const unsigned char* __restrict__ bmask,
+                      double* __restrict__ partials, const KrylovScalars* __restrict__ scal) {
+    using VT = typename SampleVec<T, V>::type;
+    if (scal && scal->done) return;
+    __shared__ double red[4];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nchunk = (ld + 32 * V - 1) / (32 * V);
+    const long long items = (long long)n * nchunk;
+    double dot = 0.0;
+    for (long long it = (long long)blockIdx.x * 4 + warp; it < items; it += (long long)gridDim.x * 4) {
+        const int row = (int)(it / nchunk), ch = (int)(it - (long long)row * nchunk);
+        const int s = (ch * 32 + lane) * V;
+        if (s >= ld) continue;
+        T acc[V];
+#pragma unroll
+        for (int c = 0; c < V; ++c) acc[c] = T(0);
+        if (!bmask[row]) {
+            const int nz1 = rowptr[row + 1];
+            for (int nz = rowptr[row]; nz < nz1; ++nz) {
+                T k[V], x[V];
+                *reinterpret_cast<VT*>(k) = *reinterpret_cast<const VT*>(kval + (size_t)nz * ld + s);
+                *reinterpret_cast<VT*>(x) = *reinterpret_cast<const VT*>(X + (size_t)col[nz] * ld + s);
+#pragma unroll
+                for (int c = 0; c < V; ++c) acc[c] = fma(k[c], x[c], acc[c]);
+            }
+        }
+        *reinterpret_cast<VT*>(Y + (size_t)row * ld + s) = *reinterpret_cast<const VT*>(acc);
+        if (partials) {
+            T xr[V];
+            *reinterpret_cast<VT*>(xr) = *reinterpret_cast<const VT*>(X + (size_t)row * ld + s);
+#pragma unroll
+            for (int c = 0; c < V; ++c) dot += (double)xr[c] * (double)acc[c];
+        }
+    }
+    if (partials) {
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
+        if (lane == 0) red[warp] = dot;
+        __syncthreads();
+        if (threadIdx.x == 0) partials[blockIdx.x] = red[0] + red[1] + red[2] + red[3];
+    }
+}
+
 // K(y_s)[nz] = sum_m y_{s,m} K_m[nz] in FP64, in the order the on-the-fly kernel sums
 // (so the FP64 apply is unchanged bit for bit); the FP32 copy rounds the FP64 sum
 __global__ void k_combine_samples(const double* __restrict__ vals, int M1, const double* __restrict__ y, long long nnz,
@@ -279,6 +332,46 @@ __global__ void k_combine_samples(const double* __restrict__ vals, int M1, const
             for (int m = 0; m < M1; ++m) c = fma(y[(size_t)s * M1 + m], vals[(size_t)nz * M1 + m], c);
         k64[t] = c;
         k32[t] = (float)c;
+    }
+}
+
+// (hi, lo) float pairs of doubles: hi = fl(x), lo = fl(x - hi), ~48 significant bits
+__global__ void k_split_hilo(const double* __restrict__ v, float2* __restrict__ o, long long n) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const double x = v[t];
+        const float h = __double2float_rn(x);
+        o[t] = make_float2(h, __double2float_rn(x - (double)h));
+    }
+}
+
+// K(y_s)[nz] in double-FP32 on the FP32 pipe (FP64 FMAs run at 1/64 of the FP32 rate
+// here): per term the exact product of the hi parts (p = a b, e = fma(a, b, -p)) plus
+// the cross terms, summed by an error-free two-sum into (hi, lo); relative error of the
+// sum ~2^-46 of sum_m |y_{s,m} K_m[nz]|.  Terms in m order, so results are reproducible.
+__global__ void k_combine_samples_df(const float2* __restrict__ vhl, int M1, const float2* __restrict__ yhl,
+                                     long long nnz, int S, int ld, double* __restrict__ k64, float* __restrict__ k32) {
+    const long long total = nnz * ld;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        const long long nz = t / ld;
+        const int s = (int)(t - nz * ld);
+        float sh = 0.0f, sl = 0.0f;
+        if (s < S)
+            for (int m = 0; m < M1; ++m) {
+                const float2 a = vhl[(size_t)nz * M1 + m], b = yhl[(size_t)s * M1 + m];
+                const float p = __fmul_rn(a.x, b.x);
+                float e = __fmaf_rn(a.x, b.x, -p);
+                e = __fmaf_rn(a.x, b.y, e);
+                e = __fmaf_rn(a.y, b.x, e);
+                const float u = __fadd_rn(sh, p);
+                const float bv = __fsub_rn(u, sh);
+                const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(u, bv)), __fsub_rn(p, bv));
+                sl = __fadd_rn(sl, __fadd_rn(err, e));
+                sh = u;
+            }
+        const float h = __fadd_rn(sh, sl);
+        const float l = __fsub_rn(sl, __fsub_rn(h, sh));
+        k64[t] = (double)h + (double)l;
+        k32[t] = h;
     }
 }
 
@@ -314,8 +407,25 @@ int sg_samples_combine(sgfem_context* ctx) {
         SG_CUDA(ctx, cudaMalloc((void**)&ctx->d_kval32, std::max<size_t>(count, 1) * sizeof(float)));
     }
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)count + 255) / 256, (int64_t)ctx->num_sms * 16));
-    k_combine_samples<<<grid, 256, 0, ctx->stream>>>(ctx->d_val64, ctx->M1, ctx->d_y64, (long long)ctx->nnz,
-                                                     (int)ctx->P, (int)ctx->ld, ctx->d_kval64, ctx->d_kval32);
+    const char* ecb = getenv("SGFEM_SAMPLES_COMBINE");
+    if (ecb && std::strcmp(ecb, "fp64") == 0) {  // exactly rounded FP64 sums on the FP64 pipe
+        k_combine_samples<<<grid, 256, 0, ctx->stream>>>(ctx->d_val64, ctx->M1, ctx->d_y64, (long long)ctx->nnz,
+                                                         (int)ctx->P, (int)ctx->ld, ctx->d_kval64, ctx->d_kval32);
+        SG_LAUNCHED(ctx);
+        return SGFEM_OK;
+    }
+    const long long nv = (long long)ctx->nnz * ctx->M1, ny = (long long)ctx->P * ctx->M1;
+    SG_TRY(sg_ensure(ctx, ctx->w_valhl, (size_t)std::max<long long>(nv, 1) * sizeof(float2)));
+    SG_TRY(sg_ensure(ctx, ctx->w_yhl, (size_t)std::max<long long>(ny, 1) * sizeof(float2)));
+    const int gs = (int)std::max<long long>(1, std::min<long long>((nv + 255) / 256, (long long)ctx->num_sms * 16));
+    k_split_hilo<<<gs, 256, 0, ctx->stream>>>(ctx->d_val64, (float2*)ctx->w_valhl.p, nv);
+    SG_LAUNCHED(ctx);
+    k_split_hilo<<<(int)std::max<long long>(1, (ny + 255) / 256), 256, 0, ctx->stream>>>(ctx->d_y64,
+                                                                                       (float2*)ctx->w_yhl.p, ny);
+    SG_LAUNCHED(ctx);
+    k_combine_samples_df<<<grid, 256, 0, ctx->stream>>>((const float2*)ctx->w_valhl.p, ctx->M1,
+                                                        (const float2*)ctx->w_yhl.p, (long long)ctx->nnz, (int)ctx->P,
+                                                        (int)ctx->ld, ctx->d_kval64, ctx->d_kval32);
     SG_LAUNCHED(ctx);
     return SGFEM_OK;
 }
@@ -326,6 +436,25 @@ int sg_launch_apply_samples(sgfem_context* ctx, int precision, const void* X, vo
     int grid = (int)std::min<int64_t>((items + 3) / 4, (int64_t)ctx->num_sms * 8);
     if (grid < 1) grid = 1;
     if (nblocks) *nblocks = grid;
+    const char* evec = getenv("SGFEM_SAMPLES_VEC");
+    if (ctx->d_kval64 && ctx->ld % 4 == 0 && !(evec && atoi(evec) == 0)) {
+        const int V = precision == SGFEM_FP64 ? 2 : 4;
+        const int64_t vitems = ctx->n * ((ctx->ld + 32 * V - 1) / (32 * V));
+        grid = (int)std::max<int64_t>(1, std::min<int64_t>((vitems + 3) / 4, (int64_t)ctx->num_sms * 8));
+        if (nblocks) *nblocks = grid;
+        if (precision == SGFEM_FP64)
+            k_apply_samples_pre_v<double, 2><<<grid, 128, 0, ctx->stream>>>(ctx->d_rowptr, ctx->d_col, ctx->d_kval64,
+                                                                            (const double*)X, (double*)Y, (int)ctx->n,
+                                                                            (int)ctx->ld, ctx->d_bmask, dot_partials,
+                                                                            skip_if_done);
+        else
+            k_apply_samples_pre_v<float, 4><<<grid, 128, 0, ctx->stream>>>(ctx->d_rowptr, ctx->d_col, ctx->d_kval32,
+                                                                           (const float*)X, (float*)Y, (int)ctx->n,
+                                                                           (int)ctx->ld, ctx->d_bmask, dot_partials,
+                                                                           skip_if_done);
+        SG_LAUNCHED(ctx);
+        return SGFEM_OK;
+    }
     if (ctx->d_kval64) {
         if (precision == SGFEM_FP64)
             k_apply_samples_pre<double><<<grid, 128, 0, ctx->stream>>>(ctx->d_rowptr, ctx->d_col, ctx->d_kval64,

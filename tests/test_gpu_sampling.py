@@ -34,6 +34,30 @@ def test_sample_solves_match_direct(built_pkg, precision):
     sp_.close()
 
 
+def test_sample_operator_forms_agree(built_pkg, monkeypatch):
+    """The sample operators K(y_s) combined in double-FP32 and applied four samples per
+    lane (default) against the exactly rounded FP64 combination applied one sample per
+    lane (SGFEM_SAMPLES_COMBINE=fp64, SGFEM_SAMPLES_VEC=0): the same solutions to 1e-9
+    in both precisions, all within 1e-8 of the oracle's direct solves (an operator off
+    at FP32 level, 1e-7, would miss both bars)."""
+    pkg, C, V, Ks, b0, y = det_setup(N=16, order=2, M=20, S=40)
+    res = {}
+    for comb, vec in (("df", "1"), ("fp64", "0")):
+        monkeypatch.setenv("SGFEM_SAMPLES_COMBINE", comb)
+        monkeypatch.setenv("SGFEM_SAMPLES_VEC", vec)
+        for prec in ("FP64", "MIXED"):
+            sp_ = pkg.SampleProblems(V, Ks, y)
+            res[comb, prec] = sp_.solve(b0, rtol=1e-12, precision=getattr(pkg, prec))
+            sp_.close()
+    for prec in ("FP64", "MIXED"):
+        a, b = res["df", prec], res["fp64", prec]
+        assert np.linalg.norm(a - b) <= 1e-9 * np.linalg.norm(b), prec
+    for s in (0, 39):
+        ref = osm.deterministic_solve(Ks, b0, V.bdofs, y[:, s])
+        for key, U in res.items():
+            assert np.linalg.norm(U[:, s] - ref) <= 1e-8 * np.linalg.norm(ref), key
+
+
 def test_sample_solves_p1_odd_count(built_pkg):
     pkg, C, V, Ks, b0, y = det_setup(N=32, order=1, M=5, S=37)
     sp_ = pkg.SampleProblems(V, Ks, y)
@@ -134,7 +158,8 @@ def test_sampling_error_forms_match_oracle(built_pkg, monkeypatch, sg_order, det
     """The error sums as quadratic forms in the error's local coefficients (the SG
     space embeds in the deterministic one: P1 in P2, equal orders) and point by point
     (no embedding, or SGFEM_SAMPLING_QF=0): both against the oracle's point-by-point
-    sums (1e-11 per (m, s)) and against each other (1e-12), for 4- and 6-point rules."""
+    sums (1e-11 per (m, s)) and against each other (1e-12), for the 3- and 9-point rules
+    of orders 2 and 4."""
     import __graft_entry__ as ge
     pkg = ge.load_package()
     M, N, Ms, S = 3, 8, 5, 37
