@@ -101,6 +101,7 @@ extern "C" int sgfem_destroy(sgfem_context* ctx) {
     free_dev(ctx->w_gsmall.p);
     free_dev(ctx->w_valhl.p);
     free_dev(ctx->w_yhl.p);
+    free_dev(ctx->w_samp.p);
     if (ctx->h_scal) cudaFreeHost(ctx->h_scal);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);

@@ -356,31 +356,39 @@ __global__ void k_sampling_reduce(const double* __restrict__ part, int groups, i
     ((mh & 1) ? el : eh)[(size_t)s * (M + 1) + m] = v;
 }
 
-struct Owned {
-    std::vector<void*> p;
-    ~Owned() {
-        for (void* q : p) cudaFree(q);
+// The arrays of one call packed at 256-byte offsets into a context buffer that only
+// grows: no cudaMalloc / cudaFree (which synchronises the device) per call.  Host
+// sources stay alive until the call's final stream synchronisation.
+struct Pack {
+    struct Item {
+        const void* src;  // nullptr: scratch
+        size_t bytes;
+        void** dst;
+    };
+    std::vector<Item> items;
+    template <typename T>
+    void up(const T* src, size_t n, T** dst) {
+        items.push_back({src, n * sizeof(T), (void**)dst});
+    }
+    template <typename T>
+    void scratch(size_t n, T** dst) {
+        items.push_back({nullptr, n * sizeof(T), (void**)dst});
+    }
+    static size_t pad(size_t b) { return (std::max<size_t>(b, 1) + 255) / 256 * 256; }
+    int commit(sgfem_context* ctx, DeviceBuf& buf) {
+        size_t total = 0;
+        for (const Item& it : items) total += pad(it.bytes);
+        SG_TRY(sg_ensure(ctx, buf, total));
+        size_t off = 0;
+        for (const Item& it : items) {
+            *it.dst = (char*)buf.p + off;
+            if (it.src && it.bytes)
+                SG_CUDA(ctx, cudaMemcpyAsync(*it.dst, it.src, it.bytes, cudaMemcpyHostToDevice, ctx->stream));
+            off += pad(it.bytes);
+        }
+        return SGFEM_OK;
     }
 };
-
-template <typename T>
-int up(sgfem_context* ctx, Owned& o, const T* src, size_t n, T** dst) {
-    void* p = nullptr;
-    SG_CUDA(ctx, cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
-    o.p.push_back(p);
-    if (n) SG_CUDA(ctx, cudaMemcpyAsync(p, src, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
-    *dst = (T*)p;
-    return SGFEM_OK;
-}
-
-template <typename T>
-int scratch(sgfem_context* ctx, Owned& o, size_t n, T** dst) {
-    void* p = nullptr;
-    SG_CUDA(ctx, cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
-    o.p.push_back(p);
-    *dst = (T*)p;
-    return SGFEM_OK;
-}
 
 // checks of the basis description; sup[k] = last dimension (1-based) with mu_k[d] > 0
 int check_basis(sgfem_context* ctx, const sgfem_sg_basis* b, std::vector<int>& sup) {
@@ -511,18 +519,19 @@ extern "C" int sgfem_evaluate_samples(sgfem_context* ctx, const double* U, int64
     for (int64_t t = 0; t < Ms * S; ++t)
         if (!std::isfinite(y[t])) return sg_fail(ctx, SGFEM_ERR_NONFINITE, "non-finite sample");
     SG_CUDA(ctx, cudaSetDevice(ctx->device));
-    Owned o;
+    Pack pk;
     const int lds = (int)((S + 31) / 32 * 32);
     std::vector<int> mi(basis->multi_indices, basis->multi_indices + basis->P * basis->M);
     int* d_mi;
     double *d_rec, *d_norms, *d_y, *d_U, *d_psi, *d_out;
-    SG_TRY(up(ctx, o, mi.data(), mi.size(), &d_mi));
-    SG_TRY(up(ctx, o, basis->recurrence, (size_t)3 * basis->maxorder, &d_rec));
-    SG_TRY(up(ctx, o, basis->norms, (size_t)basis->maxorder + 1, &d_norms));
-    SG_TRY(up(ctx, o, y, (size_t)(Ms * S), &d_y));
-    SG_TRY(up(ctx, o, U, (size_t)(n * basis->P), &d_U));
-    SG_TRY(scratch(ctx, o, (size_t)basis->P * lds, &d_psi));
-    SG_TRY(scratch(ctx, o, (size_t)(n * S), &d_out));
+    pk.up(mi.data(), mi.size(), &d_mi);
+    pk.up(basis->recurrence, (size_t)3 * basis->maxorder, &d_rec);
+    pk.up(basis->norms, (size_t)basis->maxorder + 1, &d_norms);
+    pk.up(y, (size_t)(Ms * S), &d_y);
+    pk.up(U, (size_t)(n * basis->P), &d_U);
+    pk.scratch((size_t)basis->P * lds, &d_psi);
+    pk.scratch((size_t)(n * S), &d_out);
+    SG_TRY(pk.commit(ctx, ctx->w_samp));
     // dimensions beyond Ms count as truncated: m <= Ms, so d < m only reads stored dimensions
     SG_TRY(launch_psi(ctx, basis, d_mi, d_rec, d_norms, d_y, (int)Ms, 0, (int)m, (int)S, d_psi, lds));
     dim3 grid((unsigned)((n + 63) / 64), (unsigned)((S + 63) / 64));
@@ -616,45 +625,31 @@ extern "C" int sgfem_sampling_error(sgfem_context* ctx, const double* det_soluti
     sgfem_sg_basis sorted = *basis;
     sorted.multi_indices = mi.data();
 
-    Owned o;
     const int lds = (int)((S + 31) / 32 * 32);
-    int *d_mi, *d_kptr, *d_dd, *d_sd;
-    double *d_rec, *d_norms, *d_U, *d_psi, *d_xq, *d_wq, *d_part, *d_eh, *d_el;
-    SCell* d_cg;
-    SG_TRY(up(ctx, o, mi.data(), mi.size(), &d_mi));
-    SG_TRY(up(ctx, o, basis->recurrence, (size_t)3 * basis->maxorder, &d_rec));
-    SG_TRY(up(ctx, o, basis->norms, (size_t)basis->maxorder + 1, &d_norms));
-    SG_TRY(up(ctx, o, Us.data(), Us.size(), &d_U));
-    SG_TRY(up(ctx, o, kptr.data(), kptr.size(), &d_kptr));
-    SG_TRY(up(ctx, o, cg.data(), cg.size(), &d_cg));
-    SG_TRY(up(ctx, o, ddofs.data(), ddofs.size(), &d_dd));
-    SG_TRY(up(ctx, o, sdofs.data(), sdofs.size(), &d_sd));
-    SG_TRY(up(ctx, o, quad->xref, (size_t)2 * nq, &d_xq));
-    SG_TRY(up(ctx, o, quad->w, (size_t)nq, &d_wq));
-    SG_TRY(scratch(ctx, o, (size_t)P * lds, &d_psi));
-    // Psi at the full sample y[1:M]: the context's rows are [S][M1] with y_{s,0} = 1 first
-    SG_TRY(launch_psi(ctx, &sorted, d_mi, d_rec, d_norms, ctx->d_y64, ctx->M1, 1, (int)M, (int)S, d_psi, lds));
-
     const int chunks = (int)((S + 31) / 32);
     const int target = std::max(1, ctx->num_sms) * 16;
     const int groups = (int)std::max<int64_t>(1, std::min<int64_t>(nc, (target + chunks - 1) / chunks));
     const int64_t warps = (int64_t)groups * chunks;
     const int blocks = (int)((warps + SW - 1) / SW);
     const size_t per = (size_t)(M + 1) * 2 * S;
-    SG_TRY(scratch(ctx, o, per * groups, &d_part));
-    SG_TRY(scratch(ctx, o, (size_t)(M + 1) * S, &d_eh));
-    SG_TRY(scratch(ctx, o, (size_t)(M + 1) * S, &d_el));
     // quadratic forms where the SG space embeds in the deterministic one (SGFEM_SAMPLING_QF=0:
     // the quadrature kernel always)
     std::vector<double> E, Mq, Rs;
     const char* eqf = getenv("SGFEM_SAMPLING_QF");
-    const bool qf = !(eqf && atoi(eqf) == 0) && quadform_tables(mesh->order, sg_space->order, nq, quad->xref, quad->w,
-                                                                 E, Mq, Rs);
+    bool qf = !(eqf && atoi(eqf) == 0) && quadform_tables(mesh->order, sg_space->order, nq, quad->xref, quad->w, E, Mq, Rs);
     const size_t smem_qf = sizeof(double) * ((size_t)ndd * nds + Mq.size() + (size_t)SW * (M + 1) * 2 * 32);
-    if (qf && smem_qf <= 227 * 1024) {
-        const int nt = ndd * (ndd + 1) / 2;
+    qf = qf && smem_qf <= 227 * 1024;
+    const size_t smem = sizeof(double) * ((size_t)nq * (ndd + nds + 1) +
+                                          (size_t)SW * (nq * 2 * (ndd + nds) + nq * 3 * 32 + (M + 1) * 2 * 32));
+    if (!qf && smem > 227 * 1024)
+        return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED,
+                       "sampling error: too many truncation levels or quadrature points for shared memory");
+    const int nt = ndd * (ndd + 1) / 2;
+    std::vector<double> KT, vol;
+    if (qf) {
         const int kk[6] = {0, 1, 2, 0, 0, 1}, ll[6] = {0, 1, 2, 1, 2, 2};
-        std::vector<double> KT((size_t)nc * nt), vol(nc);
+        KT.resize((size_t)nc * nt);
+        vol.resize(nc);
         for (int64_t c = 0; c < nc; ++c) {
             const double* g = cg[c].g;
             double G[6];
@@ -666,11 +661,38 @@ extern "C" int sgfem_sampling_error(sgfem_context* ctx, const double* det_soluti
             }
             vol[c] = cg[c].vol;
         }
-        double *d_KT, *d_vol, *d_E, *d_Mq;
-        SG_TRY(up(ctx, o, KT.data(), KT.size(), &d_KT));
-        SG_TRY(up(ctx, o, vol.data(), vol.size(), &d_vol));
-        SG_TRY(up(ctx, o, E.data(), E.size(), &d_E));
-        SG_TRY(up(ctx, o, Mq.data(), Mq.size(), &d_Mq));
+    }
+
+    Pack pk;
+    int *d_mi, *d_kptr, *d_dd, *d_sd;
+    double *d_rec, *d_norms, *d_U, *d_psi, *d_xq, *d_wq, *d_part, *d_eh, *d_el;
+    double *d_KT = nullptr, *d_vol = nullptr, *d_E = nullptr, *d_Mq = nullptr;
+    SCell* d_cg;
+    pk.up(mi.data(), mi.size(), &d_mi);
+    pk.up(basis->recurrence, (size_t)3 * basis->maxorder, &d_rec);
+    pk.up(basis->norms, (size_t)basis->maxorder + 1, &d_norms);
+    pk.up(Us.data(), Us.size(), &d_U);
+    pk.up(kptr.data(), kptr.size(), &d_kptr);
+    pk.up(ddofs.data(), ddofs.size(), &d_dd);
+    pk.up(sdofs.data(), sdofs.size(), &d_sd);
+    pk.scratch((size_t)P * lds, &d_psi);
+    pk.scratch(per * groups, &d_part);
+    pk.scratch((size_t)(M + 1) * S, &d_eh);
+    pk.scratch((size_t)(M + 1) * S, &d_el);
+    if (qf) {
+        pk.up(KT.data(), KT.size(), &d_KT);
+        pk.up(vol.data(), vol.size(), &d_vol);
+        pk.up(E.data(), E.size(), &d_E);
+        pk.up(Mq.data(), Mq.size(), &d_Mq);
+    } else {
+        pk.up(cg.data(), cg.size(), &d_cg);
+        pk.up(quad->xref, (size_t)2 * nq, &d_xq);
+        pk.up(quad->w, (size_t)nq, &d_wq);
+    }
+    SG_TRY(pk.commit(ctx, ctx->w_samp));
+    // Psi at the full sample y[1:M]: the context's rows are [S][M1] with y_{s,0} = 1 first
+    SG_TRY(launch_psi(ctx, &sorted, d_mi, d_rec, d_norms, ctx->d_y64, ctx->M1, 1, (int)M, (int)S, d_psi, lds));
+    if (qf) {
         QfArgs b{};
         b.ncells = (int)nc;
         b.S = (int)S;
@@ -698,11 +720,6 @@ extern "C" int sgfem_sampling_error(sgfem_context* ctx, const double* det_soluti
         ctx->sampling_form = 1;
     } else {
         ctx->sampling_form = 2;
-        const size_t smem = sizeof(double) * ((size_t)nq * (ndd + nds + 1) +
-                                              (size_t)SW * (nq * 2 * (ndd + nds) + nq * 3 * 32 + (M + 1) * 2 * 32));
-        if (smem > 227 * 1024)
-            return sg_fail(ctx, SGFEM_ERR_UNSUPPORTED,
-                           "sampling error: too many truncation levels or quadrature points for shared memory");
         ErrArgs a{};
         a.od = mesh->order;
         a.os = sg_space->order;

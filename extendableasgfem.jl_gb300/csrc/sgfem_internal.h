@@ -77,6 +77,7 @@ struct sgfem_context {
     float* d_kval32 = nullptr;
     DeviceBuf w_valhl;           // K_m values as (hi, lo) float pairs for the double-FP32 combination
     DeviceBuf w_yhl;             // sample coefficients as (hi, lo) float pairs
+    DeviceBuf w_samp;            // arrays of the last sgfem_evaluate_samples / sgfem_sampling_error
     bool samples_x_valid = false;  // w_vec[10] holds the solutions of the current samples
     int sampling_form = 0;         // last sgfem_sampling_error: 0 none, 1 quadratic forms, 2 quadrature points
     std::vector<int64_t> bdofs;  // 0-based caller numbering
