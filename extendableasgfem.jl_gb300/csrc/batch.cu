@@ -46,6 +46,17 @@ struct BProb {
     const float* vals32;          // FP32 copies for the inner PCG of the mixed solve
     const float* combg32;
     const float* dinv32;
+    // column-slot form of the apply (k_bapply_cols): passes over virtual groups of 32
+    // columns, each lane taking its column's KLE terms from the lanes that hold them
+    int npass, nf;                // passes; pair sums per warp (floats or doubles)
+    const int4* cpass;            // FP32 passes: (kind, first virtual group, groups, 0)
+    const int4* cpass64;          // FP64 passes (fewer groups per pass: register budget)
+    int npass64;
+    const int* vgcol;             // first column of each virtual group (multiple of 32)
+    const int* vgfoff;            // offset of its pair sums in the per-warp area
+    const int* vgsrc;             // offset of its source lanes in src (slots x 32)
+    const unsigned char* src;     // per slot and lane: the lane holding the term's value (31: zero)
+    const int* combf;             // per combination entry: the pair sum's place in the area
 };
 
 template <typename T> __device__ __forceinline__ const T* bvals(const BProb& d);
@@ -101,7 +112,11 @@ struct sgfem_batch {
     int blocks = 0, wpb = 4, qt = 4, ldmax = 0, m1max = 0, qnmax = 0;
     int wpb32 = 4, qt32 = 8;      // launch shape of the FP32 apply (mixed solve)
     int pf32 = 0;                 // bit 0: the FP32 apply prefetches the next nonzero into registers;
-                                  // bit 1: persistent grid over the work queue
+                                  // bit 1: persistent grid over the work queue;
+                                  // bit 2: column-slot form (k_bapply_cols)
+    int pf64 = 0, wpb64c = 4;     // FP64 apply: 4 = column-slot form with wpb64c warps per block
+    bool cols_ok = false;         // every problem has M + 1 <= 31 (the column-slot form applies)
+    int nfmax = 0;                // largest per-warp pair-sum area of the column-slot form
     std::string tuning;
     std::vector<KrylovScalars> h_scal;
     double rtol = 0.0;            // of the last solve
@@ -298,6 +313,179 @@ __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict_
         }
         __syncthreads();  // red is free before the next item
     }
+    }
+}
+
+// ---- column-slot form of the apply: the same Y = S X, scheduled by columns.
+// Lane L of a virtual group owns column vgcol + L and keeps NA pair sums
+// F[(m, c)] = sum_j K_m[i, j] X[j, c] in registers, one per slot; the M + 1 values of
+// a nonzero sit one per lane (lane m holds K_m[i, j], lanes >= M + 1 hold 0) and each
+// slot takes its term's value from the lane named by the schedule (__shfl_sync), so
+// a lane whose column couples to few terms and one coupled to all of them share the
+// instruction stream without a shared-memory gather per pair.  A pass holds GP groups
+// of one kind; X[j, c] is read once per group and nonzero (coalesced, the next
+// nonzero's values in flight while the current one is used).  After the passes the
+// pair sums go to the warp's shared area and each output column is combined from its
+// list (K_0 pair with g = 1, then the G entries) as in k_bapply.
+// kinds: slots per lane 1, 2, 4, 8, 16; groups per pass keep the pair sums of a pass at
+// <= 32 registers (FP32) or <= 16 doubles (FP64)
+__host__ __device__ constexpr int cols_na(int kind) { return kind == 0 ? 1 : kind == 1 ? 2 : kind == 2 ? 4 : kind == 3 ? 8 : 16; }
+__host__ __device__ constexpr int cols_gp(int kind, int es) {
+    return es == 4 ? (kind <= 2 ? 8 : kind == 3 ? 4 : 2) : (kind <= 1 ? 8 : kind == 2 ? 4 : kind == 3 ? 2 : 1);
+}
+
+template <typename T, int NA, int GP>
+__device__ __forceinline__ void cols_pass(const BProb& d, const T* __restrict__ Xp, const T* __restrict__ vals,
+                                          int nz0, int nz1, int vg0, int ng, T* __restrict__ sacc, int lane) {
+    // groups g >= ng of a short pass read lane 31 (zero) in every slot; columns past the
+    // row are clamped into it (their slots read zero too), so the loops below have no
+    // per-group or per-nonzero branch
+    int src[GP][NA];
+    int cbc[GP];
+    T acc[GP][NA];
+#pragma unroll
+    for (int g = 0; g < GP; ++g) {
+        const bool on = g < ng;
+        const int vg = vg0 + (on ? g : 0);
+        cbc[g] = min(d.vgcol[vg] + lane, d.ld - 1);
+        const unsigned char* sp = d.src + d.vgsrc[vg] + lane;
+#pragma unroll
+        for (int s = 0; s < NA; ++s) {
+            src[g][s] = on ? (int)sp[32 * s] : 31;
+            acc[g][s] = T(0);
+        }
+    }
+    // the row's nonzeros in chunks of CH: lane t holds the column of nonzero base + t and
+    // lane m the K_m value of each (zero past the row's end, whose column reads row 0),
+    // so the X loads of a chunk depend on no other load; they are issued two nonzeros
+    // ahead of their FMAs
+    constexpr int CH = 8;
+    for (int base = nz0; base < nz1; base += CH) {
+        const int cnt = min(CH, nz1 - base);
+        const int jl = lane < cnt ? __ldg(d.col + base + lane) : 0;
+        T kr[CH];
+#pragma unroll
+        for (int t = 0; t < CH; ++t) kr[t] = (t < cnt && lane < d.M1) ? vals[(size_t)(base + t) * d.M1 + lane] : T(0);
+        T ux[CH][GP];
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+            const T* xr = Xp + (size_t)__shfl_sync(0xffffffffu, jl, t) * d.ld;
+#pragma unroll
+            for (int g = 0; g < GP; ++g) ux[t][g] = __ldg(xr + cbc[g]);
+        }
+#pragma unroll
+        for (int t = 0; t < CH; ++t) {
+            if (t + 2 < CH) {
+                const T* xr = Xp + (size_t)__shfl_sync(0xffffffffu, jl, t + 2) * d.ld;
+#pragma unroll
+                for (int g = 0; g < GP; ++g) ux[t + 2][g] = __ldg(xr + cbc[g]);
+            }
+#pragma unroll
+            for (int g = 0; g < GP; ++g)
+#pragma unroll
+                for (int s = 0; s < NA; ++s)
+                    acc[g][s] = fma(__shfl_sync(0xffffffffu, kr[t], src[g][s]), ux[t][g], acc[g][s]);
+        }
+    }
+#pragma unroll
+    for (int g = 0; g < GP; ++g) {
+        if (g < ng) {
+            T* o = sacc + d.vgfoff[vg0 + g] + lane;
+#pragma unroll
+            for (int s = 0; s < NA; ++s) o[32 * s] = acc[g][s];
+        }
+    }
+}
+
+// work items as in k_bapply (block map or persistent queue); per_warp = largest area
+template <typename T>
+__global__ void k_bapply_cols(const BProb* __restrict__ probs, const int* __restrict__ bprob, const T* __restrict__ X,
+                              T* __restrict__ Y, double* __restrict__ partials, const KrylovScalars* __restrict__ scal,
+                              int per_warp, const int* __restrict__ vorder, int* __restrict__ wq, int nvb) {
+    __shared__ int s_item;
+    extern __shared__ __align__(16) unsigned char bsm_raw[];
+    T* bsm = reinterpret_cast<T*>(bsm_raw);
+    const int wpb = blockDim.x >> 5;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int round = 0;; ++round) {
+        int vb;
+        if (wq) {
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                const int k = atomicAdd(wq, 1);
+                s_item = k < nvb ? vorder[k] : -1;
+            }
+            __syncthreads();
+            vb = s_item;
+            if (vb < 0) break;
+        } else {
+            if (round > 0) break;
+            vb = blockIdx.x;
+        }
+        const int pi = bprob[vb];
+        const BProb& d = probs[pi];
+        const T* vals = bvals<T>(d);
+        const T* combg = bcombg<T>(d);
+        if (scal && scal[pi].done) {
+            if (threadIdx.x == 0 && partials) partials[vb] = 0.0;
+            continue;
+        }
+        T* sacc = bsm + (size_t)warp * per_warp;
+        const T* Xp = X + d.voff;
+        T* Yp = Y + d.voff;
+        double dot = 0.0;
+        const int lb = vb - d.blk0;
+        for (int row = lb * wpb + warp; row < d.n; row += d.nblk * wpb) {
+            T* yrow = Yp + (size_t)row * d.ld;
+            if (d.bmask[row]) {
+                for (int c = lane; c < d.ld; c += 32) yrow[c] = T(0);
+                continue;
+            }
+            const int nz0 = d.rowptr[row], nz1 = d.rowptr[row + 1];
+            constexpr int ES = (int)sizeof(T);
+            const int np = ES == 4 ? d.npass : d.npass64;
+            const int4* cp = ES == 4 ? d.cpass : d.cpass64;
+            for (int p = 0; p < np; ++p) {
+                const int4 ps = cp[p];
+                // passes of one group take the one-group form (no padding groups)
+                switch (2 * ps.x + (ps.z == 1)) {
+                    case 0: cols_pass<T, cols_na(0), cols_gp(0, ES)>(d, Xp, vals, nz0, nz1, ps.y, ps.z, sacc, lane); break;
+                    case 1: cols_pass<T, cols_na(0), 1>(d, Xp, vals, nz0, nz1, ps.y, 1, sacc, lane); break;
+                    case 2: cols_pass<T, cols_na(1), cols_gp(1, ES)>(d, Xp, vals, nz0, nz1, ps.y, ps.z, sacc, lane); break;
+                    case 3: cols_pass<T, cols_na(1), 1>(d, Xp, vals, nz0, nz1, ps.y, 1, sacc, lane); break;
+                    case 4: cols_pass<T, cols_na(2), cols_gp(2, ES)>(d, Xp, vals, nz0, nz1, ps.y, ps.z, sacc, lane); break;
+                    case 5: cols_pass<T, cols_na(2), 1>(d, Xp, vals, nz0, nz1, ps.y, 1, sacc, lane); break;
+                    case 6: cols_pass<T, cols_na(3), cols_gp(3, ES)>(d, Xp, vals, nz0, nz1, ps.y, ps.z, sacc, lane); break;
+                    case 7: cols_pass<T, cols_na(3), 1>(d, Xp, vals, nz0, nz1, ps.y, 1, sacc, lane); break;
+                    case 8: cols_pass<T, cols_na(4), cols_gp(4, ES)>(d, Xp, vals, nz0, nz1, ps.y, ps.z, sacc, lane); break;
+                    default: cols_pass<T, cols_na(4), 1>(d, Xp, vals, nz0, nz1, ps.y, 1, sacc, lane); break;
+                }
+            }
+            __syncwarp();
+            const T* xrow = Xp + (size_t)row * d.ld;
+            T rowdot = T(0);
+            for (int mu = lane; mu < d.ld; mu += 32) {
+                T y = T(0);
+                if (mu < d.P)
+                    for (int e = d.combptr[mu]; e < d.combptr[mu + 1]; ++e) y = fma(combg[e], sacc[d.combf[e]], y);
+                yrow[mu] = y;
+                rowdot = fma(xrow[mu], y, rowdot);
+            }
+            dot += (double)rowdot;
+            __syncwarp();  // the combination has read the area before the next row's passes
+        }
+        if (partials) {
+            __shared__ double red[32];
+            for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
+            if (lane == 0) red[warp] = dot;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double s = 0.0;
+                for (int w = 0; w < wpb; ++w) s += red[w];
+                partials[vb] = s;
+            }
+            __syncthreads();
+        }
     }
 }
 
@@ -595,21 +783,24 @@ int balloc(sgfem_batch* b, size_t bytes, void** dst) {
 }
 
 template <typename T = double>
-size_t apply_smem(const sgfem_batch* b, int wpb) {
+size_t apply_smem(const sgfem_batch* b, int wpb, int pf = 0) {
+    if (pf & 4) return (size_t)b->nfmax * sizeof(T) * wpb;
     const size_t per_warp = ((size_t)b->ldmax + b->m1max + 1 + b->qnmax + 3) & ~(size_t)3;
     return per_warp * sizeof(T) * wpb;
 }
 
 // pf bit 0: the prefetching variant (FP32, 16 or 32 pairs per lane); bit 1: persistent
-// grid over the work queue (resident blocks only, queue counter reset before the launch)
+// grid over the work queue (resident blocks only, queue counter reset before the launch);
+// bit 2: the column-slot form (qt unused)
 template <typename T>
 int launch_apply(sgfem_batch* b, int wpb, int qt, const T* X, T* Y, double* partials, const KrylovScalars* scal,
                  int pf = 0) {
-    const int per_warp = (int)(((size_t)b->ldmax + b->m1max + 1 + b->qnmax + 3) & ~(size_t)3);
-    const size_t smem = apply_smem<T>(b, wpb);
+    const int per_warp = (pf & 4) ? b->nfmax : (int)(((size_t)b->ldmax + b->m1max + 1 + b->qnmax + 3) & ~(size_t)3);
+    const size_t smem = apply_smem<T>(b, wpb, pf);
     using KF = void (*)(const BProb*, const int*, const T*, T*, double*, const KrylovScalars*, int, const int*, int*, int);
     KF kf;
-    if (pf & 1) kf = qt == 16 ? k_bapply<T, 16, true> : k_bapply<T, 32, true>;
+    if (pf & 4) kf = k_bapply_cols<T>;
+    else if (pf & 1) kf = qt == 16 ? k_bapply<T, 16, true> : k_bapply<T, 32, true>;
     else kf = qt == 4 ? k_bapply<T, 4> : qt == 8 ? k_bapply<T, 8> : qt == 16 ? k_bapply<T, 16> : k_bapply<T, 32>;
     int grid = b->blocks;
     int* wq = nullptr;
@@ -624,6 +815,26 @@ int launch_apply(sgfem_batch* b, int wpb, int qt, const T* X, T* Y, double* part
                                             b->blocks);
     BLAUNCHED(b);
     return SGFEM_OK;
+}
+
+// the apply kernel of a form and its shared-memory opt-in (above the 48 KB default)
+template <typename T>
+const void* apply_kernel(int pf, int qt) {
+    if (pf & 4) return (const void*)k_bapply_cols<T>;
+    if (pf & 1) return qt == 16 ? (const void*)k_bapply<T, 16, true> : (const void*)k_bapply<T, 32, true>;
+    return qt == 4 ? (const void*)k_bapply<T, 4> : qt == 8 ? (const void*)k_bapply<T, 8>
+         : qt == 16 ? (const void*)k_bapply<T, 16> : (const void*)k_bapply<T, 32>;
+}
+template <typename T>
+cudaError_t set_apply_smem(int pf, int qt, size_t smem) {
+    if (smem <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(apply_kernel<T>(pf, qt), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+// FP64 apply in the chosen form (pair passes or column slots)
+int apply64(sgfem_batch* b, const double* X, double* Y, double* partials, const KrylovScalars* scal) {
+    if (b->pf64 & 4) return launch_apply<double>(b, b->wpb64c, 0, X, Y, partials, scal, b->pf64);
+    return launch_apply<double>(b, b->wpb, b->qt, X, Y, partials, scal);
 }
 
 // the block map and the work-queue order (virtual blocks by descending rows x pairs each) to the device
@@ -663,13 +874,90 @@ int build_map(sgfem_batch* b, int total_blocks, std::vector<BProb>& probs, std::
     return SGFEM_OK;
 }
 
+// ---- schedule of the column-slot apply for one problem.  Column block b holds columns
+// 32 b + L; lane L's terms are the m with (m, column) in the pair list, in increasing m.
+// The block's longest list is cut into virtual groups of 16, 8, 4, 2 or 1 slots (a
+// remainder of 3 or 7 is rounded up to 4 or 8: one idle slot costs less than another
+// group); lanes with fewer terms, and columns >= P, read lane 31, which holds zero.
+// Passes take up to GP groups of one kind; the pair sums of the groups follow one
+// another in the warp's area in pass order.
+struct ColSched {
+    std::vector<int4> pass, pass64;
+    std::vector<int> vgcol, vgfoff, vgsrc, combf;
+    std::vector<unsigned char> src;
+    int nf = 0;
+};
+
+void build_cols(const sgfem_batch::HostProb& h, ColSched& cs) {
+    const int P = h.P, M1 = h.M1;
+    std::vector<std::vector<int>> terms(P);
+    for (int e : h.qtab) terms[e & 0xffff].push_back(e >> 16);
+    for (auto& t : terms) std::sort(t.begin(), t.end());
+    struct VG { int kind, col, first; };  // first: index of the lane's first term in this group
+    std::vector<VG> vgs;
+    for (int b0 = 0; b0 < P; b0 += 32) {
+        int amax = 0;
+        for (int c = b0; c < std::min(P, b0 + 32); ++c) amax = std::max(amax, (int)terms[c].size());
+        int first = 0, r = amax;
+        while (r > 0) {
+            int na = r >= 16 ? 16 : r >= 8 ? (r == 15 ? 16 : 8) : r >= 4 ? (r == 7 ? 8 : 4) : r >= 2 ? (r == 3 ? 4 : 2) : 1;
+            int kind = na == 1 ? 0 : na == 2 ? 1 : na == 4 ? 2 : na == 8 ? 3 : 4;
+            vgs.push_back({kind, b0, first});
+            first += na;
+            r -= std::min(r, na);
+        }
+    }
+    // passes: groups of one kind, in column order within the kind
+    std::vector<int> order(vgs.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return vgs[a].kind < vgs[b].kind; });
+    std::vector<int> pairpos((size_t)M1 * P, -1);  // (m, nu) -> place in the per-warp area
+    cs = ColSched{};
+    std::vector<int> kinds;
+    for (int k : order) {
+        const VG& v = vgs[k];
+        const int na = cols_na(v.kind);
+        kinds.push_back(v.kind);
+        cs.vgcol.push_back(v.col);
+        cs.vgfoff.push_back(cs.nf);
+        cs.vgsrc.push_back((int)cs.src.size());
+        for (int s = 0; s < na; ++s)
+            for (int L = 0; L < 32; ++L) {
+                const int c = v.col + L;
+                const int t = v.first + s;
+                int m = 31;
+                if (c < P && t < (int)terms[c].size()) {
+                    m = terms[c][t];
+                    pairpos[(size_t)m * P + c] = cs.nf + 32 * s + L;
+                }
+                cs.src.push_back((unsigned char)m);
+            }
+        cs.nf += 32 * na;
+    }
+    for (int es : {4, 8}) {
+        auto& pass = es == 4 ? cs.pass : cs.pass64;
+        for (size_t k = 0; k < kinds.size();) {
+            const int kind = kinds[k], gp = cols_gp(kind, es);
+            int ng = 0;
+            while (k + ng < kinds.size() && kinds[k + ng] == kind && ng < gp) ++ng;
+            pass.push_back(make_int4(kind, (int)k, ng, 0));
+            k += ng;
+        }
+    }
+    cs.combf.resize(h.combq.size());
+    for (size_t e = 0; e < h.combq.size(); ++e) {
+        const int q = h.qtab[h.combq[e]];
+        cs.combf[e] = pairpos[(size_t)(q >> 16) * P + (q & 0xffff)];
+    }
+}
+
 // ---- on-disk tuning cache: the launch shapes chosen for a set of problem shapes on a
 // device model, so that a later finalize of the same batch skips the timing sweep.
-// One line per entry: "<key hash> wpb qt bps wpb32 qt32 pf32"; the file is
+// One line per entry: "<key hash> wpb qt bps wpb32 qt32 pf32 pf64 wpb64c"; the file is
 // SGFEM_TUNE_CACHE, else $XDG_CACHE_HOME/extendableasgfem_gb300/batch_tuning.txt, else
 // $HOME/.cache/extendableasgfem_gb300/batch_tuning.txt ("off" disables it).
 struct TuneEntry {
-    int wpb, qt, bps, wpb32, qt32, pf32;
+    int wpb, qt, bps, wpb32, qt32, pf32, pf64, wpb64c;
 };
 
 std::string tune_path() {
@@ -688,7 +976,7 @@ std::string tune_path() {
 std::string tune_key(const sgfem_batch* b) {
     cudaDeviceProp pr{};
     cudaGetDeviceProperties(&pr, b->device);
-    std::string k = std::string(pr.name) + "|" + std::to_string(pr.multiProcessorCount) + "|v1";
+    std::string k = std::string(pr.name) + "|" + std::to_string(pr.multiProcessorCount) + "|v2";
     for (const auto& h : b->hp)
         k += "|" + std::to_string(h.n) + "," + std::to_string(h.P) + "," + std::to_string(h.M1) + "," +
              std::to_string(h.col.size()) + "," + std::to_string(h.qtab.size()) + "," + std::to_string(h.nl);
@@ -709,7 +997,8 @@ bool tune_lookup(const std::string& path, const std::string& key, TuneEntry& e) 
     char k[64];
     TuneEntry t{};
     bool found = false;
-    while (fscanf(f, "%63s %d %d %d %d %d %d", k, &t.wpb, &t.qt, &t.bps, &t.wpb32, &t.qt32, &t.pf32) == 7)
+    while (fscanf(f, "%63s %d %d %d %d %d %d %d %d", k, &t.wpb, &t.qt, &t.bps, &t.wpb32, &t.qt32, &t.pf32, &t.pf64,
+                  &t.wpb64c) == 9)
         if (key == k) {
             e = t;
             found = true;  // the last entry for a key wins
@@ -722,7 +1011,8 @@ void tune_store(const std::string& path, const std::string& key, const TuneEntry
     if (path.empty()) return;
     FILE* f = fopen(path.c_str(), "a");
     if (!f) return;
-    fprintf(f, "%s %d %d %d %d %d %d\n", key.c_str(), e.wpb, e.qt, e.bps, e.wpb32, e.qt32, e.pf32);
+    fprintf(f, "%s %d %d %d %d %d %d %d %d\n", key.c_str(), e.wpb, e.qt, e.bps, e.wpb32, e.qt32, e.pf32, e.pf64,
+            e.wpb64c);
     fclose(f);
 }
 
@@ -915,6 +1205,26 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
         b->m1max = std::max(b->m1max, h.M1);
         b->qnmax = std::max(b->qnmax, d.Qn);
     }
+    // column-slot schedules (every problem needs M + 1 <= 31: lane 31 holds the zero value)
+    b->cols_ok = b->m1max <= 31;
+    if (const char* ea = getenv("SGFEM_BATCH_APPLY"))
+        if (std::string(ea) == "pairs") b->cols_ok = false;
+    for (int i = 0; i < B && b->cols_ok; ++i) {
+        ColSched cs;
+        build_cols(b->hp[i], cs);
+        BProb& d = probs[i];
+        d.npass = (int)cs.pass.size();
+        d.npass64 = (int)cs.pass64.size();
+        d.nf = cs.nf;
+        SG_TRY(bupload(b, cs.pass, (int4**)&d.cpass));
+        SG_TRY(bupload(b, cs.pass64, (int4**)&d.cpass64));
+        SG_TRY(bupload(b, cs.vgcol, (int**)&d.vgcol));
+        SG_TRY(bupload(b, cs.vgfoff, (int**)&d.vgfoff));
+        SG_TRY(bupload(b, cs.vgsrc, (int**)&d.vgsrc));
+        SG_TRY(bupload(b, cs.src, (unsigned char**)&d.src));
+        SG_TRY(bupload(b, cs.combf, (int**)&d.combf));
+        b->nfmax = std::max(b->nfmax, cs.nf);
+    }
     b->total = voff;
     const size_t vb = (size_t)voff * sizeof(double);
     SG_TRY(balloc(b, vb, (void**)&b->d_x));
@@ -997,31 +1307,25 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
         const bool ok64 = (te.wpb == 4 || te.wpb == 8) && (te.qt == 8 || te.qt == 16) && te.bps >= 1 &&
                           te.bps <= 16 && (int)apply_smem(b, te.wpb) <= dev_smem;
         const bool ok32 = (te.wpb32 == 4 || te.wpb32 == 8) && (te.qt32 == 16 || te.qt32 == 32) &&
-                          te.pf32 >= 0 && te.pf32 <= 3 &&
+                          te.pf32 >= 0 && te.pf32 <= 6 && te.pf32 != 5 &&
+                          (!(te.pf32 & 4) || b->cols_ok) &&
                           (!(te.pf32 & 1) || (b->ldmax <= 32 * BPC && b->m1max <= 32 * BPV)) &&
-                          (int)apply_smem<float>(b, te.wpb32) <= dev_smem;
-        hit = ok64 && ok32;
+                          (int)apply_smem<float>(b, te.wpb32, te.pf32) <= dev_smem;
+        const bool okc64 = te.pf64 == 0 || (te.pf64 == 4 && b->cols_ok && (te.wpb64c == 4 || te.wpb64c == 8) &&
+                                            (int)apply_smem<double>(b, te.wpb64c, 4) <= dev_smem);
+        hit = ok64 && ok32 && okc64;
     }
     if (hit) {
-        const size_t sm64 = apply_smem(b, te.wpb), sm32 = apply_smem<float>(b, te.wpb32);
-        if (sm64 > 48 * 1024)
-            BCUDA(b, te.qt == 8 ? cudaFuncSetAttribute(k_bapply<double, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm64)
-                                : cudaFuncSetAttribute(k_bapply<double, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm64));
-        if (sm32 > 48 * 1024) {
-            cudaError_t e32;
-            if (te.pf32 & 1)
-                e32 = te.qt32 == 16 ? cudaFuncSetAttribute(k_bapply<float, 16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm32)
-                                    : cudaFuncSetAttribute(k_bapply<float, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm32);
-            else
-                e32 = te.qt32 == 16 ? cudaFuncSetAttribute(k_bapply<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm32)
-                                    : cudaFuncSetAttribute(k_bapply<float, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm32);
-            BCUDA(b, e32);
-        }
+        BCUDA(b, set_apply_smem<double>(0, te.qt, apply_smem(b, te.wpb)));
+        BCUDA(b, set_apply_smem<float>(te.pf32, te.qt32, apply_smem<float>(b, te.wpb32, te.pf32)));
+        if (te.pf64 & 4) BCUDA(b, set_apply_smem<double>(4, 0, apply_smem<double>(b, te.wpb64c, 4)));
         best = 0.f;
         bestc = Cand{te.wpb, te.qt, te.bps};
         b->wpb32 = te.wpb32;
         b->qt32 = te.qt32;
         b->pf32 = te.pf32;
+        b->pf64 = te.pf64;
+        b->wpb64c = te.wpb64c;
         log = "from the tuning cache " + tpath + "; ";
     }
     for (const Cand& c : cands) {
@@ -1059,40 +1363,57 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
     b->qt = bestc.qt;
     SG_TRY(build_map(b, b->num_sms * bestc.bps, probs, bprob));
     SG_TRY(upload_map(b, probs, bprob));
+    // FP64 apply in the column-slot form on the same block map (residuals of the mixed
+    // solve, every iteration of the FP64 solve)
+    std::string log64c;
+    for (int wpb : {4, 8}) {
+        if (hit || !b->cols_ok) break;
+        const size_t smem = apply_smem<double>(b, wpb, 4);
+        if ((int)smem > dev_smem) continue;
+        if (set_apply_smem<double>(4, 0, smem) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        SG_TRY(launch_apply<double>(b, wpb, 0, b->d_p, b->d_q, b->d_part, nullptr, 4));
+        BCUDA(b, cudaEventRecord(b->ev0, b->stream));
+        SG_TRY(launch_apply<double>(b, wpb, 0, b->d_p, b->d_q, b->d_part, nullptr, 4));
+        BCUDA(b, cudaEventRecord(b->ev1, b->stream));
+        BCUDA(b, cudaEventSynchronize(b->ev1));
+        float ms = 0.f;
+        BCUDA(b, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+        char buf64[64];
+        snprintf(buf64, sizeof(buf64), "cols %dw:%.3fms ", wpb, ms);
+        log64c += buf64;
+        if (ms < best) {
+            best = ms;
+            b->pf64 = 4;
+            b->wpb64c = wpb;
+        }
+    }
     // FP32 apply of the mixed solve on the same block map: more pairs per pass amortise
-    // the staging of each X row (LSU-bound rather than FP64-bound)
+    // the staging of each X row (LSU-bound rather than FP64-bound); the column-slot form
+    // (pf 4, 6) reads each X row once per column group and nonzero
     std::string log32;
     float best32 = 1e30f;
-    for (int pf : {0, 1, 2, 3})
+    for (int pf : {0, 1, 2, 3, 4, 6})
         for (int wpb : {4, 8})
             for (int qt : {16, 32}) {
                 if (hit) break;
                 if ((pf & 1) && (b->ldmax > 32 * BPC || b->m1max > 32 * BPV)) continue;
-                const size_t smem = apply_smem<float>(b, wpb);
+                if ((pf & 4) && (!b->cols_ok || qt != 16)) continue;
+                const size_t smem = apply_smem<float>(b, wpb, pf);
                 if ((int)smem > dev_smem) continue;
                 {  // the register budget of the variant must allow the block size
                     cudaFuncAttributes fa{};
-                    const cudaError_t ea = (pf & 1) ? (qt == 16 ? cudaFuncGetAttributes(&fa, k_bapply<float, 16, true>)
-                                                          : cudaFuncGetAttributes(&fa, k_bapply<float, 32, true>))
-                                              : (qt == 16 ? cudaFuncGetAttributes(&fa, k_bapply<float, 16>)
-                                                          : cudaFuncGetAttributes(&fa, k_bapply<float, 32>));
+                    const cudaError_t ea = cudaFuncGetAttributes(&fa, apply_kernel<float>(pf, qt));
                     if (ea != cudaSuccess || fa.maxThreadsPerBlock < wpb * 32) {
                         cudaGetLastError();
                         continue;
                     }
                 }
-                if (smem > 48 * 1024) {
-                    cudaError_t e;
-                    if (pf & 1)
-                        e = qt == 16 ? cudaFuncSetAttribute(k_bapply<float, 16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                                     : cudaFuncSetAttribute(k_bapply<float, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                    else
-                        e = qt == 16 ? cudaFuncSetAttribute(k_bapply<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                                     : cudaFuncSetAttribute(k_bapply<float, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                    if (e != cudaSuccess) {
-                        cudaGetLastError();
-                        continue;
-                    }
+                if (set_apply_smem<float>(pf, qt, smem) != cudaSuccess) {
+                    cudaGetLastError();
+                    continue;
                 }
                 SG_TRY(launch_apply<float>(b, wpb, qt, b->d_p32, b->d_q32, b->d_part, nullptr, pf));
                 BCUDA(b, cudaEventRecord(b->ev0, b->stream));
@@ -1103,8 +1424,11 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
                 float ms = 0.f;
                 BCUDA(b, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
                 char buf32[96];
-                snprintf(buf32, sizeof(buf32), "%s%s%dw/%dq:%.3fms ", (pf & 2) ? "queue " : "", (pf & 1) ? "prefetch " : "",
-                         wpb, qt, ms / 2);
+                if (pf & 4)
+                    snprintf(buf32, sizeof(buf32), "%scols %dw:%.3fms ", (pf & 2) ? "queue " : "", wpb, ms / 2);
+                else
+                    snprintf(buf32, sizeof(buf32), "%s%s%dw/%dq:%.3fms ", (pf & 2) ? "queue " : "",
+                             (pf & 1) ? "prefetch " : "", wpb, qt, ms / 2);
                 log32 += buf32;
                 if (ms < best32) {
                     best32 = ms;
@@ -1113,13 +1437,39 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
                     b->pf32 = pf;
                 }
             }
-    if (!hit) tune_store(tpath, tkey, TuneEntry{b->wpb, b->qt, bestc.bps, b->wpb32, b->qt32, b->pf32});
+    if (!hit)
+        tune_store(tpath, tkey, TuneEntry{b->wpb, b->qt, bestc.bps, b->wpb32, b->qt32, b->pf32, b->pf64, b->wpb64c});
+    // SGFEM_BATCH_APPLY=cols: the column-slot form for both precisions (pairs: never, at finalize)
+    if (const char* ea = getenv("SGFEM_BATCH_APPLY"))
+        if (std::string(ea) == "cols" && b->cols_ok) {
+            if (!(b->pf32 & 4)) {
+                b->pf32 = 4;
+                b->qt32 = 16;
+                b->wpb32 = (int)apply_smem<float>(b, 8, 4) <= dev_smem ? 8 : 4;
+            }
+            if (!(b->pf64 & 4)) {
+                b->pf64 = 4;
+                b->wpb64c = (int)apply_smem<double>(b, 8, 4) <= dev_smem ? 8 : 4;
+            }
+            BCUDA(b, set_apply_smem<float>(4, 16, apply_smem<float>(b, b->wpb32, 4)));
+            BCUDA(b, set_apply_smem<double>(4, 0, apply_smem<double>(b, b->wpb64c, 4)));
+        }
     if (const char* q = getenv("SGFEM_BATCH_QUEUE"))  // 1 / 0: the FP32 apply over the work queue or not
-        b->pf32 = atoi(q) ? (b->pf32 | 2) : (b->pf32 & 1);
-    char buf[256];
-    snprintf(buf, sizeof(buf), "chosen %d warps/block, %d pairs/lane, %d blocks (FP32: %s%d warps/block, %d pairs/lane); ",
-             b->wpb, b->qt * 32, b->blocks, b->pf32 == 3 ? "work queue, prefetch, " : b->pf32 == 2 ? "work queue, " : b->pf32 ? "prefetch, " : "",
-             b->wpb32, b->qt32 * 32);
+        b->pf32 = atoi(q) ? (b->pf32 | 2) : (b->pf32 & ~2);
+    if (b->pf32 & 1) {
+        // the prefetching pair form needs its shared-memory opt-in like the others
+        BCUDA(b, set_apply_smem<float>(b->pf32, b->qt32, apply_smem<float>(b, b->wpb32, b->pf32)));
+    }
+    char buf[320];
+    const char* f32form = (b->pf32 & 4) ? ((b->pf32 & 2) ? "work queue, column slots, " : "column slots, ")
+                          : b->pf32 == 3 ? "work queue, prefetch, " : b->pf32 == 2 ? "work queue, " : b->pf32 ? "prefetch, " : "";
+    if (b->pf64 & 4)
+        snprintf(buf, sizeof(buf), "chosen column slots, %d warps/block, %d blocks (FP32: %s%d warps/block, %d pairs/lane); ",
+                 b->wpb64c, b->blocks, f32form, b->wpb32, b->qt32 * 32);
+    else
+        snprintf(buf, sizeof(buf), "chosen %d warps/block, %d pairs/lane, %d blocks (FP32: %s%d warps/block, %d pairs/lane); ",
+                 b->wpb, b->qt * 32, b->blocks, f32form, b->wpb32, b->qt32 * 32);
+    log += log64c;
     b->tuning = buf + log + "FP32 " + log32;
     b->finalized = true;
     return SGFEM_OK;
@@ -1161,8 +1511,10 @@ template <typename T, typename TX>
 int batch_iteration(sgfem_batch* b, const BVecs<T, TX>& v, int maxit) {
     const int B = (int)b->hp.size();
     const bool f32 = sizeof(T) == 4;
-    SG_TRY(launch_apply<T>(b, f32 ? b->wpb32 : b->wpb, f32 ? b->qt32 : b->qt, v.p, v.q, b->d_part, b->d_scal,
-                           f32 ? b->pf32 : 0));
+    if constexpr (sizeof(T) == 4)
+        SG_TRY(launch_apply<T>(b, b->wpb32, b->qt32, v.p, v.q, b->d_part, b->d_scal, b->pf32));
+    else
+        SG_TRY(apply64(b, v.p, v.q, b->d_part, b->d_scal));
     k_bfin<<<B, BT, 0, b->stream>>>(b->d_probs, b->d_part, b->d_scal, BF_ALPHA, 0.0, maxit);
     BLAUNCHED(b);
     k_bupdate<T, TX><<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, v.x, v.p, v.r, v.q, b->d_scal,
@@ -1332,7 +1684,7 @@ extern "C" int sgfem_batch_solve(sgfem_batch* b, double rtol, int maxit, int che
             // x += d; r = b - A x (FP64)
             k_badd<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_x, b->d_d64);
             BLAUNCHED(b);
-            SG_TRY(launch_apply<double>(b, b->wpb, b->qt, b->d_x, b->d_q, b->d_part, nullptr));
+            SG_TRY(apply64(b, b->d_x, b->d_q, b->d_part, nullptr));
             k_bresid<<<b->blocks, BT, 0, b->stream>>>(b->d_probs, b->d_bprob, b->d_b, b->d_q, b->d_r, b->d_part);
             BLAUNCHED(b);
             SG_TRY(norms64(b->d_r, rr));

@@ -147,3 +147,83 @@ def test_batch_work_queue_apply_is_bitwise_the_block_map(built_pkg, monkeypatch)
     for p, x in zip(probs, out["1"]):
         ref = osg.kron_direct(p.K0, p.Ks, p.G, p.b0, p.bdofs, p.P)
         assert np.linalg.norm(x - ref) <= 1e-8 * np.linalg.norm(ref)
+
+
+def _solve_batch(pkg, probs, rtol, check_every=8):
+    B = pkg.SGBatch(0)
+    for p in probs:
+        B.add(p.V, p.TB, p.Kall, p.b0)
+    B.finalize()
+    xs, st = B.solve(rtol=rtol, check_every=check_every)
+    tuning = B.tuning
+    B.close()
+    return xs, st, tuning
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_batch_column_slot_apply_matches_kronecker_solves(built_pkg, monkeypatch, precision):
+    """The column-slot form of the batch apply (SGFEM_BATCH_APPLY=cols: lanes own
+    columns, each slot takes its KLE value from the lane holding it) in both
+    precisions: total-degree sets (M = 16 and degree 2: groups of 16 and 1 slots for
+    the low-degree columns, 4 for the others; M = 7: 8 slots; degree 3), an
+    irregular top-weight set, a P2 problem and M + 1 = 31 (the largest the form
+    takes) against the Kronecker solves."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    monkeypatch.setenv("SGFEM_BATCH_APPLY", "cols")
+    monkeypatch.setenv("SGFEM_TUNE_CACHE", "off")
+    if precision == "fp64":
+        monkeypatch.setenv("SGFEM_BATCH_PRECISION", "fp64")
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    probs = [build(5, 1, 16, pkg.total_degree_multiindices(16, 2)),
+             build(6, 1, 7, pkg.total_degree_multiindices(7, 2)),
+             build(9, 1, 5, pkg.total_degree_multiindices(5, 3)),
+             build(7, 1, 8, pkg.top_weight_multiindices(8, 40, C.decay_factors)),
+             build(4, 2, 3, pkg.total_degree_multiindices(3, 2)),
+             build(4, 1, 30, pkg.total_degree_multiindices(30, 1)),
+             build(6, 1, 2, pkg.total_degree_multiindices(2, 1))]
+    xs, st, tuning = _solve_batch(pkg, probs, 1e-10)
+    head = tuning.split(";")[0]
+    assert "chosen column slots" in head and "FP32: column slots" in head, tuning
+    assert st["converged"] == len(probs) and st["relres_max"] <= 1e-10
+    for p, x in zip(probs, xs):
+        ref = osg.kron_direct(p.K0, p.Ks, p.G, p.b0, p.bdofs, p.P)
+        assert np.linalg.norm(x - ref) <= 1e-8 * np.linalg.norm(ref)
+
+
+def test_batch_column_slot_queue_is_bitwise_the_block_map(built_pkg, monkeypatch):
+    """The column-slot FP32 apply over the persistent work queue computes every
+    item as the one-block-per-item launch does: bitwise equal mixed solves."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    monkeypatch.setenv("SGFEM_BATCH_APPLY", "cols")
+    monkeypatch.setenv("SGFEM_TUNE_CACHE", "off")
+    shapes = [(9, 3, 2), (5, 2, 2), (12, 4, 3), (6, 5, 1), (7, 12, 2)]
+    probs = [build(N, 1, M, pkg.total_degree_multiindices(M, d)) for N, M, d in shapes]
+    out = {}
+    for q in ("0", "1"):
+        monkeypatch.setenv("SGFEM_BATCH_QUEUE", q)
+        xs, st, tuning = _solve_batch(pkg, probs, 1e-10)
+        head = tuning.split(";")[0]
+        assert "column slots" in head and ("work queue" in head) == (q == "1"), tuning
+        assert st["converged"] == len(probs) and st["relres_max"] <= 1e-10
+        out[q] = xs
+    for a, b in zip(out["0"], out["1"]):
+        assert np.array_equal(a, b)
+
+
+def test_batch_column_slots_need_at_most_31_terms(built_pkg, monkeypatch):
+    """A problem with M + 1 > 31 keeps the whole batch on the pair form even when
+    the column-slot form is asked for (lane 31 must hold the zero value)."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    monkeypatch.setenv("SGFEM_BATCH_APPLY", "cols")
+    monkeypatch.setenv("SGFEM_TUNE_CACHE", "off")
+    units = [[0] * 31] + [[int(k == m) for k in range(31)] for m in range(31)]
+    probs = [build(5, 1, 31, units), build(5, 1, 2, pkg.total_degree_multiindices(2, 2))]
+    xs, st, tuning = _solve_batch(pkg, probs, 1e-10)
+    assert "column slots" not in tuning.split(";")[0], tuning
+    assert st["converged"] == len(probs)
+    for p, x in zip(probs, xs):
+        ref = osg.kron_direct(p.K0, p.Ks, p.G, p.b0, p.bdofs, p.P)
+        assert np.linalg.norm(x - ref) <= 1e-8 * np.linalg.norm(ref)
