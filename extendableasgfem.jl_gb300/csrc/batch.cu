@@ -104,7 +104,9 @@ struct sgfem_batch {
     double* d_d64 = nullptr;
     double* d_want = nullptr;     // per-problem squared inner reduction target
     float* d_t = nullptr;         // sine-transform intermediate
-    int4* d_dstmap = nullptr;     // (problem, line, mode chunk) per block of the transform passes
+    int2* d_dstmap = nullptr;     // (problem, line) per block of the transform passes
+    int* d_soff = nullptr;        // per problem: offset of its sine table in d_stab
+    float* d_stab = nullptr;      // sine tables of the lattice sizes in the batch
     int ndst = 0;
     int2* d_lat = nullptr;        // per problem: (nl, a0 as float bits); nl = 0: Jacobi
     size_t dst_smem = 0;
@@ -695,74 +697,121 @@ __global__ void __launch_bounds__(BT) k_bpz(const BProb* __restrict__ probs, con
 // S_ik = sin(pi i k / nl), i, k = 1..nl-1 (S^2 = (nl/2) I), applied as a dense
 // matrix product along every lattice line: pass 0 (x): t = S r per line j;
 // pass 1 (y): t = S (D .* (S t)) per column, D = (2/nl)^2 / (a0 (lam_kx + lam_ky)),
-// lam_k = 4 sin^2(pi k / (2 nl)); pass 2 (x): z = S t per line.  One block per
-// (problem, line, 32-mode chunk); S and the line tile in shared memory, lanes
-// over modes, FP32 arithmetic.
+// lam_k = 4 sin^2(pi k / (2 nl)); pass 2 (x): z = S t per line.  FP32 arithmetic.
+// One block per (problem, line): S (N x NP, precomputed at finalize, NP = N rounded
+// up to 16; S is symmetric, so row k holds S_ik for consecutive i) is staged in
+// shared memory once, then the line's columns go in chunks of cw: the chunk's N x cw
+// tile sits in shared memory and each warp computes a 16-row x 64-column unit with
+// 2 columns per lane, 32 FMAs per 1 tile load (float2) and 4 broadcast S loads
+// (float4).  cw = 64 * (8 / (NP / 16)) keeps the 8 warps busy on short lines.
+constexpr int DST_WARPS = 8;
 template <typename T>
-__global__ void __launch_bounds__(BT) k_bdst(const BProb* __restrict__ probs, const int4* __restrict__ map,
-                                             const int2* __restrict__ lat, int pass, const T* __restrict__ r,
-                                             float* __restrict__ t, T* __restrict__ z,
-                                             const KrylovScalars* __restrict__ scal) {
-    const int4 e = map[blockIdx.x];
-    const int pi = e.x, line = e.y, chunk = e.z;
+__global__ void __launch_bounds__(DST_WARPS * 32, 2) k_bdst(const BProb* __restrict__ probs, const int2* __restrict__ map,
+                                                         const int2* __restrict__ lat, const int* __restrict__ soff,
+                                                         const float* __restrict__ stab, int pass,
+                                                         const T* __restrict__ r, float* __restrict__ t,
+                                                         T* __restrict__ z, const KrylovScalars* __restrict__ scal) {
+    const int2 e = map[blockIdx.x];
+    const int pi = e.x, line = e.y;
     if (scal[pi].done) return;
     const BProb& d = probs[pi];
-    const int nl = lat[pi].x, N = nl - 1;
+    const int nl = lat[pi].x, N = nl - 1, NP = (N + 15) & ~15, nrb = NP / 16;
+    const int cpw = DST_WARPS / nrb, cw = 64 * cpw;
     const float a0 = __int_as_float(lat[pi].y);
-    extern __shared__ float dsm[];
-    float* S = dsm;                   // N x N
-    float* tile = S + N * N;          // N x 32 (input line)
-    float* out = tile + N * 32;       // N x 32
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
-        const int i = q / N + 1, k = q % N + 1;
-        S[q] = sinpif((float)((i * k) % (2 * nl)) / (float)nl);
+    extern __shared__ __align__(16) float dsm[];
+    float* S = dsm;              // N x NP
+    float* tile = S + N * NP;    // N x cw
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    {
+        const float4* src = reinterpret_cast<const float4*>(stab + soff[pi]);
+        float4* dst = reinterpret_cast<float4*>(S);
+        for (int q = threadIdx.x; q < N * NP / 4; q += blockDim.x) dst[q] = __ldg(src + q);
     }
-    const int c = chunk * 32 + lane;
-    const bool live = c < d.ld;
     const int stride = nl + 1;
-    // lattice point k (1..N) of this line -> row
-    auto row_of = [&](int k) { return (pass == 1) ? k * stride + line : line * stride + k; };
-    for (int k = 1 + warp; k <= N; k += nw) {
-        const long long idx = d.voff + (long long)row_of(k) * d.ld + c;
-        float v = 0.f;
-        if (live) v = (pass == 0) ? (float)r[idx] : t[idx];
-        tile[(k - 1) * 32 + lane] = v;
-    }
-    __syncthreads();
-    for (int i = warp; i < N; i += nw) {
-        float s = 0.f;
-        const float* Si = S + i * N;
-        for (int k = 0; k < N; ++k) s = fmaf(Si[k], tile[k * 32 + lane], s);
-        out[i * 32 + lane] = s;
-    }
-    __syncthreads();
-    if (pass == 1) {
-        // scale by D(kx = line, ky = i + 1) and transform again
-        const float w = 3.14159265358979f / (2.0f * (float)nl);
-        const float sx = sinf(w * (float)line);
-        const float lx = 4.f * sx * sx;
-        const float nrm = 4.f / ((float)nl * (float)nl);
-        for (int i = warp; i < N; i += nw) {
-            const float sy = sinf(w * (float)(i + 1));
-            tile[i * 32 + lane] = out[i * 32 + lane] * (nrm / (a0 * (lx + 4.f * sy * sy)));
+    auto row_of = [&](int k) { return (pass == 1) ? k * stride + line : line * stride + k; };  // k = 1..N
+    const int rb = warp % nrb, cc = warp / nrb;  // this warp's unit: rows 16 rb.., columns 64 cc + 2 lane
+    const bool busy = warp < nrb * cpw;
+    const float w = 3.14159265358979f / (2.0f * (float)nl);
+    for (int c0 = 0; c0 < d.ld; c0 += cw) {
+        __syncthreads();  // S staged / the previous chunk's tile read
+        const int cn = min(cw, d.ld - c0);  // a multiple of 4
+        for (int q = threadIdx.x; q < N * (cw / 4); q += blockDim.x) {
+            const int k = q / (cw / 4), c = 4 * (q - k * (cw / 4));
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (c < cn) {
+                const long long idx = d.voff + (long long)row_of(k + 1) * d.ld + c0 + c;
+                if (pass == 0) {
+                    if constexpr (sizeof(T) == 8) {
+                        const double2 v0 = *reinterpret_cast<const double2*>(r + idx);
+                        const double2 v1 = *reinterpret_cast<const double2*>(r + idx + 2);
+                        v = make_float4((float)v0.x, (float)v0.y, (float)v1.x, (float)v1.y);
+                    } else {
+                        v = *reinterpret_cast<const float4*>(r + idx);
+                    }
+                } else {
+                    v = *reinterpret_cast<const float4*>(t + idx);
+                }
+            }
+            *reinterpret_cast<float4*>(tile + k * cw + c) = v;
         }
         __syncthreads();
-        for (int i = warp; i < N; i += nw) {
-            float s = 0.f;
-            const float* Si = S + i * N;
-            for (int k = 0; k < N; ++k) s = fmaf(Si[k], tile[k * 32 + lane], s);
-            out[i * 32 + lane] = s;
+        float2 acc[16];
+        const int col = 64 * cc + 2 * lane;
+        auto transform = [&]() {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) acc[i] = make_float2(0.f, 0.f);
+            const float* Sr = S + 16 * rb;
+            const float* tr = tile + col;
+#pragma unroll 2
+            for (int k = 0; k < N; ++k) {
+                const float2 x = *reinterpret_cast<const float2*>(tr + k * cw);
+                const float4* s4 = reinterpret_cast<const float4*>(Sr + k * NP);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float4 sv = s4[q];
+                    acc[4 * q + 0] = __ffma2_rn(make_float2(sv.x, sv.x), x, acc[4 * q + 0]);
+                    acc[4 * q + 1] = __ffma2_rn(make_float2(sv.y, sv.y), x, acc[4 * q + 1]);
+                    acc[4 * q + 2] = __ffma2_rn(make_float2(sv.z, sv.z), x, acc[4 * q + 2]);
+                    acc[4 * q + 3] = __ffma2_rn(make_float2(sv.w, sv.w), x, acc[4 * q + 3]);
+                }
+            }
+        };
+        if (busy) transform();
+        if (pass == 1) {
+            // scale by D(kx = line, ky = i + 1), back into the tile, transform again
+            __syncthreads();  // every warp has read the tile
+            if (busy) {
+                const float sx = sinf(w * (float)line);
+                const float lx = 4.f * sx * sx;
+                const float nrm = 4.f / ((float)nl * (float)nl);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const int row = 16 * rb + i;
+                    if (row < N) {
+                        const float sy = sinf(w * (float)(row + 1));
+                        const float f = nrm / (a0 * (lx + 4.f * sy * sy));
+                        *reinterpret_cast<float2*>(tile + row * cw + col) = make_float2(acc[i].x * f, acc[i].y * f);
+                    }
+                }
+            }
+            __syncthreads();
+            if (busy) transform();
         }
-        __syncthreads();
-    }
-    if (!live) return;
-    for (int k = 1 + warp; k <= N; k += nw) {
-        const long long idx = d.voff + (long long)row_of(k) * d.ld + c;
-        if (pass == 2)
-            z[idx] = (T)out[(k - 1) * 32 + lane];
-        else
-            t[idx] = out[(k - 1) * 32 + lane];
+        if (busy && col < cn) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const int row = 16 * rb + i;
+                if (row < N) {
+                    const long long idx = d.voff + (long long)row_of(row + 1) * d.ld + c0 + col;
+                    if (pass == 2) {
+                        z[idx] = (T)acc[i].x;
+                        z[idx + 1] = (T)acc[i].y;
+                    } else {
+                        *reinterpret_cast<float2*>(t + idx) = acc[i];
+                    }
+                }
+            }
+        }
     }
 }
 
@@ -1243,9 +1292,13 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
     SG_TRY(balloc(b, vb, (void**)&b->d_d64));
     SG_TRY(balloc(b, (size_t)B * sizeof(double), (void**)&b->d_want));
     {
-        // sine-transform preconditioner: per-problem (nl, a0) and one block per (problem, line, chunk)
+        // sine-transform preconditioner: per-problem (nl, a0), the sine table of each lattice
+        // size (N x NP, zero past column N; offsets multiples of 16 floats) and one block
+        // per (problem, interior line)
         std::vector<int2> lat(B, make_int2(0, 0));
-        std::vector<int4> map;
+        std::vector<int2> map;
+        std::vector<int> soff(B, 0), toff(129, -1);
+        std::vector<float> stab;
         size_t smax = 0;
         for (int i = 0; i < B; ++i) {
             const auto& h = b->hp[i];
@@ -1254,15 +1307,23 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
             int bits;
             std::memcpy(&bits, &a0f, sizeof(int));
             lat[i] = make_int2(h.nl, bits);
-            const int N = h.nl - 1, chunks = (h.ld + 31) / 32;
-            for (int line = 1; line <= N; ++line)
-                for (int c = 0; c < chunks; ++c) map.push_back(make_int4(i, line, c, 0));
-            smax = std::max(smax, ((size_t)N * N + 2 * (size_t)N * 32) * sizeof(float));
+            const int N = h.nl - 1, NP = (N + 15) & ~15, cw = 64 * (DST_WARPS / (NP / 16));
+            if (toff[h.nl] < 0) {
+                toff[h.nl] = (int)stab.size();
+                for (int k = 1; k <= N; ++k)
+                    for (int c = 0; c < NP; ++c)
+                        stab.push_back(c < N ? (float)std::sin(M_PI * (double)((k * (c + 1)) % (2 * h.nl)) / h.nl) : 0.f);
+            }
+            soff[i] = toff[h.nl];
+            for (int line = 1; line <= N; ++line) map.push_back(make_int2(i, line));
+            smax = std::max(smax, ((size_t)N * NP + (size_t)N * cw) * sizeof(float));
         }
         SG_TRY(bupload(b, lat, &b->d_lat));
         b->ndst = (int)map.size();
         if (b->ndst > 0) {
             SG_TRY(bupload(b, map, &b->d_dstmap));
+            SG_TRY(bupload(b, soff, &b->d_soff));
+            SG_TRY(bupload(b, stab, &b->d_stab));
             SG_TRY(balloc(b, (size_t)voff * sizeof(float), (void**)&b->d_t));
             b->dst_smem = smax;
             if (smax > 48 * 1024) {
@@ -1494,7 +1555,8 @@ int batch_precondition(sgfem_batch* b, const BVecs<T, TX>& v, int maxit) {
     BLAUNCHED(b);
     if (b->ndst > 0)
         for (int pass = 0; pass < 3; ++pass) {
-            k_bdst<T><<<b->ndst, BT, b->dst_smem, b->stream>>>(b->d_probs, b->d_dstmap, b->d_lat, pass, v.r, b->d_t,
+            k_bdst<T><<<b->ndst, DST_WARPS * 32, b->dst_smem, b->stream>>>(b->d_probs, b->d_dstmap, b->d_lat, b->d_soff,
+                                                                             b->d_stab, pass, v.r, b->d_t,
                                                                v.z, b->d_scal);
             BLAUNCHED(b);
         }
