@@ -48,15 +48,19 @@ struct BProb {
     const float* dinv32;
     // column-slot form of the apply (k_bapply_cols): passes over virtual groups of 32
     // columns, each lane taking its column's KLE terms from the lanes that hold them
-    int npass, nf;                // passes; pair sums per warp (floats or doubles)
+    int npass;                    // FP32 passes
     const int4* cpass;            // FP32 passes: (kind, first virtual group, groups, 0)
     const int4* cpass64;          // FP64 passes (fewer groups per pass: register budget)
     int npass64;
     const int* vgcol;             // first column of each virtual group (multiple of 32)
-    const int* vgfoff;            // offset of its pair sums in the per-warp area
     const int* vgsrc;             // offset of its source lanes in src (slots x 32)
     const unsigned char* src;     // per slot and lane: the lane holding the term's value (31: zero)
-    const int* combf;             // per combination entry: the pair sum's place in the area
+    const int* ept32;             // combination entries by (pass, output lane), FP32 passes
+    const int* eidx32;            //   k << 16 | place of the pair sum in the pass's area
+    const float* eg32;            //   coefficient
+    const int* ept64;             // the same for the FP64 passes
+    const int* eidx64;
+    const double* eg64;
 };
 
 template <typename T> __device__ __forceinline__ const T* bvals(const BProb& d);
@@ -118,7 +122,6 @@ struct sgfem_batch {
                                   // bit 2: column-slot form (k_bapply_cols)
     int pf64 = 0, wpb64c = 4;     // FP64 apply: 4 = column-slot form with wpb64c warps per block
     bool cols_ok = false;         // every problem has M + 1 <= 31 (the column-slot form applies)
-    int nfmax = 0;                // largest per-warp pair-sum area of the column-slot form
     std::string tuning;
     std::vector<KrylovScalars> h_scal;
     double rtol = 0.0;            // of the last solve
@@ -330,10 +333,11 @@ __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict_
 // pair sums go to the warp's shared area and each output column is combined from its
 // list (K_0 pair with g = 1, then the G entries) as in k_bapply.
 // kinds: slots per lane 1, 2, 4, 8, 16; groups per pass keep the pair sums of a pass at
-// <= 32 registers (FP32) or <= 16 doubles (FP64)
+// <= 16 per lane, and the pass's X values of a chunk of nonzeros (groups x 4) within
+// the 128-register budget
 __host__ __device__ constexpr int cols_na(int kind) { return kind == 0 ? 1 : kind == 1 ? 2 : kind == 2 ? 4 : kind == 3 ? 8 : 16; }
 __host__ __device__ constexpr int cols_gp(int kind, int es) {
-    return es == 4 ? (kind <= 2 ? 8 : kind == 3 ? 4 : 2) : (kind <= 1 ? 8 : kind == 2 ? 4 : kind == 3 ? 2 : 1);
+    return es == 4 ? (kind <= 1 ? 8 : kind == 2 ? 4 : kind == 3 ? 2 : 1) : (kind <= 2 ? 4 : kind == 3 ? 2 : 1);
 }
 
 template <typename T, int NA, int GP>
@@ -357,11 +361,11 @@ __device__ __forceinline__ void cols_pass(const BProb& d, const T* __restrict__ 
             acc[g][s] = T(0);
         }
     }
-    // the row's nonzeros in chunks of CH: lane t holds the column of nonzero base + t and
+    // the row's nonzeros in chunks of CH = 4: lane t holds the column of nonzero base + t and
     // lane m the K_m value of each (zero past the row's end, whose column reads row 0),
     // so the X loads of a chunk depend on no other load; they are issued two nonzeros
     // ahead of their FMAs
-    constexpr int CH = 8;
+    constexpr int CH = 4;
     for (int base = nz0; base < nz1; base += CH) {
         const int cnt = min(CH, nz1 - base);
         const int jl = lane < cnt ? __ldg(d.col + base + lane) : 0;
@@ -389,19 +393,26 @@ __device__ __forceinline__ void cols_pass(const BProb& d, const T* __restrict__ 
                     acc[g][s] = fma(__shfl_sync(0xffffffffu, kr[t], src[g][s]), ux[t][g], acc[g][s]);
         }
     }
+    // the pass's pair sums to the warp's area: group g, slot s, lane L at (g NA + s) 32 + L
 #pragma unroll
     for (int g = 0; g < GP; ++g) {
         if (g < ng) {
-            T* o = sacc + d.vgfoff[vg0 + g] + lane;
 #pragma unroll
-            for (int s = 0; s < NA; ++s) o[32 * s] = acc[g][s];
+            for (int s = 0; s < NA; ++s) sacc[(g * NA + s) * 32 + lane] = acc[g][s];
         }
     }
 }
 
-// work items as in k_bapply (block map or persistent queue); per_warp = largest area
+// pair sums per lane of one pass: at most 16
 template <typename T>
-__global__ void k_bapply_cols(const BProb* __restrict__ probs, const int* __restrict__ bprob, const T* __restrict__ X,
+__host__ __device__ constexpr int cols_area() { return 16 * 32; }
+
+// work items as in k_bapply (block map or persistent queue); the warp's shared area is
+// the pass area (cols_area) followed by the output row (per_warp - cols_area values);
+// after every pass each lane adds the pass's entries of its own output columns
+// (32 k + lane) to the row, so no lane writes another lane's outputs
+template <typename T>
+__global__ void __launch_bounds__(256, 2) k_bapply_cols(const BProb* __restrict__ probs, const int* __restrict__ bprob, const T* __restrict__ X,
                               T* __restrict__ Y, double* __restrict__ partials, const KrylovScalars* __restrict__ scal,
                               int per_warp, const int* __restrict__ vorder, int* __restrict__ wq, int nvb) {
     __shared__ int s_item;
@@ -427,12 +438,16 @@ __global__ void k_bapply_cols(const BProb* __restrict__ probs, const int* __rest
         const int pi = bprob[vb];
         const BProb& d = probs[pi];
         const T* vals = bvals<T>(d);
-        const T* combg = bcombg<T>(d);
         if (scal && scal[pi].done) {
             if (threadIdx.x == 0 && partials) partials[vb] = 0.0;
             continue;
         }
         T* sacc = bsm + (size_t)warp * per_warp;
+        T* ys = sacc + cols_area<T>();
+        constexpr int ES = (int)sizeof(T);
+        const int* ept = ES == 4 ? d.ept32 : d.ept64;
+        const int* eidx = ES == 4 ? d.eidx32 : d.eidx64;
+        const T* eg = ES == 4 ? reinterpret_cast<const T*>(d.eg32) : reinterpret_cast<const T*>(d.eg64);
         const T* Xp = X + d.voff;
         T* Yp = Y + d.voff;
         double dot = 0.0;
@@ -444,7 +459,7 @@ __global__ void k_bapply_cols(const BProb* __restrict__ probs, const int* __rest
                 continue;
             }
             const int nz0 = d.rowptr[row], nz1 = d.rowptr[row + 1];
-            constexpr int ES = (int)sizeof(T);
+            for (int mu = lane; mu < d.ld; mu += 32) ys[mu] = T(0);
             const int np = ES == 4 ? d.npass : d.npass64;
             const int4* cp = ES == 4 ? d.cpass : d.cpass64;
             for (int p = 0; p < np; ++p) {
@@ -462,19 +477,23 @@ __global__ void k_bapply_cols(const BProb* __restrict__ probs, const int* __rest
                     case 8: cols_pass<T, cols_na(4), cols_gp(4, ES)>(d, Xp, vals, nz0, nz1, ps.y, ps.z, sacc, lane); break;
                     default: cols_pass<T, cols_na(4), 1>(d, Xp, vals, nz0, nz1, ps.y, 1, sacc, lane); break;
                 }
+                __syncwarp();  // the pass's sums are in the area
+                const int e1 = __ldg(ept + p * 32 + lane + 1);
+                for (int e = __ldg(ept + p * 32 + lane); e < e1; ++e) {
+                    const int v = __ldg(eidx + e);
+                    T* yo = ys + (v >> 16) * 32 + lane;
+                    *yo = fma(__ldg(eg + e), sacc[v & 0xffff], *yo);
+                }
+                __syncwarp();  // the area is read before the next pass writes it
             }
-            __syncwarp();
             const T* xrow = Xp + (size_t)row * d.ld;
             T rowdot = T(0);
             for (int mu = lane; mu < d.ld; mu += 32) {
-                T y = T(0);
-                if (mu < d.P)
-                    for (int e = d.combptr[mu]; e < d.combptr[mu + 1]; ++e) y = fma(combg[e], sacc[d.combf[e]], y);
+                const T y = ys[mu];
                 yrow[mu] = y;
                 rowdot = fma(xrow[mu], y, rowdot);
             }
             dot += (double)rowdot;
-            __syncwarp();  // the combination has read the area before the next row's passes
         }
         if (partials) {
             __shared__ double red[32];
@@ -833,7 +852,7 @@ int balloc(sgfem_batch* b, size_t bytes, void** dst) {
 
 template <typename T = double>
 size_t apply_smem(const sgfem_batch* b, int wpb, int pf = 0) {
-    if (pf & 4) return (size_t)b->nfmax * sizeof(T) * wpb;
+    if (pf & 4) return (size_t)(cols_area<T>() + ((b->ldmax + 3) & ~3)) * sizeof(T) * wpb;
     const size_t per_warp = ((size_t)b->ldmax + b->m1max + 1 + b->qnmax + 3) & ~(size_t)3;
     return per_warp * sizeof(T) * wpb;
 }
@@ -844,7 +863,8 @@ size_t apply_smem(const sgfem_batch* b, int wpb, int pf = 0) {
 template <typename T>
 int launch_apply(sgfem_batch* b, int wpb, int qt, const T* X, T* Y, double* partials, const KrylovScalars* scal,
                  int pf = 0) {
-    const int per_warp = (pf & 4) ? b->nfmax : (int)(((size_t)b->ldmax + b->m1max + 1 + b->qnmax + 3) & ~(size_t)3);
+    const int per_warp = (pf & 4) ? cols_area<T>() + ((b->ldmax + 3) & ~3)
+                                  : (int)(((size_t)b->ldmax + b->m1max + 1 + b->qnmax + 3) & ~(size_t)3);
     const size_t smem = apply_smem<T>(b, wpb, pf);
     using KF = void (*)(const BProb*, const int*, const T*, T*, double*, const KrylovScalars*, int, const int*, int*, int);
     KF kf;
@@ -932,9 +952,14 @@ int build_map(sgfem_batch* b, int total_blocks, std::vector<BProb>& probs, std::
 // another in the warp's area in pass order.
 struct ColSched {
     std::vector<int4> pass, pass64;
-    std::vector<int> vgcol, vgfoff, vgsrc, combf;
+    std::vector<int> vgcol, vgsrc;
     std::vector<unsigned char> src;
     int nf = 0;
+    // combination entries per precision, grouped by (pass, lane of the output column):
+    // ept[p * 32 + L] .. ept[p * 32 + L + 1] index eidx (k << 16 | place in the pass's
+    // area; output column 32 k + L) and eg (coefficient)
+    std::vector<int> ept32, eidx32, ept64, eidx64;
+    std::vector<double> eg32, eg64;
 };
 
 void build_cols(const sgfem_batch::HostProb& h, ColSched& cs) {
@@ -968,7 +993,6 @@ void build_cols(const sgfem_batch::HostProb& h, ColSched& cs) {
         const int na = cols_na(v.kind);
         kinds.push_back(v.kind);
         cs.vgcol.push_back(v.col);
-        cs.vgfoff.push_back(cs.nf);
         cs.vgsrc.push_back((int)cs.src.size());
         for (int s = 0; s < na; ++s)
             for (int L = 0; L < 32; ++L) {
@@ -977,7 +1001,7 @@ void build_cols(const sgfem_batch::HostProb& h, ColSched& cs) {
                 int m = 31;
                 if (c < P && t < (int)terms[c].size()) {
                     m = terms[c][t];
-                    pairpos[(size_t)m * P + c] = cs.nf + 32 * s + L;
+                    pairpos[(size_t)m * P + c] = (int)cs.vgcol.size() - 1 + (s << 20);
                 }
                 cs.src.push_back((unsigned char)m);
             }
@@ -993,10 +1017,36 @@ void build_cols(const sgfem_batch::HostProb& h, ColSched& cs) {
             k += ng;
         }
     }
-    cs.combf.resize(h.combq.size());
-    for (size_t e = 0; e < h.combq.size(); ++e) {
-        const int q = h.qtab[h.combq[e]];
-        cs.combf[e] = pairpos[(size_t)(q >> 16) * P + (q & 0xffff)];
+    // per precision: the pass and place of every pair, then the entries of each output
+    // column (K_0 pair with g = 1, then the G entries, in the pair form's order) by pass
+    for (int es : {4, 8}) {
+        const auto& pass = es == 4 ? cs.pass : cs.pass64;
+        std::vector<int> vpass(cs.vgcol.size()), vg_in(cs.vgcol.size());
+        for (size_t p = 0; p < pass.size(); ++p)
+            for (int g = 0; g < pass[p].z; ++g) {
+                vpass[pass[p].y + g] = (int)p;
+                vg_in[pass[p].y + g] = g;
+            }
+        std::vector<std::vector<std::pair<int, double>>> lists(pass.size() * 32);
+        for (int mu = 0; mu < P; ++mu)
+            for (int e = h.combptr[mu]; e < h.combptr[mu + 1]; ++e) {
+                const int q = h.qtab[h.combq[e]], m = q >> 16, nu = q & 0xffff;
+                const int pp = pairpos[(size_t)m * P + nu], vg = pp & 0xfffff, sl = pp >> 20;
+                const int na = cols_na(pass[vpass[vg]].x);
+                const int place = (vg_in[vg] * na + sl) * 32 + (nu & 31);
+                lists[(size_t)vpass[vg] * 32 + (mu & 31)].push_back({((mu >> 5) << 16) | place, h.combg[e]});
+            }
+        auto& ept = es == 4 ? cs.ept32 : cs.ept64;
+        auto& eidx = es == 4 ? cs.eidx32 : cs.eidx64;
+        auto& eg = es == 4 ? cs.eg32 : cs.eg64;
+        ept.assign(lists.size() + 1, 0);
+        for (size_t l = 0; l < lists.size(); ++l) {
+            for (const auto& en : lists[l]) {
+                eidx.push_back(en.first);
+                eg.push_back(en.second);
+            }
+            ept[l + 1] = (int)eidx.size();
+        }
     }
 }
 
@@ -1264,15 +1314,17 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
         BProb& d = probs[i];
         d.npass = (int)cs.pass.size();
         d.npass64 = (int)cs.pass64.size();
-        d.nf = cs.nf;
         SG_TRY(bupload(b, cs.pass, (int4**)&d.cpass));
         SG_TRY(bupload(b, cs.pass64, (int4**)&d.cpass64));
         SG_TRY(bupload(b, cs.vgcol, (int**)&d.vgcol));
-        SG_TRY(bupload(b, cs.vgfoff, (int**)&d.vgfoff));
         SG_TRY(bupload(b, cs.vgsrc, (int**)&d.vgsrc));
         SG_TRY(bupload(b, cs.src, (unsigned char**)&d.src));
-        SG_TRY(bupload(b, cs.combf, (int**)&d.combf));
-        b->nfmax = std::max(b->nfmax, cs.nf);
+        SG_TRY(bupload(b, cs.ept32, (int**)&d.ept32));
+        SG_TRY(bupload(b, cs.eidx32, (int**)&d.eidx32));
+        SG_TRY(bupload(b, std::vector<float>(cs.eg32.begin(), cs.eg32.end()), (float**)&d.eg32));
+        SG_TRY(bupload(b, cs.ept64, (int**)&d.ept64));
+        SG_TRY(bupload(b, cs.eidx64, (int**)&d.eidx64));
+        SG_TRY(bupload(b, cs.eg64, (double**)&d.eg64));
     }
     b->total = voff;
     const size_t vb = (size_t)voff * sizeof(double);
