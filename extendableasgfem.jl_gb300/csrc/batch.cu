@@ -713,49 +713,124 @@ __global__ void __launch_bounds__(BT) k_bpz(const BProb* __restrict__ probs, con
 
 // Mean-based preconditioner of a lattice problem, z = (a0 L)^-1 r on interior rows
 // (L the 5-point Laplacian of the (nl+1)^2 lattice), by the sine transform
-// S_ik = sin(pi i k / nl), i, k = 1..nl-1 (S^2 = (nl/2) I), applied as a dense
+// S_ik = sin(pi i k / nl), i, k = 1..N = nl-1 (S^2 = (nl/2) I), applied as a dense
 // matrix product along every lattice line: pass 0 (x): t = S r per line j;
 // pass 1 (y): t = S (D .* (S t)) per column, D = (2/nl)^2 / (a0 (lam_kx + lam_ky)),
 // lam_k = 4 sin^2(pi k / (2 nl)); pass 2 (x): z = S t per line.  FP32 arithmetic.
-// One block per (problem, line): S (N x NP, precomputed at finalize, NP = N rounded
-// up to 16; S is symmetric, so row k holds S_ik for consecutive i) is staged in
-// shared memory once, then the line's columns go in chunks of cw: the chunk's N x cw
-// tile sits in shared memory and each warp computes a 16-row x 64-column unit with
-// 2 columns per lane, 32 FMAs per 1 tile load (float2) and 4 broadcast S loads
-// (float4).  cw = 64 * (8 / (NP / 16)) keeps the 8 warps busy on short lines.
+// Each product is split by the parity of the output: S_{i,nl-k} = S_ik for odd i and
+// -S_ik for even i, so with u_k = x_k + x_{nl-k}, v_k = x_k - x_{nl-k} (k <= H =
+// (nl-1)/2, and the middle point x_{nl/2} for even nl, which only odd i see)
+//   y_i (odd i)  = sum_k S_ik u_k (+ sin(pi i / 2) x_{nl/2}),
+//   y_i (even i) = sum_k S_ik v_k,
+// two products of half the size: half the FMAs of S x.  In the tile the pair
+// (k, nl - k) becomes (u_k, v_k) in place, so rows 0..HU-1 hold u (and the middle
+// point) and rows HU..N-1 hold v_H..v_1.  The tables (built at finalize, transposed
+// so that row r holds the coefficients of consecutive outputs, padded with zeros to
+// 16 outputs) are TO (HU x NOP, odd outputs) and TE (H x NEP, even outputs).
+// One block per (problem, line): the tables are staged in shared memory once, then
+// the line's columns go in chunks of cw; each warp computes 16 outputs x 64 columns
+// (2 columns per lane: one float2 tile load and four broadcast float4 table loads
+// per 32 packed FMAs); cw = 64 * (8 / output blocks) keeps the 8 warps busy.
 constexpr int DST_WARPS = 8;
+
+struct DstShape {
+    int N, H, HU, no, ne, NOP, NEP, nro, nre, cpw, cw, tab;  // tab: table floats (TO, TE, LAM)
+};
+__host__ __device__ inline DstShape dst_shape(int nl) {
+    DstShape q;
+    q.N = nl - 1;
+    q.H = (nl - 1) / 2;
+    q.HU = q.H + (nl % 2 == 0 ? 1 : 0);
+    q.no = (q.N + 1) / 2;
+    q.ne = q.N / 2;
+    q.NOP = (q.no + 15) & ~15;
+    q.NEP = q.ne > 0 ? (q.ne + 15) & ~15 : 0;
+    q.nro = q.NOP / 16;
+    q.nre = q.NEP / 16;
+    q.cpw = DST_WARPS / (q.nro + q.nre);
+    q.cw = 64 * q.cpw;
+    q.tab = q.HU * q.NOP + q.H * q.NEP + ((q.N + 15) & ~15);
+    return q;
+}
+
+// (x_k, x_{nl-k}) -> (u_k, v_k) for k = 1..H over the whole N x cw tile
+__device__ __forceinline__ void dst_butterfly(float* tile, int nl, int H, int cw) {
+    for (int i = threadIdx.x; i < H * (cw / 4); i += blockDim.x) {
+        const int k = 1 + i / (cw / 4), c = 4 * (i % (cw / 4));
+        float4* pa = reinterpret_cast<float4*>(tile + (k - 1) * cw + c);
+        float4* pb = reinterpret_cast<float4*>(tile + (nl - k - 1) * cw + c);
+        const float4 a = *pa, b = *pb;
+        *pa = make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+        *pb = make_float4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w);
+    }
+}
+
+// acc[i] = sum_k tab[k * tstride + i] * tile[k * cw + col .. + 1] for 16 outputs i
+__device__ __forceinline__ void dst_unit(float2 (&acc)[16], const float* __restrict__ tab, int tstride,
+                                         const float* __restrict__ tr, int cw, int kin) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) acc[i] = make_float2(0.f, 0.f);
+#pragma unroll 2
+    for (int k = 0; k < kin; ++k) {
+        const float2 x = *reinterpret_cast<const float2*>(tr + k * cw);
+        const float4* s4 = reinterpret_cast<const float4*>(tab + k * tstride);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float4 sv = s4[j];
+            acc[4 * j + 0] = __ffma2_rn(make_float2(sv.x, sv.x), x, acc[4 * j + 0]);
+            acc[4 * j + 1] = __ffma2_rn(make_float2(sv.y, sv.y), x, acc[4 * j + 1]);
+            acc[4 * j + 2] = __ffma2_rn(make_float2(sv.z, sv.z), x, acc[4 * j + 2]);
+            acc[4 * j + 3] = __ffma2_rn(make_float2(sv.w, sv.w), x, acc[4 * j + 3]);
+        }
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(DST_WARPS * 32, 2) k_bdst(const BProb* __restrict__ probs, const int2* __restrict__ map,
-                                                         const int2* __restrict__ lat, const int* __restrict__ soff,
-                                                         const float* __restrict__ stab, int pass,
-                                                         const T* __restrict__ r, float* __restrict__ t,
-                                                         T* __restrict__ z, const KrylovScalars* __restrict__ scal) {
+                                                            const int2* __restrict__ lat, const int* __restrict__ soff,
+                                                            const float* __restrict__ stab, int pass,
+                                                            const T* __restrict__ r, float* __restrict__ t,
+                                                            T* __restrict__ z, const KrylovScalars* __restrict__ scal) {
     const int2 e = map[blockIdx.x];
     const int pi = e.x, line = e.y;
     if (scal[pi].done) return;
     const BProb& d = probs[pi];
-    const int nl = lat[pi].x, N = nl - 1, NP = (N + 15) & ~15, nrb = NP / 16;
-    const int cpw = DST_WARPS / nrb, cw = 64 * cpw;
+    const int nl = lat[pi].x;
+    const DstShape q = dst_shape(nl);
+    const int N = q.N, cw = q.cw;
     const float a0 = __int_as_float(lat[pi].y);
     extern __shared__ __align__(16) float dsm[];
-    float* S = dsm;              // N x NP
-    float* tile = S + N * NP;    // N x cw
+    float* TO = dsm;                    // HU x NOP
+    float* TE = TO + q.HU * q.NOP;      // H x NEP
+    const float* LAM = TE + q.H * q.NEP; // lam_k = 4 sin^2(pi k / (2 nl)), k = 1..N
+    float* tile = dsm + q.tab;          // N x cw
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     {
         const float4* src = reinterpret_cast<const float4*>(stab + soff[pi]);
-        float4* dst = reinterpret_cast<float4*>(S);
-        for (int q = threadIdx.x; q < N * NP / 4; q += blockDim.x) dst[q] = __ldg(src + q);
+        float4* dst = reinterpret_cast<float4*>(dsm);
+        for (int i = threadIdx.x; i < q.tab / 4; i += blockDim.x) dst[i] = __ldg(src + i);
     }
     const int stride = nl + 1;
     auto row_of = [&](int k) { return (pass == 1) ? k * stride + line : line * stride + k; };  // k = 1..N
-    const int rb = warp % nrb, cc = warp / nrb;  // this warp's unit: rows 16 rb.., columns 64 cc + 2 lane
-    const bool busy = warp < nrb * cpw;
-    const float w = 3.14159265358979f / (2.0f * (float)nl);
+    // this warp's unit: output block rb (odd outputs for rb < nro, even after), columns 64 cc + 2 lane
+    const int nrb = q.nro + q.nre;
+    const int rb = warp % nrb, cc = warp / nrb;
+    const bool busy = warp < nrb * q.cpw;
+    const bool odd = rb < q.nro;
+    const int ob = odd ? rb : rb - q.nro;                    // block within its parity
+    const float* tab = odd ? TO + 16 * ob : TE + 16 * ob;    // row r at tab + r * tstride
+    const int tstride = odd ? q.NOP : q.NEP;
+    const int kin = odd ? q.HU : q.H;                        // inner length
+    const int roff = odd ? 0 : q.HU;                         // first tile row of the inner range
+    const int nout = odd ? q.no : q.ne;
+    const int col = 64 * cc + 2 * lane;
+    float2 acc[16];
+    const float* tr = tile + roff * cw + col;
     for (int c0 = 0; c0 < d.ld; c0 += cw) {
-        __syncthreads();  // S staged / the previous chunk's tile read
+        __syncthreads();  // tables staged / the previous chunk's tile read
         const int cn = min(cw, d.ld - c0);  // a multiple of 4
-        for (int q = threadIdx.x; q < N * (cw / 4); q += blockDim.x) {
-            const int k = q / (cw / 4), c = 4 * (q - k * (cw / 4));
+        for (int i = threadIdx.x; i < N * (cw / 4); i += blockDim.x) {
+            const int k = i / (cw / 4), c = 4 * (i - k * (cw / 4));
             float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
             if (c < cn) {
                 const long long idx = d.voff + (long long)row_of(k + 1) * d.ld + c0 + c;
@@ -774,54 +849,37 @@ __global__ void __launch_bounds__(DST_WARPS * 32, 2) k_bdst(const BProb* __restr
             *reinterpret_cast<float4*>(tile + k * cw + c) = v;
         }
         __syncthreads();
-        float2 acc[16];
-        const int col = 64 * cc + 2 * lane;
-        auto transform = [&]() {
-#pragma unroll
-            for (int i = 0; i < 16; ++i) acc[i] = make_float2(0.f, 0.f);
-            const float* Sr = S + 16 * rb;
-            const float* tr = tile + col;
-#pragma unroll 2
-            for (int k = 0; k < N; ++k) {
-                const float2 x = *reinterpret_cast<const float2*>(tr + k * cw);
-                const float4* s4 = reinterpret_cast<const float4*>(Sr + k * NP);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const float4 sv = s4[q];
-                    acc[4 * q + 0] = __ffma2_rn(make_float2(sv.x, sv.x), x, acc[4 * q + 0]);
-                    acc[4 * q + 1] = __ffma2_rn(make_float2(sv.y, sv.y), x, acc[4 * q + 1]);
-                    acc[4 * q + 2] = __ffma2_rn(make_float2(sv.z, sv.z), x, acc[4 * q + 2]);
-                    acc[4 * q + 3] = __ffma2_rn(make_float2(sv.w, sv.w), x, acc[4 * q + 3]);
-                }
-            }
-        };
-        if (busy) transform();
+        dst_butterfly(tile, nl, q.H, cw);
+        __syncthreads();
+        if (busy) dst_unit(acc, tab, tstride, tr, cw, kin);
         if (pass == 1) {
-            // scale by D(kx = line, ky = i + 1), back into the tile, transform again
+            // scale output i (tile row i - 1) by D(kx = line, ky = i), split again, transform again
             __syncthreads();  // every warp has read the tile
             if (busy) {
-                const float sx = sinf(w * (float)line);
-                const float lx = 4.f * sx * sx;
+                const float lx = LAM[line - 1];
                 const float nrm = 4.f / ((float)nl * (float)nl);
 #pragma unroll
                 for (int i = 0; i < 16; ++i) {
-                    const int row = 16 * rb + i;
-                    if (row < N) {
-                        const float sy = sinf(w * (float)(row + 1));
-                        const float f = nrm / (a0 * (lx + 4.f * sy * sy));
-                        *reinterpret_cast<float2*>(tile + row * cw + col) = make_float2(acc[i].x * f, acc[i].y * f);
+                    const int j = 16 * ob + i;
+                    if (j < nout) {
+                        const int orow = odd ? 2 * j : 2 * j + 1;
+                        const float f = nrm / (a0 * (lx + LAM[orow]));
+                        *reinterpret_cast<float2*>(tile + orow * cw + col) = make_float2(acc[i].x * f, acc[i].y * f);
                     }
                 }
             }
             __syncthreads();
-            if (busy) transform();
+            dst_butterfly(tile, nl, q.H, cw);
+            __syncthreads();
+            if (busy) dst_unit(acc, tab, tstride, tr, cw, kin);
         }
         if (busy && col < cn) {
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
-                const int row = 16 * rb + i;
-                if (row < N) {
-                    const long long idx = d.voff + (long long)row_of(row + 1) * d.ld + c0 + col;
+                const int j = 16 * ob + i;
+                if (j < nout) {
+                    const int orow = odd ? 2 * j : 2 * j + 1;
+                    const long long idx = d.voff + (long long)row_of(orow + 1) * d.ld + c0 + col;
                     if (pass == 2) {
                         z[idx] = (T)acc[i].x;
                         z[idx + 1] = (T)acc[i].y;
@@ -1344,9 +1402,9 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
     SG_TRY(balloc(b, vb, (void**)&b->d_d64));
     SG_TRY(balloc(b, (size_t)B * sizeof(double), (void**)&b->d_want));
     {
-        // sine-transform preconditioner: per-problem (nl, a0), the sine table of each lattice
-        // size (N x NP, zero past column N; offsets multiples of 16 floats) and one block
-        // per (problem, interior line)
+        // sine-transform preconditioner: per-problem (nl, a0), the split sine tables of each
+        // lattice size (k_bdst; offsets multiples of 16 floats) and one block per
+        // (problem, interior line)
         std::vector<int2> lat(B, make_int2(0, 0));
         std::vector<int2> map;
         std::vector<int> soff(B, 0), toff(129, -1);
@@ -1359,16 +1417,34 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
             int bits;
             std::memcpy(&bits, &a0f, sizeof(int));
             lat[i] = make_int2(h.nl, bits);
-            const int N = h.nl - 1, NP = (N + 15) & ~15, cw = 64 * (DST_WARPS / (NP / 16));
+            const DstShape q = dst_shape(h.nl);
             if (toff[h.nl] < 0) {
+                // TO[r][j] (odd output i = 2j + 1): sin(pi i (r + 1) / nl) for r < H, sin(pi i / 2) for
+                // the middle point (r = H, even nl); TE[r][j] (even i = 2j + 2): sin(pi i (H - r) / nl)
                 toff[h.nl] = (int)stab.size();
-                for (int k = 1; k <= N; ++k)
-                    for (int c = 0; c < NP; ++c)
-                        stab.push_back(c < N ? (float)std::sin(M_PI * (double)((k * (c + 1)) % (2 * h.nl)) / h.nl) : 0.f);
+                for (int r = 0; r < q.HU; ++r)
+                    for (int j = 0; j < q.NOP; ++j) {
+                        const int io = 2 * j + 1;
+                        const int k = r < q.H ? r + 1 : 0;
+                        double v = 0.0;
+                        if (j < q.no)
+                            v = r < q.H ? std::sin(M_PI * (double)((io * k) % (2 * h.nl)) / h.nl) : std::sin(M_PI * 0.5 * io);
+                        stab.push_back((float)v);
+                    }
+                for (int r = 0; r < q.H; ++r)
+                    for (int j = 0; j < q.NEP; ++j) {
+                        const int ie = 2 * j + 2, k = q.H - r;
+                        stab.push_back(j < q.ne ? (float)std::sin(M_PI * (double)((ie * k) % (2 * h.nl)) / h.nl) : 0.f);
+                    }
+                // LAM[k - 1] = 4 sin^2(pi k / (2 nl)), the 1-D Laplacian eigenvalues of pass 1's scaling
+                for (int k = 1; k <= ((q.N + 15) & ~15); ++k) {
+                    const double sk = std::sin(M_PI * k / (2.0 * h.nl));
+                    stab.push_back(k <= q.N ? (float)(4.0 * sk * sk) : 0.f);
+                }
             }
             soff[i] = toff[h.nl];
-            for (int line = 1; line <= N; ++line) map.push_back(make_int2(i, line));
-            smax = std::max(smax, ((size_t)N * NP + (size_t)N * cw) * sizeof(float));
+            for (int line = 1; line <= q.N; ++line) map.push_back(make_int2(i, line));
+            smax = std::max(smax, ((size_t)q.tab + (size_t)q.N * q.cw) * sizeof(float));
         }
         SG_TRY(bupload(b, lat, &b->d_lat));
         b->ndst = (int)map.size();
