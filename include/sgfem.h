@@ -458,7 +458,8 @@ SGFEM_API int sgfem_adjoint_gradient(sgfem_context* ctx, const double* U, const 
  * problems marked with sgfem_batch_set_lattice, Jacobi otherwise) on all problems in
  * lock step: each phase of an iteration is one launch over every problem, a
  * batch of check_every iterations is a captured CUDA graph, converged problems
- * skip their blocks.  The apply's launch shape is chosen at finalize by timing
+ * skip their blocks.  The apply's form (pair passes, or column slots when every
+ * problem has M + 1 <= 31) and launch shape are chosen at finalize by timing
  * the candidates (sgfem_batch_tuning reports them).  x_out receives the
  * solutions, problem after problem, each n x P column-major (may be NULL).
  * Mixed precision by default: iterative refinement whose residuals are FP64
