@@ -78,6 +78,35 @@ def _lattice_size(FES):
     return nl if np.allclose(FES.dof_coords, expect, atol=1e-12) else 0
 
 
+def host_apply_column_slots(Ks, TB, bdofs, x, precision=1):
+    """sgfem_batch_host_apply: Y = S X through the column-slot schedule of the batch
+    apply, evaluated on the host (precision 1: the FP32 kernel's passes, 0: the FP64
+    kernel's); x and the result in the SGFEVector layout.  Returns (y, summary)."""
+    lib = _lib.load()
+    K0, vals = _shared_pattern_values(Ks)
+    n = K0.shape[0]
+    M = len(Ks) - 1
+    P = TB.nmodes
+    colptr = np.ascontiguousarray(K0.indptr.astype(np.int64) + 1)
+    rowval = np.ascontiguousarray(K0.indices.astype(np.int64) + 1)
+    vals = np.ascontiguousarray(vals)
+    G = sp.csc_matrix(TB.G)
+    G.sort_indices()
+    gcp = np.ascontiguousarray(G.indptr.astype(np.int64) + 1)
+    grv = np.ascontiguousarray(G.indices.astype(np.int64) + 1)
+    gv = np.ascontiguousarray(G.data.astype(np.float64))
+    bd = np.ascontiguousarray(np.asarray(bdofs, dtype=np.int64) + 1)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros(n * P)
+    msg = ctypes.create_string_buffer(256)
+    i64 = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+    rc = lib.sgfem_batch_host_apply(n, M, P, i64(colptr), i64(rowval), _lib._dp(vals), i64(gcp), i64(grv),
+                                    _lib._dp(gv), len(bd), i64(bd), int(precision), _lib._dp(x), _lib._dp(y), msg, 256)
+    if rc != _lib.OK:
+        raise _lib.SGError(rc, msg.value.decode())
+    return y, msg.value.decode()
+
+
 class SGBatch:
     def __init__(self, device=0):
         self.lib = _lib.load()

@@ -1666,6 +1666,88 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
 
 extern "C" const char* sgfem_batch_tuning(const sgfem_batch* b) { return b ? b->tuning.c_str() : ""; }
 
+// Host check of the column-slot schedule: the problem is added as sgfem_batch_add does
+// (no device work), its schedule built as at finalize, and the sums of k_bapply_cols
+// evaluated on the host in FP64 with the FP32 (precision 1) or FP64 (precision 0) pass
+// structure: every pass's pair sums (slot sources, clamped columns, padding groups) go
+// to the pass area and each output column takes its pass's entries.  X and Y are n x P
+// column-major (the SGFEVector layout); Dirichlet rows of Y are zero.
+extern "C" int sgfem_batch_host_apply(int64_t n, int64_t M, int64_t P, const int64_t* colptr, const int64_t* rowval,
+                                      const double* vals, const int64_t* Gcolptr, const int64_t* Growval,
+                                      const double* Gval, int64_t nbd, const int64_t* bdofs, int precision,
+                                      const double* X, double* Y, char* msg, int msglen) {
+    auto say = [&](const std::string& t) {
+        if (msg && msglen > 0) snprintf(msg, (size_t)msglen, "%s", t.c_str());
+    };
+    if (!X || !Y || (precision != 0 && precision != 1)) return SGFEM_ERR_ARGUMENT;
+    std::vector<double> b0(n > 0 ? (size_t)n : 1, 0.0);
+    sgfem_batch tmp;
+    const int rc = sgfem_batch_add(&tmp, n, M, P, colptr, rowval, vals, Gcolptr, Growval, Gval, nbd, bdofs, b0.data());
+    if (rc != SGFEM_OK) {
+        say(tmp.err);
+        return rc;
+    }
+    const auto& h = tmp.hp[0];
+    if (h.M1 > 31) {
+        say("the column-slot form needs M + 1 <= 31");
+        return SGFEM_ERR_UNSUPPORTED;
+    }
+    ColSched cs;
+    build_cols(h, cs);
+    const int es = precision == 1 ? 4 : 8;
+    const auto& pass = es == 4 ? cs.pass : cs.pass64;
+    const auto& ept = es == 4 ? cs.ept32 : cs.ept64;
+    const auto& eidx = es == 4 ? cs.eidx32 : cs.eidx64;
+    const auto& eg = es == 4 ? cs.eg32 : cs.eg64;
+    const int ld = h.ld, M1 = h.M1;
+    std::vector<double> area(512), ys(ld);
+    long long slots = 0;
+    for (const auto& p : pass) {
+        if (p.z < 1 || p.z > cols_gp(p.x, es) || cols_na(p.x) * p.z * 32 > 512) {
+            say("pass shape outside the kernel's limits");
+            return SGFEM_ERR_UNSUPPORTED;
+        }
+        slots += (long long)cols_na(p.x) * p.z * 32;
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        std::fill(ys.begin(), ys.end(), 0.0);
+        if (!h.bmask[i]) {
+            for (size_t pp = 0; pp < pass.size(); ++pp) {
+                const int4 p = pass[pp];
+                const int na = cols_na(p.x);
+                std::fill(area.begin(), area.end(), 0.0);
+                for (int g = 0; g < p.z; ++g) {
+                    const int vg = p.y + g;
+                    for (int L = 0; L < 32; ++L) {
+                        const int c = std::min(cs.vgcol[vg] + L, ld - 1);
+                        for (int sl = 0; sl < na; ++sl) {
+                            const int m = cs.src[(size_t)cs.vgsrc[vg] + 32 * sl + L];
+                            double f = 0.0;
+                            for (int k = h.rowptr[i]; k < h.rowptr[i + 1]; ++k) {
+                                const int j = h.col[k];
+                                const double xv = c < P ? X[(size_t)c * n + j] : 0.0;
+                                f += (m < M1 ? h.vals[(size_t)k * M1 + m] : 0.0) * xv;
+                            }
+                            area[(size_t)(g * na + sl) * 32 + L] = f;
+                        }
+                    }
+                }
+                for (int L = 0; L < 32; ++L)
+                    for (int e = ept[pp * 32 + L]; e < ept[pp * 32 + L + 1]; ++e) {
+                        const int v = eidx[e];
+                        ys[(size_t)(v >> 16) * 32 + L] += eg[e] * area[v & 0xffff];
+                    }
+            }
+        }
+        for (int64_t mu = 0; mu < P; ++mu) Y[(size_t)mu * n + i] = ys[mu];
+    }
+    char buf[160];
+    snprintf(buf, sizeof(buf), "%zu passes, %zu groups, %.3f slots per pair (%lld slots, %zu pairs)", pass.size(),
+             cs.vgcol.size(), (double)slots / (double)h.qtab.size(), slots, h.qtab.size());
+    say(buf);
+    return SGFEM_OK;
+}
+
 namespace {
 
 // z = B r (sine transform on lattice problems, Jacobi on the others), rho = r'z, beta, p = z + beta p

@@ -495,6 +495,17 @@ SGFEM_API const char* sgfem_batch_tuning(const sgfem_batch* batch);
 SGFEM_API int sgfem_batch_solve(sgfem_batch* batch, double rtol, int maxit, int check_every, double* x_out,
                                 sgfem_batch_stats* stats);
 SGFEM_API int sgfem_batch_problem_stats(const sgfem_batch* batch, int i, int* iterations, double* relres);
+/* Host check of the batch apply's column-slot form (no device work, no counterpart in
+   the reference; its result is mul! of solvers_poisson_primal.jl:86-124): one problem,
+   given as to sgfem_batch_add, is scheduled as sgfem_batch_finalize schedules it and
+   Y = S X is evaluated on the host in FP64 from the pass structure of the FP32
+   (precision 1) or FP64 (precision 0) kernel, pass area and combination entries
+   included.  X, Y: n x P column-major.  msg receives a summary of the schedule;
+   SGFEM_ERR_UNSUPPORTED when M + 1 > 31 (the form does not apply). */
+SGFEM_API int sgfem_batch_host_apply(int64_t n, int64_t M, int64_t P, const int64_t* colptr, const int64_t* rowval,
+                                     const double* vals, const int64_t* Gcolptr, const int64_t* Growval,
+                                     const double* Gval, int64_t nbdofs, const int64_t* bdofs, int precision,
+                                     const double* X, double* Y, char* msg, int msglen);
 
 /*
  * Stiffness matrices of the cosine coefficient assembled on the GPU (the

@@ -1,0 +1,63 @@
+"""The column-slot schedule of the batch apply, checked on the host.
+
+sgfem_batch_host_apply schedules one problem as sgfem_batch_finalize does
+(virtual groups of 1-16 slots per column block, passes of one kind, the
+combination entries grouped by pass) and evaluates the sums of k_bapply_cols
+on the host in FP64, so the schedule itself is compared with the oracle's
+literal mul! (solvers_poisson_primal.jl:86-124) without a GPU.  Bar: 1e-12
+relative in the 2-norm, for the FP32 and the FP64 pass structures."""
+import numpy as np
+import pytest
+
+from oracle import sg as osg
+from tests.problems import build
+
+
+def _sets(pkg):
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    return [
+        (5, 1, 16, pkg.total_degree_multiindices(16, 3)),   # 969 modes: 16 + 1 slots, 1-4 slots
+        (6, 1, 7, pkg.total_degree_multiindices(7, 2)),     # 8 slots
+        (7, 1, 8, pkg.top_weight_multiindices(8, 40, C.decay_factors)),  # irregular set
+        (4, 2, 3, pkg.total_degree_multiindices(3, 2)),     # P2
+        (4, 1, 30, pkg.total_degree_multiindices(30, 1)),   # M + 1 = 31, the largest the form takes
+        (5, 1, 2, pkg.total_degree_multiindices(2, 1)),     # 3 modes: one partly empty group
+    ]
+
+
+@pytest.mark.parametrize("precision", [1, 0])
+def test_column_slot_schedule_matches_oracle(built_pkg, precision):
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    from extendableasgfem_gb300.batch import host_apply_column_slots
+    rng = np.random.default_rng(5)
+    for args in _sets(pkg):
+        p = build(*args)
+        x = rng.standard_normal(p.n * p.P)
+        y, summary = host_apply_column_slots(p.Kall, p.TB, p.bdofs, x, precision)
+        ref = osg.mul_literal(x, p.K0, p.Ks, p.G, p.bdofs, p.P)
+        assert np.linalg.norm(y - ref) <= 1e-12 * np.linalg.norm(ref), (args[:3], summary)
+        assert "passes" in summary
+
+
+def test_column_slot_schedule_padding(built_pkg):
+    """On a total-degree set the slots stay close to the pairs (M = 16, degree 3:
+    6048 slots for 5593 pairs)."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    from extendableasgfem_gb300.batch import host_apply_column_slots
+    p = build(3, 1, 16, pkg.total_degree_multiindices(16, 3))
+    _, summary = host_apply_column_slots(p.Kall, p.TB, p.bdofs, np.zeros(p.n * p.P), 1)
+    ratio = float(summary.split(",")[2].split()[0])
+    assert ratio <= 1.1, summary
+
+
+def test_column_slot_schedule_needs_at_most_31_terms(built_pkg):
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    from extendableasgfem_gb300.batch import host_apply_column_slots
+    units = [[0] * 31] + [[int(k == m) for k in range(31)] for m in range(31)]
+    p = build(4, 1, 31, units)
+    with pytest.raises(pkg.SGError) as e:
+        host_apply_column_slots(p.Kall, p.TB, p.bdofs, np.zeros(p.n * p.P), 1)
+    assert e.value.code == 7 and "M + 1 <= 31" in str(e.value)
