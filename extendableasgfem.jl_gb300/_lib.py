@@ -112,6 +112,7 @@ SIGNATURES = {
     "sgfem_batch_add": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _I64P, _I64P, _DP, _I64P,
                                        _I64P, _DP, ctypes.c_int64, _I64P, _DP]),
     "sgfem_batch_count": (ctypes.c_int, [_P]),
+    "sgfem_batch_host_dst": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, _DP, _DP]),
     "sgfem_batch_host_apply": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _I64P, _I64P, _DP,
                                               _I64P, _I64P, _DP, ctypes.c_int64, _I64P, ctypes.c_int, _DP, _DP,
                                               ctypes.c_char_p, ctypes.c_int]),

@@ -107,6 +107,18 @@ def host_apply_column_slots(Ks, TB, bdofs, x, precision=1):
     return y, msg.value.decode()
 
 
+def host_sine_transform(nl, x):
+    """sgfem_batch_host_dst: S x for the columns of x ((nl-1) x ncols), S_ik =
+    sin(pi i k / nl), through the batch preconditioner's split tables, on the host."""
+    lib = _lib.load()
+    x = np.asfortranarray(np.asarray(x, dtype=np.float64).reshape(nl - 1, -1))
+    y = np.zeros_like(x, order="F")
+    rc = lib.sgfem_batch_host_dst(int(nl), x.shape[1], _lib._dp(x), _lib._dp(y))
+    if rc != _lib.OK:
+        raise _lib.SGError(rc, "sgfem_batch_host_dst failed")
+    return y
+
+
 class SGBatch:
     def __init__(self, device=0):
         self.lib = _lib.load()

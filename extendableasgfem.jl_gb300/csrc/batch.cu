@@ -1001,6 +1001,32 @@ int build_map(sgfem_batch* b, int total_blocks, std::vector<BProb>& probs, std::
     return SGFEM_OK;
 }
 
+// The split sine tables of one lattice size, appended to out (k_bdst's layout):
+// TO[r][j] (odd output i = 2j + 1): sin(pi i (r + 1) / nl) for r < H, sin(pi i / 2) for
+// the middle point (r = H, even nl); TE[r][j] (even output i = 2j + 2): sin(pi i (H - r)
+// / nl); LAM[k - 1] = 4 sin^2(pi k / (2 nl)), the 1-D Laplacian eigenvalues of pass 1's
+// scaling.  Columns past the last output and LAM past N are zero.
+void dst_tables(int nl, std::vector<float>& out) {
+    const DstShape q = dst_shape(nl);
+    for (int r = 0; r < q.HU; ++r)
+        for (int j = 0; j < q.NOP; ++j) {
+            const int io = 2 * j + 1;
+            const int k = r < q.H ? r + 1 : 0;
+            double v = 0.0;
+            if (j < q.no) v = r < q.H ? std::sin(M_PI * (double)((io * k) % (2 * nl)) / nl) : std::sin(M_PI * 0.5 * io);
+            out.push_back((float)v);
+        }
+    for (int r = 0; r < q.H; ++r)
+        for (int j = 0; j < q.NEP; ++j) {
+            const int ie = 2 * j + 2, k = q.H - r;
+            out.push_back(j < q.ne ? (float)std::sin(M_PI * (double)((ie * k) % (2 * nl)) / nl) : 0.f);
+        }
+    for (int k = 1; k <= ((q.N + 15) & ~15); ++k) {
+        const double sk = std::sin(M_PI * k / (2.0 * nl));
+        out.push_back(k <= q.N ? (float)(4.0 * sk * sk) : 0.f);
+    }
+}
+
 // ---- schedule of the column-slot apply for one problem.  Column block b holds columns
 // 32 b + L; lane L's terms are the m with (m, column) in the pair list, in increasing m.
 // The block's longest list is cut into virtual groups of 16, 8, 4, 2 or 1 slots (a
@@ -1419,28 +1445,8 @@ extern "C" int sgfem_batch_finalize(sgfem_batch* b) {
             lat[i] = make_int2(h.nl, bits);
             const DstShape q = dst_shape(h.nl);
             if (toff[h.nl] < 0) {
-                // TO[r][j] (odd output i = 2j + 1): sin(pi i (r + 1) / nl) for r < H, sin(pi i / 2) for
-                // the middle point (r = H, even nl); TE[r][j] (even i = 2j + 2): sin(pi i (H - r) / nl)
                 toff[h.nl] = (int)stab.size();
-                for (int r = 0; r < q.HU; ++r)
-                    for (int j = 0; j < q.NOP; ++j) {
-                        const int io = 2 * j + 1;
-                        const int k = r < q.H ? r + 1 : 0;
-                        double v = 0.0;
-                        if (j < q.no)
-                            v = r < q.H ? std::sin(M_PI * (double)((io * k) % (2 * h.nl)) / h.nl) : std::sin(M_PI * 0.5 * io);
-                        stab.push_back((float)v);
-                    }
-                for (int r = 0; r < q.H; ++r)
-                    for (int j = 0; j < q.NEP; ++j) {
-                        const int ie = 2 * j + 2, k = q.H - r;
-                        stab.push_back(j < q.ne ? (float)std::sin(M_PI * (double)((ie * k) % (2 * h.nl)) / h.nl) : 0.f);
-                    }
-                // LAM[k - 1] = 4 sin^2(pi k / (2 nl)), the 1-D Laplacian eigenvalues of pass 1's scaling
-                for (int k = 1; k <= ((q.N + 15) & ~15); ++k) {
-                    const double sk = std::sin(M_PI * k / (2.0 * h.nl));
-                    stab.push_back(k <= q.N ? (float)(4.0 * sk * sk) : 0.f);
-                }
+                dst_tables(h.nl, stab);
             }
             soff[i] = toff[h.nl];
             for (int line = 1; line <= q.N; ++line) map.push_back(make_int2(i, line));
@@ -1748,6 +1754,42 @@ extern "C" int sgfem_batch_host_apply(int64_t n, int64_t M, int64_t P, const int
     return SGFEM_OK;
 }
 
+// Host check of the batch sine transform: y = S x (S_ik = sin(pi i k / nl), i, k = 1..nl-1)
+// for ncols lines x (N x ncols, column-major), computed as k_bdst computes it from the
+// split tables (the pair (x_k, x_{nl-k}) turned into (u_k, v_k), odd outputs from u and
+// the middle point, even outputs from v), in FP64 with the FP32 table values.
+extern "C" int sgfem_batch_host_dst(int64_t nl, int64_t ncols, const double* x, double* y) {
+    if (nl < 2 || nl > 128 || ncols < 0 || (ncols > 0 && (!x || !y))) return SGFEM_ERR_ARGUMENT;
+    const DstShape q = dst_shape((int)nl);
+    std::vector<float> tab;
+    dst_tables((int)nl, tab);
+    if ((int)tab.size() != q.tab) return SGFEM_ERR_UNSUPPORTED;
+    const float* TO = tab.data();
+    const float* TE = TO + (size_t)q.HU * q.NOP;
+    std::vector<double> t(q.N);
+    for (int64_t c = 0; c < ncols; ++c) {
+        const double* xc = x + (size_t)c * q.N;
+        double* yc = y + (size_t)c * q.N;
+        for (int k = 0; k < q.N; ++k) t[k] = xc[k];
+        for (int k = 1; k <= q.H; ++k) {
+            const double a = t[k - 1], b = t[nl - k - 1];
+            t[k - 1] = a + b;
+            t[nl - k - 1] = a - b;
+        }
+        for (int j = 0; j < q.no; ++j) {
+            double s = 0.0;
+            for (int r = 0; r < q.HU; ++r) s += (double)TO[(size_t)r * q.NOP + j] * t[r];
+            yc[2 * j] = s;
+        }
+        for (int j = 0; j < q.ne; ++j) {
+            double s = 0.0;
+            for (int r = 0; r < q.H; ++r) s += (double)TE[(size_t)r * q.NEP + j] * t[q.HU + r];
+            yc[2 * j + 1] = s;
+        }
+    }
+    return SGFEM_OK;
+}
+
 namespace {
 
 // z = B r (sine transform on lattice problems, Jacobi on the others), rho = r'z, beta, p = z + beta p
@@ -1782,7 +1824,6 @@ int batch_precondition(sgfem_batch* b, const BVecs<T, TX>& v, int maxit) {
 template <typename T, typename TX>
 int batch_iteration(sgfem_batch* b, const BVecs<T, TX>& v, int maxit) {
     const int B = (int)b->hp.size();
-    const bool f32 = sizeof(T) == 4;
     if constexpr (sizeof(T) == 4)
         SG_TRY(launch_apply<T>(b, b->wpb32, b->qt32, v.p, v.q, b->d_part, b->d_scal, b->pf32));
     else

@@ -502,6 +502,13 @@ SGFEM_API int sgfem_batch_problem_stats(const sgfem_batch* batch, int i, int* it
    (precision 1) or FP64 (precision 0) kernel, pass area and combination entries
    included.  X, Y: n x P column-major.  msg receives a summary of the schedule;
    SGFEM_ERR_UNSUPPORTED when M + 1 > 31 (the form does not apply). */
+/* Host check of the batch sine-transform preconditioner's split tables (no device
+   work, no counterpart in the reference): y = S x, S_ik = sin(pi i k / nl), i, k =
+   1..nl-1, for ncols lines (x, y: (nl-1) x ncols column-major), computed as the batch
+   kernel computes it (pairs (x_k, x_{nl-k}) into sums and differences, odd outputs
+   from the sums, even outputs from the differences) with its FP32 table values, in
+   FP64.  2 <= nl <= 128. */
+SGFEM_API int sgfem_batch_host_dst(int64_t nl, int64_t ncols, const double* x, double* y);
 SGFEM_API int sgfem_batch_host_apply(int64_t n, int64_t M, int64_t P, const int64_t* colptr, const int64_t* rowval,
                                      const double* vals, const int64_t* Gcolptr, const int64_t* Growval,
                                      const double* Gval, int64_t nbdofs, const int64_t* bdofs, int precision,

@@ -61,3 +61,20 @@ def test_column_slot_schedule_needs_at_most_31_terms(built_pkg):
     with pytest.raises(pkg.SGError) as e:
         host_apply_column_slots(p.Kall, p.TB, p.bdofs, np.zeros(p.n * p.P), 1)
     assert e.value.code == 7 and "M + 1 <= 31" in str(e.value)
+
+
+@pytest.mark.parametrize("nl", [2, 3, 4, 16, 17, 64, 100, 127, 128])
+def test_split_sine_transform_matches_dense(built_pkg, nl):
+    """The batch preconditioner's sine transform, split by output parity (odd outputs
+    from x_k + x_{nl-k} and the middle point, even outputs from x_k - x_{nl-k}), equals
+    the dense S_ik = sin(pi i k / nl) within its FP32 tables (1e-6 relative), and
+    S S = (nl / 2) I."""
+    from extendableasgfem_gb300.batch import host_sine_transform
+    N = nl - 1
+    k = np.arange(1, N + 1)
+    S = np.sin(np.pi * np.outer(k, k) / nl)
+    x = np.random.default_rng(nl).standard_normal((N, 5))
+    y = host_sine_transform(nl, x)
+    assert np.linalg.norm(y - S @ x) <= 1e-6 * np.linalg.norm(S @ x)
+    z = host_sine_transform(nl, y)
+    assert np.linalg.norm(z - 0.5 * nl * x) <= 1e-6 * np.linalg.norm(0.5 * nl * x)
