@@ -328,10 +328,10 @@ __global__ void k_bapply(const BProb* __restrict__ probs, const int* __restrict_
 // slot takes its term's value from the lane named by the schedule (__shfl_sync), so
 // a lane whose column couples to few terms and one coupled to all of them share the
 // instruction stream without a shared-memory gather per pair.  A pass holds GP groups
-// of one kind; X[j, c] is read once per group and nonzero (coalesced, the next
-// nonzero's values in flight while the current one is used).  After the passes the
-// pair sums go to the warp's shared area and each output column is combined from its
-// list (K_0 pair with g = 1, then the G entries) as in k_bapply.
+// of one kind; X[j, c] is read once per group and nonzero (coalesced; a chunk's X
+// loads are issued before its FMAs).  After each pass its pair sums go to the warp's
+// shared area and every lane adds the pass's entries of its own output columns (the
+// K_0 pair with g = 1, then the G entries, as in k_bapply) to the warp's output row.
 // kinds: slots per lane 1, 2, 4, 8, 16; groups per pass keep the pair sums of a pass at
 // <= 16 per lane, and the pass's X values of a chunk of nonzeros (groups x 4) within
 // the 128-register budget
@@ -1038,7 +1038,6 @@ struct ColSched {
     std::vector<int4> pass, pass64;
     std::vector<int> vgcol, vgsrc;
     std::vector<unsigned char> src;
-    int nf = 0;
     // combination entries per precision, grouped by (pass, lane of the output column):
     // ept[p * 32 + L] .. ept[p * 32 + L + 1] index eidx (k << 16 | place in the pass's
     // area; output column 32 k + L) and eg (coefficient)
@@ -1089,7 +1088,6 @@ void build_cols(const sgfem_batch::HostProb& h, ColSched& cs) {
                 }
                 cs.src.push_back((unsigned char)m);
             }
-        cs.nf += 32 * na;
     }
     for (int es : {4, 8}) {
         auto& pass = es == 4 ? cs.pass : cs.pass64;
