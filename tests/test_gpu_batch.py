@@ -120,16 +120,18 @@ def test_batch_tuning_cache(built_pkg, monkeypatch, tmp_path):
         assert np.linalg.norm(a - b) <= 1e-9 * np.linalg.norm(b)
 
 
-def test_batch_work_queue_apply_is_bitwise_the_block_map(built_pkg, monkeypatch):
+def test_batch_work_queue_apply_is_bitwise_the_block_map(built_pkg, monkeypatch, tmp_path):
     """The FP32 apply over the persistent work queue (SGFEM_BATCH_QUEUE=1: resident
     blocks take the block map's items in descending-cost order) computes every item
     as the one-block-per-item launch does and leaves each partial in the same
-    slot, so the mixed solves are bitwise equal and meet rtol."""
+    slot, so the mixed solves are bitwise equal and meet rtol.  The two batches share
+    one tuning cache: the second takes the first's timed shapes (forms, warps, block
+    map), so only the queue bit differs between them."""
     import __graft_entry__ as ge
     pkg = ge.load_package()
     shapes = [(9, 3, 2), (5, 2, 2), (12, 4, 2), (6, 5, 1), (7, 2, 3), (16, 3, 2)]
     probs = [build(N, 1, M, pkg.total_degree_multiindices(M, d)) for N, M, d in shapes]
-    monkeypatch.setenv("SGFEM_TUNE_CACHE", "off")
+    monkeypatch.setenv("SGFEM_TUNE_CACHE", str(tmp_path / "tuning.txt"))
     out = {}
     for q in ("0", "1"):
         monkeypatch.setenv("SGFEM_BATCH_QUEUE", q)
@@ -191,13 +193,14 @@ def test_batch_column_slot_apply_matches_kronecker_solves(built_pkg, monkeypatch
         assert np.linalg.norm(x - ref) <= 1e-8 * np.linalg.norm(ref)
 
 
-def test_batch_column_slot_queue_is_bitwise_the_block_map(built_pkg, monkeypatch):
+def test_batch_column_slot_queue_is_bitwise_the_block_map(built_pkg, monkeypatch, tmp_path):
     """The column-slot FP32 apply over the persistent work queue computes every
-    item as the one-block-per-item launch does: bitwise equal mixed solves."""
+    item as the one-block-per-item launch does: bitwise equal mixed solves (one
+    shared tuning cache, so only the queue bit differs between the two batches)."""
     import __graft_entry__ as ge
     pkg = ge.load_package()
     monkeypatch.setenv("SGFEM_BATCH_APPLY", "cols")
-    monkeypatch.setenv("SGFEM_TUNE_CACHE", "off")
+    monkeypatch.setenv("SGFEM_TUNE_CACHE", str(tmp_path / "tuning.txt"))
     shapes = [(9, 3, 2), (5, 2, 2), (12, 4, 3), (6, 5, 1), (7, 12, 2)]
     probs = [build(N, 1, M, pkg.total_degree_multiindices(M, d)) for N, M, d in shapes]
     out = {}
