@@ -210,3 +210,39 @@ def test_total_degree_set_equals_filtered_tensor_set(pkg):
         ref = sorted([mi for mi in pkg.generate_multiindices(M, d) if sum(mi) <= d], key=sum)
         assert pkg.total_degree_multiindices(M, d) == ref
     assert len(pkg.total_degree_multiindices(16, 3)) == 969
+
+
+@pytest.mark.parametrize("name,obt", [("legendre", ob.LEGENDRE), ("hermite", ob.HERMITE)])
+@pytest.mark.parametrize("tail", [(10, 2), (3, 1)])
+def test_extension_couplings_match_oracle(pkg, name, obt, tail):
+    """The estimators' extended set and per extended mode j its couplings to the
+    active modes (self term, then for m = 1..M the j + e_m and j - e_m neighbours;
+    estimate.jl:343-353, :385-393), vectorised on the host, against the oracle's
+    G of the extended set and its neighbour lists: same entries in the same order,
+    coefficients equal."""
+    from extendableasgfem_gb300.estimate import extension_couplings
+    basis = pkg.LegendrePolynomials if name == "legendre" else pkg.HermitePolynomials
+    C = pkg.StochasticCoefficientCosinus(tau=0.9, start=1, decay=2, mean=1.0, maxm=150)
+    for mis in (pkg.total_degree_multiindices(5, 2), pkg.top_weight_multiindices(8, 40, C.decay_factors),
+                [[0], [1], [2]]):
+        maxdeg = max(max(m) for m in mis)
+        TB = pkg.TensorizedBasis(basis, len(mis[0]), maxdeg, maxdeg + 4, multi_indices=mis)
+        ext, (ptr, ms, nus, gs) = extension_couplings(TB.multi_indices, TB.basis, tail)
+        ext_o = om.add_boundary_modes(_copy(mis), tail_extension=tail)
+        assert [list(e) for e in ext] == [list(e) for e in ext_o]
+        G = ob.get_tensor_multiplication_with_ym(obt, ext_o)
+        plus, minus = om.get_neighbours(ext_o)
+        P_ext, nmodes, M_ext = len(ext_o), len(mis), len(ext_o[0])
+        want = []
+        for j in range(P_ext):
+            row = [(0, j, 1.0)] if j < nmodes else []
+            for m in range(1, M_ext + 1):
+                for nb in (plus[m - 1][j], minus[m - 1][j]):
+                    if 0 < nb <= nmodes:
+                        row.append((m, nb - 1, G[(m - 1) * P_ext + j, nb - 1]))
+            want.append(row)
+        got = [list(zip(ms[ptr[j]:ptr[j + 1]], nus[ptr[j]:ptr[j + 1]], gs[ptr[j]:ptr[j + 1]])) for j in range(P_ext)]
+        assert [[(int(a), int(b)) for a, b, _ in r] for r in got] == [[(a, b) for a, b, _ in r] for r in want]
+        g_got = np.array([g for r in got for _, _, g in r])
+        g_want = np.array([g for r in want for _, _, g in r])
+        assert np.allclose(g_got, g_want, rtol=1e-14, atol=0)
