@@ -78,3 +78,27 @@ def test_split_sine_transform_matches_dense(built_pkg, nl):
     assert np.linalg.norm(y - S @ x) <= 1e-6 * np.linalg.norm(S @ x)
     z = host_sine_transform(nl, y)
     assert np.linalg.norm(z - 0.5 * nl * x) <= 1e-6 * np.linalg.norm(0.5 * nl * x)
+
+
+def test_batch_host_helpers(built_pkg):
+    """The batch's host helpers: the lattice test (P1 on the unit-square mesh in
+    x-fastest order, n = (nl + 1)^2, 2 <= nl <= 128; not P2, not a perturbed mesh)
+    and the values of every K_m on K_0's pattern (refused when a K_m has an entry
+    outside it)."""
+    import scipy.sparse as sp
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    from extendableasgfem_gb300.batch import _lattice_size, _shared_pattern_values
+    assert _lattice_size(pkg.H1Pk(pkg.unit_square_mesh(16), 1)) == 16
+    assert _lattice_size(pkg.H1Pk(pkg.unit_square_mesh(16), 2)) == 0
+    assert _lattice_size(pkg.H1Pk(pkg.perturbed_unit_square_mesh(8, 0.2), 1)) == 0
+    p = build(6, 1, 3, pkg.total_degree_multiindices(3, 1))
+    K0, vals = _shared_pattern_values(p.Kall)
+    assert vals.shape == (len(p.Kall), K0.nnz)
+    for m, K in enumerate(p.Kall):
+        Km = sp.csc_matrix((vals[m], K0.indices, K0.indptr), shape=K0.shape)
+        assert abs(Km - K).max() == 0.0
+    extra = p.Kall[1].tolil()
+    extra[0, p.n - 1] = 1.0
+    with pytest.raises(ValueError):
+        _shared_pattern_values([p.Kall[0], extra.tocsc()])
