@@ -1,13 +1,17 @@
-"""Batches of independent SG problems on one GPU (host side of K8).
+"""Batches of independent SG problems on one GPU (host side of the batched solver).
 
 The reference solves one problem per solve! call (src/modelproblems/
 poisson_primal.jl:38-81).  ``SGBatch`` hands many PoissonProblemPrimal systems
 to the library at once (sgfem_batch_*): one preconditioned CG runs all of them
 in lock step, each phase one launch over every problem, iterations replayed
-from a captured CUDA graph.  P1 problems on the unit-square lattice get the
-mean-based preconditioner (sine transforms), the others Jacobi.  ``config4_problems`` draws the problem
-shapes from a SplitMix64 stream (seed = problem index):
-n = 16 + r % 113 (n x n P1 mesh), M = 4 + r % 13, total degree 1 + r % 3.
+from a captured CUDA graph; the apply's form (column slots or pair passes) and
+launch shape are timed at finalize and cached on disk.  P1 problems on the
+unit-square lattice get the mean-based preconditioner (sine transforms), the
+others Jacobi.  ``host_apply_column_slots`` and ``host_sine_transform`` evaluate
+the column-slot schedule and the split sine tables on the host (checks, no
+GPU).  ``config4_problems`` draws the problem shapes from a SplitMix64 stream
+(seed = problem index): n = 16 + r % 113 (n x n P1 mesh), M = 4 + r % 13,
+total degree 1 + r % 3.
 """
 import ctypes
 
